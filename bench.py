@@ -1,0 +1,313 @@
+"""Benchmark of the cell-model update on GB300 (one JSON line on stdout).
+
+Workload (default): the precision form -- 4,194,304 ten Tusscher 2006 epicardial cells (a
+2048 x 2048 sheet, reaction step only), FP32 gates/currents with FP64 accumulators, per-cell
+g_Na/g_Kr/g_K1 scaled by seeded U[0.9, 1.1], stimulus -52 pA/pF for 1 ms every 800 ms,
+dt = 0.01 ms. One step = one dt update of every cell. Inputs are synthetic (seeded), and the
+cell state (~430 MB) is larger than L2, so no flush is needed between steps.
+
+value     cell-steps/s, state resident in HBM, the fused driver step (cm_batch_run)
+e2e       the same through the drop-in C ABI with pinned HOST Vm/i_ext: cm_batch_step_update
+          copies Vm and i_ext in and Vm out every step (acCELLerate's CalcCellModels + Godunov)
+plain_fp64  the plain FP64 kernel on the same workload (the reference's arithmetic)
+roofline  the dominant kernel (tt2_mixed_kernel) against the measured HBM copy bandwidth
+cpu_baseline  the oracle (C restatement of the reference Calc) on the host cores, bounded sample
+
+--impl reference runs the reference's CPU implementation of the path (the oracle port of its
+Calc; the reference itself cannot be built where its sources are absent) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_CELLS = 2048 * 2048
+DT = 1e-5
+BCL = 0.8
+METRIC = "cell-steps/s on 1 GB300: surrogate+FP32 vs plain FP64 at <=1 ms APD90 error"
+UNIT = "cell-steps/s"
+# Algorithmic bytes per cell-step of tt2_mixed_kernel: 15 FP32 + 3 FP64 state read and
+# written (168 B), Vm read and written (16 B), 3 FP32 per-cell conductances read (12 B).
+MIXED_BYTES_PER_CELL_STEP = 2 * (15 * 4 + 3 * 8) + 2 * 8 + 3 * 4
+# tt2_fp64_kernel: 18 FP64 states r+w (288 B), Vm r+w (16 B), 3 FP64 conductances (24 B).
+FP64_BYTES_PER_CELL_STEP = 2 * 18 * 8 + 2 * 8 + 3 * 8
+WORKLOAD = "tt2006-epi-precision-form-2048x2048"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_batch(cm, precision, stream, n=N_CELLS, seed=2):
+    from cardiomechanics_gb300 import workloads as W
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    b = cm.Batch(p, n, precision, stream=stream)
+    sc = W.conductance_scales(seed, n, 3, 0.9, 1.1)
+    for k, name in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(name, p.get(name) * sc[k])
+    return p, b
+
+
+def time_device_steps(torch, cm, b, stream, vm, steps, warmup, t0):
+    """K fused driver steps on the batch's stream, timed with events on that stream."""
+    from cardiomechanics_gb300 import workloads as W
+    kw = dict(textbegin=0.0, textlen=1e-3, bcl=BCL, amplitude=W.TT2_STIM_NA)
+    b.run(vm, warmup, t0=t0, **kw)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    b.run(vm, steps, t0=t0 + warmup * DT, **kw)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3
+
+
+def cpu_baseline(seconds=10.0, threads=None, cells=4096):
+    """The oracle on host cores: `cells` cells of the same workload, stepped in chunks until
+    about `seconds` of wall time; returns cell-steps/s."""
+    import oracle as O
+    from cardiomechanics_gb300 import workloads as W
+    port = O.Port()
+    threads = threads or os.cpu_count() or 1
+    P = port.param_vector(O.TT2, O.load_params(O.TT2))
+    T = port.tables(O.TT2, P, DT)
+    sc = W.conductance_scales(2, N_CELLS, 3, 0.9, 1.1, cells=np.arange(cells))
+    names = port.param_names(O.TT2)
+    het = {k: P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
+    B = port.init_state(O.TT2, P, cells)
+    vm = np.full(cells, port.init_vm(O.TT2, P))
+    chunk, done, t = 500, 0, 0.0
+    start = time.perf_counter()
+    while time.perf_counter() - start < seconds:
+        port.run(O.TT2, P, T, B, vm, chunk, DT, t0=t, textbegin=0.0, textlen=1e-3, bcl=BCL, amp=W.TT2_STIM_NA,
+                 het=het, n_threads=threads)
+        done += chunk
+        t += chunk * DT
+    el = time.perf_counter() - start
+    return {"value": cells * done / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{cells} cells x {done} steps of the same workload (oracle C restatement, "
+                      f"{threads} threads, {el:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    O.build_port()
+    threads = os.cpu_count() or 1
+    samples = []
+    for _ in range(args.warmup):
+        cpu_baseline(seconds=1.0, threads=threads)
+    for _ in range(args.steps):
+        samples.append(cpu_baseline(seconds=max(2.0, 20.0 / max(1, args.steps)), threads=threads))
+    v = float(np.median([s["value"] for s in samples]))
+    cb = dict(samples[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N_CELLS / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": N_CELLS, "dt_ms": DT * 1e3, "bcl_ms": BCL * 1e3,
+                       "note": "CPU: the oracle restatement of the reference Calc on a bounded cell sample"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=40)
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import cardiomechanics_gb300 as cm
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    hbm_peak, peak_kind = peaks()
+
+    # ---- device-resident mixed form (the headline `value`)
+    p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
+    vm = torch.tensor(b.init_vm(), device="cuda")
+    b.run(vm, args.warmup, textbegin=0.0, textlen=1e-3, bcl=BCL, amplitude=cm_stim())
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        b.run(vm, args.steps, t0=args.warmup * DT, textbegin=0.0, textlen=1e-3, bcl=BCL, amplitude=cm_stim())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        t = torch.tensor([sec], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    value = world * N_CELLS * args.steps / sec
+    audit = b.audit()
+    ms_kernel = 1e3 * sec / args.steps
+    achieved = MIXED_BYTES_PER_CELL_STEP * N_CELLS / (ms_kernel / 1e3) / 1e9
+    del b
+    torch.cuda.empty_cache()
+
+    # ---- plain FP64 kernel on the same workload
+    _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
+    vm64 = torch.tensor(b64.init_vm(), device="cuda")
+    sec64 = time_device_steps(torch, cm, b64, stream, vm64, args.fp64_steps, 3, 0.0)
+    fp64_value = N_CELLS * args.fp64_steps / sec64
+    fp64_ms = 1e3 * sec64 / args.fp64_steps
+    del b64
+    torch.cuda.empty_cache()
+
+    # ---- end to end through the C ABI with pinned host buffers
+    _, be = make_batch(cm, cm.MIXED, stream.cuda_stream)
+    vm_h = torch.from_numpy(be.init_vm()).pin_memory()
+    ie_h = torch.zeros(N_CELLS, dtype=torch.float64).pin_memory()
+    amp = cm_stim()
+    for s in range(3):
+        ie_h.fill_(amp if s * DT <= 1e-3 else 0.0)
+        be.calc_update(DT, vm_h, ie_h, None, vm_range=0.2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(args.e2e_steps):
+        ie_h.fill_(amp if (s + 3) * DT <= 1e-3 else 0.0)
+        be.calc_update(DT, vm_h, ie_h, None, vm_range=0.2)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e2e_sec = max(wall, e0.elapsed_time(e1) / 1e3)
+    e2e_value = N_CELLS * args.e2e_steps / e2e_sec
+    del be
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(seconds=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_kernel, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64acc", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": N_CELLS, "model": "TenTusscher2 epi", "dt_ms": DT * 1e3,
+                       "bcl_ms": BCL * 1e3, "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.9,1.1] seed 2",
+                       "precision": "mixed (FP32 gates/currents, FP64 Vm/Na_i/K_i/CaSR)",
+                       "l2": "state 430 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas{world}"},
+            "plain_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
+                           "bytes_per_cell_step": FP64_BYTES_PER_CELL_STEP,
+                           "achieved_gbs": FP64_BYTES_PER_CELL_STEP * N_CELLS / (fp64_ms / 1e3) / 1e9},
+            "speedup_vs_plain_fp64": value / fp64_value,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * N_CELLS,
+                    "d2h_bytes_per_step": 8 * N_CELLS, "steps": args.e2e_steps,
+                    "api": "cm_batch_step_update, pinned host Vm and i_ext"},
+            "roofline": {"bound": "hbm", "kernel": "tt2_mixed_kernel", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                         "bytes_per_cell_step": MIXED_BYTES_PER_CELL_STEP, "traffic": None},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "audit_mask": audit,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cm_stim():
+    from cardiomechanics_gb300 import workloads as W
+    return W.TT2_STIM_NA
+
+
+if __name__ == "__main__":
+    main()

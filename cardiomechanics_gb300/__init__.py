@@ -1,0 +1,270 @@
+"""GB300-native cell-model update for KIT-IBT/CardioMechanics' electrophysiology reaction step.
+
+The compute lives in libcmgb300.so (hand-written sm_103a CUDA + a C ABI, declared in
+include/cardiomech_gb300.h). This module is a thin ctypes view of that ABI whose names
+follow the reference's cell-model interface:
+
+    reference (CellModel/)                          here
+    initElphyParameters(&pep, ev, emt, tinc)        Params(model, ev_path, dt)
+    initElphyModel(&pem, pep, emt) x N + Init()     Batch(params, n_cells, precision)
+    pem->AddHeteroValue(name, v)                    batch.add_hetero_value(name, values)
+    pem->Calc(tinc, Vm, i_ext, stretch, 1)          batch.calc(dt, Vm, i_ext, stretch) -> dVm
+    Vm += Calc(...) driver loop (CellModel.h:420)   batch.run(Vm, n_steps, stimulus)
+    GetBase()/GetSize(), Read/WriteStatus           batch.get_state(layout) / set_state
+    GetVm(), GetAmplitude(), GetStimTime()          batch.init_vm(), params.info
+
+There is no CPU path: without the library or without a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libcmgb300.so"
+
+TENTUSSCHER2 = 5
+COURTEMANCHE = 2
+FP64, MIXED = 0, 1
+LAYOUT_REF_BLOCK, LAYOUT_SOA = 0, 1
+AUDIT_NAN, AUDIT_VRANGE, AUDIT_CARANGE, AUDIT_GATE, AUDIT_SURROGATE, AUDIT_VMRANGE = 1, 2, 4, 8, 16, 32
+
+_STATUS = {0: "CM_OK", -1: "CM_ERR_ARG", -2: "CM_ERR_MODEL", -3: "CM_ERR_FILE", -4: "CM_ERR_PARAM",
+           -5: "CM_ERR_CUDA", -6: "CM_ERR_NOMEM", -7: "CM_ERR_UNSUPPORTED", -8: "CM_ERR_NUMERIC"}
+
+# Exported symbols of the C ABI (include/cardiomech_gb300.h).
+ABI_SYMBOLS = (
+    "cm_abi_version", "cm_last_error", "cm_model_from_name", "cm_model_info", "cm_state_name",
+    "cm_params_create", "cm_params_destroy", "cm_params_info", "cm_params_get", "cm_params_set",
+    "cm_params_table", "cm_batch_create", "cm_batch_destroy", "cm_batch_info", "cm_batch_reset",
+    "cm_batch_set_hetero", "cm_batch_set_diagnostics", "cm_batch_init_vm", "cm_batch_get_state",
+    "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
+)
+
+
+class CMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("n_state_vars", ctypes.c_int), ("ref_block_doubles", ctypes.c_int),
+                ("n_tables", ctypes.c_int), ("table_rows", ctypes.c_int), ("dt", ctypes.c_double),
+                ("init_vm", ctypes.c_double), ("amplitude", ctypes.c_double), ("stim_time", ctypes.c_double)]
+
+
+class Stimulus(ctypes.Structure):
+    _fields_ = [("t0", ctypes.c_double), ("textbegin", ctypes.c_double),
+                ("textbegin_per_cell", ctypes.POINTER(ctypes.c_double)), ("textlen", ctypes.c_double),
+                ("bcl", ctypes.c_double), ("amplitude", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library. Raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m cardiomechanics_gb300.build`")
+    L = ctypes.CDLL(str(LIB_PATH))
+    vp, dp, i64 = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int64
+    L.cm_last_error.restype = ctypes.c_char_p
+    L.cm_state_name.restype = ctypes.c_char_p
+    L.cm_model_from_name.argtypes = [ctypes.c_char_p]
+    L.cm_model_info.argtypes = [ctypes.c_int, ctypes.POINTER(Info)]
+    L.cm_params_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_char_p, ctypes.c_double]
+    L.cm_params_destroy.argtypes = [vp]
+    L.cm_params_info.argtypes = [vp, ctypes.POINTER(Info)]
+    L.cm_params_get.argtypes = [vp, ctypes.c_char_p, dp]
+    L.cm_params_set.argtypes = [vp, ctypes.c_char_p, ctypes.c_double]
+    L.cm_params_table.argtypes = [vp, ctypes.c_char_p, dp]
+    L.cm_batch_create.argtypes = [ctypes.POINTER(vp), vp, i64, ctypes.c_int, vp]
+    L.cm_batch_destroy.argtypes = [vp]
+    L.cm_batch_info.argtypes = [vp, ctypes.POINTER(Info), ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int)]
+    L.cm_batch_reset.argtypes = [vp]
+    L.cm_batch_set_hetero.argtypes = [vp, ctypes.c_char_p, vp]
+    L.cm_batch_set_diagnostics.argtypes = [vp, ctypes.c_int]
+    L.cm_batch_init_vm.argtypes = [vp, vp]
+    L.cm_batch_get_state.argtypes = [vp, ctypes.c_int, vp]
+    L.cm_batch_set_state.argtypes = [vp, ctypes.c_int, vp]
+    L.cm_batch_step.argtypes = [vp, ctypes.c_double, vp, vp, vp, vp]
+    L.cm_batch_step_update.argtypes = [vp, ctypes.c_double, vp, vp, vp, ctypes.c_double]
+    L.cm_batch_run.argtypes = [vp, vp, i64, ctypes.POINTER(Stimulus), vp, i64, i64, vp]
+    L.cm_batch_audit.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise CMError(rc, lib().cm_last_error().decode())
+
+
+def _ptr(a):
+    """Raw address of a numpy array, a torch tensor (host or device) or None."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+def _f64(a, n, name):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != n:
+            raise ValueError(f"{name}: need a contiguous float64 array of {n} elements")
+        return a
+    import torch  # device tensors are plumbing only
+    if a.dtype != torch.float64 or not a.is_contiguous() or a.numel() != n:
+        raise ValueError(f"{name}: need a contiguous float64 tensor of {n} elements")
+    return a
+
+
+def model_info(model: int) -> Info:
+    info = Info()
+    _check(lib().cm_model_info(model, ctypes.byref(info)))
+    return info
+
+
+def state_names(model: int) -> list[str]:
+    return [lib().cm_state_name(model, k).decode() for k in range(model_info(model).n_state_vars)]
+
+
+class Params:
+    """Parameter set + lookup tables for one (model, .ev file, dt): initElphyParameters."""
+
+    def __init__(self, model: int | str, ev_path: str | None = None, dt: float = 1e-5):
+        if isinstance(model, str):
+            m = lib().cm_model_from_name(model.encode())
+            if m < 0:
+                raise CMError(-2, f"unknown model {model}")
+            model = m
+        h = ctypes.c_void_p()
+        _check(lib().cm_params_create(ctypes.byref(h), model, ev_path.encode() if ev_path else None, dt))
+        self._h = h
+        self.model = model
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_params_destroy(self._h)
+            self._h = None
+
+    @property
+    def info(self) -> Info:
+        info = Info()
+        _check(lib().cm_params_info(self._h, ctypes.byref(info)))
+        return info
+
+    def get(self, name: str) -> float:
+        v = ctypes.c_double()
+        _check(lib().cm_params_get(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def set(self, name: str, value: float) -> None:
+        _check(lib().cm_params_set(self._h, name.encode(), value))
+
+    def table(self, name: str) -> np.ndarray:
+        out = np.zeros(self.info.table_rows)
+        _check(lib().cm_params_table(self._h, name.encode(), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+
+class Batch:
+    """n_cells cells of one model on the GPU: initElphyModel x n + Init()."""
+
+    def __init__(self, params: Params, n_cells: int, precision: int = FP64, stream=None):
+        h = ctypes.c_void_p()
+        s = None if stream is None else ctypes.c_void_p(int(stream))
+        _check(lib().cm_batch_create(ctypes.byref(h), params._h, int(n_cells), precision, s))
+        self._h = h
+        self.n = int(n_cells)
+        self.model = params.model
+        self.precision = precision
+        self.info = params.info
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def reset(self):
+        _check(lib().cm_batch_reset(self._h))
+
+    def add_hetero_value(self, name: str, values) -> None:
+        v = None if values is None else _f64(np.ascontiguousarray(values, np.float64)
+                                             if not hasattr(values, "data_ptr") else values, self.n, name)
+        _check(lib().cm_batch_set_hetero(self._h, name.encode(), _ptr(v)))
+
+    def set_diagnostics(self, on: bool) -> None:
+        _check(lib().cm_batch_set_diagnostics(self._h, int(on)))
+
+    def init_vm(self) -> np.ndarray:
+        out = np.zeros(self.n)
+        _check(lib().cm_batch_init_vm(self._h, _ptr(out)))
+        return out
+
+    def get_state(self, layout: int = LAYOUT_SOA) -> np.ndarray:
+        k = self.info.n_state_vars if layout == LAYOUT_SOA else self.info.ref_block_doubles
+        out = np.zeros(k * self.n)
+        _check(lib().cm_batch_get_state(self._h, layout, _ptr(out)))
+        return out.reshape((k, self.n) if layout == LAYOUT_SOA else (self.n, k))
+
+    def set_state(self, buf, layout: int = LAYOUT_SOA) -> None:
+        b = np.ascontiguousarray(buf, np.float64)
+        _check(lib().cm_batch_set_state(self._h, layout, _ptr(b)))
+
+    def calc(self, dt, Vm, i_ext=None, stretch=None, dVm=None):
+        """One reference Calc per cell; returns dVm (host numpy unless device dVm given)."""
+        Vm = _f64(Vm, self.n, "Vm")
+        i_ext = _f64(i_ext, self.n, "i_ext")
+        stretch = _f64(stretch, self.n, "stretch")
+        if dVm is None:
+            dVm = np.zeros(self.n)
+        _check(lib().cm_batch_step(self._h, dt, _ptr(Vm), _ptr(i_ext), _ptr(stretch), _ptr(dVm)))
+        return dVm
+
+    def calc_update(self, dt, Vm, i_ext=None, stretch=None, vm_range=0.0):
+        """One Calc per cell fused with Vm += dVm and the NaN/range check; Vm updated in place."""
+        Vm = _f64(Vm, self.n, "Vm")
+        i_ext = _f64(i_ext, self.n, "i_ext")
+        stretch = _f64(stretch, self.n, "stretch")
+        _check(lib().cm_batch_step_update(self._h, dt, _ptr(Vm), _ptr(i_ext), _ptr(stretch), vm_range))
+
+    def run(self, Vm, n_steps, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0, t0=0.0,
+            textbegin_per_cell=None, probe_cells=None, probe_every=0):
+        """Fused driver loop; Vm (host numpy or device tensor) updated in place. Returns the
+        probe traces (n_probe, n_rec) when probe_cells is given."""
+        Vm = _f64(Vm, self.n, "Vm")
+        tbc = None
+        if textbegin_per_cell is not None:
+            tbc = np.ascontiguousarray(textbegin_per_cell, np.float64)
+        st = Stimulus(t0, textbegin, None if tbc is None else tbc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                      textlen, bcl, amplitude)
+        pc = None
+        n_probe = 0
+        trace = None
+        if probe_cells is not None:
+            pc = np.ascontiguousarray(probe_cells, np.int64)
+            n_probe = pc.size
+            n_rec = (n_steps + probe_every - 1) // probe_every
+            trace = np.zeros((n_probe, n_rec))
+        _check(lib().cm_batch_run(self._h, _ptr(Vm), int(n_steps), ctypes.byref(st), _ptr(pc), n_probe,
+                                  int(probe_every), _ptr(trace)))
+        return trace
+
+    def audit(self, per_cell: bool = False):
+        m = ctypes.c_uint32()
+        pc = np.zeros(self.n, np.uint32) if per_cell else None
+        _check(lib().cm_batch_audit(self._h, ctypes.byref(m), _ptr(pc)))
+        return (m.value, pc) if per_cell else m.value

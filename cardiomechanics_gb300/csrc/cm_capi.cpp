@@ -1,0 +1,669 @@
+// C ABI of libcmgb300.so (declared in include/cardiomech_gb300.h): handles, argument
+// checking, host/device staging and dispatch to the kernels. No exception leaves this file.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cardiomech_gb300.h"
+#include "cm_launch.h"
+#include "cm_params.h"
+
+using namespace cm;
+
+struct cm_params_s {
+  ParamSet ps;
+};
+
+struct cm_batch_s {
+  ParamSet ps;
+  DevBatch d;
+  cudaStream_t stream = nullptr;
+  void *state_mem = nullptr;   // one allocation: FP64 block then FP32 block
+  void *table_mem = nullptr;   // rows/eca in FP64 (FP64 batches) or FP32 (mixed)
+  void *het_mem[6] = {};
+  uint32_t *audit_cell = nullptr;
+  unsigned int *audit_or = nullptr;
+  double *diag = nullptr;
+  bool diag_on = false;
+  // staging buffers for host arrays, grown on demand
+  double *stage[4] = {};
+  int64_t stage_n = 0;
+  double *tb_cell = nullptr;
+  int64_t *probe_idx = nullptr;
+  int64_t probe_cap = 0;
+  double *probe_out = nullptr;
+  int64_t probe_out_cap = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return CM_ERR_CUDA;
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+int64_t round_ld(int64_t n) { return ((n + 63) / 64) * 64; }
+
+// SOA index (model order) -> position in the mixed layout: {is_fp64, slot}.
+void mixed_slot(int model, int k, bool &fp64, int &slot) {
+  if (model == kTenTusscher2) {
+    // SOA: Ca_i CaSR CaSS Na_i K_i m h j xr1 xr2 xs r s d f f2 fCa Rq
+    static const int map32[] = {13, -1, 14, -1, -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
+    static const int map64[] = {-1, 0, -1, 1, 2};
+    if (k < 5 && map64[k] >= 0) {
+      fp64 = true;
+      slot = map64[k];
+    } else {
+      fp64 = false;
+      slot = map32[k];
+    }
+  } else {
+    // SOA: Ca_i Ca_up Ca_rel h j oi ui Xr Xs u v w Na_i K_i m oa ua d f f_Ca Ca_TRPN
+    static const int map32[] = {15, -1, -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, -1, -1, 9, 10, 11, 12, 13, 14, 16};
+    static const int map64[] = {-1, 0, 1, -1, -1, -1, -1, -1, -1, -1, -1, -1, 2, 3};
+    if (k < 14 && map64[k] >= 0) {
+      fp64 = true;
+      slot = map64[k];
+    } else {
+      fp64 = false;
+      slot = map32[k];
+    }
+  }
+}
+
+// Reference backup block index of SOA variable k (TenTusscher2.h:77-123, CourtemancheEtAl.h:32-42).
+int ref_block_index(int model, int k) {
+  if (model == kTenTusscher2) return k < 5 ? k : k + 18;
+  return k < 20 ? k : 21;
+}
+
+int ensure_stage(cm_batch_s *b, int64_t n) {
+  if (b->stage_n >= n) return CM_OK;
+  for (auto &p : b->stage) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  b->stage_n = 0;
+  for (auto &p : b->stage) CK(cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(double)));
+  b->stage_n = n;
+  return CM_OK;
+}
+
+// Device view of a caller array: the pointer itself if on the device, else a staged copy.
+int stage_in(cm_batch_s *b, const double *p, int slot, const double **out) {
+  if (!p) {
+    *out = nullptr;
+    return CM_OK;
+  }
+  if (is_device_ptr(p)) {
+    *out = p;
+    return CM_OK;
+  }
+  int rc = ensure_stage(b, b->d.n);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(b->stage[slot], p, b->d.n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  *out = b->stage[slot];
+  return CM_OK;
+}
+
+int upload_tables(cm_batch_s *b) {
+  if (b->table_mem) cudaFree(b->table_mem);
+  b->table_mem = nullptr;
+  if (b->d.precision == CM_PREC_FP64) {
+    std::vector<double> rows, eca;
+    b->ps.rows_fp64(rows, eca);
+    size_t nb = (rows.size() + eca.size()) * sizeof(double);
+    CK(cudaMalloc(&b->table_mem, nb));
+    double *dst = (double *)b->table_mem;
+    CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!eca.empty()) CK(cudaMemcpy(dst + rows.size(), eca.data(), eca.size() * sizeof(double), cudaMemcpyHostToDevice));
+    b->d.rows64 = dst;
+    b->d.eca64 = eca.empty() ? nullptr : dst + rows.size();
+  } else {
+    std::vector<float> rows, eca;
+    b->ps.rows_fp32(rows, eca);
+    size_t nb = (rows.size() + eca.size()) * sizeof(float);
+    CK(cudaMalloc(&b->table_mem, nb));
+    float *dst = (float *)b->table_mem;
+    CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (!eca.empty()) CK(cudaMemcpy(dst + rows.size(), eca.data(), eca.size() * sizeof(float), cudaMemcpyHostToDevice));
+    b->d.rows32 = dst;
+    b->d.eca32 = eca.empty() ? nullptr : dst + rows.size();
+  }
+  if (b->ps.spec->model == kTenTusscher2) b->ps.tt2_consts(b->d.tt2_64, b->d.tt2_32);
+  else b->ps.crn_consts(b->d.crn_64, b->d.crn_32);
+  return CM_OK;
+}
+
+// Host SOA (n_state x n, model order) <-> device layout.
+int soa_to_device(cm_batch_s *b, const std::vector<double> &soa) {
+  const int64_t n = b->d.n, ld = b->d.ld;
+  const int ns = b->ps.spec->n_state;
+  if (b->d.precision == CM_PREC_FP64) {
+    for (int k = 0; k < ns; k++)
+      CK(cudaMemcpyAsync(b->d.s64 + k * ld, soa.data() + (size_t)k * n, n * sizeof(double), cudaMemcpyHostToDevice,
+                         b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return CM_OK;
+  }
+  std::vector<float> f(n);
+  for (int k = 0; k < ns; k++) {
+    bool fp64;
+    int slot;
+    mixed_slot(b->d.model, k, fp64, slot);
+    if (fp64) {
+      CK(cudaMemcpy(b->d.s64 + slot * ld, soa.data() + (size_t)k * n, n * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+      for (int64_t c = 0; c < n; c++) f[c] = (float)soa[(size_t)k * n + c];
+      CK(cudaMemcpy(b->d.s32 + slot * ld, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+  }
+  return CM_OK;
+}
+
+int device_to_soa(cm_batch_s *b, std::vector<double> &soa) {
+  const int64_t n = b->d.n, ld = b->d.ld;
+  const int ns = b->ps.spec->n_state;
+  soa.assign((size_t)ns * n, 0.0);
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->d.precision == CM_PREC_FP64) {
+    for (int k = 0; k < ns; k++)
+      CK(cudaMemcpy(soa.data() + (size_t)k * n, b->d.s64 + k * ld, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return CM_OK;
+  }
+  std::vector<float> f(n);
+  for (int k = 0; k < ns; k++) {
+    bool fp64;
+    int slot;
+    mixed_slot(b->d.model, k, fp64, slot);
+    if (fp64) {
+      CK(cudaMemcpy(soa.data() + (size_t)k * n, b->d.s64 + slot * ld, n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      CK(cudaMemcpy(f.data(), b->d.s32 + slot * ld, n * sizeof(float), cudaMemcpyDeviceToHost));
+      for (int64_t c = 0; c < n; c++) soa[(size_t)k * n + c] = f[c];
+    }
+  }
+  return CM_OK;
+}
+
+void fill_info(const ParamSet &ps, cm_info *info) {
+  info->model = ps.spec->model;
+  info->n_state_vars = ps.spec->n_state;
+  info->ref_block_doubles = ps.spec->ref_block_doubles;
+  info->n_tables = ps.spec->n_tables;
+  info->table_rows = kRows;
+  info->dt = ps.dt;
+  info->init_vm = ps.init_vm();
+  info->amplitude = ps.amplitude();
+  info->stim_time = ps.stim_time();
+}
+
+}  // namespace
+
+extern "C" {
+
+int cm_abi_version(void) { return CM_ABI_VERSION; }
+
+const char *cm_last_error(void) { return g_err.c_str(); }
+
+int cm_model_from_name(const char *name) { return model_from_name(name); }
+
+int cm_model_info(int model, cm_info *info) {
+  const ModelSpec *s = find_model(model);
+  if (!s) return fail(CM_ERR_MODEL, "model not implemented: " + std::to_string(model));
+  if (!info) return fail(CM_ERR_ARG, "info is NULL");
+  memset(info, 0, sizeof(*info));
+  info->model = model;
+  info->n_state_vars = s->n_state;
+  info->ref_block_doubles = s->ref_block_doubles;
+  info->n_tables = s->n_tables;
+  info->table_rows = kRows;
+  return CM_OK;
+}
+
+const char *cm_state_name(int model, int k) {
+  const ModelSpec *s = find_model(model);
+  if (!s || k < 0 || k >= s->n_state) return nullptr;
+  return s->state_names[k];
+}
+
+int cm_params_create(cm_params_t *out, int model, const char *ev_path, double dt) {
+  if (!out) return fail(CM_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  auto *p = new (std::nothrow) cm_params_s();
+  if (!p) return fail(CM_ERR_NOMEM, "host allocation failed");
+  std::string err;
+  int rc = p->ps.init(model, ev_path, dt, err);
+  if (rc) {
+    delete p;
+    return fail(rc, err);
+  }
+  *out = p;
+  return CM_OK;
+}
+
+int cm_params_destroy(cm_params_t p) {
+  delete p;
+  return CM_OK;
+}
+
+int cm_params_info(cm_params_t p, cm_info *info) {
+  if (!p || !info) return fail(CM_ERR_ARG, "NULL argument");
+  fill_info(p->ps, info);
+  return CM_OK;
+}
+
+int cm_params_get(cm_params_t p, const char *name, double *value) {
+  if (!p || !name || !value) return fail(CM_ERR_ARG, "NULL argument");
+  int i = p->ps.index(name);
+  if (i < 0) return fail(CM_ERR_PARAM, std::string("unknown parameter ") + name);
+  *value = p->ps.vals[i];
+  return CM_OK;
+}
+
+int cm_params_set(cm_params_t p, const char *name, double value) {
+  if (!p || !name) return fail(CM_ERR_ARG, "NULL argument");
+  int i = p->ps.index(name);
+  if (i < 0) return fail(CM_ERR_PARAM, std::string("unknown parameter ") + name);
+  if (i >= p->ps.spec->n_base) return fail(CM_ERR_PARAM, std::string(name) + " is derived; set its inputs");
+  p->ps.vals[i] = value;
+  p->ps.rebuild();
+  return CM_OK;
+}
+
+int cm_params_table(cm_params_t p, const char *name, double *out) {
+  if (!p || !name || !out) return fail(CM_ERR_ARG, "NULL argument");
+  for (int k = 0; k < p->ps.spec->n_tables; k++)
+    if (!strcmp(p->ps.spec->table_names[k], name)) {
+      memcpy(out, p->ps.tables[k].data(), kRows * sizeof(double));
+      return CM_OK;
+    }
+  if (p->ps.spec->model == kCourtemanche && (!strcmp(name, "exp250") || !strcmp(name, "exp50"))) {
+    out[0] = !strcmp(name, "exp250") ? p->ps.exp250 : p->ps.exp50;
+    return CM_OK;
+  }
+  return fail(CM_ERR_PARAM, std::string("unknown table ") + name);
+}
+
+int cm_batch_destroy(cm_batch_t b);
+
+int cm_batch_create(cm_batch_t *out, cm_params_t p, int64_t n_cells, int precision, void *stream) {
+  if (!out || !p) return fail(CM_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  if (n_cells < 0) return fail(CM_ERR_ARG, "n_cells < 0");
+  if (precision != CM_PREC_FP64 && precision != CM_PREC_MIXED) return fail(CM_ERR_ARG, "unknown precision");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(CM_ERR_CUDA, "no CUDA device: this library has no CPU path");
+  }
+  auto *b = new (std::nothrow) cm_batch_s();
+  if (!b) return fail(CM_ERR_NOMEM, "host allocation failed");
+  b->ps = p->ps;
+  b->stream = (cudaStream_t)stream;
+  b->d.model = p->ps.spec->model;
+  b->d.precision = precision;
+  b->d.n = n_cells;
+  b->d.ld = round_ld(n_cells);
+  const int64_t ld = b->d.ld;
+  const size_t n64 = (size_t)n_fp64_vars(b->d.model, precision) * ld;
+  const size_t n32 = precision == CM_PREC_MIXED ? (size_t)n_fp32_vars(b->d.model) * ld : 0;
+  int rc = CM_OK;
+  cudaError_t e = cudaMalloc(&b->state_mem, std::max<size_t>(1, n64 * sizeof(double) + n32 * sizeof(float)));
+  if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(state)");
+  if (!rc) {
+    b->d.s64 = (double *)b->state_mem;
+    b->d.s32 = precision == CM_PREC_MIXED ? (float *)(b->d.s64 + n64) : nullptr;
+    e = cudaMalloc(&b->audit_cell, std::max<int64_t>(1, n_cells) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->audit_or, sizeof(unsigned int));
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(audit)");
+  }
+  if (!rc) {
+    b->d.audit_cell = b->audit_cell;
+    b->d.audit_or = b->audit_or;
+    rc = upload_tables(b);
+  }
+  if (!rc) rc = cm_batch_reset(b);
+  if (rc) {
+    std::string keep = g_err;
+    cm_batch_destroy(b);
+    g_err = keep;
+    return rc;
+  }
+  *out = b;
+  return CM_OK;
+}
+
+int cm_batch_destroy(cm_batch_t b) {
+  if (!b) return CM_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  else cudaDeviceSynchronize();
+  cudaFree(b->state_mem);
+  cudaFree(b->table_mem);
+  for (auto p : b->het_mem) cudaFree(p);
+  cudaFree(b->audit_cell);
+  cudaFree(b->audit_or);
+  cudaFree(b->diag);
+  for (auto p : b->stage) cudaFree(p);
+  cudaFree(b->tb_cell);
+  cudaFree(b->probe_idx);
+  cudaFree(b->probe_out);
+  delete b;
+  return CM_OK;
+}
+
+int cm_batch_info(cm_batch_t b, cm_info *info, int64_t *n_cells, int *precision) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (info) fill_info(b->ps, info);
+  if (n_cells) *n_cells = b->d.n;
+  if (precision) *precision = b->d.precision;
+  return CM_OK;
+}
+
+int cm_batch_reset(cm_batch_t b) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  std::vector<double> one;
+  b->ps.init_state(one);
+  const int64_t n = b->d.n;
+  std::vector<double> soa((size_t)one.size() * n);
+  for (size_t k = 0; k < one.size(); k++) std::fill(soa.begin() + k * n, soa.begin() + (k + 1) * n, one[k]);
+  int rc = soa_to_device(b, soa);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(b->audit_cell, 0, std::max<int64_t>(1, n) * sizeof(uint32_t), b->stream));
+  CK(cudaMemsetAsync(b->audit_or, 0, sizeof(unsigned int), b->stream));
+  if (b->diag) {
+    const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+    CK(cudaMemsetAsync(b->diag, 0, (size_t)nd * b->d.ld * sizeof(double), b->stream));
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return CM_OK;
+}
+
+int cm_batch_set_diagnostics(cm_batch_t b, int on) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (on && b->d.precision != CM_PREC_FP64) return fail(CM_ERR_UNSUPPORTED, "diagnostic currents need an FP64 batch");
+  if (on && !b->diag) {
+    const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+    CK(cudaMalloc(&b->diag, (size_t)nd * b->d.ld * sizeof(double)));
+    CK(cudaMemset(b->diag, 0, (size_t)nd * b->d.ld * sizeof(double)));
+  }
+  b->diag_on = on != 0;
+  b->d.diag = b->diag_on ? b->diag : nullptr;
+  return CM_OK;
+}
+
+int cm_batch_set_hetero(cm_batch_t b, const char *name, const double *values) {
+  if (!b || !name) return fail(CM_ERR_ARG, "NULL argument");
+  int slot = -1;
+  for (int k = 0; k < b->ps.spec->n_het; k++)
+    if (!strcmp(b->ps.spec->het_names[k], name)) slot = k;
+  if (slot < 0) {
+    if (b->ps.index(name) < 0) return fail(CM_ERR_PARAM, std::string("unknown parameter ") + name);
+    return fail(CM_ERR_UNSUPPORTED, std::string("per-cell values of ") + name + " are not supported");
+  }
+  if (!values) {
+    cudaFree(b->het_mem[slot]);
+    b->het_mem[slot] = nullptr;
+    b->d.het[slot] = nullptr;
+    return CM_OK;
+  }
+  const int64_t n = b->d.n;
+  std::vector<double> host(n);
+  if (is_device_ptr(values)) CK(cudaMemcpy(host.data(), values, n * sizeof(double), cudaMemcpyDeviceToHost));
+  else memcpy(host.data(), values, n * sizeof(double));
+  const size_t es = b->d.precision == CM_PREC_FP64 ? sizeof(double) : sizeof(float);
+  if (!b->het_mem[slot]) CK(cudaMalloc(&b->het_mem[slot], std::max<int64_t>(1, n) * es));
+  if (b->d.precision == CM_PREC_FP64) {
+    CK(cudaMemcpy(b->het_mem[slot], host.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> f(host.begin(), host.end());
+    CK(cudaMemcpy(b->het_mem[slot], f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  b->d.het[slot] = b->het_mem[slot];
+  return CM_OK;
+}
+
+int cm_batch_init_vm(cm_batch_t b, double *Vm) {
+  if (!b || !Vm) return fail(CM_ERR_ARG, "NULL argument");
+  std::vector<double> v(b->d.n, b->ps.init_vm());
+  if (is_device_ptr(Vm)) CK(cudaMemcpy(Vm, v.data(), b->d.n * sizeof(double), cudaMemcpyHostToDevice));
+  else memcpy(Vm, v.data(), b->d.n * sizeof(double));
+  return CM_OK;
+}
+
+int cm_batch_get_state(cm_batch_t b, int layout, double *buf) {
+  if (!b || !buf) return fail(CM_ERR_ARG, "NULL argument");
+  if (layout != CM_LAYOUT_SOA && layout != CM_LAYOUT_REF_BLOCK) return fail(CM_ERR_ARG, "unknown layout");
+  std::vector<double> soa;
+  int rc = device_to_soa(b, soa);
+  if (rc) return rc;
+  const int64_t n = b->d.n;
+  const int ns = b->ps.spec->n_state, nb = b->ps.spec->ref_block_doubles;
+  std::vector<double> out;
+  if (layout == CM_LAYOUT_SOA) {
+    out.swap(soa);
+  } else {
+    out.assign((size_t)nb * n, 0.0);
+    for (int k = 0; k < ns; k++) {
+      const int pos = ref_block_index(b->d.model, k);
+      for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + pos] = soa[(size_t)k * n + c];
+    }
+    if (b->diag) {  // diagnostic slots: TT2 Array[0..16], CRN I_SAC
+      const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+      std::vector<double> dg((size_t)nd * n);
+      for (int k = 0; k < nd; k++)
+        CK(cudaMemcpy(dg.data() + (size_t)k * n, b->diag + k * b->d.ld, n * sizeof(double), cudaMemcpyDeviceToHost));
+      const int base = b->d.model == kTenTusscher2 ? 5 : 20;
+      for (int k = 0; k < nd; k++)
+        for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + base + k] = dg[(size_t)k * n + c];
+    }
+  }
+  if (is_device_ptr(buf)) CK(cudaMemcpy(buf, out.data(), out.size() * sizeof(double), cudaMemcpyHostToDevice));
+  else memcpy(buf, out.data(), out.size() * sizeof(double));
+  return CM_OK;
+}
+
+int cm_batch_set_state(cm_batch_t b, int layout, const double *buf) {
+  if (!b || !buf) return fail(CM_ERR_ARG, "NULL argument");
+  if (layout != CM_LAYOUT_SOA && layout != CM_LAYOUT_REF_BLOCK) return fail(CM_ERR_ARG, "unknown layout");
+  const int64_t n = b->d.n;
+  const int ns = b->ps.spec->n_state, nb = b->ps.spec->ref_block_doubles;
+  const size_t count = (size_t)(layout == CM_LAYOUT_SOA ? ns : nb) * n;
+  std::vector<double> in(count);
+  if (is_device_ptr(buf)) CK(cudaMemcpy(in.data(), buf, count * sizeof(double), cudaMemcpyDeviceToHost));
+  else memcpy(in.data(), buf, count * sizeof(double));
+  std::vector<double> soa;
+  if (layout == CM_LAYOUT_SOA) {
+    soa.swap(in);
+  } else {
+    soa.assign((size_t)ns * n, 0.0);
+    for (int k = 0; k < ns; k++) {
+      const int pos = ref_block_index(b->d.model, k);
+      for (int64_t c = 0; c < n; c++) soa[(size_t)k * n + c] = in[(size_t)c * nb + pos];
+    }
+  }
+  return soa_to_device(b, soa);
+}
+
+int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext, const double *stretch, double *dVm) {
+  if (!b || !Vm || !dVm) return fail(CM_ERR_ARG, "NULL argument");
+  if (dt != b->ps.dt)
+    return fail(CM_ERR_ARG, "dt differs from the parameter set's dt (" + std::to_string(b->ps.dt) +
+                                "): the lookup tables depend on dt; create a parameter set for this dt");
+  if (b->d.n == 0) return CM_OK;
+  StepIO io;
+  int rc;
+  if ((rc = stage_in(b, Vm, 0, &io.vm))) return rc;
+  if ((rc = stage_in(b, i_ext, 1, &io.iext))) return rc;
+  if ((rc = stage_in(b, stretch, 2, &io.stretch))) return rc;
+  const bool host_out = !is_device_ptr(dVm);
+  if (host_out) {
+    if ((rc = ensure_stage(b, b->d.n))) return rc;
+    io.dvm = b->stage[3];
+  } else {
+    io.dvm = dVm;
+  }
+  CK(launch_step(b->d, io, 0, 0, b->stream));
+  if (host_out) {
+    CK(cudaMemcpyAsync(dVm, io.dvm, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+  }
+  return CM_OK;
+}
+
+int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
+                         double vm_range) {
+  if (!b || !Vm) return fail(CM_ERR_ARG, "NULL argument");
+  if (dt != b->ps.dt)
+    return fail(CM_ERR_ARG, "dt differs from the parameter set's dt (" + std::to_string(b->ps.dt) +
+                                "): the lookup tables depend on dt; create a parameter set for this dt");
+  if (b->d.n == 0) return CM_OK;
+  StepIO io;
+  int rc;
+  const bool host_vm = !is_device_ptr(Vm);
+  const double *vin;
+  if ((rc = stage_in(b, Vm, 0, &vin))) return rc;
+  io.vm = vin;
+  io.vm_out = const_cast<double *>(vin);
+  io.vm_range = vm_range;
+  if ((rc = stage_in(b, i_ext, 1, &io.iext))) return rc;
+  if ((rc = stage_in(b, stretch, 2, &io.stretch))) return rc;
+  CK(launch_step(b->d, io, 0, 0, b->stream));
+  if (host_vm) CK(cudaMemcpyAsync(Vm, io.vm_out, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  unsigned int mask = 0;
+  CK(cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (mask & (CM_AUDIT_NAN | CM_AUDIT_VMRANGE))
+    return fail(CM_ERR_NUMERIC, "Vm is NaN, infinite or outside the allowed range in at least one cell");
+  return CM_OK;
+}
+
+int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *stim, const int64_t *probe_cells,
+                 int64_t n_probe, int64_t probe_every, double *probe_vm) {
+  if (!b || !Vm) return fail(CM_ERR_ARG, "NULL argument");
+  if (n_steps < 0) return fail(CM_ERR_ARG, "n_steps < 0");
+  if (n_probe > 0 && (!probe_cells || !probe_vm || probe_every <= 0))
+    return fail(CM_ERR_ARG, "probes need probe_cells, probe_vm and probe_every > 0");
+  const int64_t n = b->d.n;
+  if (n == 0 || n_steps == 0) return CM_OK;
+  int rc;
+  const bool host_vm = !is_device_ptr(Vm);
+  double *dvm = Vm;
+  if (host_vm) {
+    if ((rc = ensure_stage(b, n))) return rc;
+    dvm = b->stage[0];
+    CK(cudaMemcpyAsync(dvm, Vm, n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
+  cm_stimulus st = {};
+  if (stim) st = *stim;
+  const bool per_cell = stim && stim->textbegin_per_cell;
+  if (per_cell) {
+    if (!b->tb_cell) CK(cudaMalloc(&b->tb_cell, std::max<int64_t>(1, n) * sizeof(double)));
+    const double *src = stim->textbegin_per_cell;
+    CK(cudaMemcpyAsync(b->tb_cell, src, n * sizeof(double),
+                       is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
+  }
+  const int64_t n_rec = n_probe > 0 ? (n_steps + probe_every - 1) / probe_every : 0;
+  if (n_probe > 0) {
+    for (int64_t i = 0; i < n_probe; i++)
+      if (probe_cells[i] < 0 || probe_cells[i] >= n) return fail(CM_ERR_ARG, "probe cell index out of range");
+    if (b->probe_cap < n_probe) {
+      cudaFree(b->probe_idx);
+      b->probe_idx = nullptr;
+      b->probe_cap = 0;
+      CK(cudaMalloc(&b->probe_idx, n_probe * sizeof(int64_t)));
+      b->probe_cap = n_probe;
+    }
+    if (b->probe_out_cap < n_probe * n_rec) {
+      cudaFree(b->probe_out);
+      b->probe_out = nullptr;
+      b->probe_out_cap = 0;
+      CK(cudaMalloc(&b->probe_out, n_probe * n_rec * sizeof(double)));
+      b->probe_out_cap = n_probe * n_rec;
+    }
+    CK(cudaMemcpyAsync(b->probe_idx, probe_cells, n_probe * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+  }
+  StepIO io;
+  io.vm = dvm;
+  io.vm_out = dvm;
+  io.textlen = st.textlen;
+  io.bcl = st.bcl;
+  io.amp = st.amplitude;
+  io.tb_cell = per_cell ? b->tb_cell : nullptr;
+  // The reference driver accumulates t += dt and advances textbegin on the host side of
+  // each cell; with one protocol for all cells the same arithmetic runs here once per step.
+  double t = st.t0, tb = st.textbegin;
+  for (int64_t s = 0; s < n_steps; s++) {
+    if (n_probe > 0 && s % probe_every == 0)
+      CK(launch_probe(dvm, b->probe_idx, n_probe, b->probe_out, n_rec, s / probe_every, b->stream));
+    io.t = t;
+    if (!per_cell) {
+      double i_ext = 0.0;
+      if (stim && t >= tb) {
+        i_ext = st.amplitude;
+        if (t >= tb + st.textlen) tb += st.bcl;
+      }
+      io.iext_uniform = i_ext;
+    }
+    CK(launch_step(b->d, io, 0, 0, b->stream));
+    t += b->ps.dt;
+  }
+  if (host_vm) CK(cudaMemcpyAsync(Vm, dvm, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (n_probe > 0) {
+    const bool host_probe = !is_device_ptr(probe_vm);
+    CK(cudaMemcpyAsync(probe_vm, b->probe_out, n_probe * n_rec * sizeof(double),
+                       host_probe ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, b->stream));
+  }
+  unsigned int mask = 0;
+  CK(cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  unsigned int m = 0;
+  CK(cudaMemcpyAsync(&m, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
+  if (per_cell && b->d.n > 0) {
+    const bool dev = is_device_ptr(per_cell);
+    CK(cudaMemcpyAsync(per_cell, b->audit_cell, b->d.n * sizeof(uint32_t),
+                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaMemsetAsync(b->audit_cell, 0, std::max<int64_t>(1, b->d.n) * sizeof(uint32_t), b->stream));
+  CK(cudaMemsetAsync(b->audit_or, 0, sizeof(unsigned int), b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (mask) *mask = m;
+  return CM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+// Shared definitions for the cell-model kernels: table geometry, per-model device
+// parameter blocks, state layouts and small numeric helpers.
+#pragma once
+
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define CM_HD __host__ __device__ __forceinline__
+#else
+#define CM_HD inline
+#include <cmath>
+#endif
+
+namespace cm {
+
+// Voltage-table geometry (reference ElphyModelBasis.h:46-56): 4000 rows, row
+// Vi = int(10 * (200 + V[mV]) + 0.5), built on V = -199.9999 + k * 0.1 (accumulated).
+constexpr int kRows = 4000;
+constexpr int kRangeHalf = 200;
+constexpr int kDivision = 10;
+
+// Row layout of the TT2 voltage table on the device (one row = 28 values, 224 B in FP64).
+// Gates are stored as (x_inf, exp(-dt/tau_x)) pairs; j_inf repeats h_inf as in the reference
+// (TenTusscher2Parameters.cpp:420).
+enum TT2Col {
+  T2_m_inf, T2_exptau_m, T2_h_inf, T2_exptau_h, T2_j_inf, T2_exptau_j, T2_Xr1_inf, T2_exptau_Xr1,
+  T2_Xr2_inf, T2_exptau_Xr2, T2_Xs_inf, T2_exptau_Xs, T2_r_inf, T2_exptau_r, T2_s_inf, T2_exptau_s,
+  T2_d_inf, T2_exptau_d, T2_f_inf, T2_exptau_f, T2_f2_inf, T2_exptau_f2, T2_rec_ipK, T2_CaL_P1,
+  T2_CaL_P2, T2_NaCa_P1, T2_NaCa_P2, T2_NaK_P1, T2_COLS
+};
+
+// Row layout of the Courtemanche voltage table (30 values, 240 B in FP64).
+enum CRNCol {
+  CR_m_m, CR_exptau_m, CR_m_h, CR_exptau_h, CR_m_j, CR_exptau_j, CR_m_oa, CR_exptau_oa, CR_m_oi,
+  CR_exptau_oi, CR_m_ua, CR_exptau_ua, CR_m_ui, CR_exptau_ui, CR_m_Xr, CR_exptau_Xr, CR_m_Xs,
+  CR_exptau_Xs, CR_m_d, CR_exptau_d, CR_m_f, CR_exptau_f, CR_m_w, CR_exptau_w, CR_expVm, CR_CK1,
+  CR_g_Kur, CR_CKr, CR_CNaK, CR_CNaCa, CR_COLS
+};
+
+// Per-cell state variables in SOA order (Vm is the caller's).
+enum TT2State {
+  S2_Cai, S2_CaSR, S2_CaSS, S2_Nai, S2_Ki, S2_m, S2_h, S2_j, S2_xr1, S2_xr2, S2_xs, S2_r, S2_s, S2_d,
+  S2_f, S2_f2, S2_fCa, S2_Rq, S2_N
+};
+enum CRNState {
+  SC_Cai, SC_Caup, SC_Carel, SC_h, SC_j, SC_oi, SC_ui, SC_Xr, SC_Xs, SC_u, SC_v, SC_w, SC_Nai, SC_Ki,
+  SC_m, SC_oa, SC_ua, SC_d, SC_f, SC_fCa, SC_CaTRPN, SC_N
+};
+
+// Hetero (per-cell parameter) slots. Each slot either points at n_cells per-cell values
+// or is null (the parameter set's value applies).
+enum TT2Het { H2_g_Na, H2_g_Kr, H2_g_K1, H2_g_Ks, H2_g_to, H2_g_CaL, H2_N };
+enum CRNHet { HC_g_Na, HC_g_to, HC_g_Ks, HC_g_CaL, HC_g_bNa, HC_g_bCa, HC_N };
+
+// Constants of TenTusscherEtAl2::Calc (TenTusscher2.cpp:615-906) prepared on the host.
+// Quantities the reference recomputes every call from parameters alone
+// (sqrt(K_o/5.4), K_o/(K_o+KmK), Vc/Vss, ...) are evaluated once, in FP64.
+template <typename R>
+struct TT2Consts {
+  R RTONF, K_o, Na_o, pKNa, pKNaNao, sqrtKo54, KoKmK, KmNa;
+  R g_pCa, KpCa, g_to, g_Kr, g_Ks, g_K1, g_bNa, g_bCa, g_Na, g_CaL, kNaCa, knak;
+  R CaiTabConst1, CaiTabConst2;
+  R Cm, max_sr, min_sr, EC, ks1, ks2, k3, k4, Vrel, Vxfer, Vmaxup, Kupsquare;
+  R Bufsr, Kbufsr, Bufss, Kbufss, Bufc, Kbufc, BufcPKbufc;
+  R VcVss, VsrVss, inversevssF2, inverseviF, inverseviF2, invVcdVsr;
+  R dt, dt1000, inv_stim_unit;  // inv_stim_unit = 1 / 2.29656e-2 (nA -> pA/pF, line 630)
+};
+
+// Constants of Courtemanche::Calc (CourtemancheEtAl.cpp:85-187).
+template <typename R>
+struct CRNConsts {
+  R RTdF, RTd2F, Na_o, K_o, Ca_o, g_Na, g_to, g_Ks, g_CaL, E_rL, g_bNa, g_bCa, k_mNai, I_pCamax,
+      k_mpCa, k_rel, I_upmax, k_up, kupleak, dt_tr, G_sac, E_sac, K_sac, alpha, ISAC_SWITCH, Ca_T50,
+      beta1, k_TRPN, n_TRPN, VreldVup, csqnkm, kmcsqnm2, kkmcsqn, CmdFvi, VupdVi, VreldVi, TRPNmax,
+      cmdnkm, kmcmdnm2, kkmcmdn, Vrel, Cmd2F, exp250, exp50;
+  R dt_ms;  // tinc * 1000 (line 87)
+};
+
+// Voltage row index exactly as the reference computes it (TenTusscher2.cpp:618,
+// CourtemancheEtAl.cpp:89), clamped to the table; out-of-table rows raise an audit bit
+// instead of reading out of bounds.
+CM_HD int vrow_fp64(double vmv, uint32_t &audit) {
+  const double x = kDivision * (kRangeHalf + vmv) + .5;
+  int vi = (x > -1.0 && x < 2147483647.0) ? (int)x : -1;  // (int) truncates toward 0
+  if (vi < 0 || vi >= kRows || x != x) {
+    audit |= 2u;
+    vi = (x != x || vi < 0) ? 0 : kRows - 1;
+  }
+  return vi;
+}
+
+CM_HD int vrow_fp32(float vmv, uint32_t &audit) {
+  const float x = kDivision * (kRangeHalf + vmv) + .5f;
+  int vi = (x > -1.0f && x < 1.0e9f) ? (int)x : -1;
+  if (vi < 0 || vi >= kRows || x != x) {
+    audit |= 2u;
+    vi = (x != x || vi < 0) ? 0 : kRows - 1;
+  }
+  return vi;
+}
+
+// New free concentration increment of a rapidly buffered species. The reference solves
+// x^2 + b x - c = 0 for the new free value x given total = x_old + B x_old/(x_old+K) + dT
+// (TenTusscher2.cpp:814-836). Writing x = x_old + d, the same conservation law gives
+//   a d^2 + (a^2 + B K - dT a) d - dT a^2 = 0,  a = x_old + K,
+// whose root is taken in the form without cancellation. Used by the mixed form in FP32,
+// where the reference form loses most digits of d (sqrt(b^2+4c) - b with b >> d).
+template <typename R>
+CM_HD R buffered_increment(R x, R dT, R B, R K) {
+  const R a = x + K;
+  const R Bq = a * a + B * K - dT * a;
+  const R disc = Bq * Bq + R(4) * a * a * a * dT;
+  const R s = sqrt(disc > R(0) ? disc : R(0));
+  return Bq > R(0) ? (R(2) * dT * a * a) / (Bq + s) : (s - Bq) / (R(2) * a);
+}
+
+}  // namespace cm

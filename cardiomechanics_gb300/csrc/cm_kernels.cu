@@ -1,0 +1,249 @@
+// Per-timestep cell-model kernels for sm_103a: one thread per cell, structure-of-arrays
+// state (coalesced: a warp touches 256 contiguous bytes per FP64 variable, 128 per FP32
+// one), voltage lookup rows read through the read-only path (cells of a tissue or of a
+// synchronously paced population share a few rows, which stay L1-resident).
+//
+// The FP64 kernels do all arithmetic in FP64 (the reference's arithmetic; the GB300 FP64
+// pipe bounds them). The mixed kernels do gates and currents in FP32 and keep four FP64
+// accumulators; they are bound by HBM bandwidth.
+#include <cuda_runtime.h>
+
+#include "cm_crn.cuh"
+#include "cm_launch.h"
+#include "cm_tt2.cuh"
+
+namespace cm {
+
+namespace {
+
+__device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
+  if (io.tb_cell) {
+    // reference driver stimulus (CellModel.h:405-419), per-cell first stimulus time
+    const double tb = io.tb_cell[c];
+    double i_ext = 0.0;
+    if (io.t >= tb) {
+      i_ext = io.amp;
+      if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
+    }
+    return i_ext;
+  }
+  return io.iext ? __ldg(io.iext + c) : io.iext_uniform;
+}
+
+__device__ __forceinline__ void finish(const DevBatch &b, const StepIO &io, int64_t c, double V, double dV,
+                                       uint32_t audit) {
+  const double vn = V + dV;
+  if (io.vm_out) io.vm_out[c] = vn;
+  if (io.dvm) io.dvm[c] = dV;
+  if (!isfinite(vn)) audit |= 1u;
+  if (io.vm_range > 0.0 && fabs(vn) > io.vm_range) audit |= 32u;
+  if (audit) {
+    atomicOr(b.audit_cell + c, audit);
+    atomicOr(b.audit_or, audit);
+  }
+}
+
+template <bool kDiag>
+__global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const StepIO io) {
+  const int64_t ld = b.ld;
+  const double *const *het = (const double *const *)b.het;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    double *s = b.s64 + c;
+    TT2Cell<double> x;
+    x.Ca_i = s[S2_Cai * ld];
+    double CaSR = s[S2_CaSR * ld];
+    x.CaSS = s[S2_CaSS * ld];
+    double Na_i = s[S2_Nai * ld], K_i = s[S2_Ki * ld];
+    x.m = s[S2_m * ld]; x.h = s[S2_h * ld]; x.j = s[S2_j * ld]; x.xr1 = s[S2_xr1 * ld];
+    x.xr2 = s[S2_xr2 * ld]; x.xs = s[S2_xs * ld]; x.r = s[S2_r * ld]; x.s = s[S2_s * ld];
+    x.d = s[S2_d * ld]; x.f = s[S2_f * ld]; x.f2 = s[S2_f2 * ld]; x.fCa = s[S2_fCa * ld];
+    x.Rq = s[S2_Rq * ld];
+    const TT2Consts<double> &C = b.tt2_64;
+    TT2Het_<double> g;
+    g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + c) : C.g_Na;
+    g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + c) : C.g_Kr;
+    g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + c) : C.g_K1;
+    g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + c) : C.g_Ks;
+    g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
+    g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
+    const double V = __ldg(io.vm + c);
+    const double iext = stim_for_cell(io, c);
+    uint32_t audit = 0;
+    const int vi = vrow_fp64(V * 1000, audit);
+    TT2Diag<double> dg;
+    const double dV = tt2_calc_fp64<kDiag>(C, b.rows64 + (size_t)vi * T2_COLS, b.eca64, x, CaSR, Na_i, K_i, g, V,
+                                           iext, audit, &dg);
+    s[S2_Cai * ld] = x.Ca_i; s[S2_CaSR * ld] = CaSR; s[S2_CaSS * ld] = x.CaSS; s[S2_Nai * ld] = Na_i;
+    s[S2_Ki * ld] = K_i; s[S2_m * ld] = x.m; s[S2_h * ld] = x.h; s[S2_j * ld] = x.j; s[S2_xr1 * ld] = x.xr1;
+    s[S2_xr2 * ld] = x.xr2; s[S2_xs * ld] = x.xs; s[S2_r * ld] = x.r; s[S2_s * ld] = x.s; s[S2_d * ld] = x.d;
+    s[S2_f * ld] = x.f; s[S2_f2 * ld] = x.f2; s[S2_fCa * ld] = x.fCa; s[S2_Rq * ld] = x.Rq;
+    if (kDiag)
+      for (int k = 0; k < 17; k++) b.diag[k * ld + c] = dg.v[k];
+    finish(b, io, c, V, dV, audit);
+  }
+}
+
+__global__ void __launch_bounds__(256) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
+  const int64_t ld = b.ld;
+  const float *const *het = (const float *const *)b.het;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    float *s = b.s32 + c;
+    double *a = b.s64 + c;
+    TT2Cell<float> x;
+    x.m = s[0]; x.h = s[ld]; x.j = s[2 * ld]; x.xr1 = s[3 * ld]; x.xr2 = s[4 * ld]; x.xs = s[5 * ld];
+    x.r = s[6 * ld]; x.s = s[7 * ld]; x.d = s[8 * ld]; x.f = s[9 * ld]; x.f2 = s[10 * ld]; x.fCa = s[11 * ld];
+    x.Rq = s[12 * ld]; x.Ca_i = s[13 * ld]; x.CaSS = s[14 * ld];
+    double CaSR = a[0], Na_i = a[ld], K_i = a[2 * ld];
+    const TT2Consts<float> &C = b.tt2_32;
+    TT2Het_<float> g;
+    g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + c) : C.g_Na;
+    g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + c) : C.g_Kr;
+    g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + c) : C.g_K1;
+    g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + c) : C.g_Ks;
+    g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
+    g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
+    const double V = __ldg(io.vm + c);
+    const float iext = (float)stim_for_cell(io, c);
+    uint32_t audit = 0;
+    const float Vf = (float)V;
+    const int vi = vrow_fp32(Vf * 1000.f, audit);
+    const float dV = tt2_calc_mixed(C, b.rows32 + (size_t)vi * T2_COLS, b.eca32, x, CaSR, Na_i, K_i, g, Vf, iext, audit);
+    s[0] = x.m; s[ld] = x.h; s[2 * ld] = x.j; s[3 * ld] = x.xr1; s[4 * ld] = x.xr2; s[5 * ld] = x.xs;
+    s[6 * ld] = x.r; s[7 * ld] = x.s; s[8 * ld] = x.d; s[9 * ld] = x.f; s[10 * ld] = x.f2; s[11 * ld] = x.fCa;
+    s[12 * ld] = x.Rq; s[13 * ld] = x.Ca_i; s[14 * ld] = x.CaSS;
+    a[0] = CaSR; a[ld] = Na_i; a[2 * ld] = K_i;
+    finish(b, io, c, V, (double)dV, audit);
+  }
+}
+
+template <bool kDiag>
+__global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const StepIO io) {
+  const int64_t ld = b.ld;
+  const double *const *het = (const double *const *)b.het;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    double *s = b.s64 + c;
+    CRNCell<double> x;
+    x.Ca_i = s[SC_Cai * ld];
+    double Ca_up = s[SC_Caup * ld], Ca_rel = s[SC_Carel * ld];
+    x.h = s[SC_h * ld]; x.j = s[SC_j * ld]; x.oi = s[SC_oi * ld]; x.ui = s[SC_ui * ld]; x.Xr = s[SC_Xr * ld];
+    x.Xs = s[SC_Xs * ld]; x.u = s[SC_u * ld]; x.v = s[SC_v * ld]; x.w = s[SC_w * ld];
+    double Na_i = s[SC_Nai * ld], K_i = s[SC_Ki * ld];
+    x.m = s[SC_m * ld]; x.oa = s[SC_oa * ld]; x.ua = s[SC_ua * ld]; x.d = s[SC_d * ld]; x.f = s[SC_f * ld];
+    x.f_Ca = s[SC_fCa * ld]; x.Ca_TRPN = s[SC_CaTRPN * ld];
+    const CRNConsts<double> &C = b.crn_64;
+    CRNHet_<double> g;
+    g.g_Na = het[HC_g_Na] ? __ldg(het[HC_g_Na] + c) : C.g_Na;
+    g.g_to = het[HC_g_to] ? __ldg(het[HC_g_to] + c) : C.g_to;
+    g.g_Ks = het[HC_g_Ks] ? __ldg(het[HC_g_Ks] + c) : C.g_Ks;
+    g.g_CaL = het[HC_g_CaL] ? __ldg(het[HC_g_CaL] + c) : C.g_CaL;
+    g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
+    g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
+    const double V = __ldg(io.vm + c);
+    const double iext = stim_for_cell(io, c);
+    const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
+    uint32_t audit = 0;
+    const int vi = vrow_fp64(V * 1000.0, audit);
+    double isac;
+    const double dV = crn_calc_fp64(C, b.rows64 + (size_t)vi * CR_COLS, x, Ca_up, Ca_rel, Na_i, K_i, g, V, iext,
+                                    stretch, isac, audit);
+    s[SC_Cai * ld] = x.Ca_i; s[SC_Caup * ld] = Ca_up; s[SC_Carel * ld] = Ca_rel; s[SC_h * ld] = x.h;
+    s[SC_j * ld] = x.j; s[SC_oi * ld] = x.oi; s[SC_ui * ld] = x.ui; s[SC_Xr * ld] = x.Xr; s[SC_Xs * ld] = x.Xs;
+    s[SC_u * ld] = x.u; s[SC_v * ld] = x.v; s[SC_w * ld] = x.w; s[SC_Nai * ld] = Na_i; s[SC_Ki * ld] = K_i;
+    s[SC_m * ld] = x.m; s[SC_oa * ld] = x.oa; s[SC_ua * ld] = x.ua; s[SC_d * ld] = x.d; s[SC_f * ld] = x.f;
+    s[SC_fCa * ld] = x.f_Ca; s[SC_CaTRPN * ld] = x.Ca_TRPN;
+    if (kDiag) b.diag[c] = isac;
+    finish(b, io, c, V, dV, audit);
+  }
+}
+
+__global__ void __launch_bounds__(256) crn_mixed_kernel(const DevBatch b, const StepIO io) {
+  const int64_t ld = b.ld;
+  const float *const *het = (const float *const *)b.het;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    float *s = b.s32 + c;
+    double *a = b.s64 + c;
+    CRNCell<float> x;
+    x.h = s[0]; x.j = s[ld]; x.oi = s[2 * ld]; x.ui = s[3 * ld]; x.Xr = s[4 * ld]; x.Xs = s[5 * ld];
+    x.u = s[6 * ld]; x.v = s[7 * ld]; x.w = s[8 * ld]; x.m = s[9 * ld]; x.oa = s[10 * ld]; x.ua = s[11 * ld];
+    x.d = s[12 * ld]; x.f = s[13 * ld]; x.f_Ca = s[14 * ld]; x.Ca_i = s[15 * ld]; x.Ca_TRPN = s[16 * ld];
+    double Ca_up = a[0], Ca_rel = a[ld], Na_i = a[2 * ld], K_i = a[3 * ld];
+    const CRNConsts<float> &C = b.crn_32;
+    CRNHet_<float> g;
+    g.g_Na = het[HC_g_Na] ? __ldg(het[HC_g_Na] + c) : C.g_Na;
+    g.g_to = het[HC_g_to] ? __ldg(het[HC_g_to] + c) : C.g_to;
+    g.g_Ks = het[HC_g_Ks] ? __ldg(het[HC_g_Ks] + c) : C.g_Ks;
+    g.g_CaL = het[HC_g_CaL] ? __ldg(het[HC_g_CaL] + c) : C.g_CaL;
+    g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
+    g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
+    const double V = __ldg(io.vm + c);
+    const float iext = (float)stim_for_cell(io, c);
+    const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
+    uint32_t audit = 0;
+    const float Vf = (float)V;
+    const int vi = vrow_fp32(Vf * 1000.f, audit);
+    const float dV = crn_calc_mixed(C, b.rows32 + (size_t)vi * CR_COLS, x, Ca_up, Ca_rel, Na_i, K_i, g, Vf, iext,
+                                    stretch, audit);
+    s[0] = x.h; s[ld] = x.j; s[2 * ld] = x.oi; s[3 * ld] = x.ui; s[4 * ld] = x.Xr; s[5 * ld] = x.Xs;
+    s[6 * ld] = x.u; s[7 * ld] = x.v; s[8 * ld] = x.w; s[9 * ld] = x.m; s[10 * ld] = x.oa; s[11 * ld] = x.ua;
+    s[12 * ld] = x.d; s[13 * ld] = x.f; s[14 * ld] = x.f_Ca; s[15 * ld] = x.Ca_i; s[16 * ld] = x.Ca_TRPN;
+    a[0] = Ca_up; a[ld] = Ca_rel; a[2 * ld] = Na_i; a[3 * ld] = K_i;
+    finish(b, io, c, V, (double)dV, audit);
+  }
+}
+
+__global__ void probe_kernel(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
+                             int64_t k) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_probe) out[i * stride + k] = vm[probe[i]];
+}
+
+}  // namespace
+
+int n_fp32_vars(int model) { return model == 5 ? 15 : 17; }
+int n_fp64_vars(int model, int precision) {
+  if (precision == 0) return model == 5 ? S2_N : SC_N;
+  return model == 5 ? 3 : 4;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_step(const DevBatch &b, const StepIO &io, int block, int grid, cudaStream_t s) {
+  if (b.n == 0) return cudaSuccess;
+  const bool diag = b.diag != nullptr;
+  if (block <= 0) block = b.precision == 0 ? 128 : 256;
+  if (grid <= 0) {
+    const int64_t need = (b.n + block - 1) / block;
+    const int64_t cap = (int64_t)sm_count() * (b.precision == 0 ? 16 : 8);
+    grid = (int)(need < cap ? need : cap);
+  }
+  if (b.model == 5) {
+    if (b.precision == 0) {
+      if (diag) tt2_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
+      else tt2_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+    } else {
+      tt2_mixed_kernel<<<grid, block, 0, s>>>(b, io);
+    }
+  } else {
+    if (b.precision == 0) {
+      if (diag) crn_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
+      else crn_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+    } else {
+      crn_mixed_kernel<<<grid, block, 0, s>>>(b, io);
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_probe(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
+                         int64_t k, cudaStream_t s) {
+  if (n_probe <= 0) return cudaSuccess;
+  probe_kernel<<<(unsigned)((n_probe + 127) / 128), 128, 0, s>>>(vm, probe, n_probe, out, stride, k);
+  return cudaGetLastError();
+}
+
+}  // namespace cm

@@ -1,0 +1,53 @@
+"""Seeded synthetic workloads for the cell-model update.
+
+Counter-based generator: value k of stream `seed` is splitmix64(seed * 2**32 + k), mapped to
+a double in [0, 1) from its top 53 bits. Stateless, so any subset of cells can be
+regenerated without generating the rest, identically in numpy and in C.
+
+Conductance jitter follows the order "one draw per cell per parameter in the listed
+order": draw index = cell * n_params + p.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M1 = np.uint64(0x9E3779B97F4A7C15)
+_M2 = np.uint64(0xBF58476D1CE4E5B9)
+_M3 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        z = np.asarray(x, np.uint64) + _M1
+        z = (z ^ (z >> np.uint64(30))) * _M2
+        z = (z ^ (z >> np.uint64(27))) * _M3
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, idx: np.ndarray) -> np.ndarray:
+    """U[0,1) doubles for draw indices idx of stream seed."""
+    with np.errstate(over="ignore"):
+        base = np.uint64(seed) << np.uint64(32)
+        z = splitmix64(np.asarray(idx, np.uint64) + base)
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def conductance_scales(seed: int, n_cells: int, n_params: int, lo: float, hi: float,
+                       cells: np.ndarray | None = None) -> np.ndarray:
+    """(n_params, len(cells)) scale factors U[lo, hi]; cells defaults to range(n_cells)."""
+    c = np.arange(n_cells, dtype=np.uint64) if cells is None else np.asarray(cells, np.uint64)
+    out = np.empty((n_params, c.size))
+    for p in range(n_params):
+        out[p] = lo + (hi - lo) * uniform(seed, c * np.uint64(n_params) + np.uint64(p))
+    return out
+
+
+# Stimulus: the ten Tusscher convention "-52 pA/pF" is the reference's i_external in nA per
+# cell, which TenTusscher2.cpp:630 divides by 2.29656e-2 to get pA/pF.
+TT2_STIM_NA = 52.0 * 2.29656e-2
+# Courtemanche takes i_external in pA/pF directly (CourtemancheEtAl.h:52 default 20).
+CRN_STIM_PAPF = 20.0
+
+# Per-cell heterogeneous conductances used by the workloads, by model.
+TT2_HETERO = ("g_Na", "g_Kr", "g_K1")
+CRN_HETERO = ("g_Na", "g_to", "g_CaL")

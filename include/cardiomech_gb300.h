@@ -1,0 +1,191 @@
+/* cardiomech_gb300.h -- C ABI of the GB300 cell-model update library (libcmgb300.so).
+ *
+ * Drop-in replacement for the per-node ionic update of KIT-IBT/CardioMechanics: the loop
+ *     for each local node l:  dVm[l] = pem[l]->Calc(dtcell, Vm[l], i_ext[l], stretch[l], 1)
+ * in acCELLerate::CalcCellModels (electrophysiology/src/acCELLerate/acCELLerate.cpp:1757-1770)
+ * and the single-cell driver's `Vm += Calc(...)` (electrophysiology/src/CellModel/CellModel.h:420)
+ * becomes one cm_batch_step() (or a fused multi-step cm_batch_run()) over all nodes on one GPU.
+ *
+ * Models: ten Tusscher-Panfilov 2006 ("TenTusscher2") and Courtemanche 1998 ("CourtemancheEtAl").
+ * Units are the reference's: Vm and dVm in volts, dt in seconds, i_ext in nA per cell for
+ * TenTusscher2 (TenTusscher2.cpp:630) and pA/pF for CourtemancheEtAl (CourtemancheEtAl.h:52).
+ *
+ * Conventions
+ *  - Every call returns CM_OK (0) or a negative cm_status; cm_last_error() describes the last
+ *    failure of the calling thread. No C++ exception crosses this boundary.
+ *  - Array arguments are plain pointers to n_cells elements. They may be host memory
+ *    (pageable or pinned) or device memory; the library tells them apart with
+ *    cudaPointerGetAttributes and copies host arrays in and out on the batch's stream.
+ *    Host arrays are only borrowed for the duration of the call.
+ *  - `stream` arguments are cudaStream_t values (NULL = the legacy default stream). Calls
+ *    that return host data synchronise that stream before returning.
+ *  - A batch is not thread-safe; different batches are independent.
+ */
+#ifndef CARDIOMECH_GB300_H
+#define CARDIOMECH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CM_ABI_VERSION 1
+
+/* Model identifiers: the reference's ElphyModelType values (CellModel/ElphyModelBasis.h:62-81). */
+typedef enum {
+  CM_MODEL_COURTEMANCHE = 2, /* EMT_CourtemancheEtAl */
+  CM_MODEL_TENTUSSCHER2 = 5  /* EMT_TenTusscher2 */
+} cm_model;
+
+typedef enum {
+  CM_OK = 0,
+  CM_ERR_ARG = -1,         /* bad argument (null handle, size, dt mismatch ...) */
+  CM_ERR_MODEL = -2,       /* model not implemented here */
+  CM_ERR_FILE = -3,        /* .ev file missing or malformed (CellModelValues.h:153-243) */
+  CM_ERR_PARAM = -4,       /* unknown or missing parameter name */
+  CM_ERR_CUDA = -5,        /* CUDA runtime failure (message in cm_last_error) */
+  CM_ERR_NOMEM = -6,       /* device or host allocation failed */
+  CM_ERR_UNSUPPORTED = -7, /* valid request this build does not serve */
+  CM_ERR_NUMERIC = -8      /* NaN / out-of-range Vm detected by a fused check */
+} cm_status;
+
+/* Arithmetic form of a batch. */
+typedef enum {
+  CM_PREC_FP64 = 0,  /* every operation in FP64, the reference's arithmetic */
+  CM_PREC_MIXED = 1  /* FP32 gates and currents; Vm, [Na]i, [K]i, [Ca]SR accumulated in FP64;
+                        buffered-Ca quadratics solved in a cancellation-free increment form */
+} cm_precision;
+
+/* State layouts for cm_batch_get_state / cm_batch_set_state. */
+typedef enum {
+  /* The reference backup block of every cell, cell after cell, byte-compatible with
+   * vbElphyModel::GetBase()/GetSize() (TenTusscher2: 36 doubles = 288 B; Courtemanche:
+   * 22 doubles = 176 B). Diagnostic slots (TT2 Array[18], CRN I_SAC) are written as
+   * the library last computed them when diagnostics are on, else 0. */
+  CM_LAYOUT_REF_BLOCK = 0,
+  /* Structure of arrays: n_state_vars arrays of n_cells doubles, in cm_model_info order. */
+  CM_LAYOUT_SOA = 1
+} cm_layout;
+
+/* Per-cell audit bits, OR-ed into the batch's audit mask by the kernels. */
+enum {
+  CM_AUDIT_NAN = 1u,          /* non-finite Vm or state after the step */
+  CM_AUDIT_VRANGE = 2u,       /* voltage index outside the lookup table: clamped */
+  CM_AUDIT_CARANGE = 4u,      /* [Ca]i index outside the ECa table (TT2): clamped */
+  CM_AUDIT_GATE = 8u,         /* a gate left [0, 1] */
+  CM_AUDIT_SURROGATE = 16u,   /* surrogate step rejected; plain integrator used */
+  CM_AUDIT_VMRANGE = 32u      /* |Vm| above the caller's vm_range after a fused update */
+};
+
+typedef struct cm_params_s *cm_params_t;
+typedef struct cm_batch_s *cm_batch_t;
+
+typedef struct {
+  int model;           /* cm_model */
+  int n_state_vars;    /* state variables in the SOA layout (Vm excluded) */
+  int ref_block_doubles; /* GetSize()/8 of the reference model */
+  int n_tables;        /* voltage-indexed lookup tables */
+  int table_rows;      /* 4000 (RangeTab * DivisionTab, ElphyModelBasis.h:50-54) */
+  double dt;           /* time step the tables were built for [s] */
+  double init_vm;      /* GetVm() [V] */
+  double amplitude;    /* GetAmplitude(): default stimulus amplitude */
+  double stim_time;    /* GetStimTime(): default stimulus duration [s] */
+} cm_info;
+
+/* Stimulus protocol evaluated on the device by cm_batch_run, per cell as the reference
+ * driver does (CellModel.h:405-419): i_ext = amplitude while t >= textbegin; at the first
+ * step with t >= textbegin + textlen the stimulus is still applied and textbegin advances
+ * by bcl. t starts at t0 and accumulates t += dt in FP64. */
+typedef struct {
+  double t0;
+  double textbegin;           /* first stimulus time [s] (all cells) */
+  const double *textbegin_per_cell; /* optional per-cell first stimulus time, overrides */
+  double textlen;             /* stimulus duration [s] */
+  double bcl;                 /* basic cycle length [s] */
+  double amplitude;           /* reference units of i_external */
+} cm_stimulus;
+
+/* ------------------------------------------------------------------ library */
+int cm_abi_version(void);
+const char *cm_last_error(void);
+/* Model type by reference name (FindElphyModelType, ElphyModelBasis.h:112-118); -1 if unknown. */
+int cm_model_from_name(const char *name);
+/* cm_info without a parameter set: n_state_vars, ref_block_doubles, n_tables, table_rows. */
+int cm_model_info(int model, cm_info *info);
+/* Name of SOA state variable k (k < n_state_vars). NULL if out of range. */
+const char *cm_state_name(int model, int k);
+
+/* ------------------------------------------------------------------ parameter sets */
+/* initElphyParameters (CellModel/CellModelLayer.h:88-150): load an .ev parameter file and
+ * build the lookup tables for time step dt [s] (TenTusscher2Parameters.cpp:384-524,
+ * CourtemancheParameters.cpp:282-395). ev_path NULL selects the built-in defaults
+ * (TenTusscher2_original_Epi.ev / CourtemancheEtAl.ev values). A parameter the model
+ * needs but the file lacks is an error (the reference warns and uses -1). */
+int cm_params_create(cm_params_t *out, int model, const char *ev_path, double dt);
+int cm_params_destroy(cm_params_t p);
+int cm_params_info(cm_params_t p, cm_info *info);
+/* Named parameter value (base or derived, as the reference's P[] array holds it). */
+int cm_params_get(cm_params_t p, const char *name, double *value);
+/* Change a base parameter; derived values and tables are rebuilt (Calculate + InitTable). */
+int cm_params_set(cm_params_t p, const char *name, double value);
+/* Copy lookup table `name` (table_rows doubles) as built on the host in FP64. */
+int cm_params_table(cm_params_t p, const char *name, double *out);
+
+/* ------------------------------------------------------------------ batches of cells */
+/* initElphyModel x n_cells (CellModelLayer.h:154-232) + Init(): device-resident state for
+ * n_cells cells of the parameter set's model, initialised from its init values. The batch
+ * keeps its own copy of the parameter set and tables. stream: cudaStream_t or NULL. */
+int cm_batch_create(cm_batch_t *out, cm_params_t p, int64_t n_cells, int precision, void *stream);
+int cm_batch_destroy(cm_batch_t b);
+int cm_batch_info(cm_batch_t b, cm_info *info, int64_t *n_cells, int *precision);
+/* Back to the initial state (vbElphyModel::Init for every cell). */
+int cm_batch_reset(cm_batch_t b);
+/* AddHeteroValue(name, values[c]) for every cell c (ElphyModelBasis.h:319-322): absolute
+ * per-cell values of a parameter read in Calc. Supported names:
+ *   TenTusscher2:     g_Na g_Kr g_K1 g_Ks g_to g_CaL
+ *   CourtemancheEtAl: g_Na g_to g_Ks g_CaL g_bNa g_bCa
+ * Others return CM_ERR_UNSUPPORTED. values == NULL removes the override. */
+int cm_batch_set_hetero(cm_batch_t b, const char *name, const double *values);
+/* Keep the reference's diagnostic values (TenTusscher2 Array[0..16] currents, Courtemanche
+ * I_SAC) on the device so that CM_LAYOUT_REF_BLOCK state reads carry them. FP64 batches only;
+ * costs 17 (TT2) or 1 (CRN) extra FP64 writes per cell-step while on. */
+int cm_batch_set_diagnostics(cm_batch_t b, int on);
+/* GetVm() for every cell into Vm (n_cells doubles). */
+int cm_batch_init_vm(cm_batch_t b, double *Vm);
+/* State transfer in the given cm_layout; buf holds n_cells * (ref_block_doubles or
+ * n_state_vars) doubles. */
+int cm_batch_get_state(cm_batch_t b, int layout, double *buf);
+int cm_batch_set_state(cm_batch_t b, int layout, const double *buf);
+
+/* One Calc for every cell: dVm[c] = Calc(dt, Vm[c], i_ext[c], stretch[c], 1), state updated
+ * in place (acCELLerate.cpp:1757-1770). dt must equal the parameter set's dt (the tables
+ * bake it in; the reference would silently use stale tables). i_ext NULL = no stimulus;
+ * stretch NULL = 1.0. dVm may alias neither Vm nor i_ext. */
+int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext, const double *stretch,
+                  double *dVm);
+
+/* cm_batch_step fused with the caller's Godunov update and check (acCELLerate.cpp:1930-1949):
+ * Vm[c] += Calc(dt, Vm[c], i_ext[c], stretch[c], 1), Vm updated in place. Returns
+ * CM_ERR_NUMERIC when a new Vm is NaN/inf or |Vm| > vm_range (vm_range <= 0: no range check);
+ * the offending cells carry CM_AUDIT_NAN / CM_AUDIT_VMRANGE in cm_batch_audit. */
+int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
+                         double vm_range);
+
+/* n_steps of the driver loop fused on the device: i_ext from the stimulus protocol,
+ * Vm[c] += Calc(dt, Vm[c], i_ext, 1, 1) (CellModel.h:405-420). Vm is updated in place.
+ * probe_cells (optional, n_probe indices) and probe_vm (n_probe * ceil(n_steps/probe_every))
+ * record Vm before every probe_every-th step, probe-major. Returns CM_ERR_NUMERIC when a
+ * cell's Vm became non-finite (the reference driver throws "Vm is NaN", CellModel.h:421). */
+int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *stim,
+                 const int64_t *probe_cells, int64_t n_probe, int64_t probe_every, double *probe_vm);
+
+/* OR of the per-cell audit bits since the last call; per_cell (optional, n_cells uint32)
+ * receives each cell's bits. Clears the bits. */
+int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CARDIOMECH_GB300_H */

@@ -1,0 +1,694 @@
+/* Test infrastructure only (the oracle). Plain-C FP64 restatement of the reference
+ * cell-model update, written from KIT-IBT/CardioMechanics
+ *   electrophysiology/src/CellModel/TenTusscher2.cpp            (Init 250-271, Calc 615-906)
+ *   electrophysiology/src/CellModel/TenTusscher2Parameters.cpp  (Calculate 313-382, InitTable 384-524)
+ *   electrophysiology/src/CellModel/CourtemancheEtAl.cpp        (Init 56-83, Calc 85-187)
+ *   electrophysiology/src/CellModel/CourtemancheParameters.cpp  (Init 246-247, Calculate 252-280,
+ *                                                                InitTable 282-395)
+ *   electrophysiology/src/CellModel/CellModel.h:405-420         (driver stimulus + Vm update)
+ * Expressions keep the reference's evaluation order so that, compiled without FP
+ * contraction against the same libm, results match the reference bit for bit; the
+ * tests pin that against oracle/_ref (the reference compiled from its own sources) and
+ * against the committed golden vectors. Used only by tests/, bench.py's CPU baseline and
+ * __graft_entry__.smoke() as the checker; never by the product.
+ */
+#include "cm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ElphyModelBasis.h:46-56 table geometry. */
+#define RANGE_TAB_HALF 200
+#define DIVISION_TAB 10
+#define D_DIVISION_TAB (1.0 / DIVISION_TAB)
+
+/* ---------------------------------------------------------------- parameter lists */
+/* Base parameters (read from the .ev file) followed by derived ones (Calculate()). */
+#define TT2_PARAMS(X)                                                                               \
+  X(R) X(Tx) X(F) X(init_m) X(init_h) X(init_j) X(init_Xr1) X(init_Xr2) X(init_Xs) X(init_r)       \
+  X(init_s) X(init_d) X(init_f) X(init_f2) X(init_fCa) X(init_Rq) X(K_o) X(Ca_o) X(Na_o) X(Vc)      \
+  X(Vsr) X(Vss) X(Vrel) X(ks1) X(ks2) X(k3) X(k4) X(EC) X(max_sr) X(min_sr) X(Vxfer) X(Bufc)        \
+  X(Kbufc) X(Bufsr) X(Kbufsr) X(Bufss) X(Kbufss) X(Vmaxup) X(Kup) X(C) X(g_Kr) X(pKNa) X(g_Ks)      \
+  X(g_K1) X(g_to) X(g_Na) X(g_bNa) X(KmK) X(KmNa) X(knak) X(g_CaL) X(g_bCa) X(kNaCa) X(KmNai)       \
+  X(KmCa) X(ksat) X(n) X(g_pCa) X(KpCa) X(g_pK) X(init_V_m) X(init_Cai) X(init_CaSR) X(init_CaSS)  \
+  X(init_Nai) X(init_Ki) X(CaiMin) X(CaiMax) X(s_inf_vHalf) X(tau_s_f1) X(tau_s_slope1)            \
+  X(tau_s_vHalf1) X(tau_s_enable) X(tau_s_add) X(m_Xr1_1) X(m_Xr1_2) X(a_Xr1_1) X(a_Xr1_2)         \
+  X(b_Xr1_1) X(b_Xr1_2) X(K_Q10Xr1) X(m_Xr2_1) X(m_Xr2_2) X(a_Xr2_1) X(a_Xr2_2) X(b_Xr2_1)         \
+  X(b_Xr2_2) X(K_Q10Xr2) X(m_Xs_1) X(m_Xs_2) X(a_Xs_1) X(a_Xs_2) X(b_Xs_1) X(b_Xs_2)               \
+  X(tau_Xs_add) X(K_Q10Xs) X(stim_duration) X(Amp) X(Vcell)                                        \
+  X(RTONF) X(inverseRTONF) X(vi) X(inverseviF) X(inverseviF2) X(inversevssF2) X(VcdVsr)            \
+  X(Kupsquare) X(BufcPKbufc) X(KmNai3) X(Nao3) X(StepCai)
+
+#define CRN_PARAMS(X)                                                                               \
+  X(R) X(Tx) X(F) X(C_m) X(Vcell) X(Vcell_outside) X(part_i) X(part_up) X(part_rel) X(Tfac) X(K_o)  \
+  X(Na_o) X(Ca_o) X(g_Na) X(g_to) X(g_Kr) X(g_Ks) X(g_CaL) X(g_K1) X(g_bNa) X(g_bCa) X(I_NaKmax)    \
+  X(k_mNai) X(k_mKo) X(I_pCamax) X(k_mpCa) X(k_NaCa) X(k_mNa) X(k_mCa) X(k_sat) X(gamm)             \
+  X(CMDNmax) X(TRPNmax) X(CSQNmax) X(K_mcmdn) X(K_mtrpn) X(K_mcsqn) X(k_rel) X(k_up) X(I_upmax)     \
+  X(Ca_upmax) X(t_tr) X(shiftm) X(shifth) X(shiftj) X(shiftoa) X(C_oa_1) X(C_oa_2) X(C_oa_3)        \
+  X(C_oa_4) X(C_oa_5) X(C_oa_6) X(CaL_fT_1) X(Init_Na_i) X(Init_K_i) X(Init_m) X(Init_oa)           \
+  X(Init_ua) X(Init_d) X(Init_f_Ca) X(Init_Ca_i) X(Init_Ca_up) X(Init_Ca_rel) X(Init_h) X(Init_j)   \
+  X(Init_oi) X(Init_ui) X(Init_Xr) X(Init_Xs) X(Init_f) X(Init_u) X(Init_v) X(Init_w) X(Init_Vm)    \
+  X(ua_a1) X(ua_a2) X(ua_a3) X(ua_a4) X(ua_a5) X(ua_b1) X(ua_b2) X(ua_b3) X(ua_m1) X(ua_m2)         \
+  X(ua_KQ10) X(ui_a1) X(ui_a2) X(ui_a3) X(ui_a4) X(ui_b1) X(ui_b2) X(ui_m1) X(ui_m2) X(ui_KQ10)     \
+  X(g_Kur1) X(g_Kur2) X(g_Kur3) X(g_Kur4) X(g_K1_1) X(g_K1_2) X(Xr_a1) X(Xr_a2) X(Xr_a3) X(Xr_b1)   \
+  X(Xr_b2) X(Xr_KQ10) X(Xr_m1) X(Xr_m2) X(g_Kr1) X(g_Kr2) X(Xs_a1) X(Xs_a2) X(Xs_a3) X(Xs_b1)       \
+  X(Xs_b2) X(Xs_KQ10) X(Xs_m1) X(Xs_m2) X(m_a1) X(m_a2) X(m_b1) X(m_b2) X(h_a1) X(h_a2) X(h_b1)     \
+  X(h_b2) X(h_b3) X(h_b4) X(h_b5) X(h_b6) X(j_a1) X(j_a2) X(j_a3) X(j_a4) X(j_a5) X(j_b1) X(j_b2)   \
+  X(j_b3) X(j_b4) X(j_b5) X(j_b6) X(tau_j_mult) X(tau_f_mult) X(E_rL) X(ISAC_SWITCH) X(alpha)       \
+  X(G_sac) X(K_sac) X(E_sac) X(Init_Ca_TRPN) X(beta1) X(Ca_T50) X(k_TRPN) X(n_TRPN)                 \
+  X(RTdF) X(FdRT) X(RTd2F) X(Vi) X(Vup) X(Vrel) X(VupdVi) X(VreldVi) X(VreldVup) X(CmdFvi)          \
+  X(Cmd2F) X(csqnkm) X(kmcsqnm2) X(kkmcsqn) X(cmdnkm) X(kmcmdnm2) X(kkmcmdn) X(kupleak) X(dt_tr)
+
+#define ENUM_TT2(x) T_##x,
+#define ENUM_CRN(x) C_##x,
+#define NAME(x) #x,
+enum { TT2_PARAMS(ENUM_TT2) T_LAST };
+enum { CRN_PARAMS(ENUM_CRN) C_LAST };
+static const char *tt2_names[] = {TT2_PARAMS(NAME)};
+static const char *crn_names[] = {CRN_PARAMS(NAME)};
+
+/* Lookup tables, in this file's order. */
+#define TT2_TABLES(X)                                                                               \
+  X(m_inf) X(h_inf) X(j_inf) X(Xr1_inf) X(Xr2_inf) X(Xs_inf) X(s_inf) X(r_inf) X(d_inf) X(f_inf)    \
+  X(f2_inf) X(exptau_m) X(exptau_h) X(exptau_j) X(exptau_Xr1) X(exptau_Xr2) X(exptau_Xs)            \
+  X(exptau_s) X(exptau_r) X(exptau_d) X(exptau_f) X(exptau_f2) X(NaK_P1) X(rec_ipK) X(NaCa_P1)      \
+  X(NaCa_P2) X(CaL_P1) X(CaL_P2) X(ECA)
+#define CRN_TABLES(X)                                                                               \
+  X(m_m) X(exptau_m) X(m_h) X(exptau_h) X(m_j) X(exptau_j) X(m_oa) X(exptau_oa) X(m_oi)             \
+  X(exptau_oi) X(m_ua) X(exptau_ua) X(m_ui) X(exptau_ui) X(m_Xr) X(exptau_Xr) X(m_Xs) X(exptau_Xs)  \
+  X(m_d) X(exptau_d) X(m_f) X(exptau_f) X(m_w) X(exptau_w) X(expVm) X(CK1) X(g_Kur) X(CKr) X(CNaK)  \
+  X(CNaCa) X(exp250_exp50)
+#define TENUM_TT2(x) TT_##x,
+#define TENUM_CRN(x) TC_##x,
+enum { TT2_TABLES(TENUM_TT2) TT_LAST };
+enum { CRN_TABLES(TENUM_CRN) TC_LAST };
+static const char *tt2_tnames[] = {TT2_TABLES(NAME)};
+static const char *crn_tnames[] = {CRN_TABLES(NAME)};
+
+int cmo_n_params(int model) { return model == CMO_TT2 ? T_LAST : (model == CMO_CRN ? C_LAST : -1); }
+const char *cmo_param_name(int model, int i) {
+  if (i < 0 || i >= cmo_n_params(model)) return 0;
+  return model == CMO_TT2 ? tt2_names[i] : crn_names[i];
+}
+int cmo_param_index(int model, const char *name) {
+  int n = cmo_n_params(model);
+  for (int i = 0; i < n; i++)
+    if (!strcmp(cmo_param_name(model, i), name)) return i;
+  return -1;
+}
+int cmo_state_doubles(int model) { return model == CMO_TT2 ? 36 : (model == CMO_CRN ? 22 : -1); }
+int cmo_n_tables(int model) { return model == CMO_TT2 ? TT_LAST : (model == CMO_CRN ? TC_LAST : -1); }
+const char *cmo_table_name(int model, int k) {
+  if (k < 0 || k >= cmo_n_tables(model)) return 0;
+  return model == CMO_TT2 ? tt2_tnames[k] : crn_tnames[k];
+}
+
+/* ---------------------------------------------------------------- TT2 */
+#define P_(x) P[T_##x]
+#define TB(x) (tables + (size_t)TT_##x * CMO_RTDT)
+
+/* TenTusscher2Parameters::Calculate (313-338): derived quantities. */
+static void tt2_derive(double *P) {
+  P_(RTONF) = P_(R) * P_(Tx) / P_(F);
+  P_(inverseRTONF) = 1 / P_(RTONF);
+  P_(vi) = 0.016404; /* overwritten constant, TenTusscher2Parameters.cpp:322 */
+  P_(inverseviF) = 1 / (P_(vi) * P_(F));
+  P_(inverseviF2) = 1. / (2 * P_(vi) * P_(F));
+  P_(inversevssF2) = 1 / (2 * (P_(vi) / 300.) * P_(F));
+  P_(VcdVsr) = P_(Vc) / P_(Vsr);
+  P_(Kupsquare) = P_(Kup) * P_(Kup);
+  P_(BufcPKbufc) = P_(Bufc) + P_(Kbufc);
+  P_(KmNai3) = P_(KmNai) * P_(KmNai) * P_(KmNai);
+  P_(Nao3) = P_(Na_o) * P_(Na_o) * P_(Na_o);
+  P_(StepCai) = (P_(CaiMax) - P_(CaiMin)) / CMO_RTDT;
+}
+
+/* TenTusscher2Parameters::InitTable (384-485). */
+static void tt2_tables(const double *P, double tinc, double *tables) {
+  for (double V = -RANGE_TAB_HALF + .0001; V < RANGE_TAB_HALF; V += D_DIVISION_TAB) {
+    int Vi = (int)(DIVISION_TAB * (RANGE_TAB_HALF + V) + .5);
+    if (Vi < 0 || Vi >= CMO_RTDT) continue;
+    const double rec_iNaK =
+        (1. / (1. + 0.1245 * exp(-0.1 * V * (P_(inverseRTONF))) + 0.0353 * exp(-V * (P_(inverseRTONF)))));
+    TB(NaK_P1)[Vi] = rec_iNaK;
+    TB(rec_ipK)[Vi] = P_(g_pK) / (1. + exp((25. - V) / 5.98));
+    const double a_m = 1. / (1. + exp((-60. - V) / 5.));
+    const double b_m = 0.1 / (1. + exp((V + 35.) / 5.)) + 0.10 / (1. + exp((V - 50.) / 200.));
+    const double tau_m = a_m * b_m;
+    TB(m_inf)[Vi] = 1. / ((1. + exp((-56.86 - V) / 9.03)) * (1. + exp((-56.86 - V) / 9.03)));
+    double tau_h, tau_j;
+    if (V >= -40.) {
+      const double AH_1 = 0.;
+      const double BH_1 = (0.77 / (0.13 * (1. + exp(-(V + 10.66) / 11.1))));
+      tau_h = 1.0 / (AH_1 + BH_1);
+    } else {
+      const double AH_2 = (0.057 * exp(-(V + 80.) / 6.8));
+      const double BH_2 = (2.7 * exp(0.079 * V) + (3.1e5) * exp(0.3485 * V));
+      tau_h = 1.0 / (AH_2 + BH_2);
+    }
+    TB(h_inf)[Vi] = 1. / ((1. + exp((V + 71.55) / 7.43)) * (1. + exp((V + 71.55) / 7.43)));
+    if (V >= -40.) {
+      const double AJ_1 = 0.;
+      const double BJ_1 = (0.6 * exp((0.057) * V) / (1. + exp(-0.1 * (V + 32.))));
+      tau_j = 1.0 / (AJ_1 + BJ_1);
+    } else {
+      const double AJ_2 = (((-2.5428e4) * exp(0.2444 * V) - (6.948e-6) * exp(-0.04391 * V)) * (V + 37.78) /
+                           (1. + exp(0.311 * (V + 79.23))));
+      const double BJ_2 = (0.02424 * exp(-0.01052 * V) / (1. + exp(-0.1378 * (V + 40.14))));
+      tau_j = 1.0 / (AJ_2 + BJ_2);
+    }
+    TB(j_inf)[Vi] = TB(h_inf)[Vi];
+    TB(Xr1_inf)[Vi] = 1. / (1. + exp((P_(m_Xr1_1) - V) / (P_(m_Xr1_2))));
+    const double a_Xr1 = 450. / (1. + exp((P_(a_Xr1_1) - V) / (P_(a_Xr1_2))));
+    const double b_Xr1 = 6. / (1. + exp((V - (P_(b_Xr1_1))) / (P_(b_Xr1_2))));
+    const double tau_Xr1 = a_Xr1 * b_Xr1 * fabs(P_(K_Q10Xr1));
+    TB(Xr2_inf)[Vi] = 1. / (1. + exp((V - (P_(m_Xr2_1))) / (P_(m_Xr2_2))));
+    const double a_Xr2 = 3. / (1. + exp((P_(a_Xr2_1) - V) / (P_(a_Xr2_2))));
+    const double b_Xr2 = 1.12 / (1. + exp((V - (P_(b_Xr2_1))) / (P_(b_Xr2_2))));
+    const double tau_Xr2 = a_Xr2 * b_Xr2 * fabs(P_(K_Q10Xr2));
+    TB(Xs_inf)[Vi] = 1. / (1. + exp((P_(m_Xs_1) - V) / P_(m_Xs_2)));
+    const double a_Xs = (1400. / (sqrt(1. + exp((P_(a_Xs_1) - V) / P_(a_Xs_2)))));
+    const double b_Xs = (1. / (1. + exp((V - P_(b_Xs_1)) / P_(b_Xs_2))));
+    const double tau_Xs = (a_Xs * b_Xs + P_(tau_Xs_add)) * fabs(P_(K_Q10Xs));
+    TB(r_inf)[Vi] = 1. / (1. + exp((20 - V) / 6.));
+    TB(s_inf)[Vi] = 1. / (1. + exp((V + (P_(s_inf_vHalf))) / 5.));
+    const double tau_r = 9.5 * exp(-(V + 40.) * (V + 40.) / 1800.) + 0.8;
+    const double tau_s =
+        P_(tau_s_f1) * exp(-(V + (P_(tau_s_vHalf1))) * (V + (P_(tau_s_vHalf1))) / P_(tau_s_slope1)) +
+        P_(tau_s_enable) * 5. / (1. + exp((V - 20.) / 5.)) + P_(tau_s_add);
+    TB(d_inf)[Vi] = 1. / (1. + exp((-8. - V) / 7.5));
+    const double a_d = 1.4 / (1. + exp((-35 - V) / 13)) + 0.25;
+    const double b_d = 1.4 / (1. + exp((V + 5) / 5));
+    const double c_d = 1. / (1. + exp((50 - V) / 20));
+    const double tau_d = a_d * b_d + c_d;
+    TB(f_inf)[Vi] = 1. / (1. + exp((V + 20) / 7));
+    const double V27square = (V + 27) * (V + 27);
+    const double exsquare = V27square / (15 * 15);
+    const double a_f = 1102.5 * exp(-exsquare);
+    const double b_f = 200. / (1. + exp((13 - V) / 10.));
+    const double g_f = (180. / (1. + exp((V + 30) / 10.))) + 20.;
+    const double tau_f = a_f + b_f + g_f;
+    TB(f2_inf)[Vi] = (.67 / (1. + exp((V + 35.) / 7.))) + .33;
+    const double a_f2 = 600. * exp(-(V + 25) * (V + 25) / 170.);
+    const double b_f2 = 31. / (1. + exp((25 - V) / 10.));
+    const double c_f2 = 16. / (1. + exp((V + 30) / 10.));
+    const double tau_f2 = a_f2 + b_f2 + c_f2;
+    TB(NaCa_P1)[Vi] = ((1. / ((P_(KmNai3)) + (P_(Nao3)))) * (1. / ((P_(KmCa)) + (P_(Ca_o)))) *
+                       (1. / (1. + (P_(ksat)) * exp(((P_(n)) - 1.) * V * (P_(inverseRTONF)))))) *
+                      (exp((P_(n)) * V * (P_(inverseRTONF))) * (P_(Ca_o)));
+    TB(NaCa_P2)[Vi] = ((1. / ((P_(KmNai3)) + (P_(Nao3)))) * (1. / ((P_(KmCa)) + (P_(Ca_o)))) *
+                       (1. / (1. + (P_(ksat)) * exp(((P_(n)) - 1.) * V * (P_(inverseRTONF)))))) *
+                      (exp(((P_(n)) - 1) * V / (P_(RTONF))) * (P_(Na_o)) * (P_(Na_o)) * (P_(Na_o)) * 2.5);
+    TB(CaL_P1)[Vi] = 4 * (V - 15.) * (P_(F)) / (P_(RTONF)) * (0.25 * exp(2 * (V - 15.) / (P_(RTONF)))) /
+                     (exp(2 * (V - 15.) / (P_(RTONF))) - 1.);
+    TB(CaL_P2)[Vi] = 4 * (V - 15.) * ((P_(F)) / (P_(RTONF))) * (1 * (P_(Ca_o))) /
+                     (exp(2 * (V - 15.) / (P_(RTONF))) - 1.);
+    const double HT = tinc * 1000;
+    TB(exptau_m)[Vi] = exp(-HT / tau_m);
+    TB(exptau_h)[Vi] = exp(-HT / tau_h);
+    TB(exptau_j)[Vi] = exp(-HT / tau_j);
+    TB(exptau_Xr1)[Vi] = exp(-HT / tau_Xr1);
+    TB(exptau_Xr2)[Vi] = exp(-HT / tau_Xr2);
+    TB(exptau_Xs)[Vi] = exp(-HT / tau_Xs);
+    TB(exptau_s)[Vi] = exp(-HT / tau_s);
+    TB(exptau_r)[Vi] = exp(-HT / tau_r);
+    TB(exptau_d)[Vi] = exp(-HT / tau_d);
+    TB(exptau_f)[Vi] = exp(-HT / tau_f);
+    TB(exptau_f2)[Vi] = exp(-HT / tau_f2);
+    const double Cai = Vi * (P_(StepCai));
+    TB(ECA)[Vi] = ((P_(RTONF)) * 0.5) * (log(((P_(Ca_o)) / Cai)));
+  }
+}
+
+/* Block offsets (TenTusscher2.h:77-123). */
+enum { S_Cai = 0, S_CaSR, S_CaSS, S_Nai, S_Ki, S_Array, S_m = 23, S_h, S_j, S_xr1, S_xr2, S_xs, S_r, S_s,
+       S_d, S_f, S_f2, S_fCa, S_Rq };
+
+/* TenTusscherEtAl2::Init (250-271). */
+static void tt2_init(const double *P, double *b) {
+  memset(b, 0, 36 * sizeof(double));
+  b[S_m] = P_(init_m); b[S_h] = P_(init_h); b[S_j] = P_(init_j); b[S_xr1] = P_(init_Xr1);
+  b[S_xr2] = P_(init_Xr2); b[S_xs] = P_(init_Xs); b[S_r] = P_(init_r); b[S_s] = P_(init_s);
+  b[S_d] = P_(init_d); b[S_f] = P_(init_f); b[S_f2] = P_(init_f2); b[S_fCa] = P_(init_fCa);
+  b[S_Rq] = P_(init_Rq); b[S_Cai] = P_(init_Cai); b[S_CaSR] = P_(init_CaSR); b[S_CaSS] = P_(init_CaSS);
+  b[S_Nai] = P_(init_Nai); b[S_Ki] = P_(init_Ki);
+}
+
+/* TenTusscherEtAl2::Calc (615-906), useCaTab on, no ischemia/Markov/SAC. */
+static double tt2_calc(const double *P, const double *tables, double *b, double tinc, double V,
+                       double i_external) {
+  double Ca_i = b[S_Cai], CaSR = b[S_CaSR], CaSS = b[S_CaSS], Na_i = b[S_Nai], K_i = b[S_Ki];
+  double m = b[S_m], h = b[S_h], j = b[S_j], xr1 = b[S_xr1], xr2 = b[S_xr2], xs = b[S_xs];
+  double r = b[S_r], s = b[S_s], d = b[S_d], f = b[S_f], f2 = b[S_f2], fCa = b[S_fCa], Rq = b[S_Rq];
+  const double svolt = V * 1000;
+  const int Vi = (int)(DIVISION_TAB * (RANGE_TAB_HALF + svolt) + .5);
+  i_external = i_external / 2.29656e-2;
+  /* function-level statics in the reference (638-640); one parameter set here */
+  const double CaiTabConst1 = -P_(CaiMin) / P_(StepCai) + 0.5;
+  const double CaiTabConst2 = 1. / P_(StepCai);
+  const int Caitab = (int)(CaiTabConst2 * Ca_i + CaiTabConst1);
+  const double K_o_int = P_(K_o);
+  const double RTONF = P_(RTONF);
+  const double EK = RTONF * (log((K_o_int / K_i)));
+  const double VminEK = svolt - EK;
+  const double ENa = RTONF * (log((P_(Na_o) / Na_i)));
+  const double VminENa = svolt - ENa;
+  const double EKs = RTONF * (log((K_o_int + P_(pKNa) * P_(Na_o)) / (K_i + P_(pKNa) * Na_i)));
+  const double AK1 = 0.1 / (1. + exp(0.06 * (VminEK - 200)));
+  const double BK1 = (3. * exp(0.0002 * (VminEK + 100)) + exp(0.1 * (VminEK - 10))) / (1. + exp(-0.5 * (VminEK)));
+  const double rec_iK1 = AK1 / (AK1 + BK1);
+  const double I_pCa = P_(g_pCa) * Ca_i / (P_(KpCa) + Ca_i);
+  const double I_pK = TB(rec_ipK)[Vi] * VminEK;
+  const double I_to = P_(g_to) * r * s * VminEK;
+  const double I_Kr = P_(g_Kr) * sqrt(K_o_int / 5.4) * xr1 * xr2 * VminEK;
+  const double I_Ks = P_(g_Ks) * xs * xs * (svolt - EKs);
+  const double I_K = I_Kr + I_Ks;
+  const double I_K1 = P_(g_K1) * sqrt(K_o_int / 5.4) * rec_iK1 * VminEK;
+  const double I_bNa = P_(g_bNa) * VminENa;
+  const double I_bCa = P_(g_bCa) * (svolt - (TB(ECA)[Caitab]));
+  const double I_Na = P_(g_Na) * m * m * m * h * j * VminENa;
+  const double I_CaL = P_(g_CaL) * d * f * f2 * fCa * (((TB(CaL_P1)[Vi]) * CaSS) - (TB(CaL_P2)[Vi]));
+  const double I_NaCa = P_(kNaCa) * (TB(NaCa_P1)[Vi]) * Na_i * Na_i * Na_i - P_(kNaCa) * (TB(NaCa_P2)[Vi]) * Ca_i;
+  const double I_NaK =
+      P_(knak) * (K_o_int / (K_o_int + P_(KmK))) * (Na_i / (Na_i + P_(KmNa))) * (TB(NaK_P1)[Vi]);
+  const double I_tot = I_K + I_K1 + I_to + I_Na + I_bNa + I_CaL + I_bCa + I_NaK + I_NaCa + I_pCa + I_pK - i_external;
+
+  const double Vss = P_(Vss), Cm = P_(C), max_sr = P_(max_sr), Bufsr = P_(Bufsr), EC = P_(EC);
+  const double Kbufsr = P_(Kbufsr), Bufss = P_(Bufss), Kbufss = P_(Kbufss), Kbufc = P_(Kbufc);
+  const double inverseviF = P_(inverseviF);
+  const double Caisquare = Ca_i * Ca_i;
+  const double CaSSsquare = CaSS * CaSS;
+  const double kCaSR = max_sr - ((max_sr - P_(min_sr)) / (1 + (EC / CaSR) * (EC / CaSR)));
+  const double k2 = P_(ks2) * kCaSR;
+  const double k1 = P_(ks1) / kCaSR;
+  const double dRq = 1000.0 * ((-k2 * CaSS * Rq) + (P_(k4) * (1.0 - Rq)));
+  Rq += tinc * dRq;
+  const double O = k1 * CaSSsquare * Rq / (P_(k3) + k1 * CaSSsquare);
+  const double I_rel = P_(Vrel) * O * (CaSR - CaSS);
+  const double I_leak = 0.00036 * (CaSR - Ca_i);
+  const double I_xfer = P_(Vxfer) * (CaSS - Ca_i);
+  const double SERCA = P_(Vmaxup) / (1. + (P_(Kupsquare) / Caisquare));
+  const double dCaSR = tinc * 1000.0 * (SERCA - I_rel - I_leak);
+  const double CaCSQN = Bufsr * CaSR / (CaSR + Kbufsr);
+  const double bjsr = Bufsr - CaCSQN - dCaSR - CaSR + Kbufsr;
+  const double cjsr = Kbufsr * (CaCSQN + dCaSR + CaSR);
+  CaSR = (sqrt(bjsr * bjsr + 4 * cjsr) - bjsr) / 2.;
+  const double CaSSBuf = Bufss * CaSS / (CaSS + Kbufss);
+  const double dCaSS =
+      tinc * 1000.0 * (-I_xfer * (P_(Vc) / Vss) + I_rel * (P_(Vsr) / Vss) + (-I_CaL * P_(inversevssF2) * Cm));
+  const double bjss = Bufss - CaSSBuf - dCaSS - CaSS + Kbufss;
+  const double cjss = Kbufss * (CaSSBuf + dCaSS + CaSS);
+  CaSS = (sqrt(bjss * bjss + 4. * cjss) - bjss) / 2.;
+  const double CaBuf = P_(Bufc) * Ca_i / (Ca_i + Kbufc);
+  const double dCai =
+      tinc * 1000.0 * ((-(I_bCa + I_pCa - 2 * I_NaCa) * P_(inverseviF2) * Cm) - (SERCA - I_leak) * (1.0 / P_(VcdVsr)) + I_xfer);
+  const double bc = P_(BufcPKbufc) - CaBuf - dCai - Ca_i;
+  const double cc = Kbufc * (CaBuf + dCai + Ca_i);
+  Ca_i = (sqrt(bc * bc + 4 * cc) - bc) / 2.;
+  const double dNai = -(I_Na + I_bNa + 3 * I_NaK + 3 * I_NaCa) * inverseviF * Cm;
+  Na_i += tinc * dNai * 1000;
+  const double dKi = -(-i_external + I_K1 + I_to + I_K - 2 * I_NaK + I_pK) * inverseviF * Cm;
+  K_i += tinc * dKi * 1000.0;
+  const double CaSS005 = (CaSS / 0.05);
+  const double FCa_INF = 0.6 / (1.0 + CaSS005 * CaSS005) + 0.4;
+  const double taufca = 0.080 / (1.0 + CaSS005 * CaSS005) + 0.002;
+
+  const double M_INF = TB(m_inf)[Vi], H_INF = TB(h_inf)[Vi], J_INF = TB(j_inf)[Vi];
+  const double Xr1_INF = TB(Xr1_inf)[Vi], Xr2_INF = TB(Xr2_inf)[Vi], Xs_INF = TB(Xs_inf)[Vi];
+  const double S_INF = TB(s_inf)[Vi], R_INF = TB(r_inf)[Vi], D_INF = TB(d_inf)[Vi];
+  const double F_INF = TB(f_inf)[Vi], F2_INF = TB(f2_inf)[Vi];
+  m = M_INF - (M_INF - m) * TB(exptau_m)[Vi];
+  h = H_INF - (H_INF - h) * TB(exptau_h)[Vi];
+  j = J_INF - (J_INF - j) * TB(exptau_j)[Vi];
+  xr1 = Xr1_INF - (Xr1_INF - xr1) * TB(exptau_Xr1)[Vi];
+  xr2 = Xr2_INF - (Xr2_INF - xr2) * TB(exptau_Xr2)[Vi];
+  xs = Xs_INF - (Xs_INF - xs) * TB(exptau_Xs)[Vi];
+  s = S_INF - (S_INF - s) * TB(exptau_s)[Vi];
+  r = R_INF - (R_INF - r) * TB(exptau_r)[Vi];
+  d = D_INF - (D_INF - d) * TB(exptau_d)[Vi];
+  f = F_INF - (F_INF - f) * TB(exptau_f)[Vi];
+  f2 = F2_INF - (F2_INF - f2) * TB(exptau_f2)[Vi];
+  fCa = FCa_INF - (FCa_INF - fCa) * exp(-tinc / taufca);
+
+  double *A = b + S_Array; /* diagnostic currents (883-899) */
+  A[0] = I_Na; A[1] = I_CaL; A[2] = I_bCa; A[3] = I_pCa; A[4] = I_to; A[5] = I_Ks; A[6] = I_Kr;
+  A[7] = I_K1; A[8] = I_pK; A[9] = I_bNa; A[10] = I_NaK; A[11] = I_NaCa; A[12] = I_rel; A[13] = I_leak;
+  A[14] = I_xfer; A[15] = SERCA; A[16] = I_tot;
+  b[S_Cai] = Ca_i; b[S_CaSR] = CaSR; b[S_CaSS] = CaSS; b[S_Nai] = Na_i; b[S_Ki] = K_i;
+  b[S_m] = m; b[S_h] = h; b[S_j] = j; b[S_xr1] = xr1; b[S_xr2] = xr2; b[S_xs] = xs; b[S_r] = r;
+  b[S_s] = s; b[S_d] = d; b[S_f] = f; b[S_f2] = f2; b[S_fCa] = fCa; b[S_Rq] = Rq;
+  return tinc * (-I_tot);
+}
+#undef P_
+#undef TB
+
+/* ---------------------------------------------------------------- Courtemanche */
+#define P_(x) P[C_##x]
+#define TB(x) (tables + (size_t)TC_##x * CMO_RTDT)
+
+/* CourtemancheParameters::Calculate (252-280). */
+static void crn_derive(double *P) {
+  P_(RTdF) = P_(R) * (P_(Tx)) / (P_(F));
+  P_(FdRT) = 1.0 / (P_(RTdF));
+  P_(RTd2F) = P_(RTdF) * .5;
+  P_(Vi) = P_(Vcell) * (P_(part_i));
+  P_(Vup) = P_(Vcell) * (P_(part_up));
+  P_(Vrel) = P_(Vcell) * (P_(part_rel));
+  P_(VupdVi) = P_(Vup) / (P_(Vi));
+  P_(VreldVi) = P_(Vrel) / (P_(Vi));
+  P_(VreldVup) = P_(Vrel) / (P_(Vup));
+  P_(CmdFvi) = P_(C_m) / (P_(F) * (P_(Vi)));
+  P_(Cmd2F) = P_(C_m) / (P_(F) * 2.0);
+  P_(csqnkm) = P_(CSQNmax) * P_(K_mcsqn);
+  P_(kmcsqnm2) = P_(K_mcsqn) * 2.0;
+  P_(kkmcsqn) = P_(K_mcsqn) * P_(K_mcsqn);
+  P_(cmdnkm) = P_(CMDNmax) * P_(K_mcmdn);
+  P_(kmcmdnm2) = P_(K_mcmdn) * 2.0;
+  P_(kkmcmdn) = P_(K_mcmdn) * P_(K_mcmdn);
+  P_(kupleak) = P_(I_upmax) / (P_(Ca_upmax));
+  P_(dt_tr) = 1.0 / (P_(t_tr));
+}
+
+/* CourtemancheParameters::InitTable (282-395) plus exp250/exp50 (Init 246-247), which are
+ * stored in the first two entries of the last table. */
+static void crn_tables(const double *P, double tinc, double *tables) {
+  tinc *= 1000;
+  const double sigma = (exp(P_(Na_o) / 67.3) - 1.0) / 7.0;
+  for (double V = -RANGE_TAB_HALF + .0001; V < RANGE_TAB_HALF; V += D_DIVISION_TAB) {
+    int Vi = (int)(DIVISION_TAB * (RANGE_TAB_HALF + V) + .5);
+    if (Vi < 0 || Vi >= CMO_RTDT) continue;
+    double a = ((fabs(V + 47.13 - P_(shiftm)) < 1e-10
+                     ? 3.2
+                     : P_(m_a1) * (V + 47.13 - P_(shiftm)) / (1.0 - exp(-(V + 47.13 - P_(shiftm)) * P_(m_a2)))));
+    double b = P_(m_b1) * exp(-(V - P_(shiftm)) / P_(m_b2));
+    TB(exptau_m)[Vi] = exp(-tinc * (a + b));
+    TB(m_m)[Vi] = a / (a + b);
+
+    if (V >= -40.0 + P_(shifth)) {
+      a = .0;
+      b = 1.0 / (P_(h_b5) * (1.0 + exp(-(V + 10.66 - P_(shifth)) / P_(h_b6))));
+    } else {
+      a = P_(h_a1) * exp(-(V + 80.0 - P_(shifth)) / P_(h_a2));
+      b = P_(h_b1) * exp(P_(h_b2) * (V - P_(shifth))) + P_(h_b3) * exp(P_(h_b4) * (V - P_(shifth)));
+    }
+    TB(exptau_h)[Vi] = exp(-tinc * (a + b));
+    TB(m_h)[Vi] = a / (a + b);
+
+    if (V >= -40.0 + P_(shiftj)) {
+      a = .0;
+      b = P_(j_b4) * exp(P_(j_b5) * (V - P_(shiftj))) / (1.0 + exp(P_(j_b6) * (V + 32.0 - P_(shiftj))));
+    } else {
+      a = (P_(j_a1) * exp(P_(j_a2) * (V - P_(shiftj))) - (P_(j_a3)) * exp(P_(j_a4) * (V - P_(shiftj)))) *
+          (V + 37.78 - P_(shiftj)) / (1.0 + exp(P_(j_a5) * (V + 79.23 - P_(shiftj))));
+      b = P_(j_b1) * exp(P_(j_b2) * (V - P_(shiftj))) / (1.0 + exp(P_(j_b3) * (V + 40.14 - P_(shiftj))));
+    }
+    TB(exptau_j)[Vi] = exp(-tinc * (a + b) / P_(tau_j_mult));
+    TB(m_j)[Vi] = a / (a + b);
+
+    a = P_(C_oa_1) / ((exp(-(V - P_(shiftoa) + 10.0) / (P_(C_oa_2)))) + (exp(-(V - P_(shiftoa) - 30.0) / (P_(C_oa_3)))));
+    b = P_(C_oa_1) / (2.5 + exp((V - P_(shiftoa) + 82.0) / (P_(C_oa_4))));
+    TB(m_oa)[Vi] = 1.0 / (1.0 + exp(-(V - P_(shiftoa) + P_(C_oa_6)) / (P_(C_oa_5))));
+    TB(exptau_oa)[Vi] = exp(-tinc * ((a + b) * P_(Tfac)));
+
+    a = 1.0 / (18.53 + exp((V + 113.7) / 10.95));
+    b = 1.0 / (35.56 + exp(-(V + 1.26) / 7.44));
+    TB(m_oi)[Vi] = 1.0 / (1.0 + exp((V + 43.1) / 5.3));
+    TB(exptau_oi)[Vi] = exp(-tinc * ((a + b) * P_(Tfac)));
+
+    a = P_(ua_a1) / ((exp((V + P_(ua_a2)) / (P_(ua_a3)))) + (exp((V + P_(ua_a4)) / (P_(ua_a5)))));
+    b = .65 / (P_(ua_b1) + exp((V + P_(ua_b2)) / (P_(ua_b3))));
+    TB(m_ua)[Vi] = 1.0 / (1.0 + exp((V + P_(ua_m1)) / (P_(ua_m2))));
+    TB(exptau_ua)[Vi] = exp(-tinc * ((a + b) * P_(ua_KQ10)));
+
+    a = P_(ui_a1) / (P_(ui_a2) + exp((V + P_(ui_a3)) / (P_(ui_a4))));
+    b = 1.0 / exp((V + P_(ui_b1)) / (P_(ui_b2)));
+    TB(m_ui)[Vi] = 1.0 / (1.0 + exp((V + P_(ui_m1)) / (P_(ui_m2))));
+    TB(exptau_ui)[Vi] = exp(-tinc * ((a + b) * P_(ui_KQ10)));
+
+    a = (fabs(V + P_(Xr_a2)) < 1e-10 ? 0.0015
+                                      : P_(Xr_a1) * (V + P_(Xr_a2)) / (1.0 - exp((V + P_(Xr_a2)) / (P_(Xr_a3)))));
+    b = (fabs(V - P_(Xr_b1)) < 1e-10 ? 3.7836118e-4
+                                      : 7.3898e-5 * (V + P_(Xr_b1)) / (exp((V + P_(Xr_b1)) / (P_(Xr_b2))) - 1.0));
+    TB(m_Xr)[Vi] = 1.0 / (1.0 + exp((V + P_(Xr_m1)) / (P_(Xr_m2))));
+    TB(exptau_Xr)[Vi] = exp(-tinc * (P_(Xr_KQ10) * (a + b)));
+
+    a = (fabs(V + P_(Xs_a2)) < 1e-10 ? 0.00068
+                                      : P_(Xs_a1) * (V + P_(Xs_a2)) / (1.0 - exp((V + P_(Xs_a2)) / (P_(Xs_a3)))));
+    b = (fabs(V + P_(Xs_b1)) < 1e-10 ? 0.000315
+                                      : (3.5e-5) * (V + P_(Xs_b1)) / (exp((V + P_(Xs_b1)) / (P_(Xs_b2))) - 1.0));
+    TB(exptau_Xs)[Vi] = exp(-tinc * (P_(Xs_KQ10) * (a + b)));
+    TB(m_Xs)[Vi] = 1.0 / sqrt(1.0 + exp((V + P_(Xs_m1)) / (P_(Xs_m2))));
+
+    a = 1.0 / (1.0 + exp(-(V + 10.0) / 6.24));
+    TB(exptau_d)[Vi] = exp(-tinc * (fabs(V + 10.0) < 1e-10 ? 1.0 / (a * 4.579)
+                                                            : 1.0 / (a * (1.0 - exp(-(V + 10.0) / 6.24)) / (0.035 * (V + 10.0)))));
+    TB(m_d)[Vi] = 1.0 / (1.0 + exp(-(V + 10.0) / 8));
+    if (V > 0) {
+      TB(exptau_f)[Vi] = exp(-tinc * (1.0 / (P_(CaL_fT_1) / (0.0197 * exp(-0.0337 * 0.0337 * (V + 10.0) * (V + 10.0)) + 0.02) *
+                                             P_(tau_f_mult))));
+    } else {
+      TB(exptau_f)[Vi] = exp(-tinc * (1.0 / (P_(CaL_fT_1) / (0.0197 * exp(-0.0337 * 0.0337 * (V + 10.0) * (V + 10.0)) + 0.02))));
+    }
+    TB(m_f)[Vi] = exp(-(V + 28.0) / 6.9) / (1.0 + exp(-(V + 28.0) / 6.9));
+
+    TB(exptau_w)[Vi] =
+        exp(-tinc * (fabs(V - 7.9) < 1e-10 ? 1.0 / (6.0 * 0.2 / 1.3)
+                                            : 1.0 / (6.0 * (1.0 - exp(-(V - 7.9) / 5.0)) / (1.0 + 0.3 * exp(-(V - 7.9) / 5.0)) / (V - 7.9))));
+    TB(m_w)[Vi] = 1.0 - 1.0 / (1.0 + exp(-(V - 40.0) / 17.0));
+
+    const double VFdRT = V * P_(FdRT);
+    TB(expVm)[Vi] = exp(-VFdRT) * P_(Na_o) * P_(Na_o) * P_(Na_o);
+    TB(g_Kur)[Vi] = P_(g_Kur1) + P_(g_Kur2) / (1.0 + exp((V + P_(g_Kur3)) / (P_(g_Kur4))));
+    TB(CKr)[Vi] = P_(g_Kr) / (1.0 + exp((V + P_(g_Kr1)) / (P_(g_Kr2))));
+    TB(CK1)[Vi] = P_(g_K1) / (1.0 + exp((V + P_(g_K1_1)) * P_(g_K1_2)));
+    TB(CNaK)[Vi] = P_(I_NaKmax) / (1.0 + .1245 * exp(-.1 * VFdRT) + .0365 * sigma * exp(-VFdRT)) * P_(K_o) /
+                   (P_(K_o) + P_(k_mKo));
+    TB(CNaCa)[Vi] = P_(k_NaCa) * exp(P_(gamm) * VFdRT) /
+                    ((P_(k_mNa) * P_(k_mNa) * P_(k_mNa) + P_(Na_o) * P_(Na_o) * P_(Na_o)) * (P_(k_mCa) + P_(Ca_o)) *
+                     (1.0 + P_(k_sat) * exp((P_(gamm) - 1.0) * VFdRT)));
+  }
+  memset(TB(exp250_exp50), 0, CMO_RTDT * sizeof(double));
+  TB(exp250_exp50)[0] = exp(250.0);
+  TB(exp250_exp50)[1] = exp(169.5);
+}
+
+enum { K_Cai = 0, K_Caup, K_Carel, K_h, K_j, K_oi, K_ui, K_Xr, K_Xs, K_u, K_v, K_w, K_Nai, K_Ki, K_m, K_oa,
+       K_ua, K_d, K_f, K_fCa, K_ISAC, K_CaTRPN };
+
+/* Courtemanche::Init (56-83). I_SAC is not set by Init; it starts at 0 here. */
+static void crn_init(const double *P, double *b) {
+  memset(b, 0, 22 * sizeof(double));
+  b[K_Nai] = P_(Init_Na_i); b[K_Ki] = P_(Init_K_i); b[K_m] = P_(Init_m); b[K_oa] = P_(Init_oa);
+  b[K_ua] = P_(Init_ua); b[K_d] = P_(Init_d); b[K_fCa] = P_(Init_f_Ca); b[K_Cai] = P_(Init_Ca_i);
+  b[K_Caup] = P_(Init_Ca_up); b[K_Carel] = P_(Init_Ca_rel); b[K_h] = P_(Init_h); b[K_j] = P_(Init_j);
+  b[K_oi] = P_(Init_oi); b[K_ui] = P_(Init_ui); b[K_Xr] = P_(Init_Xr); b[K_Xs] = P_(Init_Xs);
+  b[K_f] = P_(Init_f); b[K_u] = P_(Init_u); b[K_v] = P_(Init_v); b[K_w] = P_(Init_w);
+  b[K_CaTRPN] = P_(Init_Ca_TRPN) / P_(TRPNmax);
+}
+
+static inline double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+/* Courtemanche::Calc (85-187), ISAC and TRPN compiled in (CourtemancheParameters.h:20,23). */
+static double crn_calc(const double *P, const double *tables, double *bk, double tinc, double V,
+                       double i_external, double stretch) {
+  double Ca_i = bk[K_Cai], Ca_up = bk[K_Caup], Ca_rel = bk[K_Carel], h = bk[K_h], j = bk[K_j];
+  double oi = bk[K_oi], ui = bk[K_ui], Xr = bk[K_Xr], Xs = bk[K_Xs], u = bk[K_u], v = bk[K_v];
+  double w = bk[K_w], Na_i = bk[K_Nai], K_i = bk[K_Ki], m = bk[K_m], oa = bk[K_oa], ua = bk[K_ua];
+  double d = bk[K_d], f = bk[K_f], f_Ca = bk[K_fCa], Ca_TRPN = bk[K_CaTRPN];
+  tinc *= 1000.0;
+  const double V_int = V * 1000.0;
+  const int Vi = (int)(DIVISION_TAB * (RANGE_TAB_HALF + V_int) + .5);
+  const double dNa_i = 1.0 / Na_i;
+  const double VmE_Na = V_int - ((P_(RTdF)) * log((P_(Na_o)) * dNa_i));
+  const double VmE_K = V_int - ((P_(RTdF)) * log((P_(K_o)) / K_i));
+  const double VmE_Ca = V_int - ((P_(RTd2F)) * log((P_(Ca_o)) / (double)Ca_i));
+  const double m_m = TB(m_m)[Vi];
+  m = m_m + (m - m_m) * TB(exptau_m)[Vi];
+  m = clamp01(m);
+  const double m_h = TB(m_h)[Vi];
+  h = m_h + (h - m_h) * TB(exptau_h)[Vi];
+  const double m_j = TB(m_j)[Vi];
+  j = m_j + (j - m_j) * TB(exptau_j)[Vi];
+  const double m_oa = TB(m_oa)[Vi];
+  oa = m_oa + (oa - m_oa) * TB(exptau_oa)[Vi];
+  const double m_oi = TB(m_oi)[Vi];
+  oi = m_oi + (oi - m_oi) * TB(exptau_oi)[Vi];
+  const double m_ua = TB(m_ua)[Vi];
+  ua = m_ua + (ua - m_ua) * TB(exptau_ua)[Vi];
+  const double m_ui = TB(m_ui)[Vi];
+  ui = m_ui + (ui - m_ui) * TB(exptau_ui)[Vi];
+  const double m_Xr = TB(m_Xr)[Vi];
+  Xr = m_Xr + (Xr - m_Xr) * TB(exptau_Xr)[Vi];
+  const double m_Xs = TB(m_Xs)[Vi];
+  Xs = m_Xs + (Xs - m_Xs) * TB(exptau_Xs)[Vi];
+  const double m_d = TB(m_d)[Vi];
+  d = m_d + (d - m_d) * TB(exptau_d)[Vi];
+  const double m_f = TB(m_f)[Vi];
+  f = m_f + (f - m_f) * TB(exptau_f)[Vi];
+  f_Ca += (1.0 / (1.0 + Ca_i * 2857.1429) - f_Ca) * 0.5 * tinc;
+  const double m_w = TB(m_w)[Vi];
+  w = m_w + (w - m_w) * TB(exptau_w)[Vi];
+
+  const double I_Na = (P_(g_Na)) * m * m * m * h * j * VmE_Na;
+  const double I_to = (P_(g_to)) * oa * oa * oa * oi * VmE_K;
+  const double I_Kur = TB(g_Kur)[Vi] * ua * ua * ua * ui * VmE_K;
+  const double I_Kr = TB(CKr)[Vi] * Xr * VmE_K;
+  const double I_Ks = (P_(g_Ks)) * Xs * Xs * VmE_K;
+  const double I_CaL = (P_(g_CaL)) * d * f * f_Ca * (V_int - (P_(E_rL)));
+  const double I_K1 = TB(CK1)[Vi] * VmE_K;
+  const double I_bNa = (P_(g_bNa)) * VmE_Na;
+  const double I_bCa = (P_(g_bCa)) * VmE_Ca;
+  const double temp = (P_(k_mNai)) * dNa_i;
+  const double I_NaK = TB(CNaK)[Vi] / (1.0 + temp * sqrt(temp));
+  const double I_pCa = (P_(I_pCamax)) * Ca_i / (Ca_i + (P_(k_mpCa)));
+  const double I_NaCa = TB(CNaCa)[Vi] * ((Na_i * Na_i * Na_i * (P_(Ca_o))) - TB(expVm)[Vi] * Ca_i);
+  const double I_rel = (P_(k_rel)) * u * u * v * w * (Ca_rel - Ca_i);
+  const double I_up = (P_(I_upmax)) * Ca_i / (Ca_i + (P_(k_up)));
+  const double I_upleak = (P_(kupleak)) * Ca_up;
+  const double I_tr = (Ca_up - Ca_rel) * (P_(dt_tr));
+  double I_SAC = P_(G_sac) * (V_int - P_(E_sac)) / (1. + P_(K_sac) * exp(-P_(alpha) * (stretch - 1.)));
+  I_SAC *= P_(ISAC_SWITCH);
+  const double Ca_T50 = P_(Ca_T50) + P_(beta1) * ((stretch < 1.2 ? stretch : 1.2) - 1.);
+  const double dCaTRPN = P_(k_TRPN) * (pow(1000 * Ca_i / Ca_T50, P_(n_TRPN)) * (1. - Ca_TRPN) - Ca_TRPN);
+  Ca_TRPN += tinc * dCaTRPN;
+  Ca_up += tinc * (I_up - I_tr * (P_(VreldVup)) - I_upleak);
+  Ca_rel += tinc * ((I_tr - I_rel) / (1.0 + (P_(csqnkm)) / (Ca_rel * Ca_rel + Ca_rel * (P_(kmcsqnm2)) + (P_(kkmcsqn)))));
+  Na_i += tinc * (-3.0 * I_NaK - 3.0 * I_NaCa - I_bNa - I_Na) * (P_(CmdFvi));
+  K_i += tinc * (2.0 * I_NaK - I_K1 - I_to - I_Kur - I_Kr - I_Ks) * (P_(CmdFvi));
+  double B1 = ((2.0 * I_NaCa - I_pCa - I_CaL - I_bCa) * .5 * (P_(CmdFvi))) +
+              ((I_upleak - I_up) * (P_(VupdVi)) + I_rel * (P_(VreldVi)));
+  B1 -= P_(TRPNmax) * dCaTRPN;
+  const double B2 = 1.0 + ((P_(cmdnkm)) / ((Ca_i * Ca_i) + (Ca_i * (P_(kmcmdnm2))) + (P_(kkmcmdn))));
+  const double dCa_i = B1 / B2;
+  Ca_i += tinc * dCa_i;
+  const double Fn = exp(-((P_(Vrel)) * I_rel - (0.5 * I_CaL - 0.2 * I_NaCa) * (P_(Cmd2F))) * 731.5289);
+  const double m_u = 1.0 / (1.0 + Fn * TB(exp250_exp50)[0]);
+  u += (m_u - u) * 0.125 * tinc;
+  const double m_v = 1.0 - 1.0 / (1.0 + Fn * TB(exp250_exp50)[1]);
+  const double t_v = 1.91 + 2.09 * m_u;
+  v += (m_v - v) * tinc / t_v;
+  const double I_tot = I_Na + I_CaL + I_pCa + I_K1 + I_to + I_Kur + I_Kr + I_Ks + I_bNa + I_bCa + I_NaK + I_NaCa +
+                       I_SAC - i_external;
+  bk[K_Cai] = Ca_i; bk[K_Caup] = Ca_up; bk[K_Carel] = Ca_rel; bk[K_h] = h; bk[K_j] = j; bk[K_oi] = oi;
+  bk[K_ui] = ui; bk[K_Xr] = Xr; bk[K_Xs] = Xs; bk[K_u] = u; bk[K_v] = v; bk[K_w] = w; bk[K_Nai] = Na_i;
+  bk[K_Ki] = K_i; bk[K_m] = m; bk[K_oa] = oa; bk[K_ua] = ua; bk[K_d] = d; bk[K_f] = f; bk[K_fCa] = f_Ca;
+  bk[K_ISAC] = I_SAC; bk[K_CaTRPN] = Ca_TRPN;
+  return -.001 * I_tot * tinc;
+}
+#undef P_
+#undef TB
+
+/* ---------------------------------------------------------------- public entry points */
+static void derive(int model, double *P) {
+  if (model == CMO_TT2) tt2_derive(P);
+  else crn_derive(P);
+}
+
+int cmo_build_tables(int model, const double *P_in, double dt, double *tables) {
+  int np = cmo_n_params(model);
+  if (np < 0) return -1;
+  double *P = (double *)malloc(np * sizeof(double));
+  memcpy(P, P_in, np * sizeof(double));
+  derive(model, P);
+  memset(tables, 0, (size_t)cmo_n_tables(model) * CMO_RTDT * sizeof(double));
+  if (model == CMO_TT2) tt2_tables(P, dt, tables);
+  else crn_tables(P, dt, tables);
+  free(P);
+  return 0;
+}
+
+void cmo_init_state(int model, const double *P, double *block) {
+  if (model == CMO_TT2) tt2_init(P, block);
+  else crn_init(P, block);
+}
+
+double cmo_init_vm(int model, const double *P) { return model == CMO_TT2 ? P[T_init_V_m] : P[C_Init_Vm]; }
+
+double cmo_calc(int model, const double *P_in, const double *tables, double *block, double dt, double V,
+                double i_ext, double stretch) {
+  /* P_in holds base and derived values (the caller derives once via cmo_derive). */
+  if (model == CMO_TT2) return tt2_calc(P_in, tables, block, dt, V, i_ext);
+  return crn_calc(P_in, tables, block, dt, V, i_ext, stretch);
+}
+
+/* Fills the derived slots of P in place (Calculate()). */
+void cmo_derive(int model, double *P) { derive(model, P); }
+
+typedef struct {
+  int model;
+  const double *P;
+  const double *tables;
+  long lo, hi, n_cells;
+  double *blocks, *Vm;
+  int n_het;
+  const int *het_idx;
+  const double *het_vals;
+  long n_steps;
+  double dt, t0, textbegin;
+  const double *tb_cell;
+  double textlen, bcl, amp;
+  long rec_every;
+  double *trace;
+  int bad;
+} run_args;
+
+static void *run_range(void *argp) {
+  run_args *a = (run_args *)argp;
+  const int np = cmo_n_params(a->model), ns = cmo_state_doubles(a->model);
+  double *Pc = (double *)malloc(np * sizeof(double));
+  const long n_rec = a->rec_every > 0 ? (a->n_steps + a->rec_every - 1) / a->rec_every : 0;
+  for (long c = a->lo; c < a->hi; c++) {
+    memcpy(Pc, a->P, np * sizeof(double));
+    for (int k = 0; k < a->n_het; k++) Pc[a->het_idx[k]] = a->het_vals[(size_t)k * a->n_cells + c];
+    double *blk = a->blocks + (size_t)c * ns;
+    double t = a->t0, tb = a->tb_cell ? a->tb_cell[c] : a->textbegin, v = a->Vm[c];
+    for (long s = 0; s < a->n_steps; s++) {
+      if (a->trace && a->rec_every > 0 && s % a->rec_every == 0) a->trace[c * n_rec + s / a->rec_every] = v;
+      /* CellModel.h:405-419 with textend = thresVm = freq = HUGE */
+      double i_ext = 0.0;
+      if (t >= tb) {
+        i_ext = a->amp;
+        if (t >= tb + a->textlen) tb += a->bcl;
+      }
+      if (a->model == CMO_TT2) v += tt2_calc(Pc, a->tables, blk, a->dt, v, i_ext);
+      else v += crn_calc(Pc, a->tables, blk, a->dt, v, i_ext, 1.0);
+      t += a->dt;
+    }
+    if (isnan(v)) a->bad = 1;
+    a->Vm[c] = v;
+  }
+  free(Pc);
+  return 0;
+}
+
+int cmo_run(int model, const double *P, const double *tables, long n_cells, double *blocks, double *Vm,
+            int n_het, const int *het_idx, const double *het_vals, long n_steps, double dt, double t0,
+            double textbegin, const double *textbegin_per_cell, double textlen, double bcl, double amp,
+            long rec_every, double *trace, int n_threads) {
+  if (cmo_n_params(model) < 0) return -1;
+  if (n_threads < 1) n_threads = 1;
+  if (n_threads > n_cells) n_threads = (int)(n_cells > 0 ? n_cells : 1);
+  run_args *args = (run_args *)calloc(n_threads, sizeof(run_args));
+  pthread_t *th = (pthread_t *)calloc(n_threads, sizeof(pthread_t));
+  for (int k = 0; k < n_threads; k++) {
+    run_args *a = &args[k];
+    a->model = model; a->P = P; a->tables = tables; a->n_cells = n_cells;
+    a->lo = n_cells * k / n_threads; a->hi = n_cells * (k + 1) / n_threads;
+    a->blocks = blocks; a->Vm = Vm; a->n_het = n_het; a->het_idx = het_idx; a->het_vals = het_vals;
+    a->n_steps = n_steps; a->dt = dt; a->t0 = t0; a->textbegin = textbegin; a->tb_cell = textbegin_per_cell;
+    a->textlen = textlen; a->bcl = bcl; a->amp = amp; a->rec_every = rec_every; a->trace = trace;
+  }
+  if (n_threads == 1) {
+    run_range(&args[0]);
+  } else {
+    for (int k = 0; k < n_threads; k++) pthread_create(&th[k], 0, run_range, &args[k]);
+    for (int k = 0; k < n_threads; k++) pthread_join(th[k], 0);
+  }
+  int bad = 0;
+  for (int k = 0; k < n_threads; k++) bad |= args[k].bad;
+  free(args);
+  free(th);
+  return bad ? -3 : 0;
+}

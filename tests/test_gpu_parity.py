@@ -1,0 +1,203 @@
+"""GPU parity: the CUDA kernels through the C ABI against the oracle and the golden vectors.
+
+Tolerances:
+  FP64 batches  one Calc: rtol 1e-11 (CUDA's exp/log differ from glibc by a few ulp and the
+                kernel fuses multiply-adds); 1000 ms traces: |dVm| <= 1e-5 mV, APD90 and
+                upstroke within 1e-3 ms of the oracle.
+  mixed batches APD90 within 1 ms, upstroke within 0.1 ms, RMS Vm error <= 0.5 mV per cell.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from cardiomechanics_gb300 import analysis as A
+from cardiomechanics_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TAG = {5: "tt2", 2: "crn"}
+OM = {5: O.TT2, 2: O.CRN}
+HET = {5: W.TT2_HETERO, 2: W.CRN_HETERO}
+AMP = {5: W.TT2_STIM_NA, 2: W.CRN_STIM_PAPF}
+TLEN = {5: 1e-3, 2: 2e-3}
+
+
+def ref_block_cols(model):
+    # TT2 Array[17] is never written by the reference
+    return [c for c in range(36) if c != 22] if model == 5 else list(range(22))
+
+
+@pytest.mark.parametrize("model", [5, 2])
+def test_one_step_known_answers_fp64(gpu, model):
+    cm = gpu
+    g = np.load(O.GOLDEN / f"step_{TAG[model]}.npz")
+    dt = float(g["dt"])
+    p = cm.Params(model, None, dt)
+    n = g["state_in"].shape[0]
+    b = cm.Batch(p, n, cm.FP64)
+    b.set_diagnostics(True)
+    b.set_state(g["state_in"], cm.LAYOUT_REF_BLOCK)
+    for k, name in enumerate(g["hetero_names"]):
+        b.add_hetero_value(str(name), p.get(str(name)) * g["hetero_scale"][k])
+    dV = b.calc(dt, np.ascontiguousarray(g["vm"]), np.ascontiguousarray(g["i_ext"]))
+    S = b.get_state(cm.LAYOUT_REF_BLOCK)
+    cols = ref_block_cols(model)
+    np.testing.assert_allclose(S[:, cols], g["state_out"][:, cols], rtol=1e-11, atol=1e-250)
+    np.testing.assert_allclose(dV, g["dvm"], rtol=1e-10, atol=1e-16)
+    # rows at the table edges stay in bounds; out-of-table voltages raise the audit bit
+    assert b.audit() & cm.AUDIT_VRANGE == 0
+    b.calc(dt, np.full(n, 0.25), None)
+    assert b.audit() & cm.AUDIT_VRANGE
+
+
+def run_pair(cm, port, model, precision, n, steps, bcl, lo, hi, seed=1, rec=10):
+    dt = 1e-5
+    p = cm.Params(model, None, dt)
+    b = cm.Batch(p, n, precision)
+    sc = W.conductance_scales(seed, n, 3, lo, hi)
+    names = port.param_names(OM[model])
+    P = port.param_vector(OM[model], O.load_params(OM[model]))
+    het = {}
+    for k, name in enumerate(HET[model]):
+        het[name] = P[names.index(name)] * sc[k]
+        b.add_hetero_value(name, het[name])
+    vm = b.init_vm()
+    probes = np.arange(n)
+    tr = b.run(vm, steps, textbegin=0.0, textlen=TLEN[model], bcl=bcl, amplitude=AMP[model],
+               probe_cells=probes, probe_every=rec)
+    T = port.tables(OM[model], P, dt)
+    B = port.init_state(OM[model], P, n)
+    vo = np.full(n, port.init_vm(OM[model], P))
+    tro = port.run(OM[model], P, T, B, vo, steps, dt, textbegin=0.0, textlen=TLEN[model], bcl=bcl,
+                   amp=AMP[model], het=het, rec_every=rec, n_threads=8)
+    beats = [k * bcl for k in range(int(round(steps * dt / bcl)))]
+    u, a = A.beat_markers(tr, rec * dt, beats)
+    uo, ao = A.beat_markers(tro, rec * dt, beats)
+    return b, vm, vo, tr, tro, u, a, uo, ao, B
+
+
+@pytest.mark.parametrize("model", [5, 2])
+def test_trace_fp64(gpu, port, model):
+    b, vm, vo, tr, tro, u, a, uo, ao, B = run_pair(gpu, port, model, gpu.FP64, 64, 100000, 1.0, 0.95, 1.05)
+    assert np.all(np.isfinite(ao)) and np.all(ao > 0.15)
+    assert np.abs(tr - tro).max() <= 1e-8
+    assert np.abs(vm - vo).max() <= 1e-8
+    assert np.nanmax(np.abs(a - ao)) <= 1e-6
+    assert np.nanmax(np.abs(u - uo)) <= 1e-6
+    S = b.get_state(gpu.LAYOUT_REF_BLOCK)
+    cols = [c for c in ref_block_cols(model) if not (model == 5 and 5 <= c < 23) and not (model == 2 and c == 20)]
+    np.testing.assert_allclose(S[:, cols], B[:, cols], rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("model", [5, 2])
+def test_trace_mixed(gpu, port, model):
+    """Precision form: per-quantity error vs the FP64 oracle, 3 beats at BCL 800 ms, +-10%."""
+    b, vm, vo, tr, tro, u, a, uo, ao, B = run_pair(gpu, port, model, gpu.MIXED, 32, 240000, 0.8, 0.9, 1.1)
+    assert np.all(np.isfinite(ao))
+    assert np.nanmax(np.abs(a - ao)) <= 1e-3      # APD90 within 1 ms
+    assert np.nanmax(np.abs(u - uo)) <= 1e-4      # upstroke within 0.1 ms
+    rms = np.sqrt(((tr - tro) ** 2).mean(axis=1))
+    assert rms.max() <= 0.5e-3                    # RMS Vm error within 0.5 mV
+    S = b.get_state(gpu.LAYOUT_SOA)
+    ref_soa = B[:, [c for c in range(B.shape[1]) if (c < 5 or c >= 23)]].T if model == 5 else \
+        B[:, [c for c in range(22) if c != 20]].T
+    rel = np.abs(S - ref_soa) / np.maximum(np.abs(ref_soa), 1e-6)
+    assert rel.max() < 2e-2, rel.max(axis=1)
+
+
+def test_device_pointers_and_step_equals_run(gpu):
+    import torch
+    cm = gpu
+    p = cm.Params(5, None, 1e-5)
+    n = 1000
+    b1 = cm.Batch(p, n, cm.FP64)
+    b2 = cm.Batch(p, n, cm.FP64)
+    vm_host = b1.init_vm()
+    vm_dev = torch.tensor(vm_host, device="cuda")
+    b1.run(vm_host, 500, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=AMP[5])
+    # the same 500 steps through per-step Calc with caller-side stimulus and Vm update
+    t, tb = 0.0, 0.0
+    dv = torch.empty_like(vm_dev)
+    for s in range(500):
+        i = 0.0
+        if t >= tb:
+            i = AMP[5]
+            if t >= tb + 1e-3:
+                tb += 1.0
+        ie = torch.full_like(vm_dev, i)
+        b2.calc(1e-5, vm_dev, ie, None, dVm=dv)
+        vm_dev += dv
+        t += 1e-5
+    torch.cuda.synchronize()
+    assert np.array_equal(vm_dev.cpu().numpy(), vm_host)
+    assert np.array_equal(b1.get_state(), b2.get_state())
+
+
+def test_state_roundtrip_and_reset(gpu):
+    cm = gpu
+    for model in (5, 2):
+        p = cm.Params(model, None, 1e-5)
+        for prec in (cm.FP64, cm.MIXED):
+            b = cm.Batch(p, 300, prec)
+            s0 = b.get_state(cm.LAYOUT_REF_BLOCK)
+            vm = b.init_vm()
+            b.run(vm, 200, amplitude=AMP[model], textlen=TLEN[model])
+            s1 = b.get_state(cm.LAYOUT_REF_BLOCK)
+            assert not np.array_equal(s0, s1)
+            b.set_state(s0, cm.LAYOUT_REF_BLOCK)
+            if prec == cm.FP64:
+                assert np.array_equal(b.get_state(cm.LAYOUT_REF_BLOCK), s0)
+            b.set_state(s1, cm.LAYOUT_REF_BLOCK)
+            b.reset()
+            np.testing.assert_allclose(b.get_state(cm.LAYOUT_REF_BLOCK), s0, rtol=1e-7)
+
+
+def test_errors_and_audit(gpu):
+    cm = gpu
+    p = cm.Params(5, None, 1e-5)
+    b = cm.Batch(p, 64, cm.FP64)
+    vm = b.init_vm()
+    with pytest.raises(cm.CMError) as e:
+        b.calc(2e-5, vm)
+    assert e.value.code == -1
+    with pytest.raises(cm.CMError) as e:
+        b.add_hetero_value("g_pK", np.ones(64))
+    assert e.value.code == -7
+    with pytest.raises(cm.CMError) as e:
+        b.add_hetero_value("nonsense", np.ones(64))
+    assert e.value.code == -4
+    # NaN injected into one cell's state on the host: the fused run reports it, per cell
+    s = b.get_state()
+    s[3, 17] = np.nan  # K_i of cell 17
+    b.set_state(s)
+    with pytest.raises(cm.CMError) as e:
+        b.run(vm, 10, amplitude=AMP[5])
+    assert e.value.code == -8
+    m, per = b.audit(per_cell=True)
+    assert m & cm.AUDIT_NAN and per[17] & cm.AUDIT_NAN and per[16] == 0
+    assert b.audit() == 0
+
+
+def test_full_size_determinism_mixed(gpu):
+    """4,194,304 cells (2048 x 2048 sheet), 200 steps twice from reset: bitwise identical,
+    finite, and cells with equal conductances end equal (a size-independent property)."""
+    import torch
+    cm = gpu
+    n = 2048 * 2048
+    p = cm.Params(5, None, 1e-5)
+    b = cm.Batch(p, n, cm.MIXED)
+    sc = W.conductance_scales(2, n, 3, 0.9, 1.1)
+    sc[:, 1::2] = 1.0
+    for k, name in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(name, p.get(name) * sc[k])
+    outs = []
+    for rep in range(2):
+        b.reset()
+        vm = torch.tensor(b.init_vm(), device="cuda")
+        b.run(vm, 200, textlen=1e-3, amplitude=AMP[5])
+        outs.append(vm.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.all(np.isfinite(outs[0]))
+    odd = outs[0][1::2]
+    assert np.all(odd == odd[0])
+    assert b.audit() == 0
