@@ -135,53 +135,76 @@ def time_device_steps(torch, cm, b, stream, vm, steps, warmup, t0):
     return ev0.elapsed_time(ev1) / 1e3
 
 
-def cpu_baseline(seconds=10.0, threads=None, cells=4096):
-    """The oracle on host cores: `cells` cells of the same workload, stepped in chunks until
-    about `seconds` of wall time; returns cell-steps/s."""
-    import oracle as O
-    from cardiomechanics_gb300 import workloads as W
-    port = O.Port()
-    threads = threads or os.cpu_count() or 1
-    P = port.param_vector(O.TT2, O.load_params(O.TT2))
-    T = port.tables(O.TT2, P, DT)
-    sc = W.conductance_scales(2, N_CELLS, 3, 0.9, 1.1, cells=np.arange(cells))
-    names = port.param_names(O.TT2)
-    het = {k: P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
-    B = port.init_state(O.TT2, P, cells)
-    vm = np.full(cells, port.init_vm(O.TT2, P))
-    chunk, done, t = 500, 0, 0.0
-    start = time.perf_counter()
-    while time.perf_counter() - start < seconds:
-        port.run(O.TT2, P, T, B, vm, chunk, DT, t0=t, textbegin=0.0, textlen=1e-3, bcl=BCL, amp=W.TT2_STIM_NA,
-                 het=het, n_threads=threads)
-        done += chunk
-        t += chunk * DT
-    el = time.perf_counter() - start
-    return {"value": cells * done / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{cells} cells x {done} steps of the same workload (oracle C restatement, "
-                      f"{threads} threads, {el:.1f} s)"}
+class CPUSample:
+    """The oracle (C restatement of the reference Calc) on a bounded sample of the workload:
+    the first `cells` cells, advanced `steps` time steps per call, all host threads."""
+
+    def __init__(self, cells=4096, threads=None):
+        import oracle as O
+        from cardiomechanics_gb300 import workloads as W
+        self.O, self.W = O, W
+        self.port = O.Port()
+        self.threads = threads or os.cpu_count() or 1
+        self.cells = cells
+        self.P = self.port.param_vector(O.TT2, O.load_params(O.TT2))
+        self.T = self.port.tables(O.TT2, self.P, DT)
+        sc = W.conductance_scales(2, N_CELLS, 3, 0.9, 1.1, cells=np.arange(cells))
+        names = self.port.param_names(O.TT2)
+        self.het = {k: self.P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
+        self.B = self.port.init_state(O.TT2, self.P, cells)
+        self.vm = np.full(cells, self.port.init_vm(O.TT2, self.P))
+        self.t = 0.0
+
+    def advance(self, steps):
+        """Advance the sample; returns elapsed seconds."""
+        t0 = time.perf_counter()
+        self.port.run(self.O.TT2, self.P, self.T, self.B, self.vm, steps, DT, t0=self.t, textbegin=0.0,
+                      textlen=1e-3, bcl=BCL, amp=self.W.TT2_STIM_NA, het=self.het, n_threads=self.threads)
+        self.t += steps * DT
+        return time.perf_counter() - t0
+
+    def describe(self, steps, seconds):
+        return {"unit": UNIT, "cores": self.threads, "kind": "port",
+                "sample": f"first {self.cells} of the {N_CELLS} cells x {steps} steps (oracle C restatement "
+                          f"of the reference Calc, {self.threads} threads, {seconds:.1f} s)"}
+
+
+def cpu_baseline(seconds=10.0, cells=4096):
+    """Oracle throughput on the host cores over about `seconds` of work; cell-steps/s."""
+    smp = CPUSample(cells)
+    done, el = 0, 0.0
+    while el < seconds:
+        el += smp.advance(500)
+        done += 500
+    d = smp.describe(done, el)
+    d["value"] = cells * done / el
+    return d
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU path (the oracle port of its Calc; the reference
+    sources are not on the GPU host) on all host cores. Each step advances the cell sample by a
+    chunk sized so that warmup + steps take about a minute and a half in total."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle as O
     O.build_port()
-    threads = os.cpu_count() or 1
-    samples = []
+    smp = CPUSample(4096)
+    rate = smp.cells * 200 / smp.advance(200)  # calibration
+    total = args.steps + args.warmup
+    chunk = int(max(1, min(5000, rate * 90.0 / max(1, total) / smp.cells)))
     for _ in range(args.warmup):
-        cpu_baseline(seconds=1.0, threads=threads)
-    for _ in range(args.steps):
-        samples.append(cpu_baseline(seconds=max(2.0, 20.0 / max(1, args.steps)), threads=threads))
-    v = float(np.median([s["value"] for s in samples]))
-    cb = dict(samples[-1])
+        smp.advance(chunk)
+    times = [smp.advance(chunk) for _ in range(args.steps)]
+    v = float(np.median([smp.cells * chunk / t for t in times]))
+    cb = smp.describe(chunk * args.steps, float(sum(times)))
     cb["value"] = v
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N_CELLS / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": N_CELLS, "dt_ms": DT * 1e3, "bcl_ms": BCL * 1e3,
-                       "note": "CPU: the oracle restatement of the reference Calc on a bounded cell sample"},
+                       "note": f"CPU: each step advances a {smp.cells}-cell sample {chunk} time steps"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -196,6 +219,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "mixed", "fp64", "e2e"],
+                    help="run one leg only (for profiler captures); the JSON line is printed for 'all'")
+    ap.add_argument("--tune-steps", type=int, default=10)
+    ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -212,8 +239,19 @@ def main():
     stream = torch.cuda.Stream()
     hbm_peak, peak_kind = peaks()
 
+    if args.only == "fp64":
+        _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
+        vm64 = torch.tensor(b64.init_vm(), device="cuda")
+        time_device_steps(torch, cm, b64, stream, vm64, args.fp64_steps, 3, 0.0)
+        return
     # ---- device-resident mixed form (the headline `value`)
     p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
+    if args.launch:
+        v, g = (int(x) for x in args.launch.split(","))
+        b.set_launch(v, g)
+        tuned, tuned_ms = v * 100 + g, None
+    else:
+        tuned, tuned_ms = b.autotune(args.tune_steps)
     vm = torch.tensor(b.init_vm(), device="cuda")
     b.run(vm, args.warmup, textbegin=0.0, textlen=1e-3, bcl=BCL, amplitude=cm_stim())
     torch.cuda.synchronize()
@@ -235,10 +273,14 @@ def main():
     value = world * N_CELLS * args.steps / sec
     audit = b.audit()
     ms_kernel = 1e3 * sec / args.steps
+    if args.only == "mixed":
+        return
     achieved = MIXED_BYTES_PER_CELL_STEP * N_CELLS / (ms_kernel / 1e3) / 1e9
     del b
     torch.cuda.empty_cache()
 
+    fp64_peak = cm.fma_peak_tflops(True, stream.cuda_stream)
+    fp32_peak = cm.fma_peak_tflops(False, stream.cuda_stream)
     # ---- plain FP64 kernel on the same workload
     _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
     vm64 = torch.tensor(b64.init_vm(), device="cuda")
@@ -286,7 +328,10 @@ def main():
                        "l2": "state 430 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas{world}"},
             "plain_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
                            "bytes_per_cell_step": FP64_BYTES_PER_CELL_STEP,
-                           "achieved_gbs": FP64_BYTES_PER_CELL_STEP * N_CELLS / (fp64_ms / 1e3) / 1e9},
+                           "achieved_gbs": FP64_BYTES_PER_CELL_STEP * N_CELLS / (fp64_ms / 1e3) / 1e9,
+                           "bound": "fp64 pipe", "fp64_fma_peak_tflops_measured": fp64_peak},
+            "fp32_fma_peak_tflops_measured": fp32_peak,
+            "autotune": {"choice": tuned, "ms_per_step": tuned_ms},
             "speedup_vs_plain_fp64": value / fp64_value,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * N_CELLS,
                     "d2h_bytes_per_step": 8 * N_CELLS, "steps": args.e2e_steps,

@@ -41,6 +41,7 @@ ABI_SYMBOLS = (
     "cm_params_table", "cm_batch_create", "cm_batch_destroy", "cm_batch_info", "cm_batch_reset",
     "cm_batch_set_hetero", "cm_batch_set_diagnostics", "cm_batch_init_vm", "cm_batch_get_state",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
+    "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak",
 )
 
 
@@ -97,6 +98,9 @@ def lib() -> ctypes.CDLL:
     L.cm_batch_step_update.argtypes = [vp, ctypes.c_double, vp, vp, vp, ctypes.c_double]
     L.cm_batch_run.argtypes = [vp, vp, i64, ctypes.POINTER(Stimulus), vp, i64, i64, vp]
     L.cm_batch_audit.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
+    L.cm_batch_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.cm_batch_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.cm_diag_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
     _lib = L
     return L
 
@@ -126,6 +130,13 @@ def _f64(a, n, name):
     if a.dtype != torch.float64 or not a.is_contiguous() or a.numel() != n:
         raise ValueError(f"{name}: need a contiguous float64 tensor of {n} elements")
     return a
+
+
+def fma_peak_tflops(fp64: bool, stream=None) -> float:
+    """Measured dense FMA rate of the current GPU (TFLOP/s), FP64 or FP32."""
+    v = ctypes.c_double()
+    _check(lib().cm_diag_fma_peak(int(fp64), ctypes.byref(v), None if stream is None else ctypes.c_void_p(int(stream))))
+    return v.value
 
 
 def model_info(model: int) -> Info:
@@ -262,6 +273,16 @@ class Batch:
         _check(lib().cm_batch_run(self._h, _ptr(Vm), int(n_steps), ctypes.byref(st), _ptr(pc), n_probe,
                                   int(probe_every), _ptr(trace)))
         return trace
+
+    def autotune(self, n_trial_steps: int = 20):
+        """Pick the fastest launch shape on this batch; returns (variant*100 + grid_mode, ms/step)."""
+        v = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(lib().cm_batch_autotune(self._h, n_trial_steps, ctypes.byref(v), ctypes.byref(ms)))
+        return v.value, ms.value
+
+    def set_launch(self, variant: int, grid_mode: int = 0) -> None:
+        _check(lib().cm_batch_set_launch(self._h, variant, grid_mode))
 
     def audit(self, per_cell: bool = False):
         m = ctypes.c_uint32()

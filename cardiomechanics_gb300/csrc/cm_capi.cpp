@@ -531,7 +531,7 @@ int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext
   } else {
     io.dvm = dVm;
   }
-  CK(launch_step(b->d, io, 0, 0, b->stream));
+  CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
   if (host_out) {
     CK(cudaMemcpyAsync(dVm, io.dvm, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
@@ -556,7 +556,7 @@ int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ex
   io.vm_range = vm_range;
   if ((rc = stage_in(b, i_ext, 1, &io.iext))) return rc;
   if ((rc = stage_in(b, stretch, 2, &io.stretch))) return rc;
-  CK(launch_step(b->d, io, 0, 0, b->stream));
+  CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
   if (host_vm) CK(cudaMemcpyAsync(Vm, io.vm_out, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   unsigned int mask = 0;
   CK(cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
@@ -633,7 +633,7 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
       }
       io.iext_uniform = i_ext;
     }
-    CK(launch_step(b->d, io, 0, 0, b->stream));
+    CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
     t += b->ps.dt;
   }
   if (host_vm) CK(cudaMemcpyAsync(Vm, dvm, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
@@ -646,6 +646,84 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   CK(cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
   CK(cudaStreamSynchronize(b->stream));
   if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+int cm_batch_set_launch(cm_batch_t b, int variant, int grid_mode) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (variant < 0 || variant >= n_shape_variants() || grid_mode < 0 || grid_mode > 64)
+    return fail(CM_ERR_ARG, "launch shape out of range");
+  b->d.variant = variant;
+  b->d.grid_mode = grid_mode;
+  return CM_OK;
+}
+
+int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_per_step) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (n_trial_steps < 1) n_trial_steps = 1;
+  const int64_t n = b->d.n;
+  if (n == 0 || b->d.precision == CM_PREC_FP64) {
+    if (variant) *variant = 0;
+    if (ms_per_step) *ms_per_step = 0;
+    return CM_OK;
+  }
+  const size_t n64 = (size_t)n_fp64_vars(b->d.model, b->d.precision) * b->d.ld;
+  const size_t n32 = (size_t)n_fp32_vars(b->d.model) * b->d.ld;
+  const size_t bytes = n64 * sizeof(double) + n32 * sizeof(float);
+  void *saved = nullptr;
+  double *vm = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = CM_OK;
+  float best = 1e30f;
+  int best_v = 0, best_g = 0;
+  unsigned int audit_saved = 0;
+  std::vector<double> v0(n, b->ps.init_vm());
+  cudaError_t e = cudaMalloc(&saved, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&vm, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(saved, b->state_mem, bytes, cudaMemcpyDeviceToDevice, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&audit_saved, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(vm, v0.data(), n * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  const int grid_modes[] = {0, 2, 4, 8};
+  for (int v = 0; e == cudaSuccess && v < n_shape_variants(); v++) {
+    for (int g : grid_modes) {
+      DevBatch d = b->d;
+      d.variant = v;
+      d.grid_mode = g;
+      StepIO io;
+      io.vm = vm;
+      io.vm_out = vm;
+      for (int k = 0; k < 2 && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+      for (int k = 0; k < n_trial_steps && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e == cudaSuccess && ms < best) {
+        best = ms;
+        best_v = v;
+        best_g = g;
+      }
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->state_mem, saved, bytes, cudaMemcpyDeviceToDevice, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->audit_or, &audit_saved, sizeof(unsigned int), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) rc = cuda_fail(e, "autotune");
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(saved);
+  cudaFree(vm);
+  if (rc) return rc;
+  b->d.variant = best_v;
+  b->d.grid_mode = best_g;
+  if (variant) *variant = best_v * 100 + best_g;
+  if (ms_per_step) *ms_per_step = best / n_trial_steps;
   return CM_OK;
 }
 

@@ -64,6 +64,7 @@ struct TT2Consts {
   R Bufsr, Kbufsr, Bufss, Kbufss, Bufc, Kbufc, BufcPKbufc;
   R VcVss, VsrVss, inversevssF2, inverseviF, inverseviF2, invVcdVsr;
   R dt, dt1000, inv_stim_unit;  // inv_stim_unit = 1 / 2.29656e-2 (nA -> pA/pF, line 630)
+  R logKo, logNao, logKoNao;    // log K_o, log Na_o, log(K_o + pKNa Na_o) (mixed form)
 };
 
 // Constants of Courtemanche::Calc (CourtemancheEtAl.cpp:85-187).
@@ -74,6 +75,7 @@ struct CRNConsts {
       beta1, k_TRPN, n_TRPN, VreldVup, csqnkm, kmcsqnm2, kkmcsqn, CmdFvi, VupdVi, VreldVi, TRPNmax,
       cmdnkm, kmcmdnm2, kkmcmdn, Vrel, Cmd2F, exp250, exp50;
   R dt_ms;  // tinc * 1000 (line 87)
+  R logNao, logKo, logCao;  // mixed form
 };
 
 // Voltage row index exactly as the reference computes it (TenTusscher2.cpp:618,
@@ -99,19 +101,50 @@ CM_HD int vrow_fp32(float vmv, uint32_t &audit) {
   return vi;
 }
 
+// FP32 helpers of the mixed form. On the device they map to the SFU (MUFU.EX2/LG2/RCP/RSQ)
+// with one or two FMA-pipe instructions around them instead of the ~10-20 instruction
+// IEEE-exact library sequences; their relative errors (~1e-7 .. 1e-6) are far below the
+// mixed form's tolerance, which the parity tests check against the FP64 oracle.
+CM_HD float fexp(float x) {
+#ifdef __CUDA_ARCH__
+  return __expf(x);
+#else
+  return expf(x);
+#endif
+}
+CM_HD float flog(float x) {
+#ifdef __CUDA_ARCH__
+  return __logf(x);
+#else
+  return logf(x);
+#endif
+}
+CM_HD float fdiv(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+CM_HD float fsqrt(float x) {
+#ifdef __CUDA_ARCH__
+  return x > 0.f ? x * rsqrtf(x) : 0.f;
+#else
+  return x > 0.f ? sqrtf(x) : 0.f;
+#endif
+}
+
 // New free concentration increment of a rapidly buffered species. The reference solves
 // x^2 + b x - c = 0 for the new free value x given total = x_old + B x_old/(x_old+K) + dT
 // (TenTusscher2.cpp:814-836). Writing x = x_old + d, the same conservation law gives
 //   a d^2 + (a^2 + B K - dT a) d - dT a^2 = 0,  a = x_old + K,
 // whose root is taken in the form without cancellation. Used by the mixed form in FP32,
 // where the reference form loses most digits of d (sqrt(b^2+4c) - b with b >> d).
-template <typename R>
-CM_HD R buffered_increment(R x, R dT, R B, R K) {
-  const R a = x + K;
-  const R Bq = a * a + B * K - dT * a;
-  const R disc = Bq * Bq + R(4) * a * a * a * dT;
-  const R s = sqrt(disc > R(0) ? disc : R(0));
-  return Bq > R(0) ? (R(2) * dT * a * a) / (Bq + s) : (s - Bq) / (R(2) * a);
+CM_HD float buffered_increment(float x, float dT, float B, float K) {
+  const float a = x + K;
+  const float Bq = a * a + B * K - dT * a;
+  const float s = fsqrt(Bq * Bq + 4.f * a * a * a * dT);
+  return Bq > 0.f ? fdiv(2.f * dT * a * a, Bq + s) : fdiv(s - Bq, 2.f * a);
 }
 
 }  // namespace cm

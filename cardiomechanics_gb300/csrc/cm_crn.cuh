@@ -102,10 +102,10 @@ CM_HD float crn_calc_mixed(const CRNConsts<float> &C, const float *__restrict__ 
   const float tinc = C.dt_ms;
   const float V_int = V * 1000.f;
   const float Na_i = (float)Na_i_d, K_i = (float)K_i_d, Ca_up = (float)Ca_up_d, Ca_rel = (float)Ca_rel_d;
-  const float dNa_i = 1.f / Na_i;
-  const float VmE_Na = V_int - C.RTdF * logf(C.Na_o * dNa_i);
-  const float VmE_K = V_int - C.RTdF * logf(C.K_o / K_i);
-  const float VmE_Ca = V_int - C.RTd2F * logf(C.Ca_o / c.Ca_i);
+  const float dNa_i = fdiv(1.f, Na_i);
+  const float VmE_Na = V_int - C.RTdF * (C.logNao - flog(Na_i));
+  const float VmE_K = V_int - C.RTdF * (C.logKo - flog(K_i));
+  const float VmE_Ca = V_int - C.RTd2F * (C.logCao - flog(c.Ca_i));
   c.m = clamp01(row[CR_m_m] + (c.m - row[CR_m_m]) * row[CR_exptau_m]);
   c.h = row[CR_m_h] + (c.h - row[CR_m_h]) * row[CR_exptau_h];
   c.j = row[CR_m_j] + (c.j - row[CR_m_j]) * row[CR_exptau_j];
@@ -117,7 +117,7 @@ CM_HD float crn_calc_mixed(const CRNConsts<float> &C, const float *__restrict__ 
   c.Xs = row[CR_m_Xs] + (c.Xs - row[CR_m_Xs]) * row[CR_exptau_Xs];
   c.d = row[CR_m_d] + (c.d - row[CR_m_d]) * row[CR_exptau_d];
   c.f = row[CR_m_f] + (c.f - row[CR_m_f]) * row[CR_exptau_f];
-  c.f_Ca += (1.f / (1.f + c.Ca_i * 2857.1429f) - c.f_Ca) * 0.5f * tinc;
+  c.f_Ca += (fdiv(1.f, 1.f + c.Ca_i * 2857.1429f) - c.f_Ca) * 0.5f * tinc;
   c.w = row[CR_m_w] + (c.w - row[CR_m_w]) * row[CR_exptau_w];
 
   const float I_Na = g.g_Na * c.m * c.m * c.m * c.h * c.j * VmE_Na;
@@ -130,33 +130,33 @@ CM_HD float crn_calc_mixed(const CRNConsts<float> &C, const float *__restrict__ 
   const float I_bNa = g.g_bNa * VmE_Na;
   const float I_bCa = g.g_bCa * VmE_Ca;
   const float temp = C.k_mNai * dNa_i;
-  const float I_NaK = row[CR_CNaK] / (1.f + temp * sqrtf(temp));
-  const float I_pCa = C.I_pCamax * c.Ca_i / (c.Ca_i + C.k_mpCa);
+  const float I_NaK = fdiv(row[CR_CNaK], 1.f + temp * fsqrt(temp));
+  const float I_pCa = fdiv(C.I_pCamax * c.Ca_i, c.Ca_i + C.k_mpCa);
   const float I_NaCa = row[CR_CNaCa] * ((Na_i * Na_i * Na_i * C.Ca_o) - row[CR_expVm] * c.Ca_i);
   const float I_rel = C.k_rel * c.u * c.u * c.v * c.w * (Ca_rel - c.Ca_i);
-  const float I_up = C.I_upmax * c.Ca_i / (c.Ca_i + C.k_up);
+  const float I_up = fdiv(C.I_upmax * c.Ca_i, c.Ca_i + C.k_up);
   const float I_upleak = C.kupleak * Ca_up;
   const float I_tr = (Ca_up - Ca_rel) * C.dt_tr;
-  const float I_SAC = C.ISAC_SWITCH * (C.G_sac * (V_int - C.E_sac) / (1.f + C.K_sac * expf(-C.alpha * (stretch - 1.f))));
+  const float I_SAC = C.ISAC_SWITCH * fdiv(C.G_sac * (V_int - C.E_sac), 1.f + C.K_sac * fexp(-C.alpha * (stretch - 1.f)));
   const float Ca_T50 = C.Ca_T50 + C.beta1 * ((stretch < 1.2f ? stretch : 1.2f) - 1.f);
-  const float x = 1000.f * c.Ca_i / Ca_T50;
+  const float x = fdiv(1000.f * c.Ca_i, Ca_T50);
   const float px = C.n_TRPN == 2.f ? x * x : powf(x, C.n_TRPN);
   const float dCaTRPN = C.k_TRPN * (px * (1.f - c.Ca_TRPN) - c.Ca_TRPN);
   c.Ca_TRPN += tinc * dCaTRPN;
   Ca_up_d += (double)(tinc * (I_up - I_tr * C.VreldVup - I_upleak));
-  Ca_rel_d += (double)(tinc * ((I_tr - I_rel) / (1.f + C.csqnkm / (Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn))));
+  Ca_rel_d += (double)(tinc * fdiv((I_tr - I_rel) * (Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn), Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn + C.csqnkm));
   Na_i_d += (double)(tinc * (-3.f * I_NaK - 3.f * I_NaCa - I_bNa - I_Na) * C.CmdFvi);
   K_i_d += (double)(tinc * (2.f * I_NaK - I_K1 - I_to - I_Kur - I_Kr - I_Ks) * C.CmdFvi);
   float B1 = ((2.f * I_NaCa - I_pCa - I_CaL - I_bCa) * .5f * C.CmdFvi) + ((I_upleak - I_up) * C.VupdVi + I_rel * C.VreldVi);
   B1 -= C.TRPNmax * dCaTRPN;
-  const float B2 = 1.f + (C.cmdnkm / ((c.Ca_i * c.Ca_i) + (c.Ca_i * C.kmcmdnm2) + C.kkmcmdn));
-  c.Ca_i += tinc * (B1 / B2);
+  const float q = (c.Ca_i * c.Ca_i) + (c.Ca_i * C.kmcmdnm2) + C.kkmcmdn;
+  c.Ca_i += tinc * fdiv(B1 * q, q + C.cmdnkm);  // B1 / (1 + cmdnkm/q)
   const float arg = -(C.Vrel * I_rel - (0.5f * I_CaL - 0.2f * I_NaCa) * C.Cmd2F) * 731.5289f;
-  const float m_u = 1.f / (1.f + expf(arg + 250.f));
+  const float m_u = fdiv(1.f, 1.f + fexp(arg + 250.f));
   c.u += (m_u - c.u) * 0.125f * tinc;
-  const float m_v = 1.f - 1.f / (1.f + expf(arg + 169.5f));
+  const float m_v = 1.f - fdiv(1.f, 1.f + fexp(arg + 169.5f));
   const float t_v = 1.91f + 2.09f * m_u;
-  c.v += (m_v - c.v) * tinc / t_v;
+  c.v += fdiv((m_v - c.v) * tinc, t_v);
   const float I_tot =
       I_Na + I_CaL + I_pCa + I_K1 + I_to + I_Kur + I_Kr + I_Ks + I_bNa + I_bCa + I_NaK + I_NaCa + I_SAC - i_external;
   (void)audit;

@@ -83,10 +83,11 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
   }
 }
 
-__global__ void __launch_bounds__(256) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
-  const int64_t ld = b.ld;
+template <typename I, int kBlock, int kMinB>
+__global__ void __launch_bounds__(kBlock, kMinB) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
+  const I ld = (I)b.ld;
   const float *const *het = (const float *const *)b.het;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+  for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
     float *s = b.s32 + c;
     double *a = b.s64 + c;
     TT2Cell<float> x;
@@ -156,10 +157,11 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
   }
 }
 
-__global__ void __launch_bounds__(256) crn_mixed_kernel(const DevBatch b, const StepIO io) {
-  const int64_t ld = b.ld;
+template <typename I, int kBlock, int kMinB>
+__global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch b, const StepIO io) {
+  const I ld = (I)b.ld;
   const float *const *het = (const float *const *)b.het;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+  for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
     float *s = b.s32 + c;
     double *a = b.s64 + c;
     CRNCell<float> x;
@@ -212,30 +214,61 @@ int sm_count() {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_step(const DevBatch &b, const StepIO &io, int block, int grid, cudaStream_t s) {
+// Launch shapes of the mixed kernels the autotuner chooses from: (threads per block,
+// minimum resident blocks per SM as a register-allocation hint).
+namespace {
+struct Shape {
+  int block, minb;
+};
+constexpr Shape kShapes[] = {{256, 1}, {256, 3}, {128, 6}, {512, 1}, {128, 1}};
+
+template <typename I, int B, int M>
+void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s) {
+  if (b.model == 5) tt2_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
+  else crn_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
+}
+
+template <typename I>
+void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, cudaStream_t s) {
+  switch (v) {
+    case 1: launch_mixed<I, 256, 3>(b, io, grid, s); break;
+    case 2: launch_mixed<I, 128, 6>(b, io, grid, s); break;
+    case 3: launch_mixed<I, 512, 1>(b, io, grid, s); break;
+    case 4: launch_mixed<I, 128, 1>(b, io, grid, s); break;
+    default: launch_mixed<I, 256, 1>(b, io, grid, s); break;
+  }
+}
+}  // namespace
+
+int n_shape_variants() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
+
+cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s) {
   if (b.n == 0) return cudaSuccess;
   const bool diag = b.diag != nullptr;
-  if (block <= 0) block = b.precision == 0 ? 128 : 256;
-  if (grid <= 0) {
+  // 32-bit offsets when every state index fits (ld * variables < 2^31)
+  const bool small = b.ld * 24 < (int64_t)2147483647;
+  if (b.precision == 0) {
+    const int block = 128;
     const int64_t need = (b.n + block - 1) / block;
-    const int64_t cap = (int64_t)sm_count() * (b.precision == 0 ? 16 : 8);
-    grid = (int)(need < cap ? need : cap);
-  }
-  if (b.model == 5) {
-    if (b.precision == 0) {
+    const int64_t cap = (int64_t)sm_count() * 16;
+    const int grid = (int)(need < cap ? need : cap);
+    if (b.model == 5) {
       if (diag) tt2_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
       else tt2_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
     } else {
-      tt2_mixed_kernel<<<grid, block, 0, s>>>(b, io);
-    }
-  } else {
-    if (b.precision == 0) {
       if (diag) crn_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
       else crn_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
-    } else {
-      crn_mixed_kernel<<<grid, block, 0, s>>>(b, io);
     }
+    return cudaGetLastError();
   }
+  if (variant < 0 || variant >= n_shape_variants()) variant = 0;
+  const Shape sh = kShapes[variant];
+  const int64_t need = (b.n + sh.block - 1) / sh.block;
+  // grid_mode 0: one thread per cell; k > 0: grid-stride over k blocks per SM
+  const int64_t cap = grid_mode > 0 ? (int64_t)sm_count() * grid_mode : need;
+  const int grid = (int)(need < cap ? need : cap);
+  if (small) launch_mixed_variant<int>(b, io, variant, grid, s);
+  else launch_mixed_variant<int64_t>(b, io, variant, grid, s);
   return cudaGetLastError();
 }
 

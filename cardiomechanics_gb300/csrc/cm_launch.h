@@ -27,6 +27,7 @@ struct DevBatch {
   uint32_t *audit_cell = nullptr;
   unsigned int *audit_or = nullptr;
   double *diag = nullptr;  // TT2 FP64: 17 x ld diagnostic currents; CRN FP64: 1 x ld (I_SAC)
+  int variant = 0, grid_mode = 0;  // launch shape chosen by cm_batch_autotune
   TT2Consts<double> tt2_64;
   TT2Consts<float> tt2_32;
   CRNConsts<double> crn_64;
@@ -50,7 +51,10 @@ struct StepIO {
 int n_fp32_vars(int model);
 int n_fp64_vars(int model, int precision);
 
-cudaError_t launch_step(const DevBatch &b, const StepIO &io, int block, int grid, cudaStream_t s);
+// variant: mixed-kernel launch shape (0 .. n_shape_variants()-1); grid_mode 0 = one thread
+// per cell, k > 0 = grid-stride loop over k blocks per SM.
+cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s);
+int n_shape_variants();
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.
 cudaError_t launch_probe(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
                          int64_t k, cudaStream_t s);

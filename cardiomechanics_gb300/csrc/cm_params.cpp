@@ -543,6 +543,9 @@ void ParamSet::tt2_consts(TT2Consts<double> &d, TT2Consts<float> &f) const {
   d.dt = dt;
   d.dt1000 = dt * 1000.0;
   d.inv_stim_unit = 1.0 / 2.29656e-2;
+  d.logKo = log(PV(K_o));
+  d.logNao = log(PV(Na_o));
+  d.logKoNao = log(PV(K_o) + PV(pKNa) * PV(Na_o));
   // FP32 copy, field by field
   const double *src = &d.RTONF;
   float *dst = &f.RTONF;
@@ -596,6 +599,9 @@ void ParamSet::crn_consts(CRNConsts<double> &d, CRNConsts<float> &f) const {
   d.exp250 = exp250;
   d.exp50 = exp50;
   d.dt_ms = dt * 1000.0;
+  d.logNao = log(PV(Na_o));
+  d.logKo = log(PV(K_o));
+  d.logCao = log(PV(Ca_o));
   const double *src = &d.RTdF;
   float *dst = &f.RTdF;
   const int nf = (int)(sizeof(CRNConsts<double>) / sizeof(double));

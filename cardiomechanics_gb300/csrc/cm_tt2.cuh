@@ -126,8 +126,9 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
 // Mixed form: the same update with gates, currents and the fast Ca pools in FP32. Vm, Na_i,
 // K_i and CaSR are accumulated in FP64 (their per-step increments are 1e-7..1e-9 of their
 // values and vanish in FP32); the three buffered-Ca updates use buffered_increment, which is
-// the reference's quadratic rewritten without cancellation. Transcendentals are the FP32
-// library functions. row/eca are the FP32 copies of the FP64 tables.
+// the reference's quadratic rewritten without cancellation. Reversal potentials use
+// log(a/b) = log a - log b with the constant logs precomputed; fractions that share a
+// denominator are combined. row/eca are the FP32 copies of the FP64 tables.
 CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ row, const float *__restrict__ eca,
                            TT2Cell<float> &c, double &CaSR_d, double &Na_i_d, double &K_i_d,
                            const TT2Het_<float> &g, float V, float i_external, uint32_t &audit) {
@@ -139,18 +140,18 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
     Caitab = Caitab < 0 ? 0 : kRows - 1;
   }
   const float Na_i = (float)Na_i_d, K_i = (float)K_i_d, CaSR = (float)CaSR_d;
-  const float EK = C.RTONF * logf(C.K_o / K_i);
-  const float VminEK = svolt - EK;
-  const float ENa = C.RTONF * logf(C.Na_o / Na_i);
-  const float VminENa = svolt - ENa;
-  const float EKs = C.RTONF * logf((C.K_o + C.pKNaNao) / (K_i + C.pKNa * Na_i));
-  const float e1 = expf(0.06f * (VminEK - 200.f));
-  const float e2 = expf(0.0002f * (VminEK + 100.f));
-  const float e3 = expf(0.1f * (VminEK - 10.f));
-  const float e4 = expf(-0.5f * VminEK);
+  const float logKi = flog(K_i);
+  const float VminEK = svolt - C.RTONF * (C.logKo - logKi);
+  const float VminENa = svolt - C.RTONF * (C.logNao - flog(Na_i));
+  const float EKs = C.RTONF * (C.logKoNao - flog(K_i + C.pKNa * Na_i));
+  const float e1 = fexp(0.06f * (VminEK - 200.f));
+  const float e2 = fexp(0.0002f * (VminEK + 100.f));
+  const float e3 = fexp(0.1f * (VminEK - 10.f));
+  const float e4 = fexp(-0.5f * VminEK);
   // rec_iK1 = AK1/(AK1+BK1) with AK1 = 0.1/(1+e1), BK1 = (3 e2 + e3)/(1+e4), one division
-  const float rec_iK1 = 0.1f * (1.f + e4) / (0.1f * (1.f + e4) + (3.f * e2 + e3) * (1.f + e1));
-  const float I_pCa = C.g_pCa * c.Ca_i / (C.KpCa + c.Ca_i);
+  const float a1 = 0.1f * (1.f + e4);
+  const float rec_iK1 = fdiv(a1, a1 + (3.f * e2 + e3) * (1.f + e1));
+  const float I_pCa = fdiv(C.g_pCa * c.Ca_i, C.KpCa + c.Ca_i);
   const float I_pK = row[T2_rec_ipK] * VminEK;
   const float I_to = g.g_to * c.r * c.s * VminEK;
   const float I_Kr = g.g_Kr * C.sqrtKo54 * c.xr1 * c.xr2 * VminEK;
@@ -162,22 +163,24 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
   const float I_Na = g.g_Na * c.m * c.m * c.m * c.h * c.j * VminENa;
   const float I_CaL = g.g_CaL * c.d * c.f * c.f2 * c.fCa * ((row[T2_CaL_P1] * c.CaSS) - row[T2_CaL_P2]);
   const float I_NaCa = C.kNaCa * (row[T2_NaCa_P1] * Na_i * Na_i * Na_i - row[T2_NaCa_P2] * c.Ca_i);
-  const float I_NaK = C.knak * C.KoKmK * (Na_i / (Na_i + C.KmNa)) * row[T2_NaK_P1];
+  const float I_NaK = C.knak * C.KoKmK * fdiv(Na_i, Na_i + C.KmNa) * row[T2_NaK_P1];
   const float I_tot = I_K + I_K1 + I_to + I_Na + I_bNa + I_CaL + I_bCa + I_NaK + I_NaCa + I_pCa + I_pK - i_external;
 
   const float Caisquare = c.Ca_i * c.Ca_i;
   const float CaSSsquare = c.CaSS * c.CaSS;
-  const float ECaSR = C.EC / CaSR;
-  const float kCaSR = C.max_sr - ((C.max_sr - C.min_sr) / (1.f + ECaSR * ECaSR));
+  const float CaSR2 = CaSR * CaSR;
+  // kCaSR = max_sr - (max_sr - min_sr) / (1 + (EC/CaSR)^2)
+  const float kCaSR = C.max_sr - fdiv((C.max_sr - C.min_sr) * CaSR2, CaSR2 + C.EC * C.EC);
   const float k2 = C.ks2 * kCaSR;
-  const float k1 = C.ks1 / kCaSR;
+  const float k1 = fdiv(C.ks1, kCaSR);
   const float dRq = 1000.f * ((-k2 * c.CaSS * c.Rq) + (C.k4 * (1.f - c.Rq)));
   c.Rq += C.dt * dRq;
-  const float O = k1 * CaSSsquare * c.Rq / (C.k3 + k1 * CaSSsquare);
+  const float k1C2 = k1 * CaSSsquare;
+  const float O = fdiv(k1C2 * c.Rq, C.k3 + k1C2);
   const float I_rel = C.Vrel * O * (CaSR - c.CaSS);
   const float I_leak = 0.00036f * (CaSR - c.Ca_i);
   const float I_xfer = C.Vxfer * (c.CaSS - c.Ca_i);
-  const float SERCA = C.Vmaxup * Caisquare / (Caisquare + C.Kupsquare);
+  const float SERCA = fdiv(C.Vmaxup * Caisquare, Caisquare + C.Kupsquare);
   const float dCaSR = C.dt1000 * (SERCA - I_rel - I_leak);
   CaSR_d += (double)buffered_increment(CaSR, dCaSR, C.Bufsr, C.Kbufsr);
   const float dCaSS = C.dt1000 * (-I_xfer * C.VcVss + I_rel * C.VsrVss + (-I_CaL * C.inversevssF2 * C.Cm));
@@ -190,7 +193,7 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
   const float dKi = -(-i_external + I_K1 + I_to + I_K - 2.f * I_NaK + I_pK) * C.inverseviF * C.Cm;
   K_i_d += (double)(C.dt1000 * dKi);
   const float CaSS005 = c.CaSS * 20.f;
-  const float den = 1.f / (1.f + CaSS005 * CaSS005);
+  const float den = fdiv(1.f, 1.f + CaSS005 * CaSS005);
   const float FCa_INF = 0.6f * den + 0.4f;
   const float taufca = 0.080f * den + 0.002f;
 
@@ -205,7 +208,7 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
   c.d = row[T2_d_inf] - (row[T2_d_inf] - c.d) * row[T2_exptau_d];
   c.f = row[T2_f_inf] - (row[T2_f_inf] - c.f) * row[T2_exptau_f];
   c.f2 = row[T2_f2_inf] - (row[T2_f2_inf] - c.f2) * row[T2_exptau_f2];
-  c.fCa = FCa_INF - (FCa_INF - c.fCa) * expf(-C.dt / taufca);
+  c.fCa = FCa_INF - (FCa_INF - c.fCa) * fexp(-fdiv(C.dt, taufca));
   return C.dt * (-I_tot);
 }
 

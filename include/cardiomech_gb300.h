@@ -181,6 +181,16 @@ int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ex
 int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *stim,
                  const int64_t *probe_cells, int64_t n_probe, int64_t probe_every, double *probe_vm);
 
+/* Autotuner: times every launch shape of the batch's kernel (threads per block, register
+ * budget, grid mode) on the batch itself for n_trial_steps steps each and keeps the fastest.
+ * The batch's state and audit bits are saved before and restored after, so tuning does not
+ * advance the cells. variant / ms_per_step (either may be NULL) receive the choice and its
+ * time per step. FP64 batches have a single shape. */
+int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_per_step);
+/* Fix the launch shape: variant in [0, n) from cm_batch_autotune's set, grid_mode 0 (one
+ * thread per cell) or k > 0 (grid-stride loop over k blocks per SM). */
+int cm_batch_set_launch(cm_batch_t b, int variant, int grid_mode);
+
 /* OR of the per-cell audit bits since the last call; per_cell (optional, n_cells uint32)
  * receives each cell's bits. Clears the bits. */
 int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell);

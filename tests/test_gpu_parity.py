@@ -101,8 +101,10 @@ def test_trace_mixed(gpu, port, model):
     S = b.get_state(gpu.LAYOUT_SOA)
     ref_soa = B[:, [c for c in range(B.shape[1]) if (c < 5 or c >= 23)]].T if model == 5 else \
         B[:, [c for c in range(22) if c != 20]].T
-    rel = np.abs(S - ref_soa) / np.maximum(np.abs(ref_soa), 1e-6)
-    assert rel.max() < 2e-2, rel.max(axis=1)
+    # per-state error after 3 beats, relative to the state's scale over the population
+    scale = np.maximum(np.abs(ref_soa).max(axis=1), 1e-12)
+    err = np.abs(S - ref_soa).max(axis=1) / scale
+    assert err.max() < 1e-3, dict(zip(gpu.state_names(model), err))
 
 
 def test_device_pointers_and_step_equals_run(gpu):
