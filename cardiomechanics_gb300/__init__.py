@@ -42,6 +42,7 @@ ABI_SYMBOLS = (
     "cm_batch_set_hetero", "cm_batch_set_diagnostics", "cm_batch_init_vm", "cm_batch_get_state",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak",
+    "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
 )
 
 
@@ -100,6 +101,12 @@ def lib() -> ctypes.CDLL:
     L.cm_batch_audit.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
     L.cm_batch_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.cm_batch_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.cm_multi_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.c_int, vp]
+    L.cm_multi_destroy.argtypes = [vp]
+    L.cm_multi_run.argtypes = [vp, ctypes.POINTER(vp), i64, ctypes.POINTER(Stimulus)]
+    L.cm_multi_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.cm_multi_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.cm_diag_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
     _lib = L
     return L
@@ -289,3 +296,42 @@ class Batch:
         pc = np.zeros(self.n, np.uint32) if per_cell else None
         _check(lib().cm_batch_audit(self._h, ctypes.byref(m), _ptr(pc)))
         return (m.value, pc) if per_cell else m.value
+
+
+class Multi:
+    """Batched form: several MIXED batches (any sizes, both models) advanced in lock step by one
+    persistent launch per time step, replayed from a CUDA graph."""
+
+    def __init__(self, batches, stream=None):
+        self.batches = list(batches)
+        arr = (ctypes.c_void_p * len(self.batches))(*[b._h.value for b in self.batches])
+        h = ctypes.c_void_p()
+        s = None if stream is None else ctypes.c_void_p(int(stream))
+        _check(lib().cm_multi_create(ctypes.byref(h), arr, len(self.batches), s))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_multi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, vms, n_steps, stims):
+        """vms: one float64 array/tensor per instance (updated in place); stims: one dict per
+        instance with keys textbegin, textlen, bcl, amplitude (optional t0)."""
+        vs = [_f64(v, b.n, "Vm") for v, b in zip(vms, self.batches)]
+        ptrs = (ctypes.c_void_p * len(vs))(*[_ptr(v) for v in vs])
+        st = (Stimulus * len(vs))(*[Stimulus(d.get("t0", 0.0), d.get("textbegin", 0.0), None, d.get("textlen", 1e-3),
+                                             d.get("bcl", 1.0), d.get("amplitude", 0.0)) for d in stims])
+        _check(lib().cm_multi_run(self._h, ptrs, int(n_steps), st))
+
+    def autotune(self, n_trial_steps=5):
+        t, sh, bps, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(lib().cm_multi_autotune(self._h, n_trial_steps, ctypes.byref(t), ctypes.byref(sh), ctypes.byref(bps),
+                                       ctypes.byref(ms)))
+        return {"tile_cells": t.value, "shape": sh.value, "blocks_per_sm": bps.value, "ms_per_step": ms.value}
+
+    def set_launch(self, tile_cells, shape=0, blocks_per_sm=2):
+        _check(lib().cm_multi_set_launch(self._h, tile_cells, shape, blocks_per_sm))

@@ -11,6 +11,7 @@
 
 #include "../../include/cardiomech_gb300.h"
 #include "cm_launch.h"
+#include "cm_multi.h"
 #include "cm_params.h"
 
 using namespace cm;
@@ -34,6 +35,7 @@ struct cm_batch_s {
   double *stage[4] = {};
   int64_t stage_n = 0;
   double *tb_cell = nullptr;
+  float *vm_planes = nullptr;  // mixed batches: Vm as hi/lo planes during fused runs (2 x n)
   int64_t *probe_idx = nullptr;
   int64_t probe_cap = 0;
   double *probe_out = nullptr;
@@ -72,30 +74,19 @@ bool is_device_ptr(const void *p) {
 
 int64_t round_ld(int64_t n) { return ((n + 63) / 64) * 64; }
 
-// SOA index (model order) -> position in the mixed layout: {is_fp64, slot}.
-void mixed_slot(int model, int k, bool &fp64, int &slot) {
+// SOA index (model order) -> plane of the mixed layout; `pair` variables are compensated
+// accumulators stored as hi (plane slot) and lo (plane slot + 1).
+void mixed_slot(int model, int k, bool &pair, int &slot) {
   if (model == kTenTusscher2) {
     // SOA: Ca_i CaSR CaSS Na_i K_i m h j xr1 xr2 xs r s d f f2 fCa Rq
-    static const int map32[] = {13, -1, 14, -1, -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
-    static const int map64[] = {-1, 0, -1, 1, 2};
-    if (k < 5 && map64[k] >= 0) {
-      fp64 = true;
-      slot = map64[k];
-    } else {
-      fp64 = false;
-      slot = map32[k];
-    }
+    static const int map[] = {13, 15, 14, 17, 19, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
+    slot = map[k];
+    pair = k == 1 || k == 3 || k == 4;
   } else {
     // SOA: Ca_i Ca_up Ca_rel h j oi ui Xr Xs u v w Na_i K_i m oa ua d f f_Ca Ca_TRPN
-    static const int map32[] = {15, -1, -1, 0, 1, 2, 3, 4, 5, 6, 7, 8, -1, -1, 9, 10, 11, 12, 13, 14, 16};
-    static const int map64[] = {-1, 0, 1, -1, -1, -1, -1, -1, -1, -1, -1, -1, 2, 3};
-    if (k < 14 && map64[k] >= 0) {
-      fp64 = true;
-      slot = map64[k];
-    } else {
-      fp64 = false;
-      slot = map32[k];
-    }
+    static const int map[] = {15, 17, 19, 0, 1, 2, 3, 4, 5, 6, 7, 8, 21, 23, 9, 10, 11, 12, 13, 14, 16};
+    slot = map[k];
+    pair = k == 1 || k == 2 || k == 12 || k == 13;
   }
 }
 
@@ -174,17 +165,18 @@ int soa_to_device(cm_batch_s *b, const std::vector<double> &soa) {
     CK(cudaStreamSynchronize(b->stream));
     return CM_OK;
   }
-  std::vector<float> f(n);
+  std::vector<float> f(n), g(n);
   for (int k = 0; k < ns; k++) {
-    bool fp64;
+    bool pair;
     int slot;
-    mixed_slot(b->d.model, k, fp64, slot);
-    if (fp64) {
-      CK(cudaMemcpy(b->d.s64 + slot * ld, soa.data() + (size_t)k * n, n * sizeof(double), cudaMemcpyHostToDevice));
-    } else {
-      for (int64_t c = 0; c < n; c++) f[c] = (float)soa[(size_t)k * n + c];
-      CK(cudaMemcpy(b->d.s32 + slot * ld, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    mixed_slot(b->d.model, k, pair, slot);
+    for (int64_t c = 0; c < n; c++) {
+      const Acc a = acc_from_double(soa[(size_t)k * n + c]);
+      f[c] = pair ? a.hi : (float)soa[(size_t)k * n + c];
+      g[c] = a.lo;
     }
+    CK(cudaMemcpy(b->d.s32 + slot * ld, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    if (pair) CK(cudaMemcpy(b->d.s32 + (slot + 1) * ld, g.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   }
   return CM_OK;
 }
@@ -199,17 +191,14 @@ int device_to_soa(cm_batch_s *b, std::vector<double> &soa) {
       CK(cudaMemcpy(soa.data() + (size_t)k * n, b->d.s64 + k * ld, n * sizeof(double), cudaMemcpyDeviceToHost));
     return CM_OK;
   }
-  std::vector<float> f(n);
+  std::vector<float> f(n), g(n);
   for (int k = 0; k < ns; k++) {
-    bool fp64;
+    bool pair;
     int slot;
-    mixed_slot(b->d.model, k, fp64, slot);
-    if (fp64) {
-      CK(cudaMemcpy(soa.data() + (size_t)k * n, b->d.s64 + slot * ld, n * sizeof(double), cudaMemcpyDeviceToHost));
-    } else {
-      CK(cudaMemcpy(f.data(), b->d.s32 + slot * ld, n * sizeof(float), cudaMemcpyDeviceToHost));
-      for (int64_t c = 0; c < n; c++) soa[(size_t)k * n + c] = f[c];
-    }
+    mixed_slot(b->d.model, k, pair, slot);
+    CK(cudaMemcpy(f.data(), b->d.s32 + slot * ld, n * sizeof(float), cudaMemcpyDeviceToHost));
+    if (pair) CK(cudaMemcpy(g.data(), b->d.s32 + (slot + 1) * ld, n * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int64_t c = 0; c < n; c++) soa[(size_t)k * n + c] = pair ? acc_to_double(Acc{f[c], g[c]}) : (double)f[c];
   }
   return CM_OK;
 }
@@ -374,6 +363,7 @@ int cm_batch_destroy(cm_batch_t b) {
   cudaFree(b->diag);
   for (auto p : b->stage) cudaFree(p);
   cudaFree(b->tb_cell);
+  cudaFree(b->vm_planes);
   cudaFree(b->probe_idx);
   cudaFree(b->probe_out);
   delete b;
@@ -614,6 +604,15 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   StepIO io;
   io.vm = dvm;
   io.vm_out = dvm;
+  const bool planes = b->d.precision == CM_PREC_MIXED;
+  if (planes) {
+    if (!b->vm_planes) CK(cudaMalloc(&b->vm_planes, std::max<int64_t>(1, 2 * n) * sizeof(float)));
+    io.vm_hi = b->vm_planes;
+    io.vm_lo = b->vm_planes + n;
+    io.vm = nullptr;
+    io.vm_out = nullptr;
+    CK(launch_vm_split(dvm, io.vm_hi, io.vm_lo, n, b->stream));
+  }
   io.textlen = st.textlen;
   io.bcl = st.bcl;
   io.amp = st.amplitude;
@@ -623,7 +622,8 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   double t = st.t0, tb = st.textbegin;
   for (int64_t s = 0; s < n_steps; s++) {
     if (n_probe > 0 && s % probe_every == 0)
-      CK(launch_probe(dvm, b->probe_idx, n_probe, b->probe_out, n_rec, s / probe_every, b->stream));
+      CK(launch_probe(planes ? nullptr : dvm, io.vm_hi, io.vm_lo, b->probe_idx, n_probe, b->probe_out, n_rec,
+                      s / probe_every, b->stream));
     io.t = t;
     if (!per_cell) {
       double i_ext = 0.0;
@@ -636,6 +636,7 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
     CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
     t += b->ps.dt;
   }
+  if (planes) CK(launch_vm_join(io.vm_hi, io.vm_lo, dvm, n, b->stream));
   if (host_vm) CK(cudaMemcpyAsync(Vm, dvm, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (n_probe > 0) {
     const bool host_probe = !is_device_ptr(probe_vm);
@@ -677,7 +678,10 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
   float best = 1e30f;
   int best_v = 0, best_g = 0;
   unsigned int audit_saved = 0;
-  std::vector<double> v0(n, b->ps.init_vm());
+  // trial Vm: compensated planes (hi, lo) of the rest potential, 2 x n floats in n doubles
+  const Acc a0 = acc_from_double(b->ps.init_vm());
+  std::vector<float> v0(2 * n, a0.hi);
+  std::fill(v0.begin() + n, v0.end(), a0.lo);
   cudaError_t e = cudaMalloc(&saved, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&vm, n * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
@@ -685,7 +689,7 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
   if (e == cudaSuccess) e = cudaMemcpyAsync(saved, b->state_mem, bytes, cudaMemcpyDeviceToDevice, b->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&audit_saved, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(vm, v0.data(), n * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(vm, v0.data(), 2 * n * sizeof(float), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   const int grid_modes[] = {0, 2, 4, 8};
   for (int v = 0; e == cudaSuccess && v < n_shape_variants(); v++) {
@@ -694,8 +698,8 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
       d.variant = v;
       d.grid_mode = g;
       StepIO io;
-      io.vm = vm;
-      io.vm_out = vm;
+      io.vm_hi = (float *)vm;  // the trial Vm as compensated planes (2 x n floats fit in n doubles)
+      io.vm_lo = (float *)vm + n;
       for (int k = 0; k < 2 && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
       if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
       for (int k = 0; k < n_trial_steps && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
@@ -741,6 +745,311 @@ int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell) {
   CK(cudaMemsetAsync(b->audit_or, 0, sizeof(unsigned int), b->stream));
   CK(cudaStreamSynchronize(b->stream));
   if (mask) *mask = m;
+  return CM_OK;
+}
+
+// ------------------------------------------------------------------ batched form
+
+}  // extern "C"
+
+struct cm_multi_s {
+  std::vector<cm_batch_t> batches;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  MultiInst *d_insts = nullptr;
+  MultiTile *d_tiles = nullptr;
+  MultiClock *d_clk = nullptr;
+  unsigned int *d_counters = nullptr;
+  std::vector<double *> vm_stage;   // host Vm staged as doubles
+  std::vector<float *> vm_planes;   // every instance's Vm as hi/lo planes during a run
+  std::vector<double *> vm_dev;     // device doubles of the current run (caller's or staged)
+  int n_tiles = 0, tile_cells = 4096, shape = 0, blocks_per_sm = 2;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 32;
+};
+
+namespace {
+
+void multi_drop_graph(cm_multi_s *m) {
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  m->graph = nullptr;
+}
+
+int multi_build_tiles(cm_multi_s *m, int tile_cells) {
+  if (tile_cells < 32 || tile_cells > (1 << 24)) return fail(CM_ERR_ARG, "tile_cells out of range");
+  std::vector<MultiTile> tiles;
+  for (int i = 0; i < (int)m->batches.size(); i++) {
+    const int64_t n = m->batches[i]->d.n;
+    for (int64_t st = 0; st < n; st += tile_cells)
+      tiles.push_back({i, (int)st, (int)std::min<int64_t>(tile_cells, n - st), 0});
+  }
+  cudaFree(m->d_tiles);
+  m->d_tiles = nullptr;
+  CK(cudaMalloc(&m->d_tiles, std::max<size_t>(1, tiles.size()) * sizeof(MultiTile)));
+  if (!tiles.empty())
+    CK(cudaMemcpy(m->d_tiles, tiles.data(), tiles.size() * sizeof(MultiTile), cudaMemcpyHostToDevice));
+  m->n_tiles = (int)tiles.size();
+  m->tile_cells = tile_cells;
+  multi_drop_graph(m);
+  return CM_OK;
+}
+
+MultiLaunch multi_launch_desc(const cm_multi_s *m) {
+  MultiLaunch L;
+  L.insts = m->d_insts;
+  L.tiles = m->d_tiles;
+  L.n_tiles = m->n_tiles;
+  L.n_inst = (int)m->batches.size();
+  L.clk = m->d_clk;
+  L.counters = m->d_counters;
+  L.shape = m->shape;
+  L.grid = std::max(1, sm_count() * m->blocks_per_sm);
+  return L;
+}
+
+// Uploads the instance table (Vm pointers, protocols) and the initial clocks.
+int multi_prepare(cm_multi_s *m, double *const *Vm, const cm_stimulus *stims, std::vector<bool> &host_vm) {
+  const int n = (int)m->batches.size();
+  std::vector<MultiInst> insts(n);
+  std::vector<MultiClock> clk(n);
+  host_vm.assign(n, false);
+  if ((int)m->vm_stage.size() < n) m->vm_stage.resize(n, nullptr);
+  if ((int)m->vm_planes.size() < n) m->vm_planes.resize(n, nullptr);
+  m->vm_dev.assign(n, nullptr);
+  for (int i = 0; i < n; i++) {
+    cm_batch_s *b = m->batches[i];
+    insts[i].d = b->d;
+    double *v = Vm[i];
+    if (!v && b->d.n > 0) return fail(CM_ERR_ARG, "Vm[" + std::to_string(i) + "] is NULL");
+    if (v && !is_device_ptr(v)) {
+      host_vm[i] = true;
+      if (!m->vm_stage[i]) CK(cudaMalloc(&m->vm_stage[i], std::max<int64_t>(1, b->d.n) * sizeof(double)));
+      CK(cudaMemcpyAsync(m->vm_stage[i], v, b->d.n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+      v = m->vm_stage[i];
+    }
+    if (!m->vm_planes[i]) CK(cudaMalloc(&m->vm_planes[i], std::max<int64_t>(1, 2 * b->d.n) * sizeof(float)));
+    insts[i].vm_hi = m->vm_planes[i];
+    insts[i].vm_lo = m->vm_planes[i] + b->d.n;
+    m->vm_dev[i] = v;
+    if (v) CK(launch_vm_split(v, insts[i].vm_hi, insts[i].vm_lo, b->d.n, m->stream));
+    const cm_stimulus st = stims ? stims[i] : cm_stimulus{0, 0, nullptr, 0, 0, 0};
+    if (st.textbegin_per_cell) return fail(CM_ERR_UNSUPPORTED, "per-cell stimulus times are not supported in a multi");
+    insts[i].textlen = st.textlen;
+    insts[i].bcl = st.bcl;
+    insts[i].amp = stims ? st.amplitude : 0.0;
+    insts[i].dt = b->ps.dt;
+    clk[i].t = st.t0;
+    clk[i].tb = stims ? st.textbegin : 1e300;
+  }
+  CK(cudaMemcpyAsync(m->d_insts, insts.data(), n * sizeof(MultiInst), cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->d_clk, clk.data(), n * sizeof(MultiClock), cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemsetAsync(m->d_counters, 0, 2 * sizeof(unsigned int), m->stream));
+  return CM_OK;
+}
+
+int multi_steps(cm_multi_s *m, int64_t n_steps, bool use_graph) {
+  const MultiLaunch L = multi_launch_desc(m);
+  int64_t s = 0;
+  if (use_graph && n_steps >= m->graph_steps) {
+    if (!m->graph) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < m->graph_steps; k++) {
+        cudaError_t e = launch_multi(L, k & 1, m->stream);
+        if (e != cudaSuccess) {
+          cudaStreamEndCapture(m->stream, &g);
+          return cuda_fail(e, "launch_multi (capture)");
+        }
+      }
+      CK(cudaStreamEndCapture(m->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&m->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    for (; s + m->graph_steps <= n_steps; s += m->graph_steps) CK(cudaGraphLaunch(m->graph, m->stream));
+  }
+  for (; s < n_steps; s++) CK(launch_multi(L, (int)(s & 1), m->stream));
+  return CM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cm_multi_destroy(cm_multi_t m) {
+  if (!m) return CM_OK;
+  cudaStreamSynchronize(m->stream);
+  multi_drop_graph(m);
+  cudaFree(m->d_insts);
+  cudaFree(m->d_tiles);
+  cudaFree(m->d_clk);
+  cudaFree(m->d_counters);
+  for (auto p : m->vm_stage) cudaFree(p);
+  for (auto p : m->vm_planes) cudaFree(p);
+  if (m->own_stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return CM_OK;
+}
+
+int cm_multi_create(cm_multi_t *out, const cm_batch_t *batches, int n_batches, void *stream) {
+  if (!out || !batches || n_batches <= 0) return fail(CM_ERR_ARG, "need at least one batch");
+  *out = nullptr;
+  for (int i = 0; i < n_batches; i++) {
+    if (!batches[i]) return fail(CM_ERR_ARG, "NULL batch");
+    if (batches[i]->d.precision != CM_PREC_MIXED)
+      return fail(CM_ERR_UNSUPPORTED, "the batched form runs CM_PREC_MIXED batches");
+    if (batches[i]->d.ld * 24 >= (int64_t)2147483647) return fail(CM_ERR_ARG, "instance too large for a multi");
+  }
+  auto *m = new (std::nothrow) cm_multi_s();
+  if (!m) return fail(CM_ERR_NOMEM, "host allocation failed");
+  m->batches.assign(batches, batches + n_batches);
+  int rc = CM_OK;
+  cudaError_t e = cudaSuccess;
+  if (stream) {
+    m->stream = (cudaStream_t)stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);  // capturable
+    m->own_stream = e == cudaSuccess;
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_insts, n_batches * sizeof(MultiInst));
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_clk, 2 * n_batches * sizeof(MultiClock));
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_counters, 2 * sizeof(unsigned int));
+  if (e != cudaSuccess) rc = cuda_fail(e, "cm_multi_create");
+  if (!rc) rc = multi_build_tiles(m, m->tile_cells);
+  if (rc) {
+    std::string keep = g_err;
+    cm_multi_destroy(m);
+    g_err = keep;
+    return rc;
+  }
+  *out = m;
+  return CM_OK;
+}
+
+int cm_multi_set_launch(cm_multi_t m, int tile_cells, int shape, int blocks_per_sm) {
+  if (!m) return fail(CM_ERR_ARG, "NULL multi");
+  if (shape < 0 || shape >= n_multi_shapes() || blocks_per_sm < 1 || blocks_per_sm > 32)
+    return fail(CM_ERR_ARG, "launch shape out of range");
+  if (tile_cells != m->tile_cells) {
+    int rc = multi_build_tiles(m, tile_cells);
+    if (rc) return rc;
+  }
+  if (shape != m->shape || blocks_per_sm != m->blocks_per_sm) multi_drop_graph(m);
+  m->shape = shape;
+  m->blocks_per_sm = blocks_per_sm;
+  return CM_OK;
+}
+
+int cm_multi_run(cm_multi_t m, double *const *Vm, int64_t n_steps, const cm_stimulus *stims) {
+  if (!m || !Vm) return fail(CM_ERR_ARG, "NULL argument");
+  if (n_steps < 0) return fail(CM_ERR_ARG, "n_steps < 0");
+  std::vector<bool> host_vm;
+  int rc = multi_prepare(m, Vm, stims, host_vm);
+  if (rc) return rc;
+  if ((rc = multi_steps(m, n_steps, true))) return rc;
+  unsigned int mask = 0;
+  std::vector<unsigned int> masks(m->batches.size(), 0);
+  for (size_t i = 0; i < m->batches.size(); i++) {
+    const int64_t ni = m->batches[i]->d.n;
+    CK(launch_vm_join(m->vm_planes[i], m->vm_planes[i] + ni, m->vm_dev[i], ni, m->stream));
+    if (host_vm[i])
+      CK(cudaMemcpyAsync(Vm[i], m->vm_stage[i], m->batches[i]->d.n * sizeof(double), cudaMemcpyDeviceToHost,
+                         m->stream));
+    CK(cudaMemcpyAsync(&masks[i], m->batches[i]->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                       m->stream));
+  }
+  CK(cudaStreamSynchronize(m->stream));
+  for (auto x : masks) mask |= x;
+  if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+int cm_multi_autotune(cm_multi_t m, int n_trial_steps, int *tile_cells, int *shape, int *blocks_per_sm,
+                      double *ms_per_step) {
+  if (!m) return fail(CM_ERR_ARG, "NULL multi");
+  if (n_trial_steps < 1) n_trial_steps = 1;
+  const int n = (int)m->batches.size();
+  // save every instance's state and audit word; trial Vm starts from each model's rest value
+  std::vector<void *> saved(n, nullptr);
+  std::vector<size_t> bytes(n, 0);
+  std::vector<unsigned int> audit(n, 0);
+  std::vector<double *> vms(n, nullptr);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    cm_batch_s *b = m->batches[i];
+    bytes[i] = (size_t)n_fp64_vars(b->d.model, b->d.precision) * b->d.ld * sizeof(double) +
+               (size_t)n_fp32_vars(b->d.model) * b->d.ld * sizeof(float);
+    e = cudaMalloc(&saved[i], bytes[i]);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(saved[i], b->state_mem, bytes[i], cudaMemcpyDeviceToDevice, m->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&audit[i], b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&vms[i], std::max<int64_t>(1, b->d.n) * sizeof(double));
+    if (e == cudaSuccess) {
+      std::vector<double> v0(b->d.n, b->ps.init_vm());
+      e = cudaMemcpy(vms[i], v0.data(), b->d.n * sizeof(double), cudaMemcpyHostToDevice);
+    }
+  }
+  const int old_tile = m->tile_cells, old_shape = m->shape, old_bps = m->blocks_per_sm;
+  float best = 1e30f;
+  int bt = old_tile, bs = old_shape, bb = old_bps;
+  int rc = CM_OK;
+  if (e != cudaSuccess) rc = cuda_fail(e, "multi autotune setup");
+  std::vector<bool> host_vm;
+  const int tiles[] = {1024, 2048, 4096, 8192, 16384};
+  const int bpss[] = {1, 2, 4, 8};
+  for (int t : tiles) {
+    if (rc) break;
+    if ((rc = multi_build_tiles(m, t))) break;
+    for (int sh = 0; sh < n_multi_shapes() && !rc; sh++) {
+      for (int bps : bpss) {
+        if (multi_block(sh) * bps > 2048) continue;
+        m->shape = sh;
+        m->blocks_per_sm = bps;
+        if ((rc = multi_prepare(m, vms.data(), nullptr, host_vm))) break;
+        if ((rc = multi_steps(m, 2, false))) break;
+        cudaEventRecord(e0, m->stream);
+        if ((rc = multi_steps(m, n_trial_steps, false))) break;
+        cudaEventRecord(e1, m->stream);
+        e = cudaEventSynchronize(e1);
+        float ms = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "multi autotune");
+          break;
+        }
+        if (ms < best) {
+          best = ms;
+          bt = t;
+          bs = sh;
+          bb = bps;
+        }
+      }
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    if (saved[i]) {
+      cudaMemcpyAsync(m->batches[i]->state_mem, saved[i], bytes[i], cudaMemcpyDeviceToDevice, m->stream);
+      cudaMemcpyAsync(m->batches[i]->audit_or, &audit[i], sizeof(unsigned int), cudaMemcpyHostToDevice, m->stream);
+    }
+  }
+  cudaStreamSynchronize(m->stream);
+  for (int i = 0; i < n; i++) {
+    cudaFree(saved[i]);
+    cudaFree(vms[i]);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (!rc) rc = multi_build_tiles(m, bt);
+  if (rc) return rc;
+  m->shape = bs;
+  m->blocks_per_sm = bb;
+  multi_drop_graph(m);
+  if (tile_cells) *tile_cells = bt;
+  if (shape) *shape = bs;
+  if (blocks_per_sm) *blocks_per_sm = bb;
+  if (ms_per_step) *ms_per_step = best / n_trial_steps;
   return CM_OK;
 }
 

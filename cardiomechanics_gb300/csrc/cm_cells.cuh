@@ -1,0 +1,71 @@
+// Per-cell bodies of the mixed kernels: load one cell's state from its batch, advance it one
+// step and store it back. Shared by the single-batch kernels (cm_kernels.cu) and the
+// multi-instance kernel (cm_multi.cu).
+#pragma once
+
+#include "cm_crn.cuh"
+#include "cm_launch.h"
+#include "cm_tt2.cuh"
+
+namespace cm {
+
+template <typename I>
+__device__ __forceinline__ float tt2_mixed_cell(const DevBatch &b, I c, float V, float iext, uint32_t &audit) {
+  const I ld = (I)b.ld;
+  const float *const *het = (const float *const *)b.het;
+  float *s = b.s32 + c;
+  TT2Cell<float> x;
+  x.m = s[0]; x.h = s[ld]; x.j = s[2 * ld]; x.xr1 = s[3 * ld]; x.xr2 = s[4 * ld]; x.xs = s[5 * ld];
+  x.r = s[6 * ld]; x.s = s[7 * ld]; x.d = s[8 * ld]; x.f = s[9 * ld]; x.f2 = s[10 * ld]; x.fCa = s[11 * ld];
+  x.Rq = s[12 * ld]; x.Ca_i = s[13 * ld]; x.CaSS = s[14 * ld];
+  Acc CaSR{s[15 * ld], s[16 * ld]}, Na_i{s[17 * ld], s[18 * ld]}, K_i{s[19 * ld], s[20 * ld]};
+  const TT2Consts<float> &C = b.tt2_32;
+  TT2Het_<float> g;
+  g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + c) : C.g_Na;
+  g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + c) : C.g_Kr;
+  g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + c) : C.g_K1;
+  g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + c) : C.g_Ks;
+  g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
+  g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
+  const int vi = vrow_fp32(V * 1000.f, audit);
+  const float dV = tt2_calc_mixed(C, b.rows32 + (size_t)vi * T2_COLS, b.eca32, x, CaSR, Na_i, K_i, g, V, iext, audit);
+  s[0] = x.m; s[ld] = x.h; s[2 * ld] = x.j; s[3 * ld] = x.xr1; s[4 * ld] = x.xr2; s[5 * ld] = x.xs;
+  s[6 * ld] = x.r; s[7 * ld] = x.s; s[8 * ld] = x.d; s[9 * ld] = x.f; s[10 * ld] = x.f2; s[11 * ld] = x.fCa;
+  s[12 * ld] = x.Rq; s[13 * ld] = x.Ca_i; s[14 * ld] = x.CaSS;
+  s[15 * ld] = CaSR.hi; s[16 * ld] = CaSR.lo; s[17 * ld] = Na_i.hi; s[18 * ld] = Na_i.lo;
+  s[19 * ld] = K_i.hi; s[20 * ld] = K_i.lo;
+  return dV;
+}
+
+template <typename I>
+__device__ __forceinline__ float crn_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch,
+                                                uint32_t &audit) {
+  const I ld = (I)b.ld;
+  const float *const *het = (const float *const *)b.het;
+  float *s = b.s32 + c;
+  CRNCell<float> x;
+  x.h = s[0]; x.j = s[ld]; x.oi = s[2 * ld]; x.ui = s[3 * ld]; x.Xr = s[4 * ld]; x.Xs = s[5 * ld];
+  x.u = s[6 * ld]; x.v = s[7 * ld]; x.w = s[8 * ld]; x.m = s[9 * ld]; x.oa = s[10 * ld]; x.ua = s[11 * ld];
+  x.d = s[12 * ld]; x.f = s[13 * ld]; x.f_Ca = s[14 * ld]; x.Ca_i = s[15 * ld]; x.Ca_TRPN = s[16 * ld];
+  Acc Ca_up{s[17 * ld], s[18 * ld]}, Ca_rel{s[19 * ld], s[20 * ld]}, Na_i{s[21 * ld], s[22 * ld]},
+      K_i{s[23 * ld], s[24 * ld]};
+  const CRNConsts<float> &C = b.crn_32;
+  CRNHet_<float> g;
+  g.g_Na = het[HC_g_Na] ? __ldg(het[HC_g_Na] + c) : C.g_Na;
+  g.g_to = het[HC_g_to] ? __ldg(het[HC_g_to] + c) : C.g_to;
+  g.g_Ks = het[HC_g_Ks] ? __ldg(het[HC_g_Ks] + c) : C.g_Ks;
+  g.g_CaL = het[HC_g_CaL] ? __ldg(het[HC_g_CaL] + c) : C.g_CaL;
+  g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
+  g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
+  const int vi = vrow_fp32(V * 1000.f, audit);
+  const float dV = crn_calc_mixed(C, b.rows32 + (size_t)vi * CR_COLS, x, Ca_up, Ca_rel, Na_i, K_i, g, V, iext,
+                                  stretch, audit);
+  s[0] = x.h; s[ld] = x.j; s[2 * ld] = x.oi; s[3 * ld] = x.ui; s[4 * ld] = x.Xr; s[5 * ld] = x.Xs;
+  s[6 * ld] = x.u; s[7 * ld] = x.v; s[8 * ld] = x.w; s[9 * ld] = x.m; s[10 * ld] = x.oa; s[11 * ld] = x.ua;
+  s[12 * ld] = x.d; s[13 * ld] = x.f; s[14 * ld] = x.f_Ca; s[15 * ld] = x.Ca_i; s[16 * ld] = x.Ca_TRPN;
+  s[17 * ld] = Ca_up.hi; s[18 * ld] = Ca_up.lo; s[19 * ld] = Ca_rel.hi; s[20 * ld] = Ca_rel.lo;
+  s[21 * ld] = Na_i.hi; s[22 * ld] = Na_i.lo; s[23 * ld] = K_i.hi; s[24 * ld] = K_i.lo;
+  return dV;
+}
+
+}  // namespace cm

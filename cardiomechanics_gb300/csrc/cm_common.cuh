@@ -134,6 +134,35 @@ CM_HD float fsqrt(float x) {
 #endif
 }
 
+// Compensated FP32 accumulator (value = hi + lo, |lo| <= ulp(hi)/2): about 48 significant
+// bits with FP32-pipe instructions only. The mixed form keeps Vm, [Na]i, [K]i and [Ca]SR in
+// it: their per-step increments are 1e-7..1e-9 of their values and would vanish in plain FP32,
+// and GB300's FP64 pipe (1/64 of the FP32 rate) would bound the kernel if they were doubles.
+struct Acc {
+  float hi, lo;
+};
+
+// hi + lo += d with Knuth's two-sum (no magnitude precondition, so it also holds where Vm
+// crosses zero) followed by a fast renormalisation.
+CM_HD void acc_add(Acc &a, float d) {
+  const float s = a.hi + d;
+  const float bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (d - bp);
+  const float t = a.lo + e;
+  const float h = s + t;
+  a.lo = t - (h - s);
+  a.hi = h;
+}
+
+CM_HD Acc acc_from_double(double x) {
+  Acc a;
+  a.hi = (float)x;
+  a.lo = (float)(x - (double)a.hi);
+  return a;
+}
+
+CM_HD double acc_to_double(Acc a) { return (double)a.hi + (double)a.lo; }
+
 // New free concentration increment of a rapidly buffered species. The reference solves
 // x^2 + b x - c = 0 for the new free value x given total = x_old + B x_old/(x_old+K) + dT
 // (TenTusscher2.cpp:814-836). Writing x = x_old + d, the same conservation law gives

@@ -94,14 +94,14 @@ CM_HD double crn_calc_fp64(const CRNConsts<double> &C, const double *__restrict_
   return -.001 * I_tot * tinc;
 }
 
-// Mixed form: gates, currents, Ca_i and Ca_TRPN in FP32; Na_i, K_i, Ca_up, Ca_rel accumulated
-// in FP64. exp(250) and exp(169.5) exceed FP32, so Fn * exp(c) is evaluated as exp(arg + c).
+// Mixed form: gates, currents, Ca_i and Ca_TRPN in FP32; Na_i, K_i, Ca_up, Ca_rel in compensated
+// FP32 accumulators (Acc). exp(250) and exp(169.5) exceed FP32, so Fn * exp(c) is evaluated as exp(arg + c).
 CM_HD float crn_calc_mixed(const CRNConsts<float> &C, const float *__restrict__ row, CRNCell<float> &c,
-                           double &Ca_up_d, double &Ca_rel_d, double &Na_i_d, double &K_i_d, const CRNHet_<float> &g,
+                           Acc &Ca_up_a, Acc &Ca_rel_a, Acc &Na_a, Acc &K_a, const CRNHet_<float> &g,
                            float V, float i_external, float stretch, uint32_t &audit) {
   const float tinc = C.dt_ms;
   const float V_int = V * 1000.f;
-  const float Na_i = (float)Na_i_d, K_i = (float)K_i_d, Ca_up = (float)Ca_up_d, Ca_rel = (float)Ca_rel_d;
+  const float Na_i = Na_a.hi, K_i = K_a.hi, Ca_up = Ca_up_a.hi, Ca_rel = Ca_rel_a.hi;
   const float dNa_i = fdiv(1.f, Na_i);
   const float VmE_Na = V_int - C.RTdF * (C.logNao - flog(Na_i));
   const float VmE_K = V_int - C.RTdF * (C.logKo - flog(K_i));
@@ -143,10 +143,10 @@ CM_HD float crn_calc_mixed(const CRNConsts<float> &C, const float *__restrict__ 
   const float px = C.n_TRPN == 2.f ? x * x : powf(x, C.n_TRPN);
   const float dCaTRPN = C.k_TRPN * (px * (1.f - c.Ca_TRPN) - c.Ca_TRPN);
   c.Ca_TRPN += tinc * dCaTRPN;
-  Ca_up_d += (double)(tinc * (I_up - I_tr * C.VreldVup - I_upleak));
-  Ca_rel_d += (double)(tinc * fdiv((I_tr - I_rel) * (Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn), Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn + C.csqnkm));
-  Na_i_d += (double)(tinc * (-3.f * I_NaK - 3.f * I_NaCa - I_bNa - I_Na) * C.CmdFvi);
-  K_i_d += (double)(tinc * (2.f * I_NaK - I_K1 - I_to - I_Kur - I_Kr - I_Ks) * C.CmdFvi);
+  acc_add(Ca_up_a, tinc * (I_up - I_tr * C.VreldVup - I_upleak));
+  acc_add(Ca_rel_a, tinc * fdiv((I_tr - I_rel) * (Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn), Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn + C.csqnkm));
+  acc_add(Na_a, tinc * (-3.f * I_NaK - 3.f * I_NaCa - I_bNa - I_Na) * C.CmdFvi);
+  acc_add(K_a, tinc * (2.f * I_NaK - I_K1 - I_to - I_Kur - I_Kr - I_Ks) * C.CmdFvi);
   float B1 = ((2.f * I_NaCa - I_pCa - I_CaL - I_bCa) * .5f * C.CmdFvi) + ((I_upleak - I_up) * C.VupdVi + I_rel * C.VreldVi);
   B1 -= C.TRPNmax * dCaTRPN;
   const float q = (c.Ca_i * c.Ca_i) + (c.Ca_i * C.kmcmdnm2) + C.kkmcmdn;

@@ -8,9 +8,7 @@
 // accumulators; they are bound by HBM bandwidth.
 #include <cuda_runtime.h>
 
-#include "cm_crn.cuh"
-#include "cm_launch.h"
-#include "cm_tt2.cuh"
+#include "cm_cells.cuh"
 
 namespace cm {
 
@@ -37,6 +35,17 @@ __device__ __forceinline__ void finish(const DevBatch &b, const StepIO &io, int6
   if (io.dvm) io.dvm[c] = dV;
   if (!isfinite(vn)) audit |= 1u;
   if (io.vm_range > 0.0 && fabs(vn) > io.vm_range) audit |= 32u;
+  if (audit) {
+    atomicOr(b.audit_cell + c, audit);
+    atomicOr(b.audit_or, audit);
+  }
+}
+
+template <typename I>
+__device__ __forceinline__ void finish_acc(const DevBatch &b, I c, Acc v, uint32_t audit, const StepIO &io) {
+  io.vm_hi[c] = v.hi;
+  io.vm_lo[c] = v.lo;
+  if (!isfinite(v.hi)) audit |= 1u;
   if (audit) {
     atomicOr(b.audit_cell + c, audit);
     atomicOr(b.audit_or, audit);
@@ -85,35 +94,18 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
 
 template <typename I, int kBlock, int kMinB>
 __global__ void __launch_bounds__(kBlock, kMinB) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
-  const I ld = (I)b.ld;
-  const float *const *het = (const float *const *)b.het;
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    float *s = b.s32 + c;
-    double *a = b.s64 + c;
-    TT2Cell<float> x;
-    x.m = s[0]; x.h = s[ld]; x.j = s[2 * ld]; x.xr1 = s[3 * ld]; x.xr2 = s[4 * ld]; x.xs = s[5 * ld];
-    x.r = s[6 * ld]; x.s = s[7 * ld]; x.d = s[8 * ld]; x.f = s[9 * ld]; x.f2 = s[10 * ld]; x.fCa = s[11 * ld];
-    x.Rq = s[12 * ld]; x.Ca_i = s[13 * ld]; x.CaSS = s[14 * ld];
-    double CaSR = a[0], Na_i = a[ld], K_i = a[2 * ld];
-    const TT2Consts<float> &C = b.tt2_32;
-    TT2Het_<float> g;
-    g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + c) : C.g_Na;
-    g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + c) : C.g_Kr;
-    g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + c) : C.g_K1;
-    g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + c) : C.g_Ks;
-    g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
-    g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
-    const double V = __ldg(io.vm + c);
     const float iext = (float)stim_for_cell(io, c);
     uint32_t audit = 0;
-    const float Vf = (float)V;
-    const int vi = vrow_fp32(Vf * 1000.f, audit);
-    const float dV = tt2_calc_mixed(C, b.rows32 + (size_t)vi * T2_COLS, b.eca32, x, CaSR, Na_i, K_i, g, Vf, iext, audit);
-    s[0] = x.m; s[ld] = x.h; s[2 * ld] = x.j; s[3 * ld] = x.xr1; s[4 * ld] = x.xr2; s[5 * ld] = x.xs;
-    s[6 * ld] = x.r; s[7 * ld] = x.s; s[8 * ld] = x.d; s[9 * ld] = x.f; s[10 * ld] = x.f2; s[11 * ld] = x.fCa;
-    s[12 * ld] = x.Rq; s[13 * ld] = x.Ca_i; s[14 * ld] = x.CaSS;
-    a[0] = CaSR; a[ld] = Na_i; a[2 * ld] = K_i;
-    finish(b, io, c, V, (double)dV, audit);
+    if (io.vm_hi) {
+      Acc v{io.vm_hi[c], io.vm_lo[c]};
+      acc_add(v, tt2_mixed_cell<I>(b, c, v.hi, iext, audit));
+      finish_acc(b, c, v, audit, io);
+    } else {
+      const double V = __ldg(io.vm + c);
+      const float dV = tt2_mixed_cell<I>(b, c, (float)V, iext, audit);
+      finish(b, io, c, V, (double)dV, audit);
+    }
   }
 }
 
@@ -159,52 +151,50 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
 
 template <typename I, int kBlock, int kMinB>
 __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch b, const StepIO io) {
-  const I ld = (I)b.ld;
-  const float *const *het = (const float *const *)b.het;
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    float *s = b.s32 + c;
-    double *a = b.s64 + c;
-    CRNCell<float> x;
-    x.h = s[0]; x.j = s[ld]; x.oi = s[2 * ld]; x.ui = s[3 * ld]; x.Xr = s[4 * ld]; x.Xs = s[5 * ld];
-    x.u = s[6 * ld]; x.v = s[7 * ld]; x.w = s[8 * ld]; x.m = s[9 * ld]; x.oa = s[10 * ld]; x.ua = s[11 * ld];
-    x.d = s[12 * ld]; x.f = s[13 * ld]; x.f_Ca = s[14 * ld]; x.Ca_i = s[15 * ld]; x.Ca_TRPN = s[16 * ld];
-    double Ca_up = a[0], Ca_rel = a[ld], Na_i = a[2 * ld], K_i = a[3 * ld];
-    const CRNConsts<float> &C = b.crn_32;
-    CRNHet_<float> g;
-    g.g_Na = het[HC_g_Na] ? __ldg(het[HC_g_Na] + c) : C.g_Na;
-    g.g_to = het[HC_g_to] ? __ldg(het[HC_g_to] + c) : C.g_to;
-    g.g_Ks = het[HC_g_Ks] ? __ldg(het[HC_g_Ks] + c) : C.g_Ks;
-    g.g_CaL = het[HC_g_CaL] ? __ldg(het[HC_g_CaL] + c) : C.g_CaL;
-    g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
-    g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
-    const double V = __ldg(io.vm + c);
     const float iext = (float)stim_for_cell(io, c);
     const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
     uint32_t audit = 0;
-    const float Vf = (float)V;
-    const int vi = vrow_fp32(Vf * 1000.f, audit);
-    const float dV = crn_calc_mixed(C, b.rows32 + (size_t)vi * CR_COLS, x, Ca_up, Ca_rel, Na_i, K_i, g, Vf, iext,
-                                    stretch, audit);
-    s[0] = x.h; s[ld] = x.j; s[2 * ld] = x.oi; s[3 * ld] = x.ui; s[4 * ld] = x.Xr; s[5 * ld] = x.Xs;
-    s[6 * ld] = x.u; s[7 * ld] = x.v; s[8 * ld] = x.w; s[9 * ld] = x.m; s[10 * ld] = x.oa; s[11 * ld] = x.ua;
-    s[12 * ld] = x.d; s[13 * ld] = x.f; s[14 * ld] = x.f_Ca; s[15 * ld] = x.Ca_i; s[16 * ld] = x.Ca_TRPN;
-    a[0] = Ca_up; a[ld] = Ca_rel; a[2 * ld] = Na_i; a[3 * ld] = K_i;
-    finish(b, io, c, V, (double)dV, audit);
+    if (io.vm_hi) {
+      Acc v{io.vm_hi[c], io.vm_lo[c]};
+      acc_add(v, crn_mixed_cell<I>(b, c, v.hi, iext, stretch, audit));
+      finish_acc(b, c, v, audit, io);
+    } else {
+      const double V = __ldg(io.vm + c);
+      const float dV = crn_mixed_cell<I>(b, c, (float)V, iext, stretch, audit);
+      finish(b, io, c, V, (double)dV, audit);
+    }
   }
 }
 
-__global__ void probe_kernel(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
-                             int64_t k) {
+__global__ void probe_kernel(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
+                             int64_t n_probe, double *out, int64_t stride, int64_t k) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_probe) out[i * stride + k] = vm[probe[i]];
+  if (i < n_probe) {
+    const int64_t c = probe[i];
+    out[i * stride + k] = vm ? vm[c] : acc_to_double(Acc{vm_hi[c], vm_lo[c]});
+  }
+}
+
+__global__ void vm_split_kernel(const double *v, float *hi, float *lo, int64_t n) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const Acc a = acc_from_double(v[c]);
+    hi[c] = a.hi;
+    lo[c] = a.lo;
+  }
+}
+
+__global__ void vm_join_kernel(const float *hi, const float *lo, double *v, int64_t n) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    v[c] = acc_to_double(Acc{hi[c], lo[c]});
 }
 
 }  // namespace
 
-int n_fp32_vars(int model) { return model == 5 ? 15 : 17; }
+int n_fp32_vars(int model) { return model == 5 ? 21 : 25; }
 int n_fp64_vars(int model, int precision) {
   if (precision == 0) return model == 5 ? S2_N : SC_N;
-  return model == 5 ? 3 : 4;
+  return 0;
 }
 
 int sm_count() {
@@ -220,7 +210,8 @@ namespace {
 struct Shape {
   int block, minb;
 };
-constexpr Shape kShapes[] = {{256, 1}, {256, 3}, {128, 6}, {512, 1}, {128, 1}};
+// register budgets: (256,2) and (512,1) -> 128, (128,5) and (64,10) -> 96, (256,3) -> 80
+constexpr Shape kShapes[] = {{256, 2}, {128, 5}, {256, 3}, {512, 1}, {64, 10}};
 
 template <typename I, int B, int M>
 void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s) {
@@ -231,11 +222,11 @@ void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s)
 template <typename I>
 void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, cudaStream_t s) {
   switch (v) {
-    case 1: launch_mixed<I, 256, 3>(b, io, grid, s); break;
-    case 2: launch_mixed<I, 128, 6>(b, io, grid, s); break;
+    case 1: launch_mixed<I, 128, 5>(b, io, grid, s); break;
+    case 2: launch_mixed<I, 256, 3>(b, io, grid, s); break;
     case 3: launch_mixed<I, 512, 1>(b, io, grid, s); break;
-    case 4: launch_mixed<I, 128, 1>(b, io, grid, s); break;
-    default: launch_mixed<I, 256, 1>(b, io, grid, s); break;
+    case 4: launch_mixed<I, 64, 10>(b, io, grid, s); break;
+    default: launch_mixed<I, 256, 2>(b, io, grid, s); break;
   }
 }
 }  // namespace
@@ -272,10 +263,24 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
   return cudaGetLastError();
 }
 
-cudaError_t launch_probe(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
-                         int64_t k, cudaStream_t s) {
+cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
+                         int64_t n_probe, double *out, int64_t stride, int64_t k, cudaStream_t s) {
   if (n_probe <= 0) return cudaSuccess;
-  probe_kernel<<<(unsigned)((n_probe + 127) / 128), 128, 0, s>>>(vm, probe, n_probe, out, stride, k);
+  probe_kernel<<<(unsigned)((n_probe + 127) / 128), 128, 0, s>>>(vm, vm_hi, vm_lo, probe, n_probe, out, stride, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vm_split(const double *v, float *hi, float *lo, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t g = (n + 255) / 256;
+  vm_split_kernel<<<(unsigned)(g < 65535 ? g : 65535), 256, 0, s>>>(v, hi, lo, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vm_join(const float *hi, const float *lo, double *v, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t g = (n + 255) / 256;
+  vm_join_kernel<<<(unsigned)(g < 65535 ? g : 65535), 256, 0, s>>>(hi, lo, v, n);
   return cudaGetLastError();
 }
 

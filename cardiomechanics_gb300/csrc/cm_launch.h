@@ -12,10 +12,11 @@ namespace cm {
 
 // Device memory of one batch of cells of one model in one precision.
 //   FP64:  s64[k * ld + c], k < n_state (SOA order of the model)
-//   MIXED: s32[k * ld + c] for the FP32 variables, s64[k * ld + c] for the FP64 accumulators
-//          TT2  FP32: m h j xr1 xr2 xs r s d f f2 fCa Rq Ca_i CaSS     FP64: CaSR Na_i K_i
-//          CRN  FP32: h j oi ui Xr Xs u v w m oa ua d f f_Ca Ca_i Ca_TRPN  FP64: Ca_up Ca_rel Na_i K_i
-struct DevBatch {
+//   MIXED: s32[k * ld + c], every variable a 32-bit word; compensated accumulators take two
+//          (hi, lo) planes:
+//          TT2  m h j xr1 xr2 xs r s d f f2 fCa Rq Ca_i CaSS | CaSR Na_i K_i (hi, lo each)
+//          CRN  h j oi ui Xr Xs u v w m oa ua d f f_Ca Ca_i Ca_TRPN | Ca_up Ca_rel Na_i K_i (hi, lo)
+struct alignas(16) DevBatch {
   int model = 0;      // 2 Courtemanche, 5 TenTusscher2
   int precision = 0;  // 0 FP64, 1 mixed
   int64_t n = 0, ld = 0;
@@ -45,6 +46,8 @@ struct StepIO {
   // per-cell stimulus protocol (run mode with per-cell first stimulus times)
   double *tb_cell = nullptr;
   double t = 0.0, textlen = 0.0, bcl = 0.0, amp = 0.0;
+  // mixed batches in run mode: Vm as compensated FP32 planes (vm_hi + vm_lo), updated in place
+  float *vm_hi = nullptr, *vm_lo = nullptr;
   double vm_range = 0.0;  // > 0: flag cells whose new |Vm| exceeds it (fused update only)
 };
 
@@ -56,8 +59,11 @@ int n_fp64_vars(int model, int precision);
 cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s);
 int n_shape_variants();
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.
-cudaError_t launch_probe(const double *vm, const int64_t *probe, int64_t n_probe, double *out, int64_t stride,
-                         int64_t k, cudaStream_t s);
+cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
+                         int64_t n_probe, double *out, int64_t stride, int64_t k, cudaStream_t s);
+// Vm planes <-> doubles (the mixed form's Vm between fused runs and the caller's array).
+cudaError_t launch_vm_split(const double *v, float *hi, float *lo, int64_t n, cudaStream_t s);
+cudaError_t launch_vm_join(const float *hi, const float *lo, double *v, int64_t n, cudaStream_t s);
 int sm_count();
 
 }  // namespace cm

@@ -124,14 +124,14 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
 }
 
 // Mixed form: the same update with gates, currents and the fast Ca pools in FP32. Vm, Na_i,
-// K_i and CaSR are accumulated in FP64 (their per-step increments are 1e-7..1e-9 of their
-// values and vanish in FP32); the three buffered-Ca updates use buffered_increment, which is
+// K_i and CaSR are compensated FP32 accumulators (Acc; their per-step increments are
+// 1e-7..1e-9 of their values and vanish in plain FP32); the three buffered-Ca updates use buffered_increment, which is
 // the reference's quadratic rewritten without cancellation. Reversal potentials use
 // log(a/b) = log a - log b with the constant logs precomputed; fractions that share a
 // denominator are combined. row/eca are the FP32 copies of the FP64 tables.
 CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ row, const float *__restrict__ eca,
-                           TT2Cell<float> &c, double &CaSR_d, double &Na_i_d, double &K_i_d,
-                           const TT2Het_<float> &g, float V, float i_external, uint32_t &audit) {
+                           TT2Cell<float> &c, Acc &CaSR_a, Acc &Na_a, Acc &K_a, const TT2Het_<float> &g,
+                           float V, float i_external, uint32_t &audit) {
   const float svolt = V * 1000.f;
   i_external = i_external * C.inv_stim_unit;
   int Caitab = (int)(C.CaiTabConst2 * c.Ca_i + C.CaiTabConst1);
@@ -139,7 +139,7 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
     audit |= 4u;
     Caitab = Caitab < 0 ? 0 : kRows - 1;
   }
-  const float Na_i = (float)Na_i_d, K_i = (float)K_i_d, CaSR = (float)CaSR_d;
+  const float Na_i = Na_a.hi, K_i = K_a.hi, CaSR = CaSR_a.hi;
   const float logKi = flog(K_i);
   const float VminEK = svolt - C.RTONF * (C.logKo - logKi);
   const float VminENa = svolt - C.RTONF * (C.logNao - flog(Na_i));
@@ -182,16 +182,16 @@ CM_HD float tt2_calc_mixed(const TT2Consts<float> &C, const float *__restrict__ 
   const float I_xfer = C.Vxfer * (c.CaSS - c.Ca_i);
   const float SERCA = fdiv(C.Vmaxup * Caisquare, Caisquare + C.Kupsquare);
   const float dCaSR = C.dt1000 * (SERCA - I_rel - I_leak);
-  CaSR_d += (double)buffered_increment(CaSR, dCaSR, C.Bufsr, C.Kbufsr);
+  acc_add(CaSR_a, buffered_increment(CaSR, dCaSR, C.Bufsr, C.Kbufsr));
   const float dCaSS = C.dt1000 * (-I_xfer * C.VcVss + I_rel * C.VsrVss + (-I_CaL * C.inversevssF2 * C.Cm));
   c.CaSS += buffered_increment(c.CaSS, dCaSS, C.Bufss, C.Kbufss);
   const float dCai =
       C.dt1000 * ((-(I_bCa + I_pCa - 2.f * I_NaCa) * C.inverseviF2 * C.Cm) - (SERCA - I_leak) * C.invVcdVsr + I_xfer);
   c.Ca_i += buffered_increment(c.Ca_i, dCai, C.Bufc, C.Kbufc);
   const float dNai = -(I_Na + I_bNa + 3.f * I_NaK + 3.f * I_NaCa) * C.inverseviF * C.Cm;
-  Na_i_d += (double)(C.dt1000 * dNai);
+  acc_add(Na_a, C.dt1000 * dNai);
   const float dKi = -(-i_external + I_K1 + I_to + I_K - 2.f * I_NaK + I_pK) * C.inverseviF * C.Cm;
-  K_i_d += (double)(C.dt1000 * dKi);
+  acc_add(K_a, C.dt1000 * dKi);
   const float CaSS005 = c.CaSS * 20.f;
   const float den = fdiv(1.f, 1.f + CaSS005 * CaSS005);
   const float FCa_INF = 0.6f * den + 0.4f;

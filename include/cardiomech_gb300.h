@@ -195,6 +195,28 @@ int cm_batch_set_launch(cm_batch_t b, int variant, int grid_mode);
  * receives each cell's bits. Clears the bits. */
 int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell);
 
+/* ------------------------------------------------------------------ batched form */
+/* Many batches (instances) of uneven size and mixed model -- e.g. the per-material cell
+ * populations of acCELLerate (acltCellModel.cpp:64-126) or independent simulations -- advanced
+ * together: one persistent kernel launch per time step over tiles of all instances, each
+ * instance with its own stimulus protocol kept on the device, consecutive steps replayed from
+ * a CUDA graph. The instances stay owned by the caller and keep working on their own. Only
+ * CM_PREC_MIXED batches; each instance below 8e7 cells. */
+typedef struct cm_multi_s *cm_multi_t;
+
+int cm_multi_create(cm_multi_t *out, const cm_batch_t *batches, int n_batches, void *stream);
+int cm_multi_destroy(cm_multi_t m);
+/* n_steps of every instance's driver loop (CellModel.h:405-420) in lock step. Vm[i] points at
+ * instance i's n_cells Vm values (host or device), updated in place; stims[i] is its protocol
+ * (textbegin_per_cell not supported here). Returns CM_ERR_NUMERIC when a Vm became NaN. */
+int cm_multi_run(cm_multi_t m, double *const *Vm, int64_t n_steps, const cm_stimulus *stims);
+/* Autotuner of the batched launch: tries tile sizes, block shapes and grid sizes on the
+ * instances themselves (states saved and restored) and keeps the fastest. Any output may be
+ * NULL. */
+int cm_multi_autotune(cm_multi_t m, int n_trial_steps, int *tile_cells, int *shape, int *blocks_per_sm,
+                      double *ms_per_step);
+int cm_multi_set_launch(cm_multi_t m, int tile_cells, int shape, int blocks_per_sm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,91 @@
+"""Batched form on the GPU: instances of uneven size and mixed model in one launch per step
+give the same result, bit for bit, as each instance run alone, for every launch shape and
+with the CUDA-graph replay; the autotuner leaves the cells where they were."""
+import numpy as np
+import pytest
+
+from cardiomechanics_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def build(cm, sizes, models, seed=5):
+    out = []
+    for i, (n, m) in enumerate(zip(sizes, models)):
+        p = cm.Params(m, None, 1e-5)
+        b = cm.Batch(p, n, cm.MIXED)
+        names = W.TT2_HETERO if m == cm.TENTUSSCHER2 else W.CRN_HETERO
+        sc = W.conductance_scales(seed + i, n, 3, 0.8, 1.2)
+        for k, name in enumerate(names):
+            b.add_hetero_value(name, p.get(name) * sc[k])
+        out.append(b)
+    return out
+
+
+def stims(cm, models, bcl=0.3):
+    rng = np.random.default_rng(3)
+    return [dict(textbegin=float(rng.uniform(0, bcl)), textlen=1e-3 if m == cm.TENTUSSCHER2 else 2e-3, bcl=bcl,
+                 amplitude=W.TT2_STIM_NA if m == cm.TENTUSSCHER2 else W.CRN_STIM_PAPF) for m in models]
+
+
+def continued(s, n_steps, dt=1e-5):
+    """The protocol after n_steps of the driver loop: t and textbegin as the driver advanced them."""
+    t, tb = s.get("t0", 0.0), s["textbegin"]
+    for _ in range(n_steps):
+        if t >= tb and t >= tb + s["textlen"]:
+            tb += s["bcl"]
+        t += dt
+    d = dict(s)
+    d["t0"], d["textbegin"] = t, tb
+    return d
+
+
+def test_multi_equals_single(gpu):
+    cm = gpu
+    sizes = [1000, 37, 20000, 4096, 777, 65536]
+    models = [cm.TENTUSSCHER2, cm.COURTEMANCHE, cm.COURTEMANCHE, cm.TENTUSSCHER2, cm.TENTUSSCHER2, cm.COURTEMANCHE]
+    st = stims(cm, models)
+    steps = 3000 + 7  # crosses stimuli; graph replays of 32 steps plus a remainder
+    ref_b = build(cm, sizes, models)
+    ref_v = []
+    for b, s in zip(ref_b, st):
+        v = b.init_vm()
+        # same two segments as the multi below (Vm leaves the device between them)
+        b.run(v, 1000, **s)
+        b.run(v, steps - 1000, **continued(s, 1000))
+        ref_v.append(v)
+    for shape, (tile, bps) in enumerate([(2048, 2), (1024, 4), (4096, 1)]):
+        mb = build(cm, sizes, models)
+        multi = cm.Multi(mb)
+        multi.set_launch(tile, shape, bps)
+        vms = [b.init_vm() for b in mb]
+        multi.run(vms, 1000, st)
+        multi.run(vms, steps - 1000, [continued(x, 1000) for x in st])
+        for i in range(len(mb)):
+            assert np.array_equal(vms[i], ref_v[i]), (shape, i)
+            assert np.array_equal(mb[i].get_state(), ref_b[i].get_state()), (shape, i)
+        assert all(b.audit() == 0 for b in mb)
+
+
+def test_multi_autotune_keeps_state(gpu):
+    cm = gpu
+    sizes = [5000, 3000, 12000]
+    models = [cm.TENTUSSCHER2, cm.COURTEMANCHE, cm.TENTUSSCHER2]
+    mb = build(cm, sizes, models)
+    multi = cm.Multi(mb)
+    s0 = [b.get_state() for b in mb]
+    choice = multi.autotune(2)
+    assert choice["tile_cells"] in (1024, 2048, 4096, 8192, 16384) and choice["ms_per_step"] > 0
+    for b, s in zip(mb, s0):
+        assert np.array_equal(b.get_state(), s)
+    vms = [b.init_vm() for b in mb]
+    multi.run(vms, 64, stims(cm, models))
+    assert all(np.all(np.isfinite(v)) for v in vms)
+
+
+def test_multi_rejects_fp64(gpu):
+    cm = gpu
+    b = cm.Batch(cm.Params(5, None, 1e-5), 10, cm.FP64)
+    with pytest.raises(cm.CMError) as e:
+        cm.Multi([b])
+    assert e.value.code == -7

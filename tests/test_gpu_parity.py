@@ -6,6 +6,9 @@ Tolerances:
                 upstroke within 1e-3 ms of the oracle.
   mixed batches APD90 within 1 ms, upstroke within 0.1 ms, RMS Vm error <= 0.5 mV per cell.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -101,10 +104,27 @@ def test_trace_mixed(gpu, port, model):
     S = b.get_state(gpu.LAYOUT_SOA)
     ref_soa = B[:, [c for c in range(B.shape[1]) if (c < 5 or c >= 23)]].T if model == 5 else \
         B[:, [c for c in range(22) if c != 20]].T
-    # per-state error after 3 beats, relative to the state's scale over the population
-    scale = np.maximum(np.abs(ref_soa).max(axis=1), 1e-12)
-    err = np.abs(S - ref_soa).max(axis=1) / scale
-    assert err.max() < 1e-3, dict(zip(gpu.state_names(model), err))
+    # per-quantity error after 3 beats: gates (in [0, 1]) absolute, concentrations relative
+    names = gpu.state_names(model)
+    conc = {"Ca_i", "CaSR", "CaSS", "Na_i", "K_i", "Ca_up", "Ca_rel", "Ca_TRPN"}
+    report = {"model": "TenTusscher2" if model == 5 else "CourtemancheEtAl", "cells": int(S.shape[1]),
+              "beats": 3, "bcl_ms": 800, "conductance_jitter": 0.1,
+              "vm_rms_mv_max": float(rms.max() * 1e3), "vm_max_abs_mv": float(np.abs(tr - tro).max() * 1e3),
+              "apd90_max_abs_ms": float(np.nanmax(np.abs(a - ao)) * 1e3),
+              "upstroke_max_abs_ms": float(np.nanmax(np.abs(u - uo)) * 1e3), "states": {}}
+    for k, name in enumerate(names):
+        d = np.abs(S[k] - ref_soa[k]).max()
+        if name in conc:
+            rel = float(d / np.abs(ref_soa[k]).max())
+            report["states"][name] = {"max_rel_err": rel}
+            assert rel < 5e-3, (name, rel)
+        else:
+            report["states"][name] = {"max_abs_err": float(d)}
+            assert d < 2e-3, (name, d)
+    out = os.environ.get("CM_REPORT_DIR")
+    if out:
+        with open(os.path.join(out, f"accuracy_mixed_{TAG[model]}.json"), "w") as f:
+            json.dump(report, f, indent=1)
 
 
 def test_device_pointers_and_step_equals_run(gpu):
