@@ -43,6 +43,11 @@ ABI_SYMBOLS = (
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
+    "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
+    "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
+    "cm_surrogate_destroy", "cm_surrogate_mlp", "cm_surrogate_generate", "cm_surrogate_dataset",
+    "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
+    "cm_batch_run_surrogate",
 )
 
 
@@ -62,6 +67,14 @@ class Stimulus(ctypes.Structure):
     _fields_ = [("t0", ctypes.c_double), ("textbegin", ctypes.c_double),
                 ("textbegin_per_cell", ctypes.POINTER(ctypes.c_double)), ("textlen", ctypes.c_double),
                 ("bcl", ctypes.c_double), ("amplitude", ctypes.c_double)]
+
+
+class SurrogateStats(ctypes.Structure):
+    _fields_ = [("cell_macro_steps", ctypes.c_int64), ("surrogate", ctypes.c_int64), ("fallback", ctypes.c_int64),
+                ("audited", ctypes.c_int64), ("max_audit_err_mv", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -107,6 +120,28 @@ def lib() -> ctypes.CDLL:
     L.cm_multi_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.cm_multi_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.cm_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, vp]
+    L.cm_mlp_destroy.argtypes = [vp]
+    L.cm_mlp_n_params.argtypes = [vp]
+    L.cm_mlp_n_params.restype = ctypes.c_int64
+    for f in ("cm_mlp_get_params", "cm_mlp_set_params", "cm_mlp_get_grads"):
+        getattr(L, f).argtypes = [vp, vp]
+    L.cm_mlp_forward.argtypes = [vp, vp, i64, vp]
+    L.cm_mlp_loss_grad.argtypes = [vp, vp, vp, i64, fp]
+    L.cm_mlp_adam_step.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+    L.cm_surrogate_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.c_int, ctypes.c_uint64, vp]
+    L.cm_surrogate_destroy.argtypes = [vp]
+    L.cm_surrogate_mlp.argtypes = [vp, ctypes.POINTER(vp)]
+    L.cm_surrogate_generate.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), i64, i64, ctypes.POINTER(i64)]
+    L.cm_surrogate_dataset.argtypes = [vp, ctypes.POINTER(i64), vp, vp]
+    L.cm_surrogate_fit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint64, fp]
+    L.cm_surrogate_blob_size.argtypes = [vp]
+    L.cm_surrogate_blob_size.restype = ctypes.c_int64
+    L.cm_surrogate_get_blob.argtypes = [vp, vp]
+    L.cm_surrogate_set_blob.argtypes = [vp, vp]
+    L.cm_batch_run_surrogate.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(SurrogateStats)]
     L.cm_diag_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
     _lib = L
     return L
@@ -291,6 +326,17 @@ class Batch:
     def set_launch(self, variant: int, grid_mode: int = 0) -> None:
         _check(lib().cm_batch_set_launch(self._h, variant, grid_mode))
 
+    def run_surrogate(self, surrogate, Vm, n_macro, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0,
+                      t0=0.0, mode=0, audit_mod=100):
+        """n_macro learned macro steps (surrogate.substeps fine steps each); Vm updated in place.
+        mode 0: coarse step + network, 1: coarse step alone. Returns the run statistics."""
+        Vm = _f64(Vm, self.n, "Vm")
+        st = Stimulus(t0, textbegin, None, textlen, bcl, amplitude)
+        stats = SurrogateStats()
+        _check(lib().cm_batch_run_surrogate(self._h, surrogate._h, _ptr(Vm), int(n_macro), ctypes.byref(st), mode,
+                                            audit_mod, ctypes.byref(stats)))
+        return stats.as_dict()
+
     def audit(self, per_cell: bool = False):
         m = ctypes.c_uint32()
         pc = np.zeros(self.n, np.uint32) if per_cell else None
@@ -335,3 +381,126 @@ class Multi:
 
     def set_launch(self, tile_cells, shape=0, blocks_per_sm=2):
         _check(lib().cm_multi_set_launch(self._h, tile_cells, shape, blocks_per_sm))
+
+
+def _f32(a, n, name):
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != n:
+            raise ValueError(f"{name}: need a contiguous float32 array of {n} elements")
+        return a
+    if a.numel() != n or not a.is_contiguous():
+        raise ValueError(f"{name}: need a contiguous float32 tensor of {n} elements")
+    return a
+
+
+class Mlp:
+    """The surrogate's network: n_in -> H -> H -> n_out, tanh, BF16 tensor-core GEMMs, FP32 Adam."""
+
+    def __init__(self, n_in=22, n_hidden=128, n_out=19, seed=1, stream=None, _borrow=None):
+        self.n_in, self.n_hidden, self.n_out = n_in, n_hidden, n_out
+        if _borrow is not None:
+            self._h, self._owned = _borrow, False
+        else:
+            h = ctypes.c_void_p()
+            s = None if stream is None else ctypes.c_void_p(int(stream))
+            _check(lib().cm_mlp_create(ctypes.byref(h), n_in, n_hidden, n_out, seed, s))
+            self._h, self._owned = h, True
+        self.n_params = int(lib().cm_mlp_n_params(self._h))
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_mlp_destroy(self._h)
+            self._h = None
+
+    def shapes(self):
+        H = self.n_hidden
+        return [(H, self.n_in), (H,), (H, H), (H,), (self.n_out, H), (self.n_out,)]
+
+    def _split(self, flat):
+        out, k = [], 0
+        for shp in self.shapes():
+            n = int(np.prod(shp))
+            out.append(flat[k:k + n].reshape(shp))
+            k += n
+        return out
+
+    def get_params(self):
+        out = np.zeros(self.n_params, np.float32)
+        _check(lib().cm_mlp_get_params(self._h, out.ctypes.data))
+        return self._split(out)
+
+    def set_params(self, params):
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float32).ravel() for p in params]))
+        _check(lib().cm_mlp_set_params(self._h, flat.ctypes.data))
+
+    def get_grads(self):
+        out = np.zeros(self.n_params, np.float32)
+        _check(lib().cm_mlp_get_grads(self._h, out.ctypes.data))
+        return self._split(out)
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], self.n_out), np.float32)
+        _check(lib().cm_mlp_forward(self._h, X.ctypes.data, X.shape[0], Y.ctypes.data))
+        return Y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        loss = ctypes.c_float()
+        _check(lib().cm_mlp_loss_grad(self._h, X.ctypes.data, T.ctypes.data, X.shape[0], ctypes.byref(loss)))
+        return loss.value
+
+    def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(lib().cm_mlp_adam_step(self._h, lr, beta1, beta2, eps))
+
+
+class Surrogate:
+    """Learned macro step for TenTusscher2 (coarse physics step of substeps*dt + MLP residual)."""
+
+    def __init__(self, params: Params, substeps=10, seed=1, stream=None):
+        h = ctypes.c_void_p()
+        s = None if stream is None else ctypes.c_void_p(int(stream))
+        _check(lib().cm_surrogate_create(ctypes.byref(h), params._h, substeps, seed, s))
+        self._h = h
+        self.substeps = substeps
+        m = ctypes.c_void_p()
+        _check(lib().cm_surrogate_mlp(self._h, ctypes.byref(m)))
+        self.mlp = Mlp(_borrow=m)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            self.mlp = None
+            _lib.cm_surrogate_destroy(self._h)
+            self._h = None
+
+    def generate(self, batch, Vm, n_macro, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0, t0=0.0,
+                 cell_stride=1, max_pairs=10_000_000):
+        Vm = _f64(Vm, batch.n, "Vm")
+        st = Stimulus(t0, textbegin, None, textlen, bcl, amplitude)
+        n = ctypes.c_int64()
+        _check(lib().cm_surrogate_generate(self._h, batch._h, _ptr(Vm), int(n_macro), ctypes.byref(st),
+                                           int(cell_stride), int(max_pairs), ctypes.byref(n)))
+        return n.value
+
+    def dataset(self):
+        n = ctypes.c_int64()
+        _check(lib().cm_surrogate_dataset(self._h, ctypes.byref(n), None, None))
+        X = np.zeros((n.value, 22), np.float32)
+        T = np.zeros((n.value, 19), np.float32)
+        _check(lib().cm_surrogate_dataset(self._h, ctypes.byref(n), X.ctypes.data, T.ctypes.data))
+        return X, T
+
+    def fit(self, batch=4096, steps=2000, lr=1e-3, seed=1):
+        loss = ctypes.c_float()
+        _check(lib().cm_surrogate_fit(self._h, batch, steps, lr, seed, ctypes.byref(loss)))
+        return loss.value
+
+    def get_blob(self):
+        out = np.zeros(int(lib().cm_surrogate_blob_size(self._h)), np.float32)
+        _check(lib().cm_surrogate_get_blob(self._h, out.ctypes.data))
+        return out
+
+    def set_blob(self, blob):
+        b = np.ascontiguousarray(blob, np.float32)
+        _check(lib().cm_surrogate_set_blob(self._h, b.ctypes.data))

@@ -9,70 +9,19 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cardiomech_gb300.h"
-#include "cm_launch.h"
+#include "cm_handles.h"
 #include "cm_multi.h"
-#include "cm_params.h"
 
 using namespace cm;
 
-struct cm_params_s {
-  ParamSet ps;
-};
-
-struct cm_batch_s {
-  ParamSet ps;
-  DevBatch d;
-  cudaStream_t stream = nullptr;
-  void *state_mem = nullptr;   // one allocation: FP64 block then FP32 block
-  void *table_mem = nullptr;   // rows/eca in FP64 (FP64 batches) or FP32 (mixed)
-  void *het_mem[6] = {};
-  uint32_t *audit_cell = nullptr;
-  unsigned int *audit_or = nullptr;
-  double *diag = nullptr;
-  bool diag_on = false;
-  // staging buffers for host arrays, grown on demand
-  double *stage[4] = {};
-  int64_t stage_n = 0;
-  double *tb_cell = nullptr;
-  float *vm_planes = nullptr;  // mixed batches: Vm as hi/lo planes during fused runs (2 x n)
-  int64_t *probe_idx = nullptr;
-  int64_t probe_cap = 0;
-  double *probe_out = nullptr;
-  int64_t probe_out_cap = 0;
-};
+std::string &cm::last_error() {
+  thread_local std::string e;
+  return e;
+}
 
 namespace {
 
-thread_local std::string g_err;
-
-int fail(int code, const std::string &msg) {
-  g_err = msg;
-  return code;
-}
-
-int cuda_fail(cudaError_t e, const char *what) {
-  g_err = std::string(what) + ": " + cudaGetErrorString(e);
-  return CM_ERR_CUDA;
-}
-
-#define CK(call)                                   \
-  do {                                             \
-    cudaError_t e_ = (call);                       \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-  } while (0)
-
-bool is_device_ptr(const void *p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
-int64_t round_ld(int64_t n) { return ((n + 63) / 64) * 64; }
+int64_t round_ld(int64_t n) { return ((n + 255) / 256) * 256; }  // whole staged tiles
 
 // SOA index (model order) -> plane of the mixed layout; `pair` variables are compensated
 // accumulators stored as hi (plane slot) and lo (plane slot + 1).
@@ -221,7 +170,7 @@ extern "C" {
 
 int cm_abi_version(void) { return CM_ABI_VERSION; }
 
-const char *cm_last_error(void) { return g_err.c_str(); }
+const char *cm_last_error(void) { return cm::last_error().c_str(); }
 
 int cm_model_from_name(const char *name) { return model_from_name(name); }
 
@@ -342,9 +291,9 @@ int cm_batch_create(cm_batch_t *out, cm_params_t p, int64_t n_cells, int precisi
   }
   if (!rc) rc = cm_batch_reset(b);
   if (rc) {
-    std::string keep = g_err;
+    std::string keep = cm::last_error();
     cm_batch_destroy(b);
-    g_err = keep;
+    cm::last_error() = keep;
     return rc;
   }
   *out = b;
@@ -430,7 +379,10 @@ int cm_batch_set_hetero(cm_batch_t b, const char *name, const double *values) {
   if (is_device_ptr(values)) CK(cudaMemcpy(host.data(), values, n * sizeof(double), cudaMemcpyDeviceToHost));
   else memcpy(host.data(), values, n * sizeof(double));
   const size_t es = b->d.precision == CM_PREC_FP64 ? sizeof(double) : sizeof(float);
-  if (!b->het_mem[slot]) CK(cudaMalloc(&b->het_mem[slot], std::max<int64_t>(1, n) * es));
+  if (!b->het_mem[slot]) {  // padded to ld: staged kernels copy whole tiles
+    CK(cudaMalloc(&b->het_mem[slot], std::max<int64_t>(1, b->d.ld) * es));
+    CK(cudaMemset(b->het_mem[slot], 0, std::max<int64_t>(1, b->d.ld) * es));
+  }
   if (b->d.precision == CM_PREC_FP64) {
     CK(cudaMemcpy(b->het_mem[slot], host.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   } else {
@@ -606,9 +558,9 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   io.vm_out = dvm;
   const bool planes = b->d.precision == CM_PREC_MIXED;
   if (planes) {
-    if (!b->vm_planes) CK(cudaMalloc(&b->vm_planes, std::max<int64_t>(1, 2 * n) * sizeof(float)));
+    if (!b->vm_planes) CK(cudaMalloc(&b->vm_planes, std::max<int64_t>(1, 2 * b->d.ld) * sizeof(float)));
     io.vm_hi = b->vm_planes;
-    io.vm_lo = b->vm_planes + n;
+    io.vm_lo = b->vm_planes + b->d.ld;
     io.vm = nullptr;
     io.vm_out = nullptr;
     CK(launch_vm_split(dvm, io.vm_hi, io.vm_lo, n, b->stream));
@@ -680,16 +632,17 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
   unsigned int audit_saved = 0;
   // trial Vm: compensated planes (hi, lo) of the rest potential, 2 x n floats in n doubles
   const Acc a0 = acc_from_double(b->ps.init_vm());
-  std::vector<float> v0(2 * n, a0.hi);
-  std::fill(v0.begin() + n, v0.end(), a0.lo);
+  const int64_t ld = b->d.ld;
+  std::vector<float> v0(2 * ld, a0.hi);
+  std::fill(v0.begin() + ld, v0.end(), a0.lo);
   cudaError_t e = cudaMalloc(&saved, bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&vm, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&vm, 2 * ld * sizeof(float));
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   if (e == cudaSuccess) e = cudaMemcpyAsync(saved, b->state_mem, bytes, cudaMemcpyDeviceToDevice, b->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&audit_saved, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(vm, v0.data(), 2 * n * sizeof(float), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(vm, v0.data(), 2 * ld * sizeof(float), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   const int grid_modes[] = {0, 2, 4, 8};
   for (int v = 0; e == cudaSuccess && v < n_shape_variants(); v++) {
@@ -698,8 +651,8 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
       d.variant = v;
       d.grid_mode = g;
       StepIO io;
-      io.vm_hi = (float *)vm;  // the trial Vm as compensated planes (2 x n floats fit in n doubles)
-      io.vm_lo = (float *)vm + n;
+      io.vm_hi = (float *)vm;  // the trial Vm as compensated planes
+      io.vm_lo = (float *)vm + ld;
       for (int k = 0; k < 2 && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
       if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
       for (int k = 0; k < n_trial_steps && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
@@ -827,9 +780,9 @@ int multi_prepare(cm_multi_s *m, double *const *Vm, const cm_stimulus *stims, st
       CK(cudaMemcpyAsync(m->vm_stage[i], v, b->d.n * sizeof(double), cudaMemcpyHostToDevice, m->stream));
       v = m->vm_stage[i];
     }
-    if (!m->vm_planes[i]) CK(cudaMalloc(&m->vm_planes[i], std::max<int64_t>(1, 2 * b->d.n) * sizeof(float)));
+    if (!m->vm_planes[i]) CK(cudaMalloc(&m->vm_planes[i], std::max<int64_t>(1, 2 * b->d.ld) * sizeof(float)));
     insts[i].vm_hi = m->vm_planes[i];
-    insts[i].vm_lo = m->vm_planes[i] + b->d.n;
+    insts[i].vm_lo = m->vm_planes[i] + b->d.ld;
     m->vm_dev[i] = v;
     if (v) CK(launch_vm_split(v, insts[i].vm_hi, insts[i].vm_lo, b->d.n, m->stream));
     const cm_stimulus st = stims ? stims[i] : cm_stimulus{0, 0, nullptr, 0, 0, 0};
@@ -917,9 +870,9 @@ int cm_multi_create(cm_multi_t *out, const cm_batch_t *batches, int n_batches, v
   if (e != cudaSuccess) rc = cuda_fail(e, "cm_multi_create");
   if (!rc) rc = multi_build_tiles(m, m->tile_cells);
   if (rc) {
-    std::string keep = g_err;
+    std::string keep = cm::last_error();
     cm_multi_destroy(m);
-    g_err = keep;
+    cm::last_error() = keep;
     return rc;
   }
   *out = m;
@@ -951,7 +904,7 @@ int cm_multi_run(cm_multi_t m, double *const *Vm, int64_t n_steps, const cm_stim
   std::vector<unsigned int> masks(m->batches.size(), 0);
   for (size_t i = 0; i < m->batches.size(); i++) {
     const int64_t ni = m->batches[i]->d.n;
-    CK(launch_vm_join(m->vm_planes[i], m->vm_planes[i] + ni, m->vm_dev[i], ni, m->stream));
+    CK(launch_vm_join(m->vm_planes[i], m->vm_planes[i] + m->batches[i]->d.ld, m->vm_dev[i], ni, m->stream));
     if (host_vm[i])
       CK(cudaMemcpyAsync(Vm[i], m->vm_stage[i], m->batches[i]->d.n * sizeof(double), cudaMemcpyDeviceToHost,
                          m->stream));

@@ -1,0 +1,70 @@
+// Handle structures and shared helpers of the C ABI implementation (cm_capi.cpp, cm_sur_api.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cardiomech_gb300.h"
+#include "cm_launch.h"
+#include "cm_params.h"
+
+struct cm_params_s {
+  cm::ParamSet ps;
+};
+
+struct cm_batch_s {
+  cm::ParamSet ps;
+  cm::DevBatch d;
+  cudaStream_t stream = nullptr;
+  void *state_mem = nullptr;   // one allocation: FP64 block then FP32 block
+  void *table_mem = nullptr;   // rows/eca in FP64 (FP64 batches) or FP32 (mixed)
+  void *het_mem[6] = {};
+  uint32_t *audit_cell = nullptr;
+  unsigned int *audit_or = nullptr;
+  double *diag = nullptr;
+  bool diag_on = false;
+  // staging buffers for host arrays, grown on demand
+  double *stage[4] = {};
+  int64_t stage_n = 0;
+  double *tb_cell = nullptr;
+  float *vm_planes = nullptr;  // mixed batches: Vm as hi/lo planes during fused runs (2 x n)
+  int64_t *probe_idx = nullptr;
+  int64_t probe_cap = 0;
+  double *probe_out = nullptr;
+  int64_t probe_out_cap = 0;
+};
+
+
+namespace cm {
+
+std::string &last_error();
+
+inline int fail(int code, const std::string &msg) {
+  last_error() = msg;
+  return code;
+}
+
+inline int cuda_fail(cudaError_t e, const char *what) {
+  last_error() = std::string(what) + ": " + cudaGetErrorString(e);
+  return CM_ERR_CUDA;
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cm::cuda_fail(e_, #call); \
+  } while (0)
+
+inline bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace cm

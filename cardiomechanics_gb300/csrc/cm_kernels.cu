@@ -231,7 +231,9 @@ void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, 
 }
 }  // namespace
 
-int n_shape_variants() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
+// Variants past the register-budget shapes are the shared-memory-staged kernels (256 and
+// 128 threads per block); they apply to fused runs and fall back to shape 0 elsewhere.
+int n_shape_variants() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])) + 2; }
 
 cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s) {
   if (b.n == 0) return cudaSuccess;
@@ -253,6 +255,11 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     return cudaGetLastError();
   }
   if (variant < 0 || variant >= n_shape_variants()) variant = 0;
+  const int n_plain = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+  if (variant >= n_plain) {
+    if (staged_supported(b, io)) return launch_staged(b, io, variant == n_plain ? 256 : 128, grid_mode, s);
+    variant = 0;
+  }
   const Shape sh = kShapes[variant];
   const int64_t need = (b.n + sh.block - 1) / sh.block;
   // grid_mode 0: one thread per cell; k > 0: grid-stride over k blocks per SM

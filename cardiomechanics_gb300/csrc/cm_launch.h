@@ -58,6 +58,10 @@ int n_fp64_vars(int model, int precision);
 // per cell, k > 0 = grid-stride loop over k blocks per SM.
 cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s);
 int n_shape_variants();
+// Shared-memory-staged mixed kernels (cm_staged.cu): fused runs only (Vm planes, uniform
+// stimulus, leading dimension a multiple of 256, planes lo = hi + ld).
+bool staged_supported(const DevBatch &b, const StepIO &io);
+cudaError_t launch_staged(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s);
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.
 cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
                          int64_t n_probe, double *out, int64_t stride, int64_t k, cudaStream_t s);

@@ -1,0 +1,467 @@
+// The surrogate's MLP (n_in -> H -> H -> n_out, tanh): BF16 operands with FP32 accumulation on
+// the tensor cores (mma.sync m16n8k16), FP32 master weights and Adam. Training runs as a
+// sequence of small GEMMs with fused epilogues:
+//   forward   Z1 = X W1^T + b1, H1 = tanh Z1;  Z2 = H1 W2^T + b2, H2 = tanh Z2;  Y = H2 W3^T + b3
+//   loss      L = mean over samples and real outputs of (Y - T)^2, dY = dL/dY (padding masked)
+//   backward  dZ2 = (dY W3) * (1 - H2^2);  dZ1 = (dZ2 W2) * (1 - H1^2)
+//             dW3 = dY^T H2, dW2 = dZ2^T H1, dW1 = dZ1^T X, db = column sums
+// Every GEMM is C[m][n] = sum_k A[m][k] B[n][k] over row-major BF16 operands ("NT"), so the
+// backward products first transpose their operands with a small kernel. Dimensions are padded:
+// n_in to 32, n_out to 32, the batch to a multiple of 64.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "cm_mlp.h"
+
+namespace cm {
+
+namespace {
+
+__device__ __forceinline__ uint32_t ld_u32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+enum Epi { EPI_BIAS_TANH = 0, EPI_BIAS_F32 = 1, EPI_DTANH = 2, EPI_F32 = 3 };
+
+struct EpiArgs {
+  const float *bias;           // EPI_BIAS_*: per column n
+  __nv_bfloat16 *out_bf16;     // EPI_BIAS_TANH, EPI_DTANH
+  float *out_f32;              // EPI_BIAS_F32, EPI_F32
+  const __nv_bfloat16 *h;      // EPI_DTANH: tanh output of the layer, same shape as C
+  int ldc;
+};
+
+// C = A B^T, A: M x K (lda), B: N x K (ldb), K % 32 == 0. 64x64 block tile, 4 warps of 32x32.
+template <int EPI>
+__global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__ A, int lda,
+                                               const __nv_bfloat16 *__restrict__ B, int ldb, int M, int N, int K,
+                                               EpiArgs e) {
+  constexpr int BM = 64, BN = 64, BK = 32, LDS = BK + 8;
+  __shared__ __align__(16) __nv_bfloat16 As[BM][LDS];
+  __shared__ __align__(16) __nv_bfloat16 Bs[BN][LDS];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  float acc[2][4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    // 64 rows x 32 bf16 = 4 chunks of 16 B per row; 256 chunks per operand, 2 per thread
+    for (int i = tid; i < 256; i += 128) {
+      const int r = i >> 2, cc = (i & 3) * 8;
+      uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
+      if (m0 + r < M) va = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * lda + k0 + cc);
+      if (n0 + r < N) vb = *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + r) * ldb + k0 + cc);
+      *reinterpret_cast<uint4 *>(&As[r][cc]) = va;
+      *reinterpret_cast<uint4 *>(&Bs[r][cc]) = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int mi = 0; mi < 2; mi++) {
+        const int r = wm + mi * 16 + g;
+        af[mi][0] = ld_u32(&As[r][kk + 2 * t]);
+        af[mi][1] = ld_u32(&As[r + 8][kk + 2 * t]);
+        af[mi][2] = ld_u32(&As[r][kk + 2 * t + 8]);
+        af[mi][3] = ld_u32(&As[r + 8][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int ni = 0; ni < 4; ni++) {
+        const int c = wn + ni * 8 + g;
+        bfr[ni][0] = ld_u32(&Bs[c][kk + 2 * t]);
+        bfr[ni][1] = ld_u32(&Bs[c][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+        for (int ni = 0; ni < 4; ni++) mma_bf16(acc[mi][ni], af[mi], bfr[ni]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+    for (int ni = 0; ni < 4; ni++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int m = m0 + wm + mi * 16 + g + (q >> 1) * 8;
+        const int n = n0 + wn + ni * 8 + 2 * t + (q & 1);
+        if (m >= M || n >= N) continue;
+        float v = acc[mi][ni][q];
+        const size_t o = (size_t)m * e.ldc + n;
+        if (EPI == EPI_BIAS_TANH) {
+          e.out_bf16[o] = __float2bfloat16(tanh_fast(v + e.bias[n]));
+        } else if (EPI == EPI_BIAS_F32) {
+          e.out_f32[o] = v + e.bias[n];
+        } else if (EPI == EPI_DTANH) {
+          const float h = __bfloat162float(e.h[o]);
+          e.out_bf16[o] = __float2bfloat16(v * (1.f - h * h));
+        } else {
+          e.out_f32[o] = v;
+        }
+      }
+}
+
+// out[c][r] = in[r][c] for a rows x cols BF16 matrix.
+__global__ void transpose_bf16(const __nv_bfloat16 *__restrict__ in, __nv_bfloat16 *__restrict__ out, int rows,
+                               int cols) {
+  __shared__ __nv_bfloat16 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = by + j, c = bx + threadIdx.x;
+    tile[j][threadIdx.x] = (r < rows && c < cols) ? in[(size_t)r * cols + c] : __float2bfloat16(0.f);
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int c = bx + j, r = by + threadIdx.x;
+    if (c < cols && r < rows) out[(size_t)c * rows + r] = tile[threadIdx.x][j];
+  }
+}
+
+// dY = 2 (Y - T) / (n * n_out) on the real outputs (padding columns and rows masked), loss sum.
+__global__ void mse_grad(const float *__restrict__ Y, const float *__restrict__ T, int n, int n_real_rows, int n_out,
+                         int ldy, __nv_bfloat16 *__restrict__ dY, float *loss) {
+  __shared__ float red[256];
+  float s = 0.f;
+  const float scale = 2.f / ((float)n_real_rows * (float)n_out);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * ldy; i += gridDim.x * blockDim.x) {
+    const int r = i / ldy, c = i - r * ldy;
+    float d = 0.f;
+    if (r < n_real_rows && c < n_out) {
+      d = Y[i] - T[(size_t)r * n_out + c];
+      s += d * d;
+    }
+    dY[i] = __float2bfloat16(d * scale);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, red[0] / ((float)n_real_rows * (float)n_out));
+}
+
+// db[c] = sum_r dZ[r][c]
+__global__ void colsum_bf16(const __nv_bfloat16 *__restrict__ dZ, int rows, int cols, float *__restrict__ db) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; r++) s += __bfloat162float(dZ[(size_t)r * cols + c]);
+  db[c] = s;
+}
+
+// Adam on FP32 master weights (Kingma & Ba 2015), then the BF16 operand copy.
+__global__ void adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                     __nv_bfloat16 *__restrict__ wb, int n, float lr, float b1, float b2, float eps, float c1,
+                     float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  w[i] = wi;
+  if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+__global__ void to_bf16(const float *__restrict__ in, __nv_bfloat16 *__restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __float2bfloat16(in[i]);
+}
+
+// X rows (n_in real features, fp32) -> padded BF16 rows (ld = in_pad); rows beyond n zero.
+__global__ void pack_inputs(const float *__restrict__ X, int n, int n_in, int rows_pad, int in_pad,
+                            __nv_bfloat16 *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows_pad * in_pad; i += gridDim.x * blockDim.x) {
+    const int r = i / in_pad, c = i - r * in_pad;
+    out[i] = __float2bfloat16((r < n && c < n_in) ? X[(size_t)r * n_in + c] : 0.f);
+  }
+}
+
+// Gather a minibatch: rows idx[k] of X (n_in) and T (n_out).
+__global__ void gather_rows(const float *__restrict__ X, const float *__restrict__ T, const int64_t *__restrict__ idx,
+                            int nb, int n_in, int n_out, float *__restrict__ Xb, float *__restrict__ Tb) {
+  const int r = blockIdx.x;
+  if (r >= nb) return;
+  const int64_t s = idx[r];
+  for (int c = threadIdx.x; c < n_in; c += blockDim.x) Xb[(size_t)r * n_in + c] = X[s * n_in + c];
+  for (int c = threadIdx.x; c < n_out; c += blockDim.x) Tb[(size_t)r * n_out + c] = T[s * n_out + c];
+}
+
+template <int EPI>
+cudaError_t gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, EpiArgs e,
+                 cudaStream_t s) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  gemm_nt<EPI><<<grid, 128, 0, s>>>(A, lda, B, ldb, M, N, K, e);
+  return cudaGetLastError();
+}
+
+cudaError_t transpose(const __nv_bfloat16 *in, __nv_bfloat16 *out, int rows, int cols, cudaStream_t s) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  transpose_bf16<<<grid, block, 0, s>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+#define MCK(x)                            \
+  do {                                    \
+    cudaError_t e_ = (x);                 \
+    if (e_ != cudaSuccess) return e_;     \
+  } while (0)
+
+cudaError_t Mlp::init(int n_in_, int n_hidden_, int n_out_, uint64_t seed, cudaStream_t s) {
+  n_in = n_in_;
+  H = n_hidden_;
+  n_out = n_out_;
+  stream = s;
+  in_pad = ((n_in + 31) / 32) * 32;
+  out_pad = ((n_out + 31) / 32) * 32;
+  // parameter block (FP32 masters, padded shapes): W1 H x in_pad, b1 H, W2 H x H, b2 H, W3 out_pad x H, b3 out_pad
+  off[0] = 0;
+  size[0] = (size_t)H * in_pad;
+  size[1] = H;
+  size[2] = (size_t)H * H;
+  size[3] = H;
+  size[4] = (size_t)out_pad * H;
+  size[5] = out_pad;
+  for (int k = 1; k < 6; k++) off[k] = off[k - 1] + size[k - 1];
+  n_params = off[5] + size[5];
+  MCK(cudaMalloc(&w, n_params * sizeof(float)));
+  MCK(cudaMalloc(&g, n_params * sizeof(float)));
+  MCK(cudaMalloc(&m1, n_params * sizeof(float)));
+  MCK(cudaMalloc(&m2, n_params * sizeof(float)));
+  MCK(cudaMalloc(&wb, n_params * sizeof(__nv_bfloat16)));
+  MCK(cudaMalloc(&wt, n_params * sizeof(__nv_bfloat16)));
+  MCK(cudaMalloc(&loss, sizeof(float)));
+  MCK(cudaMemsetAsync(m1, 0, n_params * sizeof(float), stream));
+  MCK(cudaMemsetAsync(m2, 0, n_params * sizeof(float), stream));
+  // Glorot-uniform weights from a counter-based generator, zero biases; padded rows/cols zero
+  std::vector<float> h(n_params, 0.f);
+  auto u01 = [&](uint64_t k) {
+    uint64_t z = (seed << 32) + k + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  uint64_t ctr = 0;
+  auto fill = [&](int blk, int rows, int cols, int real_rows, int real_cols, int fan_in, int fan_out) {
+    const double a = std::sqrt(6.0 / (fan_in + fan_out));
+    for (int r = 0; r < rows; r++)
+      for (int c = 0; c < cols; c++) {
+        const double u = u01(ctr++);
+        h[off[blk] + (size_t)r * cols + c] = (r < real_rows && c < real_cols) ? (float)((2 * u - 1) * a) : 0.f;
+      }
+  };
+  fill(0, H, in_pad, H, n_in, n_in, H);
+  fill(2, H, H, H, H, H, H);
+  fill(4, out_pad, H, n_out, H, H, n_out);
+  MCK(cudaMemcpyAsync(w, h.data(), n_params * sizeof(float), cudaMemcpyHostToDevice, stream));
+  step = 0;
+  return sync_bf16();
+}
+
+cudaError_t Mlp::sync_bf16() {
+  to_bf16<<<(unsigned)((n_params + 255) / 256), 256, 0, stream>>>(w, wb, (int)n_params);
+  MCK(cudaGetLastError());
+  // transposed copies for the backward products: W3^T (H x out_pad), W2^T (H x H)
+  MCK(transpose(wb + off[4], wt + off[4], out_pad, H, stream));
+  MCK(transpose(wb + off[2], wt + off[2], H, H, stream));
+  return cudaSuccess;
+}
+
+void Mlp::release() {
+  for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)wt, (void *)loss, (void *)ws})
+    cudaFree(p);
+  w = g = m1 = m2 = nullptr;
+  wb = wt = nullptr;
+  loss = nullptr;
+  ws = nullptr;
+  ws_rows = 0;
+}
+
+cudaError_t Mlp::workspace(int rows) {
+  if (rows <= ws_rows) return cudaSuccess;
+  cudaFree(ws);
+  ws = nullptr;
+  ws_rows = 0;
+  // X, XT, H1, H1T, H2, H2T, dZ1, dZ1T, dZ2, dZ2T, dY, dYT (bf16) + Y, Xf, Tf (f32)
+  const size_t b16 = (size_t)rows * (2 * in_pad + 8 * H + 2 * out_pad);
+  const size_t f32 = (size_t)rows * (out_pad + n_in + n_out);
+  MCK(cudaMalloc(&ws, b16 * 2 + f32 * 4 + 64));
+  ws_rows = rows;
+  return cudaSuccess;
+}
+
+Mlp::Buffers Mlp::buffers(int rows) const {
+  Buffers B;
+  __nv_bfloat16 *p = (__nv_bfloat16 *)ws;
+  auto take = [&](size_t n) {
+    __nv_bfloat16 *q = p;
+    p += n;
+    return q;
+  };
+  B.X = take((size_t)rows * in_pad);
+  B.XT = take((size_t)rows * in_pad);
+  B.H1 = take((size_t)rows * H);
+  B.H1T = take((size_t)rows * H);
+  B.H2 = take((size_t)rows * H);
+  B.H2T = take((size_t)rows * H);
+  B.dZ1 = take((size_t)rows * H);
+  B.dZ1T = take((size_t)rows * H);
+  B.dZ2 = take((size_t)rows * H);
+  B.dZ2T = take((size_t)rows * H);
+  B.dY = take((size_t)rows * out_pad);
+  B.dYT = take((size_t)rows * out_pad);
+  float *f = reinterpret_cast<float *>(p);
+  B.Y = f;
+  B.Xf = f + (size_t)rows * out_pad;
+  B.Tf = B.Xf + (size_t)rows * n_in;
+  return B;
+}
+
+cudaError_t Mlp::forward_rows(const Buffers &B, int rows) {
+  EpiArgs e{};
+  e.bias = w + off[1];
+  e.out_bf16 = B.H1;
+  e.ldc = H;
+  MCK(gemm<EPI_BIAS_TANH>(B.X, in_pad, wb + off[0], in_pad, rows, H, in_pad, e, stream));
+  e.bias = w + off[3];
+  e.out_bf16 = B.H2;
+  MCK(gemm<EPI_BIAS_TANH>(B.H1, H, wb + off[2], H, rows, H, H, e, stream));
+  EpiArgs e3{};
+  e3.bias = w + off[5];
+  e3.out_f32 = B.Y;
+  e3.ldc = out_pad;
+  return gemm<EPI_BIAS_F32>(B.H2, H, wb + off[4], H, rows, out_pad, H, e3, stream);
+}
+
+cudaError_t Mlp::forward(const float *X, int64_t n, float *Y) {
+  const int rows = (int)(((n + 63) / 64) * 64);
+  MCK(workspace(rows));
+  Buffers B = buffers(rows);
+  pack_inputs<<<1024, 256, 0, stream>>>(X, (int)n, n_in, rows, in_pad, B.X);
+  MCK(cudaGetLastError());
+  MCK(forward_rows(B, rows));
+  // Y (rows x out_pad) -> caller's n x n_out
+  MCK(cudaMemcpy2DAsync(Y, n_out * sizeof(float), B.Y, out_pad * sizeof(float), n_out * sizeof(float), n,
+                        cudaMemcpyDeviceToDevice, stream));
+  return cudaSuccess;
+}
+
+cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
+  const int rows = (int)(((n + 63) / 64) * 64);
+  MCK(workspace(rows));
+  Buffers B = buffers(rows);
+  pack_inputs<<<1024, 256, 0, stream>>>(X, (int)n, n_in, rows, in_pad, B.X);
+  MCK(cudaGetLastError());
+  MCK(forward_rows(B, rows));
+  MCK(cudaMemsetAsync(loss, 0, sizeof(float), stream));
+  mse_grad<<<256, 256, 0, stream>>>(B.Y, T, rows, (int)n, n_out, out_pad, B.dY, loss);
+  MCK(cudaGetLastError());
+  // dZ2 = (dY W3) * (1 - H2^2): A = dY (rows x out_pad), B-operand rows = W3^T (H x out_pad)
+  EpiArgs e{};
+  e.out_bf16 = B.dZ2;
+  e.h = B.H2;
+  e.ldc = H;
+  MCK(gemm<EPI_DTANH>(B.dY, out_pad, wt + off[4], out_pad, rows, H, out_pad, e, stream));
+  e.out_bf16 = B.dZ1;
+  e.h = B.H1;
+  MCK(gemm<EPI_DTANH>(B.dZ2, H, wt + off[2], H, rows, H, H, e, stream));
+  // weight gradients: dW = dZ^T A_prev, K = rows
+  MCK(transpose(B.dY, B.dYT, rows, out_pad, stream));
+  MCK(transpose(B.H2, B.H2T, rows, H, stream));
+  MCK(transpose(B.dZ2, B.dZ2T, rows, H, stream));
+  MCK(transpose(B.H1, B.H1T, rows, H, stream));
+  MCK(transpose(B.dZ1, B.dZ1T, rows, H, stream));
+  MCK(transpose(B.X, B.XT, rows, in_pad, stream));
+  EpiArgs f{};
+  f.out_f32 = g + off[4];
+  f.ldc = H;
+  MCK(gemm<EPI_F32>(B.dYT, rows, B.H2T, rows, out_pad, H, rows, f, stream));
+  f.out_f32 = g + off[2];
+  f.ldc = H;
+  MCK(gemm<EPI_F32>(B.dZ2T, rows, B.H1T, rows, H, H, rows, f, stream));
+  f.out_f32 = g + off[0];
+  f.ldc = in_pad;
+  MCK(gemm<EPI_F32>(B.dZ1T, rows, B.XT, rows, H, in_pad, rows, f, stream));
+  colsum_bf16<<<(out_pad + 127) / 128, 128, 0, stream>>>(B.dY, rows, out_pad, g + off[5]);
+  colsum_bf16<<<(H + 127) / 128, 128, 0, stream>>>(B.dZ2, rows, H, g + off[3]);
+  colsum_bf16<<<(H + 127) / 128, 128, 0, stream>>>(B.dZ1, rows, H, g + off[1]);
+  return cudaGetLastError();
+}
+
+cudaError_t Mlp::adam_step(float lr, float b1, float b2, float eps) {
+  step++;
+  const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+  adam<<<(unsigned)((n_params + 255) / 256), 256, 0, stream>>>(w, g, m1, m2, wb, (int)n_params, lr, b1, b2, eps, c1,
+                                                                 c2);
+  MCK(cudaGetLastError());
+  // padded weight entries have zero gradients and stay zero
+  MCK(transpose(wb + off[4], wt + off[4], out_pad, H, stream));
+  MCK(transpose(wb + off[2], wt + off[2], H, H, stream));
+  return cudaSuccess;
+}
+
+cudaError_t Mlp::train(const float *X, const float *T, int64_t n, int batch, int steps, float lr, uint64_t seed,
+                       float *final_loss) {
+  batch = (batch / 64) * 64;
+  if (batch < 64) batch = 64;
+  MCK(workspace(batch));
+  Buffers B = buffers(batch);
+  int64_t *idx = nullptr;
+  MCK(cudaMalloc(&idx, batch * sizeof(int64_t)));
+  std::vector<int64_t> hidx(batch);
+  uint64_t state = seed * 0x9E3779B97F4A7C15ull + 1;
+  float lsum = 0.f;
+  int lcnt = 0;
+  cudaError_t err = cudaSuccess;
+  for (int it = 0; it < steps && err == cudaSuccess; it++) {
+    for (int k = 0; k < batch; k++) {  // xorshift sampling with replacement
+      state ^= state << 13;
+      state ^= state >> 7;
+      state ^= state << 17;
+      hidx[k] = (int64_t)(state % (uint64_t)n);
+    }
+    err = cudaMemcpyAsync(idx, hidx.data(), batch * sizeof(int64_t), cudaMemcpyHostToDevice, stream);
+    if (err == cudaSuccess) {
+      gather_rows<<<batch, 32, 0, stream>>>(X, T, idx, batch, n_in, n_out, B.Xf, B.Tf);
+      err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = loss_grad(B.Xf, B.Tf, batch);
+    if (err == cudaSuccess) err = adam_step(lr, 0.9f, 0.999f, 1e-8f);
+    if (err == cudaSuccess && it >= steps - 20) {
+      float l = 0;
+      err = cudaMemcpyAsync(&l, loss, sizeof(float), cudaMemcpyDeviceToHost, stream);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+      lsum += l;
+      lcnt++;
+    }
+  }
+  cudaFree(idx);
+  if (final_loss) *final_loss = lcnt ? lsum / lcnt : 0.f;
+  return err;
+}
+
+}  // namespace cm

@@ -1,0 +1,629 @@
+// C ABI of the learned macro step: the MLP handle and the surrogate (training-data generation
+// with the plain integrator, fitting, surrogate runs). See cm_surrogate.h for the method.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cm_handles.h"
+#include "cm_mlp.h"
+#include "cm_surrogate.h"
+
+using namespace cm;
+
+struct cm_mlp_s {
+  Mlp m;
+};
+
+struct cm_surrogate_s {
+  ParamSet fine, coarse_ps;
+  int substeps = 10;
+  cudaStream_t stream = nullptr;
+  TT2Consts<float> coarse{};
+  float *rows_coarse = nullptr, *eca = nullptr;
+  cm_mlp_s net;
+  SurNorm norm{};
+  bool fitted = false;
+  // dataset (raw and normalised)
+  float *dX = nullptr, *dT = nullptr, *nX = nullptr, *nT = nullptr;
+  int64_t cap = 0;
+  unsigned long long *d_count = nullptr;
+  // generation scratch
+  float *gX = nullptr, *gC = nullptr, *gOld = nullptr, *gT = nullptr;
+  uint8_t *gkeep = nullptr;
+  int64_t gcap = 0;
+  // run scratch
+  int *fallback = nullptr;
+  float *pred = nullptr;
+  int64_t rcap = 0;
+  unsigned int *n_fallback = nullptr;
+  unsigned long long *totals = nullptr;  // n_sur, n_fallback_total, n_audit
+  float *audit_err = nullptr;
+};
+
+namespace {
+
+// unpadded <-> padded parameter blocks of an Mlp
+void unpadded_sizes(const Mlp &m, size_t sz[6]) {
+  sz[0] = (size_t)m.H * m.n_in;
+  sz[1] = m.H;
+  sz[2] = (size_t)m.H * m.H;
+  sz[3] = m.H;
+  sz[4] = (size_t)m.n_out * m.H;
+  sz[5] = m.n_out;
+}
+
+int64_t n_unpadded(const Mlp &m) {
+  size_t sz[6];
+  unpadded_sizes(m, sz);
+  int64_t n = 0;
+  for (size_t x : sz) n += (int64_t)x;
+  return n;
+}
+
+// copies between the unpadded host layout and the padded device block (FP32)
+int mlp_copy(Mlp &m, float *dev_block, float *host, bool to_host) {
+  std::vector<float> pad(m.n_params, 0.f);
+  if (!to_host) {
+    CK(cudaMemcpy(pad.data(), dev_block, m.n_params * sizeof(float), cudaMemcpyDeviceToHost));  // keep padding
+  } else {
+    CK(cudaStreamSynchronize(m.stream));
+    CK(cudaMemcpy(pad.data(), dev_block, m.n_params * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  size_t k = 0;
+  auto blk = [&](int b, int rows, int cols, int ldp) {
+    for (int r = 0; r < rows; r++)
+      for (int c = 0; c < cols; c++, k++) {
+        float &p = pad[m.off[b] + (size_t)r * ldp + c];
+        if (to_host) host[k] = p;
+        else p = host[k];
+      }
+  };
+  blk(0, m.H, m.n_in, m.in_pad);
+  blk(1, 1, m.H, m.H);
+  blk(2, m.H, m.H, m.H);
+  blk(3, 1, m.H, m.H);
+  blk(4, m.n_out, m.H, m.H);
+  blk(5, 1, m.n_out, m.out_pad);
+  if (!to_host) CK(cudaMemcpy(dev_block, pad.data(), m.n_params * sizeof(float), cudaMemcpyHostToDevice));
+  return CM_OK;
+}
+
+// host view of an array that may live on the device
+int fetch(const float *p, size_t n, std::vector<float> &out) {
+  out.resize(n);
+  if (is_device_ptr(p)) CK(cudaMemcpy(out.data(), p, n * sizeof(float), cudaMemcpyDeviceToHost));
+  else memcpy(out.data(), p, n * sizeof(float));
+  return CM_OK;
+}
+
+// device copy of a caller array (returns the caller's pointer if already on the device)
+int to_device(const float *p, size_t n, const float **dev, float **owned) {
+  *owned = nullptr;
+  if (is_device_ptr(p)) {
+    *dev = p;
+    return CM_OK;
+  }
+  CK(cudaMalloc(owned, std::max<size_t>(1, n) * sizeof(float)));
+  CK(cudaMemcpy(*owned, p, n * sizeof(float), cudaMemcpyHostToDevice));
+  *dev = *owned;
+  return CM_OK;
+}
+
+// The reference driver's stimulus for `steps` fine steps from (t, tb), advancing them.
+bool protocol_steps(const cm_stimulus *st, int steps, double dt, double &t, double &tb, float *iext) {
+  bool on = false;
+  for (int k = 0; k < steps; k++) {
+    double i = 0.0;
+    if (st && t >= tb) {
+      i = st->amplitude;
+      if (t >= tb + st->textlen) tb += st->bcl;
+    }
+    iext[k] = (float)i;
+    on = on || i != 0.0;
+    t += dt;
+  }
+  return on;
+}
+
+int check_batch(cm_batch_s *b) {
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (b->d.model != kTenTusscher2 || b->d.precision != CM_PREC_MIXED)
+    return fail(CM_ERR_UNSUPPORTED, "the surrogate runs MIXED TenTusscher2 batches");
+  if (b->d.n >= ((int64_t)1 << 31) / 24) return fail(CM_ERR_ARG, "batch too large for the surrogate");
+  return CM_OK;
+}
+
+// Vm planes of a batch for a run: split from the caller's doubles (staged if on the host)
+int planes_in(cm_batch_s *b, double *Vm, double **dvm, bool &host_vm, cudaStream_t s) {
+  const int64_t n = b->d.n;
+  host_vm = !is_device_ptr(Vm);
+  *dvm = Vm;
+  if (host_vm) {
+    if (b->stage_n < n) {
+      for (auto &p : b->stage) {
+        cudaFree(p);
+        p = nullptr;
+      }
+      b->stage_n = 0;
+      for (auto &p : b->stage) CK(cudaMalloc(&p, std::max<int64_t>(1, n) * sizeof(double)));
+      b->stage_n = n;
+    }
+    *dvm = b->stage[0];
+    CK(cudaMemcpyAsync(*dvm, Vm, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  if (!b->vm_planes) CK(cudaMalloc(&b->vm_planes, std::max<int64_t>(1, 2 * b->d.ld) * sizeof(float)));
+  CK(launch_vm_split(*dvm, b->vm_planes, b->vm_planes + b->d.ld, n, s));
+  return CM_OK;
+}
+
+int planes_out(cm_batch_s *b, double *Vm, double *dvm, bool host_vm, cudaStream_t s) {
+  const int64_t n = b->d.n;
+  CK(launch_vm_join(b->vm_planes, b->vm_planes + b->d.ld, dvm, n, s));
+  if (host_vm) CK(cudaMemcpyAsync(Vm, dvm, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return CM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ MLP
+
+int cm_mlp_create(cm_mlp_t *out, int n_in, int n_hidden, int n_out, uint64_t seed, void *stream) {
+  if (!out || n_in < 1 || n_in > 256 || n_hidden < 64 || n_hidden % 64 || n_out < 1 || n_out > 256)
+    return fail(CM_ERR_ARG, "MLP sizes: n_in, n_out in [1, 256], n_hidden a positive multiple of 64");
+  *out = nullptr;
+  auto *m = new (std::nothrow) cm_mlp_s();
+  if (!m) return fail(CM_ERR_NOMEM, "host allocation failed");
+  cudaError_t e = m->m.init(n_in, n_hidden, n_out, seed, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    m->m.release();
+    delete m;
+    return cuda_fail(e, "cm_mlp_create");
+  }
+  *out = m;
+  return CM_OK;
+}
+
+int cm_mlp_destroy(cm_mlp_t m) {
+  if (!m) return CM_OK;
+  cudaStreamSynchronize(m->m.stream);
+  m->m.release();
+  delete m;
+  return CM_OK;
+}
+
+int64_t cm_mlp_n_params(cm_mlp_t m) { return m ? n_unpadded(m->m) : -1; }
+
+int cm_mlp_get_params(cm_mlp_t m, float *params) {
+  if (!m || !params) return fail(CM_ERR_ARG, "NULL argument");
+  std::vector<float> h(n_unpadded(m->m));
+  int rc = mlp_copy(m->m, m->m.w, h.data(), true);
+  if (rc) return rc;
+  if (is_device_ptr(params)) CK(cudaMemcpy(params, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  else memcpy(params, h.data(), h.size() * sizeof(float));
+  return CM_OK;
+}
+
+int cm_mlp_set_params(cm_mlp_t m, const float *params) {
+  if (!m || !params) return fail(CM_ERR_ARG, "NULL argument");
+  std::vector<float> h;
+  int rc = fetch(params, n_unpadded(m->m), h);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(m->m.stream));
+  if ((rc = mlp_copy(m->m, m->m.w, h.data(), false))) return rc;
+  CK(m->m.sync_bf16());
+  CK(cudaStreamSynchronize(m->m.stream));
+  return CM_OK;
+}
+
+int cm_mlp_get_grads(cm_mlp_t m, float *grads) {
+  if (!m || !grads) return fail(CM_ERR_ARG, "NULL argument");
+  std::vector<float> h(n_unpadded(m->m));
+  int rc = mlp_copy(m->m, m->m.g, h.data(), true);
+  if (rc) return rc;
+  if (is_device_ptr(grads)) CK(cudaMemcpy(grads, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  else memcpy(grads, h.data(), h.size() * sizeof(float));
+  return CM_OK;
+}
+
+int cm_mlp_forward(cm_mlp_t m, const float *X, int64_t n, float *Y) {
+  if (!m || !X || !Y || n < 0) return fail(CM_ERR_ARG, "bad argument");
+  if (n == 0) return CM_OK;
+  const float *dX;
+  float *own = nullptr, *dY = Y;
+  int rc = to_device(X, (size_t)n * m->m.n_in, &dX, &own);
+  if (rc) return rc;
+  const bool host_y = !is_device_ptr(Y);
+  if (host_y) CK(cudaMalloc(&dY, (size_t)n * m->m.n_out * sizeof(float)));
+  cudaError_t e = m->m.forward(dX, n, dY);
+  if (e == cudaSuccess && host_y)
+    e = cudaMemcpyAsync(Y, dY, (size_t)n * m->m.n_out * sizeof(float), cudaMemcpyDeviceToHost, m->m.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->m.stream);
+  cudaFree(own);
+  if (host_y) cudaFree(dY);
+  return e == cudaSuccess ? CM_OK : cuda_fail(e, "cm_mlp_forward");
+}
+
+int cm_mlp_loss_grad(cm_mlp_t m, const float *X, const float *T, int64_t n, float *loss) {
+  if (!m || !X || !T || n <= 0) return fail(CM_ERR_ARG, "bad argument");
+  const float *dX, *dT;
+  float *o1 = nullptr, *o2 = nullptr;
+  int rc = to_device(X, (size_t)n * m->m.n_in, &dX, &o1);
+  if (!rc) rc = to_device(T, (size_t)n * m->m.n_out, &dT, &o2);
+  if (rc) {
+    cudaFree(o1);
+    return rc;
+  }
+  cudaError_t e = m->m.loss_grad(dX, dT, n);
+  float l = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&l, m->m.loss, sizeof(float), cudaMemcpyDeviceToHost, m->m.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->m.stream);
+  cudaFree(o1);
+  cudaFree(o2);
+  if (e != cudaSuccess) return cuda_fail(e, "cm_mlp_loss_grad");
+  if (loss) *loss = l;
+  return CM_OK;
+}
+
+int cm_mlp_adam_step(cm_mlp_t m, float lr, float beta1, float beta2, float eps) {
+  if (!m) return fail(CM_ERR_ARG, "NULL MLP");
+  CK(m->m.adam_step(lr, beta1, beta2, eps));
+  CK(cudaStreamSynchronize(m->m.stream));
+  return CM_OK;
+}
+
+// ------------------------------------------------------------------ surrogate
+
+int cm_surrogate_destroy(cm_surrogate_t s) {
+  if (!s) return CM_OK;
+  cudaStreamSynchronize(s->stream);
+  s->net.m.release();
+  for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
+                  (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
+                  (void *)s->gkeep, (void *)s->fallback, (void *)s->pred, (void *)s->n_fallback, (void *)s->totals,
+                  (void *)s->audit_err})
+    cudaFree(p);
+  delete s;
+  return CM_OK;
+}
+
+int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64_t seed, void *stream) {
+  if (!out || !p) return fail(CM_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  if (p->ps.spec->model != kTenTusscher2) return fail(CM_ERR_UNSUPPORTED, "the surrogate covers TenTusscher2");
+  if (substeps < 1 || substeps > 64) return fail(CM_ERR_ARG, "substeps in [1, 64]");
+  auto *s = new (std::nothrow) cm_surrogate_s();
+  if (!s) return fail(CM_ERR_NOMEM, "host allocation failed");
+  s->fine = p->ps;
+  s->coarse_ps = p->ps;
+  s->substeps = substeps;
+  s->stream = (cudaStream_t)stream;
+  s->coarse_ps.dt = p->ps.dt * substeps;
+  s->coarse_ps.rebuild();  // tables for the macro step
+  TT2Consts<double> cd;
+  s->coarse_ps.tt2_consts(cd, s->coarse);
+  std::vector<float> rows, eca;
+  s->coarse_ps.rows_fp32(rows, eca);
+  int rc = CM_OK;
+  cudaError_t e = cudaMalloc(&s->rows_coarse, rows.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->eca, eca.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(s->rows_coarse, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s->eca, eca.data(), eca.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_count, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(s->d_count, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&s->n_fallback, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&s->totals, 3 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&s->audit_err, sizeof(float));
+  if (e == cudaSuccess) e = s->net.m.init(kSurIn, kSurH, kSurOut, seed, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) rc = cuda_fail(e, "cm_surrogate_create");
+  for (int k = 0; k < kSurIn; k++) s->norm.inv_sd_x[k] = 1.f;
+  for (int k = 0; k < kSurOut; k++) s->norm.sd_y[k] = 1.f;
+  if (rc) {
+    std::string keep = last_error();
+    cm_surrogate_destroy(s);
+    last_error() = keep;
+    return rc;
+  }
+  *out = s;
+  return CM_OK;
+}
+
+int cm_surrogate_mlp(cm_surrogate_t s, cm_mlp_t *mlp) {
+  if (!s || !mlp) return fail(CM_ERR_ARG, "NULL argument");
+  *mlp = &s->net;
+  return CM_OK;
+}
+
+int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_macro, const cm_stimulus *stim,
+                          int64_t cell_stride, int64_t max_pairs, int64_t *n_pairs) {
+  if (!s || !Vm || n_macro < 0 || cell_stride < 1 || max_pairs < 0) return fail(CM_ERR_ARG, "bad argument");
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (b->ps.dt != s->fine.dt) return fail(CM_ERR_ARG, "batch dt differs from the surrogate's fine dt");
+  const int64_t n = b->d.n;
+  const int64_t n_sample = (n + cell_stride - 1) / cell_stride;
+  cudaStream_t st = b->stream;
+  // dataset capacity (grows, keeping what is there)
+  if (max_pairs > s->cap) {
+    float *nx = nullptr, *nt = nullptr;
+    CK(cudaMalloc(&nx, std::max<int64_t>(1, max_pairs) * kSurIn * sizeof(float)));
+    CK(cudaMalloc(&nt, std::max<int64_t>(1, max_pairs) * kSurOut * sizeof(float)));
+    unsigned long long have = 0;
+    CK(cudaMemcpy(&have, s->d_count, sizeof(have), cudaMemcpyDeviceToHost));
+    have = std::min<unsigned long long>(have, (unsigned long long)s->cap);
+    if (have) {
+      CK(cudaMemcpy(nx, s->dX, have * kSurIn * sizeof(float), cudaMemcpyDeviceToDevice));
+      CK(cudaMemcpy(nt, s->dT, have * kSurOut * sizeof(float), cudaMemcpyDeviceToDevice));
+    }
+    cudaFree(s->dX);
+    cudaFree(s->dT);
+    s->dX = nx;
+    s->dT = nt;
+    s->cap = max_pairs;
+  }
+  if (n_sample > s->gcap) {
+    for (void *p : {(void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT, (void *)s->gkeep}) cudaFree(p);
+    CK(cudaMalloc(&s->gX, n_sample * kSurIn * sizeof(float)));
+    CK(cudaMalloc(&s->gC, n_sample * kSurOut * sizeof(float)));
+    CK(cudaMalloc(&s->gOld, n_sample * 8 * sizeof(float)));
+    CK(cudaMalloc(&s->gT, n_sample * kSurOut * sizeof(float)));
+    CK(cudaMalloc(&s->gkeep, n_sample));
+    s->gcap = n_sample;
+  }
+  double *dvm;
+  bool host_vm;
+  if ((rc = planes_in(b, Vm, &dvm, host_vm, st))) return rc;
+  float *hi = b->vm_planes, *lo = b->vm_planes + b->d.ld;
+  const cm_stimulus stv = stim ? *stim : cm_stimulus{0, 1e300, nullptr, 0, 0, 0};
+  double t = stv.t0, tb = stv.textbegin;
+  const float g0_Na = (float)s->fine.get("g_Na"), g0_Kr = (float)s->fine.get("g_Kr"), g0_K1 = (float)s->fine.get("g_K1");
+  float iext[64];
+  for (int64_t mstep = 0; mstep < n_macro; mstep++) {
+    SurGenArgs ga{};
+    ga.fine = b->d;
+    ga.coarse = s->coarse;
+    ga.rows_coarse = s->rows_coarse;
+    ga.eca = s->eca;
+    ga.vm_hi = hi;
+    ga.vm_lo = lo;
+    ga.stride = cell_stride;
+    ga.offset = 0;
+    ga.n_sample = n_sample;
+    ga.X = s->gX;
+    ga.C = s->gC;
+    ga.Old = s->gOld;
+    ga.g0_Na = g0_Na;
+    ga.g0_Kr = g0_Kr;
+    ga.g0_K1 = g0_K1;
+    CK(launch_sur_gen(ga, st));
+    const bool on = protocol_steps(stim ? &stv : nullptr, s->substeps, s->fine.dt, t, tb, iext);
+    for (int k = 0; k < s->substeps; k++) {
+      StepIO io;
+      io.vm_hi = hi;
+      io.vm_lo = lo;
+      io.iext_uniform = iext[k];
+      CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, st));
+    }
+    SurPostArgs pa{};
+    pa.fine = b->d;
+    pa.vm_hi = hi;
+    pa.vm_lo = lo;
+    pa.stride = cell_stride;
+    pa.offset = 0;
+    pa.n_sample = n_sample;
+    pa.C = s->gC;
+    pa.Old = s->gOld;
+    pa.T = s->gT;
+    pa.keep = s->gkeep;
+    pa.gate_mv_per_ms = 5.f;
+    pa.macro_ms = (float)(s->coarse_ps.dt * 1000.0);
+    pa.stim_on = on ? 1 : 0;
+    CK(launch_sur_post(pa, st));
+    CK(launch_sur_append(s->gX, s->gT, s->gkeep, n_sample, s->dX, s->dT, s->d_count, s->cap, st));
+  }
+  if ((rc = planes_out(b, Vm, dvm, host_vm, st))) return rc;
+  unsigned long long have = 0;
+  CK(cudaMemcpyAsync(&have, s->d_count, sizeof(have), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (n_pairs) *n_pairs = (int64_t)std::min<unsigned long long>(have, (unsigned long long)s->cap);
+  return CM_OK;
+}
+
+int cm_surrogate_dataset(cm_surrogate_t s, int64_t *n_pairs, float *X, float *T) {
+  if (!s) return fail(CM_ERR_ARG, "NULL surrogate");
+  unsigned long long have = 0;
+  CK(cudaMemcpy(&have, s->d_count, sizeof(have), cudaMemcpyDeviceToHost));
+  const int64_t n = (int64_t)std::min<unsigned long long>(have, (unsigned long long)s->cap);
+  if (n_pairs) *n_pairs = n;
+  if (X && n) CK(cudaMemcpy(X, s->dX, n * kSurIn * sizeof(float), cudaMemcpyDefault));
+  if (T && n) CK(cudaMemcpy(T, s->dT, n * kSurOut * sizeof(float), cudaMemcpyDefault));
+  return CM_OK;
+}
+
+int cm_surrogate_fit(cm_surrogate_t s, int batch, int steps, float lr, uint64_t seed, float *final_loss) {
+  if (!s || batch < 64 || steps < 0 || !(lr > 0)) return fail(CM_ERR_ARG, "bad argument");
+  int64_t n = 0;
+  int rc = cm_surrogate_dataset(s, &n, nullptr, nullptr);
+  if (rc) return rc;
+  if (n < batch) return fail(CM_ERR_ARG, "fewer training pairs than one minibatch");
+  // normalisation from a strided subsample of at most 2^18 rows
+  const int64_t m = std::min<int64_t>(n, (int64_t)1 << 18), stride = n / m;
+  std::vector<float> hx((size_t)n * kSurIn), ht((size_t)n * kSurOut);
+  CK(cudaMemcpy(hx.data(), s->dX, hx.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ht.data(), s->dT, ht.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < kSurIn; k++) {
+    double sum = 0, sq = 0;
+    for (int64_t r = 0; r < m; r++) {
+      const double v = hx[(size_t)(r * stride) * kSurIn + k];
+      sum += v;
+      sq += v * v;
+    }
+    const double mu = sum / m, var = std::max(0.0, sq / m - mu * mu);
+    s->norm.mu_x[k] = (float)mu;
+    s->norm.inv_sd_x[k] = (float)(1.0 / std::max(std::sqrt(var), 1e-6 * std::max(1.0, std::fabs(mu))));
+  }
+  for (int k = 0; k < kSurOut; k++) {
+    double sq = 0;
+    for (int64_t r = 0; r < m; r++) {
+      const double v = ht[(size_t)(r * stride) * kSurOut + k];
+      sq += v * v;
+    }
+    s->norm.sd_y[k] = (float)std::max(std::sqrt(sq / m), 1e-12);
+  }
+  cudaFree(s->nX);
+  cudaFree(s->nT);
+  s->nX = s->nT = nullptr;
+  CK(cudaMalloc(&s->nX, (size_t)n * kSurIn * sizeof(float)));
+  CK(cudaMalloc(&s->nT, (size_t)n * kSurOut * sizeof(float)));
+  CK(launch_sur_normalize(s->dX, s->dT, n, s->norm, s->nX, s->nT, s->stream));
+  float loss = 0;
+  CK(s->net.m.train(s->nX, s->nT, n, batch, steps, lr, seed, &loss));
+  CK(cudaStreamSynchronize(s->stream));
+  s->fitted = true;
+  if (final_loss) *final_loss = loss;
+  return CM_OK;
+}
+
+int64_t cm_surrogate_blob_size(cm_surrogate_t s) {
+  return s ? (int64_t)(sizeof(SurNorm) / sizeof(float)) + n_unpadded(s->net.m) : -1;
+}
+
+int cm_surrogate_get_blob(cm_surrogate_t s, float *blob) {
+  if (!s || !blob) return fail(CM_ERR_ARG, "NULL argument");
+  const int64_t nn = sizeof(SurNorm) / sizeof(float);
+  std::vector<float> h(cm_surrogate_blob_size(s));
+  memcpy(h.data(), &s->norm, sizeof(SurNorm));
+  int rc = mlp_copy(s->net.m, s->net.m.w, h.data() + nn, true);
+  if (rc) return rc;
+  if (is_device_ptr(blob)) CK(cudaMemcpy(blob, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  else memcpy(blob, h.data(), h.size() * sizeof(float));
+  return CM_OK;
+}
+
+int cm_surrogate_set_blob(cm_surrogate_t s, const float *blob) {
+  if (!s || !blob) return fail(CM_ERR_ARG, "NULL argument");
+  const int64_t nn = sizeof(SurNorm) / sizeof(float);
+  std::vector<float> h;
+  int rc = fetch(blob, cm_surrogate_blob_size(s), h);
+  if (rc) return rc;
+  memcpy(&s->norm, h.data(), sizeof(SurNorm));
+  CK(cudaStreamSynchronize(s->stream));
+  if ((rc = mlp_copy(s->net.m, s->net.m.w, h.data() + nn, false))) return rc;
+  CK(s->net.m.sync_bf16());
+  CK(cudaStreamSynchronize(s->stream));
+  s->fitted = true;
+  return CM_OK;
+}
+
+int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n_macro, const cm_stimulus *stim,
+                           int mode, int audit_mod, cm_surrogate_stats *stats) {
+  if (!s || !Vm || n_macro < 0 || audit_mod < 0 || (mode != 0 && mode != 1)) return fail(CM_ERR_ARG, "bad argument");
+  int rc = check_batch(b);
+  if (rc) return rc;
+  if (b->ps.dt != s->fine.dt) return fail(CM_ERR_ARG, "batch dt differs from the surrogate's fine dt");
+  const int64_t n = b->d.n;
+  cudaStream_t st = b->stream;
+  if (n > s->rcap) {
+    cudaFree(s->fallback);
+    cudaFree(s->pred);
+    s->fallback = nullptr;
+    s->pred = nullptr;
+    CK(cudaMalloc(&s->fallback, std::max<int64_t>(1, n) * sizeof(int)));
+    CK(cudaMalloc(&s->pred, std::max<int64_t>(1, n) * sizeof(float)));
+    s->rcap = n;
+  }
+  CK(cudaMemsetAsync(s->totals, 0, 3 * sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(s->audit_err, 0, sizeof(float), st));
+  double *dvm;
+  bool host_vm;
+  if ((rc = planes_in(b, Vm, &dvm, host_vm, st))) return rc;
+  float *hi = b->vm_planes, *lo = b->vm_planes + b->d.ld;
+  const cm_stimulus stv = stim ? *stim : cm_stimulus{0, 1e300, nullptr, 0, 0, 0};
+  double t = stv.t0, tb = stv.textbegin;
+  SurKernelArgs ka{};
+  ka.fine = b->d;
+  ka.coarse = s->coarse;
+  ka.rows_coarse = s->rows_coarse;
+  ka.eca = s->eca;
+  ka.vm_hi = hi;
+  ka.vm_lo = lo;
+  ka.norm = s->norm;
+  ka.w1 = s->net.m.wb + s->net.m.off[0];
+  ka.w2 = s->net.m.wb + s->net.m.off[2];
+  ka.w3 = s->net.m.wb + s->net.m.off[4];
+  ka.bias = nullptr;
+  ka.mode = mode;
+  ka.gate_mv_per_ms = 5.f;
+  ka.audit_mod = audit_mod;
+  ka.fallback = s->fallback;
+  ka.n_fallback = s->n_fallback;
+  ka.n_fallback_total = s->totals + 1;
+  ka.pred = s->pred;
+  ka.n_sur = s->totals;
+  ka.g0_Na = (float)s->fine.get("g_Na");
+  ka.g0_Kr = (float)s->fine.get("g_Kr");
+  ka.g0_K1 = (float)s->fine.get("g_K1");
+  // biases as one contiguous FP32 block b1 | b2 | b3 (the kernel's layout)
+  float *bias = nullptr;
+  CK(cudaMalloc(&bias, 288 * sizeof(float)));
+  CK(cudaMemcpyAsync(bias, s->net.m.w + s->net.m.off[1], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(bias + 128, s->net.m.w + s->net.m.off[3], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(bias + 256, s->net.m.w + s->net.m.off[5], 32 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  ka.bias = bias;
+  SurPlainArgs pa{};
+  pa.fine = b->d;
+  pa.vm_hi = hi;
+  pa.vm_lo = lo;
+  pa.list = s->fallback;
+  pa.n_list = s->n_fallback;
+  pa.substeps = s->substeps;
+  pa.audit_mod = audit_mod;
+  pa.pred = s->pred;
+  pa.audit_err = s->audit_err;
+  pa.n_audit = s->totals + 2;
+  cudaError_t e = cudaSuccess;
+  for (int64_t mstep = 0; mstep < n_macro && e == cudaSuccess; mstep++) {
+    const bool on = protocol_steps(stim ? &stv : nullptr, s->substeps, s->fine.dt, t, tb, pa.iext);
+    ka.stim_on = on ? 1 : 0;
+    ka.audit_phase = audit_mod > 0 ? (int)(mstep % audit_mod) : 0;
+    pa.audit_phase = ka.audit_phase;
+    e = cudaMemsetAsync(s->n_fallback, 0, sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = launch_sur_step(ka, n, st);
+    if (e == cudaSuccess) e = launch_sur_plain(pa, (int)n, st);
+  }
+  if (e != cudaSuccess) {
+    cudaFree(bias);
+    return cuda_fail(e, "surrogate run");
+  }
+  rc = planes_out(b, Vm, dvm, host_vm, st);
+  unsigned long long tot[3] = {0, 0, 0};
+  float aerr = 0;
+  unsigned int mask = 0;
+  if (!rc) {
+    e = cudaMemcpyAsync(tot, s->totals, sizeof(tot), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&aerr, s->audit_err, sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "surrogate run");
+  }
+  cudaFree(bias);
+  if (rc) return rc;
+  if (stats) {
+    stats->cell_macro_steps = n * n_macro;
+    stats->surrogate = (int64_t)tot[0];
+    stats->fallback = (int64_t)tot[1];
+    stats->audited = (int64_t)tot[2];
+    stats->max_audit_err_mv = aerr;
+  }
+  if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+}  // extern "C"

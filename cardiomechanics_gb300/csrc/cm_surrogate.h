@@ -1,0 +1,100 @@
+// Learned macro-step for ten Tusscher 2006 cells (cm_surrogate.cu).
+//
+// One macro step advances a cell by S fine steps (S * dt, e.g. 10 x 0.01 ms). It is the coarse
+// physics step -- the mixed-form update once with tables built for S * dt -- plus an MLP
+// correction trained on the residual between S fine steps of the plain integrator and that
+// coarse step:   x(t + S dt) = coarse(x) + sigma_y * MLP((f(x) - mu_x) / sigma_x).
+// Cells whose stimulus is on during the macro step, whose |dVm/dt| exceeds the gate (5 mV/ms,
+// the upstroke), that fail the range audit, or that fall in the rotating audit sample are
+// integrated by the plain integrator instead (S fine steps); audited cells also record how far
+// the surrogate's prediction was from the plain result.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "cm_launch.h"
+#include "cm_mlp.h"
+
+namespace cm {
+
+constexpr int kSurIn = 22;   // features
+constexpr int kSurOut = 19;  // corrected quantities
+constexpr int kSurH = 128;   // hidden width (the inference kernel is built for 128)
+
+// Features: Vm [mV], 13 gates, log Ca_i, log CaSS, CaSR, Na_i, K_i, log(g/g0) of g_Na, g_Kr, g_K1.
+// Outputs: residuals of Vm [mV], the 13 gates, Ca_i, CaSS, CaSR, Na_i, K_i.
+struct SurNorm {
+  float mu_x[kSurIn], inv_sd_x[kSurIn], sd_y[kSurOut];
+};
+
+struct SurKernelArgs {
+  DevBatch fine;       // the batch (state, fine tables, per-cell conductances)
+  TT2Consts<float> coarse;       // constants for the macro step S * dt
+  const float *rows_coarse;      // FP32 voltage table rows for S * dt
+  const float *eca;              // ECa table (dt independent)
+  float *vm_hi, *vm_lo;          // Vm planes (lo = hi + ld)
+  SurNorm norm;
+  const __nv_bfloat16 *w1, *w2, *w3;  // BF16 network: W1 [128][32], W2 [128][128], W3 [32][128]
+  const float *bias;             // b1 [128], b2 [128], b3 [32]
+  int mode;                      // 0: coarse + MLP, 1: coarse only
+  int stim_on;                   // stimulus during this macro step: every cell takes the plain path
+  float gate_mv_per_ms;          // |dVm/dt| above this: plain path
+  int audit_mod, audit_phase;    // cells with c % audit_mod == audit_phase are audited
+  int *fallback;                 // compacted list of cells for the plain integrator
+  unsigned int *n_fallback;
+  unsigned long long *n_fallback_total;  // over all macro steps
+  float *pred;                   // audited cells: surrogate prediction of Vm [mV], by cell
+  unsigned long long *n_sur;     // cells advanced by the surrogate (over all macro steps)
+  float g0_Na, g0_Kr, g0_K1;     // parameter-set conductances (feature reference)
+};
+
+struct SurPlainArgs {
+  DevBatch fine;
+  float *vm_hi, *vm_lo;
+  const int *list;
+  const unsigned int *n_list;
+  int substeps;
+  float iext[64];                // per fine step of the macro step
+  int audit_mod, audit_phase;
+  const float *pred;
+  float *audit_err;              // max |prediction - plain| Vm [mV] over audited cells (atomicMax on bits)
+  unsigned long long *n_audit;
+};
+
+struct SurGenArgs {
+  DevBatch fine;
+  TT2Consts<float> coarse;
+  const float *rows_coarse, *eca;
+  const float *vm_hi, *vm_lo;
+  int64_t stride, offset;        // sampled cells: c = offset + k * stride
+  int64_t n_sample;
+  float *X, *C;                  // features and coarse result per sample (kSurIn, kSurOut)
+  float *Old;                    // Vm, CaSR, Na_i, K_i hi/lo words at the macro-step start (8)
+  float g0_Na, g0_Kr, g0_K1;
+};
+
+struct SurPostArgs {
+  DevBatch fine;
+  const float *vm_hi, *vm_lo;
+  int64_t stride, offset, n_sample;
+  const float *C;                // coarse result (accumulator quantities: coarse increments)
+  const float *Old;              // accumulator words at the macro-step start
+  float *T;                      // residual targets (kSurOut)
+  uint8_t *keep;                 // 1: usable pair (not stimulated, not in the upstroke)
+  float gate_mv_per_ms, macro_ms;
+  int stim_on;
+};
+
+cudaError_t launch_sur_step(const SurKernelArgs &a, int64_t n, cudaStream_t s);
+cudaError_t launch_sur_plain(const SurPlainArgs &a, int max_cells, cudaStream_t s);
+cudaError_t launch_sur_gen(const SurGenArgs &a, cudaStream_t s);
+cudaError_t launch_sur_post(const SurPostArgs &a, cudaStream_t s);
+cudaError_t launch_sur_append(const float *X, const float *T, const uint8_t *keep, int64_t n, float *dX, float *dT,
+                              unsigned long long *count, int64_t cap, cudaStream_t s);
+cudaError_t launch_sur_normalize(const float *X, const float *T, int64_t n, const SurNorm &norm, float *nX, float *nT,
+                                 cudaStream_t s);
+
+}  // namespace cm

@@ -217,6 +217,63 @@ int cm_multi_autotune(cm_multi_t m, int n_trial_steps, int *tile_cells, int *sha
                       double *ms_per_step);
 int cm_multi_set_launch(cm_multi_t m, int tile_cells, int shape, int blocks_per_sm);
 
+/* ------------------------------------------------------------------ learned macro step */
+/* New with this library; the reference has no learned component. A ten Tusscher 2006
+ * macro step of S fine steps = one physics step with tables for S * dt + an MLP correction
+ * (22 -> 128 -> 128 -> 19, tanh, BF16 tensor-core GEMMs with FP32 accumulation, FP32 Adam)
+ * trained on the residual of S fine steps of the plain integrator. The plain integrator
+ * takes stimulated cells, the upstroke (|dVm/dt| > 5 mV/ms), cells failing the range audit
+ * and a rotating audit sample, and measures the surrogate against itself on that sample. */
+typedef struct cm_mlp_s *cm_mlp_t;
+/* Parameter order of get/set: W1[n_hidden][n_in] b1[n_hidden] W2[n_hidden][n_hidden]
+ * b2[n_hidden] W3[n_out][n_hidden] b3[n_out], FP32. Arrays may be host or device memory. */
+int cm_mlp_create(cm_mlp_t *out, int n_in, int n_hidden, int n_out, uint64_t seed, void *stream);
+int cm_mlp_destroy(cm_mlp_t m);
+int64_t cm_mlp_n_params(cm_mlp_t m);
+int cm_mlp_get_params(cm_mlp_t m, float *params);
+int cm_mlp_set_params(cm_mlp_t m, const float *params);
+/* Gradients of the last cm_mlp_loss_grad, same order as the parameters. */
+int cm_mlp_get_grads(cm_mlp_t m, float *grads);
+/* Y[n][n_out] = MLP(X[n][n_in]). */
+int cm_mlp_forward(cm_mlp_t m, const float *X, int64_t n, float *Y);
+/* Mean squared error over the n x n_out outputs against T and its gradients. */
+int cm_mlp_loss_grad(cm_mlp_t m, const float *X, const float *T, int64_t n, float *loss);
+int cm_mlp_adam_step(cm_mlp_t m, float lr, float beta1, float beta2, float eps);
+
+typedef struct cm_surrogate_s *cm_surrogate_t;
+typedef struct {
+  int64_t cell_macro_steps; /* cells x macro steps run */
+  int64_t surrogate;        /* advanced by the learned macro step */
+  int64_t fallback;         /* advanced by the plain integrator (stimulus, upstroke, audit) */
+  int64_t audited;          /* audit sample: surrogate prediction compared with the plain result */
+  double max_audit_err_mv;  /* largest |Vm surrogate - Vm plain| over the audit sample [mV] */
+} cm_surrogate_stats;
+
+/* TenTusscher2 parameter set p (its dt is the fine step); substeps fine steps per macro step. */
+int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64_t seed, void *stream);
+int cm_surrogate_destroy(cm_surrogate_t s);
+/* The surrogate's network (borrowed handle, valid while s lives). */
+int cm_surrogate_mlp(cm_surrogate_t s, cm_mlp_t *mlp);
+/* Training data from the plain integrator: advances the MIXED TenTusscher2 batch b by n_macro
+ * macro steps of its driver loop (Vm updated in place) and records, for every cell_stride-th
+ * cell and every macro step outside the stimulus and the upstroke, the features and the
+ * residual target; appends up to max_pairs pairs in total. n_pairs: pairs held afterwards. */
+int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_macro, const cm_stimulus *stim,
+                          int64_t cell_stride, int64_t max_pairs, int64_t *n_pairs);
+/* Number of pairs held; X (n x 22) / T (n x 19) receive them when not NULL. */
+int cm_surrogate_dataset(cm_surrogate_t s, int64_t *n_pairs, float *X, float *T);
+/* Feature/target normalisation from the data, then `steps` Adam steps on minibatches. */
+int cm_surrogate_fit(cm_surrogate_t s, int batch, int steps, float lr, uint64_t seed, float *final_loss);
+/* Trained surrogate as one FP32 blob (normalisation + network), for saving and loading. */
+int64_t cm_surrogate_blob_size(cm_surrogate_t s);
+int cm_surrogate_get_blob(cm_surrogate_t s, float *blob);
+int cm_surrogate_set_blob(cm_surrogate_t s, const float *blob);
+/* n_macro macro steps of the driver loop with the surrogate (MIXED TenTusscher2 batch; Vm in
+ * place). mode 0: coarse step + network; mode 1: coarse step alone (the method without the
+ * network). Every audit_mod-th cell, rotating, is audited (audit_mod 0: none). */
+int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n_macro, const cm_stimulus *stim,
+                           int mode, int audit_mod, cm_surrogate_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

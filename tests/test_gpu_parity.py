@@ -223,3 +223,27 @@ def test_full_size_determinism_mixed(gpu):
     odd = outs[0][1::2]
     assert np.all(odd == odd[0])
     assert b.audit() == 0
+
+
+@pytest.mark.parametrize("model", [5, 2])
+def test_launch_shapes_agree(gpu, model):
+    """Every launch shape of the mixed kernel (register budgets, grid modes, and the
+    shared-memory-staged bulk-copy kernels) integrates the same cells to the same result, up
+    to FP32 rounding differences between instruction schedules."""
+    cm = gpu
+    n = 3 * 256 + 77  # partial last tile
+    p = cm.Params(model, None, 1e-5)
+    out = []
+    for variant, grid_mode in [(0, 0), (1, 2), (3, 4), (5, 2), (6, 1), (5, 4)]:
+        b = cm.Batch(p, n, cm.MIXED)
+        sc = W.conductance_scales(4, n, 3, 0.9, 1.1)
+        for k, name in enumerate(HET[model]):
+            b.add_hetero_value(name, p.get(name) * sc[k])
+        b.set_launch(variant, grid_mode)
+        vm = b.init_vm()
+        b.run(vm, 2000, textlen=TLEN[model], amplitude=AMP[model], bcl=1.0)
+        assert b.audit() == 0
+        out.append((vm, b.get_state()))
+    for vm, st in out[1:]:
+        assert np.abs(vm - out[0][0]).max() <= 1e-6
+        np.testing.assert_allclose(st, out[0][1], rtol=1e-4, atol=1e-7)
