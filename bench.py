@@ -209,6 +209,64 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+SUR_CELLS = 1 << 20
+SUR_BCL = 0.5
+SUR_SUBSTEPS = 10
+
+
+def advance_protocol(t, tb, n_fine, bcl, textlen=1e-3):
+    """t and textbegin after n_fine steps of the reference driver loop (CellModel.h:405-420)."""
+    for _ in range(n_fine):
+        if t >= tb and t >= tb + textlen:
+            tb += bcl
+        t += DT
+    return t, tb
+
+
+def surrogate_leg(cm, torch, stream, steps, warmup, gen_frac=1.0):
+    """Learned form: a surrogate trained here on the plain integrator's trajectories (untimed),
+    then 1,048,576 jittered (+-15%) ten Tusscher cells paced at BCL 500 ms, timed over `steps`
+    macro steps of 10 x 0.01 ms (one macro step = 10 cell-steps per cell)."""
+    from cardiomechanics_gb300 import workloads as W
+    t_train = time.perf_counter()
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    sur = cm.Surrogate(p, substeps=SUR_SUBSTEPS, seed=1, stream=stream.cuda_stream)
+    pairs = 0
+    for seed, bcl, beats in ((11, 0.5, 4), (12, 0.8, 3), (13, 1.0, 2)):  # three pacing rates
+        tb_ = cm.Batch(p, 2048, cm.MIXED, stream=stream.cuda_stream)
+        sc = W.conductance_scales(seed, 2048, 3, 0.85, 1.15)
+        for k, name in enumerate(W.TT2_HETERO):
+            tb_.add_hetero_value(name, p.get(name) * sc[k])
+        v = tb_.init_vm()
+        n_macro = int(round(beats * bcl / (SUR_SUBSTEPS * DT)) * gen_frac)
+        pairs = sur.generate(tb_, v, n_macro, textlen=1e-3, bcl=bcl, amplitude=W.TT2_STIM_NA, cell_stride=4,
+                             max_pairs=20_000_000)
+    sur.fit(batch=4096, steps=max(1, int(6000 * gen_frac)), lr=1e-3, seed=1)
+    loss = sur.fit(batch=8192, steps=max(1, int(4000 * gen_frac)), lr=3e-4, seed=2)
+    t_train = time.perf_counter() - t_train
+    b = cm.Batch(p, SUR_CELLS, cm.MIXED, stream=stream.cuda_stream)
+    sc = W.conductance_scales(5, SUR_CELLS, 3, 0.85, 1.15)
+    for k, name in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(name, p.get(name) * sc[k])
+    vm = torch.tensor(b.init_vm(), device="cuda")
+    kw = dict(textlen=1e-3, bcl=SUR_BCL, amplitude=W.TT2_STIM_NA, audit_mod=100)
+    b.run_surrogate(sur, vm, warmup, t0=0.0, textbegin=0.0, **kw)
+    t, tb = advance_protocol(0.0, 0.0, warmup * SUR_SUBSTEPS, SUR_BCL)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = b.run_surrogate(sur, vm, steps, t0=t, textbegin=tb, **kw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    return {"value": SUR_CELLS * SUR_SUBSTEPS * steps / sec, "unit": UNIT, "cells": SUR_CELLS,
+            "macro_steps": steps, "substeps": SUR_SUBSTEPS, "ms_per_macro_step": 1e3 * sec / steps,
+            "bcl_ms": SUR_BCL * 1e3, "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.85,1.15]",
+            "training": {"pairs": pairs, "final_normalised_mse": loss, "seconds": t_train},
+            "stats": stats, "gpu_launches": 2 * steps}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -219,9 +277,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "mixed", "fp64", "e2e"],
+    ap.add_argument("--only", default="all", choices=["all", "mixed", "fp64", "e2e", "surrogate"],
                     help="run one leg only (for profiler captures); the JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
+    ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the learned form")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-train-frac", type=float, default=1.0,
+                    help="fraction of the surrogate's training run (profiling captures only; accuracy needs 1)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -239,6 +301,9 @@ def main():
     stream = torch.cuda.Stream()
     hbm_peak, peak_kind = peaks()
 
+    if args.only == "surrogate":
+        print(json.dumps(surrogate_leg(cm, torch, stream, args.sur_steps, 20, args.sur_train_frac)), flush=True)
+        return
     if args.only == "fp64":
         _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
         vm64 = torch.tensor(b64.init_vm(), device="cuda")
@@ -313,6 +378,11 @@ def main():
     e2e_value = N_CELLS * args.e2e_steps / e2e_sec
     del be
 
+    sur = None
+    if not args.no_surrogate:
+        torch.cuda.empty_cache()
+        sur = surrogate_leg(cm, torch, stream, args.sur_steps, 20)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(seconds=args.cpu_seconds)
@@ -333,6 +403,8 @@ def main():
             "fp32_fma_peak_tflops_measured": fp32_peak,
             "autotune": {"choice": tuned, "ms_per_step": tuned_ms},
             "speedup_vs_plain_fp64": value / fp64_value,
+            "surrogate_fp32": sur,
+            "surrogate_speedup_vs_plain_fp64": (sur["value"] / fp64_value) if sur else None,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * N_CELLS,
                     "d2h_bytes_per_step": 8 * N_CELLS, "steps": args.e2e_steps,
                     "api": "cm_batch_step_update, pinned host Vm and i_ext"},

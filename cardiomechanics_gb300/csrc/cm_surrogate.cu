@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelAr
     }
     if (valid) {
       const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
+      if (audited) a.pred[c] = __int_as_float(0x7fc00000);  // NaN unless the surrogate predicts below
       if (!fall) {
         float on[kSurOut], corr[kSurOut];
 #pragma unroll
