@@ -31,10 +31,12 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
+// tanh of two FP32 values as one packed BF16 pair (tanh.approx.bf16x2), low half = x
+__device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
+  uint32_t p, r;
+  asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(p) : "f"(x), "f"(y));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(r) : "r"(p));
+  return r;
 }
 
 enum Epi { EPI_BIAS_TANH = 0, EPI_BIAS_F32 = 1, EPI_DTANH = 2, EPI_F32 = 3 };
@@ -95,6 +97,21 @@ __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__
     }
     __syncthreads();
   }
+  if (EPI == EPI_BIAS_TANH) {  // column pairs: one packed BF16 tanh per pair, as in inference
+#pragma unroll
+    for (int mi = 0; mi < 2; mi++)
+#pragma unroll
+      for (int ni = 0; ni < 4; ni++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int m = m0 + wm + mi * 16 + g + h * 8;
+          const int n = n0 + wn + ni * 8 + 2 * t;
+          if (m >= M || n >= N) continue;  // N is even, so n + 1 < N too
+          *reinterpret_cast<uint32_t *>(e.out_bf16 + (size_t)m * e.ldc + n) =
+              tanh2_bf16(acc[mi][ni][2 * h] + e.bias[n], acc[mi][ni][2 * h + 1] + e.bias[n + 1]);
+        }
+    return;
+  }
 #pragma unroll
   for (int mi = 0; mi < 2; mi++)
 #pragma unroll
@@ -106,9 +123,7 @@ __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__
         if (m >= M || n >= N) continue;
         float v = acc[mi][ni][q];
         const size_t o = (size_t)m * e.ldc + n;
-        if (EPI == EPI_BIAS_TANH) {
-          e.out_bf16[o] = __float2bfloat16(tanh_fast(v + e.bias[n]));
-        } else if (EPI == EPI_BIAS_F32) {
+        if (EPI == EPI_BIAS_F32) {
           e.out_f32[o] = v + e.bias[n];
         } else if (EPI == EPI_DTANH) {
           const float h = __bfloat162float(e.h[o]);

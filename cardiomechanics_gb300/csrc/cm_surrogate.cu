@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "cm_bulk.cuh"
 #include "cm_cells.cuh"
 #include "cm_surrogate.h"
 
@@ -124,94 +125,98 @@ constexpr int kWarps = 8, kThreads = kWarps * 32;
 constexpr int kSmemW = (128 * kLdX + 128 * kLdH + 32 * kLdH) * 2;  // bytes
 constexpr int kSmemB = (128 + 128 + 32) * 4;
 constexpr int kSmemWarp = 32 * kLdX * 2 + 2 * 16 * kLdH * 2 + 32 * 33 * 4;
-constexpr int kSmemTotal = kSmemW + kSmemB + kWarps * kSmemWarp;
+constexpr int kStageVars = 21 + 2 + 6;                   // state planes, Vm hi/lo, hetero slots
+constexpr int kSmemStage = kStageVars * kThreads * 4;
+constexpr int kSmemTotal = kSmemW + kSmemB + kWarps * kSmemWarp + kSmemStage;
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+// tanh of two FP32 values as one packed BF16 pair (tanh.approx.bf16x2: one SFU operation)
+__device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
+  uint32_t p, r;
+  asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(p) : "f"(x), "f"(y));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(r) : "r"(p));
+  return r;
+}
+
+// One hidden layer for an m16 tile: OUT[16][128] = tanh(IN[16][K] W^T + b), fragments by
+// ldmatrix.x4 (A: rows r, k halves; B: two n8 tiles x k16 per load).
+template <int K, int LDI>
+__device__ __forceinline__ void hidden_layer(const __nv_bfloat16 *W, int ldw, const float *bias,
+                                             const __nv_bfloat16 *IN, __nv_bfloat16 *OUT, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  const int ar = lane & 15, ac = (lane >> 4) * 8;                          // A lane address
+  const int br = (lane & 7) + ((lane >> 4) << 3), bc = ((lane >> 3) & 1) * 8;  // B lane address
+#pragma unroll 1
+  for (int nc = 0; nc < 128; nc += 32) {
+    float acc[4][4] = {};
+#pragma unroll
+    for (int k = 0; k < K; k += 16) {
+      uint32_t a[4], b01[4], b23[4];
+      ldsm_x4(a, IN + ar * LDI + k + ac);
+      ldsm_x4(b01, W + (nc + br) * ldw + k + bc);
+      ldsm_x4(b23, W + (nc + 16 + br) * ldw + k + bc);
+      mma16816(acc[0], a, b01[0], b01[1]);
+      mma16816(acc[1], a, b01[2], b01[3]);
+      mma16816(acc[2], a, b23[0], b23[1]);
+      mma16816(acc[3], a, b23[2], b23[3]);
+    }
+#pragma unroll
+    for (int ni = 0; ni < 4; ni++) {
+      const int n = nc + ni * 8 + 2 * t;
+      const float b0 = bias[n], b1 = bias[n + 1];
+      *reinterpret_cast<uint32_t *>(OUT + g * kLdH + n) = tanh2_bf16(acc[ni][0] + b0, acc[ni][1] + b1);
+      *reinterpret_cast<uint32_t *>(OUT + (g + 8) * kLdH + n) = tanh2_bf16(acc[ni][2] + b0, acc[ni][3] + b1);
+    }
+  }
+}
 
 // One m16 tile: rows [r0, r0+16) of X (K = 32) through the three layers into Y (FP32).
 __device__ __forceinline__ void mlp_tile(const __nv_bfloat16 *W1, const __nv_bfloat16 *W2, const __nv_bfloat16 *W3,
                                          const float *b1, const float *b2, const float *b3, const __nv_bfloat16 *X,
                                          __nv_bfloat16 *H1, __nv_bfloat16 *H2, float *Y, int r0, int lane) {
+  hidden_layer<32, kLdX>(W1, kLdX, b1, X + r0 * kLdX, H1, lane);
+  __syncwarp();
+  hidden_layer<128, kLdH>(W2, kLdH, b2, H1, H2, lane);
+  __syncwarp();
+  // output layer: Y = H2 W3^T + b3, N = 32
   const int g = lane >> 2, t = lane & 3;
-  // layer 1: H1 = tanh(X W1^T + b1), K = 32
-#pragma unroll 1
-  for (int nc = 0; nc < 128; nc += 32) {
-    float acc[4][4] = {};
+  const int ar = lane & 15, ac = (lane >> 4) * 8;
+  const int br = (lane & 7) + ((lane >> 4) << 3), bc = ((lane >> 3) & 1) * 8;
+  float acc[4][4] = {};
 #pragma unroll
-    for (int k = 0; k < 32; k += 16) {
-      uint32_t a[4];
-      a[0] = lds_u32(X + (r0 + g) * kLdX + k + 2 * t);
-      a[1] = lds_u32(X + (r0 + g + 8) * kLdX + k + 2 * t);
-      a[2] = lds_u32(X + (r0 + g) * kLdX + k + 2 * t + 8);
-      a[3] = lds_u32(X + (r0 + g + 8) * kLdX + k + 2 * t + 8);
-#pragma unroll
-      for (int ni = 0; ni < 4; ni++) {
-        const __nv_bfloat16 *w = W1 + (nc + ni * 8 + g) * kLdX + k + 2 * t;
-        mma16816(acc[ni], a, lds_u32(w), lds_u32(w + 8));
-      }
-    }
-#pragma unroll
-    for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int r = g + (q >> 1) * 8, n = nc + ni * 8 + 2 * t + (q & 1);
-        H1[r * kLdH + n] = __float2bfloat16(tanh_approx(acc[ni][q] + b1[n]));
-      }
+  for (int k = 0; k < 128; k += 16) {
+    uint32_t a[4], b01[4], b23[4];
+    ldsm_x4(a, H2 + ar * kLdH + k + ac);
+    ldsm_x4(b01, W3 + br * kLdH + k + bc);
+    ldsm_x4(b23, W3 + (16 + br) * kLdH + k + bc);
+    mma16816(acc[0], a, b01[0], b01[1]);
+    mma16816(acc[1], a, b01[2], b01[3]);
+    mma16816(acc[2], a, b23[0], b23[1]);
+    mma16816(acc[3], a, b23[2], b23[3]);
   }
-  __syncwarp();
-  // layer 2: H2 = tanh(H1 W2^T + b2), K = 128
-#pragma unroll 1
-  for (int nc = 0; nc < 128; nc += 32) {
-    float acc[4][4] = {};
 #pragma unroll
-    for (int k = 0; k < 128; k += 16) {
-      uint32_t a[4];
-      a[0] = lds_u32(H1 + g * kLdH + k + 2 * t);
-      a[1] = lds_u32(H1 + (g + 8) * kLdH + k + 2 * t);
-      a[2] = lds_u32(H1 + g * kLdH + k + 2 * t + 8);
-      a[3] = lds_u32(H1 + (g + 8) * kLdH + k + 2 * t + 8);
+  for (int ni = 0; ni < 4; ni++)
 #pragma unroll
-      for (int ni = 0; ni < 4; ni++) {
-        const __nv_bfloat16 *w = W2 + (nc + ni * 8 + g) * kLdH + k + 2 * t;
-        mma16816(acc[ni], a, lds_u32(w), lds_u32(w + 8));
-      }
+    for (int q = 0; q < 4; q++) {
+      const int r = g + (q >> 1) * 8, n = ni * 8 + 2 * t + (q & 1);
+      Y[(r0 + r) * 33 + n] = acc[ni][q] + b3[n];
     }
-#pragma unroll
-    for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int r = g + (q >> 1) * 8, n = nc + ni * 8 + 2 * t + (q & 1);
-        H2[r * kLdH + n] = __float2bfloat16(tanh_approx(acc[ni][q] + b2[n]));
-      }
-  }
-  __syncwarp();
-  // layer 3: Y = H2 W3^T + b3, N = 32
-  {
-    float acc[4][4] = {};
-#pragma unroll
-    for (int k = 0; k < 128; k += 16) {
-      uint32_t a[4];
-      a[0] = lds_u32(H2 + g * kLdH + k + 2 * t);
-      a[1] = lds_u32(H2 + (g + 8) * kLdH + k + 2 * t);
-      a[2] = lds_u32(H2 + g * kLdH + k + 2 * t + 8);
-      a[3] = lds_u32(H2 + (g + 8) * kLdH + k + 2 * t + 8);
-#pragma unroll
-      for (int ni = 0; ni < 4; ni++) {
-        const __nv_bfloat16 *w = W3 + (ni * 8 + g) * kLdH + k + 2 * t;
-        mma16816(acc[ni], a, lds_u32(w), lds_u32(w + 8));
-      }
-    }
-#pragma unroll
-    for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int r = g + (q >> 1) * 8, n = ni * 8 + 2 * t + (q & 1);
-        Y[(r0 + r) * 33 + n] = acc[ni][q] + b3[n];
-      }
-  }
   __syncwarp();
 }
 
+// Tiles of kThreads cells: the tile's state planes, Vm planes and conductances arrive in shared
+// memory by bulk async copies (one mbarrier); every thread takes its cell into registers, then
+// thread 0 issues the next tile's copies, which land while this tile's coarse step and MLP run.
 __global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelArgs a, int n) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_abort;
   __nv_bfloat16 *W1 = (__nv_bfloat16 *)smem;
   __nv_bfloat16 *W2 = W1 + 128 * kLdX;
   __nv_bfloat16 *W3 = W2 + 128 * kLdH;
@@ -222,23 +227,75 @@ __global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelAr
   __nv_bfloat16 *H1 = X + 32 * kLdX;
   __nv_bfloat16 *H2 = H1 + 16 * kLdH;
   float *Y = (float *)(H2 + 16 * kLdH);
+  float *stage = (float *)(smem + kSmemW + kSmemB + kWarps * kSmemWarp);
+  const DevBatch &fb = a.fine;
+  const int64_t ld = fb.ld;
+  int het_pos[6];
+  int nv = 23;
+#pragma unroll
+  for (int k = 0; k < 6; k++) het_pos[k] = fb.het[k] ? nv++ : -1;
+  const uint32_t tile_bytes = (uint32_t)nv * kThreads * 4u;
+  const int n_tiles = (n + kThreads - 1) / kThreads;
+  auto issue = [&](int tile) {
+    const int64_t c0 = (int64_t)tile * kThreads;
+    mbar_expect_tx(&bar, tile_bytes);
+    for (int v = 0; v < 21; v++) bulk_g2s(stage + v * kThreads, fb.s32 + v * ld + c0, kThreads * 4u, &bar);
+    bulk_g2s(stage + 21 * kThreads, a.vm_hi + c0, kThreads * 4u, &bar);
+    bulk_g2s(stage + 22 * kThreads, a.vm_lo + c0, kThreads * 4u, &bar);
+    for (int k = 0; k < 6; k++)
+      if (het_pos[k] >= 0) bulk_g2s(stage + het_pos[k] * kThreads, (const float *)fb.het[k] + c0, kThreads * 4u, &bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
   // network into shared memory (padded rows): W1 [128][32], W2 [128][128], W3 [32][128]
   for (int i = threadIdx.x; i < 128 * 32; i += kThreads) W1[(i >> 5) * kLdX + (i & 31)] = a.w1[i];
   for (int i = threadIdx.x; i < 128 * 128; i += kThreads) W2[(i >> 7) * kLdH + (i & 127)] = a.w2[i];
   for (int i = threadIdx.x; i < 32 * 128; i += kThreads) W3[(i >> 7) * kLdH + (i & 127)] = a.w3[i];
   for (int i = threadIdx.x; i < 288; i += kThreads) bias[i] = a.bias[i];
   __syncthreads();
+  if (threadIdx.x == 0 && (int)blockIdx.x < n_tiles) issue(blockIdx.x);
   const float macro_ms = a.coarse.dt * 1000.f;
-  for (int base = blockIdx.x * kThreads; base < n; base += gridDim.x * kThreads) {
-    const int c = base + threadIdx.x;
+  const TT2Consts<float> &C = fb.tt2_32;
+  int it = 0;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
+    if (!mbar_wait(&bar, (uint32_t)(it & 1))) {
+      s_abort = 1;
+      atomicOr(fb.audit_or, kAuditTimeout);
+    }
+    __syncthreads();
+    if (s_abort) {  // the only copy in flight is the one that timed out: give it one more bounded wait
+      mbar_wait(&bar, (uint32_t)(it & 1));
+      return;
+    }
+    const int c = t * kThreads + threadIdx.x;
     const bool valid = c < n;
+    const float *S = stage + threadIdx.x;
     Cell q;
-    Acc vm{0.f, 0.f};
+    q.x.m = S[0]; q.x.h = S[kThreads]; q.x.j = S[2 * kThreads]; q.x.xr1 = S[3 * kThreads];
+    q.x.xr2 = S[4 * kThreads]; q.x.xs = S[5 * kThreads]; q.x.r = S[6 * kThreads]; q.x.s = S[7 * kThreads];
+    q.x.d = S[8 * kThreads]; q.x.f = S[9 * kThreads]; q.x.f2 = S[10 * kThreads]; q.x.fCa = S[11 * kThreads];
+    q.x.Rq = S[12 * kThreads]; q.x.Ca_i = S[13 * kThreads]; q.x.CaSS = S[14 * kThreads];
+    q.CaSR = Acc{S[15 * kThreads], S[16 * kThreads]};
+    q.Na = Acc{S[17 * kThreads], S[18 * kThreads]};
+    q.K = Acc{S[19 * kThreads], S[20 * kThreads]};
+    Acc vm{S[21 * kThreads], S[22 * kThreads]};
+    q.g.g_Na = het_pos[H2_g_Na] >= 0 ? S[het_pos[H2_g_Na] * kThreads] : C.g_Na;
+    q.g.g_Kr = het_pos[H2_g_Kr] >= 0 ? S[het_pos[H2_g_Kr] * kThreads] : C.g_Kr;
+    q.g.g_K1 = het_pos[H2_g_K1] >= 0 ? S[het_pos[H2_g_K1] * kThreads] : C.g_K1;
+    q.g.g_Ks = het_pos[H2_g_Ks] >= 0 ? S[het_pos[H2_g_Ks] * kThreads] : C.g_Ks;
+    q.g.g_to = het_pos[H2_g_to] >= 0 ? S[het_pos[H2_g_to] * kThreads] : C.g_to;
+    q.g.g_CaL = het_pos[H2_g_CaL] >= 0 ? S[het_pos[H2_g_CaL] * kThreads] : C.g_CaL;
+    __syncthreads();  // the stage buffer is free: the next tile's copies overlap this tile's work
+    if (threadIdx.x == 0 && t + (int)gridDim.x < n_tiles) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      issue(t + gridDim.x);
+    }
     float oc[kSurOut], inc[4], f[kSurIn];
     bool fall = !valid;
     if (valid) {
-      load_cell(a.fine, c, q);
-      vm = Acc{a.vm_hi[c], a.vm_lo[c]};
       coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
       const float rate = fabsf(inc[0]) / macro_ms;
       fall = a.stim_on || !(rate <= a.gate_mv_per_ms);
@@ -276,8 +333,8 @@ __global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelAr
         for (int k = 14; k < kSurOut; k++) ok = ok && on[k] > 0.f && isfinite(on[k]);
         if (!ok) {
           fall = true;
-          atomicOr(a.fine.audit_cell + c, 16u);
-          atomicOr(a.fine.audit_or, 16u);
+          atomicOr(fb.audit_cell + c, 16u);
+          atomicOr(fb.audit_or, 16u);
         } else if (audited) {
           a.pred[c] = on[0];
           fall = true;
@@ -285,7 +342,7 @@ __global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelAr
           Cell nq = q;
           Acc nv = vm;
           apply(nq, nv, on, inc, corr);
-          store_cell(a.fine, c, nq);
+          store_cell(fb, c, nq);
           a.vm_hi[c] = nv.hi;
           a.vm_lo[c] = nv.lo;
         }
