@@ -1,7 +1,7 @@
 """Benchmark of the cell-model update on GB300 (one JSON line on stdout).
 
 Workload (default): the precision form -- 4,194,304 ten Tusscher 2006 epicardial cells (a
-2048 x 2048 sheet, reaction step only), FP32 gates/currents with FP64 accumulators, per-cell
+2048 x 2048 sheet, reaction step only), FP32 gates/currents with compensated FP32 accumulators, per-cell
 g_Na/g_Kr/g_K1 scaled by seeded U[0.9, 1.1], stimulus -52 pA/pF for 1 ms every 800 ms,
 dt = 0.01 ms. One step = one dt update of every cell. Inputs are synthetic (seeded), and the
 cell state (~430 MB) is larger than L2, so no flush is needed between steps.
@@ -10,7 +10,7 @@ value     cell-steps/s, state resident in HBM, the fused driver step (cm_batch_r
 e2e       the same through the drop-in C ABI with pinned HOST Vm/i_ext: cm_batch_step_update
           copies Vm and i_ext in and Vm out every step (acCELLerate's CalcCellModels + Godunov)
 plain_fp64  the plain FP64 kernel on the same workload (the reference's arithmetic)
-roofline  the dominant kernel (tt2_mixed_kernel) against the measured HBM copy bandwidth
+roofline  the dominant kernel (the autotuned precision-form shape) against the measured HBM copy
 cpu_baseline  the oracle (C restatement of the reference Calc) on the host cores, bounded sample
 
 --impl reference runs the reference's CPU implementation of the path (the oracle port of its
@@ -37,9 +37,17 @@ DT = 1e-5
 BCL = 0.8
 METRIC = "cell-steps/s on 1 GB300: surrogate+FP32 vs plain FP64 at <=1 ms APD90 error"
 UNIT = "cell-steps/s"
-# Algorithmic bytes per cell-step of tt2_mixed_kernel: 15 FP32 + 3 FP64 state read and
-# written (168 B), Vm read and written (16 B), 3 FP32 per-cell conductances read (12 B).
+# Algorithmic bytes per cell-step of the precision-form kernel: 15 FP32 states plus the
+# CaSR/Na_i/K_i compensated pairs (2 x FP32 each) read and written (168 B), the Vm hi/lo
+# pair read and written (16 B), 3 FP32 per-cell conductances read (12 B).
 MIXED_BYTES_PER_CELL_STEP = 2 * (15 * 4 + 3 * 8) + 2 * 8 + 3 * 4
+# Launch shapes of cm_batch_set_launch (variant index -> kernel); 5 and 6 are bulk-copy staged.
+MIXED_KERNELS = ["tt2_mixed_kernel<256>", "tt2_mixed_kernel<128>", "tt2_mixed_kernel<256,3>",
+                 "tt2_mixed_kernel<512>", "tt2_mixed_kernel<64>", "mixed_staged_kernel<5,256>",
+                 "mixed_staged_kernel<5,128>"]
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu capture summarised in
+# profiles/mixed_staged_tt2_4M_cells.md (same workload, launch shape 6, grid mode 4).
+MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808}
 # tt2_fp64_kernel: 18 FP64 states r+w (288 B), Vm r+w (16 B), 3 FP64 conductances (24 B).
 FP64_BYTES_PER_CELL_STEP = 2 * 18 * 8 + 2 * 8 + 3 * 8
 WORKLOAD = "tt2006-epi-precision-form-2048x2048"
@@ -63,7 +71,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.reader = threading.Thread(target=self._read, daemon=True)
             self.reader.start()
@@ -341,6 +349,7 @@ def main():
     if args.only == "mixed":
         return
     achieved = MIXED_BYTES_PER_CELL_STEP * N_CELLS / (ms_kernel / 1e3) / 1e9
+    kernel = MIXED_KERNELS[tuned // 100] if 0 <= tuned // 100 < len(MIXED_KERNELS) else f"shape {tuned}"
     del b
     torch.cuda.empty_cache()
 
@@ -394,7 +403,7 @@ def main():
             "vs_baseline": None, "dtype": "f32+f64acc", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": N_CELLS, "model": "TenTusscher2 epi", "dt_ms": DT * 1e3,
                        "bcl_ms": BCL * 1e3, "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.9,1.1] seed 2",
-                       "precision": "mixed (FP32 gates/currents, FP64 Vm/Na_i/K_i/CaSR)",
+                       "precision": "mixed (FP32 gates/currents, compensated FP32 pairs for Vm/Na_i/K_i/CaSR)",
                        "l2": "state 430 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas{world}"},
             "plain_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": fp64_ms, "steps": args.fp64_steps,
                            "bytes_per_cell_step": FP64_BYTES_PER_CELL_STEP,
@@ -408,11 +417,13 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * N_CELLS,
                     "d2h_bytes_per_step": 8 * N_CELLS, "steps": args.e2e_steps,
                     "api": "cm_batch_step_update, pinned host Vm and i_ext"},
-            "roofline": {"bound": "hbm", "kernel": "tt2_mixed_kernel", "achieved": achieved, "peak": hbm_peak,
+            "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                         "bytes_per_cell_step": MIXED_BYTES_PER_CELL_STEP, "traffic": None},
+                         "bytes_per_cell_step": MIXED_BYTES_PER_CELL_STEP,
+                         "algorithmic_bytes_per_launch": MIXED_BYTES_PER_CELL_STEP * N_CELLS,
+                         "traffic": MEASURED_TRAFFIC.get(kernel)},
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps + 2,  # the steps plus the Vm split/join of cm_batch_run
             "clocks": clk.summary(),
             "audit_mask": audit,
         }
