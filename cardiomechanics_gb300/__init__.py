@@ -47,7 +47,7 @@ ABI_SYMBOLS = (
     "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
     "cm_surrogate_destroy", "cm_surrogate_mlp", "cm_surrogate_generate", "cm_surrogate_dataset",
     "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
-    "cm_batch_run_surrogate",
+    "cm_batch_run_surrogate", "cm_mlp_forward_static",
 )
 
 
@@ -128,6 +128,7 @@ def lib() -> ctypes.CDLL:
     for f in ("cm_mlp_get_params", "cm_mlp_set_params", "cm_mlp_get_grads"):
         getattr(L, f).argtypes = [vp, vp]
     L.cm_mlp_forward.argtypes = [vp, vp, i64, vp]
+    L.cm_mlp_forward_static.argtypes = [vp, vp, i64, vp]
     L.cm_mlp_loss_grad.argtypes = [vp, vp, vp, i64, fp]
     L.cm_mlp_adam_step.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
     L.cm_surrogate_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.c_int, ctypes.c_uint64, vp]

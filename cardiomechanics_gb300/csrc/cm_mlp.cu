@@ -385,6 +385,26 @@ cudaError_t Mlp::forward(const float *X, int64_t n, float *Y) {
   return cudaSuccess;
 }
 
+size_t Mlp::forward_scratch_bytes_per_row() const {
+  return (size_t)(in_pad + 2 * H) * sizeof(__nv_bfloat16) + (size_t)out_pad * sizeof(float);
+}
+
+cudaError_t Mlp::forward_in_scratch(void *scratch, const float *X, int64_t n, float *Y) {
+  const int rows = (int)(((n + 63) / 64) * 64);
+  // X | H1 | H2 (BF16) | Y (FP32); rows is a multiple of 64, so every part starts 256-byte aligned
+  Buffers B{};
+  B.X = (__nv_bfloat16 *)scratch;
+  B.H1 = B.X + (size_t)rows * in_pad;
+  B.H2 = B.H1 + (size_t)rows * H;
+  B.Y = (float *)(B.H2 + (size_t)rows * H);
+  pack_inputs<<<1024, 256, 0, stream>>>(X, (int)n, n_in, rows, in_pad, B.X);  // writes the padding too
+  MCK(cudaGetLastError());
+  MCK(forward_rows(B, rows));
+  MCK(cudaMemcpy2DAsync(Y, n_out * sizeof(float), B.Y, out_pad * sizeof(float), n_out * sizeof(float), n,
+                        cudaMemcpyDeviceToDevice, stream));
+  return cudaSuccess;
+}
+
 cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
   const int rows = (int)(((n + 63) / 64) * 64);
   MCK(workspace(rows));

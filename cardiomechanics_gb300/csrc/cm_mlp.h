@@ -31,6 +31,13 @@ struct Mlp {
   cudaError_t sync_bf16();  // after host-side weight changes
   // X: n x n_in (device, FP32); Y: n x n_out (device, FP32)
   cudaError_t forward(const float *X, int64_t n, float *Y);
+  // Bytes of scratch forward_in_scratch needs per row of a 64-row-padded batch: packed BF16
+  // inputs, both BF16 hidden activations and the padded FP32 outputs.
+  size_t forward_scratch_bytes_per_row() const;
+  // forward() with its intermediates in caller-provided device scratch (256-byte aligned, at
+  // least rows_pad x forward_scratch_bytes_per_row() bytes, rows_pad = n rounded up to 64);
+  // allocates nothing. Every byte of scratch it reads it has written first.
+  cudaError_t forward_in_scratch(void *scratch, const float *X, int64_t n, float *Y);
   // forward + backward on n samples (device FP32 X, T); gradients in g, mean loss in *loss
   cudaError_t loss_grad(const float *X, const float *T, int64_t n);
   cudaError_t adam_step(float lr, float b1, float b2, float eps);

@@ -10,6 +10,7 @@
 
 #include "cm_handles.h"
 #include "cm_mlp.h"
+#include "cm_noalloc.h"
 #include "cm_surrogate.h"
 
 using namespace cm;
@@ -623,6 +624,24 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     stats->max_audit_err_mv = aerr;
   }
   if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+int cm_mlp_forward_static(cm_mlp_t m, const float *X, int64_t n, float *Y) {
+  if (!m || !X || !Y || n < 0) return fail(CM_ERR_ARG, "bad argument");
+  if (n == 0) return CM_OK;
+  if (!is_device_ptr(X) || !is_device_ptr(Y))
+    return fail(CM_ERR_ARG, "cm_mlp_forward_static takes device arrays only (staging host arrays would allocate)");
+  void *scratch = nullptr;
+  size_t bytes = 0;
+  CK(static_scratch(&scratch, &bytes));
+  const int64_t max_rows = (int64_t)(bytes / m->m.forward_scratch_bytes_per_row()) / 64 * 64;
+  if (n > max_rows)
+    return fail(CM_ERR_ARG, "cm_mlp_forward_static: n = " + std::to_string(n) + " rows exceeds the static scratch (" +
+                                std::to_string(bytes) + " bytes: at most " + std::to_string(max_rows) +
+                                " rows for this network)");
+  CK(m->m.forward_in_scratch(scratch, X, n, Y));
+  CK(cudaStreamSynchronize(m->m.stream));
   return CM_OK;
 }
 

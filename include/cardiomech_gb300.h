@@ -236,6 +236,21 @@ int cm_mlp_set_params(cm_mlp_t m, const float *params);
 int cm_mlp_get_grads(cm_mlp_t m, float *grads);
 /* Y[n][n_out] = MLP(X[n][n_in]). */
 int cm_mlp_forward(cm_mlp_t m, const float *X, int64_t n, float *Y);
+/* Same result as cm_mlp_forward, for callers that must not allocate device memory during the
+   call: a host code whose pool allocator owns the whole device, or a time-stepping loop that
+   must not meet the device-wide synchronisation of cudaMalloc/cudaFree. No counterpart in the
+   reference (its cell models have no network). X (n x n_in) and Y (n x n_out) must be device
+   arrays; host arrays are rejected with CM_ERR_ARG, because staging them would allocate. The
+   intermediates live in one fixed 8 MiB __device__ array per device, so n is limited to
+   8 MiB / (2*(in_pad + 2*n_hidden) + 4*out_pad) bytes per row, rounded down to a multiple of 64
+   (11,904 rows for the 22-128-128-19 surrogate network, in_pad = out_pad = 32); larger n is
+   rejected with CM_ERR_ARG and a message giving the limit. Nothing in that array has to start
+   at zero. The first call on a device (with that device current) looks the array's address up
+   and loads it there; make that first call before any stream capture. The array is shared by
+   every caller in the process: two calls that overlap in time, from two threads or on
+   unordered streams, corrupt each other's results. Runs on the MLP's stream and returns after
+   it has finished, like cm_mlp_forward. */
+int cm_mlp_forward_static(cm_mlp_t m, const float *X, int64_t n, float *Y);
 /* Mean squared error over the n x n_out outputs against T and its gradients. */
 int cm_mlp_loss_grad(cm_mlp_t m, const float *X, const float *T, int64_t n, float *loss);
 int cm_mlp_adam_step(cm_mlp_t m, float lr, float beta1, float beta2, float eps);
