@@ -275,6 +275,61 @@ def surrogate_leg(cm, torch, stream, steps, warmup, gen_frac=1.0):
             "stats": stats, "gpu_launches": 2 * steps}
 
 
+BATCHED_SEED = 21
+BATCHED_BCL = 1.0
+# Algorithmic bytes per cell-step of the batched kernel (no per-cell conductances: each
+# instance has its own parameter set): state planes and the Vm hi/lo pair read and written.
+BATCHED_BYTES = {"TenTusscher2": 2 * 21 * 4 + 2 * 8, "CourtemancheEtAl": 2 * 25 * 4 + 2 * 8}
+
+
+def batched_leg(cm, torch, stream, steps, warmup, hbm_peak, peak_kind):
+    """Batched form: 256 instances (log-uniform 1k..1M cells, ten Tusscher 2006 or Courtemanche
+    1998, own parameter set with six conductances x U[0.8, 1.2], stimulus phase U[0, BCL)),
+    advanced in lock step by one persistent launch per step, replayed from a CUDA graph, launch
+    shape autotuned on the instances. One step = one dt update of every cell of every instance."""
+    from cardiomechanics_gb300 import workloads as W
+    inst = W.batched_instances(BATCHED_SEED)
+    batches, stims, vms = [], [], []
+    for d in inst:
+        p = cm.Params(d["model"], None, DT)
+        for nm, sc in d["scales"].items():
+            p.set(nm, p.get(nm) * sc)
+        b = cm.Batch(p, d["n"], cm.MIXED, stream=stream.cuda_stream)
+        batches.append(b)
+        vms.append(torch.tensor(b.init_vm(), device="cuda"))
+        tt2 = d["model"] == "TenTusscher2"
+        stims.append({"textbegin": d["phase"] * BATCHED_BCL, "textlen": 1e-3 if tt2 else 2e-3, "bcl": BATCHED_BCL,
+                      "amplitude": W.TT2_STIM_NA if tt2 else W.CRN_STIM_PAPF})
+    multi = cm.Multi(batches, stream=stream.cuda_stream)
+    tuned = multi.autotune(5)
+    multi.run(vms, warmup, [dict(s, t0=0.0) for s in stims])
+    timed = []
+    for s in stims:
+        t, tb = advance_protocol(0.0, s["textbegin"], warmup, s["bcl"], s["textlen"])
+        timed.append(dict(s, t0=t, textbegin=tb))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    multi.run(vms, steps, timed)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    cells = sum(d["n"] for d in inst)
+    algo = sum(d["n"] * BATCHED_BYTES[d["model"]] for d in inst)
+    achieved = algo * steps / sec / 1e9
+    out = {"value": cells * steps / sec, "unit": UNIT, "instances": len(inst), "cells": cells,
+           "tt2_instances": sum(d["model"] == "TenTusscher2" for d in inst), "steps": steps,
+           "ms_per_step": 1e3 * sec / steps, "bcl_ms": BATCHED_BCL * 1e3, "autotune": tuned,
+           "sizes": "log-uniform [1e3, 1e6] seed %d" % BATCHED_SEED,
+           "roofline": {"bound": "hbm", "kernel": "multi_kernel", "achieved": achieved, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                        "algorithmic_bytes_per_step": algo},
+           "gpu_launches": steps + 2 * len(inst)}
+    del multi, batches
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -285,11 +340,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "mixed", "fp64", "e2e", "surrogate"],
+    ap.add_argument("--only", default="all", choices=["all", "mixed", "fp64", "e2e", "surrogate", "batched"],
                     help="run one leg only (for profiler captures); the JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the learned form")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=640, help="timed steps of the batched form")
     ap.add_argument("--sur-train-frac", type=float, default=1.0,
                     help="fraction of the surrogate's training run (profiling captures only; accuracy needs 1)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
@@ -311,6 +368,9 @@ def main():
 
     if args.only == "surrogate":
         print(json.dumps(surrogate_leg(cm, torch, stream, args.sur_steps, 20, args.sur_train_frac)), flush=True)
+        return
+    if args.only == "batched":
+        print(json.dumps(batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)), flush=True)
         return
     if args.only == "fp64":
         _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
@@ -392,6 +452,11 @@ def main():
         torch.cuda.empty_cache()
         sur = surrogate_leg(cm, torch, stream, args.sur_steps, 20)
 
+    bat = None
+    if not args.no_batched:
+        torch.cuda.empty_cache()
+        bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(seconds=args.cpu_seconds)
@@ -414,6 +479,7 @@ def main():
             "speedup_vs_plain_fp64": value / fp64_value,
             "surrogate_fp32": sur,
             "surrogate_speedup_vs_plain_fp64": (sur["value"] / fp64_value) if sur else None,
+            "batched": bat,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * N_CELLS,
                     "d2h_bytes_per_step": 8 * N_CELLS, "steps": args.e2e_steps,
                     "api": "cm_batch_step_update, pinned host Vm and i_ext"},

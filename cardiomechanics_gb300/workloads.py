@@ -51,3 +51,25 @@ CRN_STIM_PAPF = 20.0
 # Per-cell heterogeneous conductances used by the workloads, by model.
 TT2_HETERO = ("g_Na", "g_Kr", "g_K1")
 CRN_HETERO = ("g_Na", "g_to", "g_CaL")
+
+# Conductances a per-instance parameter set scales in the batched form, by model (the
+# heterogeneity slots of each model).
+TT2_INSTANCE_G = ("g_Na", "g_Kr", "g_K1", "g_Ks", "g_to", "g_CaL")
+CRN_INSTANCE_G = ("g_Na", "g_to", "g_Ks", "g_CaL", "g_bNa", "g_bCa")
+
+
+def batched_instances(seed: int, n_inst: int = 256, lo: int = 1_000, hi: int = 1_000_000,
+                      g_lo: float = 0.8, g_hi: float = 1.2) -> list[dict]:
+    """Instances of the batched form: size log-uniform in [lo, hi] cells, model ten Tusscher 2006
+    or Courtemanche 1998 with equal probability, each of the model's six instance conductances
+    scaled by U[g_lo, g_hi], stimulus phase U[0, 1) of the cycle length. Draw index of instance
+    i, field k (0 size, 1 model, 2 phase, 3..8 conductances) = i * 9 + k."""
+    out = []
+    for i in range(n_inst):
+        u = uniform(seed, np.arange(i * 9, i * 9 + 9, dtype=np.uint64))
+        n = int(round(np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u[0])))
+        model = "TenTusscher2" if u[1] < 0.5 else "CourtemancheEtAl"
+        names = TT2_INSTANCE_G if model == "TenTusscher2" else CRN_INSTANCE_G
+        out.append({"n": n, "model": model, "phase": float(u[2]),
+                    "scales": {nm: g_lo + (g_hi - g_lo) * float(u[3 + k]) for k, nm in enumerate(names)}})
+    return out
