@@ -757,6 +757,7 @@ MultiLaunch multi_launch_desc(const cm_multi_s *m) {
   L.counters = m->d_counters;
   L.shape = m->shape;
   L.grid = std::max(1, sm_count() * m->blocks_per_sm);
+  L.tile_cells = m->tile_cells;
   return L;
 }
 

@@ -6,8 +6,10 @@
 // step parity), so consecutive steps are identical launches that a CUDA graph can replay.
 #include <cuda_runtime.h>
 
+#include "cm_bulk.cuh"
 #include "cm_cells.cuh"
 #include "cm_multi.h"
+#include "cm_staged_cell.cuh"
 
 namespace cm {
 
@@ -77,10 +79,129 @@ __global__ void __launch_bounds__(kBlock, kMinB)
   }
 }
 
+// The same step with each tile's cells staged through shared memory by bulk async copies in
+// sub-tiles of kT cells, double-buffered: thread 0 schedules the block's next sub-tile (the next
+// one of its tile, or a new tile from the counter) and issues its copies before the block
+// integrates the current one. The instance's descriptor is copied to shared memory when the
+// block moves to another instance. Requires tile starts and sizes in whole sub-tiles, which the
+// launcher checks. Bounded waits as in the single-batch staged kernel.
+template <int kT>
+__global__ void __launch_bounds__(kT, 2)
+    multi_staged_kernel(const MultiInst *__restrict__ insts, const MultiTile *__restrict__ tiles, int n_tiles,
+                        const MultiClock *__restrict__ clk_cur, MultiClock *__restrict__ clk_next,
+                        unsigned int *__restrict__ counter, unsigned int *__restrict__ counter_next) {
+  constexpr int NVMAX = StagedVars<2>::kState + 2 + 6;  // the larger model
+  extern __shared__ __align__(128) float stage[];      // [2][NVMAX][kT]
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ DevBatch sb;
+  __shared__ int s_tile[2], s_sub[2], s_abort;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *counter_next = 0;  // the next step's counter
+  auto issue = [&](int tile, int sub, int buf) {  // thread 0
+    const MultiTile T = tiles[tile];
+    const MultiInst *I = insts + T.inst;
+    const int64_t ld = I->d.ld;
+    const int ns = I->d.model == 5 ? StagedVars<5>::kState : StagedVars<2>::kState;
+    int nh = 0;
+    for (int k = 0; k < 6; k++) nh += I->d.het[k] ? 1 : 0;
+    const int64_t c0 = (int64_t)T.start + (int64_t)sub * kT;
+    float *dst = stage + (size_t)buf * NVMAX * kT;
+    mbar_expect_tx(&bar[buf], (uint32_t)(ns + 2 + nh) * kT * 4u);
+    for (int v = 0; v < ns; v++) bulk_g2s(dst + v * kT, I->d.s32 + v * ld + c0, kT * 4u, &bar[buf]);
+    bulk_g2s(dst + ns * kT, I->vm_hi + c0, kT * 4u, &bar[buf]);
+    bulk_g2s(dst + (ns + 1) * kT, I->vm_lo + c0, kT * 4u, &bar[buf]);
+    int pos = ns + 2;
+    for (int k = 0; k < 6; k++)
+      if (I->d.het[k]) bulk_g2s(dst + (pos++) * kT, (const float *)I->d.het[k] + c0, kT * 4u, &bar[buf]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    const int t0 = (int)atomicAdd(counter, 1u);
+    s_tile[0] = t0 < n_tiles ? t0 : -1;
+    s_sub[0] = 0;
+    if (t0 < n_tiles) issue(t0, 0, 0);
+  }
+  int cur_inst = -1;
+  int het_pos[6] = {-1, -1, -1, -1, -1, -1};
+  for (int it = 0;; it++) {
+    const int buf = it & 1;
+    __syncthreads();  // s_tile[buf] is visible; buffer buf ^ 1 and sb are free
+    const int tile = s_tile[buf];
+    if (tile < 0) break;
+    const int sub = s_sub[buf];
+    const MultiTile T = tiles[tile];
+    if (threadIdx.x == 0) {  // the block's next sub-tile, prefetched into the other buffer
+      int nt = tile, nsub = sub + 1;
+      if ((int64_t)nsub * kT >= T.count) {
+        const int a = (int)atomicAdd(counter, 1u);
+        nt = a < n_tiles ? a : -1;
+        nsub = 0;
+      }
+      s_tile[buf ^ 1] = nt;
+      s_sub[buf ^ 1] = nsub;
+      if (nt >= 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        issue(nt, nsub, buf ^ 1);
+      }
+    }
+    const MultiInst *I = insts + T.inst;
+    if (T.inst != cur_inst) {  // block-uniform
+      const int4 *src = reinterpret_cast<const int4 *>(&I->d);
+      int4 *dst = reinterpret_cast<int4 *>(&sb);
+      for (int k = threadIdx.x; k < (int)(sizeof(DevBatch) / sizeof(int4)); k += kT) dst[k] = src[k];
+      __syncthreads();
+      cur_inst = T.inst;
+      int pos = sb.model == 5 ? StagedVars<5>::kState + 2 : StagedVars<2>::kState + 2;
+#pragma unroll
+      for (int k = 0; k < 6; k++) het_pos[k] = sb.het[k] ? pos++ : -1;
+    }
+    const MultiClock ck = clk_cur[T.inst];
+    const float iext = ck.t >= ck.tb ? (float)I->amp : 0.f;
+    if (T.start == 0 && sub == 0 && threadIdx.x == 0) {  // reference driver clock (CellModel.h:405-419)
+      MultiClock nx;
+      nx.t = ck.t + I->dt;
+      nx.tb = (ck.t >= ck.tb && ck.t >= ck.tb + I->textlen) ? ck.tb + I->bcl : ck.tb;
+      clk_next[T.inst] = nx;
+    }
+    if (!mbar_wait(&bar[buf], (uint32_t)((it >> 1) & 1))) {
+      s_abort = 1;
+      atomicOr(sb.audit_or, kAuditTimeout);
+    }
+    __syncthreads();
+    if (s_abort) {
+      if (s_tile[buf ^ 1] >= 0) mbar_wait(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      return;
+    }
+    const float *S = stage + (size_t)buf * NVMAX * kT + threadIdx.x;
+    const int c = T.start + sub * kT + (int)threadIdx.x;
+    if (c < T.start + T.count) {
+      if (sb.model == 5) staged_cell<5, kT>(sb, S, het_pos, c, iext, I->vm_hi, I->vm_lo);
+      else staged_cell<2, kT>(sb, S, het_pos, c, iext, I->vm_hi, I->vm_lo);
+    }
+  }
+}
+
 struct MShape {
   int block, minb;
+  bool staged;
 };
-constexpr MShape kMShapes[] = {{256, 2}, {128, 5}, {512, 1}};
+constexpr MShape kMShapes[] = {{256, 2, false}, {128, 5, false}, {512, 1, false}, {128, 2, true}, {256, 2, true}};
+
+template <int kT>
+cudaError_t launch_multi_staged(const MultiLaunch &L, const MultiClock *cur, MultiClock *nxt, unsigned int *cnt,
+                                unsigned int *cnt_next, cudaStream_t s) {
+  constexpr size_t smem = (size_t)2 * (StagedVars<2>::kState + 2 + 6) * kT * sizeof(float);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(multi_staged_kernel<kT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  multi_staged_kernel<kT><<<L.grid, kT, smem, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next);
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -93,7 +214,15 @@ cudaError_t launch_multi(const MultiLaunch &L, int parity, cudaStream_t s) {
   unsigned int *cnt = L.counters + (parity & 1);
   unsigned int *cnt_next = L.counters + ((parity & 1) ^ 1);
   const int grid = L.grid;
-  switch (L.shape) {
+  int shape = L.shape;
+  if (shape >= 0 && shape < n_multi_shapes() && kMShapes[shape].staged) {
+    if (L.tile_cells % kMShapes[shape].block == 0) {
+      return kMShapes[shape].block == 128 ? launch_multi_staged<128>(L, cur, nxt, cnt, cnt_next, s)
+                                          : launch_multi_staged<256>(L, cur, nxt, cnt, cnt_next, s);
+    }
+    shape = 0;  // tiles not in whole sub-tiles: the unstaged kernel
+  }
+  switch (shape) {
     case 1: multi_kernel<128, 5><<<grid, 128, 0, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next); break;
     case 2: multi_kernel<512, 1><<<grid, 512, 0, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next); break;
     default: multi_kernel<256, 2><<<grid, 256, 0, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next); break;

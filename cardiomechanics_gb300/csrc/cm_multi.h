@@ -28,6 +28,7 @@ struct MultiLaunch {
   MultiClock *clk = nullptr;          // 2 x n_inst, by step parity
   unsigned int *counters = nullptr;   // 2, by step parity
   int shape = 0, grid = 0;
+  int tile_cells = 0;                 // every tile starts at a multiple of it within its instance
 };
 
 int n_multi_shapes();

@@ -54,7 +54,10 @@ def test_multi_equals_single(gpu):
         b.run(v, 1000, **s)
         b.run(v, steps - 1000, **continued(s, 1000))
         ref_v.append(v)
-    for shape, (tile, bps) in enumerate([(2048, 2), (1024, 4), (4096, 1)]):
+    # shapes 0-2: plain loads; 3-4: bulk-copy staged sub-tiles of 128 / 256 cells (the 1000-cell
+    # tiles of the last case are not whole sub-tiles: the launcher takes the plain kernel)
+    cases = [(0, 2048, 2), (1, 1024, 4), (2, 4096, 1), (3, 1024, 4), (4, 2048, 2), (3, 4096, 8), (4, 1000, 2)]
+    for shape, tile, bps in cases:
         mb = build(cm, sizes, models)
         multi = cm.Multi(mb)
         multi.set_launch(tile, shape, bps)
