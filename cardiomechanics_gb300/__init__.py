@@ -35,13 +35,17 @@ _STATUS = {0: "CM_OK", -1: "CM_ERR_ARG", -2: "CM_ERR_MODEL", -3: "CM_ERR_FILE", 
            -5: "CM_ERR_CUDA", -6: "CM_ERR_NOMEM", -7: "CM_ERR_UNSUPPORTED", -8: "CM_ERR_NUMERIC"}
 
 # Exported symbols of the C ABI (include/cardiomech_gb300.h).
+# cm_batch_run_surrogate mode bits
+SUR_COARSE_ONLY = 1
+SUR_AUDIT_FP64 = 2
+
 ABI_SYMBOLS = (
     "cm_abi_version", "cm_last_error", "cm_model_from_name", "cm_model_info", "cm_state_name",
     "cm_params_create", "cm_params_destroy", "cm_params_info", "cm_params_get", "cm_params_set",
     "cm_params_table", "cm_batch_create", "cm_batch_destroy", "cm_batch_info", "cm_batch_reset",
     "cm_batch_set_hetero", "cm_batch_set_diagnostics", "cm_batch_init_vm", "cm_batch_get_state",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
-    "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak",
+    "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
     "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
     "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
@@ -144,6 +148,7 @@ def lib() -> ctypes.CDLL:
     L.cm_batch_run_surrogate.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(SurrogateStats)]
     L.cm_diag_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
+    L.cm_diag_umma_tile.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
     _lib = L
     return L
 
@@ -173,6 +178,15 @@ def _f64(a, n, name):
     if a.dtype != torch.float64 or not a.is_contiguous() or a.numel() != n:
         raise ValueError(f"{name}: need a contiguous float64 tensor of {n} elements")
     return a
+
+
+def _per_cell_times(a, n):
+    """Per-cell first stimulus times: None, a float64 numpy array or tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray) or not hasattr(a, "data_ptr"):
+        return _f64(np.ascontiguousarray(a, np.float64), n, "textbegin_per_cell")
+    return _f64(a, n, "textbegin_per_cell")
 
 
 def fma_peak_tflops(fp64: bool, stream=None) -> float:
@@ -300,10 +314,8 @@ class Batch:
         """Fused driver loop; Vm (host numpy or device tensor) updated in place. Returns the
         probe traces (n_probe, n_rec) when probe_cells is given."""
         Vm = _f64(Vm, self.n, "Vm")
-        tbc = None
-        if textbegin_per_cell is not None:
-            tbc = np.ascontiguousarray(textbegin_per_cell, np.float64)
-        st = Stimulus(t0, textbegin, None if tbc is None else tbc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+        tbc = _per_cell_times(textbegin_per_cell, self.n)
+        st = Stimulus(t0, textbegin, None if tbc is None else ctypes.cast(_ptr(tbc), ctypes.POINTER(ctypes.c_double)),
                       textlen, bcl, amplitude)
         pc = None
         n_probe = 0
@@ -328,11 +340,14 @@ class Batch:
         _check(lib().cm_batch_set_launch(self._h, variant, grid_mode))
 
     def run_surrogate(self, surrogate, Vm, n_macro, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0,
-                      t0=0.0, mode=0, audit_mod=100):
+                      t0=0.0, mode=0, audit_mod=100, textbegin_per_cell=None):
         """n_macro learned macro steps (surrogate.substeps fine steps each); Vm updated in place.
-        mode 0: coarse step + network, 1: coarse step alone. Returns the run statistics."""
+        mode 0: coarse step + network, SUR_COARSE_ONLY: coarse step alone; | SUR_AUDIT_FP64: the
+        audit sample is integrated in FP64. Returns the run statistics."""
         Vm = _f64(Vm, self.n, "Vm")
-        st = Stimulus(t0, textbegin, None, textlen, bcl, amplitude)
+        tbc = _per_cell_times(textbegin_per_cell, self.n)
+        st = Stimulus(t0, textbegin, None if tbc is None else ctypes.cast(_ptr(tbc), ctypes.POINTER(ctypes.c_double)),
+                      textlen, bcl, amplitude)
         stats = SurrogateStats()
         _check(lib().cm_batch_run_surrogate(self._h, surrogate._h, _ptr(Vm), int(n_macro), ctypes.byref(st), mode,
                                             audit_mod, ctypes.byref(stats)))

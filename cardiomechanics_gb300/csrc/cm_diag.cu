@@ -2,9 +2,12 @@
 // GB300 rate is not in the driver's measured peaks. Each thread runs 8 independent FMA
 // chains (enough to cover the pipe latency at full occupancy); the result is written so the
 // chains are not dead code.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/cardiomech_gb300_diag.h"
+#include "cm_bulk.cuh"
+#include "cm_umma.cuh"
 
 namespace {
 
@@ -52,6 +55,78 @@ int measure(double *tflops, void *stream, int iters) {
 }
 
 }  // namespace
+
+// D (128 x N, FP32) = A (128 x K) * B (N x K)^T on the tcgen05 tensor core, operands staged in
+// shared memory in the learned macro step's layout, accumulator in TMEM read back with
+// tcgen05.ld: one tile, one block of 128 threads (thread i owns row i = TMEM lane i).
+__global__ void __launch_bounds__(128) umma_tile_kernel(const __nv_bfloat16 *__restrict__ A,
+                                                        const __nv_bfloat16 *__restrict__ B, int N, int K,
+                                                        float *__restrict__ D, unsigned int *err) {
+  using namespace cm;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  __nv_bfloat16 *sA = (__nv_bfloat16 *)smem;
+  __nv_bfloat16 *sB = sA + 128 * K;
+  const int warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 128 * K; i += 128) sA[umma::kmajor_index(i / K, i % K, K)] = A[i];
+  for (int i = threadIdx.x; i < N * K; i += 128) sB[umma::kmajor_index(i / K, i % K, K)] = B[i];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) umma::tmem_alloc(&tslot, 128);
+  umma::fence_smem_to_async();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tslot;
+  if (threadIdx.x == 0) {
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB), sbo = (uint32_t)(K / 8) * 128u;
+    const uint32_t idesc = umma::idesc_bf16_f32(128, N);
+    for (int s = 0; s < K / 16; s++)
+      umma::mma_bf16(tmem, umma::smem_desc(a0 + s * 256u, 128u, sbo), umma::smem_desc(b0 + s * 256u, 128u, sbo),
+                     idesc, s > 0);
+    umma::commit(&bar);
+  }
+  bool ok = mbar_wait(&bar, 0);
+  ok = __syncthreads_and(ok);
+  umma::fence_after_sync();
+  if (ok) {
+    for (int c0 = 0; c0 < N; c0 += 32) {
+      float v[32];
+      umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int j = 0; j < 32; j++) D[(size_t)threadIdx.x * N + c0 + j] = v[j];
+    }
+  } else {
+    if (threadIdx.x == 0) atomicOr(err, 1u);
+    mbar_wait(&bar, 0);  // one more bounded wait for the MMAs before their TMEM is released
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_free(tmem, 128);
+}
+
+extern "C" int cm_diag_umma_tile(const void *A, const void *B, int n, int k, float *D, void *stream) {
+  if (!A || !B || !D || (n != 32 && n != 64 && n != 128) || (k != 32 && k != 64 && k != 128)) return CM_DIAG_ERR;
+  const size_t smem = (size_t)(128 + n) * k * sizeof(__nv_bfloat16);
+  if (cudaFuncSetAttribute(umma_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return CM_DIAG_ERR;
+  unsigned int *err = nullptr;
+  if (cudaMalloc(&err, sizeof(unsigned int)) != cudaSuccess) return CM_DIAG_ERR;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int h = 0;
+  cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned int), s);
+  if (e == cudaSuccess) {
+    umma_tile_kernel<<<1, 128, smem, s>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, n, k, D, err);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, err, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(err);
+  return (e == cudaSuccess && h == 0) ? 0 : CM_DIAG_ERR;
+}
 
 extern "C" int cm_diag_fma_peak(int fp64, double *tflops, void *stream) {
   if (!tflops) return CM_DIAG_ERR;

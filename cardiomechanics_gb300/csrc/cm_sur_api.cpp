@@ -25,6 +25,9 @@ struct cm_surrogate_s {
   cudaStream_t stream = nullptr;
   TT2Consts<float> coarse{};
   float *rows_coarse = nullptr, *eca = nullptr;
+  // FP64 constants and tables of the fine step (the audit sample integrated in FP64)
+  TT2Consts<double> fine64{};
+  double *rows_fine64 = nullptr, *eca_fine64 = nullptr;
   cm_mlp_s net;
   SurNorm norm{};
   bool fitted = false;
@@ -43,6 +46,7 @@ struct cm_surrogate_s {
   unsigned int *n_fallback = nullptr;
   unsigned long long *totals = nullptr;  // n_sur, n_fallback_total, n_audit
   float *audit_err = nullptr;
+  float *bias_block = nullptr;  // b1 | b2 | b3 of the network, contiguous (the inference kernel's layout)
 };
 
 namespace {
@@ -288,7 +292,7 @@ int cm_surrogate_destroy(cm_surrogate_t s) {
   for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
                   (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
                   (void *)s->gkeep, (void *)s->fallback, (void *)s->pred, (void *)s->n_fallback, (void *)s->totals,
-                  (void *)s->audit_err})
+                  (void *)s->audit_err, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block})
     cudaFree(p);
   delete s;
   return CM_OK;
@@ -316,16 +320,27 @@ int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64
   if (e == cudaSuccess) e = cudaMalloc(&s->eca, eca.size() * sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(s->rows_coarse, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->eca, eca.data(), eca.size() * sizeof(float), cudaMemcpyHostToDevice);
+  {
+    TT2Consts<float> f32;
+    s->fine.tt2_consts(s->fine64, f32);
+    std::vector<double> r64, e64;
+    s->fine.rows_fp64(r64, e64);
+    if (e == cudaSuccess) e = cudaMalloc(&s->rows_fine64, r64.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->eca_fine64, e64.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(s->rows_fine64, r64.data(), r64.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->eca_fine64, e64.data(), e64.size() * sizeof(double), cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&s->d_count, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(s->d_count, 0, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&s->n_fallback, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&s->totals, 3 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&s->audit_err, sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->bias_block, 288 * sizeof(float));
   if (e == cudaSuccess) e = s->net.m.init(kSurIn, kSurH, kSurOut, seed, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) rc = cuda_fail(e, "cm_surrogate_create");
   for (int k = 0; k < kSurIn; k++) s->norm.inv_sd_x[k] = 1.f;
-  for (int k = 0; k < kSurOut; k++) s->norm.sd_y[k] = 1.f;
+  for (int k = 0; k < kSurOut; k++) s->norm.sd_y[k] = s->norm.apply_y[k] = 1.f;
   if (rc) {
     std::string keep = last_error();
     cm_surrogate_destroy(s);
@@ -345,6 +360,8 @@ int cm_surrogate_mlp(cm_surrogate_t s, cm_mlp_t *mlp) {
 int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_macro, const cm_stimulus *stim,
                           int64_t cell_stride, int64_t max_pairs, int64_t *n_pairs) {
   if (!s || !Vm || n_macro < 0 || cell_stride < 1 || max_pairs < 0) return fail(CM_ERR_ARG, "bad argument");
+  if (stim && stim->textbegin_per_cell)
+    return fail(CM_ERR_UNSUPPORTED, "training-data generation takes one stimulus protocol for all cells");
   int rc = check_batch(b);
   if (rc) return rc;
   if (b->ps.dt != s->fine.dt) return fail(CM_ERR_ARG, "batch dt differs from the surrogate's fine dt");
@@ -487,6 +504,38 @@ int cm_surrogate_fit(cm_surrogate_t s, int batch, int steps, float lr, uint64_t 
   float loss = 0;
   CK(s->net.m.train(s->nX, s->nT, n, batch, steps, lr, seed, &loss));
   CK(cudaStreamSynchronize(s->stream));
+  // R^2 of every output on a strided subsample: which corrections the network predicts
+  {
+    const int64_t mv = std::min<int64_t>(n, (int64_t)1 << 16), sv = n / mv;
+    std::vector<float> xs((size_t)mv * kSurIn), ys((size_t)mv * kSurOut);
+    for (int64_t r = 0; r < mv; r++)
+      for (int k = 0; k < kSurIn; k++)
+        xs[(size_t)r * kSurIn + k] = (hx[(size_t)(r * sv) * kSurIn + k] - s->norm.mu_x[k]) * s->norm.inv_sd_x[k];
+    float *dx = nullptr, *dy = nullptr;
+    cudaError_t e = cudaMalloc(&dx, xs.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dy, ys.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dx, xs.data(), xs.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = s->net.m.forward(dx, mv, dy);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(ys.data(), dy, ys.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return cuda_fail(e, "cm_surrogate_fit");
+    for (int k = 0; k < kSurOut; k++) {
+      double mt = 0;
+      for (int64_t r = 0; r < mv; r++) mt += ht[(size_t)(r * sv) * kSurOut + k] / s->norm.sd_y[k];
+      mt /= mv;
+      double res = 0, tot = 0;
+      for (int64_t r = 0; r < mv; r++) {
+        const double tn = ht[(size_t)(r * sv) * kSurOut + k] / s->norm.sd_y[k];
+        const double d = ys[(size_t)r * kSurOut + k] - tn;
+        res += d * d;
+        tot += (tn - mt) * (tn - mt);
+      }
+      s->norm.r2[k] = tot > 0 ? (float)(1.0 - res / tot) : 0.f;
+      s->norm.apply_y[k] = s->norm.r2[k] >= kSurMinR2 ? s->norm.sd_y[k] : 0.f;
+    }
+  }
   s->fitted = true;
   if (final_loss) *final_loss = loss;
   return CM_OK;
@@ -525,7 +574,8 @@ int cm_surrogate_set_blob(cm_surrogate_t s, const float *blob) {
 
 int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n_macro, const cm_stimulus *stim,
                            int mode, int audit_mod, cm_surrogate_stats *stats) {
-  if (!s || !Vm || n_macro < 0 || audit_mod < 0 || (mode != 0 && mode != 1)) return fail(CM_ERR_ARG, "bad argument");
+  if (!s || !Vm || n_macro < 0 || audit_mod < 0 || (mode & ~(CM_SUR_COARSE_ONLY | CM_SUR_AUDIT_FP64)))
+    return fail(CM_ERR_ARG, "bad argument");
   int rc = check_batch(b);
   if (rc) return rc;
   if (b->ps.dt != s->fine.dt) return fail(CM_ERR_ARG, "batch dt differs from the surrogate's fine dt");
@@ -560,7 +610,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.w2 = s->net.m.wb + s->net.m.off[2];
   ka.w3 = s->net.m.wb + s->net.m.off[4];
   ka.bias = nullptr;
-  ka.mode = mode;
+  ka.mode = mode & CM_SUR_COARSE_ONLY;
   ka.gate_mv_per_ms = 5.f;
   ka.audit_mod = audit_mod;
   ka.fallback = s->fallback;
@@ -572,8 +622,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.g0_Kr = (float)s->fine.get("g_Kr");
   ka.g0_K1 = (float)s->fine.get("g_K1");
   // biases as one contiguous FP32 block b1 | b2 | b3 (the kernel's layout)
-  float *bias = nullptr;
-  CK(cudaMalloc(&bias, 288 * sizeof(float)));
+  float *bias = s->bias_block;
   CK(cudaMemcpyAsync(bias, s->net.m.w + s->net.m.off[1], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(bias + 128, s->net.m.w + s->net.m.off[3], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(bias + 256, s->net.m.w + s->net.m.off[5], 32 * sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -589,9 +638,35 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   pa.pred = s->pred;
   pa.audit_err = s->audit_err;
   pa.n_audit = s->totals + 2;
+  pa.audit_fp64 = (mode & CM_SUR_AUDIT_FP64) ? 1 : 0;
+  pa.rows64 = s->rows_fine64;
+  pa.eca64 = s->eca_fine64;
+  pa.c64 = s->fine64;
   cudaError_t e = cudaSuccess;
+  const bool per_cell = stim && stim->textbegin_per_cell;
+  if (per_cell) {  // the reference driver's per-cell textbegin, advanced on the device
+    if (!b->tb_cell) CK(cudaMalloc(&b->tb_cell, std::max<int64_t>(1, n) * sizeof(double)));
+    const double *src = stim->textbegin_per_cell;
+    CK(cudaMemcpyAsync(b->tb_cell, src, n * sizeof(double),
+                       is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    ka.tb_cell = b->tb_cell;
+    pa.tb_cell = b->tb_cell;
+    pa.textlen = stv.textlen;
+    pa.bcl = stv.bcl;
+    pa.amp = stv.amplitude;
+  }
   for (int64_t mstep = 0; mstep < n_macro && e == cudaSuccess; mstep++) {
-    const bool on = protocol_steps(stim ? &stv : nullptr, s->substeps, s->fine.dt, t, tb, pa.iext);
+    bool on = false;
+    if (per_cell) {
+      for (int k = 0; k < s->substeps; k++) {
+        pa.tk[k] = t;
+        if (k + 1 < s->substeps) t += s->fine.dt;
+      }
+      ka.t_last = t;
+      t += s->fine.dt;
+    } else {
+      on = protocol_steps(stim ? &stv : nullptr, s->substeps, s->fine.dt, t, tb, pa.iext);
+    }
     ka.stim_on = on ? 1 : 0;
     ka.audit_phase = audit_mod > 0 ? (int)(mstep % audit_mod) : 0;
     pa.audit_phase = ka.audit_phase;
@@ -599,10 +674,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     if (e == cudaSuccess) e = launch_sur_step(ka, n, st);
     if (e == cudaSuccess) e = launch_sur_plain(pa, (int)n, st);
   }
-  if (e != cudaSuccess) {
-    cudaFree(bias);
-    return cuda_fail(e, "surrogate run");
-  }
+  if (e != cudaSuccess) return cuda_fail(e, "surrogate run");
   rc = planes_out(b, Vm, dvm, host_vm, st);
   unsigned long long tot[3] = {0, 0, 0};
   float aerr = 0;
@@ -614,7 +686,6 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "surrogate run");
   }
-  cudaFree(bias);
   if (rc) return rc;
   if (stats) {
     stats->cell_macro_steps = n * n_macro;

@@ -1,13 +1,15 @@
 // Surrogate macro step for ten Tusscher 2006 cells (see cm_surrogate.h): coarse physics in
-// registers, the MLP on the tensor cores per warp (mma.sync m16n8k16 BF16, FP32 accumulate,
-// weights resident in shared memory), residual add, gating and audit, compaction of the cells
-// that take the plain integrator.
+// registers, the MLP on the fifth-generation tensor cores (tcgen05.mma, BF16 operands in shared
+// memory, FP32 accumulators in tensor memory), residual add, gating and audit, compaction of the
+// cells that take the plain integrator; the plain integrator for those cells; training-data
+// generation kernels.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "cm_bulk.cuh"
 #include "cm_cells.cuh"
 #include "cm_surrogate.h"
+#include "cm_umma.cuh"
 
 namespace cm {
 
@@ -91,49 +93,20 @@ __device__ __forceinline__ void coarse(const TT2Consts<float> &Cc, const float *
 }
 
 // The surrogate result: gates and fast Ca from oc + correction; Vm, CaSR, Na_i, K_i advanced by
-// their coarse increment + correction in their accumulators.
+// their coarse increment + correction in their accumulators. Gates are probabilities: values the
+// range audit let through (within 1e-3 of [0, 1]) are clamped into it, so a small bias in a
+// correction cannot accumulate past the bounds over many macro steps.
+__device__ __forceinline__ float unit(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 __device__ __forceinline__ void apply(Cell &q, Acc &vm, const float on[kSurOut], const float inc[4],
                                       const float corr[kSurOut]) {
   acc_add(vm, (inc[0] + corr[0]) * 1e-3f);
-  q.x.m = on[1]; q.x.h = on[2]; q.x.j = on[3]; q.x.xr1 = on[4]; q.x.xr2 = on[5]; q.x.xs = on[6]; q.x.r = on[7];
-  q.x.s = on[8]; q.x.d = on[9]; q.x.f = on[10]; q.x.f2 = on[11]; q.x.fCa = on[12]; q.x.Rq = on[13];
+  q.x.m = unit(on[1]); q.x.h = unit(on[2]); q.x.j = unit(on[3]); q.x.xr1 = unit(on[4]); q.x.xr2 = unit(on[5]);
+  q.x.xs = unit(on[6]); q.x.r = unit(on[7]); q.x.s = unit(on[8]); q.x.d = unit(on[9]); q.x.f = unit(on[10]);
+  q.x.f2 = unit(on[11]); q.x.fCa = unit(on[12]); q.x.Rq = unit(on[13]);
   q.x.Ca_i = on[14]; q.x.CaSS = on[15];
   acc_add(q.CaSR, inc[1] + corr[16]);
   acc_add(q.Na, inc[2] + corr[17]);
   acc_add(q.K, inc[3] + corr[18]);
-}
-
-__device__ __forceinline__ uint32_t lds_u32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ float tanh_approx(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// shared-memory strides (BF16 elements), chosen so fragment loads hit 32 distinct banks
-constexpr int kLdX = 40, kLdH = 136;
-constexpr int kWarps = 8, kThreads = kWarps * 32;
-constexpr int kSmemW = (128 * kLdX + 128 * kLdH + 32 * kLdH) * 2;  // bytes
-constexpr int kSmemB = (128 + 128 + 32) * 4;
-constexpr int kSmemWarp = 32 * kLdX * 2 + 2 * 16 * kLdH * 2 + 32 * 33 * 4;
-constexpr int kStageVars = 21 + 2 + 6;                   // state planes, Vm hi/lo, hetero slots
-constexpr int kSmemStage = kStageVars * kThreads * 4;
-constexpr int kSmemTotal = kSmemW + kSmemB + kWarps * kSmemWarp + kSmemStage;
-
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(a));
 }
 
 // tanh of two FP32 values as one packed BF16 pair (tanh.approx.bf16x2: one SFU operation)
@@ -144,219 +117,43 @@ __device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
   return r;
 }
 
-// One hidden layer for an m16 tile: OUT[16][128] = tanh(IN[16][K] W^T + b), fragments by
-// ldmatrix.x4 (A: rows r, k halves; B: two n8 tiles x k16 per load).
-template <int K, int LDI>
-__device__ __forceinline__ void hidden_layer(const __nv_bfloat16 *W, int ldw, const float *bias,
-                                             const __nv_bfloat16 *IN, __nv_bfloat16 *OUT, int lane) {
-  const int g = lane >> 2, t = lane & 3;
-  const int ar = lane & 15, ac = (lane >> 4) * 8;                          // A lane address
-  const int br = (lane & 7) + ((lane >> 4) << 3), bc = ((lane >> 3) & 1) * 8;  // B lane address
-#pragma unroll 1
-  for (int nc = 0; nc < 128; nc += 32) {
-    float acc[4][4] = {};
-#pragma unroll
-    for (int k = 0; k < K; k += 16) {
-      uint32_t a[4], b01[4], b23[4];
-      ldsm_x4(a, IN + ar * LDI + k + ac);
-      ldsm_x4(b01, W + (nc + br) * ldw + k + bc);
-      ldsm_x4(b23, W + (nc + 16 + br) * ldw + k + bc);
-      mma16816(acc[0], a, b01[0], b01[1]);
-      mma16816(acc[1], a, b01[2], b01[3]);
-      mma16816(acc[2], a, b23[0], b23[1]);
-      mma16816(acc[3], a, b23[2], b23[3]);
-    }
-#pragma unroll
-    for (int ni = 0; ni < 4; ni++) {
-      const int n = nc + ni * 8 + 2 * t;
-      const float b0 = bias[n], b1 = bias[n + 1];
-      *reinterpret_cast<uint32_t *>(OUT + g * kLdH + n) = tanh2_bf16(acc[ni][0] + b0, acc[ni][1] + b1);
-      *reinterpret_cast<uint32_t *>(OUT + (g + 8) * kLdH + n) = tanh2_bf16(acc[ni][2] + b0, acc[ni][3] + b1);
-    }
-  }
-}
-
-// One m16 tile: rows [r0, r0+16) of X (K = 32) through the three layers into Y (FP32).
-__device__ __forceinline__ void mlp_tile(const __nv_bfloat16 *W1, const __nv_bfloat16 *W2, const __nv_bfloat16 *W3,
-                                         const float *b1, const float *b2, const float *b3, const __nv_bfloat16 *X,
-                                         __nv_bfloat16 *H1, __nv_bfloat16 *H2, float *Y, int r0, int lane) {
-  hidden_layer<32, kLdX>(W1, kLdX, b1, X + r0 * kLdX, H1, lane);
-  __syncwarp();
-  hidden_layer<128, kLdH>(W2, kLdH, b2, H1, H2, lane);
-  __syncwarp();
-  // output layer: Y = H2 W3^T + b3, N = 32
-  const int g = lane >> 2, t = lane & 3;
-  const int ar = lane & 15, ac = (lane >> 4) * 8;
-  const int br = (lane & 7) + ((lane >> 4) << 3), bc = ((lane >> 3) & 1) * 8;
-  float acc[4][4] = {};
-#pragma unroll
-  for (int k = 0; k < 128; k += 16) {
-    uint32_t a[4], b01[4], b23[4];
-    ldsm_x4(a, H2 + ar * kLdH + k + ac);
-    ldsm_x4(b01, W3 + br * kLdH + k + bc);
-    ldsm_x4(b23, W3 + (16 + br) * kLdH + k + bc);
-    mma16816(acc[0], a, b01[0], b01[1]);
-    mma16816(acc[1], a, b01[2], b01[3]);
-    mma16816(acc[2], a, b23[0], b23[1]);
-    mma16816(acc[3], a, b23[2], b23[3]);
-  }
-#pragma unroll
-  for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int r = g + (q >> 1) * 8, n = ni * 8 + 2 * t + (q & 1);
-      Y[(r0 + r) * 33 + n] = acc[ni][q] + b3[n];
-    }
-  __syncwarp();
-}
-
-// Tiles of kThreads cells: the tile's state planes, Vm planes and conductances arrive in shared
-// memory by bulk async copies (one mbarrier); every thread takes its cell into registers, then
-// thread 0 issues the next tile's copies, which land while this tile's coarse step and MLP run.
-__global__ void __launch_bounds__(kThreads, 1) sur_step_kernel(const SurKernelArgs a, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int s_abort;
-  __nv_bfloat16 *W1 = (__nv_bfloat16 *)smem;
-  __nv_bfloat16 *W2 = W1 + 128 * kLdX;
-  __nv_bfloat16 *W3 = W2 + 128 * kLdH;
-  float *bias = (float *)(smem + kSmemW);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned char *wbase = smem + kSmemW + kSmemB + warp * kSmemWarp;
-  __nv_bfloat16 *X = (__nv_bfloat16 *)wbase;
-  __nv_bfloat16 *H1 = X + 32 * kLdX;
-  __nv_bfloat16 *H2 = H1 + 16 * kLdH;
-  float *Y = (float *)(H2 + 16 * kLdH);
-  float *stage = (float *)(smem + kSmemW + kSmemB + kWarps * kSmemWarp);
-  const DevBatch &fb = a.fine;
-  const int64_t ld = fb.ld;
-  int het_pos[6];
-  int nv = 23;
-#pragma unroll
-  for (int k = 0; k < 6; k++) het_pos[k] = fb.het[k] ? nv++ : -1;
-  const uint32_t tile_bytes = (uint32_t)nv * kThreads * 4u;
-  const int n_tiles = (n + kThreads - 1) / kThreads;
-  auto issue = [&](int tile) {
-    const int64_t c0 = (int64_t)tile * kThreads;
-    mbar_expect_tx(&bar, tile_bytes);
-    for (int v = 0; v < 21; v++) bulk_g2s(stage + v * kThreads, fb.s32 + v * ld + c0, kThreads * 4u, &bar);
-    bulk_g2s(stage + 21 * kThreads, a.vm_hi + c0, kThreads * 4u, &bar);
-    bulk_g2s(stage + 22 * kThreads, a.vm_lo + c0, kThreads * 4u, &bar);
-    for (int k = 0; k < 6; k++)
-      if (het_pos[k] >= 0) bulk_g2s(stage + het_pos[k] * kThreads, (const float *)fb.het[k] + c0, kThreads * 4u, &bar);
-  };
-  if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
-    s_abort = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  // network into shared memory (padded rows): W1 [128][32], W2 [128][128], W3 [32][128]
-  for (int i = threadIdx.x; i < 128 * 32; i += kThreads) W1[(i >> 5) * kLdX + (i & 31)] = a.w1[i];
-  for (int i = threadIdx.x; i < 128 * 128; i += kThreads) W2[(i >> 7) * kLdH + (i & 127)] = a.w2[i];
-  for (int i = threadIdx.x; i < 32 * 128; i += kThreads) W3[(i >> 7) * kLdH + (i & 127)] = a.w3[i];
-  for (int i = threadIdx.x; i < 288; i += kThreads) bias[i] = a.bias[i];
-  __syncthreads();
-  if (threadIdx.x == 0 && (int)blockIdx.x < n_tiles) issue(blockIdx.x);
-  const float macro_ms = a.coarse.dt * 1000.f;
-  const TT2Consts<float> &C = fb.tt2_32;
-  int it = 0;
-  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
-    if (!mbar_wait(&bar, (uint32_t)(it & 1))) {
-      s_abort = 1;
-      atomicOr(fb.audit_or, kAuditTimeout);
-    }
-    __syncthreads();
-    if (s_abort) {  // the only copy in flight is the one that timed out: give it one more bounded wait
-      mbar_wait(&bar, (uint32_t)(it & 1));
-      return;
-    }
-    const int c = t * kThreads + threadIdx.x;
-    const bool valid = c < n;
-    const float *S = stage + threadIdx.x;
-    Cell q;
-    q.x.m = S[0]; q.x.h = S[kThreads]; q.x.j = S[2 * kThreads]; q.x.xr1 = S[3 * kThreads];
-    q.x.xr2 = S[4 * kThreads]; q.x.xs = S[5 * kThreads]; q.x.r = S[6 * kThreads]; q.x.s = S[7 * kThreads];
-    q.x.d = S[8 * kThreads]; q.x.f = S[9 * kThreads]; q.x.f2 = S[10 * kThreads]; q.x.fCa = S[11 * kThreads];
-    q.x.Rq = S[12 * kThreads]; q.x.Ca_i = S[13 * kThreads]; q.x.CaSS = S[14 * kThreads];
-    q.CaSR = Acc{S[15 * kThreads], S[16 * kThreads]};
-    q.Na = Acc{S[17 * kThreads], S[18 * kThreads]};
-    q.K = Acc{S[19 * kThreads], S[20 * kThreads]};
-    Acc vm{S[21 * kThreads], S[22 * kThreads]};
-    q.g.g_Na = het_pos[H2_g_Na] >= 0 ? S[het_pos[H2_g_Na] * kThreads] : C.g_Na;
-    q.g.g_Kr = het_pos[H2_g_Kr] >= 0 ? S[het_pos[H2_g_Kr] * kThreads] : C.g_Kr;
-    q.g.g_K1 = het_pos[H2_g_K1] >= 0 ? S[het_pos[H2_g_K1] * kThreads] : C.g_K1;
-    q.g.g_Ks = het_pos[H2_g_Ks] >= 0 ? S[het_pos[H2_g_Ks] * kThreads] : C.g_Ks;
-    q.g.g_to = het_pos[H2_g_to] >= 0 ? S[het_pos[H2_g_to] * kThreads] : C.g_to;
-    q.g.g_CaL = het_pos[H2_g_CaL] >= 0 ? S[het_pos[H2_g_CaL] * kThreads] : C.g_CaL;
-    __syncthreads();  // the stage buffer is free: the next tile's copies overlap this tile's work
-    if (threadIdx.x == 0 && t + (int)gridDim.x < n_tiles) {
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      issue(t + gridDim.x);
-    }
-    float oc[kSurOut], inc[4], f[kSurIn];
-    bool fall = !valid;
-    if (valid) {
-      coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
-      const float rate = fabsf(inc[0]) / macro_ms;
-      fall = a.stim_on || !(rate <= a.gate_mv_per_ms);
-      features(q, (vm.hi + vm.lo) * 1000.f, a.g0_Na, a.g0_Kr, a.g0_K1, f);
-    } else {
-#pragma unroll
-      for (int k = 0; k < kSurIn; k++) f[k] = a.norm.mu_x[k];
-    }
-    // normalised features into this warp's X rows (row = lane), K padded to 32 with zeros
-#pragma unroll
-    for (int k = 0; k < kSurIn; k++) X[lane * kLdX + k] = __float2bfloat16((f[k] - a.norm.mu_x[k]) * a.norm.inv_sd_x[k]);
-#pragma unroll
-    for (int k = kSurIn; k < 32; k++) X[lane * kLdX + k] = __float2bfloat16(0.f);
-    __syncwarp();
-    const bool any = __any_sync(0xffffffffu, !fall);
-    if (a.mode == 0 && any) {
-      mlp_tile(W1, W2, W3, bias, bias + 128, bias + 256, X, H1, H2, Y, 0, lane);
-      mlp_tile(W1, W2, W3, bias, bias + 128, bias + 256, X, H1, H2, Y, 16, lane);
-    }
-    if (valid) {
-      const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
-      if (audited) a.pred[c] = __int_as_float(0x7fc00000);  // NaN unless the surrogate predicts below
-      if (!fall) {
-        float on[kSurOut], corr[kSurOut];
-#pragma unroll
-        for (int k = 0; k < kSurOut; k++) {
-          corr[k] = a.mode == 0 ? a.norm.sd_y[k] * Y[lane * 33 + k] : 0.f;
-          on[k] = oc[k] + corr[k];
-        }
-        // range audit: gates in [0, 1], concentrations positive, everything finite
-        bool ok = isfinite(on[0]);
-#pragma unroll
-        for (int k = 1; k <= 13; k++) ok = ok && on[k] >= -1e-3f && on[k] <= 1.001f;
-#pragma unroll
-        for (int k = 14; k < kSurOut; k++) ok = ok && on[k] > 0.f && isfinite(on[k]);
-        if (!ok) {
-          fall = true;
-          atomicOr(fb.audit_cell + c, 16u);
-          atomicOr(fb.audit_or, 16u);
-        } else if (audited) {
-          a.pred[c] = on[0];
-          fall = true;
-        } else {
-          Cell nq = q;
-          Acc nv = vm;
-          apply(nq, nv, on, inc, corr);
-          store_cell(fb, c, nq);
-          a.vm_hi[c] = nv.hi;
-          a.vm_lo[c] = nv.lo;
-        }
-      }
-      if (fall) {
-        const unsigned int slot = atomicAdd(a.n_fallback, 1u);
-        a.fallback[slot] = c;
-        atomicAdd(a.n_fallback_total, 1ull);
-      } else {
-        atomicAdd(a.n_sur, 1ull);
-      }
-    }
-    __syncwarp();
-  }
+// One fine step of a mixed-state cell in FP64: the FP32 planes and compensated pairs widened
+// to double, the reference arithmetic (tt2_calc_fp64 with FP64 tables), the result rounded back.
+__device__ __noinline__ double tt2_fp64_from_mixed(const SurPlainArgs &a, int c, double V, double iext,
+                                                   uint32_t &audit) {
+  const DevBatch &b = a.fine;
+  const int64_t ld = b.ld;
+  float *s = b.s32 + c;
+  const float *const *het = (const float *const *)b.het;
+  TT2Cell<double> x;
+  x.m = s[0]; x.h = s[ld]; x.j = s[2 * ld]; x.xr1 = s[3 * ld]; x.xr2 = s[4 * ld]; x.xs = s[5 * ld];
+  x.r = s[6 * ld]; x.s = s[7 * ld]; x.d = s[8 * ld]; x.f = s[9 * ld]; x.f2 = s[10 * ld]; x.fCa = s[11 * ld];
+  x.Rq = s[12 * ld]; x.Ca_i = s[13 * ld]; x.CaSS = s[14 * ld];
+  double CaSR = acc_to_double(Acc{s[15 * ld], s[16 * ld]});
+  double Na_i = acc_to_double(Acc{s[17 * ld], s[18 * ld]});
+  double K_i = acc_to_double(Acc{s[19 * ld], s[20 * ld]});
+  const TT2Consts<double> &C = a.c64;
+  TT2Het_<double> g;
+  g.g_Na = het[H2_g_Na] ? (double)het[H2_g_Na][c] : C.g_Na;
+  g.g_Kr = het[H2_g_Kr] ? (double)het[H2_g_Kr][c] : C.g_Kr;
+  g.g_K1 = het[H2_g_K1] ? (double)het[H2_g_K1][c] : C.g_K1;
+  g.g_Ks = het[H2_g_Ks] ? (double)het[H2_g_Ks][c] : C.g_Ks;
+  g.g_to = het[H2_g_to] ? (double)het[H2_g_to][c] : C.g_to;
+  g.g_CaL = het[H2_g_CaL] ? (double)het[H2_g_CaL][c] : C.g_CaL;
+  const int vi = vrow_fp64(V * 1000.0, audit);
+  const double dV = tt2_calc_fp64<false>(C, a.rows64 + (size_t)vi * T2_COLS, a.eca64, x, CaSR, Na_i, K_i, g, V, iext,
+                                         audit, nullptr);
+  s[0] = (float)x.m; s[ld] = (float)x.h; s[2 * ld] = (float)x.j; s[3 * ld] = (float)x.xr1; s[4 * ld] = (float)x.xr2;
+  s[5 * ld] = (float)x.xs; s[6 * ld] = (float)x.r; s[7 * ld] = (float)x.s; s[8 * ld] = (float)x.d;
+  s[9 * ld] = (float)x.f; s[10 * ld] = (float)x.f2; s[11 * ld] = (float)x.fCa; s[12 * ld] = (float)x.Rq;
+  s[13 * ld] = (float)x.Ca_i; s[14 * ld] = (float)x.CaSS;
+  Acc t = acc_from_double(CaSR);
+  s[15 * ld] = t.hi; s[16 * ld] = t.lo;
+  t = acc_from_double(Na_i);
+  s[17 * ld] = t.hi; s[18 * ld] = t.lo;
+  t = acc_from_double(K_i);
+  s[19 * ld] = t.hi; s[20 * ld] = t.lo;
+  return dV;
 }
 
 __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
@@ -365,7 +162,25 @@ __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
     const int c = a.list[i];
     Acc v{a.vm_hi[c], a.vm_lo[c]};
     uint32_t audit = 0;
-    for (int k = 0; k < a.substeps; k++) acc_add(v, tt2_mixed_cell<int>(a.fine, c, v.hi, a.iext[k], audit));
+    const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
+    double tb = a.tb_cell ? a.tb_cell[c] : 0.0;
+    auto iext_at = [&](int k) -> double {  // reference driver stimulus (CellModel.h:405-419)
+      if (!a.tb_cell) return (double)a.iext[k];
+      double i = 0.0;
+      if (a.tk[k] >= tb) {
+        i = a.amp;
+        if (a.tk[k] >= tb + a.textlen) tb += a.bcl;
+      }
+      return i;
+    };
+    if (audited && a.audit_fp64) {
+      double V = acc_to_double(v);
+      for (int k = 0; k < a.substeps; k++) V += tt2_fp64_from_mixed(a, c, V, iext_at(k), audit);
+      v = acc_from_double(V);
+    } else {
+      for (int k = 0; k < a.substeps; k++) acc_add(v, tt2_mixed_cell<int>(a.fine, c, v.hi, (float)iext_at(k), audit));
+    }
+    if (a.tb_cell) a.tb_cell[c] = tb;
     a.vm_hi[c] = v.hi;
     a.vm_lo[c] = v.lo;
     if (!isfinite(v.hi)) audit |= 1u;
@@ -373,7 +188,7 @@ __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
       atomicOr(a.fine.audit_cell + c, audit);
       atomicOr(a.fine.audit_or, audit);
     }
-    if (a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase) {
+    if (audited) {
       const float p = a.pred[c];
       if (isfinite(p)) {
         const float err = fabsf(p - (v.hi + v.lo) * 1000.f);
@@ -453,6 +268,305 @@ __global__ void sur_normalize_kernel(const float *__restrict__ X, const float *_
   }
 }
 
+// ---------------------------------------------------------------- tcgen05 inference kernel
+// kGroups groups of 4 warps per block; a group owns tiles of 128 cells (one cell per thread,
+// thread i of the group = row i of the MLP tile = TMEM lane i). The network is resident in
+// shared memory once per block in the tensor core's K-major layout; each group has a 32 KB
+// activation tile (features, then hidden layer 1, then hidden layer 2, each overwritten once the
+// MMA that read it has completed), a bulk-copy stage for its next cell tile, and 128 TMEM
+// columns for the FP32 accumulators of the three layers (each layer's accumulator is read back
+// by tcgen05.ld before the next layer's MMA overwrites it). One elected thread per group issues
+// the MMAs; completion is signalled through an mbarrier by tcgen05.commit.
+constexpr int kTcCells = 128;
+constexpr int kTcStageVars = 21 + 2;  // state planes and the Vm pair
+constexpr int kTcW1 = 128 * 32 * 2, kTcW2 = 128 * 128 * 2, kTcW3 = 32 * 128 * 2;
+constexpr int kTcBias = 1280;                       // 288 floats, padded to keep 128-B alignment
+constexpr int kTcAct = kTcCells * 128 * 2;          // activation tile (BF16)
+constexpr int kTcStage = kTcStageVars * kTcCells * 4;
+constexpr int kTcGroupBytes = kTcAct + kTcStage;
+__host__ __device__ constexpr int tc_smem_bytes(int groups) { return kTcW1 + kTcW2 + kTcW3 + kTcBias + groups * kTcGroupBytes; }
+
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;\n" ::"r"(g + 1) : "memory"); }
+
+__device__ __forceinline__ void sts128(void *p, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};\n" ::"r"((uint32_t)__cvta_generic_to_shared(p)), "r"(a), "r"(b),
+               "r"(c), "r"(d)
+               : "memory");
+}
+
+// bf16 pair (lo = x, hi = y) without activation
+__device__ __forceinline__ uint32_t pack_bf16(float x, float y) {
+  uint32_t p;
+  asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(p) : "f"(x), "f"(y));
+  return p;
+}
+
+// One hidden-layer epilogue for this thread's row: TMEM columns [0, 128) of the group's
+// accumulator + bias -> tanh -> BF16, written as row r of a 128 x 128 K-major operand tile.
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t tacc, const float *bias, __nv_bfloat16 *act, int r) {
+#pragma unroll 1
+  for (int c0 = 0; c0 < 128; c0 += 32) {
+    float v[32];
+    umma::tmem_ld32(tacc + (uint32_t)c0, v);
+    uint32_t h[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) h[j] = tanh2_bf16(v[2 * j] + bias[c0 + 2 * j], v[2 * j + 1] + bias[c0 + 2 * j + 1]);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      sts128(act + umma::kmajor_index(r, c0 + 8 * q, 128), h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+  }
+}
+
+// Appends this lane to a warp-aggregated list: one atomic per warp; returns the lane's slot
+// (meaningful where pred). Every lane of the warp calls it.
+__device__ __forceinline__ unsigned int warp_slot(unsigned int *counter, bool pred, int lane) {
+  const unsigned int mask = __ballot_sync(0xffffffffu, pred);
+  if (!mask) return 0u;
+  const int first = __ffs(mask) - 1;
+  unsigned int base = 0;
+  if (lane == first) base = atomicAdd(counter, (unsigned int)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, first);
+  return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void warp_count(unsigned long long *counter, bool pred, int lane) {
+  const unsigned int mask = __ballot_sync(0xffffffffu, pred);
+  if (mask && lane == __ffs(mask) - 1) atomicAdd(counter, (unsigned long long)__popc(mask));
+}
+
+// Per group and tile: the features of the cells' initial state go to the tensor core first
+// (layer-1 MMA issued), the coarse physics step runs while it computes, then the three layers'
+// epilogues and MMAs alternate; the network's correction is applied to the coarse result.
+template <int kGroups>
+__global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const SurKernelArgs a, int n) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar_stage[kGroups], bar_mma[kGroups];
+  __shared__ uint32_t tslot;
+  __shared__ int s_abort[kGroups];
+  __nv_bfloat16 *W1 = (__nv_bfloat16 *)smem;
+  __nv_bfloat16 *W2 = (__nv_bfloat16 *)(smem + kTcW1);
+  __nv_bfloat16 *W3 = (__nv_bfloat16 *)(smem + kTcW1 + kTcW2);
+  float *bias = (float *)(smem + kTcW1 + kTcW2 + kTcW3);
+  const int g = threadIdx.x >> 7, r = threadIdx.x & 127, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char *gbase = smem + kTcW1 + kTcW2 + kTcW3 + kTcBias + g * kTcGroupBytes;
+  __nv_bfloat16 *act = (__nv_bfloat16 *)gbase;
+  float *stage = (float *)(gbase + kTcAct);
+  const bool leader = r == 0;
+  const DevBatch &fb = a.fine;
+  const int64_t ld = fb.ld;
+  const float *const *het = (const float *const *)fb.het;
+  const int n_tiles = (n + kTcCells - 1) / kTcCells;
+  const int t_step = (int)gridDim.x * kGroups;
+  auto issue = [&](int tile) {  // the tile's 21 state planes and Vm pair
+    const int64_t c0 = (int64_t)tile * kTcCells;
+    mbar_expect_tx(&bar_stage[g], (uint32_t)kTcStageVars * kTcCells * 4u);
+    for (int v = 0; v < 21; v++) bulk_g2s(stage + v * kTcCells, fb.s32 + v * ld + c0, kTcCells * 4u, &bar_stage[g]);
+    bulk_g2s(stage + 21 * kTcCells, a.vm_hi + c0, kTcCells * 4u, &bar_stage[g]);
+    bulk_g2s(stage + 22 * kTcCells, a.vm_lo + c0, kTcCells * 4u, &bar_stage[g]);
+  };
+  if (leader) {
+    mbar_init(&bar_stage[g], 1);
+    mbar_init(&bar_mma[g], 1);
+    s_abort[g] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // network into shared memory in the K-major layout; consecutive threads take consecutive rows
+  // of one 16-byte K chunk, so each quarter-warp stores 128 contiguous bytes
+  {
+    const uint4 *w1 = (const uint4 *)a.w1, *w2 = (const uint4 *)a.w2, *w3 = (const uint4 *)a.w3;
+    for (int i = threadIdx.x; i < 128 * 4; i += kGroups * 128) {
+      const int row = i & 127, ch = i >> 7;
+      *(uint4 *)(W1 + umma::kmajor_index(row, ch * 8, 32)) = w1[row * 4 + ch];
+    }
+    for (int i = threadIdx.x; i < 128 * 16; i += kGroups * 128) {
+      const int row = i & 127, ch = i >> 7;
+      *(uint4 *)(W2 + umma::kmajor_index(row, ch * 8, 128)) = w2[row * 16 + ch];
+    }
+    for (int i = threadIdx.x; i < 32 * 16; i += kGroups * 128) {
+      const int row = i & 31, ch = i >> 5;
+      *(uint4 *)(W3 + umma::kmajor_index(row, ch * 8, 128)) = w3[row * 16 + ch];
+    }
+    for (int i = threadIdx.x; i < 288; i += kGroups * 128) bias[i] = a.bias[i];
+  }
+  const bool mlp_on = a.mode == 0 && !a.stim_on;
+  constexpr uint32_t kCols = kGroups == 1 ? 128 : (kGroups == 2 ? 256 : 512);
+  if (mlp_on && warp == 0) umma::tmem_alloc(&tslot, kCols);
+  umma::fence_smem_to_async();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tbase = mlp_on ? tslot : 0u;
+  const uint32_t tacc = tbase + (uint32_t)(g * 128) + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
+  const uint32_t tacc_mma = tbase + (uint32_t)(g * 128);
+  int t = blockIdx.x * kGroups + g;
+  if (leader && t < n_tiles) issue(t);
+  const float macro_ms = a.coarse.dt * 1000.f;
+  const TT2Consts<float> &C = fb.tt2_32;
+  uint32_t ps = 0, pm = 0;  // mbarrier phase parities
+  const uint32_t act_s = smem_u32(act), w1_s = smem_u32(W1), w2_s = smem_u32(W2), w3_s = smem_u32(W3);
+  auto wait_mma = [&]() {
+    if (!mbar_wait(&bar_mma[g], pm)) {
+      s_abort[g] = 1;
+      atomicOr(fb.audit_or, kAuditTimeout);
+    }
+    pm ^= 1u;
+    umma::fence_after_sync();
+  };
+  auto operands_ready = [&]() {  // this group's act rows written -> the leader may issue the next MMA
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    group_sync(g);
+  };
+  for (; t < n_tiles; t += t_step) {
+    if (!mbar_wait(&bar_stage[g], ps)) {
+      s_abort[g] = 1;
+      atomicOr(fb.audit_or, kAuditTimeout);
+    }
+    ps ^= 1u;
+    group_sync(g);
+    if (s_abort[g]) {
+      mbar_wait(&bar_stage[g], ps ^ 1u);  // the copy that timed out: one more bounded wait
+      break;
+    }
+    const int c = t * kTcCells + r;
+    const bool valid = c < n;
+    const float *S = stage + r;
+    Cell q;
+    q.x.m = S[0]; q.x.h = S[kTcCells]; q.x.j = S[2 * kTcCells]; q.x.xr1 = S[3 * kTcCells];
+    q.x.xr2 = S[4 * kTcCells]; q.x.xs = S[5 * kTcCells]; q.x.r = S[6 * kTcCells]; q.x.s = S[7 * kTcCells];
+    q.x.d = S[8 * kTcCells]; q.x.f = S[9 * kTcCells]; q.x.f2 = S[10 * kTcCells]; q.x.fCa = S[11 * kTcCells];
+    q.x.Rq = S[12 * kTcCells]; q.x.Ca_i = S[13 * kTcCells]; q.x.CaSS = S[14 * kTcCells];
+    q.CaSR = Acc{S[15 * kTcCells], S[16 * kTcCells]};
+    q.Na = Acc{S[17 * kTcCells], S[18 * kTcCells]};
+    q.K = Acc{S[19 * kTcCells], S[20 * kTcCells]};
+    Acc vm{S[21 * kTcCells], S[22 * kTcCells]};
+    const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
+    q.g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
+    q.g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + cc) : C.g_Kr;
+    q.g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + cc) : C.g_K1;
+    q.g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + cc) : C.g_Ks;
+    q.g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + cc) : C.g_to;
+    q.g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + cc) : C.g_CaL;
+    group_sync(g);  // the stage is free: the next tile's copies overlap this tile's work
+    if (leader && t + t_step < n_tiles) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      issue(t + t_step);
+    }
+    if (mlp_on) {  // features of the initial state -> row r of the 128 x 32 input tile
+      float f[kSurIn];
+      features(q, (vm.hi + vm.lo) * 1000.f, a.g0_Na, a.g0_Kr, a.g0_K1, f);
+      uint32_t xb[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int k0 = 2 * j, k1 = 2 * j + 1;
+        const float x0 = (valid && k0 < kSurIn) ? (f[k0] - a.norm.mu_x[k0]) * a.norm.inv_sd_x[k0] : 0.f;
+        const float x1 = (valid && k1 < kSurIn) ? (f[k1] - a.norm.mu_x[k1]) * a.norm.inv_sd_x[k1] : 0.f;
+        xb[j] = pack_bf16(x0, x1);
+      }
+#pragma unroll
+      for (int qd = 0; qd < 4; qd++)
+        sts128(act + umma::kmajor_index(r, 8 * qd, 32), xb[4 * qd], xb[4 * qd + 1], xb[4 * qd + 2], xb[4 * qd + 3]);
+      operands_ready();
+      if (leader) {  // layer 1: D = X W1^T (K = 32), computed while the coarse step runs
+        umma::fence_after_sync();
+        constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+          umma::mma_bf16(tacc_mma, umma::smem_desc(act_s + s * 256u, 128u, 512u), umma::smem_desc(w1_s + s * 256u, 128u, 512u), id, s);
+        umma::commit(&bar_mma[g]);
+      }
+    }
+    // coarse physics step (registers only)
+    float oc[kSurOut], inc[4];
+    bool fall = !valid;
+    if (valid) {
+      coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
+      const float rate = fabsf(inc[0]) / macro_ms;
+      const bool stim = a.stim_on || (a.tb_cell && a.t_last >= a.tb_cell[c]);
+      fall = stim || !(rate <= a.gate_mv_per_ms);
+    }
+    float y[32];
+    if (mlp_on) {
+      wait_mma();
+      tc_hidden_epilogue(tacc, bias, act, r);
+      operands_ready();
+      if (leader) {  // layer 2: D = H1 W2^T, K = 128
+        umma::fence_after_sync();
+        constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
+#pragma unroll
+        for (int s = 0; s < 8; s++)
+          umma::mma_bf16(tacc_mma, umma::smem_desc(act_s + s * 256u, 128u, 2048u), umma::smem_desc(w2_s + s * 256u, 128u, 2048u), id, s);
+        umma::commit(&bar_mma[g]);
+      }
+      wait_mma();
+      tc_hidden_epilogue(tacc, bias + 128, act, r);
+      operands_ready();
+      if (leader) {  // output layer: D = H2 W3^T, N = 32
+        umma::fence_after_sync();
+        constexpr uint32_t id = umma::idesc_bf16_f32(128, 32);
+#pragma unroll
+        for (int s = 0; s < 8; s++)
+          umma::mma_bf16(tacc_mma, umma::smem_desc(act_s + s * 256u, 128u, 2048u), umma::smem_desc(w3_s + s * 256u, 128u, 2048u), id, s);
+        umma::commit(&bar_mma[g]);
+      }
+      wait_mma();
+      umma::tmem_ld32(tacc, y);
+      umma::fence_before_sync();
+#pragma unroll
+      for (int k = 0; k < kSurOut; k++) y[k] += bias[256 + k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 32; k++) y[k] = 0.f;
+    }
+    bool took = false;
+    if (valid) {
+      const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
+      if (audited) a.pred[c] = __int_as_float(0x7fc00000);  // NaN unless the surrogate predicts below
+      if (!fall) {
+        float on[kSurOut], corr[kSurOut];
+#pragma unroll
+        for (int k = 0; k < kSurOut; k++) {
+          corr[k] = a.mode == 0 ? a.norm.apply_y[k] * y[k] : 0.f;
+          on[k] = oc[k] + corr[k];
+        }
+        // range audit: gates in [0, 1], concentrations positive, everything finite
+        bool ok = isfinite(on[0]);
+#pragma unroll
+        for (int k = 1; k <= 13; k++) ok = ok && on[k] >= -1e-3f && on[k] <= 1.001f;
+#pragma unroll
+        for (int k = 14; k < kSurOut; k++) ok = ok && on[k] > 0.f && isfinite(on[k]);
+        if (!ok) {
+          fall = true;
+          atomicOr(fb.audit_cell + c, 16u);
+          atomicOr(fb.audit_or, 16u);
+        } else if (audited) {
+          a.pred[c] = on[0];
+          fall = true;
+        } else {
+          Cell nq = q;
+          Acc nvm = vm;
+          apply(nq, nvm, on, inc, corr);
+          store_cell(fb, c, nq);
+          a.vm_hi[c] = nvm.hi;
+          a.vm_lo[c] = nvm.lo;
+          took = true;
+        }
+      }
+    }
+    const bool listed = valid && fall;
+    const unsigned int slot = warp_slot(a.n_fallback, listed, lane);
+    if (listed) a.fallback[slot] = c;
+    warp_count(a.n_fallback_total, listed, lane);
+    warp_count(a.n_sur, took, lane);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (mlp_on && warp == 0) umma::tmem_free(tslot, kCols);
+}
+
+constexpr int kTcGroups = 4;
+
 }  // namespace
 
 cudaError_t launch_sur_append(const float *X, const float *T, const uint8_t *keep, int64_t n, float *dX, float *dT,
@@ -472,17 +586,18 @@ cudaError_t launch_sur_normalize(const float *X, const float *T, int64_t n, cons
 }
 
 cudaError_t launch_sur_step(const SurKernelArgs &a, int64_t n, cudaStream_t s) {
+  constexpr int smem = tc_smem_bytes(kTcGroups);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sur_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal);
+    cudaError_t e = cudaFuncSetAttribute(sur_step_tc_kernel<kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   if (n <= 0) return cudaSuccess;
-  const int64_t need = (n + kThreads - 1) / kThreads;
+  const int64_t need = (n + kTcCells * kTcGroups - 1) / (kTcCells * kTcGroups);
   const int64_t cap = (int64_t)sm_count();
   const int grid = (int)(need < cap ? need : cap);
-  sur_step_kernel<<<grid, kThreads, kSmemTotal, s>>>(a, (int)n);
+  sur_step_tc_kernel<kTcGroups><<<grid, kTcGroups * 128, smem, s>>>(a, (int)n);
   return cudaGetLastError();
 }
 

@@ -26,8 +26,14 @@ constexpr int kSurH = 128;   // hidden width (the inference kernel is built for 
 
 // Features: Vm [mV], 13 gates, log Ca_i, log CaSS, CaSR, Na_i, K_i, log(g/g0) of g_Na, g_Kr, g_K1.
 // Outputs: residuals of Vm [mV], the 13 gates, Ca_i, CaSS, CaSR, Na_i, K_i.
+// Feature normalisation, target scales, the scale at which each output's correction is applied
+// (sd_y where the network predicts that output's residual better than its mean, R^2 >= kSurMinR2
+// on the training data; 0 where it does not, and the coarse step's value is kept), and the R^2.
+// Corrections the network predicts poorly are biased noise that accumulates over macro steps;
+// the gates' clamp into [0, 1] (apply() in cm_surrogate.cu) bounds what remains of that.
+constexpr float kSurMinR2 = 0.0f;
 struct SurNorm {
-  float mu_x[kSurIn], inv_sd_x[kSurIn], sd_y[kSurOut];
+  float mu_x[kSurIn], inv_sd_x[kSurIn], sd_y[kSurOut], apply_y[kSurOut], r2[kSurOut];
 };
 
 struct SurKernelArgs {
@@ -49,6 +55,10 @@ struct SurKernelArgs {
   float *pred;                   // audited cells: surrogate prediction of Vm [mV], by cell
   unsigned long long *n_sur;     // cells advanced by the surrogate (over all macro steps)
   float g0_Na, g0_Kr, g0_K1;     // parameter-set conductances (feature reference)
+  // per-cell stimulus protocol (else stim_on for all cells): first stimulus time by cell, and
+  // the time of the macro step's last fine step; a cell is stimulated when t_last >= tb_cell[c]
+  const double *tb_cell;
+  double t_last;
 };
 
 struct SurPlainArgs {
@@ -62,6 +72,14 @@ struct SurPlainArgs {
   const float *pred;
   float *audit_err;              // max |prediction - plain| Vm [mV] over audited cells (atomicMax on bits)
   unsigned long long *n_audit;
+  int audit_fp64;                // audited cells: the S fine steps in FP64 (tables rows64/eca64, constants c64)
+  const double *rows64, *eca64;
+  TT2Consts<double> c64;
+  // per-cell stimulus protocol (else iext[] for all cells): the reference driver's logic per
+  // fine step k at time tk[k], advancing tb_cell in place
+  double *tb_cell;
+  double tk[64];
+  double textlen, bcl, amp;
 };
 
 struct SurGenArgs {

@@ -73,3 +73,15 @@ def batched_instances(seed: int, n_inst: int = 256, lo: int = 1_000, hi: int = 1
         out.append({"n": n, "model": model, "phase": float(u[2]),
                     "scales": {nm: g_lo + (g_hi - g_lo) * float(u[3 + k]) for k, nm in enumerate(names)}})
     return out
+
+
+def full_form_instances(seed: int, n_inst: int = 64, total: int = 1 << 24, align: int = 256) -> list[dict]:
+    """Instances of the full chosen form: n_inst sizes with log-uniform weights over a factor of
+    64, scaled to `total` cells and rounded to multiples of `align` (the last instance takes the
+    remainder), and a stimulus phase U[0, 1) of the cycle length each. Draw index of instance i,
+    field k (0 size, 1 phase) = i * 2 + k."""
+    u = uniform(seed, np.arange(2 * n_inst, dtype=np.uint64)).reshape(n_inst, 2)
+    w = np.exp(np.log(64.0) * u[:, 0])
+    sizes = np.maximum(align, np.floor(w / w.sum() * total / align).astype(np.int64) * align)
+    sizes[-1] += total - sizes.sum()
+    return [{"n": int(sizes[i]), "phase": float(u[i, 1])} for i in range(n_inst)]

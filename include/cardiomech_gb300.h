@@ -54,8 +54,9 @@ typedef enum {
 /* Arithmetic form of a batch. */
 typedef enum {
   CM_PREC_FP64 = 0,  /* every operation in FP64, the reference's arithmetic */
-  CM_PREC_MIXED = 1  /* FP32 gates and currents; Vm, [Na]i, [K]i, [Ca]SR accumulated in FP64;
-                        buffered-Ca quadratics solved in a cancellation-free increment form */
+  CM_PREC_MIXED = 1  /* FP32 gates and currents; Vm, [Na]i, [K]i, [Ca]SR (Courtemanche: [Ca]up,
+                        [Ca]rel) accumulated as compensated FP32 pairs (hi + lo); buffered-Ca
+                        quadratics solved in a cancellation-free increment form */
 } cm_precision;
 
 /* State layouts for cm_batch_get_state / cm_batch_set_state. */
@@ -277,15 +278,27 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
                           int64_t cell_stride, int64_t max_pairs, int64_t *n_pairs);
 /* Number of pairs held; X (n x 22) / T (n x 19) receive them when not NULL. */
 int cm_surrogate_dataset(cm_surrogate_t s, int64_t *n_pairs, float *X, float *T);
-/* Feature/target normalisation from the data, then `steps` Adam steps on minibatches. */
+/* Feature/target normalisation from the data, then `steps` Adam steps on minibatches. Then
+ * every output's R^2 on a subsample of the data decides whether its correction is applied
+ * (R^2 >= 0) or the coarse step's value is kept: a correction the network predicts worse than
+ * the mean residual is noise that would accumulate over the macro steps. */
 int cm_surrogate_fit(cm_surrogate_t s, int batch, int steps, float lr, uint64_t seed, float *final_loss);
-/* Trained surrogate as one FP32 blob (normalisation + network), for saving and loading. */
+/* Trained surrogate as one FP32 blob, for saving and loading: feature means (22), inverse
+ * standard deviations (22), target scales (19), applied correction scales (19, 0 where the
+ * correction is not applied; a caller may zero more of them), the outputs' R^2 on the training
+ * data (19), then the network's parameters as cm_mlp_get_params orders them. */
 int64_t cm_surrogate_blob_size(cm_surrogate_t s);
 int cm_surrogate_get_blob(cm_surrogate_t s, float *blob);
 int cm_surrogate_set_blob(cm_surrogate_t s, const float *blob);
+/* Mode bits of cm_batch_run_surrogate. */
+enum {
+  CM_SUR_COARSE_ONLY = 1, /* coarse step alone: the method without the network */
+  CM_SUR_AUDIT_FP64 = 2   /* the audit sample takes its S fine steps in FP64 (else FP32 mixed) */
+};
 /* n_macro macro steps of the driver loop with the surrogate (MIXED TenTusscher2 batch; Vm in
- * place). mode 0: coarse step + network; mode 1: coarse step alone (the method without the
- * network). Every audit_mod-th cell, rotating, is audited (audit_mod 0: none). */
+ * place). mode 0: coarse step + network, audited cells integrated by the mixed plain step;
+ * CM_SUR_* bits change that. Every audit_mod-th cell, rotating, is audited (audit_mod 0: none):
+ * it takes the plain integrator and its surrogate prediction of Vm is compared with the result. */
 int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n_macro, const cm_stimulus *stim,
                            int mode, int audit_mod, cm_surrogate_stats *stats);
 

@@ -13,6 +13,12 @@ extern "C" {
  * or FP32, measured with independent FMA chains on the given stream (NULL = default). */
 int cm_diag_fma_peak(int fp64, double *tflops, void *stream);
 
+/* One 128 x n tile D = A * B^T on the tcgen05 tensor core (BF16 operands, FP32 accumulation in
+ * tensor memory), with the operand layout and descriptors of the learned macro step: A is
+ * 128 x k and B n x k, row-major BF16 device arrays; D is 128 x n FP32 (device). n in {32, 64,
+ * 128}, k in {32, 64, 128}. Checks the tensor-core path against a host product. */
+int cm_diag_umma_tile(const void *A, const void *B, int n, int k, float *D, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

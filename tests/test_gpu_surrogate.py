@@ -98,6 +98,9 @@ def test_surrogate_accuracy_and_gain(trained, port):
         assert np.all(np.isfinite(a)), mode
     print("surrogate", res)
     assert res[0]["sur"] > 0.9 * n * n_macro  # most cell-macro-steps use the learned step
+    # the network's outputs pass the range audit: few fallbacks beyond the coarse-only run's
+    # (stimulus, fast upstroke, audit sample)
+    assert res[0]["fb"] <= 1.5 * res[1]["fb"], res
     # spec bars against the FP64 oracle, with the network
     assert res[0]["apd"] <= 1.0 and res[0]["rms"] <= 0.5, res
     # what the network gains: on the rotating audit sample the learned macro step is compared with
@@ -113,3 +116,100 @@ def test_surrogate_blob_roundtrip(trained):
     other = cm.Surrogate(p, substeps=S, seed=7)
     other.set_blob(blob)
     np.testing.assert_array_equal(other.get_blob(), blob)
+
+
+def test_surrogate_fp64_audit(trained, port):
+    """The audit sample integrated in FP64 (the reference arithmetic) instead of the mixed step:
+    the run stays within the bars and the audit compares the network with FP64 steps."""
+    cm, p, sur, _ = trained
+    n, bcl = 128, 0.5
+    n_macro = int(round(bcl / (S * DT)))
+    b, sc = population(cm, p, n, seed=98)
+    names = port.param_names(O.TT2)
+    P = port.param_vector(O.TT2, O.load_params(O.TT2))
+    het = {k: P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
+    B = port.init_state(O.TT2, P, n)
+    vo = np.full(n, port.init_vm(O.TT2, P))
+    tro = port.run(O.TT2, P, port.tables(O.TT2, P, DT), B, vo, n_macro * S, DT, textlen=1e-3, bcl=bcl, amp=AMP,
+                   het=het, rec_every=S, n_threads=8)
+    tro = np.concatenate([tro, vo[:, None]], axis=1)
+    vm = b.init_vm()
+    tr, stats = run_traces(cm, b, sur, vm, n_macro, bcl, cm.SUR_AUDIT_FP64)
+    u, a = A.beat_markers(tr, S * DT, [0.0])
+    uo, ao = A.beat_markers(tro, S * DT, [0.0])
+    rms = (np.sqrt(((tr - tro) ** 2).mean(axis=1)) * 1e3).max()
+    audited = sum(s["audited"] for s in stats)
+    err = max(s["max_audit_err_mv"] for s in stats)
+    print("fp64 audit", dict(apd=np.nanmax(np.abs(a - ao)) * 1e3, rms=rms, audited=audited, err=err))
+    assert audited > 0 and np.isfinite(err) and err < 1.0
+    assert np.nanmax(np.abs(a - ao)) * 1e3 <= 1.0 and rms <= 0.5
+
+
+def test_inference_kernel_matches_network(trained):
+    """The tensor-core inference inside the macro step gives the network's output: for every one
+    of the 19 outputs, the state after one macro step with the network minus the state after the
+    coarse step alone (same initial state) equals sd_y * net(features), the network evaluated by
+    the training GEMMs, cell by cell. BF16 operands on both sides; the features differ in their
+    last FP32 bits only, so the tolerance is 5 % of the output's scale plus the state's FP32
+    rounding."""
+    cm, p, sur, _ = trained
+    n = 1000
+    b, sc = population(cm, p, n, seed=97)
+    vm = b.init_vm()
+    b.run(vm, 3000, textbegin=0.0, textlen=1e-3, bcl=0.8, amplitude=AMP)  # 30 ms: plateau
+    s0, v0 = b.get_state(), vm.copy()
+    kw = dict(t0=3000 * DT, textbegin=0.8, textlen=1e-3, bcl=0.8, amplitude=AMP, audit_mod=0)
+    va = v0.copy()
+    st0 = b.run_surrogate(sur, va, 1, mode=0, **kw)
+    sa = b.get_state()
+    b.set_state(s0)
+    vb = v0.copy()
+    st1 = b.run_surrogate(sur, vb, 1, mode=cm.SUR_COARSE_ONLY, **kw)
+    sb = b.get_state()
+    assert st0["surrogate"] == n and st1["surrogate"] == n, (st0, st1)
+    names = cm.state_names(cm.TENTUSSCHER2)
+    idx = {k: i for i, k in enumerate(names)}
+    gates = ["m", "h", "j", "xr1", "xr2", "xs", "r", "s", "d", "f", "f2", "fCa", "Rq"]
+    outs = gates + ["Ca_i", "CaSS", "CaSR", "Na_i", "K_i"]
+    S0 = {k: s0[idx[k]] for k in names}
+    F = np.stack([v0 * 1e3] + [S0[k] for k in gates] +
+                 [np.log(np.maximum(S0["Ca_i"], 1e-12)), np.log(np.maximum(S0["CaSS"], 1e-12)), S0["CaSR"],
+                  S0["Na_i"], S0["K_i"], np.log(sc[0]), np.log(sc[1]), np.log(sc[2])], axis=1)
+    blob = sur.get_blob()
+    mu, inv_sd, sd_y, apply_y = blob[:22], blob[22:44], blob[44:63], blob[63:82]
+    assert apply_y[0] > 0  # the Vm correction is one the network predicts
+    Y = sur.mlp.forward(((F - mu) * inv_sd).astype(np.float32)).astype(np.float64)
+    got = [(va - vb) * 1e3] + [sa[idx[k]] - sb[idx[k]] for k in outs]
+    scale = [np.abs(v0 * 1e3)] + [np.abs(sb[idx[k]]) for k in outs]
+    worst = 0.0
+    for k in range(19):
+        want = apply_y[k] * Y[:, k]
+        tol = 0.05 * sd_y[k] * np.maximum(1.0, np.abs(Y[:, k])) + 4 * np.spacing(scale[k].astype(np.float32))
+        err = np.abs(got[k] - want)
+        worst = max(worst, float((err / tol).max()))
+        assert np.all(err <= tol), (k, float(err.max()), float(tol.min()), int((err > tol).sum()))
+    print("inference: worst error / tolerance", worst)
+
+
+def test_surrogate_per_cell_stimulus(trained):
+    """Per-cell first stimulus times (the reference driver's textbegin per cell): one batch with
+    two stimulus phases equals two batches with one phase each, cell by cell."""
+    cm, p, sur, _ = trained
+    n, bcl, n_macro = 256, 0.5, 2500
+    phases = (0.0, 0.2)
+    kw = dict(textlen=1e-3, bcl=bcl, amplitude=AMP, audit_mod=0)
+    sep = []
+    for k, ph in enumerate(phases):
+        b, _ = population(cm, p, n, seed=60 + k)
+        v = b.init_vm()
+        b.run_surrogate(sur, v, n_macro, textbegin=ph, **kw)
+        sep.append(v)
+    both = cm.Batch(p, 2 * n, cm.MIXED)
+    scs = [W.conductance_scales(60 + k, n, 3, 0.85, 1.15) for k in range(2)]
+    for j, name in enumerate(W.TT2_HETERO):
+        both.add_hetero_value(name, p.get(name) * np.concatenate([scs[0][j], scs[1][j]]))
+    v = both.init_vm()
+    tbc = np.repeat(np.array(phases), n)
+    st = both.run_surrogate(sur, v, n_macro, textbegin_per_cell=tbc, **kw)
+    assert st["surrogate"] > 0.9 * 2 * n * n_macro
+    np.testing.assert_allclose(v, np.concatenate(sep), rtol=0, atol=1e-9)
