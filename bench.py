@@ -76,7 +76,7 @@ SUR_PLAIN_BYTES_PER_LISTED_CELL = 10 * SUR_BYTES_PER_CELL + 4
 SUR_MLP_FLOPS_PER_CELL = 2 * (128 * 32 + 128 * 128 + 32 * 128)
 # ncu (profiles/sur_step_tc_tt2_1M_cells.md): DRAM bytes of one sur_step launch over 1,048,576
 # cells at steady state, scaled by cells
-SUR_STEP_TRAFFIC_PER_CELL = None
+SUR_STEP_TRAFFIC_PER_CELL = (109_223_680 + 36_175_616) / 1_048_576
 
 
 def dist_env():
@@ -142,6 +142,15 @@ def peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def bf16_peak():
+    """(TFLOP/s, kind): the measured dense BF16 rate for a kernel timed inside a long step."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), "measured sustained"
+    return 1700.0, "fallback sustained"
 
 
 def make_batch(cm, precision, stream, n=N_CELLS, seed=2):
@@ -371,9 +380,13 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     value = FULL_CELLS * SUR_SUBSTEPS * steps / sec
     ms = 1e3 * sec / steps
     listed = stats["fallback"] / max(1, steps)  # cells the plain integrator advanced per macro step
-    algo = FULL_CELLS * SUR_BYTES_PER_CELL + listed * SUR_PLAIN_BYTES_PER_LISTED_CELL
-    achieved = algo / (ms / 1e3) / 1e9
-    tflops = FULL_CELLS * SUR_MLP_FLOPS_PER_CELL / (ms / 1e3) / 1e12
+    # the macro-step kernel alone, timed by the library's events around each of its launches
+    ms_k = stats["ms_step_kernel"] / steps
+    ms_p = stats["ms_plain_kernel"] / steps
+    algo = FULL_CELLS * SUR_BYTES_PER_CELL
+    achieved = algo / (ms_k / 1e3) / 1e9
+    tflops = FULL_CELLS * SUR_MLP_FLOPS_PER_CELL / (ms_k / 1e3) / 1e12
+    tpk, tpk_kind = bf16_peak()
 
     # ---- end to end: one C-ABI call per macro step with pinned host Vm and stimulus times
     for d, tb in zip(inst, tbs):
@@ -420,11 +433,16 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     fp64_value = FULL_CELLS * fp64_steps / sec64
     return {
         "value": value, "seconds": sec, "ms_per_step": ms, "stats": stats, "clocks": clk.summary(),
-        "roofline": {"bound": "hbm", "kernel": "macro step: sur_step_tc_kernel<4> + sur_plain_kernel",
-                     "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_kind": peak_kind, "algorithmic_bytes_per_step": algo,
-                     "traffic": (SUR_STEP_TRAFFIC_PER_CELL * FULL_CELLS) if SUR_STEP_TRAFFIC_PER_CELL else None,
-                     "tensor": {"mlp_tflops": tflops, "peak_bf16_tflops": None, "frac": None}},
+        "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<4>", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": algo,
+                     "traffic": SUR_STEP_TRAFFIC_PER_CELL * FULL_CELLS,
+                     "traffic_note": "ncu DRAM bytes of one 1,048,576-cell launch, scaled by cells",
+                     "tensor": {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s", "frac": tflops / tpk,
+                                "peak_kind": tpk_kind, "flops_per_launch": FULL_CELLS * SUR_MLP_FLOPS_PER_CELL},
+                     "issue_bound": "see profiles/sur_step_tc_tt2_1M_cells.md"},
+        "sur_plain_kernel": {"ms_per_launch": ms_p, "listed_cells_per_launch": listed,
+                             "algorithmic_bytes_per_launch": listed * SUR_PLAIN_BYTES_PER_LISTED_CELL},
         "e2e": {"value": FULL_CELLS * SUR_SUBSTEPS * e2e_steps / e2e_sec, "unit": UNIT,
                 "h2d_bytes_per_step": 16 * FULL_CELLS, "d2h_bytes_per_step": 8 * FULL_CELLS, "steps": e2e_steps,
                 "api": "cm_batch_run_surrogate per macro step, pinned host Vm and per-cell stimulus times"},
@@ -645,6 +663,7 @@ def main():
             "training": training,
             "e2e": full["e2e"],
             "roofline": full["roofline"],
+            "sur_plain_kernel": full["sur_plain_kernel"],
             "precision_form": prec,
             "learned_form": learned,
             "batched": bat,

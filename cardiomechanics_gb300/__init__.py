@@ -75,7 +75,8 @@ class Stimulus(ctypes.Structure):
 
 class SurrogateStats(ctypes.Structure):
     _fields_ = [("cell_macro_steps", ctypes.c_int64), ("surrogate", ctypes.c_int64), ("fallback", ctypes.c_int64),
-                ("audited", ctypes.c_int64), ("max_audit_err_mv", ctypes.c_double)]
+                ("audited", ctypes.c_int64), ("max_audit_err_mv", ctypes.c_double),
+                ("ms_step_kernel", ctypes.c_double), ("ms_plain_kernel", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

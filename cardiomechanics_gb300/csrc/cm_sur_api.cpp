@@ -47,6 +47,7 @@ struct cm_surrogate_s {
   unsigned long long *totals = nullptr;  // n_sur, n_fallback_total, n_audit
   float *audit_err = nullptr;
   float *bias_block = nullptr;  // b1 | b2 | b3 of the network, contiguous (the inference kernel's layout)
+  std::vector<cudaEvent_t> ev;  // 3 per macro step of a chunk: kernel timing of runs
 };
 
 namespace {
@@ -288,6 +289,7 @@ int cm_mlp_adam_step(cm_mlp_t m, float lr, float beta1, float beta2, float eps) 
 int cm_surrogate_destroy(cm_surrogate_t s) {
   if (!s) return CM_OK;
   cudaStreamSynchronize(s->stream);
+  for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
   s->net.m.release();
   for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
                   (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
@@ -655,6 +657,13 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     pa.bcl = stv.bcl;
     pa.amp = stv.amplitude;
   }
+  constexpr int kEvChunk = 256;
+  while (s->ev.size() < 3 * (size_t)kEvChunk) {
+    cudaEvent_t ev;
+    CK(cudaEventCreate(&ev));
+    s->ev.push_back(ev);
+  }
+  double ms_step = 0, ms_plain = 0;
   for (int64_t mstep = 0; mstep < n_macro && e == cudaSuccess; mstep++) {
     bool on = false;
     if (per_cell) {
@@ -671,8 +680,23 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     ka.audit_phase = audit_mod > 0 ? (int)(mstep % audit_mod) : 0;
     pa.audit_phase = ka.audit_phase;
     e = cudaMemsetAsync(s->n_fallback, 0, sizeof(unsigned int), st);
+    // the two kernels bracketed by events; every kEvChunk steps the chunk's times are summed
+    const int j = (int)(mstep % kEvChunk);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j], st);
     if (e == cudaSuccess) e = launch_sur_step(ka, n, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j + 1], st);
     if (e == cudaSuccess) e = launch_sur_plain(pa, (int)n, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j + 2], st);
+    if (e == cudaSuccess && (j == kEvChunk - 1 || mstep == n_macro - 1)) {
+      e = cudaEventSynchronize(s->ev[3 * j + 2]);
+      for (int i = 0; i <= j && e == cudaSuccess; i++) {
+        float a = 0.f, b2 = 0.f;
+        e = cudaEventElapsedTime(&a, s->ev[3 * i], s->ev[3 * i + 1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&b2, s->ev[3 * i + 1], s->ev[3 * i + 2]);
+        ms_step += a;
+        ms_plain += b2;
+      }
+    }
   }
   if (e != cudaSuccess) return cuda_fail(e, "surrogate run");
   rc = planes_out(b, Vm, dvm, host_vm, st);
@@ -693,6 +717,8 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     stats->fallback = (int64_t)tot[1];
     stats->audited = (int64_t)tot[2];
     stats->max_audit_err_mv = aerr;
+    stats->ms_step_kernel = ms_step;
+    stats->ms_plain_kernel = ms_plain;
   }
   if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
   return CM_OK;

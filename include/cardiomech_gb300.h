@@ -263,6 +263,8 @@ typedef struct {
   int64_t fallback;         /* advanced by the plain integrator (stimulus, upstroke, audit) */
   int64_t audited;          /* audit sample: surrogate prediction compared with the plain result */
   double max_audit_err_mv;  /* largest |Vm surrogate - Vm plain| over the audit sample [mV] */
+  double ms_step_kernel;    /* device time of the macro-step kernel, summed over the call (CUDA events) */
+  double ms_plain_kernel;   /* device time of the plain-integrator kernel for the listed cells, summed */
 } cm_surrogate_stats;
 
 /* TenTusscher2 parameter set p (its dt is the fine step); substeps fine steps per macro step. */
