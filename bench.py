@@ -12,10 +12,11 @@ set; per-cell stimulus times carry the phases). Inputs are synthetic (seeded); t
 (~2 GB) is larger than L2, so no flush is needed between steps.
 
 value         cell-steps/s of the headline, state resident in HBM (CUDA events, batch stream)
-e2e           the same through the C ABI with pinned HOST Vm and stimulus times, one
-              cm_batch_run_surrogate call per macro step (copies in and out every step)
+e2e           the same through the C ABI with Vm in pinned HOST memory, one
+              cm_batch_run_surrogate call per macro step (Vm copied in and out every step)
 plain_fp64    the plain FP64 kernel (the reference's arithmetic) on the same 16.7M cells
-roofline      the macro step (sur_step_tc_kernel + sur_plain_kernel) against measured HBM
+roofline      the macro-step kernel (timed by the library's CUDA events) against measured HBM,
+              with its tensor-core fraction beside it
 precision_form  4,194,304 cells (2048 x 2048), FP32 + compensated accumulators, BCL 800 ms,
               +-10 %: the HBM-bound plain kernel with its own roofline
 learned_form  1,048,576 cells, BCL 500 ms, +-15 %: the surrogate alone (mixed-precision audit)
@@ -337,15 +338,6 @@ def full_form_population(cm, p, precision, stream):
     return inst, b
 
 
-def instance_times(inst, t, n_fine, bcl=FULL_BCL):
-    """Per-instance textbegin after n_fine driver steps from t (phase * bcl at t = 0), and t."""
-    out, t1 = [], t
-    for d in inst:
-        t1, tb = advance_protocol(t, d["tb"], n_fine, bcl)
-        out.append(tb)
-    return out, t1
-
-
 def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_steps, hbm_peak, peak_kind,
                   barrier=lambda: None):
     """The headline: see the module docstring. Returns the leg's figures."""
@@ -360,9 +352,10 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
         return torch.tensor(np.repeat(np.array(tbs), sizes), dtype=torch.float64, device="cuda")
 
     vm = torch.tensor(b.init_vm(), device="cuda")
-    b.run_surrogate(sur, vm, warmup, t0=0.0, textbegin_per_cell=tb_cells([d["tb"] for d in inst]), **kw)
-    tbs, t = instance_times(inst, 0.0, warmup * SUR_SUBSTEPS)
-    tbc = tb_cells(tbs)
+    # per-cell first stimulus times on the device: each run advances them in place (driver state)
+    tbc = tb_cells([d["tb"] for d in inst])
+    b.run_surrogate(sur, vm, warmup, t0=0.0, textbegin_per_cell=tbc, **kw)
+    t = advance_protocol(0.0, 0.0, warmup * SUR_SUBSTEPS, 1e9)[0]
     torch.cuda.synchronize()
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -374,9 +367,7 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
         e1.record(stream)
         torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
-    for d, tb in zip(inst, tbs):
-        d["tb"] = tb
-    tbs, t = instance_times(inst, t, steps * SUR_SUBSTEPS)
+    t = advance_protocol(t, 0.0, steps * SUR_SUBSTEPS, 1e9)[0]
     value = FULL_CELLS * SUR_SUBSTEPS * steps / sec
     ms = 1e3 * sec / steps
     listed = stats["fallback"] / max(1, steps)  # cells the plain integrator advanced per macro step
@@ -388,12 +379,9 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     tflops = FULL_CELLS * SUR_MLP_FLOPS_PER_CELL / (ms_k / 1e3) / 1e12
     tpk, tpk_kind = bf16_peak()
 
-    # ---- end to end: one C-ABI call per macro step with pinned host Vm and stimulus times
-    for d, tb in zip(inst, tbs):
-        d["tb"] = tb
+    # ---- end to end: one C-ABI call per macro step with the cells' Vm in pinned HOST memory
+    # (copied in and out by the call); the stimulus times stay on the device
     vm_h = vm.cpu().pin_memory()
-    tb_h = torch.from_numpy(np.repeat(np.array(tbs), sizes)).pin_memory()
-    starts = np.concatenate([[0], np.cumsum(sizes)])
     del vm
     torch.cuda.synchronize()
     w0 = time.perf_counter()
@@ -401,17 +389,13 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(e2e_steps):
-        b.run_surrogate(sur, vm_h, 1, t0=t, textbegin_per_cell=tb_h, **kw)
-        for i, d in enumerate(inst):  # the driver's per-instance clock on the host
-            _, tb = advance_protocol(t, d["tb"], SUR_SUBSTEPS, FULL_BCL)
-            if tb != d["tb"]:
-                d["tb"] = tb
-                tb_h[starts[i]:starts[i + 1]] = tb
-        t = advance_protocol(t, 0.0, SUR_SUBSTEPS, 1e9)[0]
+        b.run_surrogate(sur, vm_h, 1, t0=t, textbegin_per_cell=tbc, **kw)
+        for _k in range(SUR_SUBSTEPS):
+            t += DT
     f1.record(stream)
     torch.cuda.synchronize()
     e2e_sec = max(time.perf_counter() - w0, f0.elapsed_time(f1) / 1e3)
-    del b
+    del b, tbc
     torch.cuda.empty_cache()
 
     # ---- plain FP64 kernel on the same cells and protocol
@@ -419,7 +403,6 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     v64 = torch.tensor(b64.init_vm(), device="cuda")
     tb64 = tb_cells([d["phase"] * FULL_BCL for d in inst])
     b64.run(v64, 3, textlen=1e-3, bcl=FULL_BCL, amplitude=W.TT2_STIM_NA, textbegin_per_cell=tb64)
-    tb64 = tb_cells(instance_times([dict(tb=d["phase"] * FULL_BCL) for d in inst], 0.0, 3)[0])
     torch.cuda.synchronize()
     g0 = torch.cuda.Event(enable_timing=True)
     g1 = torch.cuda.Event(enable_timing=True)
@@ -433,7 +416,8 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     fp64_value = FULL_CELLS * fp64_steps / sec64
     return {
         "value": value, "seconds": sec, "ms_per_step": ms, "stats": stats, "clocks": clk.summary(),
-        "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<4>", "achieved": achieved, "peak": hbm_peak,
+        "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<3, audit> (3 MLP groups + the FP64 audit group)",
+                     "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": algo,
                      "traffic": SUR_STEP_TRAFFIC_PER_CELL * FULL_CELLS,
@@ -444,8 +428,9 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
         "sur_plain_kernel": {"ms_per_launch": ms_p, "listed_cells_per_launch": listed,
                              "algorithmic_bytes_per_launch": listed * SUR_PLAIN_BYTES_PER_LISTED_CELL},
         "e2e": {"value": FULL_CELLS * SUR_SUBSTEPS * e2e_steps / e2e_sec, "unit": UNIT,
-                "h2d_bytes_per_step": 16 * FULL_CELLS, "d2h_bytes_per_step": 8 * FULL_CELLS, "steps": e2e_steps,
-                "api": "cm_batch_run_surrogate per macro step, pinned host Vm and per-cell stimulus times"},
+                "h2d_bytes_per_step": 8 * FULL_CELLS, "d2h_bytes_per_step": 8 * FULL_CELLS, "steps": e2e_steps,
+                "api": "cm_batch_run_surrogate per macro step, Vm in pinned host memory; per-cell stimulus "
+                       "times kept on the device (advanced in place by the library)"},
         "plain_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * sec64 / fp64_steps,
                        "steps": fp64_steps, "cells": FULL_CELLS, "bytes_per_cell_step": FP64_BYTES_PER_CELL_STEP,
                        "achieved_gbs": FP64_BYTES_PER_CELL_STEP * FULL_CELLS / (sec64 / fp64_steps) / 1e9,

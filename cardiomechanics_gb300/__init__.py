@@ -44,6 +44,7 @@ ABI_SYMBOLS = (
     "cm_params_create", "cm_params_destroy", "cm_params_info", "cm_params_get", "cm_params_set",
     "cm_params_table", "cm_batch_create", "cm_batch_destroy", "cm_batch_info", "cm_batch_reset",
     "cm_batch_set_hetero", "cm_batch_set_diagnostics", "cm_batch_init_vm", "cm_batch_get_state",
+    "cm_batch_step_update_act",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
@@ -51,7 +52,7 @@ ABI_SYMBOLS = (
     "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
     "cm_surrogate_destroy", "cm_surrogate_mlp", "cm_surrogate_generate", "cm_surrogate_dataset",
     "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
-    "cm_batch_run_surrogate", "cm_mlp_forward_static",
+    "cm_batch_run_surrogate", "cm_mlp_forward_static", "cm_surrogate_flush_audit",
 )
 
 
@@ -115,6 +116,8 @@ def lib() -> ctypes.CDLL:
     L.cm_batch_set_state.argtypes = [vp, ctypes.c_int, vp]
     L.cm_batch_step.argtypes = [vp, ctypes.c_double, vp, vp, vp, vp]
     L.cm_batch_step_update.argtypes = [vp, ctypes.c_double, vp, vp, vp, ctypes.c_double]
+    L.cm_batch_step_update_act.argtypes = [vp, ctypes.c_double, vp, vp, vp, ctypes.c_double, vp, ctypes.c_double,
+                                           ctypes.c_double]
     L.cm_batch_run.argtypes = [vp, vp, i64, ctypes.POINTER(Stimulus), vp, i64, i64, vp]
     L.cm_batch_audit.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
     L.cm_batch_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
@@ -134,6 +137,7 @@ def lib() -> ctypes.CDLL:
         getattr(L, f).argtypes = [vp, vp]
     L.cm_mlp_forward.argtypes = [vp, vp, i64, vp]
     L.cm_mlp_forward_static.argtypes = [vp, vp, i64, vp]
+    L.cm_surrogate_flush_audit.argtypes = [vp, ctypes.c_int, vp]
     L.cm_mlp_loss_grad.argtypes = [vp, vp, vp, i64, fp]
     L.cm_mlp_adam_step.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
     L.cm_surrogate_create.argtypes = [ctypes.POINTER(vp), vp, ctypes.c_int, ctypes.c_uint64, vp]
@@ -309,6 +313,16 @@ class Batch:
         i_ext = _f64(i_ext, self.n, "i_ext")
         stretch = _f64(stretch, self.n, "stretch")
         _check(lib().cm_batch_step_update(self._h, dt, _ptr(Vm), _ptr(i_ext), _ptr(stretch), vm_range))
+
+    def calc_update_act(self, dt, Vm, act_time, t, threshold, i_ext=None, stretch=None, vm_range=0.0):
+        """calc_update plus activation times: act_time (float64, -1 = not yet activated) gets t
+        for every cell whose new Vm reaches threshold; updated in place."""
+        Vm = _f64(Vm, self.n, "Vm")
+        act_time = _f64(act_time, self.n, "act_time")
+        i_ext = _f64(i_ext, self.n, "i_ext")
+        stretch = _f64(stretch, self.n, "stretch")
+        _check(lib().cm_batch_step_update_act(self._h, dt, _ptr(Vm), _ptr(i_ext), _ptr(stretch), vm_range,
+                                              _ptr(act_time), t, threshold))
 
     def run(self, Vm, n_steps, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0, t0=0.0,
             textbegin_per_cell=None, probe_cells=None, probe_every=0):
@@ -512,6 +526,12 @@ class Surrogate:
         loss = ctypes.c_float()
         _check(lib().cm_surrogate_fit(self._h, batch, steps, lr, seed, ctypes.byref(loss)))
         return loss.value
+
+    def flush_audit(self, mode=0):
+        """Audit the last run's pending sample now; returns its statistics."""
+        st = SurrogateStats()
+        _check(lib().cm_surrogate_flush_audit(self._h, int(mode), ctypes.byref(st)))
+        return st.as_dict()
 
     def get_blob(self):
         out = np.zeros(int(lib().cm_surrogate_blob_size(self._h)), np.float32)

@@ -483,6 +483,11 @@ int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext
 
 int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
                          double vm_range) {
+  return cm_batch_step_update_act(b, dt, Vm, i_ext, stretch, vm_range, nullptr, 0.0, 0.0);
+}
+
+int cm_batch_step_update_act(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
+                             double vm_range, double *act_time, double t, double act_threshold) {
   if (!b || !Vm) return fail(CM_ERR_ARG, "NULL argument");
   if (dt != b->ps.dt)
     return fail(CM_ERR_ARG, "dt differs from the parameter set's dt (" + std::to_string(b->ps.dt) +
@@ -498,8 +503,17 @@ int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ex
   io.vm_range = vm_range;
   if ((rc = stage_in(b, i_ext, 1, &io.iext))) return rc;
   if ((rc = stage_in(b, stretch, 2, &io.stretch))) return rc;
+  const bool host_act = act_time && !is_device_ptr(act_time);
+  if (act_time) {
+    const double *ain;
+    if ((rc = stage_in(b, act_time, 3, &ain))) return rc;
+    io.act = const_cast<double *>(ain);
+    io.act_time = t;
+    io.act_threshold = act_threshold;
+  }
   CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
   if (host_vm) CK(cudaMemcpyAsync(Vm, io.vm_out, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (host_act) CK(cudaMemcpyAsync(act_time, io.act, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   unsigned int mask = 0;
   CK(cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream));
   CK(cudaStreamSynchronize(b->stream));
@@ -527,12 +541,8 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   cm_stimulus st = {};
   if (stim) st = *stim;
   const bool per_cell = stim && stim->textbegin_per_cell;
-  if (per_cell) {
-    if (!b->tb_cell) CK(cudaMalloc(&b->tb_cell, std::max<int64_t>(1, n) * sizeof(double)));
-    const double *src = stim->textbegin_per_cell;
-    CK(cudaMemcpyAsync(b->tb_cell, src, n * sizeof(double),
-                       is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->stream));
-  }
+  double *tb_cell = nullptr;
+  if (per_cell && (rc = per_cell_times(b, stim->textbegin_per_cell, b->stream, &tb_cell))) return rc;
   const int64_t n_rec = n_probe > 0 ? (n_steps + probe_every - 1) / probe_every : 0;
   if (n_probe > 0) {
     for (int64_t i = 0; i < n_probe; i++)
@@ -568,7 +578,7 @@ int cm_batch_run(cm_batch_t b, double *Vm, int64_t n_steps, const cm_stimulus *s
   io.textlen = st.textlen;
   io.bcl = st.bcl;
   io.amp = st.amplitude;
-  io.tb_cell = per_cell ? b->tb_cell : nullptr;
+  io.tb_cell = tb_cell;
   // The reference driver accumulates t += dt and advances textbegin on the host side of
   // each cell; with one protocol for all cells the same arithmetic runs here once per step.
   double t = st.t0, tb = st.textbegin;

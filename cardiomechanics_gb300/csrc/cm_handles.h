@@ -67,4 +67,17 @@ inline bool is_device_ptr(const void *p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// The driver's per-cell first stimulus times for a run: a device array is used (and advanced)
+// in place; a host array is copied to the batch's own buffer, which the run advances.
+inline int per_cell_times(cm_batch_s *b, const double *src, cudaStream_t s, double **out) {
+  if (is_device_ptr(src)) {
+    *out = const_cast<double *>(src);
+    return CM_OK;
+  }
+  if (!b->tb_cell) CK(cudaMalloc(&b->tb_cell, std::max<int64_t>(1, b->d.n) * sizeof(double)));
+  CK(cudaMemcpyAsync(b->tb_cell, src, b->d.n * sizeof(double), cudaMemcpyHostToDevice, s));
+  *out = b->tb_cell;
+  return CM_OK;
+}
+
 }  // namespace cm

@@ -35,6 +35,7 @@ __device__ __forceinline__ void finish(const DevBatch &b, const StepIO &io, int6
   if (io.dvm) io.dvm[c] = dV;
   if (!isfinite(vn)) audit |= 1u;
   if (io.vm_range > 0.0 && fabs(vn) > io.vm_range) audit |= 32u;
+  if (io.act && io.act[c] == -1.0 && vn >= io.act_threshold) io.act[c] = io.act_time;
   if (audit) {
     atomicOr(b.audit_cell + c, audit);
     atomicOr(b.audit_or, audit);

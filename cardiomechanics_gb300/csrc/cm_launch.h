@@ -49,6 +49,10 @@ struct StepIO {
   // mixed batches in run mode: Vm as compensated FP32 planes (vm_hi + vm_lo), updated in place
   float *vm_hi = nullptr, *vm_lo = nullptr;
   double vm_range = 0.0;  // > 0: flag cells whose new |Vm| exceeds it (fused update only)
+  // fused update only: activation times (acCELLerate.cpp:1997-2005): a cell whose entry is still
+  // -1 and whose new Vm reaches act_threshold gets act_time
+  double *act = nullptr;
+  double act_time = 0.0, act_threshold = 0.0;
 };
 
 int n_fp32_vars(int model);

@@ -41,8 +41,16 @@ struct cm_surrogate_s {
   int64_t gcap = 0;
   // run scratch
   int *fallback = nullptr;
-  float *pred = nullptr;
   int64_t rcap = 0;
+  // audit: two snapshot buffers (even / odd macro steps) and their counters; the macro step k
+  // writes buffer k % 2 and audits buffer (k - 1) % 2
+  float *snap = nullptr;
+  unsigned int *n_snap = nullptr;
+  int64_t snap_cap = 0;
+  int pending = -1;  // buffer holding the last macro step's sample, not audited yet (-1: none)
+  // FP32 constants and tables of the fine step (the mixed-form audit)
+  TT2Consts<float> fine32{};
+  float *rows_fine32 = nullptr, *eca_fine32 = nullptr;
   unsigned int *n_fallback = nullptr;
   unsigned long long *totals = nullptr;  // n_sur, n_fallback_total, n_audit
   float *audit_err = nullptr;
@@ -173,6 +181,34 @@ int planes_out(cm_batch_s *b, double *Vm, double *dvm, bool host_vm, cudaStream_
   return CM_OK;
 }
 
+// The audit of one snapshot buffer (its entries, FP64 or mixed), as the kernels take it.
+SurAuditArgs audit_args(const cm_surrogate_s *s, int buf, bool fp64) {
+  SurAuditArgs aa{};
+  aa.snap = s->snap + (size_t)buf * kSnapPlanes * s->snap_cap;
+  aa.n_snap = s->n_snap + buf;
+  aa.snap_cap = (int)s->snap_cap;
+  aa.substeps = s->substeps;
+  aa.fp64 = fp64 ? 1 : 0;
+  aa.c64 = s->fine64;
+  aa.rows64 = s->rows_fine64;
+  aa.eca64 = s->eca_fine64;
+  aa.c32 = s->fine32;
+  aa.rows32 = s->rows_fine32;
+  aa.eca32 = s->eca_fine32;
+  aa.audit_err = s->audit_err;
+  aa.n_audit = s->totals + 2;
+  return aa;
+}
+
+// Audits the pending sample on its own (a kernel of its own) and clears it.
+int flush_pending(cm_surrogate_s *s, bool fp64, cudaStream_t st) {
+  if (s->pending < 0) return CM_OK;
+  CK(launch_sur_audit(audit_args(s, s->pending, fp64), st));
+  CK(cudaMemsetAsync(s->n_snap + s->pending, 0, sizeof(unsigned int), st));
+  s->pending = -1;
+  return CM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -293,8 +329,10 @@ int cm_surrogate_destroy(cm_surrogate_t s) {
   s->net.m.release();
   for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
                   (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
-                  (void *)s->gkeep, (void *)s->fallback, (void *)s->pred, (void *)s->n_fallback, (void *)s->totals,
-                  (void *)s->audit_err, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block})
+                  (void *)s->gkeep, (void *)s->fallback, (void *)s->snap, (void *)s->n_snap, (void *)s->n_fallback,
+                  (void *)s->totals,
+                  (void *)s->audit_err, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block,
+                  (void *)s->rows_fine32, (void *)s->eca_fine32})
     cudaFree(p);
   delete s;
   return CM_OK;
@@ -323,8 +361,13 @@ int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64
   if (e == cudaSuccess) e = cudaMemcpy(s->rows_coarse, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->eca, eca.data(), eca.size() * sizeof(float), cudaMemcpyHostToDevice);
   {
-    TT2Consts<float> f32;
-    s->fine.tt2_consts(s->fine64, f32);
+    s->fine.tt2_consts(s->fine64, s->fine32);
+    std::vector<float> r32, e32;
+    s->fine.rows_fp32(r32, e32);
+    if (e == cudaSuccess) e = cudaMalloc(&s->rows_fine32, r32.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&s->eca_fine32, e32.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(s->rows_fine32, r32.data(), r32.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->eca_fine32, e32.data(), e32.size() * sizeof(float), cudaMemcpyHostToDevice);
     std::vector<double> r64, e64;
     s->fine.rows_fp64(r64, e64);
     if (e == cudaSuccess) e = cudaMalloc(&s->rows_fine64, r64.size() * sizeof(double));
@@ -585,15 +628,33 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   cudaStream_t st = b->stream;
   if (n > s->rcap) {
     cudaFree(s->fallback);
-    cudaFree(s->pred);
     s->fallback = nullptr;
-    s->pred = nullptr;
     CK(cudaMalloc(&s->fallback, std::max<int64_t>(1, n) * sizeof(int)));
-    CK(cudaMalloc(&s->pred, std::max<int64_t>(1, n) * sizeof(float)));
     s->rcap = n;
   }
   CK(cudaMemsetAsync(s->totals, 0, 3 * sizeof(unsigned long long), st));
   CK(cudaMemsetAsync(s->audit_err, 0, sizeof(float), st));
+  const bool audit_fp64 = (mode & CM_SUR_AUDIT_FP64) != 0;
+  const int64_t snap_need = audit_mod > 0 ? (n + audit_mod - 1) / audit_mod + 32 : 32;
+  if (snap_need > s->snap_cap || audit_mod == 0) {
+    if ((rc = flush_pending(s, audit_fp64, st))) return rc;  // before its buffer goes or no audit follows
+  }
+  if (snap_need > s->snap_cap) {
+    CK(cudaStreamSynchronize(st));
+    cudaFree(s->snap);
+    s->snap = nullptr;
+    s->snap_cap = 0;
+    CK(cudaMalloc(&s->snap, 2 * (size_t)kSnapPlanes * snap_need * sizeof(float)));
+    s->snap_cap = snap_need;
+  }
+  if (!s->n_snap) {
+    CK(cudaMalloc(&s->n_snap, 2 * sizeof(unsigned int)));
+    CK(cudaMemsetAsync(s->n_snap, 0, 2 * sizeof(unsigned int), st));
+  }
+  // the first macro step writes the buffer that holds no pending sample and audits the other
+  // (the pending sample of the previous call, or nothing: its counter is zero)
+  int wbuf = s->pending >= 0 ? (s->pending ^ 1) : 0;
+  if (s->pending < 0) CK(cudaMemsetAsync(s->n_snap, 0, 2 * sizeof(unsigned int), st));
   double *dvm;
   bool host_vm;
   if ((rc = planes_in(b, Vm, &dvm, host_vm, st))) return rc;
@@ -618,7 +679,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.fallback = s->fallback;
   ka.n_fallback = s->n_fallback;
   ka.n_fallback_total = s->totals + 1;
-  ka.pred = s->pred;
+  ka.snap_cap = (int)s->snap_cap;
   ka.n_sur = s->totals;
   ka.g0_Na = (float)s->fine.get("g_Na");
   ka.g0_Kr = (float)s->fine.get("g_Kr");
@@ -636,23 +697,13 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   pa.list = s->fallback;
   pa.n_list = s->n_fallback;
   pa.substeps = s->substeps;
-  pa.audit_mod = audit_mod;
-  pa.pred = s->pred;
-  pa.audit_err = s->audit_err;
-  pa.n_audit = s->totals + 2;
-  pa.audit_fp64 = (mode & CM_SUR_AUDIT_FP64) ? 1 : 0;
-  pa.rows64 = s->rows_fine64;
-  pa.eca64 = s->eca_fine64;
-  pa.c64 = s->fine64;
   cudaError_t e = cudaSuccess;
   const bool per_cell = stim && stim->textbegin_per_cell;
   if (per_cell) {  // the reference driver's per-cell textbegin, advanced on the device
-    if (!b->tb_cell) CK(cudaMalloc(&b->tb_cell, std::max<int64_t>(1, n) * sizeof(double)));
-    const double *src = stim->textbegin_per_cell;
-    CK(cudaMemcpyAsync(b->tb_cell, src, n * sizeof(double),
-                       is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
-    ka.tb_cell = b->tb_cell;
-    pa.tb_cell = b->tb_cell;
+    double *tbc = nullptr;
+    if ((rc = per_cell_times(b, stim->textbegin_per_cell, st, &tbc))) return rc;
+    ka.tb_cell = tbc;
+    pa.tb_cell = tbc;
     pa.textlen = stv.textlen;
     pa.bcl = stv.bcl;
     pa.amp = stv.amplitude;
@@ -678,13 +729,19 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     }
     ka.stim_on = on ? 1 : 0;
     ka.audit_phase = audit_mod > 0 ? (int)(mstep % audit_mod) : 0;
-    pa.audit_phase = ka.audit_phase;
+    const int buf = wbuf;
+    wbuf ^= 1;
+    ka.snap = s->snap + (size_t)buf * kSnapPlanes * s->snap_cap;
+    ka.n_snap = s->n_snap + buf;
+    const SurAuditArgs aa = audit_args(s, buf ^ 1, audit_fp64);  // the previous step's sample
     e = cudaMemsetAsync(s->n_fallback, 0, sizeof(unsigned int), st);
     // the two kernels bracketed by events; every kEvChunk steps the chunk's times are summed
     const int j = (int)(mstep % kEvChunk);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j], st);
-    if (e == cudaSuccess) e = launch_sur_step(ka, n, st);
+    if (e == cudaSuccess) e = launch_sur_step(ka, audit_mod > 0 ? &aa : nullptr, n, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j + 1], st);
+    // the previous step's sample is audited: the next step writes its buffer from zero
+    if (e == cudaSuccess && audit_mod > 0) e = cudaMemsetAsync(s->n_snap + (buf ^ 1), 0, sizeof(unsigned int), st);
     if (e == cudaSuccess) e = launch_sur_plain(pa, (int)n, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j + 2], st);
     if (e == cudaSuccess && (j == kEvChunk - 1 || mstep == n_macro - 1)) {
@@ -699,6 +756,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     }
   }
   if (e != cudaSuccess) return cuda_fail(e, "surrogate run");
+  // the last step's sample is audited by the next run's first macro step, or by
+  // cm_surrogate_flush_audit
+  if (audit_mod > 0 && n_macro > 0) s->pending = wbuf ^ 1;
   rc = planes_out(b, Vm, dvm, host_vm, st);
   unsigned long long tot[3] = {0, 0, 0};
   float aerr = 0;
@@ -721,6 +781,27 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     stats->ms_plain_kernel = ms_plain;
   }
   if (mask & CM_AUDIT_NAN) return fail(CM_ERR_NUMERIC, "Vm is NaN or infinite in at least one cell");
+  return CM_OK;
+}
+
+int cm_surrogate_flush_audit(cm_surrogate_t s, int mode, cm_surrogate_stats *stats) {
+  if (!s) return fail(CM_ERR_ARG, "NULL surrogate");
+  if (stats) *stats = cm_surrogate_stats{};
+  if (s->pending < 0) return CM_OK;
+  cudaStream_t st = s->stream;
+  CK(cudaMemsetAsync(s->totals, 0, 3 * sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(s->audit_err, 0, sizeof(float), st));
+  int rc = flush_pending(s, (mode & CM_SUR_AUDIT_FP64) != 0, st);
+  if (rc) return rc;
+  unsigned long long tot[3] = {0, 0, 0};
+  float aerr = 0.f;
+  CK(cudaMemcpyAsync(tot, s->totals, sizeof(tot), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&aerr, s->audit_err, sizeof(float), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (stats) {
+    stats->audited = (int64_t)tot[2];
+    stats->max_audit_err_mv = aerr;
+  }
   return CM_OK;
 }
 

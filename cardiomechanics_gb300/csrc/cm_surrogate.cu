@@ -117,68 +117,23 @@ __device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
   return r;
 }
 
-// One fine step of a mixed-state cell in FP64: the FP32 planes and compensated pairs widened
-// to double, the reference arithmetic (tt2_calc_fp64 with FP64 tables), the result rounded back.
-__device__ __noinline__ double tt2_fp64_from_mixed(const SurPlainArgs &a, int c, double V, double iext,
-                                                   uint32_t &audit) {
-  const DevBatch &b = a.fine;
-  const int64_t ld = b.ld;
-  float *s = b.s32 + c;
-  const float *const *het = (const float *const *)b.het;
-  TT2Cell<double> x;
-  x.m = s[0]; x.h = s[ld]; x.j = s[2 * ld]; x.xr1 = s[3 * ld]; x.xr2 = s[4 * ld]; x.xs = s[5 * ld];
-  x.r = s[6 * ld]; x.s = s[7 * ld]; x.d = s[8 * ld]; x.f = s[9 * ld]; x.f2 = s[10 * ld]; x.fCa = s[11 * ld];
-  x.Rq = s[12 * ld]; x.Ca_i = s[13 * ld]; x.CaSS = s[14 * ld];
-  double CaSR = acc_to_double(Acc{s[15 * ld], s[16 * ld]});
-  double Na_i = acc_to_double(Acc{s[17 * ld], s[18 * ld]});
-  double K_i = acc_to_double(Acc{s[19 * ld], s[20 * ld]});
-  const TT2Consts<double> &C = a.c64;
-  TT2Het_<double> g;
-  g.g_Na = het[H2_g_Na] ? (double)het[H2_g_Na][c] : C.g_Na;
-  g.g_Kr = het[H2_g_Kr] ? (double)het[H2_g_Kr][c] : C.g_Kr;
-  g.g_K1 = het[H2_g_K1] ? (double)het[H2_g_K1][c] : C.g_K1;
-  g.g_Ks = het[H2_g_Ks] ? (double)het[H2_g_Ks][c] : C.g_Ks;
-  g.g_to = het[H2_g_to] ? (double)het[H2_g_to][c] : C.g_to;
-  g.g_CaL = het[H2_g_CaL] ? (double)het[H2_g_CaL][c] : C.g_CaL;
-  const int vi = vrow_fp64(V * 1000.0, audit);
-  const double dV = tt2_calc_fp64<false>(C, a.rows64 + (size_t)vi * T2_COLS, a.eca64, x, CaSR, Na_i, K_i, g, V, iext,
-                                         audit, nullptr);
-  s[0] = (float)x.m; s[ld] = (float)x.h; s[2 * ld] = (float)x.j; s[3 * ld] = (float)x.xr1; s[4 * ld] = (float)x.xr2;
-  s[5 * ld] = (float)x.xs; s[6 * ld] = (float)x.r; s[7 * ld] = (float)x.s; s[8 * ld] = (float)x.d;
-  s[9 * ld] = (float)x.f; s[10 * ld] = (float)x.f2; s[11 * ld] = (float)x.fCa; s[12 * ld] = (float)x.Rq;
-  s[13 * ld] = (float)x.Ca_i; s[14 * ld] = (float)x.CaSS;
-  Acc t = acc_from_double(CaSR);
-  s[15 * ld] = t.hi; s[16 * ld] = t.lo;
-  t = acc_from_double(Na_i);
-  s[17 * ld] = t.hi; s[18 * ld] = t.lo;
-  t = acc_from_double(K_i);
-  s[19 * ld] = t.hi; s[20 * ld] = t.lo;
-  return dV;
-}
-
 __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
   const unsigned int n = *a.n_list;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int c = a.list[i];
     Acc v{a.vm_hi[c], a.vm_lo[c]};
     uint32_t audit = 0;
-    const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
     double tb = a.tb_cell ? a.tb_cell[c] : 0.0;
-    auto iext_at = [&](int k) -> double {  // reference driver stimulus (CellModel.h:405-419)
-      if (!a.tb_cell) return (double)a.iext[k];
-      double i = 0.0;
-      if (a.tk[k] >= tb) {
-        i = a.amp;
-        if (a.tk[k] >= tb + a.textlen) tb += a.bcl;
+    for (int k = 0; k < a.substeps; k++) {
+      float iext = a.iext[k];
+      if (a.tb_cell) {  // reference driver stimulus (CellModel.h:405-419), per cell
+        iext = 0.f;
+        if (a.tk[k] >= tb) {
+          iext = (float)a.amp;
+          if (a.tk[k] >= tb + a.textlen) tb += a.bcl;
+        }
       }
-      return i;
-    };
-    if (audited && a.audit_fp64) {
-      double V = acc_to_double(v);
-      for (int k = 0; k < a.substeps; k++) V += tt2_fp64_from_mixed(a, c, V, iext_at(k), audit);
-      v = acc_from_double(V);
-    } else {
-      for (int k = 0; k < a.substeps; k++) acc_add(v, tt2_mixed_cell<int>(a.fine, c, v.hi, (float)iext_at(k), audit));
+      acc_add(v, tt2_mixed_cell<int>(a.fine, c, v.hi, iext, audit));
     }
     if (a.tb_cell) a.tb_cell[c] = tb;
     a.vm_hi[c] = v.hi;
@@ -188,15 +143,77 @@ __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
       atomicOr(a.fine.audit_cell + c, audit);
       atomicOr(a.fine.audit_or, audit);
     }
-    if (audited) {
-      const float p = a.pred[c];
-      if (isfinite(p)) {
-        const float err = fabsf(p - (v.hi + v.lo) * 1000.f);
-        atomicMax((int *)a.audit_err, __float_as_int(err));  // non-negative floats order as ints
-        atomicAdd(a.n_audit, 1ull);
-      }
+  }
+}
+
+// The audit of one snapshot: the audited cell integrated over the macro step by the plain method
+// in FP64 (the reference arithmetic: the FP32 state widened, FP64 tables and constants) or in the
+// mixed form; returns |prediction - plain| for Vm [mV] (a NaN counts as the largest error).
+__device__ __forceinline__ float audit_entry(const SurAuditArgs &a, unsigned int i) {
+  const int64_t cap = a.snap_cap;
+  const float *S = a.snap + i;
+  uint32_t audit = 0;
+  float err;
+  if (a.fp64) {
+    TT2Cell<double> x;
+    x.m = S[0]; x.h = S[cap]; x.j = S[2 * cap]; x.xr1 = S[3 * cap]; x.xr2 = S[4 * cap]; x.xs = S[5 * cap];
+    x.r = S[6 * cap]; x.s = S[7 * cap]; x.d = S[8 * cap]; x.f = S[9 * cap]; x.f2 = S[10 * cap];
+    x.fCa = S[11 * cap]; x.Rq = S[12 * cap]; x.Ca_i = S[13 * cap]; x.CaSS = S[14 * cap];
+    double CaSR = acc_to_double(Acc{S[15 * cap], S[16 * cap]});
+    double Na_i = acc_to_double(Acc{S[17 * cap], S[18 * cap]});
+    double K_i = acc_to_double(Acc{S[19 * cap], S[20 * cap]});
+    double V = acc_to_double(Acc{S[21 * cap], S[22 * cap]});
+    TT2Het_<double> g;
+    g.g_Na = S[23 * cap]; g.g_Kr = S[24 * cap]; g.g_K1 = S[25 * cap];
+    g.g_Ks = S[26 * cap]; g.g_to = S[27 * cap]; g.g_CaL = S[28 * cap];
+    for (int k = 0; k < a.substeps; k++) {
+      const int vi = vrow_fp64(V * 1000.0, audit);
+      V += tt2_calc_fp64<false>(a.c64, a.rows64 + (size_t)vi * T2_COLS, a.eca64, x, CaSR, Na_i, K_i, g, V, 0.0, audit,
+                                nullptr);
+    }
+    err = fabsf(S[29 * cap] - (float)(V * 1000.0));
+  } else {
+    TT2Cell<float> x;
+    x.m = S[0]; x.h = S[cap]; x.j = S[2 * cap]; x.xr1 = S[3 * cap]; x.xr2 = S[4 * cap]; x.xs = S[5 * cap];
+    x.r = S[6 * cap]; x.s = S[7 * cap]; x.d = S[8 * cap]; x.f = S[9 * cap]; x.f2 = S[10 * cap];
+    x.fCa = S[11 * cap]; x.Rq = S[12 * cap]; x.Ca_i = S[13 * cap]; x.CaSS = S[14 * cap];
+    Acc CaSR{S[15 * cap], S[16 * cap]}, Na_i{S[17 * cap], S[18 * cap]}, K_i{S[19 * cap], S[20 * cap]};
+    Acc V{S[21 * cap], S[22 * cap]};
+    TT2Het_<float> g;
+    g.g_Na = S[23 * cap]; g.g_Kr = S[24 * cap]; g.g_K1 = S[25 * cap];
+    g.g_Ks = S[26 * cap]; g.g_to = S[27 * cap]; g.g_CaL = S[28 * cap];
+    for (int k = 0; k < a.substeps; k++) {
+      const int vi = vrow_fp32(V.hi * 1000.f, audit);
+      acc_add(V, tt2_calc_mixed(a.c32, a.rows32 + (size_t)vi * T2_COLS, a.eca32, x, CaSR, Na_i, K_i, g, V.hi, 0.f,
+                                audit));
+    }
+    err = fabsf(S[29 * cap] - (V.hi + V.lo) * 1000.f);
+  }
+  return err == err ? err : 3.4e38f;
+}
+
+// Audits of entries [first, n) with stride `stride` by a set of threads that form whole warps:
+// one atomic maximum and one count per warp and round.
+__device__ __forceinline__ void audit_range(const SurAuditArgs &a, unsigned int first, unsigned int stride) {
+  const unsigned int n = min(*a.n_snap, (unsigned int)a.snap_cap);
+  const int lane = threadIdx.x & 31;
+  const unsigned int wfirst = first - (unsigned int)lane;  // the warp's first entry
+  for (unsigned int i0 = wfirst; i0 < n; i0 += stride) {
+    const unsigned int i = i0 + lane;
+    const bool valid = i < n;
+    float err = valid ? audit_entry(a, i) : 0.f;
+    for (int o = 16; o > 0; o >>= 1) err = fmaxf(err, __shfl_xor_sync(0xffffffffu, err, o));
+    const unsigned int cnt = __popc(__ballot_sync(0xffffffffu, valid));
+    if (lane == 0 && cnt) {
+      atomicMax((int *)a.audit_err, __float_as_int(err));  // non-negative floats order as ints
+      atomicAdd(a.n_audit, (unsigned long long)cnt);
     }
   }
+}
+
+// The audit of the last macro step of a run (the others run inside the next macro step).
+__global__ void __launch_bounds__(128) sur_audit_kernel(const SurAuditArgs a) {
+  audit_range(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 __global__ void __launch_bounds__(128) sur_gen_kernel(const SurGenArgs a) {
@@ -337,8 +354,10 @@ __device__ __forceinline__ void warp_count(unsigned long long *counter, bool pre
 // Per group and tile: the features of the cells' initial state go to the tensor core first
 // (layer-1 MMA issued), the coarse physics step runs while it computes, then the three layers'
 // epilogues and MMAs alternate; the network's correction is applied to the coarse result.
-template <int kGroups>
-__global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const SurKernelArgs a, int n) {
+// kAudit: one more group of 4 warps that audits the previous macro step's snapshots (a.prev)
+// while the kGroups MLP groups integrate this one; it uses the FP64 pipe the MLP groups leave idle.
+template <int kGroups, bool kAudit>
+__global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs a, const SurAuditArgs prev, int n) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar_stage[kGroups], bar_mma[kGroups];
   __shared__ uint32_t tslot;
@@ -364,7 +383,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
     bulk_g2s(stage + 21 * kTcCells, a.vm_hi + c0, kTcCells * 4u, &bar_stage[g]);
     bulk_g2s(stage + 22 * kTcCells, a.vm_lo + c0, kTcCells * 4u, &bar_stage[g]);
   };
-  if (leader) {
+  if (leader && g < kGroups) {
     mbar_init(&bar_stage[g], 1);
     mbar_init(&bar_mma[g], 1);
     s_abort[g] = 0;
@@ -374,19 +393,19 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
   // of one 16-byte K chunk, so each quarter-warp stores 128 contiguous bytes
   {
     const uint4 *w1 = (const uint4 *)a.w1, *w2 = (const uint4 *)a.w2, *w3 = (const uint4 *)a.w3;
-    for (int i = threadIdx.x; i < 128 * 4; i += kGroups * 128) {
+    for (int i = threadIdx.x; i < 128 * 4; i += blockDim.x) {
       const int row = i & 127, ch = i >> 7;
       *(uint4 *)(W1 + umma::kmajor_index(row, ch * 8, 32)) = w1[row * 4 + ch];
     }
-    for (int i = threadIdx.x; i < 128 * 16; i += kGroups * 128) {
+    for (int i = threadIdx.x; i < 128 * 16; i += blockDim.x) {
       const int row = i & 127, ch = i >> 7;
       *(uint4 *)(W2 + umma::kmajor_index(row, ch * 8, 128)) = w2[row * 16 + ch];
     }
-    for (int i = threadIdx.x; i < 32 * 16; i += kGroups * 128) {
+    for (int i = threadIdx.x; i < 32 * 16; i += blockDim.x) {
       const int row = i & 31, ch = i >> 5;
       *(uint4 *)(W3 + umma::kmajor_index(row, ch * 8, 128)) = w3[row * 16 + ch];
     }
-    for (int i = threadIdx.x; i < 288; i += kGroups * 128) bias[i] = a.bias[i];
+    for (int i = threadIdx.x; i < 288; i += blockDim.x) bias[i] = a.bias[i];
   }
   const bool mlp_on = a.mode == 0 && !a.stim_on;
   constexpr uint32_t kCols = kGroups == 1 ? 128 : (kGroups == 2 ? 256 : 512);
@@ -398,7 +417,10 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
   const uint32_t tbase = mlp_on ? tslot : 0u;
   const uint32_t tacc = tbase + (uint32_t)(g * 128) + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
   const uint32_t tacc_mma = tbase + (uint32_t)(g * 128);
-  int t = blockIdx.x * kGroups + g;
+  if (kAudit && g == kGroups) {  // the audit group: entries of the previous step's snapshot
+    audit_range(prev, blockIdx.x * 128 + r, gridDim.x * 128);
+  }
+  int t = (kAudit && g == kGroups) ? n_tiles : blockIdx.x * kGroups + g;
   if (leader && t < n_tiles) issue(t);
   const float macro_ms = a.coarse.dt * 1000.f;
   const TT2Consts<float> &C = fb.tt2_32;
@@ -519,9 +541,8 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
       for (int k = 0; k < 32; k++) y[k] = 0.f;
     }
     bool took = false;
+    float pred = 0.f;
     if (valid) {
-      const bool audited = a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
-      if (audited) a.pred[c] = __int_as_float(0x7fc00000);  // NaN unless the surrogate predicts below
       if (!fall) {
         float on[kSurOut], corr[kSurOut];
 #pragma unroll
@@ -539,9 +560,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
           fall = true;
           atomicOr(fb.audit_cell + c, 16u);
           atomicOr(fb.audit_or, 16u);
-        } else if (audited) {
-          a.pred[c] = on[0];
-          fall = true;
         } else {
           Cell nq = q;
           Acc nvm = vm;
@@ -549,9 +567,24 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
           store_cell(fb, c, nq);
           a.vm_hi[c] = nvm.hi;
           a.vm_lo[c] = nvm.lo;
+          pred = (nvm.hi + nvm.lo) * 1000.f;
           took = true;
         }
       }
+    }
+    // audit sample: the accepted steps of this step's audited cells, with their initial state
+    const bool snap = took && a.audit_mod > 0 && (c % a.audit_mod) == a.audit_phase;
+    const unsigned int si = warp_slot(a.n_snap, snap, lane);
+    if (snap && si < (unsigned int)a.snap_cap) {
+      float *D = a.snap + si;
+      const int64_t cap = a.snap_cap;
+      D[0] = q.x.m; D[cap] = q.x.h; D[2 * cap] = q.x.j; D[3 * cap] = q.x.xr1; D[4 * cap] = q.x.xr2;
+      D[5 * cap] = q.x.xs; D[6 * cap] = q.x.r; D[7 * cap] = q.x.s; D[8 * cap] = q.x.d; D[9 * cap] = q.x.f;
+      D[10 * cap] = q.x.f2; D[11 * cap] = q.x.fCa; D[12 * cap] = q.x.Rq; D[13 * cap] = q.x.Ca_i;
+      D[14 * cap] = q.x.CaSS; D[15 * cap] = q.CaSR.hi; D[16 * cap] = q.CaSR.lo; D[17 * cap] = q.Na.hi;
+      D[18 * cap] = q.Na.lo; D[19 * cap] = q.K.hi; D[20 * cap] = q.K.lo; D[21 * cap] = vm.hi; D[22 * cap] = vm.lo;
+      D[23 * cap] = q.g.g_Na; D[24 * cap] = q.g.g_Kr; D[25 * cap] = q.g.g_K1; D[26 * cap] = q.g.g_Ks;
+      D[27 * cap] = q.g.g_to; D[28 * cap] = q.g.g_CaL; D[29 * cap] = pred;
     }
     const bool listed = valid && fall;
     const unsigned int slot = warp_slot(a.n_fallback, listed, lane);
@@ -565,7 +598,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) sur_step_tc_kernel(const Sur
   if (mlp_on && warp == 0) umma::tmem_free(tslot, kCols);
 }
 
-constexpr int kTcGroups = 4;
 
 }  // namespace
 
@@ -585,19 +617,31 @@ cudaError_t launch_sur_normalize(const float *X, const float *T, int64_t n, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_sur_step(const SurKernelArgs &a, int64_t n, cudaStream_t s) {
-  constexpr int smem = tc_smem_bytes(kTcGroups);
+template <int kG, bool kAudit>
+cudaError_t launch_sur_step_t(const SurKernelArgs &a, const SurAuditArgs &prev, int64_t n, cudaStream_t s) {
+  constexpr int smem = tc_smem_bytes(kG);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sur_step_tc_kernel<kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(sur_step_tc_kernel<kG, kAudit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
     if (e != cudaSuccess) return e;
     configured = true;
   }
   if (n <= 0) return cudaSuccess;
-  const int64_t need = (n + kTcCells * kTcGroups - 1) / (kTcCells * kTcGroups);
+  const int64_t need = (n + kTcCells * kG - 1) / (kTcCells * kG);
   const int64_t cap = (int64_t)sm_count();
   const int grid = (int)(need < cap ? need : cap);
-  sur_step_tc_kernel<kTcGroups><<<grid, kTcGroups * 128, smem, s>>>(a, (int)n);
+  sur_step_tc_kernel<kG, kAudit><<<grid, (kG + (kAudit ? 1 : 0)) * 128, smem, s>>>(a, prev, (int)n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sur_step(const SurKernelArgs &a, const SurAuditArgs *prev, int64_t n, cudaStream_t s) {
+  if (prev) return launch_sur_step_t<3, true>(a, *prev, n, s);
+  return launch_sur_step_t<4, false>(a, SurAuditArgs{}, n, s);
+}
+
+cudaError_t launch_sur_audit(const SurAuditArgs &a, cudaStream_t s) {
+  sur_audit_kernel<<<sm_count() * 4, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

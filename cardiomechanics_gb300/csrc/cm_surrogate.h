@@ -52,7 +52,11 @@ struct SurKernelArgs {
   int *fallback;                 // compacted list of cells for the plain integrator
   unsigned int *n_fallback;
   unsigned long long *n_fallback_total;  // over all macro steps
-  float *pred;                   // audited cells: surrogate prediction of Vm [mV], by cell
+  // audit sample: cells with c % audit_mod == audit_phase whose surrogate step was accepted are
+  // copied, with their initial state and the prediction, into a snapshot for the audit kernel
+  float *snap;                   // kSnapPlanes planes of snap_cap entries
+  unsigned int *n_snap;
+  int snap_cap;
   unsigned long long *n_sur;     // cells advanced by the surrogate (over all macro steps)
   float g0_Na, g0_Kr, g0_K1;     // parameter-set conductances (feature reference)
   // per-cell stimulus protocol (else stim_on for all cells): first stimulus time by cell, and
@@ -61,6 +65,10 @@ struct SurKernelArgs {
   double t_last;
 };
 
+// Snapshot of an audited cell: 21 state planes, Vm hi / lo, the six conductances, the
+// surrogate's prediction of Vm [mV] after the macro step.
+constexpr int kSnapPlanes = 21 + 2 + 6 + 1;
+
 struct SurPlainArgs {
   DevBatch fine;
   float *vm_hi, *vm_lo;
@@ -68,18 +76,26 @@ struct SurPlainArgs {
   const unsigned int *n_list;
   int substeps;
   float iext[64];                // per fine step of the macro step
-  int audit_mod, audit_phase;
-  const float *pred;
-  float *audit_err;              // max |prediction - plain| Vm [mV] over audited cells (atomicMax on bits)
-  unsigned long long *n_audit;
-  int audit_fp64;                // audited cells: the S fine steps in FP64 (tables rows64/eca64, constants c64)
-  const double *rows64, *eca64;
-  TT2Consts<double> c64;
   // per-cell stimulus protocol (else iext[] for all cells): the reference driver's logic per
   // fine step k at time tk[k], advancing tb_cell in place
   double *tb_cell;
   double tk[64];
   double textlen, bcl, amp;
+};
+
+// The audit of one macro step: every snapshot integrated by the plain method over the S fine
+// steps (no stimulus: stimulated cells never take the surrogate) in FP64 (the reference
+// arithmetic, FP64 tables) or in the mixed form, and compared with the prediction.
+struct SurAuditArgs {
+  const float *snap;
+  const unsigned int *n_snap;
+  int snap_cap, substeps, fp64;
+  TT2Consts<double> c64;
+  const double *rows64, *eca64;
+  TT2Consts<float> c32;
+  const float *rows32, *eca32;
+  float *audit_err;              // max |prediction - plain| Vm [mV] (atomicMax on the float bits)
+  unsigned long long *n_audit;
 };
 
 struct SurGenArgs {
@@ -106,8 +122,12 @@ struct SurPostArgs {
   int stim_on;
 };
 
-cudaError_t launch_sur_step(const SurKernelArgs &a, int64_t n, cudaStream_t s);
+// prev: the previous macro step's audit, run by an extra warp group of the same launch (the
+// macro step then uses 3 MLP groups); NULL: no audit group, 4 MLP groups.
+cudaError_t launch_sur_step(const SurKernelArgs &a, const SurAuditArgs *prev, int64_t n, cudaStream_t s);
 cudaError_t launch_sur_plain(const SurPlainArgs &a, int max_cells, cudaStream_t s);
+// the audit of the last macro step of a run
+cudaError_t launch_sur_audit(const SurAuditArgs &a, cudaStream_t s);
 cudaError_t launch_sur_gen(const SurGenArgs &a, cudaStream_t s);
 cudaError_t launch_sur_post(const SurPostArgs &a, cudaStream_t s);
 cudaError_t launch_sur_append(const float *X, const float *T, const uint8_t *keep, int64_t n, float *dX, float *dT,

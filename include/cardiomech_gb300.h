@@ -102,7 +102,10 @@ typedef struct {
 typedef struct {
   double t0;
   double textbegin;           /* first stimulus time [s] (all cells) */
-  const double *textbegin_per_cell; /* optional per-cell first stimulus time, overrides */
+  /* Optional per-cell first stimulus time, overrides textbegin. A device array is the driver's
+   * per-cell textbegin state: the run advances it in place, so the next call continues from it.
+   * A host array is only read (the run advances a copy). */
+  const double *textbegin_per_cell;
   double textlen;             /* stimulus duration [s] */
   double bcl;                 /* basic cycle length [s] */
   double amplitude;           /* reference units of i_external */
@@ -173,6 +176,14 @@ int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext
  * the offending cells carry CM_AUDIT_NAN / CM_AUDIT_VMRANGE in cm_batch_audit. */
 int cm_batch_step_update(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
                          double vm_range);
+/* cm_batch_step_update with acCELLerate::IntraStep's activation times fused into the same pass
+ * (acCELLerate.cpp:1997-2005): a cell whose act_time entry is still -1 and whose new Vm reaches
+ * act_threshold [V] gets act_time = t [s]. act_time: n_cells doubles, host or device, updated in
+ * place. The reference checks the Vm after its diffusion solve; this checks the Vm after the
+ * reaction step, which is the same Vm when the step is the whole update (single cells, reaction-
+ * only runs, or a splitting whose diffusion follows and is checked by the caller). */
+int cm_batch_step_update_act(cm_batch_t b, double dt, double *Vm, const double *i_ext, const double *stretch,
+                             double vm_range, double *act_time, double t, double act_threshold);
 
 /* n_steps of the driver loop fused on the device: i_ext from the stimulus protocol,
  * Vm[c] += Calc(dt, Vm[c], i_ext, 1, 1) (CellModel.h:405-420). Vm is updated in place.
@@ -295,14 +306,24 @@ int cm_surrogate_set_blob(cm_surrogate_t s, const float *blob);
 /* Mode bits of cm_batch_run_surrogate. */
 enum {
   CM_SUR_COARSE_ONLY = 1, /* coarse step alone: the method without the network */
-  CM_SUR_AUDIT_FP64 = 2   /* the audit sample takes its S fine steps in FP64 (else FP32 mixed) */
+  CM_SUR_AUDIT_FP64 = 2   /* the audit repeats its S fine steps in FP64 (else in the mixed form) */
 };
 /* n_macro macro steps of the driver loop with the surrogate (MIXED TenTusscher2 batch; Vm in
- * place). mode 0: coarse step + network, audited cells integrated by the mixed plain step;
- * CM_SUR_* bits change that. Every audit_mod-th cell, rotating, is audited (audit_mod 0: none):
- * it takes the plain integrator and its surrogate prediction of Vm is compared with the result. */
+ * place). mode 0: coarse step + network; CM_SUR_* bits change that. Cells with stimulus,
+ * |dVm/dt| above 5 mV/ms or a step the range audit rejects take S plain fine steps instead.
+ * Audit (audit_mod > 0): every audit_mod-th cell, rotating, whose learned step was accepted is
+ * integrated again from the same initial state by the plain method (FP64 with
+ * CM_SUR_AUDIT_FP64, else the mixed form), during the next macro step, and the learned Vm is
+ * compared with the result (stats: audited, max_audit_err_mv). The audited cell keeps its
+ * learned step. The last macro step's sample is audited by the next call (see
+ * cm_surrogate_flush_audit), so a call's stats count the audits completed during it. */
 int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n_macro, const cm_stimulus *stim,
                            int mode, int audit_mod, cm_surrogate_stats *stats);
+/* The audit sample of a run's last macro step is audited by the next run's first macro step
+ * (inside the same launch); this audits it now instead -- after the last run of a simulation --
+ * and reports it in stats (audited, max_audit_err_mv; the other fields 0). mode: the
+ * CM_SUR_AUDIT_FP64 bit chooses the audit's arithmetic. */
+int cm_surrogate_flush_audit(cm_surrogate_t s, int mode, cm_surrogate_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -127,6 +127,73 @@ def test_trace_mixed(gpu, port, model):
             json.dump(report, f, indent=1)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_per_cell_stimulus_times(gpu, port, precision):
+    """The driver protocol with a first stimulus time per cell, against the oracle's loop; a
+    device array of times is advanced in place (a second run continues from it), a host array
+    is left as it was."""
+    import torch
+    cm = gpu
+    n, dt, bcl, steps = 96, 1e-5, 0.3, 20000
+    prec = cm.FP64 if precision == "fp64" else cm.MIXED
+    tbc0 = np.linspace(0.0, 0.25, n)
+    p = cm.Params(5, None, dt)
+    b = cm.Batch(p, n, prec)
+    vm = b.init_vm()
+    tb_host = tbc0.copy()
+    b.run(vm, steps // 2, textlen=1e-3, bcl=bcl, amplitude=AMP[5], textbegin_per_cell=tb_host)
+    assert np.array_equal(tb_host, tbc0)
+    # the same first half with the times on the device, then the second half continuing from them
+    b2 = cm.Batch(p, n, prec)
+    vm2 = b2.init_vm()
+    tb_dev = torch.tensor(tbc0, device="cuda")
+    b2.run(vm2, steps // 2, textlen=1e-3, bcl=bcl, amplitude=AMP[5], textbegin_per_cell=tb_dev)
+    np.testing.assert_array_equal(vm2, vm)
+    t_half = 0.0
+    for _ in range(steps // 2):
+        t_half += dt
+    b2.run(vm2, steps - steps // 2, t0=t_half, textlen=1e-3, bcl=bcl, amplitude=AMP[5], textbegin_per_cell=tb_dev)
+    P = port.param_vector(O.TT2, O.load_params(O.TT2))
+    B = port.init_state(O.TT2, P, n)
+    vo = np.full(n, port.init_vm(O.TT2, P))
+    port.run(O.TT2, P, port.tables(O.TT2, P, dt), B, vo, steps, dt, textlen=1e-3, bcl=bcl, amp=AMP[5],
+             textbegin_per_cell=tbc0, n_threads=8)
+    t_end = 2 * t_half
+    if precision == "fp64":
+        assert np.abs(vm2 - vo).max() <= 1e-8, np.abs(vm2 - vo).max()
+    else:  # within 0.5 mV, away from the upstrokes in progress at the end (a 1 us shift is mV there)
+        calm = ~((tbc0 > t_end - 5e-3) & (tbc0 <= t_end))
+        assert np.abs(vm2 - vo)[calm].max() <= 5e-4, np.abs(vm2 - vo)[calm].max()
+    # the times advanced as the driver advances textbegin: past every stimulus that has ended
+    tb_end = tb_dev.cpu().numpy()
+    assert np.all(tb_end >= tbc0) and np.any(tb_end > tbc0)
+    assert np.all(tb_end + 1e-3 + 2 * dt >= t_end)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_update_activation_times(gpu, precision):
+    """The fused Godunov update with activation times (acCELLerate.cpp:1997-2005): every cell's
+    entry becomes the time of the first step whose new Vm reaches the threshold, as a host loop
+    over the returned Vm finds it; entries already set stay."""
+    cm = gpu
+    n, dt, thr = 64, 1e-5, -0.04
+    b = cm.Batch(cm.Params(5, None, dt), n, cm.FP64 if precision == "fp64" else cm.MIXED)
+    vm = b.init_vm()
+    act = np.full(n, -1.0)
+    act[5] = 123.0  # already activated: must stay
+    first = act.copy()
+    onset = 3 * np.arange(n)
+    t = 0.0
+    for k in range(420):
+        iext = np.where((k >= onset) & (k < onset + 100), AMP[5], 0.0)
+        b.calc_update_act(dt, vm, act, t, thr, i_ext=iext, vm_range=0.2)
+        newly = (first == -1.0) & (vm >= thr)
+        first[newly] = t
+        t += dt
+    np.testing.assert_array_equal(act, first)
+    assert act[5] == 123.0 and (act > 0).sum() == n
+
+
 def test_device_pointers_and_step_equals_run(gpu):
     import torch
     cm = gpu

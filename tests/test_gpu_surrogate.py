@@ -143,6 +143,10 @@ def test_surrogate_fp64_audit(trained, port):
     print("fp64 audit", dict(apd=np.nanmax(np.abs(a - ao)) * 1e3, rms=rms, audited=audited, err=err))
     assert audited > 0 and np.isfinite(err) and err < 1.0
     assert np.nanmax(np.abs(a - ao)) * 1e3 <= 1.0 and rms <= 0.5
+    # the last macro step's sample waits for the next run; flushing audits it now, once
+    fl = sur.flush_audit(cm.SUR_AUDIT_FP64)
+    assert fl["audited"] > 0 and fl["max_audit_err_mv"] < 1.0
+    assert sur.flush_audit(cm.SUR_AUDIT_FP64)["audited"] == 0
 
 
 def test_inference_kernel_matches_network(trained):
