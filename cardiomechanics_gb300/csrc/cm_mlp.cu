@@ -107,8 +107,11 @@ __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__
           const int m = m0 + wm + mi * 16 + g + h * 8;
           const int n = n0 + wn + ni * 8 + 2 * t;
           if (m >= M || n >= N) continue;  // N is even, so n + 1 < N too
+          // hidden biases in BF16, as the inference kernel feeds them to the tensor core
+          const float b0 = __bfloat162float(__float2bfloat16(e.bias[n]));
+          const float b1 = __bfloat162float(__float2bfloat16(e.bias[n + 1]));
           *reinterpret_cast<uint32_t *>(e.out_bf16 + (size_t)m * e.ldc + n) =
-              tanh2_bf16(acc[mi][ni][2 * h] + e.bias[n], acc[mi][ni][2 * h + 1] + e.bias[n + 1]);
+              tanh2_bf16(acc[mi][ni][2 * h] + b0, acc[mi][ni][2 * h + 1] + b1);
         }
     return;
   }

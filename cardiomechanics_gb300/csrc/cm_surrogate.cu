@@ -294,14 +294,18 @@ __global__ void sur_normalize_kernel(const float *__restrict__ X, const float *_
 // columns for the FP32 accumulators of the three layers (each layer's accumulator is read back
 // by tcgen05.ld before the next layer's MMA overwrites it). One elected thread per group issues
 // the MMAs; completion is signalled through an mbarrier by tcgen05.commit.
+// The hidden biases are added on the tensor core: b1 as column 22 of W1 against a constant 1 in
+// column 22 of the input tile, b2 by one more MMA of a constant 128 x 16 tile whose column 0 is 1
+// against a 128 x 16 tile whose column 0 is b2. b3 (19 values) is added in the epilogue.
 constexpr int kTcCells = 128;
-constexpr int kTcStageVars = 21 + 2;  // state planes and the Vm pair
+constexpr int kTcStageVars = 21;  // the tile's state planes (Vm is read with plain loads)
 constexpr int kTcW1 = 128 * 32 * 2, kTcW2 = 128 * 128 * 2, kTcW3 = 32 * 128 * 2;
-constexpr int kTcBias = 1280;                       // 288 floats, padded to keep 128-B alignment
+constexpr int kTcOnes = 128 * 16 * 2, kTcB2 = 128 * 16 * 2, kTcB3 = 32 * 4;
+constexpr int kTcHead = kTcW1 + kTcW2 + kTcW3 + kTcOnes + kTcB2 + kTcB3;
 constexpr int kTcAct = kTcCells * 128 * 2;          // activation tile (BF16)
 constexpr int kTcStage = kTcStageVars * kTcCells * 4;
 constexpr int kTcGroupBytes = kTcAct + kTcStage;
-__host__ __device__ constexpr int tc_smem_bytes(int groups) { return kTcW1 + kTcW2 + kTcW3 + kTcBias + groups * kTcGroupBytes; }
+__host__ __device__ constexpr int tc_smem_bytes(int groups) { return kTcHead + groups * kTcGroupBytes; }
 
 __device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;\n" ::"r"(g + 1) : "memory"); }
 
@@ -319,15 +323,15 @@ __device__ __forceinline__ uint32_t pack_bf16(float x, float y) {
 }
 
 // One hidden-layer epilogue for this thread's row: TMEM columns [0, 128) of the group's
-// accumulator + bias -> tanh -> BF16, written as row r of a 128 x 128 K-major operand tile.
-__device__ __forceinline__ void tc_hidden_epilogue(uint32_t tacc, const float *bias, __nv_bfloat16 *act, int r) {
+// accumulator (bias included) -> tanh -> BF16, written as row r of a 128 x 128 K-major tile.
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t tacc, __nv_bfloat16 *act, int r) {
 #pragma unroll 1
   for (int c0 = 0; c0 < 128; c0 += 32) {
     float v[32];
     umma::tmem_ld32(tacc + (uint32_t)c0, v);
     uint32_t h[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) h[j] = tanh2_bf16(v[2 * j] + bias[c0 + 2 * j], v[2 * j + 1] + bias[c0 + 2 * j + 1]);
+    for (int j = 0; j < 16; j++) h[j] = tanh2_bf16(v[2 * j], v[2 * j + 1]);
 #pragma unroll
     for (int q = 0; q < 4; q++)
       sts128(act + umma::kmajor_index(r, c0 + 8 * q, 128), h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
@@ -365,9 +369,11 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   __nv_bfloat16 *W1 = (__nv_bfloat16 *)smem;
   __nv_bfloat16 *W2 = (__nv_bfloat16 *)(smem + kTcW1);
   __nv_bfloat16 *W3 = (__nv_bfloat16 *)(smem + kTcW1 + kTcW2);
-  float *bias = (float *)(smem + kTcW1 + kTcW2 + kTcW3);
+  __nv_bfloat16 *ONES = (__nv_bfloat16 *)(smem + kTcW1 + kTcW2 + kTcW3);
+  __nv_bfloat16 *B2T = (__nv_bfloat16 *)(smem + kTcW1 + kTcW2 + kTcW3 + kTcOnes);
+  float *b3 = (float *)(smem + kTcW1 + kTcW2 + kTcW3 + kTcOnes + kTcB2);
   const int g = threadIdx.x >> 7, r = threadIdx.x & 127, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned char *gbase = smem + kTcW1 + kTcW2 + kTcW3 + kTcBias + g * kTcGroupBytes;
+  unsigned char *gbase = smem + kTcHead + g * kTcGroupBytes;
   __nv_bfloat16 *act = (__nv_bfloat16 *)gbase;
   float *stage = (float *)(gbase + kTcAct);
   const bool leader = r == 0;
@@ -376,12 +382,11 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   const float *const *het = (const float *const *)fb.het;
   const int n_tiles = (n + kTcCells - 1) / kTcCells;
   const int t_step = (int)gridDim.x * kGroups;
-  auto issue = [&](int tile) {  // the tile's 21 state planes and Vm pair
+  auto issue = [&](int tile) {  // the tile's 21 state planes
     const int64_t c0 = (int64_t)tile * kTcCells;
     mbar_expect_tx(&bar_stage[g], (uint32_t)kTcStageVars * kTcCells * 4u);
-    for (int v = 0; v < 21; v++) bulk_g2s(stage + v * kTcCells, fb.s32 + v * ld + c0, kTcCells * 4u, &bar_stage[g]);
-    bulk_g2s(stage + 21 * kTcCells, a.vm_hi + c0, kTcCells * 4u, &bar_stage[g]);
-    bulk_g2s(stage + 22 * kTcCells, a.vm_lo + c0, kTcCells * 4u, &bar_stage[g]);
+    for (int v = 0; v < kTcStageVars; v++)
+      bulk_g2s(stage + v * kTcCells, fb.s32 + v * ld + c0, kTcCells * 4u, &bar_stage[g]);
   };
   if (leader && g < kGroups) {
     mbar_init(&bar_stage[g], 1);
@@ -405,7 +410,16 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       const int row = i & 31, ch = i >> 5;
       *(uint4 *)(W3 + umma::kmajor_index(row, ch * 8, 128)) = w3[row * 16 + ch];
     }
-    for (int i = threadIdx.x; i < 288; i += blockDim.x) bias[i] = a.bias[i];
+    // the bias operands: ONES (column 0 = 1), B2T (column 0 = b2), b3 in FP32
+    const __nv_bfloat16 one = __float2bfloat16(1.f), zero = __float2bfloat16(0.f);
+    for (int i = threadIdx.x; i < 128 * 16; i += blockDim.x) {
+      const int row = i >> 4, k = i & 15;
+      ONES[umma::kmajor_index(row, k, 16)] = k == 0 ? one : zero;
+      B2T[umma::kmajor_index(row, k, 16)] = k == 0 ? __float2bfloat16(a.bias[128 + row]) : zero;
+    }
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) b3[i] = a.bias[256 + i];
+    __syncthreads();  // W1's rows are in place: column 22 (padding, zero) takes b1
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) W1[umma::kmajor_index(i, kSurIn, 32)] = __float2bfloat16(a.bias[i]);
   }
   const bool mlp_on = a.mode == 0 && !a.stim_on;
   constexpr uint32_t kCols = kGroups == 1 ? 128 : (kGroups == 2 ? 256 : 512);
@@ -426,6 +440,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   const TT2Consts<float> &C = fb.tt2_32;
   uint32_t ps = 0, pm = 0;  // mbarrier phase parities
   const uint32_t act_s = smem_u32(act), w1_s = smem_u32(W1), w2_s = smem_u32(W2), w3_s = smem_u32(W3);
+  const uint32_t ones_s = smem_u32(ONES), b2_s = smem_u32(B2T);
   auto wait_mma = [&]() {
     if (!mbar_wait(&bar_mma[g], pm)) {
       s_abort[g] = 1;
@@ -461,7 +476,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     q.CaSR = Acc{S[15 * kTcCells], S[16 * kTcCells]};
     q.Na = Acc{S[17 * kTcCells], S[18 * kTcCells]};
     q.K = Acc{S[19 * kTcCells], S[20 * kTcCells]};
-    Acc vm{S[21 * kTcCells], S[22 * kTcCells]};
+    Acc vm{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};  // c < ld: in the planes for padding cells too
     const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
     q.g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
     q.g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + cc) : C.g_Kr;
@@ -481,8 +496,11 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
 #pragma unroll
       for (int j = 0; j < 16; j++) {
         const int k0 = 2 * j, k1 = 2 * j + 1;
-        const float x0 = (valid && k0 < kSurIn) ? (f[k0] - a.norm.mu_x[k0]) * a.norm.inv_sd_x[k0] : 0.f;
-        const float x1 = (valid && k1 < kSurIn) ? (f[k1] - a.norm.mu_x[k1]) * a.norm.inv_sd_x[k1] : 0.f;
+        // column kSurIn = 1 carries b1; padding 0
+        const float x0 = k0 < kSurIn ? (valid ? (f[k0] - a.norm.mu_x[k0]) * a.norm.inv_sd_x[k0] : 0.f)
+                                     : (k0 == kSurIn ? 1.f : 0.f);
+        const float x1 = k1 < kSurIn ? (valid ? (f[k1] - a.norm.mu_x[k1]) * a.norm.inv_sd_x[k1] : 0.f)
+                                     : (k1 == kSurIn ? 1.f : 0.f);
         xb[j] = pack_bf16(x0, x1);
       }
 #pragma unroll
@@ -510,7 +528,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     float y[32];
     if (mlp_on) {
       wait_mma();
-      tc_hidden_epilogue(tacc, bias, act, r);
+      tc_hidden_epilogue(tacc, act, r);
       operands_ready();
       if (leader) {  // layer 2: D = H1 W2^T, K = 128
         umma::fence_after_sync();
@@ -518,10 +536,12 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
 #pragma unroll
         for (int s = 0; s < 8; s++)
           umma::mma_bf16(tacc_mma, umma::smem_desc(act_s + s * 256u, 128u, 2048u), umma::smem_desc(w2_s + s * 256u, 128u, 2048u), id, s);
+        // + ONES (128 x 16) B2T^T: every row gets b2
+        umma::mma_bf16(tacc_mma, umma::smem_desc(ones_s, 128u, 256u), umma::smem_desc(b2_s, 128u, 256u), id, 1u);
         umma::commit(&bar_mma[g]);
       }
       wait_mma();
-      tc_hidden_epilogue(tacc, bias + 128, act, r);
+      tc_hidden_epilogue(tacc, act, r);
       operands_ready();
       if (leader) {  // output layer: D = H2 W3^T, N = 32
         umma::fence_after_sync();
@@ -535,7 +555,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       umma::tmem_ld32(tacc, y);
       umma::fence_before_sync();
 #pragma unroll
-      for (int k = 0; k < kSurOut; k++) y[k] += bias[256 + k];
+      for (int k = 0; k < kSurOut; k++) y[k] += b3[k];
     } else {
 #pragma unroll
       for (int k = 0; k < 32; k++) y[k] = 0.f;

@@ -2,8 +2,9 @@
 
 The network is n_in -> H -> H -> n_out with tanh hidden layers and a linear output; loss is
 the mean of squared errors over all outputs. With bf16=True the operands are rounded to BF16
-at the points where the GPU kernels round them (inputs, weights, hidden pre-activations and
-activations, the output gradient and the back-propagated pre-activation gradients), so the GPU gradients can
+at the points where the GPU kernels round them (inputs, weights, hidden biases, hidden
+pre-activations and activations, the output gradient and the back-propagated pre-activation
+gradients), so the GPU gradients can
 be compared tightly; with bf16=False it is plain FP64 (what the finite-difference check uses).
 Only tests import this module.
 """
@@ -28,9 +29,10 @@ def forward(params, X, bf16_ops=True):
     W1, b1, W2, b2, W3, b3 = [np.asarray(p, np.float64) for p in params]
     r = lambda x: _r(x, bf16_ops)  # noqa: E731
     Xr = r(X)
-    # the GPU rounds the pre-activation to BF16 pairs and takes tanh in BF16 (tanh.approx.bf16x2)
-    H1 = r(np.tanh(r(Xr @ r(W1).T + b1)))
-    H2 = r(np.tanh(r(H1 @ r(W2).T + b2)))
+    # the GPU rounds the pre-activation to BF16 pairs and takes tanh in BF16 (tanh.approx.bf16x2);
+    # the hidden biases enter in BF16 (the inference kernel adds them on the tensor core)
+    H1 = r(np.tanh(r(Xr @ r(W1).T + r(b1))))
+    H2 = r(np.tanh(r(H1 @ r(W2).T + r(b2))))
     Y = H2 @ r(W3).T + b3
     return Y, (Xr, H1, H2)
 
