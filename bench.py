@@ -416,7 +416,7 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     fp64_value = FULL_CELLS * fp64_steps / sec64
     return {
         "value": value, "seconds": sec, "ms_per_step": ms, "stats": stats, "clocks": clk.summary(),
-        "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<3, audit> (3 MLP groups + the FP64 audit group)",
+        "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<4, audit> (4 groups; group 3 audits first)",
                      "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": algo,

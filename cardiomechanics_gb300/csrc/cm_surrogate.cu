@@ -358,14 +358,16 @@ __device__ __forceinline__ void warp_count(unsigned long long *counter, bool pre
 // Per group and tile: the features of the cells' initial state go to the tensor core first
 // (layer-1 MMA issued), the coarse physics step runs while it computes, then the three layers'
 // epilogues and MMAs alternate; the network's correction is applied to the coarse result.
-// kAudit: one more group of 4 warps that audits the previous macro step's snapshots (a.prev)
-// while the kGroups MLP groups integrate this one; it uses the FP64 pipe the MLP groups leave idle.
+// The block's tiles (blockIdx.x + k * gridDim.x) go to its groups through a shared-memory counter,
+// so a group that starts late still takes an even share. kAudit: group kGroups - 1 first audits
+// the previous macro step's snapshots (prev) -- on the FP64 pipe the MLP groups leave idle --
+// and then takes tiles like the others.
 template <int kGroups, bool kAudit>
 __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs a, const SurAuditArgs prev, int n) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar_stage[kGroups], bar_mma[kGroups];
   __shared__ uint32_t tslot;
-  __shared__ int s_abort[kGroups];
+  __shared__ int s_abort[kGroups], s_tile[kGroups], s_next;
   __nv_bfloat16 *W1 = (__nv_bfloat16 *)smem;
   __nv_bfloat16 *W2 = (__nv_bfloat16 *)(smem + kTcW1);
   __nv_bfloat16 *W3 = (__nv_bfloat16 *)(smem + kTcW1 + kTcW2);
@@ -381,13 +383,16 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   const int64_t ld = fb.ld;
   const float *const *het = (const float *const *)fb.het;
   const int n_tiles = (n + kTcCells - 1) / kTcCells;
-  const int t_step = (int)gridDim.x * kGroups;
+  auto grab = [&]() -> int {  // the block's next tile (leader threads)
+    return (int)blockIdx.x + atomicAdd(&s_next, 1) * (int)gridDim.x;
+  };
   auto issue = [&](int tile) {  // the tile's 21 state planes
     const int64_t c0 = (int64_t)tile * kTcCells;
     mbar_expect_tx(&bar_stage[g], (uint32_t)kTcStageVars * kTcCells * 4u);
     for (int v = 0; v < kTcStageVars; v++)
       bulk_g2s(stage + v * kTcCells, fb.s32 + v * ld + c0, kTcCells * 4u, &bar_stage[g]);
   };
+  if (threadIdx.x == 0) s_next = 0;
   if (leader && g < kGroups) {
     mbar_init(&bar_stage[g], 1);
     mbar_init(&bar_mma[g], 1);
@@ -431,11 +436,16 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   const uint32_t tbase = mlp_on ? tslot : 0u;
   const uint32_t tacc = tbase + (uint32_t)(g * 128) + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lanes
   const uint32_t tacc_mma = tbase + (uint32_t)(g * 128);
-  if (kAudit && g == kGroups) {  // the audit group: entries of the previous step's snapshot
+  if (kAudit && g == kGroups - 1) {  // the audit group: entries of the previous step's snapshot
     audit_range(prev, blockIdx.x * 128 + r, gridDim.x * 128);
   }
-  int t = (kAudit && g == kGroups) ? n_tiles : blockIdx.x * kGroups + g;
-  if (leader && t < n_tiles) issue(t);
+  if (leader) {
+    const int t0 = grab();
+    s_tile[g] = t0;
+    if (t0 < n_tiles) issue(t0);
+  }
+  group_sync(g);
+  int t = s_tile[g];
   const float macro_ms = a.coarse.dt * 1000.f;
   const TT2Consts<float> &C = fb.tt2_32;
   uint32_t ps = 0, pm = 0;  // mbarrier phase parities
@@ -454,7 +464,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     umma::fence_before_sync();
     group_sync(g);
   };
-  for (; t < n_tiles; t += t_step) {
+  while (t < n_tiles) {
     if (!mbar_wait(&bar_stage[g], ps)) {
       s_abort[g] = 1;
       atomicOr(fb.audit_or, kAuditTimeout);
@@ -485,9 +495,13 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     q.g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + cc) : C.g_to;
     q.g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + cc) : C.g_CaL;
     group_sync(g);  // the stage is free: the next tile's copies overlap this tile's work
-    if (leader && t + t_step < n_tiles) {
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      issue(t + t_step);
+    if (leader) {
+      const int tn = grab();
+      s_tile[g] = tn;
+      if (tn < n_tiles) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        issue(tn);
+      }
     }
     if (mlp_on) {  // features of the initial state -> row r of the 128 x 32 input tile
       float f[kSurIn];
@@ -611,6 +625,8 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     if (listed) a.fallback[slot] = c;
     warp_count(a.n_fallback_total, listed, lane);
     warp_count(a.n_sur, took, lane);
+    group_sync(g);  // the leader's next tile index is visible
+    t = s_tile[g];
   }
   umma::fence_before_sync();
   __syncthreads();
@@ -637,8 +653,9 @@ cudaError_t launch_sur_normalize(const float *X, const float *T, int64_t n, cons
   return cudaGetLastError();
 }
 
-template <int kG, bool kAudit>
+template <bool kAudit>
 cudaError_t launch_sur_step_t(const SurKernelArgs &a, const SurAuditArgs &prev, int64_t n, cudaStream_t s) {
+  constexpr int kG = 4;
   constexpr int smem = tc_smem_bytes(kG);
   static bool configured = false;
   if (!configured) {
@@ -651,13 +668,13 @@ cudaError_t launch_sur_step_t(const SurKernelArgs &a, const SurAuditArgs &prev, 
   const int64_t need = (n + kTcCells * kG - 1) / (kTcCells * kG);
   const int64_t cap = (int64_t)sm_count();
   const int grid = (int)(need < cap ? need : cap);
-  sur_step_tc_kernel<kG, kAudit><<<grid, (kG + (kAudit ? 1 : 0)) * 128, smem, s>>>(a, prev, (int)n);
+  sur_step_tc_kernel<kG, kAudit><<<grid, kG * 128, smem, s>>>(a, prev, (int)n);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sur_step(const SurKernelArgs &a, const SurAuditArgs *prev, int64_t n, cudaStream_t s) {
-  if (prev) return launch_sur_step_t<3, true>(a, *prev, n, s);
-  return launch_sur_step_t<4, false>(a, SurAuditArgs{}, n, s);
+  if (prev) return launch_sur_step_t<true>(a, *prev, n, s);
+  return launch_sur_step_t<false>(a, SurAuditArgs{}, n, s);
 }
 
 cudaError_t launch_sur_audit(const SurAuditArgs &a, cudaStream_t s) {
