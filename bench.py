@@ -75,9 +75,9 @@ SUR_BYTES_PER_CELL = 2 * (21 * 4 + 2 * 4) + 3 * 4
 SUR_PLAIN_BYTES_PER_LISTED_CELL = 10 * SUR_BYTES_PER_CELL + 4
 # MLP FLOPs per cell of one macro step on the tensor core (padded shapes 32-128-128-32)
 SUR_MLP_FLOPS_PER_CELL = 2 * (128 * 32 + 128 * 128 + 32 * 128)
-# ncu (profiles/sur_step_tc_tt2_1M_cells.md): DRAM bytes of one sur_step launch over 1,048,576
+# ncu (profiles/sur_step_tc_tt2_1M_cells.md): DRAM bytes of one macro-step launch over 1,048,576
 # cells at steady state, scaled by cells
-SUR_STEP_TRAFFIC_PER_CELL = (109_223_680 + 36_175_616) / 1_048_576
+SUR_STEP_TRAFFIC_PER_CELL = (110_488_832 + 37_235_712) / 1_048_576
 
 
 def dist_env():
