@@ -21,6 +21,7 @@ precision_form  4,194,304 cells (2048 x 2048), FP32 + compensated accumulators, 
               +-10 %: the HBM-bound plain kernel with its own roofline
 learned_form  1,048,576 cells, BCL 500 ms, +-15 %: the surrogate alone (mixed-precision audit)
 batched       256 instances (1k-1M cells, TT2 and Courtemanche, own parameter sets and phases)
+plain_small   65,536 cells in plain FP64 (the CPU-runnable case of the plain method)
 cpu_baseline  the oracle (C restatement of the reference Calc) on the host cores, bounded sample
 
 --impl reference runs the reference's CPU implementation of the path (the oracle port of its
@@ -82,6 +83,15 @@ SUR_STEP_TRAFFIC_PER_CELL = (110_488_832 + 37_235_712) / 1_048_576
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def max_over_ranks(torch, seconds, world, device="cuda"):
+    """The replicas' timed region ends when the slowest rank's does: the maximum over ranks."""
+    if world <= 1:
+        return seconds
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 class ClockSampler:
@@ -498,6 +508,34 @@ def batched_leg(cm, torch, stream, steps, warmup, hbm_peak, peak_kind, n_inst=25
     return out
 
 
+def plain_small_leg(cm, torch, stream, steps=2000):
+    """The plain method's small case: 65,536 TT2 epi cells in FP64 (the reference arithmetic),
+    g_Na/g_Kr/g_K1 x U[0.95, 1.05] (seed 1), -52 pA/pF for 1 ms every 1000 ms, timed over
+    `steps` of the 100,000-step (1000 ms) run."""
+    from cardiomechanics_gb300 import workloads as W
+    n = 65536
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    b = cm.Batch(p, n, cm.FP64, stream=stream.cuda_stream)
+    sc = W.conductance_scales(1, n, 3, 0.95, 1.05)
+    for k, name in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(name, p.get(name) * sc[k])
+    vm = torch.tensor(b.init_vm(), device="cuda")
+    kw = dict(textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=W.TT2_STIM_NA)
+    b.run(vm, 20, **kw)
+    t = advance_protocol(0.0, 0.0, 20, 1e9)[0]
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(vm, steps, t0=t, **kw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    return {"value": n * steps / sec, "unit": UNIT, "cells": n, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+            "precision": "FP64", "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.95,1.05] seed 1", "bcl_ms": 1000.0,
+            "note": "65,536 cells leave most of the GPU's FP64 pipes idle; the 4.2M-cell figure is plain_fp64"}
+
+
 def precision_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     """Precision form: 4,194,304 cells, the HBM-bound plain kernel (autotuned launch shape)."""
     p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
@@ -604,11 +642,7 @@ def main():
     # ---- the headline: full chosen form at scale
     full = full_form_leg(cm, torch, stream, p, sur, args.steps, args.warmup, args.e2e_steps, args.fp64_steps,
                          hbm_peak, peak_kind, barrier)
-    sec = full["seconds"]
-    if world > 1:
-        t = torch.tensor([sec], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec = float(t.item())
+    sec = max_over_ranks(torch, full["seconds"], world)
     value = world * FULL_CELLS * SUR_SUBSTEPS * args.steps / sec
     if args.only == "full":
         if rank == 0:
@@ -620,6 +654,7 @@ def main():
     del sur
     torch.cuda.empty_cache()
     prec = precision_leg(cm, torch, stream, args, hbm_peak, peak_kind)
+    small = plain_small_leg(cm, torch, stream)
     bat = None
     if not args.no_batched:
         bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
@@ -650,6 +685,7 @@ def main():
             "roofline": full["roofline"],
             "sur_plain_kernel": full["sur_plain_kernel"],
             "precision_form": prec,
+            "plain_small": small,
             "learned_form": learned,
             "batched": bat,
             "fp32_fma_peak_tflops_measured": fp32_peak,

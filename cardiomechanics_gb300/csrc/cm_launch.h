@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "cm_common.cuh"
@@ -73,5 +74,18 @@ cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_l
 cudaError_t launch_vm_split(const double *v, float *hi, float *lo, int64_t n, cudaStream_t s);
 cudaError_t launch_vm_join(const float *hi, const float *lo, double *v, int64_t n, cudaStream_t s);
 int sm_count();
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, once per
+// device for the call site that owns `done` (the attribute belongs to the device's module).
+inline cudaError_t smem_limit(const void *func, int bytes, std::atomic<uint64_t> &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load() & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.fetch_or(bit);
+  return e;
+}
 
 }  // namespace cm

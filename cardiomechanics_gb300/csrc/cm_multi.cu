@@ -193,12 +193,9 @@ template <int kT>
 cudaError_t launch_multi_staged(const MultiLaunch &L, const MultiClock *cur, MultiClock *nxt, unsigned int *cnt,
                                 unsigned int *cnt_next, cudaStream_t s) {
   constexpr size_t smem = (size_t)2 * (StagedVars<2>::kState + 2 + 6) * kT * sizeof(float);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(multi_staged_kernel<kT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)multi_staged_kernel<kT>, (int)smem, done);
+  if (e != cudaSuccess) return e;
   multi_staged_kernel<kT><<<L.grid, kT, smem, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next);
   return cudaGetLastError();
 }

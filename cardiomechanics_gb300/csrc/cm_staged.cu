@@ -85,13 +85,9 @@ template <int kModel, int kThreads>
 cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_sm, cudaStream_t s) {
   constexpr int NVMAX = StagedVars<kModel>::kState + 2 + 6;
   const size_t smem = (size_t)2 * NVMAX * kThreads * sizeof(float);
-  static bool configured = false;  // one attribute call per instantiation and process
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(mixed_staged_kernel<kModel, kThreads>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<uint64_t> done{0};  // one attribute call per instantiation and device
+  cudaError_t e = smem_limit((const void *)mixed_staged_kernel<kModel, kThreads>, (int)smem, done);
+  if (e != cudaSuccess) return e;
   const int n_tiles = (int)((b.n + kThreads - 1) / kThreads);
   int grid = sm_count() * (blocks_per_sm > 0 ? blocks_per_sm : 2);
   if (grid > n_tiles) grid = n_tiles;

@@ -657,13 +657,9 @@ template <bool kAudit>
 cudaError_t launch_sur_step_t(const SurKernelArgs &a, const SurAuditArgs &prev, int64_t n, cudaStream_t s) {
   constexpr int kG = 4;
   constexpr int smem = tc_smem_bytes(kG);
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(sur_step_tc_kernel<kG, kAudit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)sur_step_tc_kernel<kG, kAudit>, smem, done);
+  if (e != cudaSuccess) return e;
   if (n <= 0) return cudaSuccess;
   const int64_t need = (n + kTcCells * kG - 1) / (kTcCells * kG);
   const int64_t cap = (int64_t)sm_count();
