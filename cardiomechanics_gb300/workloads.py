@@ -47,15 +47,21 @@ def conductance_scales(seed: int, n_cells: int, n_params: int, lo: float, hi: fl
 TT2_STIM_NA = 52.0 * 2.29656e-2
 # Courtemanche takes i_external in pA/pF directly (CourtemancheEtAl.h:52 default 20).
 CRN_STIM_PAPF = 20.0
+# O'Hara-Rudy adds i_external to its total current in uA/uF; its parameter files give
+# amplitude -50 for 1 ms (OHaraRudy_*.ev, GetAmplitude() = amplitude, OHaraRudy.h:84).
+ORD_STIM = -50.0
 
 # Per-cell heterogeneous conductances used by the workloads, by model.
 TT2_HETERO = ("g_Na", "g_Kr", "g_K1")
 CRN_HETERO = ("g_Na", "g_to", "g_CaL")
+ORD_HETERO = ("INaF_Multiplier", "IKr_Multiplier", "IK1_Multiplier")
 
 # Conductances a per-instance parameter set scales in the batched form, by model (the
 # heterogeneity slots of each model).
 TT2_INSTANCE_G = ("g_Na", "g_Kr", "g_K1", "g_Ks", "g_to", "g_CaL")
 CRN_INSTANCE_G = ("g_Na", "g_to", "g_Ks", "g_CaL", "g_bNa", "g_bCa")
+ORD_INSTANCE_G = ("INaF_Multiplier", "INaL_Multiplier", "Ito_Multiplier", "IKr_Multiplier", "IKs_Multiplier",
+                  "IK1_Multiplier")
 
 
 def batched_instances(seed: int, n_inst: int = 256, lo: int = 1_000, hi: int = 1_000_000,

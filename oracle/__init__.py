@@ -3,7 +3,7 @@
 Two implementations, both FP64 on the CPU:
 
 * ``Port``  -- oracle/cm_oracle.c, a plain-C restatement of the reference's
-  TenTusscher2 / Courtemanche Calc and InitTable (see that file for file:line
+  TenTusscher2 / Courtemanche / OHaraRudy Calc and InitTable (see that file for file:line
   citations). Builds anywhere with gcc; it is the checker on machines without the
   reference tree and the timed CPU baseline.
 * ``Ref``   -- oracle/_ref/libcmref.so, the reference's own CellModel library compiled
@@ -30,10 +30,12 @@ REF_SO = HERE / "_ref" / "libcmref.so"
 REF_TREE = Path(os.environ.get("CM_REFERENCE_TREE", "/root/reference"))
 GOLDEN = HERE.parent / "tests" / "golden"
 
-TT2, CRN = 0, 1
-MODEL_NAMES = {TT2: "TenTusscher2", CRN: "CourtemancheEtAl"}
+TT2, CRN, ORD = 0, 1, 2
+MODEL_NAMES = {TT2: "TenTusscher2", CRN: "CourtemancheEtAl", ORD: "OHaraRudy"}
 # Reference ElphyModelType values (ElphyModelBasis.h:62-81).
-REF_EMT = {TT2: 5, CRN: 2}
+REF_EMT = {TT2: 5, CRN: 2, ORD: 12}
+# O'Hara-Rudy cell types of the reference's parameter files (celltype 0 / 1 / 2).
+ORD_VARIANTS = ("endo", "epi", "mid")
 RTDT = 4000
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -57,8 +59,12 @@ def build_ref() -> Path | None:
 
 
 def load_params(model: int, variant: str = "epi") -> dict:
-    """Resolved reference parameter set (names -> FP64 values) from the golden fixture."""
-    name = "params_tt2_epi.json" if model == TT2 else "params_crn.json"
+    """Resolved reference parameter set (names -> FP64 values) from the golden fixture.
+    For O'Hara-Rudy, variant is the cell type (endo, epi, mid); the other models have one set."""
+    if model == ORD:
+        name = f"params_ord_{variant}.json"
+    else:
+        name = "params_tt2_epi.json" if model == TT2 else "params_crn.json"
     with open(GOLDEN / name) as f:
         return json.load(f)["params"]
 
@@ -195,6 +201,8 @@ class Ref:
     @staticmethod
     def ev_path(model, variant="epi"):
         d = REF_TREE / "electrophysiology" / "data"
+        if model == ORD:
+            return str(d / f"OHaraRudy_{variant}.ev")
         return str(d / ("TenTusscher2_original_Epi.ev" if model == TT2 else "CourtemancheEtAl.ev"))
 
     def create(self, model, dt, n_cells, ev=None):

@@ -5,6 +5,8 @@
  *   electrophysiology/src/CellModel/CourtemancheEtAl.cpp        (Init 56-83, Calc 85-187)
  *   electrophysiology/src/CellModel/CourtemancheParameters.cpp  (Init 246-247, Calculate 252-280,
  *                                                                InitTable 282-395)
+ *   electrophysiology/src/CellModel/OHaraRudy.cpp               (Init 54-102, Calc 105-663)
+ *   electrophysiology/src/CellModel/OHaraRudyParameters.cpp     (Calculate 246-316; no tables)
  *   electrophysiology/src/CellModel/CellModel.h:405-420         (driver stimulus + Vm update)
  * Expressions keep the reference's evaluation order so that, compiled without FP
  * contraction against the same libm, results match the reference bit for bit; the
@@ -61,13 +63,54 @@
   X(RTdF) X(FdRT) X(RTd2F) X(Vi) X(Vup) X(Vrel) X(VupdVi) X(VreldVi) X(VreldVup) X(CmdFvi)          \
   X(Cmd2F) X(csqnkm) X(kmcsqnm2) X(kkmcsqn) X(cmdnkm) X(kmcmdnm2) X(kkmcmdn) X(kupleak) X(dt_tr)
 
+/* O'Hara-Rudy 2011 as compiled in the reference (ISAC, TRPN, HF, HFM, DUTTA and PASSINI all
+ * defined, OHaraRudyParameters.h:20-36): the .ev parameters in the order of
+ * NS_OHaraRudyParameters::varType (OHaraRudyParameters.h:40-180), then the values
+ * OHaraRudyParameters::Calculate derives (246-316). */
+#define ORD_PARAMS(X)                                                                               \
+  X(amplitude) X(duration) X(celltype) X(Na_o) X(Ca_o) X(K_o) X(INaF_Multiplier) X(INaL_Multiplier) \
+  X(Ito_Multiplier) X(PCa_Multiplier) X(IKr_Multiplier) X(IKs_Multiplier) X(IK1_Multiplier)         \
+  X(INaCa_Multiplier) X(INaK_Multiplier) X(IKb_Multiplier) X(INab_Multiplier) X(ICab_Multiplier)    \
+  X(IpCa_Multiplier) X(Init_Vm) X(Init_Na_i) X(Init_Na_ss) X(Init_K_i) X(Init_K_ss) X(Init_Ca_i)    \
+  X(Init_Ca_ss) X(Init_Ca_nsr) X(Init_Ca_jsr) X(Init_m) X(Init_h_fast) X(Init_h_slow) X(Init_j)      \
+  X(Init_h_CaMK_slow) X(Init_j_CaMK) X(Init_m_L) X(Init_h_L) X(Init_h_L_CaMK) X(Init_a)             \
+  X(Init_i_fast) X(Init_i_slow) X(Init_a_CaMK) X(Init_i_CaMK_fast) X(Init_i_CaMK_slow) X(Init_d)    \
+  X(Init_f_fast) X(Init_f_slow) X(Init_f_Ca_fast) X(Init_f_Ca_slow) X(Init_j_Ca) X(Init_n)          \
+  X(Init_f_CaMK_fast) X(Init_f_Ca_CaMK_fast) X(Init_x_r_fast) X(Init_x_r_slow) X(Init_x_s1)         \
+  X(Init_x_s2) X(Init_x_K1) X(Init_J_rel_NP) X(Init_J_rel_CaMK) X(Init_CaMK_trap) X(ISAC_SWITCH)    \
+  X(alpha) X(G_sac) X(K_sac) X(E_sac) X(Init_Ca_TRPN) X(beta1) X(Ca_T50) X(k_TRPN) X(n_TRPN)        \
+  X(HFM_Multiplier) X(HF_Gomez_1) X(HF_Gomez_2) X(HF_Gomez_3) X(HF_Gomez_4) X(HF_Gomez_5)           \
+  X(HF_Gomez_6) X(HF_Gomez_7) X(HF_Gomez_8) X(HF_Gomez_9) X(HF_Gomez_0)                             \
+  X(R) X(T) X(F) X(L) X(r) X(tau_h_L) X(A_h_fast) X(A_h_slow) X(v_cell) X(A_geo) X(A_cap) X(v_myo)  \
+  X(v_nsr) X(v_jsr) X(v_ss) X(P_CaNa) X(P_CaK) X(P_Ca_CaMK) X(P_CaNa_CaMK) X(P_CaK_CaMK)            \
+  X(A_f_fast) X(A_f_slow) X(k_Na1) X(k_Na2) X(k_asymm) X(k_Ca_on) X(k_Ca_off) X(k_m_1) X(k_p_2)     \
+  X(k_p_4) X(MgADP) X(MgATP) X(K_MgATP) X(beta_tau) X(P_Ca) X(h_10) X(h_11) X(h_12) X(k_1) X(k_2)   \
+  X(k_5) X(beta_1) X(alpha_2) X(alpha_4) X(alpha_rel) X(beta_tau_CaMK) X(alpha_rel_CaMK)            \
+  X(tau_h_LCaMK) X(RToverF)
+
 #define ENUM_TT2(x) T_##x,
 #define ENUM_CRN(x) C_##x,
+#define ENUM_ORD(x) O_##x,
 #define NAME(x) #x,
 enum { TT2_PARAMS(ENUM_TT2) T_LAST };
 enum { CRN_PARAMS(ENUM_CRN) C_LAST };
+enum { ORD_PARAMS(ENUM_ORD) O_LAST };
 static const char *tt2_names[] = {TT2_PARAMS(NAME)};
 static const char *crn_names[] = {CRN_PARAMS(NAME)};
+static const char *ord_names[] = {ORD_PARAMS(NAME)};
+
+/* The reference backup block of OHaraRudy (GetBase() = &m, OHaraRudy.h:31-52): 42 states,
+ * h_CaMK_fast included although Calc never touches it, then the 17 currents it stores. */
+enum {
+  OB_m, OB_h_fast, OB_h_slow, OB_j, OB_h_CaMK_fast, OB_h_CaMK_slow, OB_j_CaMK, OB_m_L, OB_h_L, OB_h_L_CaMK,
+  OB_a, OB_i_fast, OB_i_slow, OB_a_CaMK, OB_i_CaMK_fast, OB_i_CaMK_slow, OB_d, OB_f_fast, OB_f_slow,
+  OB_f_Ca_fast, OB_f_Ca_slow, OB_j_Ca, OB_n, OB_f_CaMK_fast, OB_f_Ca_CaMK_fast, OB_x_r_fast, OB_x_r_slow,
+  OB_x_s1, OB_x_s2, OB_x_K1, OB_Na_i, OB_Na_ss, OB_K_i, OB_K_ss, OB_Ca_i, OB_Ca_ss, OB_Ca_nsr, OB_Ca_jsr,
+  OB_CaMK_trap, OB_J_rel_NP, OB_J_rel_CaMK, OB_Ca_TRPN,
+  OB_I_Na_fast, OB_I_Na_late, OB_I_to, OB_I_CaL, OB_I_CaNa, OB_I_CaK, OB_I_Kr, OB_I_Ks, OB_I_K1,
+  OB_I_NaCa_i, OB_I_NaCa_ss, OB_I_NaK, OB_I_Nab, OB_I_Cab, OB_I_Kb, OB_I_pCa, OB_I_SAC,
+  ORD_BLOCK
+};
 
 /* Lookup tables, in this file's order. */
 #define TT2_TABLES(X)                                                                               \
@@ -87,10 +130,12 @@ enum { CRN_TABLES(TENUM_CRN) TC_LAST };
 static const char *tt2_tnames[] = {TT2_TABLES(NAME)};
 static const char *crn_tnames[] = {CRN_TABLES(NAME)};
 
-int cmo_n_params(int model) { return model == CMO_TT2 ? T_LAST : (model == CMO_CRN ? C_LAST : -1); }
+int cmo_n_params(int model) {
+  return model == CMO_TT2 ? T_LAST : (model == CMO_CRN ? C_LAST : (model == CMO_ORD ? O_LAST : -1));
+}
 const char *cmo_param_name(int model, int i) {
   if (i < 0 || i >= cmo_n_params(model)) return 0;
-  return model == CMO_TT2 ? tt2_names[i] : crn_names[i];
+  return model == CMO_TT2 ? tt2_names[i] : (model == CMO_CRN ? crn_names[i] : ord_names[i]);
 }
 int cmo_param_index(int model, const char *name) {
   int n = cmo_n_params(model);
@@ -98,8 +143,14 @@ int cmo_param_index(int model, const char *name) {
     if (!strcmp(cmo_param_name(model, i), name)) return i;
   return -1;
 }
-int cmo_state_doubles(int model) { return model == CMO_TT2 ? 36 : (model == CMO_CRN ? 22 : -1); }
-int cmo_n_tables(int model) { return model == CMO_TT2 ? TT_LAST : (model == CMO_CRN ? TC_LAST : -1); }
+int cmo_state_doubles(int model) {
+  return model == CMO_TT2 ? 36 : (model == CMO_CRN ? 22 : (model == CMO_ORD ? ORD_BLOCK : -1));
+}
+/* O'Hara-Rudy evaluates every gate directly (its InitTable loop body is empty,
+ * OHaraRudyParameters.cpp:318-441): no tables. */
+int cmo_n_tables(int model) {
+  return model == CMO_TT2 ? TT_LAST : (model == CMO_CRN ? TC_LAST : (model == CMO_ORD ? 0 : -1));
+}
 const char *cmo_table_name(int model, int k) {
   if (k < 0 || k >= cmo_n_tables(model)) return 0;
   return model == CMO_TT2 ? tt2_tnames[k] : crn_tnames[k];
@@ -580,10 +631,476 @@ static double crn_calc(const double *P, const double *tables, double *bk, double
 #undef P_
 #undef TB
 
+/* ---------------------------------------------------------------- O'Hara-Rudy */
+#define P_(x) P[O_##x]
+
+/* OHaraRudyParameters::Calculate (246-316). */
+static void ord_derive(double *P) {
+  P_(R) = 8314.0;
+  P_(T) = 310.0;
+  P_(F) = 96485.0;
+  P_(L) = 0.01;
+  P_(r) = 0.0011;
+  P_(tau_h_L) = 200.0;
+  P_(A_h_fast) = 0.99;
+  P_(A_h_slow) = 0.01;
+  P_(A_f_fast) = 0.6;
+  P_(k_Na1) = 15.0;
+  P_(k_Na2) = 5.0;
+  P_(k_asymm) = 12.5;
+  P_(k_Ca_on) = 1.5e6;
+  P_(k_Ca_off) = 5.0e3;
+  P_(k_m_1) = 182.4;
+  P_(k_p_2) = 687.2;
+  P_(k_p_4) = 639.0;
+  P_(MgADP) = 0.05;
+  P_(MgATP) = 9.8;
+  P_(K_MgATP) = 1.698e-7;
+  P_(beta_tau) = 4.75;
+  P_(P_Ca) = P_(PCa_Multiplier) * 0.0001;
+  /* geometry (275-282): the reference takes pi as 3.14 */
+  P_(v_cell) = 1000.0 * 3.14 * P_(r) * P_(r) * P_(L);
+  P_(A_geo) = 2.0 * 3.14 * P_(r) * P_(r) + 2.0 * 3.14 * P_(r) * P_(L);
+  P_(A_cap) = 2.0 * P_(A_geo);
+  P_(v_myo) = 0.68 * P_(v_cell);
+  P_(v_nsr) = 0.0552 * P_(v_cell);
+  P_(v_jsr) = 0.0048 * P_(v_cell);
+  P_(v_ss) = 0.02 * P_(v_cell);
+  /* permeabilities (285-289); the CaMK-phosphorylated P_CaK uses 3.5743e-4, the other 3.574e-4 */
+  P_(P_CaNa) = 0.00125 * P_(P_Ca);
+  P_(P_CaK) = 3.574e-04 * P_(P_Ca);
+  P_(P_Ca_CaMK) = 1.1 * P_(P_Ca);
+  P_(P_CaNa_CaMK) = 0.00125 * P_(P_Ca_CaMK);
+  P_(P_CaK_CaMK) = 3.5743e-04 * P_(P_Ca_CaMK);
+  P_(A_f_slow) = 1.0 - P_(A_f_fast);
+  /* Na/Ca exchanger and Na/K pump rate constants (295-310) */
+  P_(h_10) = P_(k_asymm) + 1.0 + (P_(Na_o) * (1.0 + P_(Na_o) / P_(k_Na2))) / P_(k_Na1);
+  P_(h_11) = (P_(Na_o) * P_(Na_o)) / (P_(h_10) * P_(k_Na1) * P_(k_Na2));
+  P_(h_12) = 1.0 / P_(h_10);
+  P_(k_1) = P_(h_12) * P_(Ca_o) * P_(k_Ca_on);
+  P_(k_2) = P_(k_Ca_off);
+  P_(k_5) = P_(k_Ca_off);
+  P_(beta_1) = P_(k_m_1) * P_(MgADP);
+  P_(alpha_2) = P_(k_p_2);
+  P_(alpha_4) = (P_(k_p_4) * (P_(MgATP) / P_(K_MgATP))) / (1.0 + (P_(MgATP) / P_(K_MgATP)));
+  P_(alpha_rel) = 0.5 * P_(beta_tau);
+  P_(beta_tau_CaMK) = 1.25 * P_(beta_tau);
+  P_(alpha_rel_CaMK) = 0.5 * P_(beta_tau_CaMK);
+  P_(tau_h_LCaMK) = 3.0 * P_(tau_h_L);
+  P_(RToverF) = (P_(R) * P_(T)) / P_(F);
+}
+
+/* OHaraRudy::Init (54-102). h_CaMK_fast is never initialised nor read by the reference;
+ * it is 0 here. Ca_TRPN is kept as a fraction of its maximum (Init_Ca_TRPN / 0.07). */
+static void ord_init(const double *P, double *b) {
+  memset(b, 0, ORD_BLOCK * sizeof(double));
+  b[OB_m] = P_(Init_m); b[OB_h_fast] = P_(Init_h_fast); b[OB_h_slow] = P_(Init_h_slow); b[OB_j] = P_(Init_j);
+  b[OB_h_CaMK_slow] = P_(Init_h_CaMK_slow); b[OB_j_CaMK] = P_(Init_j_CaMK); b[OB_m_L] = P_(Init_m_L);
+  b[OB_h_L] = P_(Init_h_L); b[OB_h_L_CaMK] = P_(Init_h_L_CaMK); b[OB_a] = P_(Init_a);
+  b[OB_i_fast] = P_(Init_i_fast); b[OB_i_slow] = P_(Init_i_slow); b[OB_a_CaMK] = P_(Init_a_CaMK);
+  b[OB_i_CaMK_fast] = P_(Init_i_CaMK_fast); b[OB_i_CaMK_slow] = P_(Init_i_CaMK_slow); b[OB_d] = P_(Init_d);
+  b[OB_f_fast] = P_(Init_f_fast); b[OB_f_slow] = P_(Init_f_slow); b[OB_f_Ca_fast] = P_(Init_f_Ca_fast);
+  b[OB_f_Ca_slow] = P_(Init_f_Ca_slow); b[OB_j_Ca] = P_(Init_j_Ca); b[OB_n] = P_(Init_n);
+  b[OB_f_CaMK_fast] = P_(Init_f_CaMK_fast); b[OB_f_Ca_CaMK_fast] = P_(Init_f_Ca_CaMK_fast);
+  b[OB_x_r_fast] = P_(Init_x_r_fast); b[OB_x_r_slow] = P_(Init_x_r_slow); b[OB_x_s1] = P_(Init_x_s1);
+  b[OB_x_s2] = P_(Init_x_s2); b[OB_x_K1] = P_(Init_x_K1); b[OB_Na_i] = P_(Init_Na_i); b[OB_Na_ss] = P_(Init_Na_ss);
+  b[OB_K_i] = P_(Init_K_i); b[OB_K_ss] = P_(Init_K_ss); b[OB_Ca_i] = P_(Init_Ca_i); b[OB_Ca_ss] = P_(Init_Ca_ss);
+  b[OB_Ca_nsr] = P_(Init_Ca_nsr); b[OB_Ca_jsr] = P_(Init_Ca_jsr); b[OB_CaMK_trap] = P_(Init_CaMK_trap);
+  b[OB_J_rel_NP] = P_(Init_J_rel_NP); b[OB_J_rel_CaMK] = P_(Init_J_rel_CaMK);
+  b[OB_Ca_TRPN] = P_(Init_Ca_TRPN) / 0.07;
+}
+
+/* Gate update of the reference: x = x_inf - (x_inf - x) * exp(-tinc / tau). */
+static inline double ord_gate(double inf, double x, double tinc, double tau) {
+  return inf - (inf - x) * exp(-tinc / tau);
+}
+
+/* OHaraRudy::Calc (105-663), every expression in the reference's evaluation order. The
+ * block is the reference backup block (states then the currents it stores). */
+static double ord_calc(const double *P, double *b, double tinc, double V, double i_external, double stretch) {
+  tinc *= 1000.0;
+  const double V_m = V * 1000.0;
+  const double lambda_m = 1.2 < stretch ? 1.2 : stretch; /* std::min(1.2, stretch) (109) */
+  /* CaMK (115-131) */
+  const double KmCaMK = 0.15, aCaMK = 0.05, bCaMK = 0.00068, CaMKo = 0.05, KmCaM = 0.0015;
+  double CaMK_trap = b[OB_CaMK_trap];
+  const double Ca_ss = b[OB_Ca_ss], Ca_i = b[OB_Ca_i], Na_i = b[OB_Na_i], Na_ss = b[OB_Na_ss];
+  const double K_i = b[OB_K_i], K_ss = b[OB_K_ss], Ca_nsr = b[OB_Ca_nsr], Ca_jsr = b[OB_Ca_jsr];
+  const double CaMK_bound = CaMKo * ((1.0 - CaMK_trap) / (1.0 + (KmCaM / Ca_ss)));
+  const double CaMK_active = (CaMK_bound + CaMK_trap) * P_(HF_Gomez_1);
+  const double dCaMK_trap = aCaMK * CaMK_bound * (CaMK_bound + CaMK_trap) - (bCaMK * CaMK_trap);
+  CaMK_trap += tinc * dCaMK_trap;
+  b[OB_CaMK_trap] = CaMK_trap;
+  /* reversal potentials (133-138) */
+  const double E_Na = P_(RToverF) * log(P_(Na_o) / Na_i);
+  const double E_K = P_(RToverF) * log(P_(K_o) / K_i);
+  const double PKNa = 0.01833;
+  const double E_Ks = P_(RToverF) * log((P_(K_o) + PKNa * P_(Na_o)) / (K_i + PKNa * Na_i));
+  const double VFFoverRT = (V_m * P_(F) * P_(F)) / (P_(R) * P_(T));
+  const double VFoverRT = (V_m * P_(F)) / (P_(R) * P_(T));
+  const double util_1 = P_(A_cap) / (P_(F) * P_(v_myo));
+  const double util_2 = P_(v_ss) / P_(v_myo);
+  const double util_3 = P_(A_cap) / (P_(F) * P_(v_ss));
+
+  /* I_Na (146-202): Passini h_inf / h_CaMK_inf, Dutta tau_h_fast / tau_j */
+  const double m_inf = 1.0 / (1.0 + exp(-(V_m + 39.57) / 9.871));
+  const double tau_m = 1.0 / (6.765 * exp((V_m + 11.64) / 34.77) + 8.552 * exp(-(V_m + 77.42) / 5.955));
+  b[OB_m] = ord_gate(m_inf, b[OB_m], tinc, tau_m);
+  const double h_inf = 1.0 / (1.0 + exp((V_m + 78.5) / 6.22));
+  const double tau_h_fast = 1.0 / (3.686e-6 * exp(-(V_m + 3.8875) / 7.8579) + 16.0 * exp((V_m - 0.4963) / 9.1843));
+  const double tau_h_slow = 1.0 / (0.009794 * exp(-(V_m + 17.95) / 28.05) + 0.3343 * exp((V_m + 5.730) / 56.66));
+  b[OB_h_fast] = ord_gate(h_inf, b[OB_h_fast], tinc, tau_h_fast);
+  b[OB_h_slow] = ord_gate(h_inf, b[OB_h_slow], tinc, tau_h_slow);
+  const double h = P_(A_h_fast) * b[OB_h_fast] + P_(A_h_slow) * b[OB_h_slow];
+  const double j_inf = h_inf;
+  const double tau_j = 4.8590 + 1.0 / (0.8628 * exp(-(V_m + 116.7258) / 7.6005) + 1.1096 * exp((V_m + 6.2719) / 9.0358));
+  b[OB_j] = ord_gate(j_inf, b[OB_j], tinc, tau_j);
+  const double h_CaMK_inf = 1.0 / (1.0 + exp((V_m + 84.7) / 6.22));
+  const double tau_h_CaMK_slow = 3.0 * tau_h_slow;
+  b[OB_h_CaMK_slow] = ord_gate(h_CaMK_inf, b[OB_h_CaMK_slow], tinc, tau_h_CaMK_slow);
+  const double h_CaMK = P_(A_h_fast) * b[OB_h_fast] + P_(A_h_slow) * b[OB_h_CaMK_slow];
+  const double tau_j_CaMK = 1.46 * tau_j;
+  b[OB_j_CaMK] = ord_gate(j_inf, b[OB_j_CaMK], tinc, tau_j_CaMK);
+  const double phi_INa_CaMK = 1.0 / (1.0 + KmCaMK / CaMK_active);
+  const double G_Na_fast = 75.0;
+  const double m = b[OB_m];
+  const double I_Na_fast = P_(INaF_Multiplier) * G_Na_fast * (V_m - E_Na) * m * m * m *
+                           ((1.0 - phi_INa_CaMK) * h * b[OB_j] + phi_INa_CaMK * h_CaMK * b[OB_j_CaMK]);
+
+  /* I_NaL (204-224) */
+  double thL_mod = 1.0;
+  thL_mod *= P_(HF_Gomez_2);
+  const double m_L_inf = 1.0 / (1.0 + exp(-(V_m + 42.85) / 5.264));
+  b[OB_m_L] = ord_gate(m_L_inf, b[OB_m_L], tinc, tau_m);
+  const double h_L_inf = 1.0 / (1.0 + exp((V_m + 87.61) / 7.488));
+  b[OB_h_L] = ord_gate(h_L_inf, b[OB_h_L], tinc, thL_mod * P_(tau_h_L));
+  const double h_L_CaMK_inf = 1.0 / (1.0 + exp((V_m + 93.81) / 7.488));
+  const double tau_h_L_CaMK = 3.0 * P_(tau_h_L) * thL_mod;
+  b[OB_h_L_CaMK] = ord_gate(h_L_CaMK_inf, b[OB_h_L_CaMK], tinc, tau_h_L_CaMK);
+  const double G_Na_L = 0.0075;
+  const double I_Na_late = P_(INaL_Multiplier) * P_(HF_Gomez_3) * G_Na_L * (V_m - E_Na) * b[OB_m_L] *
+                           ((1.0 - phi_INa_CaMK) * b[OB_h_L] + phi_INa_CaMK * b[OB_h_L_CaMK]);
+
+  /* I_to (226-262) */
+  const double a_inf = 1.0 / (1.0 + exp(-(V_m - 14.34) / 14.82));
+  const double tau_a =
+      1.0515 / (1.0 / (1.2089 * (1.0 + exp(-(V_m - 18.4099) / 29.3814))) + 3.5 / (1.0 + exp((V_m + 100.0) / 29.3814)));
+  b[OB_a] = ord_gate(a_inf, b[OB_a], tinc, tau_a);
+  const double i_inf = 1.0 / (1.0 + exp((V_m + 43.94) / 5.711));
+  const double delta_epi = P_(celltype) == 1.0 ? (1.0 - 0.95 / (1.0 + exp((V_m + 70.0) / 5.0))) : 1.0;
+  const double tau_i_fast_base = 4.562 + 1.0 / (0.3933 * exp(-(V_m + 100.0) / 100.0) + 0.08004 * exp((V_m + 50.0) / 16.59));
+  const double tau_i_slow_base =
+      23.62 + 1.0 / (0.001416 * exp(-(V_m + 96.52) / 59.05) + 1.7808e-08 * exp((V_m + 114.1) / 8.079));
+  const double tau_i_fast = tau_i_fast_base * delta_epi;
+  const double tau_i_slow = tau_i_slow_base * delta_epi;
+  b[OB_i_fast] = ord_gate(i_inf, b[OB_i_fast], tinc, tau_i_fast);
+  b[OB_i_slow] = ord_gate(i_inf, b[OB_i_slow], tinc, tau_i_slow);
+  const double A_i_fast = 1.0 / (1.0 + exp((V_m - 213.6) / 151.2));
+  const double A_i_slow = 1.0 - A_i_fast;
+  const double i = A_i_fast * b[OB_i_fast] + A_i_slow * b[OB_i_slow];
+  const double a_CaMK_inf = 1.0 / (1.0 + exp(-(V_m - 24.34) / 14.82));
+  b[OB_a_CaMK] = ord_gate(a_CaMK_inf, b[OB_a_CaMK], tinc, tau_a);
+  const double delta_CaMK_develop = 1.354 + 1.0e-04 / (exp((V_m - 167.4) / 15.89) + exp(-(V_m - 12.23) / 0.2154));
+  const double delta_CaMK_recover = 1.0 - 0.5 / (1.0 + exp((V_m + 70.0) / 20.0));
+  const double tau_i_CaMK_fast = tau_i_fast * delta_CaMK_develop * delta_CaMK_recover;
+  const double tau_i_CaMK_slow = tau_i_slow * delta_CaMK_develop * delta_CaMK_recover;
+  b[OB_i_CaMK_fast] = ord_gate(i_inf, b[OB_i_CaMK_fast], tinc, tau_i_CaMK_fast);
+  b[OB_i_CaMK_slow] = ord_gate(i_inf, b[OB_i_CaMK_slow], tinc, tau_i_CaMK_slow);
+  const double i_CaMK = A_i_fast * b[OB_i_CaMK_fast] + A_i_slow * b[OB_i_CaMK_slow];
+  const double G_to = 0.02;
+  const double I_to = P_(Ito_Multiplier) * P_(HF_Gomez_4) * G_to * (V_m - E_K) *
+                      ((1.0 - phi_INa_CaMK) * b[OB_a] * i + phi_INa_CaMK * b[OB_a_CaMK] * i_CaMK);
+
+  /* I_CaL, I_CaNa, I_CaK (264-329) */
+  const double d_inf = 1.0 / (1.0 + exp(-(V_m + 3.940) / 4.230));
+  const double tau_d = 0.6 + 1.0 / (exp(-0.05 * (V_m + 6.0)) + exp(0.09 * (V_m + 14.0)));
+  b[OB_d] = ord_gate(d_inf, b[OB_d], tinc, tau_d);
+  const double f_inf = 1.0 / (1.0 + exp((V_m + 19.58) / 3.696));
+  const double tau_f_fast = 7.0 + 1.0 / (0.0045 * exp(-(V_m + 20.0) / 10.0) + 0.0045 * exp((V_m + 20.0) / 10.0));
+  const double tau_f_slow = 1000.0 + 1.0 / (3.5e-05 * exp(-(V_m + 5.0) / 4.0) + 3.5e-05 * exp((V_m + 5.0) / 6.0));
+  b[OB_f_fast] = ord_gate(f_inf, b[OB_f_fast], tinc, tau_f_fast);
+  b[OB_f_slow] = ord_gate(f_inf, b[OB_f_slow], tinc, tau_f_slow);
+  const double f = P_(A_f_fast) * b[OB_f_fast] + P_(A_f_slow) * b[OB_f_slow];
+  const double tau_f_Ca_fast = 7.0 + 1.0 / (0.04 * exp(-(V_m - 4.0) / 7.0) + 0.04 * exp((V_m - 4.0) / 7.0));
+  const double tau_f_Ca_slow = 100.0 + 1.0 / (0.00012 * exp(-V_m / 3.0) + 0.00012 * exp(V_m / 7.0));
+  b[OB_f_Ca_fast] = ord_gate(f_inf, b[OB_f_Ca_fast], tinc, tau_f_Ca_fast);
+  b[OB_f_Ca_slow] = ord_gate(f_inf, b[OB_f_Ca_slow], tinc, tau_f_Ca_slow);
+  const double A_f_Ca_fast = 0.3 + 0.6 / (1.0 + exp((V_m - 10.0) / 10.0));
+  const double A_f_Ca_slow = 1.0 - A_f_Ca_fast;
+  const double f_Ca = A_f_Ca_fast * b[OB_f_Ca_fast] + A_f_Ca_slow * b[OB_f_Ca_slow];
+  const double tau_j_Ca = 75.0;
+  b[OB_j_Ca] = ord_gate(f_inf, b[OB_j_Ca], tinc, tau_j_Ca);
+  const double tau_f_CaMK_fast = 2.5 * tau_f_fast;
+  b[OB_f_CaMK_fast] = ord_gate(f_inf, b[OB_f_CaMK_fast], tinc, tau_f_CaMK_fast);
+  const double f_CaMK = P_(A_f_fast) * b[OB_f_CaMK_fast] + P_(A_f_slow) * b[OB_f_slow];
+  const double tau_f_Ca_CaMK_fast = 2.5 * tau_f_Ca_fast;
+  b[OB_f_Ca_CaMK_fast] = ord_gate(f_inf, b[OB_f_Ca_CaMK_fast], tinc, tau_f_Ca_CaMK_fast);
+  const double f_Ca_CaMK = A_f_Ca_fast * b[OB_f_Ca_CaMK_fast] + A_f_Ca_slow * b[OB_f_Ca_slow];
+  const double j_Ca = b[OB_j_Ca];
+  const double k_m2_n = j_Ca * 1.0;
+  const double Kmn = 0.002, k2n = 1000.0;
+  const double alpha_n = 1.0 / ((k2n / k_m2_n) + pow((1.0 + (Kmn / Ca_ss)), 4.0));
+  b[OB_n] = alpha_n * (k2n / k_m2_n) - (alpha_n * (k2n / k_m2_n) - b[OB_n]) * exp(-k_m2_n * tinc);
+  const double n = b[OB_n];
+  const double z_Ca = 2.0, z_Na = 1.0, z_K = 1.0;
+  const double exp_z_Ca = exp(z_Ca * VFoverRT);
+  const double exp_z_Na = exp(z_Na * VFoverRT);
+  const double exp_z_K = exp(z_K * VFoverRT);
+  const double gamma_Cai = 1.0, gamma_Cao = 0.341, gamma_Nai = 0.75, gamma_Nao = 0.75, gamma_Ki = 0.75,
+               gamma_Ko = 0.75;
+  const double Psi_Ca =
+      z_Ca * z_Ca * VFFoverRT * (gamma_Cai * Ca_ss * exp_z_Ca - gamma_Cao * P_(Ca_o)) / (exp_z_Ca - 1.0);
+  const double Psi_CaNa =
+      z_Na * z_Na * VFFoverRT * (gamma_Nai * Na_ss * exp_z_Na - gamma_Nao * P_(Na_o)) / (exp_z_Na - 1.0);
+  const double Psi_CaK = z_K * z_K * VFFoverRT * (gamma_Ki * K_ss * exp_z_K - gamma_Ko * P_(K_o)) / (exp_z_K - 1.0);
+  const double I_CaL_b = P_(P_Ca) * Psi_Ca;
+  const double I_CaNa_b = P_(P_CaNa) * Psi_CaNa;
+  const double I_CaK_b = P_(P_CaK) * Psi_CaK;
+  const double I_CaL_CaMK = P_(P_Ca_CaMK) * Psi_Ca;
+  const double I_CaNa_CaMK = P_(P_CaNa_CaMK) * Psi_CaNa;
+  const double I_CaK_CaMK = P_(P_CaK_CaMK) * Psi_CaK;
+  const double d = b[OB_d], phi = phi_INa_CaMK;
+  const double I_CaL = I_CaL_b * d * (1.0 - phi) * (f * (1.0 - n) + f_Ca * n * j_Ca) +
+                       I_CaL_CaMK * d * phi * (f_CaMK * (1.0 - n) + f_Ca_CaMK * n * j_Ca);
+  const double I_CaNa = I_CaNa_b * d * (1.0 - phi) * (f * (1.0 - n) + f_Ca * n * j_Ca) +
+                        I_CaNa_CaMK * d * phi * (f_CaMK * (1.0 - n) + f_Ca_CaMK * n * j_Ca);
+  const double I_CaK = I_CaK_b * d * (1.0 - phi) * (f * (1.0 - n) + f_Ca * n * j_Ca) +
+                       I_CaK_CaMK * d * phi * (f_CaMK * (1.0 - n) + f_Ca_CaMK * n * j_Ca);
+
+  /* I_Kr (331-344) */
+  const double x_r_inf = 1.0 / (1.0 + exp((-(V_m + 8.337)) / 6.789));
+  const double tau_x_r_fast =
+      12.98 + 1.0 / (0.3652 * exp((V_m - 31.66) / 3.869) + 4.123e-05 * exp((-(V_m - 47.78)) / 20.38));
+  const double tau_x_r_slow =
+      1.865 + 1.0 / (0.06629 * exp((V_m - 34.7) / 7.355) + 1.128e-05 * exp((-(V_m - 29.74)) / 25.94));
+  const double A_x_r_fast = 1.0 / (1.0 + exp((V_m + 54.81) / 38.21));
+  const double A_x_r_slow = 1.0 - A_x_r_fast;
+  b[OB_x_r_fast] = ord_gate(x_r_inf, b[OB_x_r_fast], tinc, tau_x_r_fast);
+  b[OB_x_r_slow] = ord_gate(x_r_inf, b[OB_x_r_slow], tinc, tau_x_r_slow);
+  const double x_r = A_x_r_fast * b[OB_x_r_fast] + A_x_r_slow * b[OB_x_r_slow];
+  const double R_Kr = 1.0 / ((1.0 + exp((V_m + 55.0) / 75.0)) * (1.0 + exp((V_m - 10.0) / 30.0)));
+  const double G_Kr = 0.046;
+  const double I_Kr = P_(IKr_Multiplier) * G_Kr * sqrt(P_(K_o) / 5.4) * x_r * (V_m - E_K) * R_Kr;
+
+  /* I_Ks (346-355) */
+  const double x_s1_inf = 1.0 / (1.0 + exp(-(V_m + 11.6) / 8.932));
+  const double tau_x_s1 = 817.3 + 1.0 / (2.326e-04 * exp((V_m + 48.28) / 17.80) + 0.001292 * exp(-(V_m + 210.0) / 230.0));
+  b[OB_x_s1] = ord_gate(x_s1_inf, b[OB_x_s1], tinc, tau_x_s1);
+  const double tau_x_s2 = 1.0 / (0.01 * exp((V_m - 50.0) / 20.0) + 0.0193 * exp(-(V_m + 66.54) / 31.0));
+  b[OB_x_s2] = ord_gate(x_s1_inf, b[OB_x_s2], tinc, tau_x_s2);
+  const double G_Ks = 0.0034;
+  const double I_Ks = P_(IKs_Multiplier) * G_Ks * (1.0 + 0.6 / (1.0 + pow((3.8e-05 / Ca_i), 1.4))) * b[OB_x_s1] *
+                      b[OB_x_s2] * (V_m - E_Ks);
+
+  /* I_K1 (357-367) */
+  const double x_K1_inf = 1.0 / (1.0 + exp(-(V_m + 2.5538 * P_(K_o) + 144.59) / (1.5692 * P_(K_o) + 3.8115)));
+  const double tau_x_K1 = 122.2 / (exp(-(V_m + 127.2) / 20.36) + exp((V_m + 236.8) / 69.33));
+  b[OB_x_K1] = ord_gate(x_K1_inf, b[OB_x_K1], tinc, tau_x_K1);
+  const double R_K1 = 1.0 / (1.0 + exp((V_m + 105.8 - 2.6 * P_(K_o)) / 9.493));
+  const double G_K1 = 0.1908;
+  const double I_K1 = P_(IK1_Multiplier) * P_(HF_Gomez_5) * G_K1 * sqrt(P_(K_o)) * b[OB_x_K1] * (V_m - E_K) * R_K1;
+
+  /* I_NaCa_i (369-413) */
+  const double kna3 = 88.12, wna = 6.0e4, wca = 6.0e4, wnaca = 5.0e3, qna = 0.5224, qca = 0.1670;
+  const double h_Ca = exp(qca * VFoverRT);
+  const double h_Na = exp(qna * VFoverRT);
+  const double h_1_i = 1.0 + (Na_i * (1.0 + h_Na)) / kna3;
+  const double h_2_i = (Na_i * h_Na) / (kna3 * h_1_i);
+  const double h_3_i = 1.0 / h_1_i;
+  const double h_4_i = 1.0 + (Na_i * (1.0 + Na_i / P_(k_Na2))) / P_(k_Na1);
+  const double h_5_i = (Na_i * Na_i) / (h_4_i * P_(k_Na1) * P_(k_Na2));
+  const double h_6_i = 1.0 / h_4_i;
+  const double h_7 = 1.0 + (P_(Na_o) * (1.0 + 1.0 / h_Na)) / kna3;
+  const double h_8 = P_(Na_o) / (kna3 * h_Na * h_7);
+  const double h_9 = 1.0 / h_7;
+  const double k_3_d = h_9 * wca;
+  const double k_3_dd = h_8 * wnaca;
+  const double k_3 = k_3_d + k_3_dd;
+  const double k_4_d_i = (h_3_i * wca) / h_Ca;
+  const double k_4_dd_i = h_2_i * wnaca;
+  const double k_4_i = k_4_d_i + k_4_dd_i;
+  const double k_6_i = h_6_i * Ca_i * P_(k_Ca_on);
+  const double k_7_i = h_5_i * h_2_i * wna;
+  const double k_8 = h_8 * P_(h_11) * wna;
+  const double k_1 = P_(k_1), k_2 = P_(k_2), k_5 = P_(k_5);
+  const double x_1_i = k_2 * k_4_i * (k_7_i + k_6_i) + k_5 * k_7_i * (k_2 + k_3);
+  const double x_2_i = k_1 * k_7_i * (k_4_i + k_5) + k_4_i * k_6_i * (k_1 + k_8);
+  const double x_3_i = k_1 * k_3 * (k_7_i + k_6_i) + k_8 * k_6_i * (k_2 + k_3);
+  const double x_4_i = k_2 * k_8 * (k_4_i + k_5) + k_3 * k_5 * (k_1 + k_8);
+  const double E_1_i = x_1_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_2_i = x_2_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_3_i = x_3_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_4_i = x_4_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double KmCaAct = 150.0e-6;
+  const double allo_i = 1.0 / (1.0 + (KmCaAct / Ca_i) * (KmCaAct / Ca_i));
+  const double J_NaCa_Na_i = 3.0 * (E_4_i * k_7_i - E_1_i * k_8) + E_3_i * k_4_dd_i - E_2_i * k_3_dd;
+  const double J_NaCa_Ca_i = E_2_i * k_2 - E_1_i * k_1;
+  const double G_NaCa = 0.0008;
+  const double I_NaCa_i = P_(INaCa_Multiplier) * P_(HF_Gomez_6) * G_NaCa * 0.8 * allo_i *
+                          (z_Na * J_NaCa_Na_i + z_Ca * J_NaCa_Ca_i);
+
+  /* I_NaCa_ss (415-443) */
+  const double h_1_ss = 1.0 + (Na_ss * (1.0 + h_Na)) / kna3;
+  const double h_2_ss = (Na_ss * h_Na) / (kna3 * h_1_ss);
+  const double h_3_ss = 1.0 / h_1_ss;
+  const double h_4_ss = 1.0 + (Na_ss * (1.0 + Na_ss / P_(k_Na2))) / P_(k_Na1);
+  const double h_5_ss = (Na_ss * Na_ss) / (h_4_ss * P_(k_Na1) * P_(k_Na2));
+  const double h_6_ss = 1.0 / h_4_ss;
+  const double k_4_d_ss = (h_3_ss * wca) / h_Ca;
+  const double k_4_dd_ss = h_2_ss * wnaca;
+  const double k_4_ss = k_4_d_ss + k_4_dd_ss;
+  const double k_6_ss = h_6_ss * Ca_ss * P_(k_Ca_on);
+  const double k_7_ss = h_5_ss * h_2_ss * wna;
+  const double x_1_ss = k_2 * k_4_ss * (k_7_ss + k_6_ss) + k_5 * k_7_ss * (k_2 + k_3);
+  const double x_2_ss = k_1 * k_7_ss * (k_4_ss + k_5) + k_4_ss * k_6_ss * (k_1 + k_8);
+  const double x_3_ss = k_1 * k_3 * (k_7_ss + k_6_ss) + k_8 * k_6_ss * (k_2 + k_3);
+  const double x_4_ss = k_2 * k_8 * (k_4_ss + k_5) + k_3 * k_5 * (k_1 + k_8);
+  const double E_1_ss = x_1_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_2_ss = x_2_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_3_ss = x_3_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_4_ss = x_4_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double allo_ss = 1.0 / (1.0 + (KmCaAct / Ca_ss) * (KmCaAct / Ca_ss));
+  const double J_NaCa_Na_ss = 3.0 * (E_4_ss * k_7_ss - E_1_ss * k_8) + E_3_ss * k_4_dd_ss - E_2_ss * k_3_dd;
+  const double J_NaCa_Ca_ss = E_2_ss * k_2 - E_1_ss * k_1;
+  const double I_NaCa_ss = P_(INaCa_Multiplier) * P_(HF_Gomez_6) * G_NaCa * 0.2 * allo_ss *
+                           (z_Na * J_NaCa_Na_ss + z_Ca * J_NaCa_Ca_ss);
+
+  /* I_NaK (445-498) */
+  const double k1p = 949.5, k2m = 39.4, k3p = 1899.0, k3m = 79300.0, k4m = 40.0, Knai0 = 9.073, Knao0 = 27.78,
+               delta = -0.1550;
+  const double K_Nai = Knai0 * exp(delta * VFoverRT * 1 / 3);
+  const double K_Nao = Knao0 * exp((1.0 - delta) * VFoverRT * 1 / 3);
+  const double Kki = 0.5, Kko = 0.3582, H = 1.0e-7, eP = 4.2, Khp = 1.698e-7, Knap = 224.0, Kxkur = 292.0;
+  const double Pnak = eP / (1.0 + H / Khp + Na_i / Knap + K_i / Kxkur);
+  const double alpha_1 = (k1p * pow((Na_i / K_Nai), 3.0)) /
+                         (pow((1.0 + Na_i / K_Nai), 3.0) + pow((1.0 + K_i / Kki), 2.0) - 1.0);
+  const double beta_2 = (k2m * pow((P_(Na_o) / K_Nao), 3.0)) /
+                        (pow((1.0 + P_(Na_o) / K_Nao), 3.0) + pow((1.0 + P_(K_o) / Kko), 2.0) - 1.0);
+  const double alpha_3 = (k3p * pow((P_(K_o) / Kko), 2.0)) /
+                         (pow((1.0 + P_(Na_o) / K_Nao), 3.0) + pow((1.0 + P_(K_o) / Kko), 2.0) - 1.0);
+  const double beta_3 = (k3m * Pnak * H) / (1.0 + P_(MgATP));
+  const double beta_4 = (k4m * pow((K_i / Kki), 2.0)) /
+                        (pow((1.0 + Na_i / K_Nai), 3.0) + pow((1.0 + K_i / Kki), 2.0) - 1.0);
+  const double al2 = P_(alpha_2), al4 = P_(alpha_4), be1 = P_(beta_1);
+  const double x_1 = al4 * alpha_1 * al2 + beta_2 * beta_4 * beta_3 + al2 * beta_4 * beta_3 + beta_3 * alpha_1 * al2;
+  const double x_2 = beta_2 * be1 * beta_4 + alpha_1 * al2 * alpha_3 + alpha_3 * be1 * beta_4 + al2 * alpha_3 * beta_4;
+  const double x_3 = al2 * alpha_3 * al4 + beta_3 * beta_2 * be1 + beta_2 * be1 * al4 + alpha_3 * al4 * be1;
+  const double x_4 = beta_4 * beta_3 * beta_2 + alpha_3 * al4 * alpha_1 + beta_2 * al4 * alpha_1 + beta_3 * beta_2 * alpha_1;
+  const double E_1 = x_1 / (x_1 + x_2 + x_3 + x_4);
+  const double E_2 = x_2 / (x_1 + x_2 + x_3 + x_4);
+  const double E_3 = x_3 / (x_1 + x_2 + x_3 + x_4);
+  const double E_4 = x_4 / (x_1 + x_2 + x_3 + x_4);
+  const double J_NaK_Na = 3.0 * (E_1 * alpha_3 - E_2 * beta_3);
+  const double J_NaK_K = 2.0 * (E_4 * be1 - E_3 * alpha_1);
+  const double P_NaK = 30.0;
+  const double I_NaK = P_(INaK_Multiplier) * P_(HF_Gomez_7) * P_NaK * (z_Na * J_NaK_Na + z_K * J_NaK_K);
+
+  /* background currents, I_pCa (500-517) */
+  const double x_Kb = 1.0 / (1.0 + exp(-(V_m - 14.48) / (18.34)));
+  const double G_Kb = 0.003;
+  const double I_Kb = P_(IKb_Multiplier) * G_Kb * x_Kb * (V_m - E_K);
+  const double P_Nab = 3.75e-10;
+  const double I_Nab =
+      P_(INab_Multiplier) * P_Nab * z_Na * z_Na * VFFoverRT * ((Na_i * exp_z_Na - P_(Na_o)) / (exp_z_Na - 1.0));
+  const double P_Cab = 2.5e-8;
+  const double I_Cab = P_(ICab_Multiplier) * P_Cab * z_Ca * z_Ca * VFFoverRT *
+                       ((gamma_Cai * Ca_i * exp_z_Ca - gamma_Cao * P_(Ca_o)) / (exp_z_Ca - 1.0));
+  const double G_pCa = 0.0005;
+  const double I_pCa = P_(IpCa_Multiplier) * G_pCa * (Ca_i / (0.0005 + Ca_i));
+
+  /* stretch-activated current (519-523) */
+  double I_SAC = P_(G_sac) * (V_m - P_(E_sac)) / (1. + P_(K_sac) * exp(-P_(alpha) * (stretch - 1.)));
+  I_SAC *= P_(ISAC_SWITCH);
+
+  /* total current (525-533) */
+  const double cur_I_tot = I_Na_fast + I_Na_late + I_to + I_CaL + I_CaNa + I_CaK + I_Kr + I_Ks + I_K1 + I_NaCa_i +
+                           I_NaCa_ss + I_NaK + I_Nab + I_Cab + I_Kb + I_pCa + I_SAC + i_external;
+  const double I_tot = -cur_I_tot;
+
+  /* diffusion fluxes (535-541) */
+  const double J_diff_Na = (Na_ss - Na_i) / 2.0;
+  const double J_diff_Ca = (Ca_ss - Ca_i) / 0.2;
+  const double J_diff_K = (K_ss - K_i) / 2.0;
+
+  /* SR release (543-565); celltype 2 (M cells) scales the steady state by 1.7 */
+  double J_rel_NP_inf = (P_(alpha_rel) * (-I_CaL)) / (1.0 + pow((1.5 * P_(HF_Gomez_8) / Ca_jsr), 8.0));
+  double J_rel_CaMK_inf = (P_(alpha_rel_CaMK) * (-I_CaL)) / (1.0 + pow((1.5 * P_(HF_Gomez_8) / Ca_jsr), 8.0));
+  if (P_(celltype) == 2.0) {
+    J_rel_NP_inf *= 1.7;
+    J_rel_CaMK_inf *= 1.7;
+  }
+  const double tau_rel_NP_b = P_(beta_tau) / (1.0 + (0.0123 / Ca_jsr));
+  const double tau_rel_NP = tau_rel_NP_b < 0.001 ? 0.001 : tau_rel_NP_b;
+  b[OB_J_rel_NP] = ord_gate(J_rel_NP_inf, b[OB_J_rel_NP], tinc, tau_rel_NP);
+  const double tau_rel_CaMK_b = P_(beta_tau_CaMK) / (1.0 + (0.0123 / Ca_jsr));
+  const double tau_rel_CaMK = tau_rel_CaMK_b < 0.001 ? 0.001 : tau_rel_CaMK_b;
+  b[OB_J_rel_CaMK] = ord_gate(J_rel_CaMK_inf, b[OB_J_rel_CaMK], tinc, tau_rel_CaMK);
+  const double J_rel = (1.0 - phi) * b[OB_J_rel_NP] + phi * b[OB_J_rel_CaMK];
+
+  /* SERCA uptake and leak (567-588); celltype 1 (epicardial) scales uptake by 1.3 */
+  double J_up_NP = (0.004375 * Ca_i) / (0.00092 + Ca_i);
+  const double DJ_up_CaMK = 1.75, DK_m_PLB = 0.00017;
+  double J_up_CaMK = (1.0 + DJ_up_CaMK) * (0.004375 * Ca_i) / (0.00092 - DK_m_PLB + Ca_i);
+  if (P_(celltype) == 1.0) {
+    J_up_NP *= 1.3;
+    J_up_CaMK *= 1.3;
+  }
+  const double J_leak = P_(HF_Gomez_9) * (0.0039375 * Ca_nsr) / 15.0;
+  const double J_up = P_(HF_Gomez_0) * ((1.0 - phi) * J_up_NP + phi * J_up_CaMK - J_leak);
+  const double J_tr = (Ca_nsr - Ca_jsr) / 100.0;
+
+  /* concentrations (594-605) */
+  const double cur_Nai = I_Na_fast + I_Na_late + 3.0 * I_NaCa_i + 3.0 * I_NaK + I_Nab;
+  const double dNa_i = -(cur_Nai)*util_1 + J_diff_Na * util_2;
+  b[OB_Na_i] = Na_i + tinc * dNa_i;
+  const double dNa_ss = -(I_CaNa + 3.0 * I_NaCa_ss) * util_3 - J_diff_Na;
+  b[OB_Na_ss] = Na_ss + tinc * dNa_ss;
+  const double cur_Ki = I_to + I_Kr + I_Ks + I_K1 + I_Kb + i_external - 2.0 * I_NaK;
+  const double dK_i = -(cur_Ki)*util_1 + J_diff_K * util_2;
+  b[OB_K_i] = K_i + tinc * dK_i;
+  const double dK_ss = -(I_CaK * util_3) - J_diff_K;
+  b[OB_K_ss] = K_ss + tinc * dK_ss;
+
+  /* calcium buffering, troponin and the calcium compartments (607-660) */
+  double cmdnmax = 0.05;
+  if (P_(celltype) == 1) cmdnmax *= 1.3;
+  const double kmcmdn = 0.00238, trpnmax = 0.07, BSRmax = 0.047, KmBSR = 0.00087, BSLmax = 1.124, KmBSL = 0.0087,
+               csqnmax = 10.0, kmcsqn = 0.8;
+  const double Ca_T50 = (P_(Ca_T50) + P_(beta1) * (lambda_m - 1.0)) * P_(HFM_Multiplier);
+  const double Ca_TRPN = b[OB_Ca_TRPN];
+  const double dCaTRPN = P_(k_TRPN) * (pow(1000 * Ca_i / Ca_T50, P_(n_TRPN)) * (1. - Ca_TRPN) - Ca_TRPN);
+  b[OB_Ca_TRPN] = Ca_TRPN + tinc * dCaTRPN;
+  const double I_Trpn = trpnmax * dCaTRPN;
+  const double beta_Cai = 1.0 / (1.0 + ((cmdnmax * kmcmdn) / pow((kmcmdn + Ca_i), 2.0)));
+  const double cur_Cai = I_pCa + I_Cab - 2.0 * I_NaCa_i;
+  const double dCa_i =
+      beta_Cai * (-(cur_Cai)*0.5 * util_1 - J_up * (P_(v_nsr) / P_(v_myo)) + J_diff_Ca * util_2 - I_Trpn);
+  b[OB_Ca_i] = Ca_i + tinc * dCa_i;
+  const double beta_Cass =
+      1.0 / (1.0 + ((BSRmax * KmBSR) / pow((KmBSR + Ca_ss), 2.0)) + ((BSLmax * KmBSL) / pow((KmBSL + Ca_ss), 2.0)));
+  const double dCa_ss =
+      beta_Cass * (-(I_CaL - 2.0 * I_NaCa_ss) * 0.5 * util_3 + J_rel * (P_(v_jsr) / P_(v_ss)) - J_diff_Ca);
+  b[OB_Ca_ss] = Ca_ss + tinc * dCa_ss;
+  const double dCa_nsr = J_up - (J_tr * (P_(v_jsr) / P_(v_nsr)));
+  b[OB_Ca_nsr] = Ca_nsr + tinc * dCa_nsr;
+  const double beta_Cajsr = 1.0 / (1.0 + ((csqnmax * kmcsqn) / pow((kmcsqn + Ca_jsr), 2.0)));
+  const double dCa_jsr = beta_Cajsr * (J_tr - J_rel);
+  b[OB_Ca_jsr] = Ca_jsr + tinc * dCa_jsr;
+
+  /* the currents the reference keeps in its block (OHaraRudy.h:48-52) */
+  b[OB_I_Na_fast] = I_Na_fast; b[OB_I_Na_late] = I_Na_late; b[OB_I_to] = I_to; b[OB_I_CaL] = I_CaL;
+  b[OB_I_CaNa] = I_CaNa; b[OB_I_CaK] = I_CaK; b[OB_I_Kr] = I_Kr; b[OB_I_Ks] = I_Ks; b[OB_I_K1] = I_K1;
+  b[OB_I_NaCa_i] = I_NaCa_i; b[OB_I_NaCa_ss] = I_NaCa_ss; b[OB_I_NaK] = I_NaK; b[OB_I_Nab] = I_Nab;
+  b[OB_I_Cab] = I_Cab; b[OB_I_Kb] = I_Kb; b[OB_I_pCa] = I_pCa; b[OB_I_SAC] = I_SAC;
+  return 0.001 * tinc * I_tot;
+}
+#undef P_
+
 /* ---------------------------------------------------------------- public entry points */
 static void derive(int model, double *P) {
   if (model == CMO_TT2) tt2_derive(P);
-  else crn_derive(P);
+  else if (model == CMO_CRN) crn_derive(P);
+  else ord_derive(P);
 }
 
 int cmo_build_tables(int model, const double *P_in, double dt, double *tables) {
@@ -592,25 +1109,29 @@ int cmo_build_tables(int model, const double *P_in, double dt, double *tables) {
   double *P = (double *)malloc(np * sizeof(double));
   memcpy(P, P_in, np * sizeof(double));
   derive(model, P);
-  memset(tables, 0, (size_t)cmo_n_tables(model) * CMO_RTDT * sizeof(double));
+  if (cmo_n_tables(model) > 0) memset(tables, 0, (size_t)cmo_n_tables(model) * CMO_RTDT * sizeof(double));
   if (model == CMO_TT2) tt2_tables(P, dt, tables);
-  else crn_tables(P, dt, tables);
+  else if (model == CMO_CRN) crn_tables(P, dt, tables);
   free(P);
   return 0;
 }
 
 void cmo_init_state(int model, const double *P, double *block) {
   if (model == CMO_TT2) tt2_init(P, block);
-  else crn_init(P, block);
+  else if (model == CMO_CRN) crn_init(P, block);
+  else ord_init(P, block);
 }
 
-double cmo_init_vm(int model, const double *P) { return model == CMO_TT2 ? P[T_init_V_m] : P[C_Init_Vm]; }
+double cmo_init_vm(int model, const double *P) {
+  return model == CMO_TT2 ? P[T_init_V_m] : (model == CMO_CRN ? P[C_Init_Vm] : P[O_Init_Vm]);
+}
 
 double cmo_calc(int model, const double *P_in, const double *tables, double *block, double dt, double V,
                 double i_ext, double stretch) {
   /* P_in holds base and derived values (the caller derives once via cmo_derive). */
   if (model == CMO_TT2) return tt2_calc(P_in, tables, block, dt, V, i_ext);
-  return crn_calc(P_in, tables, block, dt, V, i_ext, stretch);
+  if (model == CMO_CRN) return crn_calc(P_in, tables, block, dt, V, i_ext, stretch);
+  return ord_calc(P_in, block, dt, V, i_ext, stretch);
 }
 
 /* Fills the derived slots of P in place (Calculate()). */
@@ -653,7 +1174,8 @@ static void *run_range(void *argp) {
         if (t >= tb + a->textlen) tb += a->bcl;
       }
       if (a->model == CMO_TT2) v += tt2_calc(Pc, a->tables, blk, a->dt, v, i_ext);
-      else v += crn_calc(Pc, a->tables, blk, a->dt, v, i_ext, 1.0);
+      else if (a->model == CMO_CRN) v += crn_calc(Pc, a->tables, blk, a->dt, v, i_ext, 1.0);
+      else v += ord_calc(Pc, blk, a->dt, v, i_ext, 1.0);
       t += a->dt;
     }
     if (isnan(v)) a->bad = 1;

@@ -1,11 +1,14 @@
 /* Test infrastructure only (the oracle): a plain-C, FP64 restatement of the reference
- * cell-model update for ten Tusscher-Panfilov 2006 and Courtemanche 1998, used by the
+ * cell-model update for ten Tusscher-Panfilov 2006, Courtemanche 1998 and O'Hara-Rudy 2011
+ * (the reference's variant: Passini/Dutta I_Na gates, troponin, SAC), used by the
  * tests as the checker and by bench.py as the timed CPU baseline. The product never
  * links or calls it.
  *
  * State blocks use the reference's backup layout (GetBase()/GetSize()):
  *   TT2 (36 doubles, TenTusscher2.h:77-123):  Ca_i CaSR CaSS Na_i K_i Array[18] m h j xr1 xr2 xs r s d f f2 fCa Rq
  *   CRN (22 doubles, CourtemancheEtAl.h:32-42): Ca_i Ca_up Ca_rel h j oi ui Xr Xs u v w Na_i K_i m oa ua d f f_Ca I_SAC Ca_TRPN
+ *   ORd (59 doubles, OHaraRudy.h:31-52): 42 states from m to Ca_TRPN (h_CaMK_fast unused), then
+ *        I_Na_fast I_Na_late I_to I_CaL I_CaNa I_CaK I_Kr I_Ks I_K1 I_NaCa_i I_NaCa_ss I_NaK I_Nab I_Cab I_Kb I_pCa I_SAC
  *
  * Parameter vectors P are indexed by this file's own parameter lists (names as in the
  * reference .ev files); derived quantities are recomputed here (restating
@@ -18,7 +21,7 @@
 extern "C" {
 #endif
 
-enum { CMO_TT2 = 0, CMO_CRN = 1 };
+enum { CMO_TT2 = 0, CMO_CRN = 1, CMO_ORD = 2 };
 enum { CMO_RTDT = 4000 };
 
 int cmo_n_params(int model);

@@ -1,16 +1,19 @@
 """Generate the golden vectors in this folder by running the reference's own CellModel
 library (compiled from the reference sources by oracle/Makefile, target `ref`).
 
-    python tests/golden/make_golden.py            # needs the reference tree (CM_REFERENCE_TREE)
+    python tests/golden/make_golden.py [tt2] [crn] [ord]   # needs the reference tree (CM_REFERENCE_TREE)
 
 Outputs (all seeded, deterministic):
   params_tt2_epi.json / params_crn.json  resolved parameter sets after Init + Calculate
                                          (TenTusscher2_original_Epi.ev, CourtemancheEtAl.ev)
+  params_ord_<v>.json                    O'Hara-Rudy, v = endo / epi / mid (OHaraRudy_<v>.ev)
   tables_<m>.npz    sha256 of every lookup table's bytes + every 50th row, dt = 1e-5 s
+                    (TT2 and CRN; O'Hara-Rudy has none)
   step_<m>.npz      one-Calc known answers: states sampled along paced trajectories,
-                    table-edge voltages, with and without stimulus
+                    table-edge voltages, with and without stimulus (O'Hara-Rudy: one
+                    file per cell type, step_ord_<v>.npz)
   trace_<m>.npz     multi-beat driver runs of jittered cells: Vm every 100 steps and the
-                    final state blocks
+                    final state blocks (O'Hara-Rudy: trace_ord_<v>.npz)
 """
 from __future__ import annotations
 
@@ -31,29 +34,38 @@ OUT = Path(__file__).resolve().parent
 DT = 1e-5
 
 
-def tag(model):
+def tag(model, variant=None):
+    if model == O.ORD:
+        return f"ord_{variant}"
     return "tt2" if model == O.TT2 else "crn"
 
 
 def hetero_names(model):
-    return W.TT2_HETERO if model == O.TT2 else W.CRN_HETERO
+    return {O.TT2: W.TT2_HETERO, O.CRN: W.CRN_HETERO, O.ORD: W.ORD_HETERO}[model]
 
 
 def amp(model):
-    return W.TT2_STIM_NA if model == O.TT2 else W.CRN_STIM_PAPF
+    return {O.TT2: W.TT2_STIM_NA, O.CRN: W.CRN_STIM_PAPF, O.ORD: W.ORD_STIM}[model]
 
 
 def stim_len(model):
-    """1 ms for TT2 (the workloads); Courtemanche's own GetStimTime() = 2 ms (CourtemancheEtAl.h:54)."""
-    return 1e-3 if model == O.TT2 else 2e-3
+    """1 ms for TT2 (the workloads); Courtemanche's own GetStimTime() = 2 ms (CourtemancheEtAl.h:54);
+    O'Hara-Rudy's duration parameter, 1 ms."""
+    return 2e-3 if model == O.CRN else 1e-3
 
 
-def dump_params(ref, model):
-    cells = ref.create(model, DT, 1)
+def ev_of(model, variant):
+    return O.Ref.ev_path(model, variant) if variant else O.Ref.ev_path(model)
+
+
+def dump_params(ref, model, variant=None):
+    ev = ev_of(model, variant)
+    cells = ref.create(model, DT, 1, ev=ev)
     p = {k: v for k, v in cells.params().items() if k}
-    name = "params_tt2_epi.json" if model == O.TT2 else "params_crn.json"
+    name = f"params_{tag(model, variant)}.json" if model == O.ORD else (
+        "params_tt2_epi.json" if model == O.TT2 else "params_crn.json")
     meta = {"model": O.MODEL_NAMES[model],
-            "ev_file": Path(O.Ref.ev_path(model)).name,
+            "ev_file": Path(ev).name,
             "init_vm": cells.init_vm(),
             "generator": "tests/golden/make_golden.py"}
     with open(OUT / name, "w") as f:
@@ -77,10 +89,11 @@ def dump_tables(ref, port, model):
                         rows=np.array(rows), dt=DT)
 
 
-def dump_step(ref, model):
+def dump_step(ref, model, variant=None):
     """States along paced trajectories of 8 jittered cells, snapshotted every 25 ms."""
     n = 8
-    cells = ref.create(model, DT, n)
+    ev = ev_of(model, variant)
+    cells = ref.create(model, DT, n, ev=ev)
     hn = hetero_names(model)
     p = cells.params()
     sc = W.conductance_scales(7, n, len(hn), 0.8, 1.2)
@@ -94,6 +107,12 @@ def dump_step(ref, model):
         vms.append(vm.copy())
         cells.run(vm, 2500, DT, t0=t, textbegin=0.0, textlen=stim_len(model), bcl=1.0, amp=amp(model))
         t += 2500 * DT
+    if model == O.ORD:
+        # h_CaMK_fast (slot 4) is never initialised by the reference, and the stored currents
+        # (slots 42..58) are not set before the first Calc; neither is read by Calc
+        for s in states:
+            s[:, 4] = 0.0
+        states[0][:, 42:] = 0.0
     S = np.concatenate(states)
     V = np.concatenate(vms)
     het = np.tile(sc, (1, 40))
@@ -106,20 +125,20 @@ def dump_step(ref, model):
     rng = np.random.default_rng(11)
     iext = np.where(rng.random(m) < 0.3, amp(model), 0.0)
     # one Calc per row: one reference cell per row with its own hetero values
-    kat = ref.create(model, DT, m)
+    kat = ref.create(model, DT, m, ev=ev)
     for k, name in enumerate(hn):
         kat.add_hetero(name, p[name] * het[k])
     kat.set_state(S)
     dV = kat.calc(DT, V, iext)
     S1 = kat.get_state()
-    np.savez_compressed(OUT / f"step_{tag(model)}.npz", state_in=S, vm=V, i_ext=iext, hetero_names=np.array(hn),
+    np.savez_compressed(OUT / f"step_{tag(model, variant)}.npz", state_in=S, vm=V, i_ext=iext, hetero_names=np.array(hn),
                         hetero_scale=het, state_out=S1, dvm=dV, dt=DT)
 
 
-def dump_trace(ref, model):
+def dump_trace(ref, model, variant=None):
     """4 jittered cells, BCL 500 ms, 2 beats, reference driver loop; Vm every 100 steps."""
     n, steps = 4, 100000
-    cells = ref.create(model, DT, n)
+    cells = ref.create(model, DT, n, ev=ev_of(model, variant))
     hn = hetero_names(model)
     p = cells.params()
     sc = W.conductance_scales(1, n, len(hn), 0.95, 1.05)
@@ -127,21 +146,29 @@ def dump_trace(ref, model):
         cells.add_hetero(name, p[name] * sc[k])
     vm = np.full(n, cells.init_vm())
     tr = cells.run(vm, steps, DT, textbegin=0.0, textlen=stim_len(model), bcl=0.5, amp=amp(model), rec_every=100)
-    np.savez_compressed(OUT / f"trace_{tag(model)}.npz", hetero_names=np.array(hn), hetero_scale=sc,
+    np.savez_compressed(OUT / f"trace_{tag(model, variant)}.npz", hetero_names=np.array(hn), hetero_scale=sc,
                         n_steps=steps, dt=DT, bcl=0.5, textlen=stim_len(model), amp=amp(model), rec_every=100,
                         trace=tr, final_state=cells.get_state(), final_vm=vm)
 
 
-def main():
+def main(which):
     ref = O.Ref()
     port = O.Port()
     for model in (O.TT2, O.CRN):
+        if tag(model) not in which:
+            continue
         dump_params(ref, model)
         dump_tables(ref, port, model)
         dump_step(ref, model)
         dump_trace(ref, model)
         print("wrote golden vectors for", O.MODEL_NAMES[model])
+    if "ord" in which:
+        for v in O.ORD_VARIANTS:
+            dump_params(ref, O.ORD, v)
+            dump_step(ref, O.ORD, v)
+            dump_trace(ref, O.ORD, v)
+            print("wrote golden vectors for", O.MODEL_NAMES[O.ORD], v)
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]) or {"tt2", "crn", "ord"})
