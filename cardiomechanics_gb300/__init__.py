@@ -27,6 +27,7 @@ LIB_PATH = _PKG / "_lib" / "libcmgb300.so"
 
 TENTUSSCHER2 = 5
 COURTEMANCHE = 2
+OHARARUDY = 12
 FP64, MIXED = 0, 1
 LAYOUT_REF_BLOCK, LAYOUT_SOA = 0, 1
 AUDIT_NAN, AUDIT_VRANGE, AUDIT_CARANGE, AUDIT_GATE, AUDIT_SURROGATE, AUDIT_VMRANGE = 1, 2, 4, 8, 16, 32
@@ -376,7 +377,7 @@ class Batch:
 
 
 class Multi:
-    """Batched form: several MIXED batches (any sizes, both models) advanced in lock step by one
+    """Batched form: several MIXED batches (any sizes; TenTusscher2 and Courtemanche) advanced in lock step by one
     persistent launch per time step, replayed from a CUDA graph."""
 
     def __init__(self, batches, stream=None):

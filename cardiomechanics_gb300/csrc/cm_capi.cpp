@@ -26,7 +26,9 @@ int64_t round_ld(int64_t n) { return ((n + 255) / 256) * 256; }  // whole staged
 // SOA index (model order) -> plane of the mixed layout; `pair` variables are compensated
 // accumulators stored as hi (plane slot) and lo (plane slot + 1).
 void mixed_slot(int model, int k, bool &pair, int &slot) {
-  if (model == kTenTusscher2) {
+  if (model == kOHaraRudy) {
+    slot = ord_mixed_plane(k, pair);
+  } else if (model == kTenTusscher2) {
     // SOA: Ca_i CaSR CaSS Na_i K_i m h j xr1 xr2 xs r s d f f2 fCa Rq
     static const int map[] = {13, 15, 14, 17, 19, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
     slot = map[k];
@@ -39,9 +41,11 @@ void mixed_slot(int model, int k, bool &pair, int &slot) {
   }
 }
 
-// Reference backup block index of SOA variable k (TenTusscher2.h:77-123, CourtemancheEtAl.h:32-42).
+// Reference backup block index of SOA variable k (TenTusscher2.h:77-123, CourtemancheEtAl.h:32-42,
+// OHaraRudy.h:31-43: slot 4 is h_CaMK_fast, which the SOA layout leaves out).
 int ref_block_index(int model, int k) {
   if (model == kTenTusscher2) return k < 5 ? k : k + 18;
+  if (model == kOHaraRudy) return k < 4 ? k : k + 1;
   return k < 20 ? k : 21;
 }
 
@@ -81,9 +85,9 @@ int upload_tables(cm_batch_s *b) {
     std::vector<double> rows, eca;
     b->ps.rows_fp64(rows, eca);
     size_t nb = (rows.size() + eca.size()) * sizeof(double);
-    CK(cudaMalloc(&b->table_mem, nb));
+    CK(cudaMalloc(&b->table_mem, std::max<size_t>(nb, 16)));
     double *dst = (double *)b->table_mem;
-    CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!rows.empty()) CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (!eca.empty()) CK(cudaMemcpy(dst + rows.size(), eca.data(), eca.size() * sizeof(double), cudaMemcpyHostToDevice));
     b->d.rows64 = dst;
     b->d.eca64 = eca.empty() ? nullptr : dst + rows.size();
@@ -91,17 +95,23 @@ int upload_tables(cm_batch_s *b) {
     std::vector<float> rows, eca;
     b->ps.rows_fp32(rows, eca);
     size_t nb = (rows.size() + eca.size()) * sizeof(float);
-    CK(cudaMalloc(&b->table_mem, nb));
+    CK(cudaMalloc(&b->table_mem, std::max<size_t>(nb, 16)));
     float *dst = (float *)b->table_mem;
-    CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (!rows.empty()) CK(cudaMemcpy(dst, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (!eca.empty()) CK(cudaMemcpy(dst + rows.size(), eca.data(), eca.size() * sizeof(float), cudaMemcpyHostToDevice));
     b->d.rows32 = dst;
     b->d.eca32 = eca.empty() ? nullptr : dst + rows.size();
   }
   if (b->ps.spec->model == kTenTusscher2) b->ps.tt2_consts(b->d.tt2_64, b->d.tt2_32);
+  else if (b->ps.spec->model == kOHaraRudy) b->ps.ord_consts(b->d.ord_64, b->d.ord_32);
   else b->ps.crn_consts(b->d.crn_64, b->d.crn_32);
   return CM_OK;
 }
+
+// Diagnostic values an FP64 batch can record per cell, and where they sit in the reference
+// block: TT2 Array[0..16], CRN I_SAC, ORd its 17 stored currents.
+int diag_count(int model) { return model == kCourtemanche ? 1 : 17; }
+int diag_block_base(int model) { return model == kTenTusscher2 ? 5 : (model == kOHaraRudy ? 42 : 20); }
 
 // Host SOA (n_state x n, model order) <-> device layout.
 int soa_to_device(cm_batch_s *b, const std::vector<double> &soa) {
@@ -339,7 +349,7 @@ int cm_batch_reset(cm_batch_t b) {
   CK(cudaMemsetAsync(b->audit_cell, 0, std::max<int64_t>(1, n) * sizeof(uint32_t), b->stream));
   CK(cudaMemsetAsync(b->audit_or, 0, sizeof(unsigned int), b->stream));
   if (b->diag) {
-    const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+    const int nd = diag_count(b->d.model);
     CK(cudaMemsetAsync(b->diag, 0, (size_t)nd * b->d.ld * sizeof(double), b->stream));
   }
   CK(cudaStreamSynchronize(b->stream));
@@ -350,7 +360,7 @@ int cm_batch_set_diagnostics(cm_batch_t b, int on) {
   if (!b) return fail(CM_ERR_ARG, "NULL batch");
   if (on && b->d.precision != CM_PREC_FP64) return fail(CM_ERR_UNSUPPORTED, "diagnostic currents need an FP64 batch");
   if (on && !b->diag) {
-    const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+    const int nd = diag_count(b->d.model);
     CK(cudaMalloc(&b->diag, (size_t)nd * b->d.ld * sizeof(double)));
     CK(cudaMemset(b->diag, 0, (size_t)nd * b->d.ld * sizeof(double)));
   }
@@ -419,11 +429,11 @@ int cm_batch_get_state(cm_batch_t b, int layout, double *buf) {
       for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + pos] = soa[(size_t)k * n + c];
     }
     if (b->diag) {  // diagnostic slots: TT2 Array[0..16], CRN I_SAC
-      const int nd = b->d.model == kTenTusscher2 ? 17 : 1;
+      const int nd = diag_count(b->d.model);
       std::vector<double> dg((size_t)nd * n);
       for (int k = 0; k < nd; k++)
         CK(cudaMemcpy(dg.data() + (size_t)k * n, b->diag + k * b->d.ld, n * sizeof(double), cudaMemcpyDeviceToHost));
-      const int base = b->d.model == kTenTusscher2 ? 5 : 20;
+      const int base = diag_block_base(b->d.model);
       for (int k = 0; k < nd; k++)
         for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + base + k] = dg[(size_t)k * n + c];
     }
@@ -862,6 +872,8 @@ int cm_multi_create(cm_multi_t *out, const cm_batch_t *batches, int n_batches, v
     if (!batches[i]) return fail(CM_ERR_ARG, "NULL batch");
     if (batches[i]->d.precision != CM_PREC_MIXED)
       return fail(CM_ERR_UNSUPPORTED, "the batched form runs CM_PREC_MIXED batches");
+    if (batches[i]->d.model == kOHaraRudy)
+      return fail(CM_ERR_UNSUPPORTED, "the batched form covers TenTusscher2 and CourtemancheEtAl batches");
     if (batches[i]->d.ld * 24 >= (int64_t)2147483647) return fail(CM_ERR_ARG, "instance too large for a multi");
   }
   auto *m = new (std::nothrow) cm_multi_s();

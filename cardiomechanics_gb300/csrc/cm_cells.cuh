@@ -5,6 +5,7 @@
 
 #include "cm_crn.cuh"
 #include "cm_launch.h"
+#include "cm_ord.cuh"
 #include "cm_tt2.cuh"
 
 namespace cm {
@@ -65,6 +66,55 @@ __device__ __forceinline__ float crn_mixed_cell(const DevBatch &b, I c, float V,
   s[12 * ld] = x.d; s[13 * ld] = x.f; s[14 * ld] = x.f_Ca; s[15 * ld] = x.Ca_i; s[16 * ld] = x.Ca_TRPN;
   s[17 * ld] = Ca_up.hi; s[18 * ld] = Ca_up.lo; s[19 * ld] = Ca_rel.hi; s[20 * ld] = Ca_rel.lo;
   s[21 * ld] = Na_i.hi; s[22 * ld] = Na_i.lo; s[23 * ld] = K_i.hi; s[24 * ld] = K_i.lo;
+  return dV;
+}
+
+template <typename I>
+__device__ __forceinline__ float ord_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch) {
+  const I ld = (I)b.ld;
+  const float *const *het = (const float *const *)b.het;
+  float *s = b.s32 + c;
+  float x[SO_N];
+  Acc acc[6];
+#pragma unroll
+  for (int k = 0; k < SO_N; k++) {
+    bool pair;
+    const int p = ord_mixed_plane(k, pair);
+    if (!pair) x[k] = s[p * ld];
+  }
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    acc[q].hi = s[(kORDPlain + 2 * q) * ld];
+    acc[q].lo = s[(kORDPlain + 2 * q + 1) * ld];
+    x[ord_pair_var(q)] = acc[q].hi;
+  }
+  const ORDConsts<float> &C = b.ord_32;
+  ORDHet_<float> g;
+  g.INaF = het[HO_INaF] ? __ldg(het[HO_INaF] + c) : C.INaF;
+  g.INaL = het[HO_INaL] ? __ldg(het[HO_INaL] + c) : C.INaL;
+  g.Ito = het[HO_Ito] ? __ldg(het[HO_Ito] + c) : C.Ito;
+  g.IKr = het[HO_IKr] ? __ldg(het[HO_IKr] + c) : C.IKr;
+  g.IKs = het[HO_IKs] ? __ldg(het[HO_IKs] + c) : C.IKs;
+  g.IK1 = het[HO_IK1] ? __ldg(het[HO_IK1] + c) : C.IK1;
+  ORDIncr<float> inc;
+  const float dV = ord_calc<float, false>(C, x, inc, g, V, iext, stretch, nullptr);
+  acc_add(acc[0], inc.Na_i);
+  acc_add(acc[1], inc.Na_ss);
+  acc_add(acc[2], inc.K_i);
+  acc_add(acc[3], inc.K_ss);
+  acc_add(acc[4], inc.Ca_nsr);
+  acc_add(acc[5], inc.Ca_jsr);
+#pragma unroll
+  for (int k = 0; k < SO_N; k++) {
+    bool pair;
+    const int p = ord_mixed_plane(k, pair);
+    if (!pair) s[p * ld] = x[k];
+  }
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    s[(kORDPlain + 2 * q) * ld] = acc[q].hi;
+    s[(kORDPlain + 2 * q + 1) * ld] = acc[q].lo;
+  }
   return dV;
 }
 

@@ -47,10 +47,42 @@ enum CRNState {
   SC_m, SC_oa, SC_ua, SC_d, SC_f, SC_fCa, SC_CaTRPN, SC_N
 };
 
+// O'Hara-Rudy: the reference block order (OHaraRudy.h:31-43) without h_CaMK_fast, which the
+// reference declares but never sets or reads.
+enum ORDState {
+  SO_m, SO_h_fast, SO_h_slow, SO_j, SO_h_CaMK_slow, SO_j_CaMK, SO_m_L, SO_h_L, SO_h_L_CaMK, SO_a, SO_i_fast,
+  SO_i_slow, SO_a_CaMK, SO_i_CaMK_fast, SO_i_CaMK_slow, SO_d, SO_f_fast, SO_f_slow, SO_f_Ca_fast, SO_f_Ca_slow,
+  SO_j_Ca, SO_n, SO_f_CaMK_fast, SO_f_Ca_CaMK_fast, SO_x_r_fast, SO_x_r_slow, SO_x_s1, SO_x_s2, SO_x_K1,
+  SO_Na_i, SO_Na_ss, SO_K_i, SO_K_ss, SO_Ca_i, SO_Ca_ss, SO_Ca_nsr, SO_Ca_jsr, SO_CaMK_trap, SO_J_rel_NP,
+  SO_J_rel_CaMK, SO_Ca_TRPN, SO_N
+};
+// The 17 currents the reference keeps after the states (OHaraRudy.h:48-52); the FP64
+// kernel writes them when diagnostics are on.
+constexpr int kORDCurrents = 17;
+
+// O'Hara-Rudy mixed form: planes 0..34 are the FP32 states (ORDState order, the six
+// compensated concentrations left out), planes 35..46 the (hi, lo) pairs of Na_i, Na_ss, K_i,
+// K_ss, Ca_nsr and Ca_jsr.
+constexpr int kORDPlain = 35;
+
+// ORDState variable of pair q (Na_i, Na_ss, K_i, K_ss, Ca_nsr, Ca_jsr).
+CM_HD int ord_pair_var(int q) { return q < 4 ? SO_Na_i + q : SO_Ca_nsr + (q - 4); }
+
+// Plane of ORDState variable k in the mixed layout (for a pair, its hi plane; lo follows).
+CM_HD int ord_mixed_plane(int k, bool &pair) {
+  pair = false;
+  if (k < SO_Na_i) return k;
+  if (k == SO_Ca_i || k == SO_Ca_ss) return k - 4;
+  if (k >= SO_CaMK_trap) return k - 6;
+  pair = true;
+  return k <= SO_K_ss ? kORDPlain + 2 * (k - SO_Na_i) : kORDPlain + 8 + 2 * (k - SO_Ca_nsr);
+}
+
 // Hetero (per-cell parameter) slots. Each slot either points at n_cells per-cell values
 // or is null (the parameter set's value applies).
 enum TT2Het { H2_g_Na, H2_g_Kr, H2_g_K1, H2_g_Ks, H2_g_to, H2_g_CaL, H2_N };
 enum CRNHet { HC_g_Na, HC_g_to, HC_g_Ks, HC_g_CaL, HC_g_bNa, HC_g_bCa, HC_N };
+enum ORDHet { HO_INaF, HO_INaL, HO_Ito, HO_IKr, HO_IKs, HO_IK1, HO_N };
 
 // Constants of TenTusscherEtAl2::Calc (TenTusscher2.cpp:615-906) prepared on the host.
 // Quantities the reference recomputes every call from parameters alone
@@ -76,6 +108,29 @@ struct CRNConsts {
       cmdnkm, kmcmdnm2, kkmcmdn, Vrel, Cmd2F, exp250, exp50;
   R dt_ms;  // tinc * 1000 (line 87)
   R logNao, logKo, logCao;  // mixed form
+};
+
+// Constants of OHaraRudy::Calc (OHaraRudy.cpp:105-663) prepared on the host: every value
+// that depends on parameters alone (F/RT, volume ratios, sqrt(K_o), the cell-type factors,
+// products of multipliers) is evaluated once in FP64. The heterogeneity slots' multipliers
+// (INaF, INaL, Ito, IKr, IKs, IK1) stay separate because they may be per cell.
+template <typename R>
+struct ORDConsts {
+  R dt_ms;                                      // tinc * 1000 (line 106)
+  R RToverF, FoRT, FFoRT, Na_o, K_o, Ca_o;      // F/(R T) and F^2/(R T)
+  R util_1, util_2, util_3, vnsr_vmyo, vjsr_vss, vjsr_vnsr;
+  R A_h_fast, A_h_slow, A_f_fast, A_f_slow, tau_h_L_mod, tau_h_L_CaMK;  // tau_h_L scaled by HF_Gomez_2
+  R INaF, INaL, Ito, IKr, IKs, IK1;  // the multipliers a cell may replace
+  R HF1, HF3, HF4, HF5, INaCa_HF6, INaK_HF7, IKb, INab, ICab, IpCa;
+  R P_Ca, P_CaNa, P_CaK, P_Ca_CaMK, P_CaNa_CaMK, P_CaK_CaMK;
+  R k_Na1, k_Na2, k_Ca_on, h_11, k_1, k_2, k_5, beta_1, alpha_2, alpha_4, MgATP1;  // MgATP1 = 1 + MgATP
+  R alpha_rel, alpha_rel_CaMK, beta_tau, beta_tau_CaMK, rel_scale, HF8x15;  // rel_scale 1.7 for M cells; 1.5 HF8
+  R up_scale, HF9, HF0, cmdnmax;                      // up_scale 1.3 epicardial; cmdnmax 0.05 (x1.3 epi)
+  R epi;                                              // 1 for celltype 1 (delta_epi applies), else 0
+  R sqrtKo54, sqrtKo, EKs_num, xK1_shift, xK1_slope, RK1_shift;  // K_o-only terms of I_Kr, I_Ks, I_K1
+  R G_sac, E_sac, K_sac, alpha_sac, ISAC_SWITCH;
+  R Ca_T50, beta1, HFM, k_TRPN, n_TRPN;
+  R logNao, logKo, logEKs_num;  // mixed form
 };
 
 // Voltage row index exactly as the reference computes it (TenTusscher2.cpp:618,

@@ -168,6 +168,62 @@ __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch
   }
 }
 
+template <bool kDiag>
+__global__ void __launch_bounds__(128) ord_fp64_kernel(const DevBatch b, const StepIO io) {
+  const int64_t ld = b.ld;
+  const double *const *het = (const double *const *)b.het;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    double *s = b.s64 + c;
+    double x[SO_N];
+#pragma unroll
+    for (int k = 0; k < SO_N; k++) x[k] = s[k * ld];
+    const ORDConsts<double> &C = b.ord_64;
+    ORDHet_<double> g;
+    g.INaF = het[HO_INaF] ? __ldg(het[HO_INaF] + c) : C.INaF;
+    g.INaL = het[HO_INaL] ? __ldg(het[HO_INaL] + c) : C.INaL;
+    g.Ito = het[HO_Ito] ? __ldg(het[HO_Ito] + c) : C.Ito;
+    g.IKr = het[HO_IKr] ? __ldg(het[HO_IKr] + c) : C.IKr;
+    g.IKs = het[HO_IKs] ? __ldg(het[HO_IKs] + c) : C.IKs;
+    g.IK1 = het[HO_IK1] ? __ldg(het[HO_IK1] + c) : C.IK1;
+    const double V = __ldg(io.vm + c);
+    const double iext = stim_for_cell(io, c);
+    const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
+    ORDIncr<double> inc;
+    double cur[kORDCurrents];
+    const double dV = ord_calc<double, kDiag>(C, x, inc, g, V, iext, stretch, cur);
+    // the reference's `X += tinc * dX` (OHaraRudy.cpp:597-659)
+    x[SO_Na_i] += inc.Na_i;
+    x[SO_Na_ss] += inc.Na_ss;
+    x[SO_K_i] += inc.K_i;
+    x[SO_K_ss] += inc.K_ss;
+    x[SO_Ca_nsr] += inc.Ca_nsr;
+    x[SO_Ca_jsr] += inc.Ca_jsr;
+#pragma unroll
+    for (int k = 0; k < SO_N; k++) s[k * ld] = x[k];
+    if (kDiag)
+#pragma unroll
+      for (int k = 0; k < kORDCurrents; k++) b.diag[k * ld + c] = cur[k];
+    finish(b, io, c, V, dV, 0u);
+  }
+}
+
+template <typename I, int kBlock, int kMinB>
+__global__ void __launch_bounds__(kBlock, kMinB) ord_mixed_kernel(const DevBatch b, const StepIO io) {
+  for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
+    const float iext = (float)stim_for_cell(io, c);
+    const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
+    if (io.vm_hi) {
+      Acc v{io.vm_hi[c], io.vm_lo[c]};
+      acc_add(v, ord_mixed_cell<I>(b, c, v.hi, iext, stretch));
+      finish_acc(b, c, v, 0u, io);
+    } else {
+      const double V = __ldg(io.vm + c);
+      const float dV = ord_mixed_cell<I>(b, c, (float)V, iext, stretch);
+      finish(b, io, c, V, (double)dV, 0u);
+    }
+  }
+}
+
 __global__ void probe_kernel(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
                              int64_t n_probe, double *out, int64_t stride, int64_t k) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -192,9 +248,9 @@ __global__ void vm_join_kernel(const float *hi, const float *lo, double *v, int6
 
 }  // namespace
 
-int n_fp32_vars(int model) { return model == 5 ? 21 : 25; }
+int n_fp32_vars(int model) { return model == 5 ? 21 : (model == 12 ? kORDPlain + 12 : 25); }
 int n_fp64_vars(int model, int precision) {
-  if (precision == 0) return model == 5 ? S2_N : SC_N;
+  if (precision == 0) return model == 5 ? S2_N : (model == 12 ? SO_N : SC_N);
   return 0;
 }
 
@@ -217,6 +273,7 @@ constexpr Shape kShapes[] = {{256, 2}, {128, 5}, {256, 3}, {512, 1}, {64, 10}};
 template <typename I, int B, int M>
 void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s) {
   if (b.model == 5) tt2_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
+  else if (b.model == 12) ord_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
   else crn_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
 }
 
@@ -240,7 +297,7 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
   if (b.n == 0) return cudaSuccess;
   const bool diag = b.diag != nullptr;
   // 32-bit offsets when every state index fits (ld * variables < 2^31)
-  const bool small = b.ld * 24 < (int64_t)2147483647;
+  const bool small = b.ld * (n_fp32_vars(b.model) + 1) < (int64_t)2147483647;
   if (b.precision == 0) {
     const int block = 128;
     const int64_t need = (b.n + block - 1) / block;
@@ -249,6 +306,9 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     if (b.model == 5) {
       if (diag) tt2_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
       else tt2_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+    } else if (b.model == 12) {
+      if (diag) ord_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
+      else ord_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
     } else {
       if (diag) crn_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
       else crn_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);

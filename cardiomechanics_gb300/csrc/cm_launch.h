@@ -17,8 +17,10 @@ namespace cm {
 //          (hi, lo) planes:
 //          TT2  m h j xr1 xr2 xs r s d f f2 fCa Rq Ca_i CaSS | CaSR Na_i K_i (hi, lo each)
 //          CRN  h j oi ui Xr Xs u v w m oa ua d f f_Ca Ca_i Ca_TRPN | Ca_up Ca_rel Na_i K_i (hi, lo)
+//          ORd  the 35 states of ORDState other than the six below, in that order |
+//               Na_i Na_ss K_i K_ss Ca_nsr Ca_jsr (hi, lo)
 struct alignas(16) DevBatch {
-  int model = 0;      // 2 Courtemanche, 5 TenTusscher2
+  int model = 0;      // 2 Courtemanche, 5 TenTusscher2, 12 OHaraRudy
   int precision = 0;  // 0 FP64, 1 mixed
   int64_t n = 0, ld = 0;
   double *s64 = nullptr;
@@ -28,12 +30,14 @@ struct alignas(16) DevBatch {
   const void *het[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // double* (FP64) / float* (mixed)
   uint32_t *audit_cell = nullptr;
   unsigned int *audit_or = nullptr;
-  double *diag = nullptr;  // TT2 FP64: 17 x ld diagnostic currents; CRN FP64: 1 x ld (I_SAC)
+  double *diag = nullptr;  // FP64 only: TT2 and ORd 17 x ld diagnostic currents; CRN 1 x ld (I_SAC)
   int variant = 0, grid_mode = 0;  // launch shape chosen by cm_batch_autotune
   TT2Consts<double> tt2_64;
   TT2Consts<float> tt2_32;
   CRNConsts<double> crn_64;
   CRNConsts<float> crn_32;
+  ORDConsts<double> ord_64;
+  ORDConsts<float> ord_32;
 };
 
 // Per-launch inputs/outputs (device pointers).

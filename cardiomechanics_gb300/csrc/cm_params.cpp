@@ -1,8 +1,9 @@
-// Parameter sets of the two models: built-in defaults, .ev loading, derived values and the
+// Parameter sets of the models: built-in defaults, .ev loading, derived values and the
 // FP64 voltage lookup tables. The arithmetic of derive() and build_tables() follows the
 // reference expression by expression (TenTusscher2Parameters.cpp:313-485,
-// CourtemancheParameters.cpp:246-395) so that, against the same libm, the tables agree
-// with the reference bit for bit; the kernels then only read them.
+// CourtemancheParameters.cpp:246-395, OHaraRudyParameters.cpp:246-316) so that, against the
+// same libm, derived values and tables agree with the reference bit for bit; the kernels
+// then only read them. O'Hara-Rudy has no tables: its Calc evaluates every gate directly.
 #include "cm_params.h"
 
 #include <cmath>
@@ -109,12 +110,55 @@ const char *const kCRNState[] = {"Ca_i", "Ca_up", "Ca_rel", "h", "j", "oi", "ui"
                                  "w", "Na_i", "K_i", "m", "oa", "ua", "d", "f", "f_Ca", "Ca_TRPN"};
 const char *const kCRNHet[] = {"g_Na", "g_to", "g_Ks", "g_CaL", "g_bNa", "g_bCa"};
 
+
+// ----------------------------------------------------------------- O'Hara-Rudy
+// Defaults: the values of the reference's OHaraRudy.ev (= OHaraRudy_endo.ev, celltype 0);
+// OHaraRudy_epi.ev (celltype 1) and OHaraRudy_mid.ev (celltype 2) load through .ev files.
+// Order: NS_OHaraRudyParameters::varType (OHaraRudyParameters.h:40-180).
+const ParamDef kORDBase[] = {
+    {"amplitude", -50.0}, {"duration", 0.001}, {"celltype", 0.0}, {"Na_o", 140.0}, {"Ca_o", 1.8}, {"K_o", 5.4},
+    {"INaF_Multiplier", 1.0}, {"INaL_Multiplier", 1.0}, {"Ito_Multiplier", 1.0}, {"PCa_Multiplier", 1.0},
+    {"IKr_Multiplier", 1.0}, {"IKs_Multiplier", 1.0}, {"IK1_Multiplier", 1.0}, {"INaCa_Multiplier", 1.0},
+    {"INaK_Multiplier", 1.0}, {"IKb_Multiplier", 1.0}, {"INab_Multiplier", 1.0}, {"ICab_Multiplier", 1.0},
+    {"IpCa_Multiplier", 1.0}, {"Init_Vm", -0.087962}, {"Init_Na_i", 7.440001}, {"Init_Na_ss", 7.440078},
+    {"Init_K_i", 144.078}, {"Init_K_ss", 144.078}, {"Init_Ca_i", 7.8e-05}, {"Init_Ca_ss", 7.7e-05},
+    {"Init_Ca_nsr", 1.698587}, {"Init_Ca_jsr", 1.605945}, {"Init_m", 0.007374}, {"Init_h_fast", 0.820716},
+    {"Init_h_slow", 0.820717}, {"Init_j", 0.820534}, {"Init_h_CaMK_slow", 0.628164}, {"Init_j_CaMK", 0.819121},
+    {"Init_m_L", 0.00019}, {"Init_h_L", 0.48385}, {"Init_h_L_CaMK", 0.249012}, {"Init_a", 0.001004},
+    {"Init_i_fast", 0.999551}, {"Init_i_slow", 0.487698}, {"Init_a_CaMK", 0.000511},
+    {"Init_i_CaMK_fast", 0.999551}, {"Init_i_CaMK_slow", 0.538887}, {"Init_d", 0.0}, {"Init_f_fast", 1.0},
+    {"Init_f_slow", 0.88001}, {"Init_f_Ca_fast", 1.0}, {"Init_f_Ca_slow", 0.99884}, {"Init_j_Ca", 0.999717},
+    {"Init_n", 0.001876}, {"Init_f_CaMK_fast", 1.0}, {"Init_f_Ca_CaMK_fast", 1.0}, {"Init_x_r_fast", 1.2e-05},
+    {"Init_x_r_slow", 0.551134}, {"Init_x_s1", 0.322839}, {"Init_x_s2", 0.000194}, {"Init_x_K1", 0.99677},
+    {"Init_J_rel_NP", 0.0}, {"Init_J_rel_CaMK", 0.0}, {"Init_CaMK_trap", 0.01941}, {"ISAC_SWITCH", 0.0},
+    {"alpha", 3.0}, {"G_sac", 0.27}, {"K_sac", 100.0}, {"E_sac", 0.0}, {"Init_Ca_TRPN", 0.000654},
+    {"beta1", -1.2}, {"Ca_T50", 0.805}, {"k_TRPN", 0.1}, {"n_TRPN", 2.0}, {"HFM_Multiplier", 1.0},
+    {"HF_Gomez_1", 1.0}, {"HF_Gomez_2", 1.0}, {"HF_Gomez_3", 1.0}, {"HF_Gomez_4", 1.0}, {"HF_Gomez_5", 1.0},
+    {"HF_Gomez_6", 1.0}, {"HF_Gomez_7", 1.0}, {"HF_Gomez_8", 1.0}, {"HF_Gomez_9", 1.0}, {"HF_Gomez_0", 1.0},
+};
+const char *const kORDDerived[] = {
+    "R", "T", "F", "L", "r", "tau_h_L", "A_h_fast", "A_h_slow", "v_cell", "A_geo", "A_cap", "v_myo", "v_nsr",
+    "v_jsr", "v_ss", "P_CaNa", "P_CaK", "P_Ca_CaMK", "P_CaNa_CaMK", "P_CaK_CaMK", "A_f_fast", "A_f_slow",
+    "k_Na1", "k_Na2", "k_asymm", "k_Ca_on", "k_Ca_off", "k_m_1", "k_p_2", "k_p_4", "MgADP", "MgATP", "K_MgATP",
+    "beta_tau", "P_Ca", "h_10", "h_11", "h_12", "k_1", "k_2", "k_5", "beta_1", "alpha_2", "alpha_4", "alpha_rel",
+    "beta_tau_CaMK", "alpha_rel_CaMK", "tau_h_LCaMK", "RToverF"};
+const char *const kORDState[] = {
+    "m", "h_fast", "h_slow", "j", "h_CaMK_slow", "j_CaMK", "m_L", "h_L", "h_L_CaMK", "a", "i_fast", "i_slow",
+    "a_CaMK", "i_CaMK_fast", "i_CaMK_slow", "d", "f_fast", "f_slow", "f_Ca_fast", "f_Ca_slow", "j_Ca", "n",
+    "f_CaMK_fast", "f_Ca_CaMK_fast", "x_r_fast", "x_r_slow", "x_s1", "x_s2", "x_K1", "Na_i", "Na_ss", "K_i",
+    "K_ss", "Ca_i", "Ca_ss", "Ca_nsr", "Ca_jsr", "CaMK_trap", "J_rel_NP", "J_rel_CaMK", "Ca_TRPN"};
+const char *const kORDHet[] = {"INaF_Multiplier", "INaL_Multiplier", "Ito_Multiplier",
+                               "IKr_Multiplier",  "IKs_Multiplier",  "IK1_Multiplier"};
+
 #define COUNT(a) (int)(sizeof(a) / sizeof(a[0]))
 const ModelSpec kSpecs[] = {
     {kTenTusscher2, "TenTusscher2", kTT2Base, COUNT(kTT2Base), kTT2Derived, COUNT(kTT2Derived), kTT2Tables,
      COUNT(kTT2Tables), kTT2State, COUNT(kTT2State), 36, kTT2Het, COUNT(kTT2Het), 0, 0},
     {kCourtemanche, "CourtemancheEtAl", kCRNBase, COUNT(kCRNBase), kCRNDerived, COUNT(kCRNDerived), kCRNTables,
      COUNT(kCRNTables), kCRNState, COUNT(kCRNState), 22, kCRNHet, COUNT(kCRNHet), 20.0, 0.002},
+    // block: 42 states (h_CaMK_fast included) and 17 currents (OHaraRudy.h:31-52)
+    {kOHaraRudy, "OHaraRudy", kORDBase, COUNT(kORDBase), kORDDerived, COUNT(kORDDerived), nullptr, 0, kORDState,
+     COUNT(kORDState), 59, kORDHet, COUNT(kORDHet), 0, 0},
 };
 
 // ----------------------------------------------------------------- .ev files
@@ -261,6 +305,8 @@ void ParamSet::derive() {
     PV(KmNai3) = PV(KmNai) * PV(KmNai) * PV(KmNai);
     PV(Nao3) = PV(Na_o) * PV(Na_o) * PV(Na_o);
     PV(StepCai) = (PV(CaiMax) - PV(CaiMin)) / kRows;
+  } else if (spec->model == kOHaraRudy) {
+    derive_ord();
   } else {
     // CourtemancheParameters::Calculate (252-280)
     PV(RTdF) = PV(R) * PV(Tx) / PV(F);
@@ -285,8 +331,62 @@ void ParamSet::derive() {
   }
 }
 
+// OHaraRudyParameters::Calculate (246-316), value by value in the reference's order.
+void ParamSet::derive_ord() {
+  PV(R) = 8314.0;
+  PV(T) = 310.0;
+  PV(F) = 96485.0;
+  PV(L) = 0.01;
+  PV(r) = 0.0011;
+  PV(tau_h_L) = 200.0;
+  PV(A_h_fast) = 0.99;
+  PV(A_h_slow) = 0.01;
+  PV(A_f_fast) = 0.6;
+  PV(k_Na1) = 15.0;
+  PV(k_Na2) = 5.0;
+  PV(k_asymm) = 12.5;
+  PV(k_Ca_on) = 1.5e6;
+  PV(k_Ca_off) = 5.0e3;
+  PV(k_m_1) = 182.4;
+  PV(k_p_2) = 687.2;
+  PV(k_p_4) = 639.0;
+  PV(MgADP) = 0.05;
+  PV(MgATP) = 9.8;
+  PV(K_MgATP) = 1.698e-7;
+  PV(beta_tau) = 4.75;
+  PV(P_Ca) = PV(PCa_Multiplier) * 0.0001;
+  PV(v_cell) = 1000.0 * 3.14 * PV(r) * PV(r) * PV(L);  // the reference's pi is 3.14
+  PV(A_geo) = 2.0 * 3.14 * PV(r) * PV(r) + 2.0 * 3.14 * PV(r) * PV(L);
+  PV(A_cap) = 2.0 * PV(A_geo);
+  PV(v_myo) = 0.68 * PV(v_cell);
+  PV(v_nsr) = 0.0552 * PV(v_cell);
+  PV(v_jsr) = 0.0048 * PV(v_cell);
+  PV(v_ss) = 0.02 * PV(v_cell);
+  PV(P_CaNa) = 0.00125 * PV(P_Ca);
+  PV(P_CaK) = 3.574e-04 * PV(P_Ca);
+  PV(P_Ca_CaMK) = 1.1 * PV(P_Ca);
+  PV(P_CaNa_CaMK) = 0.00125 * PV(P_Ca_CaMK);
+  PV(P_CaK_CaMK) = 3.5743e-04 * PV(P_Ca_CaMK);
+  PV(A_f_slow) = 1.0 - PV(A_f_fast);
+  PV(h_10) = PV(k_asymm) + 1.0 + (PV(Na_o) * (1.0 + PV(Na_o) / PV(k_Na2))) / PV(k_Na1);
+  PV(h_11) = (PV(Na_o) * PV(Na_o)) / (PV(h_10) * PV(k_Na1) * PV(k_Na2));
+  PV(h_12) = 1.0 / PV(h_10);
+  PV(k_1) = PV(h_12) * PV(Ca_o) * PV(k_Ca_on);
+  PV(k_2) = PV(k_Ca_off);
+  PV(k_5) = PV(k_Ca_off);
+  PV(beta_1) = PV(k_m_1) * PV(MgADP);
+  PV(alpha_2) = PV(k_p_2);
+  PV(alpha_4) = (PV(k_p_4) * (PV(MgATP) / PV(K_MgATP))) / (1.0 + (PV(MgATP) / PV(K_MgATP)));
+  PV(alpha_rel) = 0.5 * PV(beta_tau);
+  PV(beta_tau_CaMK) = 1.25 * PV(beta_tau);
+  PV(alpha_rel_CaMK) = 0.5 * PV(beta_tau_CaMK);
+  PV(tau_h_LCaMK) = 3.0 * PV(tau_h_L);
+  PV(RToverF) = (PV(R) * PV(T)) / PV(F);
+}
+
 void ParamSet::build_tables() {
   tables.assign(spec->n_tables, std::vector<double>(kRows, 0.0));
+  if (spec->n_tables == 0) return;  // O'Hara-Rudy: closed forms only (its InitTable loop is empty)
   auto T = [&](const char *n) -> std::vector<double> & {
     for (int k = 0; k < spec->n_tables; k++)
       if (!strcmp(spec->table_names[k], n)) return tables[k];
@@ -465,10 +565,14 @@ void ParamSet::build_tables() {
 double ParamSet::init_vm() const {
   return spec->model == kTenTusscher2 ? vals[index("init_V_m")] : vals[index("Init_Vm")];
 }
+// GetAmplitude() / GetStimTime(): TT2 and O'Hara-Rudy read parameters (OHaraRudy.h:84-86),
+// Courtemanche returns constants.
 double ParamSet::amplitude() const {
+  if (spec->model == kOHaraRudy) return vals[index("amplitude")];
   return spec->model == kTenTusscher2 ? vals[index("Amp")] : spec->default_amplitude;
 }
 double ParamSet::stim_time() const {
+  if (spec->model == kOHaraRudy) return vals[index("duration")];
   return spec->model == kTenTusscher2 ? vals[index("stim_duration")] : spec->default_stim_time;
 }
 
@@ -480,6 +584,10 @@ void ParamSet::init_state(std::vector<double> &s) const {
                           "init_h", "init_j", "init_Xr1", "init_Xr2", "init_Xs", "init_r",
                           "init_s", "init_d", "init_f", "init_f2", "init_fCa", "init_Rq"};
     for (int k = 0; k < S2_N; k++) s[k] = vals[index(init[k])];
+  } else if (spec->model == kOHaraRudy) {
+    // OHaraRudy::Init (54-102): Init_<name> for every state; troponin as a fraction of trpnmax
+    for (int k = 0; k < SO_Ca_TRPN; k++) s[k] = vals[index((std::string("Init_") + spec->state_names[k]).c_str())];
+    s[SO_Ca_TRPN] = vals[index("Init_Ca_TRPN")] / 0.07;
   } else {
     // Courtemanche::Init (56-83)
     const char *init[] = {"Init_Ca_i", "Init_Ca_up", "Init_Ca_rel", "Init_h", "Init_j", "Init_oi",
@@ -608,7 +716,104 @@ void ParamSet::crn_consts(CRNConsts<double> &d, CRNConsts<float> &f) const {
   for (int k = 0; k < nf; k++) dst[k] = (float)src[k];  // exp250/exp50 become inf; unused in FP32
 }
 
+void ParamSet::ord_consts(ORDConsts<double> &d, ORDConsts<float> &f) const {
+  d.dt_ms = dt * 1000.0;
+  d.RToverF = PV(RToverF);
+  d.FoRT = PV(F) / (PV(R) * PV(T));
+  d.FFoRT = PV(F) * PV(F) / (PV(R) * PV(T));
+  d.Na_o = PV(Na_o);
+  d.K_o = PV(K_o);
+  d.Ca_o = PV(Ca_o);
+  d.util_1 = PV(A_cap) / (PV(F) * PV(v_myo));
+  d.util_2 = PV(v_ss) / PV(v_myo);
+  d.util_3 = PV(A_cap) / (PV(F) * PV(v_ss));
+  d.vnsr_vmyo = PV(v_nsr) / PV(v_myo);
+  d.vjsr_vss = PV(v_jsr) / PV(v_ss);
+  d.vjsr_vnsr = PV(v_jsr) / PV(v_nsr);
+  d.A_h_fast = PV(A_h_fast);
+  d.A_h_slow = PV(A_h_slow);
+  d.A_f_fast = PV(A_f_fast);
+  d.A_f_slow = PV(A_f_slow);
+  d.tau_h_L_mod = PV(HF_Gomez_2) * PV(tau_h_L);               // (211, 215)
+  d.tau_h_L_CaMK = 3.0 * PV(tau_h_L) * PV(HF_Gomez_2);       // (218)
+  d.INaF = PV(INaF_Multiplier);
+  d.INaL = PV(INaL_Multiplier);
+  d.Ito = PV(Ito_Multiplier);
+  d.IKr = PV(IKr_Multiplier);
+  d.IKs = PV(IKs_Multiplier);
+  d.IK1 = PV(IK1_Multiplier);
+  d.HF1 = PV(HF_Gomez_1);
+  d.HF3 = PV(HF_Gomez_3);
+  d.HF4 = PV(HF_Gomez_4);
+  d.HF5 = PV(HF_Gomez_5);
+  d.INaCa_HF6 = PV(INaCa_Multiplier) * PV(HF_Gomez_6);
+  d.INaK_HF7 = PV(INaK_Multiplier) * PV(HF_Gomez_7);
+  d.IKb = PV(IKb_Multiplier);
+  d.INab = PV(INab_Multiplier);
+  d.ICab = PV(ICab_Multiplier);
+  d.IpCa = PV(IpCa_Multiplier);
+  d.P_Ca = PV(P_Ca);
+  d.P_CaNa = PV(P_CaNa);
+  d.P_CaK = PV(P_CaK);
+  d.P_Ca_CaMK = PV(P_Ca_CaMK);
+  d.P_CaNa_CaMK = PV(P_CaNa_CaMK);
+  d.P_CaK_CaMK = PV(P_CaK_CaMK);
+  d.k_Na1 = PV(k_Na1);
+  d.k_Na2 = PV(k_Na2);
+  d.k_Ca_on = PV(k_Ca_on);
+  d.h_11 = PV(h_11);
+  d.k_1 = PV(k_1);
+  d.k_2 = PV(k_2);
+  d.k_5 = PV(k_5);
+  d.beta_1 = PV(beta_1);
+  d.alpha_2 = PV(alpha_2);
+  d.alpha_4 = PV(alpha_4);
+  d.MgATP1 = 1.0 + PV(MgATP);
+  d.alpha_rel = PV(alpha_rel);
+  d.alpha_rel_CaMK = PV(alpha_rel_CaMK);
+  d.beta_tau = PV(beta_tau);
+  d.beta_tau_CaMK = PV(beta_tau_CaMK);
+  // cell-type branches of Calc: M cells release 1.7x (557-560), epicardial cells take up 1.3x
+  // (575-578), buffer 1.3x calmodulin (609-611) and inactivate I_to faster (delta_epi, 234)
+  const double ct = PV(celltype);
+  d.rel_scale = ct == 2.0 ? 1.7 : 1.0;
+  d.HF8x15 = 1.5 * PV(HF_Gomez_8);
+  d.up_scale = ct == 1.0 ? 1.3 : 1.0;
+  d.HF9 = PV(HF_Gomez_9);
+  d.HF0 = PV(HF_Gomez_0);
+  d.cmdnmax = ct == 1.0 ? 0.05 * 1.3 : 0.05;
+  d.epi = ct == 1.0 ? 1.0 : 0.0;
+  d.sqrtKo54 = sqrt(PV(K_o) / 5.4);
+  d.sqrtKo = sqrt(PV(K_o));
+  d.EKs_num = PV(K_o) + 0.01833 * PV(Na_o);
+  d.xK1_shift = 2.5538 * PV(K_o) + 144.59;
+  d.xK1_slope = 1.5692 * PV(K_o) + 3.8115;
+  d.RK1_shift = 105.8 - 2.6 * PV(K_o);
+  d.G_sac = PV(G_sac);
+  d.E_sac = PV(E_sac);
+  d.K_sac = PV(K_sac);
+  d.alpha_sac = PV(alpha);
+  d.ISAC_SWITCH = PV(ISAC_SWITCH);
+  d.Ca_T50 = PV(Ca_T50);
+  d.beta1 = PV(beta1);
+  d.HFM = PV(HFM_Multiplier);
+  d.k_TRPN = PV(k_TRPN);
+  d.n_TRPN = PV(n_TRPN);
+  d.logNao = log(PV(Na_o));
+  d.logKo = log(PV(K_o));
+  d.logEKs_num = log(d.EKs_num);
+  const double *src = &d.dt_ms;
+  float *dst = &f.dt_ms;
+  const int nf = (int)(sizeof(ORDConsts<double>) / sizeof(double));
+  for (int k = 0; k < nf; k++) dst[k] = (float)src[k];
+}
+
 void ParamSet::rows_fp64(std::vector<double> &rows, std::vector<double> &eca) const {
+  if (spec->model == kOHaraRudy) {  // no voltage tables
+    rows.clear();
+    eca.clear();
+    return;
+  }
   if (spec->model == kTenTusscher2) {
     // column -> reference table name
     const char *col[T2_COLS] = {"m_inf", "exptau_m", "h_inf", "exptau_h", "j_inf", "exptau_j", "Xr1_inf",

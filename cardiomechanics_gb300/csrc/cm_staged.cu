@@ -99,7 +99,8 @@ cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_
 }  // namespace
 
 bool staged_supported(const DevBatch &b, const StepIO &io) {
-  return b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext && b.ld % 256 == 0 &&
+  return (b.model == 5 || b.model == 2) && b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext &&
+         b.ld % 256 == 0 &&
          io.vm_lo == io.vm_hi + b.ld && b.n < (int64_t)1 << 30;
 }
 
