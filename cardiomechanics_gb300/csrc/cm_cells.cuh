@@ -69,53 +69,62 @@ __device__ __forceinline__ float crn_mixed_cell(const DevBatch &b, I c, float V,
   return dV;
 }
 
+// O'Hara-Rudy state stores over a batch's device memory (see ord_calc): every state read
+// and written in place as ord_calc reaches it.
+struct ORDStore64 {
+  double *s;     // state of this cell: s[k * ld]
+  int64_t ld;
+  double *diag;  // 17 x ld currents of this cell, or nullptr
+  __device__ __forceinline__ double get(int k) const { return s[k * ld]; }
+  __device__ __forceinline__ void set(int k, double v) { s[k * ld] = v; }
+  // the reference's `X += tinc * dX` (OHaraRudy.cpp:597-659)
+  __device__ __forceinline__ void add(int k, double x, double d) { s[k * ld] = x + d; }
+  __device__ __forceinline__ void cur(int k, double v) {
+    if (diag) diag[k * ld] = v;
+  }
+};
+
 template <typename I>
-__device__ __forceinline__ float ord_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch) {
-  const I ld = (I)b.ld;
-  const float *const *het = (const float *const *)b.het;
-  float *s = b.s32 + c;
-  float x[SO_N];
-  Acc acc[6];
-#pragma unroll
-  for (int k = 0; k < SO_N; k++) {
+struct ORDStore32 {
+  float *s;  // mixed planes of this cell: s[plane * ld]
+  I ld;
+  __device__ __forceinline__ float get(int k) const {
     bool pair;
-    const int p = ord_mixed_plane(k, pair);
-    if (!pair) x[k] = s[p * ld];
+    return s[ord_mixed_plane(k, pair) * ld];
   }
-#pragma unroll
-  for (int q = 0; q < 6; q++) {
-    acc[q].hi = s[(kORDPlain + 2 * q) * ld];
-    acc[q].lo = s[(kORDPlain + 2 * q + 1) * ld];
-    x[ord_pair_var(q)] = acc[q].hi;
+  __device__ __forceinline__ void set(int k, float v) {
+    bool pair;
+    s[ord_mixed_plane(k, pair) * ld] = v;
   }
-  const ORDConsts<float> &C = b.ord_32;
-  ORDHet_<float> g;
+  // compensated add on the (hi, lo) pair; x is the hi word get() returned
+  __device__ __forceinline__ void add(int k, float x, float d) {
+    bool pair;
+    const I p = (I)ord_mixed_plane(k, pair);
+    Acc a{x, s[(p + 1) * ld]};
+    acc_add(a, d);
+    s[p * ld] = a.hi;
+    s[(p + 1) * ld] = a.lo;
+  }
+  __device__ __forceinline__ void cur(int, float) {}
+};
+
+template <typename R, typename I>
+__device__ __forceinline__ ORDHet_<R> ord_het(const DevBatch &b, const ORDConsts<R> &C, I c) {
+  const R *const *het = (const R *const *)b.het;
+  ORDHet_<R> g;
   g.INaF = het[HO_INaF] ? __ldg(het[HO_INaF] + c) : C.INaF;
   g.INaL = het[HO_INaL] ? __ldg(het[HO_INaL] + c) : C.INaL;
   g.Ito = het[HO_Ito] ? __ldg(het[HO_Ito] + c) : C.Ito;
   g.IKr = het[HO_IKr] ? __ldg(het[HO_IKr] + c) : C.IKr;
   g.IKs = het[HO_IKs] ? __ldg(het[HO_IKs] + c) : C.IKs;
   g.IK1 = het[HO_IK1] ? __ldg(het[HO_IK1] + c) : C.IK1;
-  ORDIncr<float> inc;
-  const float dV = ord_calc<float, false>(C, x, inc, g, V, iext, stretch, nullptr);
-  acc_add(acc[0], inc.Na_i);
-  acc_add(acc[1], inc.Na_ss);
-  acc_add(acc[2], inc.K_i);
-  acc_add(acc[3], inc.K_ss);
-  acc_add(acc[4], inc.Ca_nsr);
-  acc_add(acc[5], inc.Ca_jsr);
-#pragma unroll
-  for (int k = 0; k < SO_N; k++) {
-    bool pair;
-    const int p = ord_mixed_plane(k, pair);
-    if (!pair) s[p * ld] = x[k];
-  }
-#pragma unroll
-  for (int q = 0; q < 6; q++) {
-    s[(kORDPlain + 2 * q) * ld] = acc[q].hi;
-    s[(kORDPlain + 2 * q + 1) * ld] = acc[q].lo;
-  }
-  return dV;
+  return g;
+}
+
+template <typename I>
+__device__ __forceinline__ float ord_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch) {
+  ORDStore32<I> x{b.s32 + c, (I)b.ld};
+  return ord_calc<float>(b.ord_32, x, ord_het<float>(b, b.ord_32, c), V, iext, stretch);
 }
 
 }  // namespace cm

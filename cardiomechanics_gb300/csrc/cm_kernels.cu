@@ -170,39 +170,12 @@ __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch
 
 template <bool kDiag>
 __global__ void __launch_bounds__(128) ord_fp64_kernel(const DevBatch b, const StepIO io) {
-  const int64_t ld = b.ld;
-  const double *const *het = (const double *const *)b.het;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
-    double *s = b.s64 + c;
-    double x[SO_N];
-#pragma unroll
-    for (int k = 0; k < SO_N; k++) x[k] = s[k * ld];
-    const ORDConsts<double> &C = b.ord_64;
-    ORDHet_<double> g;
-    g.INaF = het[HO_INaF] ? __ldg(het[HO_INaF] + c) : C.INaF;
-    g.INaL = het[HO_INaL] ? __ldg(het[HO_INaL] + c) : C.INaL;
-    g.Ito = het[HO_Ito] ? __ldg(het[HO_Ito] + c) : C.Ito;
-    g.IKr = het[HO_IKr] ? __ldg(het[HO_IKr] + c) : C.IKr;
-    g.IKs = het[HO_IKs] ? __ldg(het[HO_IKs] + c) : C.IKs;
-    g.IK1 = het[HO_IK1] ? __ldg(het[HO_IK1] + c) : C.IK1;
+    ORDStore64 x{b.s64 + c, b.ld, kDiag ? b.diag + c : nullptr};
     const double V = __ldg(io.vm + c);
     const double iext = stim_for_cell(io, c);
     const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
-    ORDIncr<double> inc;
-    double cur[kORDCurrents];
-    const double dV = ord_calc<double, kDiag>(C, x, inc, g, V, iext, stretch, cur);
-    // the reference's `X += tinc * dX` (OHaraRudy.cpp:597-659)
-    x[SO_Na_i] += inc.Na_i;
-    x[SO_Na_ss] += inc.Na_ss;
-    x[SO_K_i] += inc.K_i;
-    x[SO_K_ss] += inc.K_ss;
-    x[SO_Ca_nsr] += inc.Ca_nsr;
-    x[SO_Ca_jsr] += inc.Ca_jsr;
-#pragma unroll
-    for (int k = 0; k < SO_N; k++) s[k * ld] = x[k];
-    if (kDiag)
-#pragma unroll
-      for (int k = 0; k < kORDCurrents; k++) b.diag[k * ld + c] = cur[k];
+    const double dV = ord_calc<double>(b.ord_64, x, ord_het<double>(b, b.ord_64, c), V, iext, stretch);
     finish(b, io, c, V, dV, 0u);
   }
 }
