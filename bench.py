@@ -62,6 +62,14 @@ MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808}
 # tt2_fp64_kernel: 18 FP64 states r+w (288 B), Vm r+w (16 B), 3 FP64 conductances (24 B).
 FP64_BYTES_PER_CELL_STEP = 2 * 18 * 8 + 2 * 8 + 3 * 8
 WORKLOAD = "tt2006-epi-precision-form-2048x2048"
+# O'Hara-Rudy leg: 4,194,304 endocardial cells, INaF/IKr/IK1 multipliers x U[0.9, 1.1], -50 uA/uF
+# x 1 ms every 1000 ms. Mixed form: 35 FP32 planes + 6 compensated pairs r+w (376 B), Vm pair r+w
+# (16 B), 3 FP32 multipliers (12 B). FP64 form: 41 FP64 states r+w (656 B), Vm r+w (16 B), 3
+# FP64 multipliers (24 B).
+ORD_CELLS = 2048 * 2048
+ORD_BCL = 1.0
+ORD_MIXED_BYTES_PER_CELL_STEP = 2 * (35 + 12) * 4 + 2 * 2 * 4 + 3 * 4
+ORD_FP64_BYTES_PER_CELL_STEP = 2 * 41 * 8 + 2 * 8 + 3 * 8
 FULL_CELLS = 1 << 24
 FULL_INSTANCES = 64
 FULL_BCL = 0.5
@@ -536,6 +544,88 @@ def plain_small_leg(cm, torch, stream, steps=2000):
             "note": "65,536 cells leave most of the GPU's FP64 pipes idle; the 4.2M-cell figure is plain_fp64"}
 
 
+class ORDCPUSample:
+    """The oracle's O'Hara-Rudy (C restatement of the reference Calc, FP64) on the first `cells`
+    cells of the O'Hara-Rudy leg, all host threads."""
+
+    def __init__(self, cells=2048, threads=None):
+        import oracle as O
+        from cardiomechanics_gb300 import workloads as W
+        self.O, self.W, self.port = O, W, O.Port()
+        self.threads = threads or os.cpu_count() or 1
+        self.cells = cells
+        self.P = self.port.param_vector(O.ORD, O.load_params(O.ORD, "endo"))
+        sc = W.conductance_scales(3, ORD_CELLS, 3, 0.9, 1.1, cells=np.arange(cells))
+        names = self.port.param_names(O.ORD)
+        self.het = {k: self.P[names.index(k)] * sc[i] for i, k in enumerate(W.ORD_HETERO)}
+        self.B = self.port.init_state(O.ORD, self.P, cells)
+        self.vm = np.full(cells, self.port.init_vm(O.ORD, self.P))
+
+    def rate(self, seconds):
+        done, el, t = 0, 0.0, 0.0
+        while el < seconds:
+            t0 = time.perf_counter()
+            self.port.run(self.O.ORD, self.P, np.zeros((0, self.O.RTDT)), self.B, self.vm, 200, DT, t0=t,
+                          textbegin=0.0, textlen=1e-3, bcl=1e9, amp=self.W.ORD_STIM, het=self.het,
+                          n_threads=self.threads)
+            el += time.perf_counter() - t0
+            done += 200
+            t += 200 * DT
+        return {"value": self.cells * done / el, "unit": UNIT, "cores": self.threads, "kind": "port",
+                "sample": f"first {self.cells} of the {ORD_CELLS} O'Hara-Rudy cells x {done} steps of 0.01 ms "
+                          f"(oracle C restatement of the reference Calc in FP64, {self.threads} threads, {el:.1f} s)"}
+
+
+def ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak=None, cpu_seconds=0.0):
+    """O'Hara-Rudy 2011 (the reference's variant), 4,194,304 endocardial cells: the mixed form
+    (autotuned launch shape) and the plain FP64 form, each timed with events on its stream."""
+    from cardiomechanics_gb300 import workloads as W
+    n = args.ord_cells
+    p = cm.Params(cm.OHARARUDY, None, DT)
+    sc = W.conductance_scales(3, n, 3, 0.9, 1.1)
+    kw = dict(textbegin=0.0, textlen=1e-3, bcl=ORD_BCL, amplitude=W.ORD_STIM)
+    out = {"workload": f"ord2011-endo-{n}-cells", "cells": n, "bcl_ms": ORD_BCL * 1e3,
+           "conductance_jitter": "INaF,IKr,IK1 multipliers x U[0.9,1.1] seed 3", "stimulus": "-50 uA/uF x 1 ms"}
+    for prec, steps, name in ((cm.MIXED, args.ord_steps, "mixed"), (cm.FP64, args.fp64_steps, "fp64")):
+        b = cm.Batch(p, n, prec, stream=stream.cuda_stream)
+        for k, h in enumerate(W.ORD_HETERO):
+            b.add_hetero_value(h, p.get(h) * sc[k])
+        tuned = None
+        if prec == cm.MIXED:
+            tuned = b.autotune(args.tune_steps)
+        vm = torch.tensor(b.init_vm(), device="cuda")
+        b.run(vm, 3, **kw)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(vm, steps, t0=3 * DT, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        bps = ORD_MIXED_BYTES_PER_CELL_STEP if prec == cm.MIXED else ORD_FP64_BYTES_PER_CELL_STEP
+        achieved = bps * n * steps / sec / 1e9
+        leg = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+               "audit_mask": b.audit(), "gpu_launches": steps,
+               "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                       "peak_kind": peak_kind, "bytes_per_cell_step": bps}}
+        if tuned is not None:
+            leg["autotune"] = {"choice": tuned[0], "ms_per_step": tuned[1]}
+            leg["precision"] = "mixed (FP32 gates/currents, compensated FP32 pairs for Vm, Na_i, Na_ss, K_i, " \
+                               "K_ss, Ca_nsr, Ca_jsr)"
+        else:
+            leg["precision"] = "FP64 (the reference arithmetic)"
+            if fp64_peak:
+                leg["fp64_fma_peak_tflops_measured"] = fp64_peak
+        out[name] = leg
+        del b, vm
+        torch.cuda.empty_cache()
+    out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    if cpu_seconds > 0:
+        out["cpu_baseline"] = ORDCPUSample().rate(cpu_seconds)
+    return out
+
+
 def precision_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     """Precision form: 4,194,304 cells, the HBM-bound plain kernel (autotuned launch shape)."""
     p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
@@ -587,7 +677,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
-                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched"],
+                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord"],
                     help="run one leg only (profiler captures); the contract's JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
@@ -599,6 +689,9 @@ def main():
     ap.add_argument("--sur-train-frac", type=float, default=1.0,
                     help="fraction of the surrogate's training run (profiling captures only; accuracy needs 1)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
+    ap.add_argument("--ord-steps", type=int, default=500, help="timed steps of the O'Hara-Rudy mixed form")
+    ap.add_argument("--ord-cells", type=int, default=ORD_CELLS, help="O'Hara-Rudy cells (fewer only for captures)")
+    ap.add_argument("--no-ord", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -626,6 +719,10 @@ def main():
         return
     if args.only == "mixed":
         print(json.dumps(precision_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
+        return
+    if args.only == "ord":
+        print(json.dumps(ord_leg(cm, torch, stream, args, hbm_peak, peak_kind,
+                                 cpu_seconds=0.0 if args.no_cpu else 5.0)), flush=True)
         return
     p, sur, training = train_surrogate(cm, stream, args.sur_train_frac)
     if args.only == "surrogate":
@@ -658,6 +755,10 @@ def main():
     bat = None
     if not args.no_batched:
         bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
+    ordl = None
+    if not args.no_ord:
+        ordl = ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak,
+                       cpu_seconds=5.0 if (rank == 0 and not args.no_cpu) else 0.0)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(seconds=args.cpu_seconds)
@@ -688,6 +789,7 @@ def main():
             "plain_small": small,
             "learned_form": learned,
             "batched": bat,
+            "ohara_rudy": ordl,
             "fp32_fma_peak_tflops_measured": fp32_peak,
             "cpu_baseline": cpu,
             "gpu_launches": full["gpu_launches"],
