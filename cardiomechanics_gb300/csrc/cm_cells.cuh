@@ -75,6 +75,7 @@ struct ORDStore64 {
   double *s;     // state of this cell: s[k * ld]
   int64_t ld;
   double *diag;  // 17 x ld currents of this cell, or nullptr
+  __device__ __forceinline__ void fetch(int) {}
   __device__ __forceinline__ double get(int k) const { return s[k * ld]; }
   __device__ __forceinline__ void set(int k, double v) { s[k * ld] = v; }
   // the reference's `X += tinc * dX` (OHaraRudy.cpp:597-659)
@@ -84,26 +85,45 @@ struct ORDStore64 {
   }
 };
 
+// The FP32 store reads the cell's words in two batches, each before any write that could
+// precede it: a load placed after a store to the same planes could not be moved above it (the
+// planes might alias), so loads taken one by one as ord_calc reaches them would each wait out
+// the full memory latency, and loading all 47 words at once would not fit the registers.
+// Batch 0 (when the store is made): CaMK, the I_Na/I_NaL/I_to gates, Na_i, K_i, Ca_ss; batch 1
+// (fetch(1), before I_CaL): everything else.
 template <typename I>
 struct ORDStore32 {
   float *s;  // mixed planes of this cell: s[plane * ld]
   I ld;
-  __device__ __forceinline__ float get(int k) const {
-    bool pair;
-    return s[ord_mixed_plane(k, pair) * ld];
+  float v[SO_N];  // this step's inputs (hi words for the pairs)
+  float lo[6];    // lo words of the pairs, ord_pair_var order
+  __device__ __forceinline__ static bool first(int k) {
+    return k <= SO_i_CaMK_slow || k == SO_Na_i || k == SO_K_i || k == SO_Ca_ss || k == SO_CaMK_trap;
   }
-  __device__ __forceinline__ void set(int k, float v) {
+  __device__ __forceinline__ ORDStore32(float *s_, I ld_) : s(s_), ld(ld_) { fetch(0); }
+  __device__ __forceinline__ void fetch(int part) {
+#pragma unroll
+    for (int k = 0; k < SO_N; k++) {
+      bool pair;
+      if (first(k) == (part == 0)) v[k] = s[ord_mixed_plane(k, pair) * ld];
+    }
+    if (part == 1) {
+#pragma unroll
+      for (int q = 0; q < 6; q++) lo[q] = s[(kORDPlain + 2 * q + 1) * ld];
+    }
+  }
+  __device__ __forceinline__ float get(int k) const { return v[k]; }
+  __device__ __forceinline__ void set(int k, float x) {
     bool pair;
-    s[ord_mixed_plane(k, pair) * ld] = v;
+    s[ord_mixed_plane(k, pair) * ld] = x;
   }
   // compensated add on the (hi, lo) pair; x is the hi word get() returned
   __device__ __forceinline__ void add(int k, float x, float d) {
-    bool pair;
-    const I p = (I)ord_mixed_plane(k, pair);
-    Acc a{x, s[(p + 1) * ld]};
+    const int q = k <= SO_K_ss ? k - SO_Na_i : 4 + (k - SO_Ca_nsr);
+    Acc a{x, lo[q]};
     acc_add(a, d);
-    s[p * ld] = a.hi;
-    s[(p + 1) * ld] = a.lo;
+    s[(kORDPlain + 2 * q) * ld] = a.hi;
+    s[(kORDPlain + 2 * q + 1) * ld] = a.lo;
   }
   __device__ __forceinline__ void cur(int, float) {}
 };
@@ -123,7 +143,7 @@ __device__ __forceinline__ ORDHet_<R> ord_het(const DevBatch &b, const ORDConsts
 
 template <typename I>
 __device__ __forceinline__ float ord_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch) {
-  ORDStore32<I> x{b.s32 + c, (I)b.ld};
+  ORDStore32<I> x(b.s32 + c, (I)b.ld);
   return ord_calc<float>(b.ord_32, x, ord_het<float>(b, b.ord_32, c), V, iext, stretch);
 }
 

@@ -75,6 +75,7 @@ CM_HD R o_sig(R z) {  // 1 / (1 + exp(z))
 }
 
 // One Calc of one cell. The state store S is the cell's view of its batch:
+//   void fetch(int part)       part 1: the store may read its remaining inputs now (before I_CaL)
 //   R get(int k)               state k (ORDState order) as this step reads it
 //   void set(int k, R v)       new value of a plain state, stored as soon as it is final
 //   void add(int k, R x, R d)  x + d for Na_i, Na_ss, K_i, K_ss, Ca_nsr, Ca_jsr (x = get(k))
@@ -188,6 +189,7 @@ CM_HD R ord_calc(const ORDConsts<R> &C, S &x, const ORDHet_<R> &g, R V, R i_exte
   }
 
   // I_CaL, I_CaNa, I_CaK (264-329)
+  x.fetch(1);
   const R em1_Ca = o_expm1(R(2) * VFoverRT), em1_1 = o_expm1(VFoverRT);
   const R exp_z_Ca = em1_Ca + R(1), exp_z_1 = em1_1 + R(1);
   R I_CaL, s_Nass, s_Kss;
