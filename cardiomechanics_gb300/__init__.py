@@ -54,6 +54,7 @@ ABI_SYMBOLS = (
     "cm_surrogate_destroy", "cm_surrogate_mlp", "cm_surrogate_generate", "cm_surrogate_dataset",
     "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
     "cm_batch_run_surrogate", "cm_mlp_forward_static", "cm_surrogate_flush_audit",
+    "cm_diffusion_create", "cm_diffusion_destroy", "cm_diffusion_apply", "cm_batch_run_diffuse",
 )
 
 
@@ -120,6 +121,11 @@ def lib() -> ctypes.CDLL:
     L.cm_batch_step_update_act.argtypes = [vp, ctypes.c_double, vp, vp, vp, ctypes.c_double, vp, ctypes.c_double,
                                            ctypes.c_double]
     L.cm_batch_run.argtypes = [vp, vp, i64, ctypes.POINTER(Stimulus), vp, i64, i64, vp]
+    L.cm_diffusion_create.argtypes = [ctypes.POINTER(vp), i64, vp, vp, vp, vp, ctypes.c_double]
+    L.cm_diffusion_destroy.argtypes = [vp]
+    L.cm_diffusion_apply.argtypes = [vp, vp, vp]
+    L.cm_batch_run_diffuse.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), ctypes.c_double, vp,
+                                       ctypes.c_double]
     L.cm_batch_audit.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), vp]
     L.cm_batch_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.cm_batch_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
@@ -369,11 +375,61 @@ class Batch:
                                             audit_mod, ctypes.byref(stats)))
         return stats.as_dict()
 
+    def run_diffuse(self, diffusion, Vm, n_steps, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0,
+                    t0=0.0, textbegin_per_cell=None, vm_range=0.0, act=None, act_threshold=-0.02):
+        """n_steps monodomain steps coupled by `diffusion` (acCELLerate::IntraStep's explicit
+        path): i_ext = scale * (A Vm) + stimulus, Vm += Calc(...), range check, activation
+        times in `act` (float64, -1 = not yet). Vm and act updated in place."""
+        Vm = _f64(Vm, self.n, "Vm")
+        act = _f64(act, self.n, "act")
+        tbc = _per_cell_times(textbegin_per_cell, self.n)
+        st = Stimulus(t0, textbegin, None if tbc is None else ctypes.cast(_ptr(tbc), ctypes.POINTER(ctypes.c_double)),
+                      textlen, bcl, amplitude)
+        _check(lib().cm_batch_run_diffuse(self._h, diffusion._h, _ptr(Vm), int(n_steps), ctypes.byref(st),
+                                          vm_range, _ptr(act), act_threshold))
+
     def audit(self, per_cell: bool = False):
         m = ctypes.c_uint32()
         pc = np.zeros(self.n, np.uint32) if per_cell else None
         _check(lib().cm_batch_audit(self._h, ctypes.byref(m), _ptr(pc)))
         return (m.value, pc) if per_cell else m.value
+
+
+class Diffusion:
+    """The monodomain coupling operator: Intra.A (CSR) and the per-node conversion of A*Vm to
+    the cell model's i_external (the reference's -Volume()/volume_local*1e9)."""
+
+    def __init__(self, rowptr, col, val, scale=None, uniform_scale=1.0):
+        rowptr = np.ascontiguousarray(rowptr, np.int64)
+        col = np.ascontiguousarray(col, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        n = rowptr.size - 1
+        sc = None if scale is None else np.ascontiguousarray(scale, np.float64)
+        if sc is not None and sc.size != n:
+            raise ValueError("scale: need one value per row")
+        if col.size != val.size or (n >= 0 and col.size < (rowptr[-1] if n > 0 else 0)):
+            raise ValueError("col/val shorter than rowptr[-1]")
+        h = ctypes.c_void_p()
+        _check(lib().cm_diffusion_create(ctypes.byref(h), n, _ptr(rowptr), _ptr(col), _ptr(val), _ptr(sc),
+                                         float(uniform_scale)))
+        self._h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_diffusion_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def apply(self, x, y=None):
+        """y = scale * (A x) in FP64 on the GPU."""
+        x = _f64(x if hasattr(x, "data_ptr") else np.ascontiguousarray(x, np.float64), self.n, "x")
+        if y is None:
+            y = np.zeros(self.n)
+        _check(lib().cm_diffusion_apply(self._h, _ptr(x), _ptr(y)))
+        return y
 
 
 class Multi:

@@ -49,18 +49,6 @@ int ref_block_index(int model, int k) {
   return k < 20 ? k : 21;
 }
 
-int ensure_stage(cm_batch_s *b, int64_t n) {
-  if (b->stage_n >= n) return CM_OK;
-  for (auto &p : b->stage) {
-    if (p) cudaFree(p);
-    p = nullptr;
-  }
-  b->stage_n = 0;
-  for (auto &p : b->stage) CK(cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(double)));
-  b->stage_n = n;
-  return CM_OK;
-}
-
 // Device view of a caller array: the pointer itself if on the device, else a staged copy.
 int stage_in(cm_batch_s *b, const double *p, int slot, const double **out) {
   if (!p) {
@@ -323,6 +311,7 @@ int cm_batch_destroy(cm_batch_t b) {
   for (auto p : b->stage) cudaFree(p);
   cudaFree(b->tb_cell);
   cudaFree(b->vm_planes);
+  cudaFree(b->vm_planes2);
   cudaFree(b->probe_idx);
   cudaFree(b->probe_out);
   delete b;

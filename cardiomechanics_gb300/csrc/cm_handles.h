@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -30,6 +31,7 @@ struct cm_batch_s {
   int64_t stage_n = 0;
   double *tb_cell = nullptr;
   float *vm_planes = nullptr;  // mixed batches: Vm as hi/lo planes during fused runs (2 x n)
+  float *vm_planes2 = nullptr; // the second pair of Vm planes of coupled runs (cm_batch_run_diffuse)
   int64_t *probe_idx = nullptr;
   int64_t probe_cap = 0;
   double *probe_out = nullptr;
@@ -65,6 +67,19 @@ inline bool is_device_ptr(const void *p) {
     return false;
   }
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Grows the batch's four staging buffers to n doubles each.
+inline int ensure_stage(cm_batch_s *b, int64_t n) {
+  if (b->stage_n >= n) return CM_OK;
+  for (auto &p : b->stage) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  b->stage_n = 0;
+  for (auto &p : b->stage) CK(cudaMalloc(&p, std::max<int64_t>(n, 1) * sizeof(double)));
+  b->stage_n = n;
+  return CM_OK;
 }
 
 // The driver's per-cell first stimulus times for a run: a device array is used (and advanced)

@@ -28,6 +28,45 @@ __device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
   return io.iext ? __ldg(io.iext + c) : io.iext_uniform;
 }
 
+// Monodomain coupling current of cell c: scale_c * (A x)_c with A's row c in its 32-row slice
+// (acCELLerate.cpp:1849 MatMult and 1880-1887 conversion). FP64: entries summed in CSR order.
+// Padding entries of a slice carry value 0 and the row's own column.
+__device__ __forceinline__ double coupling_fp64(const StepIO &io, const double *x, int64_t c) {
+  const int64_t s = c >> 5;
+  const int64_t e1 = io.sl_ptr[s + 1];
+  double acc = 0.0;
+  for (int64_t e = io.sl_ptr[s] + (c & 31); e < e1; e += 32) acc += io.sl_val64[e] * __ldg(x + io.sl_col[e]);
+  return acc * (io.dscale64 ? __ldg(io.dscale64 + c) : io.dscale_u);
+}
+
+// Mixed form: rowsum_c x_c + sum_j A_cj (x_j - x_c) on the previous step's hi plane; the
+// differences of neighbouring potentials are small, so FP32 keeps them (the plain sum would
+// cancel a diagonal ~6 orders above the result at rest).
+template <typename I>
+__device__ __forceinline__ float coupling_f32(const StepIO &io, I c) {
+  const float *x = io.vm_hi;
+  const float xc = x[c];
+  const int64_t s = (int64_t)c >> 5;
+  const int64_t e1 = io.sl_ptr[s + 1];
+  float acc = __ldg(io.rowsum32 + c) * xc;
+  for (int64_t e = io.sl_ptr[s] + (c & 31); e < e1; e += 32) acc += io.sl_val32[e] * (x[io.sl_col[e]] - xc);
+  return acc * (io.dscale32 ? __ldg(io.dscale32 + c) : (float)io.dscale_u);
+}
+
+// i_external of an FP64 cell update: the stimulus plus, with a coupling operator, its current.
+__device__ __forceinline__ double iext_fp64(const StepIO &io, int64_t c) {
+  double i = stim_for_cell(io, c);
+  if (io.sl_ptr) i += coupling_fp64(io, io.vm, c);
+  return i;
+}
+
+template <typename I>
+__device__ __forceinline__ float iext_f32(const StepIO &io, I c) {
+  float i = (float)stim_for_cell(io, c);
+  if (io.sl_ptr) i += coupling_f32<I>(io, c);
+  return i;
+}
+
 __device__ __forceinline__ void finish(const DevBatch &b, const StepIO &io, int64_t c, double V, double dV,
                                        uint32_t audit) {
   const double vn = V + dV;
@@ -44,9 +83,11 @@ __device__ __forceinline__ void finish(const DevBatch &b, const StepIO &io, int6
 
 template <typename I>
 __device__ __forceinline__ void finish_acc(const DevBatch &b, I c, Acc v, uint32_t audit, const StepIO &io) {
-  io.vm_hi[c] = v.hi;
-  io.vm_lo[c] = v.lo;
+  (io.vm_hi_out ? io.vm_hi_out : io.vm_hi)[c] = v.hi;
+  (io.vm_lo_out ? io.vm_lo_out : io.vm_lo)[c] = v.lo;
   if (!isfinite(v.hi)) audit |= 1u;
+  if (io.vm_range > 0.0 && fabsf(v.hi) > (float)io.vm_range) audit |= 32u;
+  if (io.act && io.act[c] == -1.0 && v.hi >= (float)io.act_threshold) io.act[c] = io.act_time;
   if (audit) {
     atomicOr(b.audit_cell + c, audit);
     atomicOr(b.audit_or, audit);
@@ -77,7 +118,7 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
     g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
     g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
     const double V = __ldg(io.vm + c);
-    const double iext = stim_for_cell(io, c);
+    const double iext = iext_fp64(io, c);
     uint32_t audit = 0;
     const int vi = vrow_fp64(V * 1000, audit);
     TT2Diag<double> dg;
@@ -96,7 +137,7 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
 template <typename I, int kBlock, int kMinB>
 __global__ void __launch_bounds__(kBlock, kMinB) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = (float)stim_for_cell(io, c);
+    const float iext = iext_f32<I>(io, c);
     uint32_t audit = 0;
     if (io.vm_hi) {
       Acc v{io.vm_hi[c], io.vm_lo[c]};
@@ -133,7 +174,7 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
     g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
     g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
     const double V = __ldg(io.vm + c);
-    const double iext = stim_for_cell(io, c);
+    const double iext = iext_fp64(io, c);
     const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
     uint32_t audit = 0;
     const int vi = vrow_fp64(V * 1000.0, audit);
@@ -153,7 +194,7 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
 template <typename I, int kBlock, int kMinB>
 __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = (float)stim_for_cell(io, c);
+    const float iext = iext_f32<I>(io, c);
     const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
     uint32_t audit = 0;
     if (io.vm_hi) {
@@ -173,7 +214,7 @@ __global__ void __launch_bounds__(128) ord_fp64_kernel(const DevBatch b, const S
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
     ORDStore64 x{b.s64 + c, b.ld, kDiag ? b.diag + c : nullptr};
     const double V = __ldg(io.vm + c);
-    const double iext = stim_for_cell(io, c);
+    const double iext = iext_fp64(io, c);
     const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
     const double dV = ord_calc<double>(b.ord_64, x, ord_het<double>(b, b.ord_64, c), V, iext, stretch);
     finish(b, io, c, V, dV, 0u);
@@ -183,7 +224,7 @@ __global__ void __launch_bounds__(128) ord_fp64_kernel(const DevBatch b, const S
 template <typename I, int kBlock, int kMinB>
 __global__ void __launch_bounds__(kBlock, kMinB) ord_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = (float)stim_for_cell(io, c);
+    const float iext = iext_f32<I>(io, c);
     const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
     if (io.vm_hi) {
       Acc v{io.vm_hi[c], io.vm_lo[c]};
@@ -195,6 +236,11 @@ __global__ void __launch_bounds__(kBlock, kMinB) ord_mixed_kernel(const DevBatch
       finish(b, io, c, V, (double)dV, 0u);
     }
   }
+}
+
+__global__ void diffusion_apply_kernel(const StepIO io, const double *x, double *y, int64_t n) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    y[c] = coupling_fp64(io, x, c);
 }
 
 __global__ void probe_kernel(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
@@ -301,6 +347,14 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
   const int grid = (int)(need < cap ? need : cap);
   if (small) launch_mixed_variant<int>(b, io, variant, grid, s);
   else launch_mixed_variant<int64_t>(b, io, variant, grid, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diffusion_apply(const StepIO &io, const double *x, double *y, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t g = (n + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  diffusion_apply_kernel<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(io, x, y, n);
   return cudaGetLastError();
 }
 

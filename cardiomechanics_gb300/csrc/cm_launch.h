@@ -58,7 +58,23 @@ struct StepIO {
   // -1 and whose new Vm reaches act_threshold gets act_time
   double *act = nullptr;
   double act_time = 0.0, act_threshold = 0.0;
+  // monodomain coupling (cm_batch_run_diffuse): i_ext += scale * (A x), A in 32-row slices
+  // (slice s: entries sl_ptr[s] .. sl_ptr[s+1], entry k of row 32 s + r at sl_ptr[s] + 32 k + r).
+  // FP64 batches: x = vm (the previous step's Vm; the new one goes to vm_out), sum in CSR order.
+  // Mixed batches: x = the previous step's hi plane, rowsum32 * x_l + sum val32 (x_j - x_l)
+  // (val32 holds the off-diagonal entries only); the new Vm goes to vm_hi_out / vm_lo_out.
+  const int64_t *sl_ptr = nullptr;
+  const int32_t *sl_col = nullptr;
+  const double *sl_val64 = nullptr;
+  const float *sl_val32 = nullptr, *rowsum32 = nullptr;
+  const double *dscale64 = nullptr;  // per node, or nullptr for dscale_u
+  const float *dscale32 = nullptr;
+  double dscale_u = 0.0;
+  float *vm_hi_out = nullptr, *vm_lo_out = nullptr;  // mixed: new Vm planes (nullptr: in place)
 };
+
+// y = scale * (A x) for a coupling operator (cm_diffusion_apply); io carries the operator.
+cudaError_t launch_diffusion_apply(const StepIO &io, const double *x, double *y, int64_t n, cudaStream_t s);
 
 int n_fp32_vars(int model);
 int n_fp64_vars(int model, int precision);

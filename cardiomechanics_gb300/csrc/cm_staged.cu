@@ -100,6 +100,7 @@ cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_
 
 bool staged_supported(const DevBatch &b, const StepIO &io) {
   return (b.model == 5 || b.model == 2) && b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext &&
+         !io.sl_ptr && !io.vm_hi_out && !io.act && io.vm_range <= 0.0 &&
          b.ld % 256 == 0 &&
          io.vm_lo == io.vm_hi + b.ld && b.n < (int64_t)1 << 30;
 }

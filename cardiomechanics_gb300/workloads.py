@@ -91,3 +91,38 @@ def full_form_instances(seed: int, n_inst: int = 64, total: int = 1 << 24, align
     sizes = np.maximum(align, np.floor(w / w.sum() * total / align).astype(np.int64) * align)
     sizes[-1] += total - sizes.sum()
     return [{"n": int(sizes[i]), "phase": float(u[i, 1])} for i in range(n_inst)]
+
+
+# Monodomain coupling: i_external per unit of A*Vm when A is a stiffness-type operator in 1/s
+# (A*Vm in V/s, the local diffusion term being -A*Vm): TT2 takes nA per cell and converts with
+# 2.29656e-2 nA per pA/pF (TenTusscher2.cpp:630), Courtemanche pA/pF, O'Hara-Rudy uA/uF with the
+# sign of an outward current (OHaraRudy.cpp:525-533).
+COUPLING_SCALE = {5: -2.29656e-2, 2: -1.0, 12: 1.0}
+
+
+def grid_laplacian(nx: int, ny: int, nz: int = 1, d_over_h2: float = 1.0e4):
+    """Finite-difference operator K of D * Laplacian on an nx x ny x nz grid with no-flux edges,
+    in CSR (rowptr int64, col int32, val float64), node l = x + nx (y + ny z), columns sorted:
+    K_ll = d_over_h2 * (number of neighbours), K_lm = -d_over_h2 for each neighbour m. The
+    default 1e4 / s is D = 0.1 mm^2/ms on a 0.1 mm grid."""
+    n = nx * ny * nz
+    idx = np.arange(n, dtype=np.int64)
+    x, y, z = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    cols, vals = [], []
+    nb = np.zeros(n, np.int64)
+    offs = []
+    for d, ok in ((-nx * ny, z > 0), (-nx, y > 0), (-1, x > 0), (1, x < nx - 1), (nx, y < ny - 1),
+                  (nx * ny, z < nz - 1)):
+        offs.append((d, ok))
+        nb += ok
+    entries = []
+    for d, ok in offs[:3]:
+        entries.append((np.where(ok, idx + d, -1), np.where(ok, -d_over_h2, 0.0)))
+    entries.append((idx, nb * d_over_h2))
+    for d, ok in offs[3:]:
+        entries.append((np.where(ok, idx + d, -1), np.where(ok, -d_over_h2, 0.0)))
+    C = np.stack([e[0] for e in entries], axis=1)
+    V = np.stack([e[1] for e in entries], axis=1)
+    keep = C >= 0
+    rowptr = np.concatenate([[0], np.cumsum(keep.sum(axis=1))]).astype(np.int64)
+    return rowptr, C[keep].astype(np.int32), V[keep].astype(np.float64)

@@ -207,6 +207,44 @@ int cm_batch_set_launch(cm_batch_t b, int variant, int grid_mode);
  * receives each cell's bits. Clears the bits. */
 int cm_batch_audit(cm_batch_t b, uint32_t *mask, uint32_t *per_cell);
 
+/* ------------------------------------------------------------------ monodomain coupling */
+/* The explicit monodomain step of acCELLerate::IntraStep (acCELLerate.cpp:1839-2005, the
+ * path without a mass matrix, Gauss points or implicit smoothing, Godunov current scheme):
+ *     B = Intra.A * Vm                                   (MatMult, line 1849)
+ *     i_ext[l] = scale[l] * B[l] + stimulus[l]           (nA/cell conversion 1880-1887,
+ *                                                         injected-current conditions 1892)
+ *     dVm[l] = Calc(dtcell, Vm[l], i_ext[l], 1, 1)       (CalcCellModels 1757-1770)
+ *     Vm[l] += dVm[l], NaN / vm_def_range check          (1930-1949)
+ *     activation times                                   (1997-2005)
+ * with the matrix-vector product, the cell update, the check and the activation times fused
+ * into one pass over the nodes per step. The reference's scale is -Volume()/volume_local*1e9. */
+typedef struct cm_diffusion_s *cm_diffusion_t;
+
+/* A: n x n in CSR (rowptr[n + 1] with rowptr[0] = 0, col[rowptr[n]] in [0, n), val), host
+ * memory, as MatGetRowIJ / MatSeqAIJGetArray give it; the library keeps its own device copy
+ * (slices of 32 rows stored column-major within the slice, so consecutive nodes' entries are
+ * adjacent). scale: n doubles (host), or NULL for uniform_scale at every node. Row l of A
+ * belongs to cell l of the batches it is used with. CM_ERR_ARG for malformed CSR. */
+int cm_diffusion_create(cm_diffusion_t *out, int64_t n, const int64_t *rowptr, const int32_t *col,
+                        const double *val, const double *scale, double uniform_scale);
+int cm_diffusion_destroy(cm_diffusion_t d);
+/* y[l] = scale[l] * (A x)[l] in FP64, entries summed in CSR order. x, y: n doubles, host or
+ * device, not aliased. */
+int cm_diffusion_apply(cm_diffusion_t d, const double *x, double *y);
+
+/* n_steps monodomain steps (above) of batch b coupled by d (same n), fused on the device. Vm:
+ * n doubles, host or device, updated in place; each step's product reads the previous step's
+ * Vm of every node (the new values go to a second buffer). stim: the driver's stimulus protocol
+ * as in cm_batch_run, whose current is added to i_ext (per-cell first-stimulus times give
+ * regional stimuli: a cell with textbegin beyond the run is never stimulated). FP64 batches form
+ * A*Vm in FP64 in CSR order; mixed batches in FP32 as rowsum(A)_l Vm_l + sum_j A_lj (Vm_j - Vm_l)
+ * (no cancellation of the large diagonal). vm_range > 0: |Vm| beyond it is an error, as
+ * vm_def_range. act (optional, n doubles, host or device): cells whose entry is -1 and whose new
+ * Vm reaches act_threshold [V] get the step's time. Returns CM_ERR_NUMERIC if a Vm became
+ * non-finite or left the range. */
+int cm_batch_run_diffuse(cm_batch_t b, cm_diffusion_t d, double *Vm, int64_t n_steps, const cm_stimulus *stim,
+                         double vm_range, double *act, double act_threshold);
+
 /* ------------------------------------------------------------------ batched form */
 /* Many batches (instances) of uneven size and mixed model -- e.g. the per-material cell
  * populations of acCELLerate (acltCellModel.cpp:64-126) or independent simulations -- advanced

@@ -87,6 +87,13 @@ class Port:
         L.cmo_calc.argtypes = [ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double]
         L.cmo_calc.restype = ctypes.c_double
+        _lp = ctypes.POINTER(ctypes.c_long)
+        _ip = ctypes.POINTER(ctypes.c_int)
+        L.cmo_mono_run.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_long, _dp, _dp, ctypes.c_int, _ip, _dp, _lp,
+                                   _ip, _dp, _dp, ctypes.c_double, ctypes.c_long, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_long, _dp,
+                                   ctypes.c_int]
         L.cmo_run.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_long, _dp, _dp, ctypes.c_int,
                               ctypes.POINTER(ctypes.c_int), _dp, ctypes.c_long, ctypes.c_double,
                               ctypes.c_double, ctypes.c_double, _dp, ctypes.c_double, ctypes.c_double,
@@ -163,6 +170,37 @@ class Port:
                             _ptr(trace), n_threads)
         if rc != 0:
             raise FloatingPointError(f"oracle run failed rc={rc}")
+        return trace
+
+
+    def mono_run(self, model, P, T, blocks, Vm, n_steps, dt, rowptr, col, val, *, scale=None,
+                 uniform_scale=1.0, t0=0.0, textbegin=0.0, textbegin_per_cell=None, textlen=1e-3, bcl=1.0,
+                 amp=0.0, het=None, act=None, act_threshold=-0.02, vm_range=0.0, rec_every=0, n_threads=1):
+        """Explicit monodomain steps (acCELLerate::IntraStep, Godunov): B = A Vm in CSR order,
+        i_ext = B * scale + stimulus, Vm += Calc. blocks, Vm and act updated in place; returns
+        the Vm trace (n_cells, n_rec) when rec_every > 0."""
+        n = blocks.shape[0]
+        assert blocks.flags.c_contiguous and Vm.flags.c_contiguous
+        het = het or {}
+        idx = (ctypes.c_int * max(1, len(het)))(*[self.L.cmo_param_index(model, k.encode()) for k in het])
+        assert all(i >= 0 for i in list(idx)[:len(het)]), "unknown hetero parameter"
+        hv = np.ascontiguousarray(np.stack([np.asarray(v, np.float64) for v in het.values()])) if het else None
+        rp = np.ascontiguousarray(rowptr, np.int64).astype(np.dtype("l"))
+        cl = np.ascontiguousarray(col, np.int32).astype(np.intc)
+        vl = np.ascontiguousarray(val, np.float64)
+        sc = None if scale is None else np.ascontiguousarray(scale, np.float64)
+        tbc = None if textbegin_per_cell is None else np.ascontiguousarray(textbegin_per_cell, np.float64)
+        n_rec = (n_steps + rec_every - 1) // rec_every if rec_every > 0 else 0
+        trace = np.zeros((n, n_rec)) if n_rec else None
+        if act is not None:
+            assert act.dtype == np.float64 and act.flags.c_contiguous and act.size == n
+        rc = self.L.cmo_mono_run(model, _ptr(P), _ptr(T), n, _ptr(blocks), _ptr(Vm), len(het), idx, _ptr(hv),
+                                 rp.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                                 cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(vl), _ptr(sc),
+                                 uniform_scale, n_steps, dt, t0, textbegin, _ptr(tbc), textlen, bcl, amp, _ptr(act),
+                                 act_threshold, vm_range, rec_every, _ptr(trace), n_threads)
+        if rc != 0:
+            raise FloatingPointError(f"oracle monodomain run failed rc={rc}")
         return trace
 
 

@@ -14,6 +14,7 @@
  * against the committed golden vectors. Used only by tests/, bench.py's CPU baseline and
  * __graft_entry__.smoke() as the checker; never by the product.
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers under -std=c11 */
 #include "cm_oracle.h"
 
 #include <math.h>
@@ -1212,5 +1213,124 @@ int cmo_run(int model, const double *P, const double *tables, long n_cells, doub
   for (int k = 0; k < n_threads; k++) bad |= args[k].bad;
   free(args);
   free(th);
+  return bad ? -3 : 0;
+}
+
+/* ---------------------------------------------------------------- monodomain coupling */
+/* The explicit monodomain step of acCELLerate::IntraStep (acCELLerate.cpp:1839-2005; no mass
+ * matrix, no Gauss points, no implicit smoothing, Godunov current scheme):
+ *   B = A * Vm                           MatMult (1849), row entries summed in CSR order
+ *   i_ext = B * scale + stimulus         nA/cell conversion (1880-1887), conditions (1892)
+ *   dVm = Calc(dt, Vm, i_ext, 1, 1)      CalcCellModels (1757-1770)
+ *   Vm += dVm, NaN / range check         (1930-1949)
+ *   act = t where act == -1 and Vm >= threshold   (1997-2005)
+ * The stimulus follows the driver rule (CellModel.h:405-419) with per-cell first times. */
+typedef struct {
+  int model;
+  const double *P, *tables;
+  long n_cells, lo, hi;
+  double *blocks, *v_old, *v_new, *B;
+  int n_het;
+  const int *het_idx;
+  const double *het_vals;
+  const long *rowptr;
+  const int *col;
+  const double *val, *scale;
+  double uniform_scale;
+  long n_steps;
+  double dt, t0, textlen, bcl, amp, act_threshold, vm_range;
+  double *tb, *act;
+  long rec_every;
+  double *trace;
+  pthread_barrier_t *bar;
+  int bad;
+} mono_args;
+
+static void *mono_range(void *argp) {
+  mono_args *a = (mono_args *)argp;
+  const int np = cmo_n_params(a->model), ns = cmo_state_doubles(a->model);
+  double *Pc = (double *)malloc(np * sizeof(double));
+  const long n_rec = a->rec_every > 0 ? (a->n_steps + a->rec_every - 1) / a->rec_every : 0;
+  double *vo = a->v_old, *vn = a->v_new;
+  double t = a->t0;
+  for (long s = 0; s < a->n_steps; s++) {
+    for (long i = a->lo; i < a->hi; i++) {
+      double b = 0.0;
+      for (long e = a->rowptr[i]; e < a->rowptr[i + 1]; e++) b += a->val[e] * vo[a->col[e]];
+      a->B[i] = b;
+      if (a->trace && a->rec_every > 0 && s % a->rec_every == 0) a->trace[i * n_rec + s / a->rec_every] = vo[i];
+    }
+    pthread_barrier_wait(a->bar);
+    for (long c = a->lo; c < a->hi; c++) {
+      memcpy(Pc, a->P, np * sizeof(double));
+      for (int k = 0; k < a->n_het; k++) Pc[a->het_idx[k]] = a->het_vals[(size_t)k * a->n_cells + c];
+      double stim = 0.0;
+      if (t >= a->tb[c]) {
+        stim = a->amp;
+        if (t >= a->tb[c] + a->textlen) a->tb[c] += a->bcl;
+      }
+      const double i_ext = a->B[c] * (a->scale ? a->scale[c] : a->uniform_scale) + stim;
+      double *blk = a->blocks + (size_t)c * ns;
+      double dv;
+      if (a->model == CMO_TT2) dv = tt2_calc(Pc, a->tables, blk, a->dt, vo[c], i_ext);
+      else if (a->model == CMO_CRN) dv = crn_calc(Pc, a->tables, blk, a->dt, vo[c], i_ext, 1.0);
+      else dv = ord_calc(Pc, blk, a->dt, vo[c], i_ext, 1.0);
+      const double v = vo[c] + dv;
+      vn[c] = v;
+      if (isnan(v) || (a->vm_range > 0.0 && (v > a->vm_range || v < -a->vm_range))) a->bad = 1;
+      if (a->act && a->act[c] == -1.0 && v >= a->act_threshold) a->act[c] = t;
+    }
+    pthread_barrier_wait(a->bar);
+    double *tmp = vo;
+    vo = vn;
+    vn = tmp;
+    t += a->dt;
+  }
+  free(Pc);
+  return 0;
+}
+
+int cmo_mono_run(int model, const double *P, const double *tables, long n_cells, double *blocks, double *Vm,
+                 int n_het, const int *het_idx, const double *het_vals, const long *rowptr, const int *col,
+                 const double *val, const double *scale, double uniform_scale, long n_steps, double dt, double t0,
+                 double textbegin, const double *textbegin_per_cell, double textlen, double bcl, double amp,
+                 double *act, double act_threshold, double vm_range, long rec_every, double *trace, int n_threads) {
+  if (cmo_n_params(model) < 0 || n_cells <= 0) return -1;
+  if (n_threads < 1) n_threads = 1;
+  if (n_threads > n_cells) n_threads = (int)n_cells;
+  double *v2 = (double *)malloc(n_cells * sizeof(double));
+  double *B = (double *)malloc(n_cells * sizeof(double));
+  double *tb = (double *)malloc(n_cells * sizeof(double));
+  for (long c = 0; c < n_cells; c++) tb[c] = textbegin_per_cell ? textbegin_per_cell[c] : textbegin;
+  mono_args *args = (mono_args *)calloc(n_threads, sizeof(mono_args));
+  pthread_t *th = (pthread_t *)calloc(n_threads, sizeof(pthread_t));
+  pthread_barrier_t bar;
+  pthread_barrier_init(&bar, 0, n_threads);
+  for (int k = 0; k < n_threads; k++) {
+    mono_args *a = &args[k];
+    a->model = model; a->P = P; a->tables = tables; a->n_cells = n_cells;
+    a->lo = n_cells * k / n_threads; a->hi = n_cells * (k + 1) / n_threads;
+    a->blocks = blocks; a->v_old = Vm; a->v_new = v2; a->B = B;
+    a->n_het = n_het; a->het_idx = het_idx; a->het_vals = het_vals;
+    a->rowptr = rowptr; a->col = col; a->val = val; a->scale = scale; a->uniform_scale = uniform_scale;
+    a->n_steps = n_steps; a->dt = dt; a->t0 = t0; a->textlen = textlen; a->bcl = bcl; a->amp = amp;
+    a->act_threshold = act_threshold; a->vm_range = vm_range; a->tb = tb; a->act = act;
+    a->rec_every = rec_every; a->trace = trace; a->bar = &bar;
+  }
+  if (n_threads == 1) {
+    mono_range(&args[0]);
+  } else {
+    for (int k = 0; k < n_threads; k++) pthread_create(&th[k], 0, mono_range, &args[k]);
+    for (int k = 0; k < n_threads; k++) pthread_join(th[k], 0);
+  }
+  if (n_steps % 2) memcpy(Vm, v2, n_cells * sizeof(double)); /* the last step wrote the second buffer */
+  int bad = 0;
+  for (int k = 0; k < n_threads; k++) bad |= args[k].bad;
+  pthread_barrier_destroy(&bar);
+  free(args);
+  free(th);
+  free(v2);
+  free(B);
+  free(tb);
   return bad ? -3 : 0;
 }

@@ -52,6 +52,17 @@ int cmo_run(int model, const double *P, const double *tables, long n_cells, doub
             double textbegin, const double *textbegin_per_cell, double textlen, double bcl, double amp,
             long rec_every, double *trace, int n_threads);
 
+/* Explicit monodomain steps (acCELLerate::IntraStep, Godunov): per step B = A*Vm (CSR, row
+ * entries summed in order), i_ext = B*scale + stimulus, Vm += Calc(dt, Vm, i_ext, 1, 1), then
+ * activation times (act[c] = t where act[c] == -1 and the new Vm >= act_threshold). scale NULL:
+ * uniform_scale. trace (optional): Vm before every rec_every-th step. Returns -3 when a Vm became
+ * NaN or left +-vm_range (vm_range > 0). */
+int cmo_mono_run(int model, const double *P, const double *tables, long n_cells, double *blocks, double *Vm,
+                 int n_het, const int *het_idx, const double *het_vals, const long *rowptr, const int *col,
+                 const double *val, const double *scale, double uniform_scale, long n_steps, double dt, double t0,
+                 double textbegin, const double *textbegin_per_cell, double textlen, double bcl, double amp,
+                 double *act, double act_threshold, double vm_range, long rec_every, double *trace, int n_threads);
+
 #ifdef __cplusplus
 }
 #endif
