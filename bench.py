@@ -70,6 +70,16 @@ ORD_CELLS = 2048 * 2048
 ORD_BCL = 1.0
 ORD_MIXED_BYTES_PER_CELL_STEP = 2 * (35 + 12) * 4 + 2 * 2 * 4 + 3 * 4
 ORD_FP64_BYTES_PER_CELL_STEP = 2 * 41 * 8 + 2 * 8 + 3 * 8
+# Tissue leg (monodomain coupling): a 256 x 256 x 64 slab of TT2 epi cells on a 0.1 mm grid
+# (D = 0.1 mm^2/ms, 7-point operator, no-flux faces), the x < 3 planes stimulated once. Mixed
+# form per node-step: 21 state planes r+w (168 B), Vm hi/lo read + new hi/lo written (16 B), 3
+# FP32 conductances (12 B), operator row: 7 entries x (4 B column + 4 B value) (56 B) + row sum
+# (4 B), per-cell first-stimulus time (8 B), neighbours' Vm from cache (counted once, 4 B).
+TISSUE_DIMS = (256, 256, 64)
+TISSUE_MIXED_BYTES = 168 + 16 + 12 + 56 + 4 + 8 + 4
+# FP64 form: 18 states r+w (288 B), Vm r + w (16 B), 3 conductances (24 B), 7 x (4 + 8 B) (84 B),
+# stimulus time (8 B), neighbours (8 B).
+TISSUE_FP64_BYTES = 288 + 16 + 24 + 84 + 8 + 8
 FULL_CELLS = 1 << 24
 FULL_INSTANCES = 64
 FULL_BCL = 0.5
@@ -626,6 +636,77 @@ def ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak=None, cpu_se
     return out
 
 
+def tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind):
+    """Monodomain coupling: the intra product fused with the TT2 update, Godunov step, range check
+    and activation times (cm_batch_run_diffuse) on a 4,194,304-node slab; the same step split
+    into cm_diffusion_apply + cm_batch_step_update_act beside it; the FP64 form."""
+    from cardiomechanics_gb300 import workloads as W
+    nx, ny, nz = TISSUE_DIMS if args.tissue_dims is None else tuple(args.tissue_dims)
+    n = nx * ny * nz
+    rp, col, val = W.grid_laplacian(nx, ny, nz)
+    d = cm.Diffusion(rp, col, val, uniform_scale=W.COUPLING_SCALE[5])
+    del rp, col, val
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    sc = W.conductance_scales(5, n, 3, 0.95, 1.05)
+    tb = torch.tensor(np.where(np.arange(n) % nx < 3, 0.0, 1e9), device="cuda")
+    out = {"workload": f"tt2006-epi-slab-{nx}x{ny}x{nz}", "nodes": n, "grid_mm": 0.1, "D_mm2_per_ms": 0.1,
+           "operator": "7-point finite differences, no-flux faces", "stimulus": "x < 3 planes, 2 x -52 pA/pF x 1 ms"}
+    kw = dict(textlen=1e-3, bcl=1e9, amplitude=2 * W.TT2_STIM_NA, act_threshold=-0.02, vm_range=0.2)
+    for prec, steps, name in ((cm.MIXED, args.tissue_steps, "fused_mixed"), (cm.FP64, args.fp64_steps, "fused_fp64")):
+        b = cm.Batch(p, n, prec, stream=stream.cuda_stream)
+        for k, h in enumerate(W.TT2_HETERO):
+            b.add_hetero_value(h, p.get(h) * sc[k])
+        vm = torch.tensor(b.init_vm(), device="cuda")
+        act = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+        tbc = tb.clone()
+        b.run_diffuse(d, vm, 3, textbegin_per_cell=tbc, act=act, **kw)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run_diffuse(d, vm, steps, t0=3 * DT, textbegin_per_cell=tbc, act=act, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        bps = TISSUE_MIXED_BYTES if prec == cm.MIXED else TISSUE_FP64_BYTES
+        achieved = bps * n * steps / sec / 1e9
+        out[name] = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+                     "activated": int((act >= 0).sum().item()), "audit_mask": b.audit(),
+                     "gpu_launches": steps + 2,
+                     "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                             "peak_kind": peak_kind, "bytes_per_node_step": bps}}
+        del b, vm, act
+        torch.cuda.empty_cache()
+    # the split form a caller would write without the fused entry point (mixed batch, device arrays)
+    b = cm.Batch(p, n, cm.MIXED, stream=stream.cuda_stream)
+    for k, h in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(h, p.get(h) * sc[k])
+    vm = torch.tensor(b.init_vm(), device="cuda")
+    act = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    iext = torch.zeros(n, dtype=torch.float64, device="cuda")
+    steps = max(10, args.tissue_steps // 5)
+    for k in range(3):
+        d.apply(vm, iext)
+        b.calc_update_act(DT, vm, act, k * DT, -0.02, i_ext=iext)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(steps):
+        d.apply(vm, iext)
+        b.calc_update_act(DT, vm, act, (3 + k) * DT, -0.02, i_ext=iext)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    out["split_mixed"] = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+                          "note": "cm_diffusion_apply + cm_batch_step_update_act per step (two launches, "
+                                  "i_ext through HBM, FP64 Vm), each call synchronising"}
+    out["fused_vs_split"] = out["fused_mixed"]["value"] / out["split_mixed"]["value"]
+    del b, vm, act, iext, d
+    torch.cuda.empty_cache()
+    return out
+
+
 def precision_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     """Precision form: 4,194,304 cells, the HBM-bound plain kernel (autotuned launch shape)."""
     p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
@@ -677,7 +758,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
-                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord"],
+                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tissue"],
                     help="run one leg only (profiler captures); the contract's JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
@@ -692,6 +773,9 @@ def main():
     ap.add_argument("--ord-steps", type=int, default=500, help="timed steps of the O'Hara-Rudy mixed form")
     ap.add_argument("--ord-cells", type=int, default=ORD_CELLS, help="O'Hara-Rudy cells (fewer only for captures)")
     ap.add_argument("--no-ord", action="store_true")
+    ap.add_argument("--tissue-steps", type=int, default=500, help="timed steps of the coupled (tissue) leg")
+    ap.add_argument("--tissue-dims", type=int, nargs=3, default=None, help="slab size (fewer nodes only for captures)")
+    ap.add_argument("--no-tissue", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -719,6 +803,9 @@ def main():
         return
     if args.only == "mixed":
         print(json.dumps(precision_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
+        return
+    if args.only == "tissue":
+        print(json.dumps(tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
         return
     if args.only == "ord":
         print(json.dumps(ord_leg(cm, torch, stream, args, hbm_peak, peak_kind,
@@ -755,6 +842,7 @@ def main():
     bat = None
     if not args.no_batched:
         bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
+    tissue = None if args.no_tissue else tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)
     ordl = None
     if not args.no_ord:
         ordl = ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak,
@@ -790,6 +878,7 @@ def main():
             "learned_form": learned,
             "batched": bat,
             "ohara_rudy": ordl,
+            "tissue": tissue,
             "fp32_fma_peak_tflops_measured": fp32_peak,
             "cpu_baseline": cpu,
             "gpu_launches": full["gpu_launches"],

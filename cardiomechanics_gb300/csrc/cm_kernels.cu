@@ -29,13 +29,32 @@ __device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
 }
 
 // Monodomain coupling current of cell c: scale_c * (A x)_c with A's row c in its 32-row slice
-// (acCELLerate.cpp:1849 MatMult and 1880-1887 conversion). FP64: entries summed in CSR order.
-// Padding entries of a slice carry value 0 and the row's own column.
+// (acCELLerate.cpp:1849 MatMult and 1880-1887 conversion). Padding entries of a slice carry
+// value 0 and the row's own column. The first kCouplingBatch entries of the row are fetched in
+// two rounds -- all columns and values, then all neighbour potentials -- so a row costs two
+// memory latencies rather than two per entry; longer rows continue entry by entry.
+constexpr int kCouplingBatch = 8;
+
+// FP64: entries summed in CSR order.
 __device__ __forceinline__ double coupling_fp64(const StepIO &io, const double *x, int64_t c) {
   const int64_t s = c >> 5;
-  const int64_t e1 = io.sl_ptr[s + 1];
+  const int64_t e0 = io.sl_ptr[s] + (c & 31), e1 = io.sl_ptr[s + 1];
+  int32_t cj[kCouplingBatch];
+  double aj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) {
+    const int64_t e = e0 + 32 * k;
+    cj[k] = e < e1 ? io.sl_col[e] : (int32_t)c;
+    aj[k] = e < e1 ? io.sl_val64[e] : 0.0;
+  }
+  double xj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) xj[k] = __ldg(x + cj[k]);
   double acc = 0.0;
-  for (int64_t e = io.sl_ptr[s] + (c & 31); e < e1; e += 32) acc += io.sl_val64[e] * __ldg(x + io.sl_col[e]);
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++)
+    if (e0 + 32 * k < e1) acc += aj[k] * xj[k];
+  for (int64_t e = e0 + 32 * kCouplingBatch; e < e1; e += 32) acc += io.sl_val64[e] * __ldg(x + io.sl_col[e]);
   return acc * (io.dscale64 ? __ldg(io.dscale64 + c) : io.dscale_u);
 }
 
@@ -45,25 +64,40 @@ __device__ __forceinline__ double coupling_fp64(const StepIO &io, const double *
 template <typename I>
 __device__ __forceinline__ float coupling_f32(const StepIO &io, I c) {
   const float *x = io.vm_hi;
-  const float xc = x[c];
   const int64_t s = (int64_t)c >> 5;
-  const int64_t e1 = io.sl_ptr[s + 1];
+  const int64_t e0 = io.sl_ptr[s] + (c & 31), e1 = io.sl_ptr[s + 1];
+  int32_t cj[kCouplingBatch];
+  float aj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) {
+    const int64_t e = e0 + 32 * k;
+    cj[k] = e < e1 ? io.sl_col[e] : (int32_t)c;
+    aj[k] = e < e1 ? io.sl_val32[e] : 0.f;
+  }
+  const float xc = x[c];
+  float xj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) xj[k] = x[cj[k]];
   float acc = __ldg(io.rowsum32 + c) * xc;
-  for (int64_t e = io.sl_ptr[s] + (c & 31); e < e1; e += 32) acc += io.sl_val32[e] * (x[io.sl_col[e]] - xc);
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) acc += aj[k] * (xj[k] - xc);
+  for (int64_t e = e0 + 32 * kCouplingBatch; e < e1; e += 32) acc += io.sl_val32[e] * (x[io.sl_col[e]] - xc);
   return acc * (io.dscale32 ? __ldg(io.dscale32 + c) : (float)io.dscale_u);
 }
 
-// i_external of an FP64 cell update: the stimulus plus, with a coupling operator, its current.
+// i_external of a cell update: the stimulus plus, in coupled kernels (kCoupled, launched for
+// cm_batch_run_diffuse only), the coupling current.
+template <bool kCoupled>
 __device__ __forceinline__ double iext_fp64(const StepIO &io, int64_t c) {
   double i = stim_for_cell(io, c);
-  if (io.sl_ptr) i += coupling_fp64(io, io.vm, c);
+  if (kCoupled) i += coupling_fp64(io, io.vm, c);
   return i;
 }
 
-template <typename I>
+template <bool kCoupled, typename I>
 __device__ __forceinline__ float iext_f32(const StepIO &io, I c) {
   float i = (float)stim_for_cell(io, c);
-  if (io.sl_ptr) i += coupling_f32<I>(io, c);
+  if (kCoupled) i += coupling_f32<I>(io, c);
   return i;
 }
 
@@ -94,7 +128,7 @@ __device__ __forceinline__ void finish_acc(const DevBatch &b, I c, Acc v, uint32
   }
 }
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled>
 __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const StepIO io) {
   const int64_t ld = b.ld;
   const double *const *het = (const double *const *)b.het;
@@ -118,7 +152,7 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
     g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + c) : C.g_to;
     g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + c) : C.g_CaL;
     const double V = __ldg(io.vm + c);
-    const double iext = iext_fp64(io, c);
+    const double iext = iext_fp64<kCoupled>(io, c);
     uint32_t audit = 0;
     const int vi = vrow_fp64(V * 1000, audit);
     TT2Diag<double> dg;
@@ -134,10 +168,10 @@ __global__ void __launch_bounds__(128) tt2_fp64_kernel(const DevBatch b, const S
   }
 }
 
-template <typename I, int kBlock, int kMinB>
+template <typename I, int kBlock, int kMinB, bool kCoupled = false>
 __global__ void __launch_bounds__(kBlock, kMinB) tt2_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = iext_f32<I>(io, c);
+    const float iext = iext_f32<kCoupled>(io, c);
     uint32_t audit = 0;
     if (io.vm_hi) {
       Acc v{io.vm_hi[c], io.vm_lo[c]};
@@ -151,7 +185,7 @@ __global__ void __launch_bounds__(kBlock, kMinB) tt2_mixed_kernel(const DevBatch
   }
 }
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled>
 __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const StepIO io) {
   const int64_t ld = b.ld;
   const double *const *het = (const double *const *)b.het;
@@ -174,7 +208,7 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
     g.g_bNa = het[HC_g_bNa] ? __ldg(het[HC_g_bNa] + c) : C.g_bNa;
     g.g_bCa = het[HC_g_bCa] ? __ldg(het[HC_g_bCa] + c) : C.g_bCa;
     const double V = __ldg(io.vm + c);
-    const double iext = iext_fp64(io, c);
+    const double iext = iext_fp64<kCoupled>(io, c);
     const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
     uint32_t audit = 0;
     const int vi = vrow_fp64(V * 1000.0, audit);
@@ -191,10 +225,10 @@ __global__ void __launch_bounds__(128) crn_fp64_kernel(const DevBatch b, const S
   }
 }
 
-template <typename I, int kBlock, int kMinB>
+template <typename I, int kBlock, int kMinB, bool kCoupled = false>
 __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = iext_f32<I>(io, c);
+    const float iext = iext_f32<kCoupled>(io, c);
     const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
     uint32_t audit = 0;
     if (io.vm_hi) {
@@ -209,22 +243,22 @@ __global__ void __launch_bounds__(kBlock, kMinB) crn_mixed_kernel(const DevBatch
   }
 }
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled>
 __global__ void __launch_bounds__(128) ord_fp64_kernel(const DevBatch b, const StepIO io) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
     ORDStore64 x{b.s64 + c, b.ld, kDiag ? b.diag + c : nullptr};
     const double V = __ldg(io.vm + c);
-    const double iext = iext_fp64(io, c);
+    const double iext = iext_fp64<kCoupled>(io, c);
     const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
     const double dV = ord_calc<double>(b.ord_64, x, ord_het<double>(b, b.ord_64, c), V, iext, stretch);
     finish(b, io, c, V, dV, 0u);
   }
 }
 
-template <typename I, int kBlock, int kMinB>
+template <typename I, int kBlock, int kMinB, bool kCoupled = false>
 __global__ void __launch_bounds__(kBlock, kMinB) ord_mixed_kernel(const DevBatch b, const StepIO io) {
   for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
-    const float iext = iext_f32<I>(io, c);
+    const float iext = iext_f32<kCoupled>(io, c);
     const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
     if (io.vm_hi) {
       Acc v{io.vm_hi[c], io.vm_lo[c]};
@@ -298,6 +332,12 @@ void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s)
 
 template <typename I>
 void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, cudaStream_t s) {
+  if (io.sl_ptr) {  // coupled runs: one shape (256 threads, 128 registers)
+    if (b.model == 5) tt2_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
+    else if (b.model == 12) ord_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
+    else crn_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
+    return;
+  }
   switch (v) {
     case 1: launch_mixed<I, 128, 5>(b, io, grid, s); break;
     case 2: launch_mixed<I, 256, 3>(b, io, grid, s); break;
@@ -323,14 +363,14 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     const int64_t cap = (int64_t)sm_count() * 16;
     const int grid = (int)(need < cap ? need : cap);
     if (b.model == 5) {
-      if (diag) tt2_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
-      else tt2_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+      if (diag) if (io.sl_ptr) tt2_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else tt2_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
+      else if (io.sl_ptr) tt2_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else tt2_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);
     } else if (b.model == 12) {
-      if (diag) ord_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
-      else ord_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+      if (diag) if (io.sl_ptr) ord_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else ord_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
+      else if (io.sl_ptr) ord_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else ord_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);
     } else {
-      if (diag) crn_fp64_kernel<true><<<grid, block, 0, s>>>(b, io);
-      else crn_fp64_kernel<false><<<grid, block, 0, s>>>(b, io);
+      if (diag) if (io.sl_ptr) crn_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else crn_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
+      else if (io.sl_ptr) crn_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else crn_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);
     }
     return cudaGetLastError();
   }
@@ -340,7 +380,7 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     if (staged_supported(b, io)) return launch_staged(b, io, variant == n_plain ? 256 : 128, grid_mode, s);
     variant = 0;
   }
-  const Shape sh = kShapes[variant];
+  const Shape sh = io.sl_ptr ? Shape{256, 2} : kShapes[variant];  // coupled runs: one shape
   const int64_t need = (b.n + sh.block - 1) / sh.block;
   // grid_mode 0: one thread per cell; k > 0: grid-stride over k blocks per SM
   const int64_t cap = grid_mode > 0 ? (int64_t)sm_count() * grid_mode : need;
