@@ -74,12 +74,13 @@ ORD_FP64_BYTES_PER_CELL_STEP = 2 * 41 * 8 + 2 * 8 + 3 * 8
 # (D = 0.1 mm^2/ms, 7-point operator, no-flux faces), the x < 3 planes stimulated once. Mixed
 # form per node-step: 21 state planes r+w (168 B), Vm hi/lo read + new hi/lo written (16 B), 3
 # FP32 conductances (12 B), operator row: 7 entries x (4 B column + 4 B value) (56 B) + row sum
-# (4 B), per-cell first-stimulus time (8 B), neighbours' Vm from cache (counted once, 4 B).
+# (4 B), per-cell first-stimulus time (8 B), activation time read (8 B; written once per cell),
+# neighbours' Vm from cache (counted once, 4 B).
 TISSUE_DIMS = (256, 256, 64)
-TISSUE_MIXED_BYTES = 168 + 16 + 12 + 56 + 4 + 8 + 4
+TISSUE_MIXED_BYTES = 168 + 16 + 12 + 56 + 4 + 8 + 8 + 4
 # FP64 form: 18 states r+w (288 B), Vm r + w (16 B), 3 conductances (24 B), 7 x (4 + 8 B) (84 B),
-# stimulus time (8 B), neighbours (8 B).
-TISSUE_FP64_BYTES = 288 + 16 + 24 + 84 + 8 + 8
+# stimulus time (8 B), activation time (8 B), neighbours (8 B).
+TISSUE_FP64_BYTES = 288 + 16 + 24 + 84 + 8 + 8 + 8
 FULL_CELLS = 1 << 24
 FULL_INSTANCES = 64
 FULL_BCL = 0.5

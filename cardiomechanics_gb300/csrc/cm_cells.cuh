@@ -10,6 +10,21 @@
 
 namespace cm {
 
+// Stimulus current of cell c: the reference driver's rule (CellModel.h:405-419) with per-cell
+// first stimulus times, advanced in place; else the per-cell array or the uniform value.
+__device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
+  if (io.tb_cell) {
+    const double tb = io.tb_cell[c];
+    double i_ext = 0.0;
+    if (io.t >= tb) {
+      i_ext = io.amp;
+      if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
+    }
+    return i_ext;
+  }
+  return io.iext ? __ldg(io.iext + c) : io.iext_uniform;
+}
+
 template <typename I>
 __device__ __forceinline__ float tt2_mixed_cell(const DevBatch &b, I c, float V, float iext, uint32_t &audit) {
   const I ld = (I)b.ld;

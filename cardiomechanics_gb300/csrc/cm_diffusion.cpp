@@ -15,6 +15,7 @@ using namespace cm;
 
 struct cm_diffusion_s {
   int64_t n = 0, n_slices = 0, entries = 0;
+  int wmax = 0;  // widest slice
   int64_t *sl_ptr = nullptr;  // n_slices + 1 entry offsets
   int32_t *sl_col = nullptr;
   double *val64 = nullptr;
@@ -32,6 +33,7 @@ struct cm_diffusion_s {
     io.dscale64 = scale64;
     io.dscale32 = scale32;
     io.dscale_u = uniform;
+    io.sl_wmax = wmax;
   }
 };
 
@@ -90,9 +92,13 @@ int cm_diffusion_create(cm_diffusion_t *out, int64_t n, const int64_t *rowptr, c
     ptr[s + 1] = ptr[s] + 32 * w;
   }
   const int64_t ent = ptr[ns];
+  int64_t wmax = 0;
+  for (int64_t s = 0; s < ns; s++) wmax = std::max(wmax, (ptr[s + 1] - ptr[s]) / 32);
+  // per-node planes padded to whole 256-cell tiles (the staged kernel copies whole tiles)
+  const int64_t npad = ((n + 255) / 256) * 256;
   std::vector<int32_t> c32(ent);
   std::vector<double> v64(ent, 0.0);
-  std::vector<float> v32(ent, 0.f), rs(n), sc32;
+  std::vector<float> v32(ent, 0.f), rs(npad, 0.f), sc32;
   for (int64_t s = 0; s < ns; s++) {
     const int64_t w = (ptr[s + 1] - ptr[s]) / 32;
     for (int64_t r = 0; r < 32; r++) {
@@ -119,6 +125,7 @@ int cm_diffusion_create(cm_diffusion_t *out, int64_t n, const int64_t *rowptr, c
   d->n = n;
   d->n_slices = ns;
   d->entries = ent;
+  d->wmax = (int)std::min<int64_t>(wmax, 1 << 20);
   d->uniform = uniform_scale;
   int rc = upload(&d->sl_ptr, ptr);
   if (!rc) rc = upload(&d->sl_col, c32);
@@ -127,7 +134,8 @@ int cm_diffusion_create(cm_diffusion_t *out, int64_t n, const int64_t *rowptr, c
   if (!rc) rc = upload(&d->rowsum32, rs);
   if (!rc && scale) {
     std::vector<double> s64(scale, scale + n);
-    sc32.assign(scale, scale + n);
+    sc32.assign(npad, 0.f);
+    std::copy(scale, scale + n, sc32.begin());
     rc = upload(&d->scale64, s64);
     if (!rc) rc = upload(&d->scale32, sc32);
   }

@@ -14,20 +14,6 @@ namespace cm {
 
 namespace {
 
-__device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
-  if (io.tb_cell) {
-    // reference driver stimulus (CellModel.h:405-419), per-cell first stimulus time
-    const double tb = io.tb_cell[c];
-    double i_ext = 0.0;
-    if (io.t >= tb) {
-      i_ext = io.amp;
-      if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
-    }
-    return i_ext;
-  }
-  return io.iext ? __ldg(io.iext + c) : io.iext_uniform;
-}
-
 // Monodomain coupling current of cell c: scale_c * (A x)_c with A's row c in its 32-row slice
 // (acCELLerate.cpp:1849 MatMult and 1880-1887 conversion). Padding entries of a slice carry
 // value 0 and the row's own column. The first kCouplingBatch entries of the row are fetched in
@@ -374,6 +360,8 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     }
     return cudaGetLastError();
   }
+  // coupled runs of TT2 / Courtemanche: the staged kernel with the operator staged too
+  if (io.sl_ptr && coupled_staged_supported(b, io)) return launch_coupled_staged(b, io, s);
   if (variant < 0 || variant >= n_shape_variants()) variant = 0;
   const int n_plain = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
   if (variant >= n_plain) {

@@ -70,8 +70,15 @@ struct StepIO {
   const double *dscale64 = nullptr;  // per node, or nullptr for dscale_u
   const float *dscale32 = nullptr;
   double dscale_u = 0.0;
+  int sl_wmax = 0;  // widest slice (entries per row); rowsum32 / dscale32 padded to whole 256-cell tiles
   float *vm_hi_out = nullptr, *vm_lo_out = nullptr;  // mixed: new Vm planes (nullptr: in place)
 };
+
+// Coupled runs of TT2 / Courtemanche mixed batches through the staged kernel (cm_staged.cu):
+// the tile's operator slices are staged with its state. false when the batch or the operator
+// does not fit (then the register kernel runs).
+bool coupled_staged_supported(const DevBatch &b, const StepIO &io);
+cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, cudaStream_t s);
 
 // y = scale * (A x) for a coupling operator (cm_diffusion_apply); io carries the operator.
 cudaError_t launch_diffusion_apply(const StepIO &io, const double *x, double *y, int64_t n, cudaStream_t s);

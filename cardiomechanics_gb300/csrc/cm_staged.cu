@@ -96,7 +96,163 @@ cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_
   return cudaGetLastError();
 }
 
+// Coupled runs (cm_batch_run_diffuse): the staged kernel plus the tile's monodomain operator.
+// A tile of kThreads cells is kThreads / 32 consecutive slices, whose entries are one contiguous
+// run of the operator's column and value arrays (each slice 32 * width entries, so the run starts
+// and ends on 128-byte boundaries); both runs are bulk-copied with the state, next to the row
+// sums and the per-node scales (padded to whole tiles by cm_diffusion_create). Only the
+// neighbours' potentials are read from global memory (the previous step's hi plane); the new Vm
+// pair goes to the other pair of planes.
+constexpr int kCoupledWmax = 16;  // widest operator slice staged (entries per row)
+
+template <int kModel, int kThreads>
+__global__ void __launch_bounds__(kThreads, 2) coupled_staged_kernel(const DevBatch b, const StepIO io) {
+  constexpr int NS = StagedVars<kModel>::kState;
+  constexpr int NVMAX = NS + 2 + 6 + 2;
+  constexpr int kSlices = kThreads / 32;
+  extern __shared__ __align__(128) float stage[];  // [2][NVMAX * kThreads + 2 * W * kThreads]
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_abort;
+  __shared__ int s_off[2][kSlices + 1];  // slice entry offsets from the tile's first entry
+  const int64_t ld = b.ld;
+  const int n = (int)b.n;
+  const int n_tiles = (n + kThreads - 1) / kThreads;
+  const int64_t n_slices = ((int64_t)n + 31) / 32;
+  const int W = io.sl_wmax;
+  const size_t buf_floats = (size_t)NVMAX * kThreads + 2 * (size_t)W * kThreads;
+  int het_pos[6];
+  int nv = NS + 2;
+#pragma unroll
+  for (int k = 0; k < 6; k++) het_pos[k] = b.het[k] ? nv++ : -1;
+  const int rs_pos = nv++;
+  const int sc_pos = io.dscale32 ? nv++ : -1;
+  const uint32_t plane_bytes = (uint32_t)nv * kThreads * 4u;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int tile, int buf) {
+    float *dst = stage + (size_t)buf * buf_floats;
+    const int64_t c0 = (int64_t)tile * kThreads;
+    const int64_t s0 = c0 / 32, s1 = s0 + kSlices < n_slices ? s0 + kSlices : n_slices;
+    const int64_t e0 = io.sl_ptr[s0], e1 = io.sl_ptr[s1];
+    for (int k = 0; k <= kSlices; k++) s_off[buf][k] = (int)(io.sl_ptr[s0 + k < s1 ? s0 + k : s1] - e0);
+    const uint32_t ent_bytes = (uint32_t)(e1 - e0) * 4u;
+    mbar_expect_tx(&bar[buf], plane_bytes + 2u * ent_bytes);
+    for (int v = 0; v < NS; v++) bulk_g2s(dst + v * kThreads, b.s32 + v * ld + c0, kThreads * 4u, &bar[buf]);
+    bulk_g2s(dst + NS * kThreads, io.vm_hi + c0, kThreads * 4u, &bar[buf]);
+    bulk_g2s(dst + (NS + 1) * kThreads, io.vm_lo + c0, kThreads * 4u, &bar[buf]);
+    for (int k = 0; k < 6; k++)
+      if (het_pos[k] >= 0)
+        bulk_g2s(dst + het_pos[k] * kThreads, (const float *)b.het[k] + c0, kThreads * 4u, &bar[buf]);
+    bulk_g2s(dst + rs_pos * kThreads, io.rowsum32 + c0, kThreads * 4u, &bar[buf]);
+    if (sc_pos >= 0) bulk_g2s(dst + sc_pos * kThreads, io.dscale32 + c0, kThreads * 4u, &bar[buf]);
+    if (ent_bytes) {
+      float *ent = dst + (size_t)NVMAX * kThreads;
+      bulk_g2s(ent, io.sl_col + e0, ent_bytes, &bar[buf]);
+      bulk_g2s(ent + (size_t)W * kThreads, io.sl_val32 + e0, ent_bytes, &bar[buf]);
+    }
+  };
+  int it = 0;
+  int t = blockIdx.x;
+  if (t < n_tiles && threadIdx.x == 0) issue(t, 0);
+  for (; t < n_tiles; t += gridDim.x, it++) {
+    const int buf = it & 1;
+    const int next = t + gridDim.x;
+    // the cell's stimulus time and activation entry do not depend on the stage: read them now,
+    // while the tile's copies may still be landing
+    const int c = t * kThreads + threadIdx.x;
+    const double tb = (io.tb_cell && c < n) ? io.tb_cell[c] : 0.0;
+    const double a0 = (io.act && c < n) ? io.act[c] : 0.0;
+    __syncthreads();  // every thread is done with buffer buf ^ 1 (used two tiles ago)
+    if (next < n_tiles && threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      issue(next, buf ^ 1);
+    }
+    if (!mbar_wait(&bar[buf], (uint32_t)((it >> 1) & 1))) {
+      s_abort = 1;
+      atomicOr(b.audit_or, kAuditTimeout);
+    }
+    __syncthreads();
+    if (s_abort) {
+      if (next < n_tiles) mbar_wait(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      return;
+    }
+    const float *base = stage + (size_t)buf * buf_floats;
+    const float *S = base + threadIdx.x;
+    if (c >= n) continue;
+    // coupling current: rowsum x_c + sum_j A_cj (x_j - x_c), entries from the stage
+    const int32_t *ecol = (const int32_t *)(base + (size_t)NVMAX * kThreads);
+    const float *eval = base + (size_t)NVMAX * kThreads + (size_t)W * kThreads;
+    const int sl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o0 = s_off[buf][sl] + lane, o1 = s_off[buf][sl + 1];
+    const float xc = S[NS * kThreads];
+    int32_t cj[kCoupledWmax];
+    float aj[kCoupledWmax], xj[kCoupledWmax];
+#pragma unroll
+    for (int k = 0; k < kCoupledWmax; k++) {
+      const int e = o0 + 32 * k;
+      cj[k] = e < o1 ? ecol[e] : c;
+      aj[k] = e < o1 ? eval[e] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kCoupledWmax; k++) xj[k] = io.vm_hi[cj[k]];
+    float acc = S[rs_pos * kThreads] * xc;
+#pragma unroll
+    for (int k = 0; k < kCoupledWmax; k++) acc += aj[k] * (xj[k] - xc);
+    const float scale = sc_pos >= 0 ? S[sc_pos * kThreads] : (float)io.dscale_u;
+    float stim = (float)io.iext_uniform;  // the driver's rule (CellModel.h:405-419), per-cell times
+    if (io.tb_cell) {
+      stim = 0.f;
+      if (io.t >= tb) {
+        stim = (float)io.amp;
+        if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
+      }
+    }
+    const float iext = stim + acc * scale;
+    const Acc v = staged_cell<kModel, kThreads>(b, S, het_pos, c, iext, io.vm_hi_out, io.vm_lo_out);
+    uint32_t audit = 0;
+    if (io.vm_range > 0.0 && fabsf(v.hi) > (float)io.vm_range) audit |= 32u;
+    if (io.act && a0 == -1.0 && v.hi >= (float)io.act_threshold) io.act[c] = io.act_time;
+    if (audit) {
+      atomicOr(b.audit_cell + c, audit);
+      atomicOr(b.audit_or, audit);
+    }
+  }
+}
+
+template <int kModel>
+cudaError_t launch_coupled_t(const DevBatch &b, const StepIO &io, cudaStream_t s) {
+  constexpr int kThreads = 256;
+  constexpr int NVMAX = StagedVars<kModel>::kState + 2 + 6 + 2;
+  const size_t smem = (size_t)2 * ((size_t)NVMAX * kThreads + 2 * (size_t)io.sl_wmax * kThreads) * sizeof(float);
+  const size_t smem_max = (size_t)2 * ((size_t)NVMAX * kThreads + 2 * (size_t)kCoupledWmax * kThreads) * sizeof(float);
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)coupled_staged_kernel<kModel, kThreads>, (int)smem_max, done);
+  if (e != cudaSuccess) return e;
+  const int n_tiles = (int)((b.n + kThreads - 1) / kThreads);
+  int grid = sm_count() * 2;
+  if (grid > n_tiles) grid = n_tiles;
+  if (grid < 1) grid = 1;
+  coupled_staged_kernel<kModel, kThreads><<<grid, kThreads, smem, s>>>(b, io);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+bool coupled_staged_supported(const DevBatch &b, const StepIO &io) {
+  return (b.model == 5 || b.model == 2) && b.precision == 1 && io.sl_ptr && io.sl_val32 && io.rowsum32 &&
+         io.sl_wmax >= 1 && io.sl_wmax <= kCoupledWmax && io.vm_hi && io.vm_hi_out && io.vm_lo == io.vm_hi + b.ld &&
+         io.vm_lo_out == io.vm_hi_out + b.ld && !io.iext && b.ld % 256 == 0 && b.n < (int64_t)1 << 30;
+}
+
+cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, cudaStream_t s) {
+  if (b.n == 0) return cudaSuccess;
+  return b.model == 5 ? launch_coupled_t<5>(b, io, s) : launch_coupled_t<2>(b, io, s);
+}
 
 bool staged_supported(const DevBatch &b, const StepIO &io) {
   return (b.model == 5 || b.model == 2) && b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext &&

@@ -21,9 +21,10 @@ struct StagedVars<2> {
 
 // S: stage + threadIdx.x; planes 0..NS-1 state, NS / NS+1 Vm hi / lo, het_pos[k] the present
 // conductance slots (-1: parameter-set value).
+// Returns the new Vm pair (also written to vm_hi / vm_lo).
 template <int kModel, int kT>
-__device__ __forceinline__ void staged_cell(const DevBatch &b, const float *S, const int (&het_pos)[6], int c,
-                                            float iext, float *vm_hi, float *vm_lo) {
+__device__ __forceinline__ Acc staged_cell(const DevBatch &b, const float *S, const int (&het_pos)[6], int c,
+                                           float iext, float *vm_hi, float *vm_lo) {
   constexpr int NS = StagedVars<kModel>::kState;
   constexpr int kThreads = kT;
   const int64_t ld = b.ld;
@@ -88,6 +89,7 @@ __device__ __forceinline__ void staged_cell(const DevBatch &b, const float *S, c
     atomicOr(b.audit_cell + c, audit);
     atomicOr(b.audit_or, audit);
   }
+  return vm;
 }
 
 }  // namespace cm
