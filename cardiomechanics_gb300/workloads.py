@@ -50,11 +50,14 @@ CRN_STIM_PAPF = 20.0
 # O'Hara-Rudy adds i_external to its total current in uA/uF; its parameter files give
 # amplitude -50 for 1 ms (OHaraRudy_*.ev, GetAmplitude() = amplitude, OHaraRudy.h:84).
 ORD_STIM = -50.0
+# Tomek: the same convention, amplitude -53 for 1 ms (Tomek_*.ev).
+TOM_STIM = -53.0
 
 # Per-cell heterogeneous conductances used by the workloads, by model.
 TT2_HETERO = ("g_Na", "g_Kr", "g_K1")
 CRN_HETERO = ("g_Na", "g_to", "g_CaL")
 ORD_HETERO = ("INaF_Multiplier", "IKr_Multiplier", "IK1_Multiplier")
+TOM_HETERO = ORD_HETERO
 
 # Conductances a per-instance parameter set scales in the batched form, by model (the
 # heterogeneity slots of each model).
@@ -97,7 +100,7 @@ def full_form_instances(seed: int, n_inst: int = 64, total: int = 1 << 24, align
 # (A*Vm in V/s, the local diffusion term being -A*Vm): TT2 takes nA per cell and converts with
 # 2.29656e-2 nA per pA/pF (TenTusscher2.cpp:630), Courtemanche pA/pF, O'Hara-Rudy uA/uF with the
 # sign of an outward current (OHaraRudy.cpp:525-533).
-COUPLING_SCALE = {5: -2.29656e-2, 2: -1.0, 12: 1.0}
+COUPLING_SCALE = {5: -2.29656e-2, 2: -1.0, 12: 1.0, 14: 1.0}
 
 
 def grid_laplacian(nx: int, ny: int, nz: int = 1, d_over_h2: float = 1.0e4):

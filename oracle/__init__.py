@@ -3,7 +3,7 @@
 Two implementations, both FP64 on the CPU:
 
 * ``Port``  -- oracle/cm_oracle.c, a plain-C restatement of the reference's
-  TenTusscher2 / Courtemanche / OHaraRudy Calc and InitTable (see that file for file:line
+  TenTusscher2 / Courtemanche / OHaraRudy / Tomek Calc and InitTable (see that file for file:line
   citations). Builds anywhere with gcc; it is the checker on machines without the
   reference tree and the timed CPU baseline.
 * ``Ref``   -- oracle/_ref/libcmref.so, the reference's own CellModel library compiled
@@ -30,12 +30,13 @@ REF_SO = HERE / "_ref" / "libcmref.so"
 REF_TREE = Path(os.environ.get("CM_REFERENCE_TREE", "/root/reference"))
 GOLDEN = HERE.parent / "tests" / "golden"
 
-TT2, CRN, ORD = 0, 1, 2
-MODEL_NAMES = {TT2: "TenTusscher2", CRN: "CourtemancheEtAl", ORD: "OHaraRudy"}
+TT2, CRN, ORD, TOM = 0, 1, 2, 3
+MODEL_NAMES = {TT2: "TenTusscher2", CRN: "CourtemancheEtAl", ORD: "OHaraRudy", TOM: "Tomek"}
 # Reference ElphyModelType values (ElphyModelBasis.h:62-81).
-REF_EMT = {TT2: 5, CRN: 2, ORD: 12}
-# O'Hara-Rudy cell types of the reference's parameter files (celltype 0 / 1 / 2).
+REF_EMT = {TT2: 5, CRN: 2, ORD: 12, TOM: 14}
+# O'Hara-Rudy and Tomek cell types of the reference's parameter files (celltype 0 / 1 / 2).
 ORD_VARIANTS = ("endo", "epi", "mid")
+TOM_VARIANTS = ORD_VARIANTS
 RTDT = 4000
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -61,8 +62,8 @@ def build_ref() -> Path | None:
 def load_params(model: int, variant: str = "epi") -> dict:
     """Resolved reference parameter set (names -> FP64 values) from the golden fixture.
     For O'Hara-Rudy, variant is the cell type (endo, epi, mid); the other models have one set."""
-    if model == ORD:
-        name = f"params_ord_{variant}.json"
+    if model in (ORD, TOM):
+        name = f"params_{'ord' if model == ORD else 'tom'}_{variant}.json"
     else:
         name = "params_tt2_epi.json" if model == TT2 else "params_crn.json"
     with open(GOLDEN / name) as f:
@@ -239,8 +240,8 @@ class Ref:
     @staticmethod
     def ev_path(model, variant="epi"):
         d = REF_TREE / "electrophysiology" / "data"
-        if model == ORD:
-            return str(d / f"OHaraRudy_{variant}.ev")
+        if model in (ORD, TOM):
+            return str(d / f"{MODEL_NAMES[model]}_{variant}.ev")
         return str(d / ("TenTusscher2_original_Epi.ev" if model == TT2 else "CourtemancheEtAl.ev"))
 
     def create(self, model, dt, n_cells, ev=None):

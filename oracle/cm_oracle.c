@@ -7,6 +7,8 @@
  *                                                                InitTable 282-395)
  *   electrophysiology/src/CellModel/OHaraRudy.cpp               (Init 54-102, Calc 105-663)
  *   electrophysiology/src/CellModel/OHaraRudyParameters.cpp     (Calculate 246-316; no tables)
+ *   electrophysiology/src/CellModel/Tomek.cpp                   (Init 55-107, Calc 110-656)
+ *   electrophysiology/src/CellModel/TomekParameters.cpp         (Calculate 233-302; no tables)
  *   electrophysiology/src/CellModel/CellModel.h:405-420         (driver stimulus + Vm update)
  * Expressions keep the reference's evaluation order so that, compiled without FP
  * contraction against the same libm, results match the reference bit for bit; the
@@ -89,16 +91,57 @@
   X(k_5) X(beta_1) X(alpha_2) X(alpha_4) X(alpha_rel) X(beta_tau_CaMK) X(alpha_rel_CaMK)            \
   X(tau_h_LCaMK) X(RToverF)
 
+/* Tomek 2019 (ToR-ORd) as compiled in the reference (ISAC and TRPN defined,
+ * TomekParameters.h:18-23): NS_TomekParameters::varType order (TomekParameters.h:28-165), the
+ * values TomekParameters::Calculate derives (233-302) in the middle of the list as there. */
+#define TOM_PARAMS(X)                                                                               \
+  X(amplitude) X(duration) X(celltype) X(Na_o) X(Ca_o) X(K_o) X(Cl_o) X(INaF_Multiplier)            \
+  X(INaL_Multiplier) X(Ito_Multiplier) X(PCa_Multiplier) X(IKr_Multiplier) X(IKs_Multiplier)        \
+  X(IK1_Multiplier) X(INaCa_Multiplier) X(INaK_Multiplier) X(IKb_Multiplier) X(INab_Multiplier)     \
+  X(ICab_Multiplier) X(IpCa_Multiplier) X(Init_Vm) X(Init_Na_i) X(Init_Na_ss) X(Init_K_i)           \
+  X(Init_K_ss) X(Init_Ca_i) X(Init_Ca_ss) X(Init_Ca_nsr) X(Init_Ca_jsr) X(Init_Cl_i) X(Init_m)      \
+  X(Init_A_h) X(Init_B_h) X(Init_h) X(Init_A_j) X(Init_B_j) X(Init_j) X(Init_h_p) X(Init_j_p)       \
+  X(Init_m_L) X(Init_h_L) X(Init_h_L_CaMK) X(Init_a) X(Init_i_fast) X(Init_i_slow) X(Init_a_CaMK)   \
+  X(Init_i_CaMK_fast) X(Init_i_CaMK_slow) X(Init_d) X(Init_f_fast) X(Init_f_slow) X(Init_f_Ca_fast) \
+  X(Init_f_Ca_slow) X(Init_j_Ca) X(Init_n_ss) X(Init_n_i) X(Init_f_CaMK_fast)                       \
+  X(Init_f_Ca_CaMK_fast) X(Init_C_0) X(Init_C_1) X(Init_C_2) X(Init_O) X(Init_I) X(Init_x_s1)       \
+  X(Init_x_s2) X(Init_J_rel_NP) X(Init_J_rel_CaMK) X(Init_CaMK_trap)                                \
+  X(R) X(T) X(F) X(L) X(r) X(tau_h_L) X(A_h) X(v_cell) X(A_geo) X(A_cap) X(v_myo) X(v_nsr) X(v_jsr) \
+  X(v_ss) X(P_CaNa) X(P_CaK) X(P_Ca_CaMK) X(P_CaNa_CaMK) X(P_CaK_CaMK) X(A_f_fast) X(A_f_slow)      \
+  X(k_Na1) X(k_Na2) X(k_asymm) X(k_Ca_on) X(k_Ca_off) X(k_m_1) X(k_p_2) X(k_p_4) X(MgADP) X(MgATP)  \
+  X(K_MgATP) X(beta_tau) X(P_Ca) X(h_10) X(h_11) X(h_12) X(k_1) X(k_2) X(k_5) X(beta_1) X(alpha_2)  \
+  X(alpha_4) X(alpha_rel) X(beta_tau_CaMK) X(alpha_rel_CaMK) X(tau_h_LCaMK) X(RToverF)              \
+  X(ISAC_SWITCH) X(alpha) X(G_sac) X(K_sac) X(E_sac) X(Init_Ca_TRPN) X(beta1) X(Ca_T50) X(k_TRPN)   \
+  X(n_TRPN)
+
 #define ENUM_TT2(x) T_##x,
 #define ENUM_CRN(x) C_##x,
 #define ENUM_ORD(x) O_##x,
+#define ENUM_TOM(x) M_##x,
 #define NAME(x) #x,
 enum { TT2_PARAMS(ENUM_TT2) T_LAST };
 enum { CRN_PARAMS(ENUM_CRN) C_LAST };
 enum { ORD_PARAMS(ENUM_ORD) O_LAST };
+enum { TOM_PARAMS(ENUM_TOM) M_LAST };
 static const char *tt2_names[] = {TT2_PARAMS(NAME)};
 static const char *crn_names[] = {CRN_PARAMS(NAME)};
 static const char *ord_names[] = {ORD_PARAMS(NAME)};
+static const char *tom_names[] = {TOM_PARAMS(NAME)};
+
+/* The reference backup block of Tomek (GetBase() = &m, Tomek.h:33-52): 48 states (A_h, B_h, A_j,
+ * B_j are rates Calc recomputes; Cl_i never changes), then the 36 values Calc stores. */
+enum {
+  MB_m, MB_A_h, MB_B_h, MB_h, MB_A_j, MB_B_j, MB_j, MB_h_p, MB_j_p, MB_m_L, MB_h_L, MB_h_L_CaMK, MB_a,
+  MB_i_fast, MB_i_slow, MB_a_CaMK, MB_i_CaMK_fast, MB_i_CaMK_slow, MB_d, MB_f_fast, MB_f_slow, MB_f_Ca_fast,
+  MB_f_Ca_slow, MB_j_Ca, MB_f_CaMK_fast, MB_f_Ca_CaMK_fast, MB_n_ss, MB_n_i, MB_C_0, MB_C_1, MB_C_2, MB_O, MB_I,
+  MB_x_s1, MB_x_s2, MB_Na_i, MB_Na_ss, MB_K_i, MB_K_ss, MB_Ca_i, MB_Ca_ss, MB_Ca_nsr, MB_Ca_jsr, MB_Cl_i,
+  MB_CaMK_trap, MB_J_rel_NP, MB_J_rel_CaMK, MB_Ca_TRPN,
+  MB_I_Na, MB_I_Na_late, MB_I_to, MB_I_CaL, MB_I_CaNa, MB_I_CaK, MB_I_CaL_i, MB_I_CaL_ss, MB_I_CaNa_i,
+  MB_I_CaNa_ss, MB_I_CaK_i, MB_I_CaK_ss, MB_I_Kr, MB_I_Ks, MB_I_K1, MB_I_NaCa_i, MB_I_NaCa_ss, MB_I_NaK,
+  MB_I_CaCl_junc, MB_I_CaCl_sl, MB_I_CaCl, MB_I_Nab, MB_I_Cab, MB_I_Kb, MB_I_Clb, MB_I_pCa, MB_J_diff_Na,
+  MB_J_diff_Ca, MB_J_diff_K, MB_J_leak, MB_J_rel, MB_J_tr, MB_J_up, MB_cur_I_tot, MB_I_tot, MB_I_SAC,
+  TOM_BLOCK
+};
 
 /* The reference backup block of OHaraRudy (GetBase() = &m, OHaraRudy.h:31-52): 42 states,
  * h_CaMK_fast included although Calc never touches it, then the 17 currents it stores. */
@@ -132,11 +175,13 @@ static const char *tt2_tnames[] = {TT2_TABLES(NAME)};
 static const char *crn_tnames[] = {CRN_TABLES(NAME)};
 
 int cmo_n_params(int model) {
-  return model == CMO_TT2 ? T_LAST : (model == CMO_CRN ? C_LAST : (model == CMO_ORD ? O_LAST : -1));
+  return model == CMO_TT2 ? T_LAST
+                          : (model == CMO_CRN ? C_LAST : (model == CMO_ORD ? O_LAST : (model == CMO_TOM ? M_LAST : -1)));
 }
 const char *cmo_param_name(int model, int i) {
   if (i < 0 || i >= cmo_n_params(model)) return 0;
-  return model == CMO_TT2 ? tt2_names[i] : (model == CMO_CRN ? crn_names[i] : ord_names[i]);
+  return model == CMO_TT2 ? tt2_names[i]
+                          : (model == CMO_CRN ? crn_names[i] : (model == CMO_ORD ? ord_names[i] : tom_names[i]));
 }
 int cmo_param_index(int model, const char *name) {
   int n = cmo_n_params(model);
@@ -145,12 +190,13 @@ int cmo_param_index(int model, const char *name) {
   return -1;
 }
 int cmo_state_doubles(int model) {
-  return model == CMO_TT2 ? 36 : (model == CMO_CRN ? 22 : (model == CMO_ORD ? ORD_BLOCK : -1));
+  return model == CMO_TT2 ? 36
+                          : (model == CMO_CRN ? 22 : (model == CMO_ORD ? ORD_BLOCK : (model == CMO_TOM ? TOM_BLOCK : -1)));
 }
 /* O'Hara-Rudy evaluates every gate directly (its InitTable loop body is empty,
  * OHaraRudyParameters.cpp:318-441): no tables. */
 int cmo_n_tables(int model) {
-  return model == CMO_TT2 ? TT_LAST : (model == CMO_CRN ? TC_LAST : (model == CMO_ORD ? 0 : -1));
+  return model == CMO_TT2 ? TT_LAST : (model == CMO_CRN ? TC_LAST : (model == CMO_ORD || model == CMO_TOM ? 0 : -1));
 }
 const char *cmo_table_name(int model, int k) {
   if (k < 0 || k >= cmo_n_tables(model)) return 0;
@@ -1097,11 +1143,525 @@ static double ord_calc(const double *P, double *b, double tinc, double V, double
 }
 #undef P_
 
+/* ---------------------------------------------------------------- Tomek */
+#define P_(x) P[M_##x]
+
+/* TomekParameters::Calculate (233-302): as O'Hara-Rudy's, with one A_h. */
+static void tom_derive(double *P) {
+  P_(R) = 8314.0;
+  P_(T) = 310.0;
+  P_(F) = 96485.0;
+  P_(L) = 0.01;
+  P_(r) = 0.0011;
+  P_(tau_h_L) = 200.0;
+  P_(A_h) = 0.99;
+  P_(A_f_fast) = 0.6;
+  P_(k_Na1) = 15.0;
+  P_(k_Na2) = 5.0;
+  P_(k_asymm) = 12.5;
+  P_(k_Ca_on) = 1.5e6;
+  P_(k_Ca_off) = 5.0e3;
+  P_(k_m_1) = 182.4;
+  P_(k_p_2) = 687.2;
+  P_(k_p_4) = 639.0;
+  P_(MgADP) = 0.05;
+  P_(MgATP) = 9.8;
+  P_(K_MgATP) = 1.698e-7;
+  P_(beta_tau) = 4.75;
+  P_(P_Ca) = P_(PCa_Multiplier) * 0.0001;
+  P_(v_cell) = 1000.0 * 3.14 * P_(r) * P_(r) * P_(L);
+  P_(A_geo) = 2.0 * 3.14 * P_(r) * P_(r) + 2.0 * 3.14 * P_(r) * P_(L);
+  P_(A_cap) = 2.0 * P_(A_geo);
+  P_(v_myo) = 0.68 * P_(v_cell);
+  P_(v_nsr) = 0.0552 * P_(v_cell);
+  P_(v_jsr) = 0.0048 * P_(v_cell);
+  P_(v_ss) = 0.02 * P_(v_cell);
+  P_(P_CaNa) = 0.00125 * P_(P_Ca);
+  P_(P_CaK) = 3.574e-04 * P_(P_Ca);
+  P_(P_Ca_CaMK) = 1.1 * P_(P_Ca);
+  P_(P_CaNa_CaMK) = 0.00125 * P_(P_Ca_CaMK);
+  P_(P_CaK_CaMK) = 3.5743e-04 * P_(P_Ca_CaMK);
+  P_(A_f_slow) = 1.0 - P_(A_f_fast);
+  P_(h_10) = P_(k_asymm) + 1.0 + (P_(Na_o) * (1.0 + P_(Na_o) / P_(k_Na2))) / P_(k_Na1);
+  P_(h_11) = (P_(Na_o) * P_(Na_o)) / (P_(h_10) * P_(k_Na1) * P_(k_Na2));
+  P_(h_12) = 1.0 / P_(h_10);
+  P_(k_1) = P_(h_12) * P_(Ca_o) * P_(k_Ca_on);
+  P_(k_2) = P_(k_Ca_off);
+  P_(k_5) = P_(k_Ca_off);
+  P_(beta_1) = P_(k_m_1) * P_(MgADP);
+  P_(alpha_2) = P_(k_p_2);
+  P_(alpha_4) = (P_(k_p_4) * (P_(MgATP) / P_(K_MgATP))) / (1.0 + (P_(MgATP) / P_(K_MgATP)));
+  P_(alpha_rel) = 0.5 * P_(beta_tau);
+  P_(beta_tau_CaMK) = 1.25 * P_(beta_tau);
+  P_(alpha_rel_CaMK) = 0.5 * P_(beta_tau_CaMK);
+  P_(tau_h_LCaMK) = 3.0 * P_(tau_h_L);
+  P_(RToverF) = (P_(R) * P_(T)) / P_(F);
+}
+
+/* Tomek::Init (55-107): A_j and B_j are not set there (Calc sets them before use); 0 here. */
+static void tom_init(const double *P, double *b) {
+  memset(b, 0, TOM_BLOCK * sizeof(double));
+  b[MB_m] = P_(Init_m); b[MB_A_h] = P_(Init_A_h); b[MB_B_h] = P_(Init_B_h); b[MB_h] = P_(Init_h);
+  b[MB_j] = P_(Init_j); b[MB_h_p] = P_(Init_h_p); b[MB_j_p] = P_(Init_j_p); b[MB_m_L] = P_(Init_m_L);
+  b[MB_h_L] = P_(Init_h_L); b[MB_h_L_CaMK] = P_(Init_h_L_CaMK); b[MB_a] = P_(Init_a);
+  b[MB_i_fast] = P_(Init_i_fast); b[MB_i_slow] = P_(Init_i_slow); b[MB_a_CaMK] = P_(Init_a_CaMK);
+  b[MB_i_CaMK_fast] = P_(Init_i_CaMK_fast); b[MB_i_CaMK_slow] = P_(Init_i_CaMK_slow); b[MB_d] = P_(Init_d);
+  b[MB_f_fast] = P_(Init_f_fast); b[MB_f_slow] = P_(Init_f_slow); b[MB_f_Ca_fast] = P_(Init_f_Ca_fast);
+  b[MB_f_Ca_slow] = P_(Init_f_Ca_slow); b[MB_j_Ca] = P_(Init_j_Ca); b[MB_n_ss] = P_(Init_n_ss);
+  b[MB_n_i] = P_(Init_n_i); b[MB_f_CaMK_fast] = P_(Init_f_CaMK_fast); b[MB_f_Ca_CaMK_fast] = P_(Init_f_Ca_CaMK_fast);
+  b[MB_C_0] = P_(Init_C_0); b[MB_C_1] = P_(Init_C_1); b[MB_C_2] = P_(Init_C_2); b[MB_O] = P_(Init_O);
+  b[MB_I] = P_(Init_I); b[MB_x_s1] = P_(Init_x_s1); b[MB_x_s2] = P_(Init_x_s2); b[MB_Na_i] = P_(Init_Na_i);
+  b[MB_Na_ss] = P_(Init_Na_ss); b[MB_K_i] = P_(Init_K_i); b[MB_K_ss] = P_(Init_K_ss); b[MB_Ca_i] = P_(Init_Ca_i);
+  b[MB_Ca_ss] = P_(Init_Ca_ss); b[MB_Ca_nsr] = P_(Init_Ca_nsr); b[MB_Ca_jsr] = P_(Init_Ca_jsr);
+  b[MB_Cl_i] = P_(Init_Cl_i); b[MB_CaMK_trap] = P_(Init_CaMK_trap); b[MB_J_rel_NP] = P_(Init_J_rel_NP);
+  b[MB_J_rel_CaMK] = P_(Init_J_rel_CaMK); b[MB_Ca_TRPN] = P_(Init_Ca_TRPN) / 0.07;
+}
+
+/* Ionic-strength activity coefficient of Tomek::Calc (272-279): exp(-constA z^2 (sqrt(I)/(1+sqrt(I)) - 0.3 I)). */
+static inline double tom_gamma(double constA, double z2, double I) {
+  return exp((-constA * z2 * ((sqrt(I) / (1. + sqrt(I))) - (0.3 * I))));
+}
+
+/* Tomek::Calc (110-656), the reference's evaluation order. */
+static double tom_calc(const double *P, double *b, double tinc, double V, double i_external, double stretch) {
+  tinc *= 1000.0;
+  const double V_m = V * 1000.0;
+  const double lambda_m = 1.2 < stretch ? 1.2 : stretch;
+  const double KmCaMK = 0.15, aCaMK = 0.05, bCaMK = 0.00068, CaMKo = 0.05, KmCaM = 0.0015;
+  const double Na_i = b[MB_Na_i], Na_ss = b[MB_Na_ss], K_i = b[MB_K_i], K_ss = b[MB_K_ss], Ca_i = b[MB_Ca_i],
+               Ca_ss = b[MB_Ca_ss], Ca_nsr = b[MB_Ca_nsr], Ca_jsr = b[MB_Ca_jsr], Cl_i = b[MB_Cl_i];
+  double CaMK_trap = b[MB_CaMK_trap];
+  /* CaMK (127-132) */
+  const double CaMK_bound = ((CaMKo * (1.0 - CaMK_trap)) / (1.0 + (KmCaM / Ca_ss)));
+  const double CaMK_active = (CaMK_bound + CaMK_trap);
+  const double dCaMK_trap = ((aCaMK * CaMK_bound * (CaMK_bound + CaMK_trap)) - (bCaMK * CaMK_trap));
+  CaMK_trap += tinc * dCaMK_trap;
+  b[MB_CaMK_trap] = CaMK_trap;
+  /* reversal potentials (135-140) */
+  const double E_Na = P_(RToverF) * log(P_(Na_o) / Na_i);
+  const double E_K = P_(RToverF) * log(P_(K_o) / K_i);
+  const double PKNa = 0.01833;
+  const double E_Ks = P_(RToverF) * log((P_(K_o) + PKNa * P_(Na_o)) / (K_i + PKNa * Na_i));
+  const double zcl = 1.0;
+  const double E_Cl = ((P_(R) * P_(T)) / (zcl * P_(F))) * log((Cl_i / P_(Cl_o)));
+  const double VFFoverRT = (V_m * P_(F) * P_(F)) / (P_(R) * P_(T));
+  const double VFoverRT = (V_m * P_(F)) / (P_(R) * P_(T));
+  const double util_1 = P_(A_cap) / (P_(F) * P_(v_myo));
+  const double util_2 = P_(v_ss) / P_(v_myo);
+  const double util_3 = P_(A_cap) / (P_(F) * P_(v_ss));
+
+  /* I_Na (150-182): ten Tusscher gates with a CaMK-phosphorylated pair (h_p, j_p) */
+  const double m_inf = 1.0 / ((1.0 + exp(-(V_m + 56.86) / 9.03)) * (1.0 + exp(-(V_m + 56.86) / 9.03)));
+  const double tau_m = 0.1292 * exp(-(((V_m + 45.79) / 15.54) * ((V_m + 45.79) / 15.54))) +
+                       0.06487 * exp(-(((V_m - 4.823) / 51.12) * ((V_m - 4.823) / 51.12)));
+  b[MB_m] = m_inf - (m_inf - b[MB_m]) * exp(-tinc / tau_m);
+  double A_h, B_h, A_j, B_j;
+  if (V_m < -40.0) {
+    A_h = (0.057 * exp((-(V_m + 80.0) / 6.8)));
+    B_h = ((2.7 * exp((0.079 * V_m))) + (3.1e5 * exp((0.3485 * V_m))));
+    A_j = ((((-2.5428e4 * exp((0.2444 * V_m))) - (6.948e-6 * exp((-0.04391 * V_m)))) * (V_m + 37.78)) /
+           (1.0 + exp((0.311 * (V_m + 79.23)))));
+    B_j = ((0.02424 * exp((-0.01052 * V_m))) / (1.0 + exp((-0.1378 * (V_m + 40.14)))));
+  } else {
+    A_h = 0.0;
+    B_h = (0.77 / (0.13 * (1. + exp((-(V_m + 10.66) / 11.1)))));
+    A_j = 0.0;
+    B_j = ((0.6 * exp((0.057 * V_m))) / (1.0 + exp((-0.1 * (V_m + 32.0)))));
+  }
+  b[MB_A_h] = A_h; b[MB_B_h] = B_h; b[MB_A_j] = A_j; b[MB_B_j] = B_j;
+  const double tau_h = 1.0 / (A_h + B_h);
+  const double h_inf = (1.0 / ((1.0 + exp(((V_m + 71.55) / 7.43))) * (1.0 + exp(((V_m + 71.55) / 7.43)))));
+  b[MB_h] = h_inf - (h_inf - b[MB_h]) * exp(-tinc / tau_h);
+  const double tau_j = 1.0 / (A_j + B_j);
+  const double j_inf = (1.0 / ((1.0 + exp(((V_m + 71.55) / 7.43))) * (1.0 + exp(((V_m + 71.55) / 7.43)))));
+  b[MB_j] = j_inf - (j_inf - b[MB_j]) * exp(-tinc / tau_j);
+  const double h_p_inf = (1.0 / ((1.0 + exp(((V_m + 77.55) / 7.43))) * (1.0 + exp(((V_m + 77.55) / 7.43)))));
+  b[MB_h_p] = h_p_inf - (h_p_inf - b[MB_h_p]) * exp(-tinc / tau_h);
+  const double tau_j_p = 1.46 * tau_j;
+  b[MB_j_p] = j_inf - (j_inf - b[MB_j_p]) * exp(-tinc / tau_j_p);
+  const double phi_INa_CaMK = 1.0 / (1.0 + KmCaMK / CaMK_active);
+  const double G_Na = 11.7802;
+  const double m = b[MB_m];
+  const double I_Na = P_(INaF_Multiplier) * G_Na * (V_m - E_Na) * m * m * m *
+                      ((1.0 - phi_INa_CaMK) * b[MB_h] * b[MB_j] + (phi_INa_CaMK * b[MB_h_p] * b[MB_j_p]));
+
+  /* I_NaL (186-198) */
+  const double thL_mod = 1.0;
+  const double m_L_inf = 1.0 / (1.0 + exp(-(V_m + 42.85) / 5.264));
+  b[MB_m_L] = m_L_inf - (m_L_inf - b[MB_m_L]) * exp(-tinc / tau_m);
+  const double h_L_inf = 1.0 / (1.0 + exp((V_m + 87.61) / 7.488));
+  b[MB_h_L] = h_L_inf - (h_L_inf - b[MB_h_L]) * exp(-tinc / (thL_mod * P_(tau_h_L)));
+  const double h_L_CaMK_inf = 1.0 / (1.0 + exp((V_m + 93.81) / 7.488));
+  const double tau_h_L_CaMK = 3.0 * P_(tau_h_L) * thL_mod;
+  b[MB_h_L_CaMK] = h_L_CaMK_inf - (h_L_CaMK_inf - b[MB_h_L_CaMK]) * exp(-tinc / tau_h_L_CaMK);
+  const double G_Na_L = 0.0279;
+  const double I_Na_late = P_(INaL_Multiplier) * G_Na_L * (V_m - E_Na) * b[MB_m_L] *
+                           ((1.0 - phi_INa_CaMK) * b[MB_h_L] + phi_INa_CaMK * b[MB_h_L_CaMK]);
+
+  /* I_to (200-231) */
+  const double a_inf = 1.0 / (1.0 + exp(-(V_m - 14.34) / 14.82));
+  const double tau_a =
+      1.0515 / (1.0 / (1.2089 * (1.0 + exp(-(V_m - 18.4099) / 29.3814))) + 3.5 / (1.0 + exp((V_m + 100.0) / 29.3814)));
+  b[MB_a] = a_inf - (a_inf - b[MB_a]) * exp(-tinc / tau_a);
+  const double i_inf = 1.0 / (1.0 + exp((V_m + 43.94) / 5.711));
+  const double delta_epi = P_(celltype) == 1.0 ? (1.0 - 0.95 / (1.0 + exp((V_m + 70.0) / 5.0))) : 1.0;
+  const double tau_i_fast_base = 4.562 + 1.0 / (0.3933 * exp(-(V_m + 100.0) / 100.0) + 0.08004 * exp((V_m + 50.0) / 16.59));
+  const double tau_i_slow_base =
+      23.62 + 1.0 / (0.001416 * exp(-(V_m + 96.52) / 59.05) + 1.780e-08 * exp((V_m + 114.1) / 8.079));
+  const double tau_i_fast = tau_i_fast_base * delta_epi;
+  const double tau_i_slow = tau_i_slow_base * delta_epi;
+  b[MB_i_fast] = i_inf - (i_inf - b[MB_i_fast]) * exp(-tinc / tau_i_fast);
+  b[MB_i_slow] = i_inf - (i_inf - b[MB_i_slow]) * exp(-tinc / tau_i_slow);
+  const double A_i_fast = 1.0 / (1.0 + exp((V_m - 213.6) / 151.2));
+  const double A_i_slow = 1.0 - A_i_fast;
+  const double i = A_i_fast * b[MB_i_fast] + A_i_slow * b[MB_i_slow];
+  const double a_CaMK_inf = 1.0 / (1.0 + exp(-(V_m - 24.34) / 14.82));
+  b[MB_a_CaMK] = a_CaMK_inf - (a_CaMK_inf - b[MB_a_CaMK]) * exp(-tinc / tau_a);
+  const double delta_CaMK_develop = 1.354 + 1.0e-04 / (exp((V_m - 167.4) / 15.89) + exp(-(V_m - 12.23) / 0.2154));
+  const double delta_CaMK_recover = 1.0 - 0.5 / (1.0 + exp((V_m + 70.0) / 20.0));
+  const double tau_i_CaMK_fast = tau_i_fast * delta_CaMK_develop * delta_CaMK_recover;
+  const double tau_i_CaMK_slow = tau_i_slow * delta_CaMK_develop * delta_CaMK_recover;
+  b[MB_i_CaMK_fast] = i_inf - (i_inf - b[MB_i_CaMK_fast]) * exp(-tinc / tau_i_CaMK_fast);
+  b[MB_i_CaMK_slow] = i_inf - (i_inf - b[MB_i_CaMK_slow]) * exp(-tinc / tau_i_CaMK_slow);
+  const double i_CaMK = A_i_fast * b[MB_i_CaMK_fast] + A_i_slow * b[MB_i_CaMK_slow];
+  const double G_to = 0.16;
+  const double I_to = P_(Ito_Multiplier) * G_to * (V_m - E_K) *
+                      ((1.0 - phi_INa_CaMK) * b[MB_a] * i + phi_INa_CaMK * b[MB_a_CaMK] * i_CaMK);
+
+  /* I_CaL, I_CaNa, I_CaK (233-327): subspace (80 %) and myoplasm (20 %) parts, each with its own
+   * n gate and activity coefficients from the local ionic strength */
+  double d_inf = 1.0763 * exp((-1.007 * exp((-0.0829 * V_m))));
+  if (V_m > 31.4978) d_inf = 1.0;
+  const double tau_d = 0.6 + 1.0 / (exp(-0.05 * (V_m + 6.0)) + exp(0.09 * (V_m + 14.0)));
+  b[MB_d] = d_inf - (d_inf - b[MB_d]) * exp(-tinc / tau_d);
+  const double f_inf = 1.0 / (1.0 + exp((V_m + 19.58) / 3.696));
+  const double tau_f_fast = 7.0 + 1.0 / (0.0045 * exp(-(V_m + 20.0) / 10.0) + 0.0045 * exp((V_m + 20.0) / 10.0));
+  const double tau_f_slow = 1000.0 + 1.0 / (3.5e-05 * exp(-(V_m + 5.0) / 4.0) + 3.5e-05 * exp((V_m + 5.0) / 6.0));
+  const double A_f_Ca_fast = 0.3 + 0.6 / (1.0 + exp((V_m - 10.0) / 10.0));
+  const double A_f_Ca_slow = 1.0 - A_f_Ca_fast;
+  b[MB_f_fast] = f_inf - (f_inf - b[MB_f_fast]) * exp(-tinc / tau_f_fast);
+  b[MB_f_slow] = f_inf - (f_inf - b[MB_f_slow]) * exp(-tinc / tau_f_slow);
+  const double f = P_(A_f_fast) * b[MB_f_fast] + P_(A_f_slow) * b[MB_f_slow];
+  const double tau_f_Ca_fast = 7.0 + 1.0 / (0.04 * exp(-(V_m - 4.0) / 7.0) + 0.04 * exp((V_m - 4.0) / 7.0));
+  const double tau_f_Ca_slow = 100.0 + 1.0 / (0.00012 * exp(-V_m / 3.0) + 0.00012 * exp(V_m / 7.0));
+  b[MB_f_Ca_fast] = f_inf - (f_inf - b[MB_f_Ca_fast]) * exp(-tinc / tau_f_Ca_fast);
+  b[MB_f_Ca_slow] = f_inf - (f_inf - b[MB_f_Ca_slow]) * exp(-tinc / tau_f_Ca_slow);
+  const double f_Ca = A_f_Ca_fast * b[MB_f_Ca_fast] + A_f_Ca_slow * b[MB_f_Ca_slow];
+  const double j_Ca_inf = 1. / (1 + exp((V_m + 18.08) / (2.7916)));
+  const double tau_j_Ca = 75.0;
+  b[MB_j_Ca] = j_Ca_inf - (j_Ca_inf - b[MB_j_Ca]) * exp(-tinc / tau_j_Ca);
+  const double tau_f_CaMK_fast = 2.5 * tau_f_fast;
+  b[MB_f_CaMK_fast] = f_inf - (f_inf - b[MB_f_CaMK_fast]) * exp(-tinc / tau_f_CaMK_fast);
+  const double f_CaMK = P_(A_f_fast) * b[MB_f_CaMK_fast] + P_(A_f_slow) * b[MB_f_slow];
+  const double tau_f_Ca_CaMK_fast = 2.5 * tau_f_Ca_fast;
+  b[MB_f_Ca_CaMK_fast] = f_inf - (f_inf - b[MB_f_Ca_CaMK_fast]) * exp(-tinc / tau_f_Ca_CaMK_fast);
+  const double f_Ca_CaMK = A_f_Ca_fast * b[MB_f_Ca_CaMK_fast] + A_f_Ca_slow * b[MB_f_Ca_slow];
+  const double j_Ca = b[MB_j_Ca];
+  const double k_m2_n = j_Ca * 1.0;
+  const double Kmn = 0.002, k2n = 500.0;
+  const double alpha_n_Ca_ss = 1.0 / ((k2n / k_m2_n) + pow((1.0 + (Kmn / Ca_ss)), 4.0));
+  b[MB_n_ss] = alpha_n_Ca_ss * (k2n / k_m2_n) - (alpha_n_Ca_ss * (k2n / k_m2_n) - b[MB_n_ss]) * exp(-k_m2_n * tinc);
+  const double I_o = (0.5 * (P_(Na_o) + P_(K_o) + P_(Cl_o) + (4. * P_(Ca_o))) / 1000.);
+  const double I_ss = ((0.5 * (Na_ss + K_ss + Cl_i + (4. * Ca_ss))) / 1000.);
+  const double constA = (1.82e6 * pow((74. * 310.), -1.5));
+  const double gamma_Ca_ss = tom_gamma(constA, 4., I_ss);
+  const double gamma_Ca_o = tom_gamma(constA, 4., I_o);
+  const double gamma_Na_ss = tom_gamma(constA, 1., I_ss);
+  const double gamma_Na_o = tom_gamma(constA, 1., I_o);
+  const double gamma_K_ss = tom_gamma(constA, 1., I_ss);
+  const double gamma_K_o = tom_gamma(constA, 1., I_o);
+  const double Psi_Ca_ss = ((4. * VFFoverRT * ((gamma_Ca_ss * Ca_ss * exp((2. * VFoverRT))) - (gamma_Ca_o * P_(Ca_o)))) /
+                            (exp((2. * VFoverRT)) - 1.));
+  const double Psi_CaNa_ss = ((1. * VFFoverRT * ((gamma_Na_ss * Na_ss * exp((1. * VFoverRT))) - (gamma_Na_o)*P_(Na_o))) /
+                              (exp((1. * VFoverRT)) - 1.));
+  const double Psi_CaK_ss = ((1. * VFFoverRT * ((gamma_K_ss * K_ss * exp((1. * VFoverRT))) - (gamma_K_o * P_(K_o)))) /
+                             (exp((1. * VFoverRT)) - 1.));
+  /* the reference scales the L-type permeability by IpCa_Multiplier (line 290) */
+  const double PCa_b = 8.3757e-05;
+  const double PCa = P_(IpCa_Multiplier) * PCa_b;
+  const double PCaNa = (0.00125 * PCa), PCaK = (3.574e-4 * PCa), PCap = (1.1 * PCa), PCaNap = (0.00125 * PCap),
+               PCaKp = (3.574e-4 * PCap);
+  const double ICaL_fractionSS = 0.8;
+  const double phi = 1.0 / (1.0 + KmCaMK / CaMK_active);
+  const double d = b[MB_d], n_ss = b[MB_n_ss];
+  const double I_CaL_ss = (ICaL_fractionSS * (((1. - phi) * PCa * Psi_Ca_ss * d * ((f * (1. - n_ss)) + (j_Ca * f_Ca * n_ss))) +
+                                             (phi * PCap * Psi_Ca_ss * d * ((f_CaMK * (1. - n_ss)) + (j_Ca * f_Ca_CaMK * n_ss)))));
+  const double I_CaNa_ss =
+      (ICaL_fractionSS * (((1. - phi) * PCaNa * Psi_CaNa_ss * d * ((f * (1. - n_ss)) + (j_Ca * f_Ca * n_ss))) +
+                          (phi * PCaNap * Psi_CaNa_ss * d * ((f_CaMK * (1. - n_ss)) + (j_Ca * f_Ca_CaMK * n_ss)))));
+  const double I_CaK_ss = (ICaL_fractionSS * (((1. - phi) * PCaK * Psi_CaK_ss * d * ((f * (1. - n_ss)) + (j_Ca * f_Ca * n_ss))) +
+                                             (phi * PCaKp * Psi_CaK_ss * d * ((f_CaMK * (1. - n_ss)) + (j_Ca * f_Ca_CaMK * n_ss)))));
+  const double alpha_n_Ca_i =
+      1.0 / ((k2n / k_m2_n) + ((1. + (Kmn / Ca_i)) * (1. + (Kmn / Ca_i)) * (1. + (Kmn / Ca_i)) * (1. + (Kmn / Ca_i))));
+  b[MB_n_i] = alpha_n_Ca_i * (k2n / k_m2_n) - (alpha_n_Ca_i * (k2n / k_m2_n) - b[MB_n_i]) * exp(-k_m2_n * tinc);
+  const double n_i = b[MB_n_i];
+  const double I_i = ((0.5 * (Na_i + K_i + Cl_i + (4. * Ca_i))) / 1000.);
+  const double gamma_Ca_i = tom_gamma(constA, 4., I_i);
+  const double gamma_Na_i = tom_gamma(constA, 1., I_i);
+  const double gamma_K_i = tom_gamma(constA, 1., I_i);
+  const double Psi_Ca_i = ((4. * VFFoverRT * ((gamma_Ca_i * Ca_i * exp((2. * VFoverRT))) - (gamma_Ca_o * P_(Ca_o)))) /
+                           (exp((2. * VFoverRT)) - 1.));
+  const double Psi_CaNa_i = (1. * VFFoverRT * ((gamma_Na_i * Na_i * exp((1. * VFoverRT))) - (gamma_Na_o * P_(Na_o))) /
+                             (exp((1. * VFoverRT)) - 1.));
+  const double Psi_CaK_i = ((1. * VFFoverRT * ((gamma_K_i * K_i * exp((1. * VFoverRT))) - (gamma_K_o * P_(K_o)))) /
+                            (exp((1. * VFoverRT)) - 1.));
+  const double I_CaL_i = ((1. - ICaL_fractionSS) * (((1. - phi) * PCa * Psi_Ca_i * d * ((f * (1. - n_i)) + (j_Ca * f_Ca * n_i))) +
+                                                   (phi * PCap * Psi_Ca_i * d * ((f_CaMK * (1. - n_i)) + (j_Ca * f_Ca_CaMK * n_i)))));
+  const double I_CaNa_i =
+      ((1. - ICaL_fractionSS) * (((1. - phi) * PCaNa * Psi_CaNa_i * d * ((f * (1. - n_i)) + (j_Ca * f_Ca * n_i))) +
+                                 (phi * PCaNap * Psi_CaNa_i * d * ((f_CaMK * (1. - n_i)) + (j_Ca * f_Ca_CaMK * n_i)))));
+  const double I_CaK_i =
+      ((1. - ICaL_fractionSS) * (((1. - phi) * PCaK * Psi_CaK_i * d * ((f * (1. - n_i)) + (j_Ca * f_Ca * n_i))) +
+                                 (phi * PCaKp * Psi_CaK_i * d * ((f_CaMK * (1. - n_i)) + (j_Ca * f_Ca_CaMK * n_i)))));
+  const double I_CaL = I_CaL_ss + I_CaL_i;
+  const double I_CaNa = I_CaNa_ss + I_CaNa_i;
+  const double I_CaK = I_CaK_ss + I_CaK_i;
+
+  /* I_Kr (329-351): five-state Markov chain, explicit Euler in the reference's order */
+  const double alpha_Kr = 0.1161 * exp(0.299 * VFoverRT);
+  const double beta_Kr = 0.2442 * exp(-1.604 * VFoverRT);
+  const double alpha_Kr_1 = 1.25 * 0.1235, beta_Kr_1 = 0.1911;
+  const double alpha_Kr_2 = 0.0578 * exp(0.971 * VFoverRT);
+  const double beta_Kr_2 = 0.349e-3 * exp(-1.062 * VFoverRT);
+  const double alpha_Kr_i = 0.2533 * exp(0.5953 * VFoverRT);
+  const double beta_Kr_i = 0.06525 * exp(-0.8209 * VFoverRT);
+  const double alpha_C2_to_I = 0.52e-4 * exp(1.525 * VFoverRT);
+  const double beta_I_to_C2 = (beta_Kr_2 * beta_Kr_i * alpha_C2_to_I) / (alpha_Kr_2 * alpha_Kr_i);
+  const double dC_0 = b[MB_C_1] * beta_Kr - b[MB_C_0] * alpha_Kr;
+  b[MB_C_0] += tinc * dC_0;
+  const double dC_1 = b[MB_C_0] * alpha_Kr + b[MB_C_2] * beta_Kr_1 - b[MB_C_1] * (beta_Kr + alpha_Kr_1);
+  b[MB_C_1] += tinc * dC_1;
+  const double dC_2 = b[MB_C_1] * alpha_Kr_1 + b[MB_O] * beta_Kr_2 + b[MB_I] * beta_I_to_C2 -
+                      b[MB_C_2] * (beta_Kr_1 + alpha_Kr_2 + alpha_C2_to_I);
+  b[MB_C_2] += tinc * dC_2;
+  const double dO = (((alpha_Kr_2 * b[MB_C_2]) + (beta_Kr_i * b[MB_I])) - ((beta_Kr_2 + alpha_Kr_i) * b[MB_O]));
+  b[MB_O] += tinc * dO;
+  const double dI = (((alpha_C2_to_I * b[MB_C_2]) + (alpha_Kr_i * b[MB_O])) - ((beta_I_to_C2 + beta_Kr_i) * b[MB_I]));
+  b[MB_I] += tinc * dI;
+  const double G_Kr = 0.0321;
+  const double I_Kr = P_(IKr_Multiplier) * G_Kr * sqrt(P_(K_o) / 5.0) * b[MB_O] * (V_m - E_K);
+
+  /* I_Ks (355-363) */
+  const double x_s1_inf = 1.0 / (1.0 + exp(-(V_m + 11.6) / 8.932));
+  const double tau_x_s1 = 817.3 + 1.0 / (2.326e-04 * exp((V_m + 48.28) / 17.80) + 0.001292 * exp(-(V_m + 210.0) / 230.0));
+  b[MB_x_s1] = x_s1_inf - (x_s1_inf - b[MB_x_s1]) * exp(-tinc / tau_x_s1);
+  const double tau_x_s2 = 1.0 / (0.01 * exp((V_m - 50.0) / 20.0) + 0.0193 * exp(-(V_m + 66.54) / 31.0));
+  b[MB_x_s2] = x_s1_inf - (x_s1_inf - b[MB_x_s2]) * exp(-tinc / tau_x_s2);
+  const double G_Ks = 0.0011;
+  const double I_Ks = P_(IKs_Multiplier) * G_Ks * (1.0 + (0.6 / (1.0 + pow((3.8e-05 / (Ca_i)), 1.4)))) * b[MB_x_s1] *
+                      b[MB_x_s2] * (V_m - E_Ks);
+
+  /* I_K1 (365-370): instantaneous rectification */
+  const double a_K1 = 4.094 / (1.0 + exp(0.1217 * (V_m - E_K - 49.934)));
+  const double b_K1 = (15.72 * exp(0.0674 * (V_m - E_K - 3.257)) + exp(0.0618 * (V_m - E_K - 594.31))) /
+                      (1.0 + exp(-0.1629 * (V_m - E_K + 14.207)));
+  const double K1_SS = (a_K1) / (a_K1 + b_K1);
+  const double G_K1 = 0.6992;
+  const double I_K1 = P_(IK1_Multiplier) * G_K1 * sqrt(P_(K_o) / 5.0) * K1_SS * (V_m - E_K);
+
+  /* I_NaCa_i, I_NaCa_ss (373-451): O'Hara-Rudy's exchanger with 0.0034 x (0.65 | 0.35) */
+  const double kna3 = 88.12, wna = 6.0e4, wca = 6.0e4, wnaca = 5.0e3, qna = 0.5224, qca = 0.1670;
+  const double z_Ca = 2.0, z_Na = 1.0, z_K = 1.0;
+  const double exp_z_Ca = exp(z_Ca * VFoverRT);
+  const double exp_z_Na = exp(z_Na * VFoverRT);
+  const double h_Ca = exp(qca * VFoverRT);
+  const double h_Na = exp(qna * VFoverRT);
+  const double h_1_i = 1.0 + (Na_i * (1.0 + h_Na)) / kna3;
+  const double h_2_i = (Na_i * h_Na) / (kna3 * h_1_i);
+  const double h_3_i = 1.0 / h_1_i;
+  const double h_4_i = 1.0 + (Na_i * (1.0 + Na_i / P_(k_Na2))) / P_(k_Na1);
+  const double h_5_i = (Na_i * Na_i) / (h_4_i * P_(k_Na1) * P_(k_Na2));
+  const double h_6_i = 1.0 / h_4_i;
+  const double h_7 = 1.0 + (P_(Na_o) * (1.0 + 1.0 / h_Na)) / kna3;
+  const double h_8 = P_(Na_o) / (kna3 * h_Na * h_7);
+  const double h_9 = 1.0 / h_7;
+  const double k_3_d = h_9 * wca;
+  const double k_3_dd = h_8 * wnaca;
+  const double k_3 = k_3_d + k_3_dd;
+  const double k_4_d_i = (h_3_i * wca) / h_Ca;
+  const double k_4_dd_i = h_2_i * wnaca;
+  const double k_4_i = k_4_d_i + k_4_dd_i;
+  const double k_6_i = h_6_i * Ca_i * P_(k_Ca_on);
+  const double k_7_i = h_5_i * h_2_i * wna;
+  const double k_8 = h_8 * P_(h_11) * wna;
+  const double k_1 = P_(k_1), k_2 = P_(k_2), k_5 = P_(k_5);
+  const double x_1_i = k_2 * k_4_i * (k_7_i + k_6_i) + k_5 * k_7_i * (k_2 + k_3);
+  const double x_2_i = k_1 * k_7_i * (k_4_i + k_5) + k_4_i * k_6_i * (k_1 + k_8);
+  const double x_3_i = k_1 * k_3 * (k_7_i + k_6_i) + k_8 * k_6_i * (k_2 + k_3);
+  const double x_4_i = k_2 * k_8 * (k_4_i + k_5) + k_3 * k_5 * (k_1 + k_8);
+  const double E_1_i = x_1_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_2_i = x_2_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_3_i = x_3_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double E_4_i = x_4_i / (x_1_i + x_2_i + x_3_i + x_4_i);
+  const double KmCaAct = 150.0e-6;
+  const double allo_i = 1.0 / (1.0 + ((KmCaAct / Ca_i) * (KmCaAct / Ca_i)));
+  const double J_NaCa_Na_i = 3.0 * (E_4_i * k_7_i - E_1_i * k_8) + E_3_i * k_4_dd_i - E_2_i * k_3_dd;
+  const double J_NaCa_Ca_i = E_2_i * k_2 - E_1_i * k_1;
+  const double G_NaCa = 0.0034;
+  const double I_NaCa_i = P_(INaCa_Multiplier) * G_NaCa * 0.65 * allo_i * (z_Na * J_NaCa_Na_i + z_Ca * J_NaCa_Ca_i);
+  const double h_1_ss = 1.0 + (Na_ss * (1.0 + h_Na)) / kna3;
+  const double h_2_ss = (Na_ss * h_Na) / (kna3 * h_1_ss);
+  const double h_3_ss = 1.0 / h_1_ss;
+  const double h_4_ss = 1.0 + (Na_ss * (1.0 + Na_ss / P_(k_Na2))) / P_(k_Na1);
+  const double h_5_ss = (Na_ss * Na_ss) / (h_4_ss * P_(k_Na1) * P_(k_Na2));
+  const double h_6_ss = 1.0 / h_4_ss;
+  const double k_4_d_ss = (h_3_ss * wca) / h_Ca;
+  const double k_4_dd_ss = h_2_ss * wnaca;
+  const double k_4_ss = k_4_d_ss + k_4_dd_ss;
+  const double k_6_ss = h_6_ss * Ca_ss * P_(k_Ca_on);
+  const double k_7_ss = h_5_ss * h_2_ss * wna;
+  const double x_1_ss = k_2 * k_4_ss * (k_7_ss + k_6_ss) + k_5 * k_7_ss * (k_2 + k_3);
+  const double x_2_ss = k_1 * k_7_ss * (k_4_ss + k_5) + k_4_ss * k_6_ss * (k_1 + k_8);
+  const double x_3_ss = k_1 * k_3 * (k_7_ss + k_6_ss) + k_8 * k_6_ss * (k_2 + k_3);
+  const double x_4_ss = k_2 * k_8 * (k_4_ss + k_5) + k_3 * k_5 * (k_1 + k_8);
+  const double E_1_ss = x_1_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_2_ss = x_2_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_3_ss = x_3_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double E_4_ss = x_4_ss / (x_1_ss + x_2_ss + x_3_ss + x_4_ss);
+  const double allo_ss = 1.0 / (1.0 + (KmCaAct / Ca_ss) * (KmCaAct / Ca_ss));
+  const double J_NaCa_Na_ss = 3.0 * (E_4_ss * k_7_ss - E_1_ss * k_8) + E_3_ss * k_4_dd_ss - E_2_ss * k_3_dd;
+  const double J_NaCa_Ca_ss = E_2_ss * k_2 - E_1_ss * k_1;
+  const double I_NaCa_ss =
+      P_(INaCa_Multiplier) * G_NaCa * 0.35 * allo_ss * (z_Na * J_NaCa_Na_ss + z_Ca * J_NaCa_Ca_ss);
+
+  /* I_NaK (453-503) */
+  const double k1p = 949.5, k2m = 39.4, k3p = 1899.0, k3m = 79300.0, k4m = 40.0, Knai0 = 9.073, Knao0 = 27.78,
+               delta = -0.1550;
+  const double K_Nai = Knai0 * exp(delta * VFoverRT * 1 / 3);
+  const double K_Nao = Knao0 * exp((1.0 - delta) * VFoverRT * 1 / 3);
+  const double Kki = 0.5, Kko = 0.3582, H = 1.0e-7, eP = 4.2, Khp = 1.698e-7, Knap = 224.0, Kxkur = 292.0;
+  const double Pnak = eP / (1.0 + H / Khp + Na_i / Knap + K_i / Kxkur);
+  const double alpha_1 = (k1p * pow((Na_i / K_Nai), 3.0)) /
+                         (pow((1.0 + Na_i / K_Nai), 3.0) + pow((1.0 + K_i / Kki), 2.0) - 1.0);
+  const double beta_2 = (k2m * pow((P_(Na_o) / K_Nao), 3.0)) /
+                        (pow((1.0 + P_(Na_o) / K_Nao), 3.0) + pow((1.0 + P_(K_o) / Kko), 2.0) - 1.0);
+  const double alpha_3 = (k3p * pow((P_(K_o) / Kko), 2.0)) /
+                         (pow((1.0 + P_(Na_o) / K_Nao), 3.0) + pow((1.0 + P_(K_o) / Kko), 2.0) - 1.0);
+  const double beta_3 = (k3m * Pnak * H) / (1.0 + P_(MgATP));
+  const double beta_4 = (k4m * pow((K_i / Kki), 2.0)) /
+                        (pow((1.0 + Na_i / K_Nai), 3.0) + pow((1.0 + K_i / Kki), 2.0) - 1.0);
+  const double al2 = P_(alpha_2), al4 = P_(alpha_4), be1 = P_(beta_1);
+  const double x_1 = al4 * alpha_1 * al2 + beta_2 * beta_4 * beta_3 + al2 * beta_4 * beta_3 + beta_3 * alpha_1 * al2;
+  const double x_2 = beta_2 * be1 * beta_4 + alpha_1 * al2 * alpha_3 + alpha_3 * be1 * beta_4 + al2 * alpha_3 * beta_4;
+  const double x_3 = al2 * alpha_3 * al4 + beta_3 * beta_2 * be1 + beta_2 * be1 * al4 + alpha_3 * al4 * be1;
+  const double x_4 = beta_4 * beta_3 * beta_2 + alpha_3 * al4 * alpha_1 + beta_2 * al4 * alpha_1 + beta_3 * beta_2 * alpha_1;
+  const double E_1 = x_1 / (x_1 + x_2 + x_3 + x_4);
+  const double E_2 = x_2 / (x_1 + x_2 + x_3 + x_4);
+  const double E_3 = x_3 / (x_1 + x_2 + x_3 + x_4);
+  const double E_4 = x_4 / (x_1 + x_2 + x_3 + x_4);
+  const double J_NaK_Na = 3.0 * (E_1 * alpha_3 - E_2 * beta_3);
+  const double J_NaK_K = 2.0 * (E_4 * be1 - E_3 * alpha_1);
+  const double P_NaK = 15.4509;
+  const double I_NaK = P_(INaK_Multiplier) * P_NaK * (z_Na * J_NaK_Na + z_K * J_NaK_K);
+
+  /* I_CaCl, background currents, I_pCa, I_SAC (505-538) */
+  const double I_CaCl_junc = (0.2843 * (V_m - E_Cl)) / (1. + (0.1 / Ca_ss));
+  const double I_CaCl_sl = (0 * 0.2843 * (V_m - E_Cl)) / (1. + (0.1 / Ca_i));
+  const double I_CaCl = I_CaCl_junc + I_CaCl_sl;
+  const double x_Kb = 1.0 / (1.0 + exp(-(V_m - 10.8968) / (23.9871)));
+  const double G_Kb = 0.0189;
+  const double I_Kb = P_(IKb_Multiplier) * G_Kb * x_Kb * (V_m - E_K);
+  const double P_Nab = 1.9239e-9;
+  const double I_Nab =
+      P_(INab_Multiplier) * P_Nab * z_Na * z_Na * VFFoverRT * ((Na_i * exp_z_Na - P_(Na_o)) / (exp_z_Na - 1.0));
+  const double P_Cab = 5.9194e-8;
+  const double I_Cab = P_(ICab_Multiplier) * P_Cab * z_Ca * z_Ca * VFFoverRT *
+                       ((gamma_Ca_i * Ca_i * exp_z_Ca - gamma_Ca_o * P_(Ca_o)) / (exp_z_Ca - 1.0));
+  const double P_Clb = 1.98e-3;
+  const double I_Clb = P_Clb * (V_m - E_Cl);
+  const double G_pCa = 0.0005;
+  const double I_pCa = P_(IpCa_Multiplier) * ((G_pCa * Ca_i) / (0.0005 + Ca_i));
+  double I_SAC = P_(G_sac) * (V_m - P_(E_sac)) / (1. + P_(K_sac) * exp(-P_(alpha) * (stretch - 1.)));
+  I_SAC *= P_(ISAC_SWITCH);
+
+  /* total current (540-548) */
+  const double cur_I_tot = I_Na + I_Na_late + I_to + I_CaL + I_CaNa + I_CaK + I_Kr + I_Ks + I_K1 + I_NaCa_i + I_NaCa_ss +
+                           I_NaK + I_Nab + I_Cab + I_Kb + I_pCa + I_Clb + I_CaCl + I_SAC + i_external;
+  const double I_tot = -cur_I_tot;
+
+  /* fluxes (550-590) */
+  const double J_diff_Na = (Na_ss - Na_i) / 2.0;
+  const double J_diff_Ca = (Ca_ss - Ca_i) / 0.2;
+  const double J_diff_K = (K_ss - K_i) / 2.0;
+  const double K_inf_rel = 1.7;
+  double J_rel_NP_inf = (P_(alpha_rel) * (-I_CaL)) / (1.0 + pow((K_inf_rel / Ca_jsr), 8.0));
+  double J_rel_CaMK_inf = (P_(alpha_rel_CaMK) * (-I_CaL)) / (1.0 + pow((K_inf_rel / Ca_jsr), 8.0));
+  if (P_(celltype) == 2.0) {
+    J_rel_NP_inf *= 1.7;
+    J_rel_CaMK_inf *= 1.7;
+  }
+  const double tau_rel_NP_b = P_(beta_tau) / (1.0 + (0.0123 / Ca_jsr));
+  const double tau_rel_NP = tau_rel_NP_b < 0.001 ? 0.001 : tau_rel_NP_b;
+  b[MB_J_rel_NP] = J_rel_NP_inf - (J_rel_NP_inf - b[MB_J_rel_NP]) * exp(-tinc / tau_rel_NP);
+  const double tau_rel_CaMK_b = P_(beta_tau_CaMK) / (1.0 + (0.0123 / Ca_jsr));
+  const double tau_rel_CaMK = tau_rel_CaMK_b < 0.001 ? 0.001 : tau_rel_CaMK_b;
+  b[MB_J_rel_CaMK] = J_rel_CaMK_inf - (J_rel_CaMK_inf - b[MB_J_rel_CaMK]) * exp(-tinc / tau_rel_CaMK);
+  const double J_rel = 1.5378 * (1.0 - phi) * b[MB_J_rel_NP] + phi * b[MB_J_rel_CaMK];
+  double J_up_NP = (0.005425 * Ca_i) / (0.00092 + Ca_i);
+  double J_up_CaMK = (2.75 * 0.005425 * Ca_i) / (0.00092 - 0.00017 + Ca_i);
+  if (P_(celltype) == 1.0) {
+    J_up_NP *= 1.3;
+    J_up_CaMK *= 1.3;
+  }
+  const double J_leak = (0.0048825 * Ca_nsr) / 15.0;
+  const double J_up = ((1.0 - phi) * J_up_NP + (phi * J_up_CaMK) - J_leak);
+  const double J_tr = (Ca_nsr - Ca_jsr) / 60.0;
+
+  /* concentrations (592-654) */
+  const double cur_Nai = I_Na + I_Na_late + 3.0 * I_NaCa_i + I_CaNa_i + 3.0 * I_NaK + I_Nab;
+  const double dNa_i = -(cur_Nai)*util_1 + J_diff_Na * util_2;
+  b[MB_Na_i] = Na_i + tinc * dNa_i;
+  const double dNa_ss = -(I_CaNa_ss + 3.0 * I_NaCa_ss) * util_3 - J_diff_Na;
+  b[MB_Na_ss] = Na_ss + tinc * dNa_ss;
+  const double cur_Ki = I_to + I_Kr + I_Ks + I_K1 + I_Kb + i_external - 2.0 * I_NaK + I_CaK_i;
+  const double dK_i = -(cur_Ki)*util_1 + J_diff_K * util_2;
+  b[MB_K_i] = K_i + tinc * dK_i;
+  const double dK_ss = -(I_CaK_ss)*util_3 - J_diff_K;
+  b[MB_K_ss] = K_ss + tinc * dK_ss;
+  double cmdnmax = 0.05;
+  if (P_(celltype) == 1) cmdnmax *= 1.3;
+  const double kmcmdn = 0.00238, trpnmax = 0.07, BSRmax = 0.047, KmBSR = 0.00087, BSLmax = 1.124, KmBSL = 0.0087,
+               csqnmax = 10.0, kmcsqn = 0.8;
+  const double Ca_T50 = (P_(Ca_T50) + P_(beta1) * (lambda_m - 1.0));
+  const double Ca_TRPN = b[MB_Ca_TRPN];
+  const double dCaTRPN = P_(k_TRPN) * (pow(1000 * Ca_i / Ca_T50, P_(n_TRPN)) * (1. - Ca_TRPN) - Ca_TRPN);
+  b[MB_Ca_TRPN] = Ca_TRPN + tinc * dCaTRPN;
+  const double I_Trpn = trpnmax * dCaTRPN;
+  const double beta_Cai = 1.0 / (1.0 + ((cmdnmax * kmcmdn) / pow((kmcmdn + Ca_i), 2.0)));
+  const double cur_Cai = I_CaL_i + I_pCa + I_Cab - 2.0 * I_NaCa_i;
+  const double dCa_i =
+      beta_Cai * (-(cur_Cai)*0.5 * util_1 - J_up * (P_(v_nsr) / P_(v_myo)) + J_diff_Ca * util_2 - I_Trpn);
+  b[MB_Ca_i] = Ca_i + tinc * dCa_i;
+  const double beta_Cass =
+      1.0 / (1.0 + ((BSRmax * KmBSR) / pow((KmBSR + Ca_ss), 2.0)) + ((BSLmax * KmBSL) / pow((KmBSL + Ca_ss), 2.0)));
+  const double dCa_ss =
+      beta_Cass * (-(I_CaL_ss - 2.0 * I_NaCa_ss) * 0.5 * util_3 + J_rel * (P_(v_jsr) / P_(v_ss)) - J_diff_Ca);
+  b[MB_Ca_ss] = Ca_ss + tinc * dCa_ss;
+  const double dCa_nsr = J_up - ((J_tr * P_(v_jsr)) / P_(v_nsr));
+  b[MB_Ca_nsr] = Ca_nsr + tinc * dCa_nsr;
+  const double beta_Cajsr = 1.0 / (1.0 + ((csqnmax * kmcsqn) / pow((kmcsqn + Ca_jsr), 2.0)));
+  const double dCa_jsr = beta_Cajsr * (J_tr - J_rel);
+  b[MB_Ca_jsr] = Ca_jsr + tinc * dCa_jsr;
+
+  /* the values the reference keeps in its block (Tomek.h:47-52) */
+  b[MB_I_Na] = I_Na; b[MB_I_Na_late] = I_Na_late; b[MB_I_to] = I_to; b[MB_I_CaL] = I_CaL; b[MB_I_CaNa] = I_CaNa;
+  b[MB_I_CaK] = I_CaK; b[MB_I_CaL_i] = I_CaL_i; b[MB_I_CaL_ss] = I_CaL_ss; b[MB_I_CaNa_i] = I_CaNa_i;
+  b[MB_I_CaNa_ss] = I_CaNa_ss; b[MB_I_CaK_i] = I_CaK_i; b[MB_I_CaK_ss] = I_CaK_ss; b[MB_I_Kr] = I_Kr;
+  b[MB_I_Ks] = I_Ks; b[MB_I_K1] = I_K1; b[MB_I_NaCa_i] = I_NaCa_i; b[MB_I_NaCa_ss] = I_NaCa_ss; b[MB_I_NaK] = I_NaK;
+  b[MB_I_CaCl_junc] = I_CaCl_junc; b[MB_I_CaCl_sl] = I_CaCl_sl; b[MB_I_CaCl] = I_CaCl; b[MB_I_Nab] = I_Nab;
+  b[MB_I_Cab] = I_Cab; b[MB_I_Kb] = I_Kb; b[MB_I_Clb] = I_Clb; b[MB_I_pCa] = I_pCa; b[MB_J_diff_Na] = J_diff_Na;
+  b[MB_J_diff_Ca] = J_diff_Ca; b[MB_J_diff_K] = J_diff_K; b[MB_J_leak] = J_leak; b[MB_J_rel] = J_rel;
+  b[MB_J_tr] = J_tr; b[MB_J_up] = J_up; b[MB_cur_I_tot] = cur_I_tot; b[MB_I_tot] = I_tot; b[MB_I_SAC] = I_SAC;
+  return 0.001 * tinc * I_tot;
+}
+#undef P_
+
 /* ---------------------------------------------------------------- public entry points */
 static void derive(int model, double *P) {
   if (model == CMO_TT2) tt2_derive(P);
   else if (model == CMO_CRN) crn_derive(P);
-  else ord_derive(P);
+  else if (model == CMO_ORD) ord_derive(P);
+  else tom_derive(P);
 }
 
 int cmo_build_tables(int model, const double *P_in, double dt, double *tables) {
@@ -1120,11 +1680,13 @@ int cmo_build_tables(int model, const double *P_in, double dt, double *tables) {
 void cmo_init_state(int model, const double *P, double *block) {
   if (model == CMO_TT2) tt2_init(P, block);
   else if (model == CMO_CRN) crn_init(P, block);
-  else ord_init(P, block);
+  else if (model == CMO_ORD) ord_init(P, block);
+  else tom_init(P, block);
 }
 
 double cmo_init_vm(int model, const double *P) {
-  return model == CMO_TT2 ? P[T_init_V_m] : (model == CMO_CRN ? P[C_Init_Vm] : P[O_Init_Vm]);
+  return model == CMO_TT2 ? P[T_init_V_m]
+                          : (model == CMO_CRN ? P[C_Init_Vm] : (model == CMO_ORD ? P[O_Init_Vm] : P[M_Init_Vm]));
 }
 
 double cmo_calc(int model, const double *P_in, const double *tables, double *block, double dt, double V,
@@ -1132,7 +1694,8 @@ double cmo_calc(int model, const double *P_in, const double *tables, double *blo
   /* P_in holds base and derived values (the caller derives once via cmo_derive). */
   if (model == CMO_TT2) return tt2_calc(P_in, tables, block, dt, V, i_ext);
   if (model == CMO_CRN) return crn_calc(P_in, tables, block, dt, V, i_ext, stretch);
-  return ord_calc(P_in, block, dt, V, i_ext, stretch);
+  if (model == CMO_ORD) return ord_calc(P_in, block, dt, V, i_ext, stretch);
+  return tom_calc(P_in, block, dt, V, i_ext, stretch);
 }
 
 /* Fills the derived slots of P in place (Calculate()). */
@@ -1176,7 +1739,8 @@ static void *run_range(void *argp) {
       }
       if (a->model == CMO_TT2) v += tt2_calc(Pc, a->tables, blk, a->dt, v, i_ext);
       else if (a->model == CMO_CRN) v += crn_calc(Pc, a->tables, blk, a->dt, v, i_ext, 1.0);
-      else v += ord_calc(Pc, blk, a->dt, v, i_ext, 1.0);
+      else if (a->model == CMO_ORD) v += ord_calc(Pc, blk, a->dt, v, i_ext, 1.0);
+      else v += tom_calc(Pc, blk, a->dt, v, i_ext, 1.0);
       t += a->dt;
     }
     if (isnan(v)) a->bad = 1;
@@ -1274,7 +1838,8 @@ static void *mono_range(void *argp) {
       double dv;
       if (a->model == CMO_TT2) dv = tt2_calc(Pc, a->tables, blk, a->dt, vo[c], i_ext);
       else if (a->model == CMO_CRN) dv = crn_calc(Pc, a->tables, blk, a->dt, vo[c], i_ext, 1.0);
-      else dv = ord_calc(Pc, blk, a->dt, vo[c], i_ext, 1.0);
+      else if (a->model == CMO_ORD) dv = ord_calc(Pc, blk, a->dt, vo[c], i_ext, 1.0);
+      else dv = tom_calc(Pc, blk, a->dt, vo[c], i_ext, 1.0);
       const double v = vo[c] + dv;
       vn[c] = v;
       if (isnan(v) || (a->vm_range > 0.0 && (v > a->vm_range || v < -a->vm_range))) a->bad = 1;

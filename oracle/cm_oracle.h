@@ -1,6 +1,6 @@
 /* Test infrastructure only (the oracle): a plain-C, FP64 restatement of the reference
- * cell-model update for ten Tusscher-Panfilov 2006, Courtemanche 1998 and O'Hara-Rudy 2011
- * (the reference's variant: Passini/Dutta I_Na gates, troponin, SAC), used by the
+ * cell-model update for ten Tusscher-Panfilov 2006, Courtemanche 1998, O'Hara-Rudy 2011
+ * (the reference's variant: Passini/Dutta I_Na gates, troponin, SAC) and Tomek 2019, used by the
  * tests as the checker and by bench.py as the timed CPU baseline. The product never
  * links or calls it.
  *
@@ -9,6 +9,7 @@
  *   CRN (22 doubles, CourtemancheEtAl.h:32-42): Ca_i Ca_up Ca_rel h j oi ui Xr Xs u v w Na_i K_i m oa ua d f f_Ca I_SAC Ca_TRPN
  *   ORd (59 doubles, OHaraRudy.h:31-52): 42 states from m to Ca_TRPN (h_CaMK_fast unused), then
  *        I_Na_fast I_Na_late I_to I_CaL I_CaNa I_CaK I_Kr I_Ks I_K1 I_NaCa_i I_NaCa_ss I_NaK I_Nab I_Cab I_Kb I_pCa I_SAC
+ *   Tomek (84 doubles, Tomek.h:33-52): 48 states from m to Ca_TRPN, then 36 stored currents and fluxes
  *
  * Parameter vectors P are indexed by this file's own parameter lists (names as in the
  * reference .ev files); derived quantities are recomputed here (restating
@@ -21,7 +22,7 @@
 extern "C" {
 #endif
 
-enum { CMO_TT2 = 0, CMO_CRN = 1, CMO_ORD = 2 };
+enum { CMO_TT2 = 0, CMO_CRN = 1, CMO_ORD = 2, CMO_TOM = 3 };
 enum { CMO_RTDT = 4000 };
 
 int cmo_n_params(int model);

@@ -52,7 +52,7 @@ extern "C" {
 const char *ref_last_error() { return g_err.c_str(); }
 
 // model: reference ElphyModelType value (EMT_TenTusscher2 = 5, EMT_CourtemancheEtAl = 2,
-// EMT_OHaraRudy = 12).
+// EMT_OHaraRudy = 12, EMT_Tomek = 14).
 void *ref_create(int model, const char *ev_path, double dt, int n_cells) {
   try {
     if (!getenv("kaRootDir")) {
@@ -172,6 +172,7 @@ int ref_n_params(void *hv) {
     case EMT_TenTusscher2: n = NS_TenTusscher2Parameters::vtLast; break;
     case EMT_CourtemancheEtAl: n = NS_CourtemancheParameters::vtLast; break;
     case EMT_OHaraRudy: n = NS_OHaraRudyParameters::vtLast; break;
+    case EMT_Tomek: n = NS_TomekParameters::vtLast; break;
     default: return -1;
   }
   return n;

@@ -1,12 +1,13 @@
 """Generate the golden vectors in this folder by running the reference's own CellModel
 library (compiled from the reference sources by oracle/Makefile, target `ref`).
 
-    python tests/golden/make_golden.py [tt2] [crn] [ord]   # needs the reference tree (CM_REFERENCE_TREE)
+    python tests/golden/make_golden.py [tt2] [crn] [ord] [tom]   # needs the reference tree (CM_REFERENCE_TREE)
 
 Outputs (all seeded, deterministic):
   params_tt2_epi.json / params_crn.json  resolved parameter sets after Init + Calculate
                                          (TenTusscher2_original_Epi.ev, CourtemancheEtAl.ev)
   params_ord_<v>.json                    O'Hara-Rudy, v = endo / epi / mid (OHaraRudy_<v>.ev)
+  params_tom_<v>.json                    Tomek, the same cell types (Tomek_<v>.ev)
   tables_<m>.npz    sha256 of every lookup table's bytes + every 50th row, dt = 1e-5 s
                     (TT2 and CRN; O'Hara-Rudy has none)
   step_<m>.npz      one-Calc known answers: states sampled along paced trajectories,
@@ -35,17 +36,17 @@ DT = 1e-5
 
 
 def tag(model, variant=None):
-    if model == O.ORD:
-        return f"ord_{variant}"
+    if model in (O.ORD, O.TOM):
+        return f"{'ord' if model == O.ORD else 'tom'}_{variant}"
     return "tt2" if model == O.TT2 else "crn"
 
 
 def hetero_names(model):
-    return {O.TT2: W.TT2_HETERO, O.CRN: W.CRN_HETERO, O.ORD: W.ORD_HETERO}[model]
+    return {O.TT2: W.TT2_HETERO, O.CRN: W.CRN_HETERO, O.ORD: W.ORD_HETERO, O.TOM: W.TOM_HETERO}[model]
 
 
 def amp(model):
-    return {O.TT2: W.TT2_STIM_NA, O.CRN: W.CRN_STIM_PAPF, O.ORD: W.ORD_STIM}[model]
+    return {O.TT2: W.TT2_STIM_NA, O.CRN: W.CRN_STIM_PAPF, O.ORD: W.ORD_STIM, O.TOM: W.TOM_STIM}[model]
 
 
 def stim_len(model):
@@ -62,7 +63,7 @@ def dump_params(ref, model, variant=None):
     ev = ev_of(model, variant)
     cells = ref.create(model, DT, 1, ev=ev)
     p = {k: v for k, v in cells.params().items() if k}
-    name = f"params_{tag(model, variant)}.json" if model == O.ORD else (
+    name = f"params_{tag(model, variant)}.json" if model in (O.ORD, O.TOM) else (
         "params_tt2_epi.json" if model == O.TT2 else "params_crn.json")
     meta = {"model": O.MODEL_NAMES[model],
             "ev_file": Path(ev).name,
@@ -113,6 +114,10 @@ def dump_step(ref, model, variant=None):
         for s in states:
             s[:, 4] = 0.0
         states[0][:, 42:] = 0.0
+    if model == O.TOM:
+        # A_j, B_j (slots 4, 5) are set by the first Calc, the stored currents (48..83) too
+        states[0][:, 4:6] = 0.0
+        states[0][:, 48:] = 0.0
     S = np.concatenate(states)
     V = np.concatenate(vms)
     het = np.tile(sc, (1, 40))
@@ -162,13 +167,15 @@ def main(which):
         dump_step(ref, model)
         dump_trace(ref, model)
         print("wrote golden vectors for", O.MODEL_NAMES[model])
-    if "ord" in which:
+    for model, key in ((O.ORD, "ord"), (O.TOM, "tom")):
+        if key not in which:
+            continue
         for v in O.ORD_VARIANTS:
-            dump_params(ref, O.ORD, v)
-            dump_step(ref, O.ORD, v)
-            dump_trace(ref, O.ORD, v)
-            print("wrote golden vectors for", O.MODEL_NAMES[O.ORD], v)
+            dump_params(ref, model, v)
+            dump_step(ref, model, v)
+            dump_trace(ref, model, v)
+            print("wrote golden vectors for", O.MODEL_NAMES[model], v)
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"tt2", "crn", "ord"})
+    main(set(sys.argv[1:]) or {"tt2", "crn", "ord", "tom"})
