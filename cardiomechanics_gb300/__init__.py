@@ -28,6 +28,7 @@ LIB_PATH = _PKG / "_lib" / "libcmgb300.so"
 TENTUSSCHER2 = 5
 COURTEMANCHE = 2
 OHARARUDY = 12
+TOMEK = 14
 FP64, MIXED = 0, 1
 LAYOUT_REF_BLOCK, LAYOUT_SOA = 0, 1
 AUDIT_NAN, AUDIT_VRANGE, AUDIT_CARANGE, AUDIT_GATE, AUDIT_SURROGATE, AUDIT_VMRANGE = 1, 2, 4, 8, 16, 32

@@ -28,6 +28,8 @@ int64_t round_ld(int64_t n) { return ((n + 255) / 256) * 256; }  // whole staged
 void mixed_slot(int model, int k, bool &pair, int &slot) {
   if (model == kOHaraRudy) {
     slot = ord_mixed_plane(k, pair);
+  } else if (model == kTomek) {
+    slot = tom_mixed_plane(k, pair);
   } else if (model == kTenTusscher2) {
     // SOA: Ca_i CaSR CaSS Na_i K_i m h j xr1 xr2 xs r s d f f2 fCa Rq
     static const int map[] = {13, 15, 14, 17, 19, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
@@ -42,10 +44,12 @@ void mixed_slot(int model, int k, bool &pair, int &slot) {
 }
 
 // Reference backup block index of SOA variable k (TenTusscher2.h:77-123, CourtemancheEtAl.h:32-42,
-// OHaraRudy.h:31-43: slot 4 is h_CaMK_fast, which the SOA layout leaves out).
+// OHaraRudy.h:31-43: slot 4 is h_CaMK_fast, which the SOA layout leaves out; Tomek.h:33-44:
+// slots 1, 2, 4, 5 are the rates A_h, B_h, A_j, B_j).
 int ref_block_index(int model, int k) {
   if (model == kTenTusscher2) return k < 5 ? k : k + 18;
   if (model == kOHaraRudy) return k < 4 ? k : k + 1;
+  if (model == kTomek) return k == 0 ? 0 : (k == 1 ? 3 : (k == 2 ? 6 : k + 4));
   return k < 20 ? k : 21;
 }
 
@@ -92,14 +96,22 @@ int upload_tables(cm_batch_s *b) {
   }
   if (b->ps.spec->model == kTenTusscher2) b->ps.tt2_consts(b->d.tt2_64, b->d.tt2_32);
   else if (b->ps.spec->model == kOHaraRudy) b->ps.ord_consts(b->d.ord_64, b->d.ord_32);
+  else if (b->ps.spec->model == kTomek) b->ps.tom_consts(b->d.tom_64, b->d.tom_32);
   else b->ps.crn_consts(b->d.crn_64, b->d.crn_32);
   return CM_OK;
 }
 
-// Diagnostic values an FP64 batch can record per cell, and where they sit in the reference
-// block: TT2 Array[0..16], CRN I_SAC, ORd its 17 stored currents.
-int diag_count(int model) { return model == kCourtemanche ? 1 : 17; }
-int diag_block_base(int model) { return model == kTenTusscher2 ? 5 : (model == kOHaraRudy ? 42 : 20); }
+// Diagnostic values an FP64 batch can record per cell, and where value k sits in the reference
+// block: TT2 Array[0..16], CRN I_SAC, ORd its 17 stored currents, Tomek its 36 stored values
+// (slots 48..83) and the four I_Na rates (slots 1, 2, 4, 5).
+int diag_count(int model) { return model == kCourtemanche ? 1 : (model == kTomek ? kTOMDiag : 17); }
+int diag_block_pos(int model, int k) {
+  if (model == kTomek) {
+    static const int rates[4] = {1, 2, 4, 5};
+    return k < kTOMStored ? 48 + k : rates[k - kTOMStored];
+  }
+  return (model == kTenTusscher2 ? 5 : (model == kOHaraRudy ? 42 : 20)) + k;
+}
 
 // Host SOA (n_state x n, model order) <-> device layout.
 int soa_to_device(cm_batch_s *b, const std::vector<double> &soa) {
@@ -422,9 +434,10 @@ int cm_batch_get_state(cm_batch_t b, int layout, double *buf) {
       std::vector<double> dg((size_t)nd * n);
       for (int k = 0; k < nd; k++)
         CK(cudaMemcpy(dg.data() + (size_t)k * n, b->diag + k * b->d.ld, n * sizeof(double), cudaMemcpyDeviceToHost));
-      const int base = diag_block_base(b->d.model);
-      for (int k = 0; k < nd; k++)
-        for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + base + k] = dg[(size_t)k * n + c];
+      for (int k = 0; k < nd; k++) {
+        const int pos = diag_block_pos(b->d.model, k);
+        for (int64_t c = 0; c < n; c++) out[(size_t)c * nb + pos] = dg[(size_t)k * n + c];
+      }
     }
   }
   if (is_device_ptr(buf)) CK(cudaMemcpy(buf, out.data(), out.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -863,7 +876,7 @@ int cm_multi_create(cm_multi_t *out, const cm_batch_t *batches, int n_batches, v
     if (!batches[i]) return fail(CM_ERR_ARG, "NULL batch");
     if (batches[i]->d.precision != CM_PREC_MIXED)
       return fail(CM_ERR_UNSUPPORTED, "the batched form runs CM_PREC_MIXED batches");
-    if (batches[i]->d.model == kOHaraRudy)
+    if (batches[i]->d.model == kOHaraRudy || batches[i]->d.model == kTomek)
       return fail(CM_ERR_UNSUPPORTED, "the batched form covers TenTusscher2 and CourtemancheEtAl batches");
     if (batches[i]->d.ld * 24 >= (int64_t)2147483647) return fail(CM_ERR_ARG, "instance too large for a multi");
   }

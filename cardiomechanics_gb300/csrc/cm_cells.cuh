@@ -5,7 +5,7 @@
 
 #include "cm_crn.cuh"
 #include "cm_launch.h"
-#include "cm_ord.cuh"
+#include "cm_tom.cuh"
 #include "cm_tt2.cuh"
 
 namespace cm {
@@ -143,8 +143,10 @@ struct ORDStore32 {
   __device__ __forceinline__ void cur(int, float) {}
 };
 
-template <typename R, typename I>
-__device__ __forceinline__ ORDHet_<R> ord_het(const DevBatch &b, const ORDConsts<R> &C, I c) {
+// The six per-cell multiplier slots (INaF, INaL, Ito, IKr, IKs, IK1) of O'Hara-Rudy and Tomek:
+// the cell's own value where a slot is set, else the parameter set's.
+template <typename R, typename CT, typename I>
+__device__ __forceinline__ ORDHet_<R> ord_het(const DevBatch &b, const CT &C, I c) {
   const R *const *het = (const R *const *)b.het;
   ORDHet_<R> g;
   g.INaF = het[HO_INaF] ? __ldg(het[HO_INaF] + c) : C.INaF;
@@ -154,6 +156,51 @@ __device__ __forceinline__ ORDHet_<R> ord_het(const DevBatch &b, const ORDConsts
   g.IKs = het[HO_IKs] ? __ldg(het[HO_IKs] + c) : C.IKs;
   g.IK1 = het[HO_IK1] ? __ldg(het[HO_IK1] + c) : C.IK1;
   return g;
+}
+
+// Tomek FP32 store: the O'Hara-Rudy store's two-batch loads over the Tomek planes. Batch 0:
+// CaMK, the I_Na/I_NaL/I_to gates, Na_i, K_i, Ca_ss, Cl_i; batch 1 (before I_CaL): the rest.
+template <typename I>
+struct TOMStore32 {
+  float *s;  // mixed planes of this cell: s[plane * ld]
+  I ld;
+  float v[SM_N];  // this step's inputs (hi words for the pairs)
+  float lo[6];    // lo words of Na_i, Na_ss, K_i, K_ss, Ca_nsr, Ca_jsr
+  __device__ __forceinline__ static bool first(int k) {
+    return k <= SM_i_CaMK_slow || k == SM_Na_i || k == SM_K_i || k == SM_Ca_ss || k == SM_Cl_i ||
+           k == SM_CaMK_trap;
+  }
+  __device__ __forceinline__ TOMStore32(float *s_, I ld_) : s(s_), ld(ld_) { fetch(0); }
+  __device__ __forceinline__ void fetch(int part) {
+#pragma unroll
+    for (int k = 0; k < SM_N; k++) {
+      bool pair;
+      if (first(k) == (part == 0)) v[k] = s[tom_mixed_plane(k, pair) * ld];
+    }
+    if (part == 1) {
+#pragma unroll
+      for (int q = 0; q < 6; q++) lo[q] = s[(kTOMPlain + 2 * q + 1) * ld];
+    }
+  }
+  __device__ __forceinline__ float get(int k) const { return v[k]; }
+  __device__ __forceinline__ void set(int k, float x) {
+    bool pair;
+    s[tom_mixed_plane(k, pair) * ld] = x;
+  }
+  __device__ __forceinline__ void add(int k, float x, float d) {
+    const int q = k <= SM_K_ss ? k - SM_Na_i : 4 + (k - SM_Ca_nsr);
+    Acc a{x, lo[q]};
+    acc_add(a, d);
+    s[(kTOMPlain + 2 * q) * ld] = a.hi;
+    s[(kTOMPlain + 2 * q + 1) * ld] = a.lo;
+  }
+  __device__ __forceinline__ void cur(int, float) {}
+};
+
+template <typename I>
+__device__ __forceinline__ float tom_mixed_cell(const DevBatch &b, I c, float V, float iext, float stretch) {
+  TOMStore32<I> x(b.s32 + c, (I)b.ld);
+  return tom_calc<float>(b.tom_32, x, ord_het<float>(b, b.tom_32, c), V, iext, stretch);
 }
 
 template <typename I>

@@ -78,6 +78,32 @@ CM_HD int ord_mixed_plane(int k, bool &pair) {
   return k <= SO_K_ss ? kORDPlain + 2 * (k - SO_Na_i) : kORDPlain + 8 + 2 * (k - SO_Ca_nsr);
 }
 
+// Tomek 2019: the reference block's states (Tomek.h:33-44) without A_h, B_h, A_j, B_j, which
+// Calc recomputes from Vm every step before using them.
+enum TOMState {
+  SM_m, SM_h, SM_j, SM_h_p, SM_j_p, SM_m_L, SM_h_L, SM_h_L_CaMK, SM_a, SM_i_fast, SM_i_slow, SM_a_CaMK,
+  SM_i_CaMK_fast, SM_i_CaMK_slow, SM_d, SM_f_fast, SM_f_slow, SM_f_Ca_fast, SM_f_Ca_slow, SM_j_Ca,
+  SM_f_CaMK_fast, SM_f_Ca_CaMK_fast, SM_n_ss, SM_n_i, SM_C_0, SM_C_1, SM_C_2, SM_O, SM_I, SM_x_s1, SM_x_s2,
+  SM_Na_i, SM_Na_ss, SM_K_i, SM_K_ss, SM_Ca_i, SM_Ca_ss, SM_Ca_nsr, SM_Ca_jsr, SM_Cl_i, SM_CaMK_trap, SM_J_rel_NP,
+  SM_J_rel_CaMK, SM_Ca_TRPN, SM_N
+};
+// Diagnostic values of a Tomek FP64 batch: the 36 values Calc stores after the states
+// (Tomek.h:47-52, block slots 48..83), then the rates A_h, B_h, A_j, B_j (block slots 1, 2, 4, 5).
+constexpr int kTOMStored = 36;
+constexpr int kTOMDiag = kTOMStored + 4;
+
+// Tomek mixed form: planes 0..37 the FP32 states (TOMState order without the six compensated
+// concentrations), planes 38..49 the (hi, lo) pairs of Na_i, Na_ss, K_i, K_ss, Ca_nsr, Ca_jsr.
+constexpr int kTOMPlain = 38;
+CM_HD int tom_mixed_plane(int k, bool &pair) {
+  pair = false;
+  if (k < SM_Na_i) return k;
+  if (k == SM_Ca_i || k == SM_Ca_ss) return k - 4;
+  if (k >= SM_Cl_i) return k - 6;
+  pair = true;
+  return k <= SM_K_ss ? kTOMPlain + 2 * (k - SM_Na_i) : kTOMPlain + 8 + 2 * (k - SM_Ca_nsr);
+}
+
 // Hetero (per-cell parameter) slots. Each slot either points at n_cells per-cell values
 // or is null (the parameter set's value applies).
 enum TT2Het { H2_g_Na, H2_g_Kr, H2_g_K1, H2_g_Ks, H2_g_to, H2_g_CaL, H2_N };
@@ -131,6 +157,21 @@ struct ORDConsts {
   R G_sac, E_sac, K_sac, alpha_sac, ISAC_SWITCH;
   R Ca_T50, beta1, HFM, k_TRPN, n_TRPN;
   R logNao, logKo, logEKs_num;  // mixed form
+};
+
+// Constants of Tomek::Calc (Tomek.cpp:110-656) prepared on the host, as ORDConsts. The
+// outside activity coefficients depend on the bath alone (lines 271-279).
+template <typename R>
+struct TOMConsts {
+  R dt_ms, RToverF, FoRT, FFoRT, RToF, Na_o, K_o, Ca_o, Cl_o;
+  R util_1, util_2, util_3, vnsr_vmyo, vjsr_vss, vjsr_vnsr;
+  R A_h, A_f_fast, A_f_slow, tau_h_L, tau_h_L_CaMK;
+  R INaF, INaL, Ito, IKr, IKs, IK1;  // the multipliers a cell may replace
+  R INaCa, INaK, IKb, INab, ICab, IpCa, PCa;  // PCa = IpCa_Multiplier * 8.3757e-5 (line 292)
+  R k_Na1, k_Na2, k_Ca_on, h_11, k_1, k_2, k_5, beta_1, alpha_2, alpha_4, MgATP1;
+  R alpha_rel, alpha_rel_CaMK, beta_tau, beta_tau_CaMK, rel_scale, up_scale, cmdnmax, epi;
+  R sqrtKo5, EKs_num, constA, gamma_Ca_o, gamma_Na_o, gamma_K_o;
+  R G_sac, E_sac, K_sac, alpha_sac, ISAC_SWITCH, Ca_T50, beta1, k_TRPN, n_TRPN;
 };
 
 // Voltage row index exactly as the reference computes it (TenTusscher2.cpp:618,

@@ -258,6 +258,35 @@ __global__ void __launch_bounds__(kBlock, kMinB) ord_mixed_kernel(const DevBatch
   }
 }
 
+template <bool kDiag, bool kCoupled>
+__global__ void __launch_bounds__(128) tom_fp64_kernel(const DevBatch b, const StepIO io) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < b.n; c += (int64_t)gridDim.x * blockDim.x) {
+    ORDStore64 x{b.s64 + c, b.ld, kDiag ? b.diag + c : nullptr};
+    const double V = __ldg(io.vm + c);
+    const double iext = iext_fp64<kCoupled>(io, c);
+    const double stretch = io.stretch ? __ldg(io.stretch + c) : 1.0;
+    const double dV = tom_calc<double>(b.tom_64, x, ord_het<double>(b, b.tom_64, c), V, iext, stretch);
+    finish(b, io, c, V, dV, 0u);
+  }
+}
+
+template <typename I, int kBlock, int kMinB, bool kCoupled = false>
+__global__ void __launch_bounds__(kBlock, kMinB) tom_mixed_kernel(const DevBatch b, const StepIO io) {
+  for (I c = (I)blockIdx.x * blockDim.x + threadIdx.x; c < (I)b.n; c += (I)gridDim.x * blockDim.x) {
+    const float iext = iext_f32<kCoupled>(io, c);
+    const float stretch = io.stretch ? (float)__ldg(io.stretch + c) : 1.f;
+    if (io.vm_hi) {
+      Acc v{io.vm_hi[c], io.vm_lo[c]};
+      acc_add(v, tom_mixed_cell<I>(b, c, v.hi, iext, stretch));
+      finish_acc(b, c, v, 0u, io);
+    } else {
+      const double V = __ldg(io.vm + c);
+      const float dV = tom_mixed_cell<I>(b, c, (float)V, iext, stretch);
+      finish(b, io, c, V, (double)dV, 0u);
+    }
+  }
+}
+
 __global__ void diffusion_apply_kernel(const StepIO io, const double *x, double *y, int64_t n) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
     y[c] = coupling_fp64(io, x, c);
@@ -287,9 +316,11 @@ __global__ void vm_join_kernel(const float *hi, const float *lo, double *v, int6
 
 }  // namespace
 
-int n_fp32_vars(int model) { return model == 5 ? 21 : (model == 12 ? kORDPlain + 12 : 25); }
+int n_fp32_vars(int model) {
+  return model == 5 ? 21 : (model == 12 ? kORDPlain + 12 : (model == 14 ? kTOMPlain + 12 : 25));
+}
 int n_fp64_vars(int model, int precision) {
-  if (precision == 0) return model == 5 ? S2_N : (model == 12 ? SO_N : SC_N);
+  if (precision == 0) return model == 5 ? S2_N : (model == 12 ? SO_N : (model == 14 ? SM_N : SC_N));
   return 0;
 }
 
@@ -313,6 +344,7 @@ template <typename I, int B, int M>
 void launch_mixed(const DevBatch &b, const StepIO &io, int grid, cudaStream_t s) {
   if (b.model == 5) tt2_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
   else if (b.model == 12) ord_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
+  else if (b.model == 14) tom_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
   else crn_mixed_kernel<I, B, M><<<grid, B, 0, s>>>(b, io);
 }
 
@@ -321,6 +353,7 @@ void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, 
   if (io.sl_ptr) {  // coupled runs: one shape (256 threads, 128 registers)
     if (b.model == 5) tt2_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
     else if (b.model == 12) ord_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
+    else if (b.model == 14) tom_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
     else crn_mixed_kernel<I, 256, 2, true><<<grid, 256, 0, s>>>(b, io);
     return;
   }
@@ -354,6 +387,9 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
     } else if (b.model == 12) {
       if (diag) if (io.sl_ptr) ord_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else ord_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
       else if (io.sl_ptr) ord_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else ord_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);
+    } else if (b.model == 14) {
+      if (diag) if (io.sl_ptr) tom_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else tom_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
+      else if (io.sl_ptr) tom_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else tom_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);
     } else {
       if (diag) if (io.sl_ptr) crn_fp64_kernel<true, true><<<grid, block, 0, s>>>(b, io); else crn_fp64_kernel<true, false><<<grid, block, 0, s>>>(b, io);
       else if (io.sl_ptr) crn_fp64_kernel<false, true><<<grid, block, 0, s>>>(b, io); else crn_fp64_kernel<false, false><<<grid, block, 0, s>>>(b, io);

@@ -19,8 +19,9 @@ namespace cm {
 //          CRN  h j oi ui Xr Xs u v w m oa ua d f f_Ca Ca_i Ca_TRPN | Ca_up Ca_rel Na_i K_i (hi, lo)
 //          ORd  the 35 states of ORDState other than the six below, in that order |
 //               Na_i Na_ss K_i K_ss Ca_nsr Ca_jsr (hi, lo)
+//          Tom  the 38 states of TOMState other than the same six, in that order | the six (hi, lo)
 struct alignas(16) DevBatch {
-  int model = 0;      // 2 Courtemanche, 5 TenTusscher2, 12 OHaraRudy
+  int model = 0;      // 2 Courtemanche, 5 TenTusscher2, 12 OHaraRudy, 14 Tomek
   int precision = 0;  // 0 FP64, 1 mixed
   int64_t n = 0, ld = 0;
   double *s64 = nullptr;
@@ -30,7 +31,7 @@ struct alignas(16) DevBatch {
   const void *het[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // double* (FP64) / float* (mixed)
   uint32_t *audit_cell = nullptr;
   unsigned int *audit_or = nullptr;
-  double *diag = nullptr;  // FP64 only: TT2 and ORd 17 x ld diagnostic currents; CRN 1 x ld (I_SAC)
+  double *diag = nullptr;  // FP64 only: TT2 and ORd 17 x ld diagnostic currents; CRN 1 x ld (I_SAC); Tomek 40 x ld
   int variant = 0, grid_mode = 0;  // launch shape chosen by cm_batch_autotune
   TT2Consts<double> tt2_64;
   TT2Consts<float> tt2_32;
@@ -38,6 +39,8 @@ struct alignas(16) DevBatch {
   CRNConsts<float> crn_32;
   ORDConsts<double> ord_64;
   ORDConsts<float> ord_32;
+  TOMConsts<double> tom_64;
+  TOMConsts<float> tom_32;
 };
 
 // Per-launch inputs/outputs (device pointers).

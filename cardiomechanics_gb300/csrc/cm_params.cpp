@@ -150,6 +150,44 @@ const char *const kORDState[] = {
 const char *const kORDHet[] = {"INaF_Multiplier", "INaL_Multiplier", "Ito_Multiplier",
                                "IKr_Multiplier",  "IKs_Multiplier",  "IK1_Multiplier"};
 
+// ----------------------------------------------------------------- Tomek
+// Defaults: the values of the reference's Tomek.ev (= Tomek_endo.ev, celltype 0); Tomek_epi.ev
+// (celltype 1) and Tomek_mid.ev (celltype 2) load through .ev files.
+// Order: NS_TomekParameters::varType (TomekParameters.h:28-164), the derived values apart.
+const ParamDef kTOMBase[] = {
+    {"amplitude", -53.0}, {"duration", 0.001}, {"celltype", 0.0}, {"Na_o", 140.0}, {"Ca_o", 1.8}, {"K_o", 5.0},
+    {"Cl_o", 150.0}, {"INaF_Multiplier", 1.0}, {"INaL_Multiplier", 1.0}, {"Ito_Multiplier", 1.0},
+    {"PCa_Multiplier", 1.0}, {"IKr_Multiplier", 1.0}, {"IKs_Multiplier", 1.0}, {"IK1_Multiplier", 1.0},
+    {"INaCa_Multiplier", 1.0}, {"INaK_Multiplier", 1.0}, {"IKb_Multiplier", 1.0}, {"INab_Multiplier", 1.0},
+    {"ICab_Multiplier", 1.0}, {"IpCa_Multiplier", 1.0}, {"Init_Vm", -0.08908318}, {"Init_Na_i", 12.04906},
+    {"Init_Na_ss", 12.04937}, {"Init_K_i", 143.6267}, {"Init_K_ss", 143.6266}, {"Init_Ca_i", 7.217757e-05},
+    {"Init_Ca_ss", 6.296698e-05}, {"Init_Ca_nsr", 1.521204}, {"Init_Ca_jsr", 1.522335}, {"Init_Cl_i", 24.0},
+    {"Init_m", 0.0007521806}, {"Init_A_h", 0.2167647}, {"Init_B_h", 0.002371305}, {"Init_h", 0.8348669},
+    {"Init_A_j", 0.01745803}, {"Init_B_j", 7.277467e-05}, {"Init_j", 0.8349011}, {"Init_h_p", 0.6810231},
+    {"Init_j_p", 0.8347477}, {"Init_m_L", 0.0001533095}, {"Init_h_L", 0.5375133}, {"Init_h_L_CaMK", 0.2980653},
+    {"Init_a", 0.0009307173}, {"Init_i_fast", 0.9996311}, {"Init_i_slow", 0.5974533},
+    {"Init_a_CaMK", 0.0004742092}, {"Init_i_CaMK_fast", 0.9996311}, {"Init_i_CaMK_slow", 0.660594},
+    {"Init_d", 0.0}, {"Init_f_fast", 1.0}, {"Init_f_slow", 0.9405982}, {"Init_f_Ca_fast", 1.0},
+    {"Init_f_Ca_slow", 0.9999026}, {"Init_j_Ca", 0.9999791}, {"Init_n_ss", 0.0004337198},
+    {"Init_n_i", 0.0007353402}, {"Init_f_CaMK_fast", 1.0}, {"Init_f_Ca_CaMK_fast", 1.0},
+    {"Init_C_0", 1.024884}, {"Init_C_1", 0.0008543031}, {"Init_C_2", 0.000704028}, {"Init_O", 0.0003399541},
+    {"Init_I", 1.181451e-05}, {"Init_x_s1", 0.2385143}, {"Init_x_s2", 0.0001707914},
+    {"Init_J_rel_NP", 6.426104e-77}, {"Init_J_rel_CaMK", 2.843667e-62}, {"Init_CaMK_trap", 0.01118689},
+    {"ISAC_SWITCH", 0.0}, {"alpha", 3.0}, {"G_sac", 0.27}, {"K_sac", 100.0}, {"E_sac", 0.0},
+    {"Init_Ca_TRPN", 0.0005577823}, {"beta1", -2.4}, {"Ca_T50", 0.805}, {"k_TRPN", 0.1}, {"n_TRPN", 2.0},
+};
+const char *const kTOMDerived[] = {
+    "R", "T", "F", "L", "r", "tau_h_L", "A_h", "v_cell", "A_geo", "A_cap", "v_myo", "v_nsr", "v_jsr", "v_ss",
+    "P_CaNa", "P_CaK", "P_Ca_CaMK", "P_CaNa_CaMK", "P_CaK_CaMK", "A_f_fast", "A_f_slow", "k_Na1", "k_Na2",
+    "k_asymm", "k_Ca_on", "k_Ca_off", "k_m_1", "k_p_2", "k_p_4", "MgADP", "MgATP", "K_MgATP", "beta_tau",
+    "P_Ca", "h_10", "h_11", "h_12", "k_1", "k_2", "k_5", "beta_1", "alpha_2", "alpha_4", "alpha_rel",
+    "beta_tau_CaMK", "alpha_rel_CaMK", "tau_h_LCaMK", "RToverF"};
+const char *const kTOMState[] = {
+    "m", "h", "j", "h_p", "j_p", "m_L", "h_L", "h_L_CaMK", "a", "i_fast", "i_slow", "a_CaMK", "i_CaMK_fast",
+    "i_CaMK_slow", "d", "f_fast", "f_slow", "f_Ca_fast", "f_Ca_slow", "j_Ca", "f_CaMK_fast", "f_Ca_CaMK_fast",
+    "n_ss", "n_i", "C_0", "C_1", "C_2", "O", "I", "x_s1", "x_s2", "Na_i", "Na_ss", "K_i", "K_ss", "Ca_i",
+    "Ca_ss", "Ca_nsr", "Ca_jsr", "Cl_i", "CaMK_trap", "J_rel_NP", "J_rel_CaMK", "Ca_TRPN"};
+
 #define COUNT(a) (int)(sizeof(a) / sizeof(a[0]))
 const ModelSpec kSpecs[] = {
     {kTenTusscher2, "TenTusscher2", kTT2Base, COUNT(kTT2Base), kTT2Derived, COUNT(kTT2Derived), kTT2Tables,
@@ -159,6 +197,9 @@ const ModelSpec kSpecs[] = {
     // block: 42 states (h_CaMK_fast included) and 17 currents (OHaraRudy.h:31-52)
     {kOHaraRudy, "OHaraRudy", kORDBase, COUNT(kORDBase), kORDDerived, COUNT(kORDDerived), nullptr, 0, kORDState,
      COUNT(kORDState), 59, kORDHet, COUNT(kORDHet), 0, 0},
+    // block: 48 states (the rates A_h, B_h, A_j, B_j included) and 36 stored values (Tomek.h:33-52)
+    {kTomek, "Tomek", kTOMBase, COUNT(kTOMBase), kTOMDerived, COUNT(kTOMDerived), nullptr, 0, kTOMState,
+     COUNT(kTOMState), 84, kORDHet, COUNT(kORDHet), 0, 0},
 };
 
 // ----------------------------------------------------------------- .ev files
@@ -307,6 +348,8 @@ void ParamSet::derive() {
     PV(StepCai) = (PV(CaiMax) - PV(CaiMin)) / kRows;
   } else if (spec->model == kOHaraRudy) {
     derive_ord();
+  } else if (spec->model == kTomek) {
+    derive_tom();
   } else {
     // CourtemancheParameters::Calculate (252-280)
     PV(RTdF) = PV(R) * PV(Tx) / PV(F);
@@ -341,6 +384,58 @@ void ParamSet::derive_ord() {
   PV(tau_h_L) = 200.0;
   PV(A_h_fast) = 0.99;
   PV(A_h_slow) = 0.01;
+  PV(A_f_fast) = 0.6;
+  PV(k_Na1) = 15.0;
+  PV(k_Na2) = 5.0;
+  PV(k_asymm) = 12.5;
+  PV(k_Ca_on) = 1.5e6;
+  PV(k_Ca_off) = 5.0e3;
+  PV(k_m_1) = 182.4;
+  PV(k_p_2) = 687.2;
+  PV(k_p_4) = 639.0;
+  PV(MgADP) = 0.05;
+  PV(MgATP) = 9.8;
+  PV(K_MgATP) = 1.698e-7;
+  PV(beta_tau) = 4.75;
+  PV(P_Ca) = PV(PCa_Multiplier) * 0.0001;
+  PV(v_cell) = 1000.0 * 3.14 * PV(r) * PV(r) * PV(L);  // the reference's pi is 3.14
+  PV(A_geo) = 2.0 * 3.14 * PV(r) * PV(r) + 2.0 * 3.14 * PV(r) * PV(L);
+  PV(A_cap) = 2.0 * PV(A_geo);
+  PV(v_myo) = 0.68 * PV(v_cell);
+  PV(v_nsr) = 0.0552 * PV(v_cell);
+  PV(v_jsr) = 0.0048 * PV(v_cell);
+  PV(v_ss) = 0.02 * PV(v_cell);
+  PV(P_CaNa) = 0.00125 * PV(P_Ca);
+  PV(P_CaK) = 3.574e-04 * PV(P_Ca);
+  PV(P_Ca_CaMK) = 1.1 * PV(P_Ca);
+  PV(P_CaNa_CaMK) = 0.00125 * PV(P_Ca_CaMK);
+  PV(P_CaK_CaMK) = 3.5743e-04 * PV(P_Ca_CaMK);
+  PV(A_f_slow) = 1.0 - PV(A_f_fast);
+  PV(h_10) = PV(k_asymm) + 1.0 + (PV(Na_o) * (1.0 + PV(Na_o) / PV(k_Na2))) / PV(k_Na1);
+  PV(h_11) = (PV(Na_o) * PV(Na_o)) / (PV(h_10) * PV(k_Na1) * PV(k_Na2));
+  PV(h_12) = 1.0 / PV(h_10);
+  PV(k_1) = PV(h_12) * PV(Ca_o) * PV(k_Ca_on);
+  PV(k_2) = PV(k_Ca_off);
+  PV(k_5) = PV(k_Ca_off);
+  PV(beta_1) = PV(k_m_1) * PV(MgADP);
+  PV(alpha_2) = PV(k_p_2);
+  PV(alpha_4) = (PV(k_p_4) * (PV(MgATP) / PV(K_MgATP))) / (1.0 + (PV(MgATP) / PV(K_MgATP)));
+  PV(alpha_rel) = 0.5 * PV(beta_tau);
+  PV(beta_tau_CaMK) = 1.25 * PV(beta_tau);
+  PV(alpha_rel_CaMK) = 0.5 * PV(beta_tau_CaMK);
+  PV(tau_h_LCaMK) = 3.0 * PV(tau_h_L);
+  PV(RToverF) = (PV(R) * PV(T)) / PV(F);
+}
+
+// TomekParameters::Calculate (233-302): O'Hara-Rudy's derivation with one A_h.
+void ParamSet::derive_tom() {
+  PV(R) = 8314.0;
+  PV(T) = 310.0;
+  PV(F) = 96485.0;
+  PV(L) = 0.01;
+  PV(r) = 0.0011;
+  PV(tau_h_L) = 200.0;
+  PV(A_h) = 0.99;
   PV(A_f_fast) = 0.6;
   PV(k_Na1) = 15.0;
   PV(k_Na2) = 5.0;
@@ -565,14 +660,15 @@ void ParamSet::build_tables() {
 double ParamSet::init_vm() const {
   return spec->model == kTenTusscher2 ? vals[index("init_V_m")] : vals[index("Init_Vm")];
 }
-// GetAmplitude() / GetStimTime(): TT2 and O'Hara-Rudy read parameters (OHaraRudy.h:84-86),
+// GetAmplitude() / GetStimTime(): TT2, O'Hara-Rudy and Tomek read parameters (OHaraRudy.h:84-86,
+// Tomek.h:100-102),
 // Courtemanche returns constants.
 double ParamSet::amplitude() const {
-  if (spec->model == kOHaraRudy) return vals[index("amplitude")];
+  if (spec->model == kOHaraRudy || spec->model == kTomek) return vals[index("amplitude")];
   return spec->model == kTenTusscher2 ? vals[index("Amp")] : spec->default_amplitude;
 }
 double ParamSet::stim_time() const {
-  if (spec->model == kOHaraRudy) return vals[index("duration")];
+  if (spec->model == kOHaraRudy || spec->model == kTomek) return vals[index("duration")];
   return spec->model == kTenTusscher2 ? vals[index("stim_duration")] : spec->default_stim_time;
 }
 
@@ -588,6 +684,10 @@ void ParamSet::init_state(std::vector<double> &s) const {
     // OHaraRudy::Init (54-102): Init_<name> for every state; troponin as a fraction of trpnmax
     for (int k = 0; k < SO_Ca_TRPN; k++) s[k] = vals[index((std::string("Init_") + spec->state_names[k]).c_str())];
     s[SO_Ca_TRPN] = vals[index("Init_Ca_TRPN")] / 0.07;
+  } else if (spec->model == kTomek) {
+    // Tomek::Init (55-107): the same rule
+    for (int k = 0; k < SM_Ca_TRPN; k++) s[k] = vals[index((std::string("Init_") + spec->state_names[k]).c_str())];
+    s[SM_Ca_TRPN] = vals[index("Init_Ca_TRPN")] / 0.07;
   } else {
     // Courtemanche::Init (56-83)
     const char *init[] = {"Init_Ca_i", "Init_Ca_up", "Init_Ca_rel", "Init_h", "Init_j", "Init_oi",
@@ -808,8 +908,89 @@ void ParamSet::ord_consts(ORDConsts<double> &d, ORDConsts<float> &f) const {
   for (int k = 0; k < nf; k++) dst[k] = (float)src[k];
 }
 
+void ParamSet::tom_consts(TOMConsts<double> &d, TOMConsts<float> &f) const {
+  d.dt_ms = dt * 1000.0;
+  d.RToverF = PV(RToverF);
+  d.FoRT = PV(F) / (PV(R) * PV(T));
+  d.FFoRT = PV(F) * PV(F) / (PV(R) * PV(T));
+  d.RToF = (PV(R) * PV(T)) / PV(F);  // E_Cl's factor, z_Cl = 1 (Tomek.cpp:139-140)
+  d.Na_o = PV(Na_o);
+  d.K_o = PV(K_o);
+  d.Ca_o = PV(Ca_o);
+  d.Cl_o = PV(Cl_o);
+  d.util_1 = PV(A_cap) / (PV(F) * PV(v_myo));
+  d.util_2 = PV(v_ss) / PV(v_myo);
+  d.util_3 = PV(A_cap) / (PV(F) * PV(v_ss));
+  d.vnsr_vmyo = PV(v_nsr) / PV(v_myo);
+  d.vjsr_vss = PV(v_jsr) / PV(v_ss);
+  d.vjsr_vnsr = PV(v_jsr) / PV(v_nsr);
+  d.A_h = PV(A_h);
+  d.A_f_fast = PV(A_f_fast);
+  d.A_f_slow = PV(A_f_slow);
+  d.tau_h_L = PV(tau_h_L);
+  d.tau_h_L_CaMK = 3.0 * PV(tau_h_L);
+  d.INaF = PV(INaF_Multiplier);
+  d.INaL = PV(INaL_Multiplier);
+  d.Ito = PV(Ito_Multiplier);
+  d.IKr = PV(IKr_Multiplier);
+  d.IKs = PV(IKs_Multiplier);
+  d.IK1 = PV(IK1_Multiplier);
+  d.INaCa = PV(INaCa_Multiplier);
+  d.INaK = PV(INaK_Multiplier);
+  d.IKb = PV(IKb_Multiplier);
+  d.INab = PV(INab_Multiplier);
+  d.ICab = PV(ICab_Multiplier);
+  d.IpCa = PV(IpCa_Multiplier);
+  // the reference scales the L-type permeability by IpCa_Multiplier, not PCa_Multiplier (292)
+  d.PCa = PV(IpCa_Multiplier) * 8.3757e-05;
+  d.k_Na1 = PV(k_Na1);
+  d.k_Na2 = PV(k_Na2);
+  d.k_Ca_on = PV(k_Ca_on);
+  d.h_11 = PV(h_11);
+  d.k_1 = PV(k_1);
+  d.k_2 = PV(k_2);
+  d.k_5 = PV(k_5);
+  d.beta_1 = PV(beta_1);
+  d.alpha_2 = PV(alpha_2);
+  d.alpha_4 = PV(alpha_4);
+  d.MgATP1 = 1.0 + PV(MgATP);
+  d.alpha_rel = PV(alpha_rel);
+  d.alpha_rel_CaMK = PV(alpha_rel_CaMK);
+  d.beta_tau = PV(beta_tau);
+  d.beta_tau_CaMK = PV(beta_tau_CaMK);
+  // cell-type branches of Calc: M cells release 1.7x (558-561), epicardial cells take up 1.3x
+  // (576-579), buffer 1.3x calmodulin (606-607) and inactivate I_to faster (delta_epi, 206)
+  const double ct = PV(celltype);
+  d.rel_scale = ct == 2.0 ? 1.7 : 1.0;
+  d.up_scale = ct == 1.0 ? 1.3 : 1.0;
+  d.cmdnmax = ct == 1.0 ? 0.05 * 1.3 : 0.05;
+  d.epi = ct == 1.0 ? 1.0 : 0.0;
+  d.sqrtKo5 = sqrt(PV(K_o) / 5.0);
+  d.EKs_num = PV(K_o) + 0.01833 * PV(Na_o);
+  // activity coefficients of the bath (271-279): ionic strength I_o [M], Davies' constant
+  d.constA = 1.82e6 * pow(74. * 310., -1.5);
+  const double I_o = 0.5 * (PV(Na_o) + PV(K_o) + PV(Cl_o) + 4. * PV(Ca_o)) / 1000.;
+  auto gamma = [&](double z2) { return exp(-d.constA * z2 * (sqrt(I_o) / (1. + sqrt(I_o)) - 0.3 * I_o)); };
+  d.gamma_Ca_o = gamma(4.);
+  d.gamma_Na_o = gamma(1.);
+  d.gamma_K_o = gamma(1.);
+  d.G_sac = PV(G_sac);
+  d.E_sac = PV(E_sac);
+  d.K_sac = PV(K_sac);
+  d.alpha_sac = PV(alpha);
+  d.ISAC_SWITCH = PV(ISAC_SWITCH);
+  d.Ca_T50 = PV(Ca_T50);
+  d.beta1 = PV(beta1);
+  d.k_TRPN = PV(k_TRPN);
+  d.n_TRPN = PV(n_TRPN);
+  const double *src = &d.dt_ms;
+  float *dst = &f.dt_ms;
+  const int nf = (int)(sizeof(TOMConsts<double>) / sizeof(double));
+  for (int k = 0; k < nf; k++) dst[k] = (float)src[k];
+}
+
 void ParamSet::rows_fp64(std::vector<double> &rows, std::vector<double> &eca) const {
-  if (spec->model == kOHaraRudy) {  // no voltage tables
+  if (spec->model == kOHaraRudy || spec->model == kTomek) {  // no voltage tables
     rows.clear();
     eca.clear();
     return;

@@ -10,7 +10,7 @@
 namespace cm {
 
 // Reference ElphyModelType values (ElphyModelBasis.h:62-81).
-enum ModelId { kCourtemanche = 2, kTenTusscher2 = 5, kOHaraRudy = 12 };
+enum ModelId { kCourtemanche = 2, kTenTusscher2 = 5, kOHaraRudy = 12, kTomek = 14 };
 
 struct ParamDef {
   const char *name;
@@ -24,7 +24,7 @@ struct ModelSpec {
   int n_base;
   const char *const *derived;      // names of the values Calculate() derives
   int n_derived;
-  const char *const *table_names;  // reference table array names (none for O'Hara-Rudy)
+  const char *const *table_names;  // reference table array names (none for O'Hara-Rudy, Tomek)
   int n_tables;
   const char *const *state_names;  // SOA state order
   int n_state;
@@ -60,6 +60,7 @@ class ParamSet {
   void tt2_consts(TT2Consts<double> &d, TT2Consts<float> &f) const;
   void crn_consts(CRNConsts<double> &d, CRNConsts<float> &f) const;
   void ord_consts(ORDConsts<double> &d, ORDConsts<float> &f) const;
+  void tom_consts(TOMConsts<double> &d, TOMConsts<float> &f) const;
   // Row-major voltage tables (kRows x cols) and the TT2 ECa table.
   void rows_fp64(std::vector<double> &rows, std::vector<double> &eca) const;
   void rows_fp32(std::vector<float> &rows, std::vector<float> &eca) const;
@@ -69,6 +70,7 @@ class ParamSet {
  private:
   void derive();
   void derive_ord();
+  void derive_tom();
   void build_tables();
 };
 

@@ -39,10 +39,12 @@ def test_abi_version_and_models(cmlib):
     assert L.cm_model_from_name(b"TenTusscher2") == 5
     assert L.cm_model_from_name(b"CourtemancheEtAl") == 2
     assert L.cm_model_from_name(b"OHaraRudy") == 12
+    assert L.cm_model_from_name(b"Tomek") == 14
     assert L.cm_model_from_name(b"OHaraRudyIso") == -1
     assert cmlib.model_info(5).ref_block_doubles == 36
     assert cmlib.model_info(2).ref_block_doubles == 22
     assert cmlib.model_info(12).ref_block_doubles == 59
+    assert cmlib.model_info(14).ref_block_doubles == 84
     assert cmlib.state_names(5)[:5] == ["Ca_i", "CaSR", "CaSS", "Na_i", "K_i"]
     with pytest.raises(cmlib.CMError):
         cmlib.model_info(13)

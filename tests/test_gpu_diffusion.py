@@ -1,5 +1,5 @@
 """GPU parity of the monodomain coupling (cm_diffusion_*, cm_batch_run_diffuse) against the
-oracle's explicit monodomain loop (cmo_mono_run) on tissue sheets, for the three models.
+oracle's explicit monodomain loop (cmo_mono_run) on tissue sheets, for the four models.
 
 Tolerances:
   product alone (FP64)   rtol 1e-13 against the CSR sum in order (the kernel fuses multiply-adds)
@@ -16,10 +16,10 @@ from cardiomechanics_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 DT = 1e-5
-OM = {5: O.TT2, 2: O.CRN, 12: O.ORD}
-AMP = {5: 2 * W.TT2_STIM_NA, 2: 2 * W.CRN_STIM_PAPF, 12: 2 * W.ORD_STIM}
-HET = {5: W.TT2_HETERO, 2: W.CRN_HETERO, 12: W.ORD_HETERO}
-TLEN = {5: 1e-3, 2: 2e-3, 12: 1e-3}  # Courtemanche: its own 2 ms stimulus (CourtemancheEtAl.h:54)
+OM = {5: O.TT2, 2: O.CRN, 12: O.ORD, 14: O.TOM}
+AMP = {5: 2 * W.TT2_STIM_NA, 2: 2 * W.CRN_STIM_PAPF, 12: 2 * W.ORD_STIM, 14: 2 * W.TOM_STIM}
+HET = {5: W.TT2_HETERO, 2: W.CRN_HETERO, 12: W.ORD_HETERO, 14: W.TOM_HETERO}
+TLEN = {5: 1e-3, 2: 2e-3, 12: 1e-3, 14: 1e-3}  # Courtemanche: its own 2 ms stimulus (CourtemancheEtAl.h:54)
 
 
 def csr_random(n, seed=3):
@@ -67,7 +67,7 @@ def sheet(cm, port, model, precision, nx, ny, steps, *, seed=1):
     n = nx * ny
     rp, col, val = W.grid_laplacian(nx, ny)
     p = cm.Params(model, None, DT)
-    P = port.param_vector(OM[model], O.load_params(OM[model], "endo" if model == 12 else "epi"))
+    P = port.param_vector(OM[model], O.load_params(OM[model], "endo" if model in (12, 14) else "epi"))
     names = port.param_names(OM[model])
     sc = W.conductance_scales(seed, n, 3, 0.95, 1.05)
     het = {k: P[names.index(k)] * sc[i] for i, k in enumerate(HET[model])}
@@ -80,7 +80,7 @@ def sheet(cm, port, model, precision, nx, ny, steps, *, seed=1):
     act = np.full(n, -1.0)
     b.run_diffuse(d, vm, steps, textbegin_per_cell=tb, textlen=TLEN[model], bcl=1.0, amplitude=AMP[model], act=act,
                   act_threshold=-0.02, vm_range=0.2)
-    T = port.tables(OM[model], P, DT) if model != 12 else np.zeros((0, O.RTDT))
+    T = port.tables(OM[model], P, DT) if model not in (12, 14) else np.zeros((0, O.RTDT))
     B = port.init_state(OM[model], P, n)
     vo = np.full(n, port.init_vm(OM[model], P))
     ao = np.full(n, -1.0)
@@ -90,7 +90,7 @@ def sheet(cm, port, model, precision, nx, ny, steps, *, seed=1):
     return b, vm, vo, act, ao
 
 
-@pytest.mark.parametrize("model,nx,ny,steps", [(5, 48, 16, 2500), (2, 40, 12, 2500), (12, 32, 10, 2000)])
+@pytest.mark.parametrize("model,nx,ny,steps", [(5, 48, 16, 2500), (2, 40, 12, 2500), (12, 32, 10, 2000), (14, 32, 10, 2000)])
 def test_sheet_fp64(gpu, port, model, nx, ny, steps):
     b, vm, vo, act, ao = sheet(gpu, port, model, gpu.FP64, nx, ny, steps)
     assert np.sum(ao >= 0) > nx * ny // 3          # the wave crossed a good part of the sheet
@@ -100,7 +100,7 @@ def test_sheet_fp64(gpu, port, model, nx, ny, steps):
     assert b.audit() == 0
 
 
-@pytest.mark.parametrize("model,nx,ny,steps", [(5, 48, 16, 2500), (2, 40, 12, 2500), (12, 32, 10, 2000)])
+@pytest.mark.parametrize("model,nx,ny,steps", [(5, 48, 16, 2500), (2, 40, 12, 2500), (12, 32, 10, 2000), (14, 32, 10, 2000)])
 def test_sheet_mixed(gpu, port, model, nx, ny, steps):
     b, vm, vo, act, ao = sheet(gpu, port, model, gpu.MIXED, nx, ny, steps)
     hit = ao >= 0
