@@ -70,6 +70,18 @@ ORD_CELLS = 2048 * 2048
 ORD_BCL = 1.0
 ORD_MIXED_BYTES_PER_CELL_STEP = 2 * (35 + 12) * 4 + 2 * 2 * 4 + 3 * 4
 ORD_FP64_BYTES_PER_CELL_STEP = 2 * 41 * 8 + 2 * 8 + 3 * 8
+# Tomek: 38 FP32 states + 6 compensated pairs; 44 FP64 states (Vm pair and 3 multipliers as ORd)
+TOM_MIXED_BYTES_PER_CELL_STEP = 2 * (38 + 12) * 4 + 2 * 2 * 4 + 3 * 4
+TOM_FP64_BYTES_PER_CELL_STEP = 2 * 44 * 8 + 2 * 8 + 3 * 8
+# The closed-form ventricular models timed beside the headline: the model's C-ABI id, the
+# oracle's, its workload name, stimulus and bytes per cell step (mixed, FP64).
+IONIC_LEGS = {
+    "ohara_rudy": dict(model=12, oracle="ORD", label="ord2011", title="O'Hara-Rudy", stim="ORD_STIM",
+                       het="ORD_HETERO", mixed_bytes=ORD_MIXED_BYTES_PER_CELL_STEP,
+                       fp64_bytes=ORD_FP64_BYTES_PER_CELL_STEP),
+    "tomek": dict(model=14, oracle="TOM", label="tomek2019", title="Tomek", stim="TOM_STIM", het="TOM_HETERO",
+                  mixed_bytes=TOM_MIXED_BYTES_PER_CELL_STEP, fp64_bytes=TOM_FP64_BYTES_PER_CELL_STEP),
+}
 # Tissue leg (monodomain coupling): a 256 x 256 x 64 slab of TT2 epi cells on a 0.1 mm grid
 # (D = 0.1 mm^2/ms, 7-point operator, no-flux faces), the x < 3 planes stimulated once. Mixed
 # form per node-step: 21 state planes r+w (168 B), Vm hi/lo read + new hi/lo written (16 B), 3
@@ -555,54 +567,67 @@ def plain_small_leg(cm, torch, stream, steps=2000):
             "note": "65,536 cells leave most of the GPU's FP64 pipes idle; the 4.2M-cell figure is plain_fp64"}
 
 
-class ORDCPUSample:
-    """The oracle's O'Hara-Rudy (C restatement of the reference Calc, FP64) on the first `cells`
-    cells of the O'Hara-Rudy leg, all host threads."""
+class IonicCPUSample:
+    """The oracle's restatement of a closed-form ventricular model (O'Hara-Rudy or Tomek, the
+    reference Calc in FP64) on the first `cells` cells of that model's leg, all host threads."""
 
-    def __init__(self, cells=2048, threads=None):
+    def __init__(self, leg, cells=2048, threads=None):
         import oracle as O
         from cardiomechanics_gb300 import workloads as W
         self.O, self.W, self.port = O, W, O.Port()
+        self.spec = IONIC_LEGS[leg]
+        self.m = getattr(O, self.spec["oracle"])
+        self.stim = getattr(W, self.spec["stim"])
         self.threads = threads or os.cpu_count() or 1
         self.cells = cells
-        self.P = self.port.param_vector(O.ORD, O.load_params(O.ORD, "endo"))
+        self.P = self.port.param_vector(self.m, O.load_params(self.m, "endo"))
         sc = W.conductance_scales(3, ORD_CELLS, 3, 0.9, 1.1, cells=np.arange(cells))
-        names = self.port.param_names(O.ORD)
-        self.het = {k: self.P[names.index(k)] * sc[i] for i, k in enumerate(W.ORD_HETERO)}
-        self.B = self.port.init_state(O.ORD, self.P, cells)
-        self.vm = np.full(cells, self.port.init_vm(O.ORD, self.P))
+        names = self.port.param_names(self.m)
+        self.het = {k: self.P[names.index(k)] * sc[i] for i, k in enumerate(getattr(W, self.spec["het"]))}
+        self.B = self.port.init_state(self.m, self.P, cells)
+        self.vm = np.full(cells, self.port.init_vm(self.m, self.P))
 
     def rate(self, seconds):
         done, el, t = 0, 0.0, 0.0
         while el < seconds:
             t0 = time.perf_counter()
-            self.port.run(self.O.ORD, self.P, np.zeros((0, self.O.RTDT)), self.B, self.vm, 200, DT, t0=t,
-                          textbegin=0.0, textlen=1e-3, bcl=1e9, amp=self.W.ORD_STIM, het=self.het,
+            self.port.run(self.m, self.P, np.zeros((0, self.O.RTDT)), self.B, self.vm, 200, DT, t0=t,
+                          textbegin=0.0, textlen=1e-3, bcl=1e9, amp=self.stim, het=self.het,
                           n_threads=self.threads)
             el += time.perf_counter() - t0
             done += 200
             t += 200 * DT
         return {"value": self.cells * done / el, "unit": UNIT, "cores": self.threads, "kind": "port",
-                "sample": f"first {self.cells} of the {ORD_CELLS} O'Hara-Rudy cells x {done} steps of 0.01 ms "
-                          f"(oracle C restatement of the reference Calc in FP64, {self.threads} threads, {el:.1f} s)"}
+                "sample": f"first {self.cells} of the {ORD_CELLS} {self.spec['title']} cells x {done} steps of "
+                          f"0.01 ms (oracle C restatement of the reference Calc in FP64, {self.threads} threads, "
+                          f"{el:.1f} s)"}
 
 
-def ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak=None, cpu_seconds=0.0):
-    """O'Hara-Rudy 2011 (the reference's variant), 4,194,304 endocardial cells: the mixed form
-    (autotuned launch shape) and the plain FP64 form, each timed with events on its stream."""
+def ionic_leg(cm, torch, stream, args, hbm_peak, peak_kind, leg, fp64_peak=None, cpu_seconds=0.0):
+    """A closed-form ventricular model (O'Hara-Rudy 2011 or Tomek 2019, the reference's
+    variants), 4,194,304 endocardial cells: the mixed form (autotuned launch shape) and the
+    plain FP64 form, each timed with events on its stream."""
     from cardiomechanics_gb300 import workloads as W
+    spec = IONIC_LEGS[leg]
+    stim = getattr(W, spec["stim"])
+    hetn = getattr(W, spec["het"])
     n = args.ord_cells
-    p = cm.Params(cm.OHARARUDY, None, DT)
+    p = cm.Params(spec["model"], None, DT)
     sc = W.conductance_scales(3, n, 3, 0.9, 1.1)
-    kw = dict(textbegin=0.0, textlen=1e-3, bcl=ORD_BCL, amplitude=W.ORD_STIM)
-    out = {"workload": f"ord2011-endo-{n}-cells", "cells": n, "bcl_ms": ORD_BCL * 1e3,
-           "conductance_jitter": "INaF,IKr,IK1 multipliers x U[0.9,1.1] seed 3", "stimulus": "-50 uA/uF x 1 ms"}
+    kw = dict(textbegin=0.0, textlen=1e-3, bcl=ORD_BCL, amplitude=stim)
+    out = {"workload": f"{spec['label']}-endo-{n}-cells", "cells": n, "bcl_ms": ORD_BCL * 1e3,
+           "conductance_jitter": "INaF,IKr,IK1 multipliers x U[0.9,1.1] seed 3",
+           "stimulus": f"{stim:g} uA/uF x 1 ms"}
     for prec, steps, name in ((cm.MIXED, args.ord_steps, "mixed"), (cm.FP64, args.fp64_steps, "fp64")):
         b = cm.Batch(p, n, prec, stream=stream.cuda_stream)
-        for k, h in enumerate(W.ORD_HETERO):
+        for k, h in enumerate(hetn):
             b.add_hetero_value(h, p.get(h) * sc[k])
         tuned = None
-        if prec == cm.MIXED:
+        if prec == cm.MIXED and args.launch:
+            v, g = (int(x) for x in args.launch.split(","))
+            b.set_launch(v, g)
+            tuned = (f"{v},{g} (fixed)", None)
+        elif prec == cm.MIXED:
             tuned = b.autotune(args.tune_steps)
         vm = torch.tensor(b.init_vm(), device="cuda")
         b.run(vm, 3, **kw)
@@ -614,26 +639,26 @@ def ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak=None, cpu_se
         e1.record(stream)
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
-        bps = ORD_MIXED_BYTES_PER_CELL_STEP if prec == cm.MIXED else ORD_FP64_BYTES_PER_CELL_STEP
+        bps = spec["mixed_bytes"] if prec == cm.MIXED else spec["fp64_bytes"]
         achieved = bps * n * steps / sec / 1e9
-        leg = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+        res = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
                "audit_mask": b.audit(), "gpu_launches": steps,
                "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                        "peak_kind": peak_kind, "bytes_per_cell_step": bps}}
         if tuned is not None:
-            leg["autotune"] = {"choice": tuned[0], "ms_per_step": tuned[1]}
-            leg["precision"] = "mixed (FP32 gates/currents, compensated FP32 pairs for Vm, Na_i, Na_ss, K_i, " \
+            res["autotune"] = {"choice": tuned[0], "ms_per_step": tuned[1]}
+            res["precision"] = "mixed (FP32 gates/currents, compensated FP32 pairs for Vm, Na_i, Na_ss, K_i, " \
                                "K_ss, Ca_nsr, Ca_jsr)"
         else:
-            leg["precision"] = "FP64 (the reference arithmetic)"
+            res["precision"] = "FP64 (the reference arithmetic)"
             if fp64_peak:
-                leg["fp64_fma_peak_tflops_measured"] = fp64_peak
-        out[name] = leg
+                res["fp64_fma_peak_tflops_measured"] = fp64_peak
+        out[name] = res
         del b, vm
         torch.cuda.empty_cache()
     out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     if cpu_seconds > 0:
-        out["cpu_baseline"] = ORDCPUSample().rate(cpu_seconds)
+        out["cpu_baseline"] = IonicCPUSample(leg).rate(cpu_seconds)
     return out
 
 
@@ -759,7 +784,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
-                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tissue"],
+                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tomek", "tissue"],
                     help="run one leg only (profiler captures); the contract's JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
@@ -771,9 +796,11 @@ def main():
     ap.add_argument("--sur-train-frac", type=float, default=1.0,
                     help="fraction of the surrogate's training run (profiling captures only; accuracy needs 1)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
-    ap.add_argument("--ord-steps", type=int, default=500, help="timed steps of the O'Hara-Rudy mixed form")
-    ap.add_argument("--ord-cells", type=int, default=ORD_CELLS, help="O'Hara-Rudy cells (fewer only for captures)")
-    ap.add_argument("--no-ord", action="store_true")
+    ap.add_argument("--ord-steps", type=int, default=500,
+                    help="timed steps of the O'Hara-Rudy and Tomek mixed forms")
+    ap.add_argument("--ord-cells", type=int, default=ORD_CELLS,
+                    help="O'Hara-Rudy and Tomek cells (fewer only for captures)")
+    ap.add_argument("--no-ord", action="store_true", help="skip the O'Hara-Rudy and Tomek legs")
     ap.add_argument("--tissue-steps", type=int, default=500, help="timed steps of the coupled (tissue) leg")
     ap.add_argument("--tissue-dims", type=int, nargs=3, default=None, help="slab size (fewer nodes only for captures)")
     ap.add_argument("--no-tissue", action="store_true")
@@ -808,9 +835,10 @@ def main():
     if args.only == "tissue":
         print(json.dumps(tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
         return
-    if args.only == "ord":
-        print(json.dumps(ord_leg(cm, torch, stream, args, hbm_peak, peak_kind,
-                                 cpu_seconds=0.0 if args.no_cpu else 5.0)), flush=True)
+    if args.only in ("ord", "tomek"):
+        leg = "ohara_rudy" if args.only == "ord" else "tomek"
+        print(json.dumps(ionic_leg(cm, torch, stream, args, hbm_peak, peak_kind, leg,
+                                   cpu_seconds=0.0 if args.no_cpu else 5.0)), flush=True)
         return
     p, sur, training = train_surrogate(cm, stream, args.sur_train_frac)
     if args.only == "surrogate":
@@ -844,10 +872,11 @@ def main():
     if not args.no_batched:
         bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
     tissue = None if args.no_tissue else tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)
-    ordl = None
-    if not args.no_ord:
-        ordl = ord_leg(cm, torch, stream, args, hbm_peak, peak_kind, fp64_peak,
-                       cpu_seconds=5.0 if (rank == 0 and not args.no_cpu) else 0.0)
+    ionic = {}
+    for leg in IONIC_LEGS:
+        ionic[leg] = None if args.no_ord else ionic_leg(
+            cm, torch, stream, args, hbm_peak, peak_kind, leg, fp64_peak,
+            cpu_seconds=5.0 if (rank == 0 and not args.no_cpu) else 0.0)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(seconds=args.cpu_seconds)
@@ -878,7 +907,8 @@ def main():
             "plain_small": small,
             "learned_form": learned,
             "batched": bat,
-            "ohara_rudy": ordl,
+            "ohara_rudy": ionic["ohara_rudy"],
+            "tomek": ionic["tomek"],
             "tissue": tissue,
             "fp32_fma_peak_tflops_measured": fp32_peak,
             "cpu_baseline": cpu,
