@@ -52,10 +52,11 @@ UNIT = "cell-steps/s"
 # CaSR/Na_i/K_i compensated pairs (2 x FP32 each) read and written (168 B), the Vm hi/lo
 # pair read and written (16 B), 3 FP32 per-cell conductances read (12 B).
 MIXED_BYTES_PER_CELL_STEP = 2 * (15 * 4 + 3 * 8) + 2 * 8 + 3 * 4
-# Launch shapes of cm_batch_set_launch (variant index -> kernel); 5 and 6 are bulk-copy staged.
+# Launch shapes of cm_batch_set_launch (variant index -> kernel); 5 and 6 are bulk-copy staged,
+# 7 and 8 the same with a producer warp and mbarrier hand-over.
 MIXED_KERNELS = ["tt2_mixed_kernel<256>", "tt2_mixed_kernel<128>", "tt2_mixed_kernel<256,3>",
                  "tt2_mixed_kernel<512>", "tt2_mixed_kernel<64>", "mixed_staged_kernel<5,256>",
-                 "mixed_staged_kernel<5,128>"]
+                 "mixed_staged_kernel<5,128>", "mixed_pipe_kernel<5,256,2>", "mixed_pipe_kernel<5,128,3>"]
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu capture summarised in
 # profiles/mixed_staged_tt2_4M_cells.md (same workload, launch shape 6, grid mode 4).
 MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808}

@@ -28,6 +28,10 @@ static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint
       : "memory");
 }
 
+static __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // true when the phase with the given parity has completed; false after kSpinLimit polls
 static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);

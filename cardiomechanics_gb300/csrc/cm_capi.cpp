@@ -675,8 +675,9 @@ int cm_batch_autotune(cm_batch_t b, int n_trial_steps, int *variant, double *ms_
       StepIO io;
       io.vm_hi = (float *)vm;  // the trial Vm as compensated planes
       io.vm_lo = (float *)vm + ld;
-      // the last two variants are the staged kernels; a batch they do not cover would time shape 0
-      if (v >= n_shape_variants() - 2 && !staged_supported(d, io)) continue;
+      // the variants past the register shapes are the staged kernels; a batch they do not cover
+      // would time shape 0
+      if (v >= n_register_shapes() && !staged_supported(d, io)) continue;
       for (int k = 0; k < 2 && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);
       if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
       for (int k = 0; k < n_trial_steps && e == cudaSuccess; k++) e = launch_step(d, io, v, g, b->stream);

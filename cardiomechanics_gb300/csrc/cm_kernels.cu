@@ -367,9 +367,12 @@ void launch_mixed_variant(const DevBatch &b, const StepIO &io, int v, int grid, 
 }
 }  // namespace
 
-// Variants past the register-budget shapes are the shared-memory-staged kernels (256 and
-// 128 threads per block); they apply to fused runs and fall back to shape 0 elsewhere.
-int n_shape_variants() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])) + 2; }
+// Variants past the register-budget shapes are the shared-memory-staged kernels: the
+// double-buffered block (256 and 128 threads per block), then the producer/consumer pipeline
+// (256 consumer threads with 2 stages, 128 with 3). They apply to fused runs and fall back to
+// shape 0 elsewhere.
+int n_register_shapes() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
+int n_shape_variants() { return n_register_shapes() + 4; }
 
 cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int grid_mode, cudaStream_t s) {
   if (b.n == 0) return cudaSuccess;
@@ -399,9 +402,13 @@ cudaError_t launch_step(const DevBatch &b, const StepIO &io, int variant, int gr
   // coupled runs of TT2 / Courtemanche: the staged kernel with the operator staged too
   if (io.sl_ptr && coupled_staged_supported(b, io)) return launch_coupled_staged(b, io, s);
   if (variant < 0 || variant >= n_shape_variants()) variant = 0;
-  const int n_plain = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+  const int n_plain = n_register_shapes();
   if (variant >= n_plain) {
-    if (staged_supported(b, io)) return launch_staged(b, io, variant == n_plain ? 256 : 128, grid_mode, s);
+    if (staged_supported(b, io)) {
+      const int k = variant - n_plain;
+      return k < 2 ? launch_staged(b, io, k == 0 ? 256 : 128, grid_mode, s)
+                   : launch_pipe(b, io, k == 2 ? 256 : 128, grid_mode, s);
+    }
     variant = 0;
   }
   const Shape sh = io.sl_ptr ? Shape{256, 2} : kShapes[variant];  // coupled runs: one shape

@@ -97,6 +97,9 @@ int n_shape_variants();
 // stimulus, leading dimension a multiple of 256, planes lo = hi + ld).
 bool staged_supported(const DevBatch &b, const StepIO &io);
 cudaError_t launch_staged(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s);
+// The staged kernel as a producer/consumer pipeline (one bulk-copy warp, mbarrier hand-over).
+cudaError_t launch_pipe(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s);
+int n_register_shapes();  // variants below this index are the register kernels
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.
 cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
                          int64_t n_probe, double *out, int64_t stride, int64_t k, cudaStream_t s);

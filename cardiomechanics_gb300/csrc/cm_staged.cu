@@ -23,8 +23,7 @@ namespace {
 template <int kModel, int kThreads>
 __global__ void __launch_bounds__(kThreads, 2) mixed_staged_kernel(const DevBatch b, const StepIO io) {
   constexpr int NS = StagedVars<kModel>::kState;
-  constexpr int NVMAX = NS + 2 + 6;
-  extern __shared__ __align__(128) float stage[];  // [2][NVMAX][kThreads]
+  extern __shared__ __align__(128) float stage[];  // [2][nv][kThreads]
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ int s_abort;
   const int64_t ld = b.ld;
@@ -36,6 +35,7 @@ __global__ void __launch_bounds__(kThreads, 2) mixed_staged_kernel(const DevBatc
 #pragma unroll
   for (int k = 0; k < 6; k++) het_pos[k] = b.het[k] ? nv++ : -1;
   const uint32_t tile_bytes = (uint32_t)nv * kThreads * 4u;
+  const size_t buf_floats = (size_t)nv * kThreads;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kThreads, 2) mixed_staged_kernel(const DevBatc
   }
   __syncthreads();
   auto issue = [&](int tile, int buf) {
-    float *dst = stage + (size_t)buf * NVMAX * kThreads;
+    float *dst = stage + buf * buf_floats;
     const int64_t c0 = (int64_t)tile * kThreads;
     mbar_expect_tx(&bar[buf], tile_bytes);
     for (int v = 0; v < NS; v++) bulk_g2s(dst + v * kThreads, b.s32 + v * ld + c0, kThreads * 4u, &bar[buf]);
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kThreads, 2) mixed_staged_kernel(const DevBatc
       if (next < n_tiles) mbar_wait(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
       return;
     }
-    const float *S = stage + (size_t)buf * NVMAX * kThreads + threadIdx.x;
+    const float *S = stage + buf * buf_floats + threadIdx.x;
     const int c = t * kThreads + threadIdx.x;
     if (c >= n) continue;
     staged_cell<kModel, kThreads>(b, S, het_pos, c, (float)io.iext_uniform, io.vm_hi, io.vm_lo);
@@ -83,10 +83,15 @@ __global__ void __launch_bounds__(kThreads, 2) mixed_staged_kernel(const DevBatc
 
 template <int kModel, int kThreads>
 cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_sm, cudaStream_t s) {
+  // the stage holds the state planes, the Vm pair and the present hetero planes, twice; the
+  // attribute allows all six hetero planes, a launch takes what its batch stages
   constexpr int NVMAX = StagedVars<kModel>::kState + 2 + 6;
-  const size_t smem = (size_t)2 * NVMAX * kThreads * sizeof(float);
+  int nv = StagedVars<kModel>::kState + 2;
+  for (int k = 0; k < 6; k++) nv += b.het[k] ? 1 : 0;
+  const size_t smem = (size_t)2 * nv * kThreads * sizeof(float);
   static std::atomic<uint64_t> done{0};  // one attribute call per instantiation and device
-  cudaError_t e = smem_limit((const void *)mixed_staged_kernel<kModel, kThreads>, (int)smem, done);
+  cudaError_t e = smem_limit((const void *)mixed_staged_kernel<kModel, kThreads>,
+                             (int)((size_t)2 * NVMAX * kThreads * sizeof(float)), done);
   if (e != cudaSuccess) return e;
   const int n_tiles = (int)((b.n + kThreads - 1) / kThreads);
   int grid = sm_count() * (blocks_per_sm > 0 ? blocks_per_sm : 2);
@@ -94,6 +99,109 @@ cudaError_t launch_staged_t(const DevBatch &b, const StepIO &io, int blocks_per_
   if (grid < 1) grid = 1;
   mixed_staged_kernel<kModel, kThreads><<<grid, kThreads, smem, s>>>(b, io);
   return cudaGetLastError();
+}
+
+// The staged kernel as a producer/consumer pipeline: one extra warp only issues the tiles' bulk
+// copies into kStages stage buffers; the kThreads / 32 consumer warps integrate. A stage is
+// handed over by two mbarriers: `full` (the producer's expect_tx plus the copies' bytes) and
+// `empty` (one arrival per consumer warp when it is done with the stage). No block-wide barrier
+// inside the loop: a warp that finishes its part of a tile moves on to the next staged tile
+// while slower warps still work on this one.
+//
+// Every wait is bounded. A consumer whose `full` wait runs out sets CM_AUDIT_TIMEOUT and leaves;
+// the producer then runs out on `empty`, sets the same bit, waits (bounded) for the copies it
+// issued that no consumer took, and leaves.
+template <int kModel, int kThreads, int kStages>
+__global__ void __launch_bounds__(kThreads + 32, 2) mixed_pipe_kernel(const DevBatch b, const StepIO io) {
+  constexpr int NS = StagedVars<kModel>::kState;
+  constexpr int kWarps = kThreads / 32;
+  extern __shared__ __align__(128) float stage[];  // [kStages][nv][kThreads]
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+  const int64_t ld = b.ld;
+  const int n = (int)b.n;
+  const int n_tiles = (n + kThreads - 1) / kThreads;
+  int het_pos[6];
+  int nv = NS + 2;
+#pragma unroll
+  for (int k = 0; k < 6; k++) het_pos[k] = b.het[k] ? nv++ : -1;
+  const uint32_t tile_bytes = (uint32_t)nv * kThreads * 4u;
+  const size_t buf_floats = (size_t)nv * kThreads;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < kStages; k++) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], kWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x >= kThreads) {  // the producer warp: lane 0 issues, the other lanes leave
+    if (threadIdx.x != kThreads) return;
+    int it = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
+      const int st = it % kStages;
+      if (it >= kStages && !mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1))) {
+        atomicOr(b.audit_or, kAuditTimeout);
+        // the copies of the last kStages tiles may still be landing: wait for them, bounded
+        for (int j = it - kStages; j < it; j++)
+          if (j >= 0) mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1));
+        return;
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      float *dst = stage + st * buf_floats;
+      const int64_t c0 = (int64_t)t * kThreads;
+      mbar_expect_tx(&full[st], tile_bytes);
+      for (int v = 0; v < NS; v++) bulk_g2s(dst + v * kThreads, b.s32 + v * ld + c0, kThreads * 4u, &full[st]);
+      bulk_g2s(dst + NS * kThreads, io.vm_hi + c0, kThreads * 4u, &full[st]);
+      bulk_g2s(dst + (NS + 1) * kThreads, io.vm_lo + c0, kThreads * 4u, &full[st]);
+      for (int k = 0; k < 6; k++)
+        if (het_pos[k] >= 0)
+          bulk_g2s(dst + het_pos[k] * kThreads, (const float *)b.het[k] + c0, kThreads * 4u, &full[st]);
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  int it = 0;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
+    const int st = it % kStages;
+    if (!mbar_wait(&full[st], (uint32_t)((it / kStages) & 1))) {
+      atomicOr(b.audit_or, kAuditTimeout);
+      return;
+    }
+    const int c = t * kThreads + threadIdx.x;
+    if (c < n)
+      staged_cell<kModel, kThreads>(b, stage + st * buf_floats + threadIdx.x, het_pos, c, (float)io.iext_uniform,
+                                    io.vm_hi, io.vm_lo);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+  }
+}
+
+template <int kModel, int kThreads, int kStages>
+cudaError_t launch_pipe_t(const DevBatch &b, const StepIO &io, int blocks_per_sm, cudaStream_t s) {
+  constexpr int NVMAX = StagedVars<kModel>::kState + 2 + 6;
+  int nv = StagedVars<kModel>::kState + 2;
+  for (int k = 0; k < 6; k++) nv += b.het[k] ? 1 : 0;
+  const size_t smem = (size_t)kStages * nv * kThreads * sizeof(float);
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)mixed_pipe_kernel<kModel, kThreads, kStages>,
+                             (int)((size_t)kStages * NVMAX * kThreads * sizeof(float)), done);
+  if (e != cudaSuccess) return e;
+  const int n_tiles = (int)((b.n + kThreads - 1) / kThreads);
+  int grid = sm_count() * (blocks_per_sm > 0 ? blocks_per_sm : 2);
+  if (grid > n_tiles) grid = n_tiles;
+  if (grid < 1) grid = 1;
+  mixed_pipe_kernel<kModel, kThreads, kStages><<<grid, kThreads + 32, smem, s>>>(b, io);
+  return cudaGetLastError();
+}
+
+template <int kThreads, int kStages>
+cudaError_t launch_pipe_m(const DevBatch &b, const StepIO &io, int blocks_per_sm, cudaStream_t s) {
+  switch (b.model) {
+    case 5: return launch_pipe_t<5, kThreads, kStages>(b, io, blocks_per_sm, s);
+    case 2: return launch_pipe_t<2, kThreads, kStages>(b, io, blocks_per_sm, s);
+    case 12: return launch_pipe_t<12, kThreads, kStages>(b, io, blocks_per_sm, s);
+    default: return launch_pipe_t<14, kThreads, kStages>(b, io, blocks_per_sm, s);
+  }
 }
 
 // Coupled runs (cm_batch_run_diffuse): the staged kernel plus the tile's monodomain operator.
@@ -255,10 +363,15 @@ cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, cudaStrea
 }
 
 bool staged_supported(const DevBatch &b, const StepIO &io) {
-  return (b.model == 5 || b.model == 2) && b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext &&
+  return (b.model == 5 || b.model == 2 || b.model == 12 || b.model == 14) && b.precision == 1 && io.vm_hi && io.vm_lo && !io.tb_cell && !io.iext &&
          !io.sl_ptr && !io.vm_hi_out && !io.act && io.vm_range <= 0.0 &&
          b.ld % 256 == 0 &&
          io.vm_lo == io.vm_hi + b.ld && b.n < (int64_t)1 << 30;
+}
+
+cudaError_t launch_pipe(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s) {
+  if (b.n == 0) return cudaSuccess;
+  return threads == 128 ? launch_pipe_m<128, 3>(b, io, blocks_per_sm, s) : launch_pipe_m<256, 2>(b, io, blocks_per_sm, s);
 }
 
 cudaError_t launch_staged(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s) {
@@ -266,6 +379,14 @@ cudaError_t launch_staged(const DevBatch &b, const StepIO &io, int threads, int 
   if (b.model == 5) {
     if (threads == 128) return launch_staged_t<5, 128>(b, io, blocks_per_sm, s);
     return launch_staged_t<5, 256>(b, io, blocks_per_sm, s);
+  }
+  if (b.model == 12) {
+    if (threads == 128) return launch_staged_t<12, 128>(b, io, blocks_per_sm, s);
+    return launch_staged_t<12, 256>(b, io, blocks_per_sm, s);
+  }
+  if (b.model == 14) {
+    if (threads == 128) return launch_staged_t<14, 128>(b, io, blocks_per_sm, s);
+    return launch_staged_t<14, 256>(b, io, blocks_per_sm, s);
   }
   if (threads == 128) return launch_staged_t<2, 128>(b, io, blocks_per_sm, s);
   return launch_staged_t<2, 256>(b, io, blocks_per_sm, s);

@@ -18,6 +18,58 @@ template <>
 struct StagedVars<2> {
   static constexpr int kState = 25;
 };
+template <>
+struct StagedVars<12> {
+  static constexpr int kState = kORDPlain + 12;  // O'Hara-Rudy mixed planes
+};
+template <>
+struct StagedVars<14> {
+  static constexpr int kState = kTOMPlain + 12;  // Tomek mixed planes
+};
+
+// O'Hara-Rudy (12) / Tomek (14) state store over a staged tile: every state is read from the
+// stage when ord_calc / tom_calc reaches it (a shared-memory load, no long wait), every new value
+// goes straight to its global plane.
+template <int kModel, int kT>
+struct StagedStore {
+  const float *S;  // this cell's column of the stage (plane stride kT)
+  float *s;        // this cell's global planes (stride ld)
+  int64_t ld;
+  __device__ __forceinline__ static int plane(int k, bool &pair) {
+    return kModel == 12 ? ord_mixed_plane(k, pair) : tom_mixed_plane(k, pair);
+  }
+  __device__ __forceinline__ void fetch(int) {}
+  __device__ __forceinline__ float get(int k) const {
+    bool pair;
+    return S[plane(k, pair) * kT];
+  }
+  __device__ __forceinline__ void set(int k, float x) {
+    bool pair;
+    s[plane(k, pair) * ld] = x;
+  }
+  // compensated add on the (hi, lo) pair; x is the hi word get() returned
+  __device__ __forceinline__ void add(int k, float x, float d) {
+    bool pair;
+    const int q = plane(k, pair);
+    Acc a{x, S[(q + 1) * kT]};
+    acc_add(a, d);
+    s[q * ld] = a.hi;
+    s[(q + 1) * ld] = a.lo;
+  }
+  __device__ __forceinline__ void cur(int, float) {}
+};
+
+template <int kT, typename CT>
+__device__ __forceinline__ ORDHet_<float> staged_ord_het(const CT &C, const float *S, const int (&het_pos)[6]) {
+  ORDHet_<float> g;
+  g.INaF = het_pos[HO_INaF] >= 0 ? S[het_pos[HO_INaF] * kT] : C.INaF;
+  g.INaL = het_pos[HO_INaL] >= 0 ? S[het_pos[HO_INaL] * kT] : C.INaL;
+  g.Ito = het_pos[HO_Ito] >= 0 ? S[het_pos[HO_Ito] * kT] : C.Ito;
+  g.IKr = het_pos[HO_IKr] >= 0 ? S[het_pos[HO_IKr] * kT] : C.IKr;
+  g.IKs = het_pos[HO_IKs] >= 0 ? S[het_pos[HO_IKs] * kT] : C.IKs;
+  g.IK1 = het_pos[HO_IK1] >= 0 ? S[het_pos[HO_IK1] * kT] : C.IK1;
+  return g;
+}
 
 // S: stage + threadIdx.x; planes 0..NS-1 state, NS / NS+1 Vm hi / lo, het_pos[k] the present
 // conductance slots (-1: parameter-set value).
@@ -31,7 +83,13 @@ __device__ __forceinline__ Acc staged_cell(const DevBatch &b, const float *S, co
   uint32_t audit = 0;
   Acc vm{S[NS * kThreads], S[(NS + 1) * kThreads]};
   float *s = b.s32 + c;
-  if (kModel == 5) {
+  if constexpr (kModel == 12) {
+    StagedStore<12, kThreads> x{S, s, ld};
+    acc_add(vm, ord_calc<float>(b.ord_32, x, staged_ord_het<kThreads>(b.ord_32, S, het_pos), vm.hi, iext, 1.f));
+  } else if constexpr (kModel == 14) {
+    StagedStore<14, kThreads> x{S, s, ld};
+    acc_add(vm, tom_calc<float>(b.tom_32, x, staged_ord_het<kThreads>(b.tom_32, S, het_pos), vm.hi, iext, 1.f));
+  } else if constexpr (kModel == 5) {
     const TT2Consts<float> &C = b.tt2_32;
     TT2Cell<float> x;
     x.m = S[0]; x.h = S[kThreads]; x.j = S[2 * kThreads]; x.xr1 = S[3 * kThreads]; x.xr2 = S[4 * kThreads];

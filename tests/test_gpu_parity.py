@@ -20,9 +20,9 @@ pytestmark = pytest.mark.gpu
 
 TAG = {5: "tt2", 2: "crn"}
 OM = {5: O.TT2, 2: O.CRN}
-HET = {5: W.TT2_HETERO, 2: W.CRN_HETERO}
-AMP = {5: W.TT2_STIM_NA, 2: W.CRN_STIM_PAPF}
-TLEN = {5: 1e-3, 2: 2e-3}
+HET = {5: W.TT2_HETERO, 2: W.CRN_HETERO, 12: W.ORD_HETERO, 14: W.TOM_HETERO}
+AMP = {5: W.TT2_STIM_NA, 2: W.CRN_STIM_PAPF, 12: W.ORD_STIM, 14: W.TOM_STIM}
+TLEN = {5: 1e-3, 2: 2e-3, 12: 1e-3, 14: 1e-3}
 
 
 def ref_block_cols(model):
@@ -292,16 +292,17 @@ def test_full_size_determinism_mixed(gpu):
     assert b.audit() == 0
 
 
-@pytest.mark.parametrize("model", [5, 2])
+@pytest.mark.parametrize("model", [5, 2, 12, 14])
 def test_launch_shapes_agree(gpu, model):
-    """Every launch shape of the mixed kernel (register budgets, grid modes, and the
-    shared-memory-staged bulk-copy kernels) integrates the same cells to the same result, up
-    to FP32 rounding differences between instruction schedules."""
+    """Every launch shape of the mixed kernel (register budgets, grid modes, the
+    shared-memory-staged bulk-copy kernels and their producer/consumer pipelines) integrates the
+    same cells to the same result, up to FP32 rounding differences between instruction
+    schedules."""
     cm = gpu
     n = 3 * 256 + 77  # partial last tile
     p = cm.Params(model, None, 1e-5)
     out = []
-    for variant, grid_mode in [(0, 0), (1, 2), (3, 4), (5, 2), (6, 1), (5, 4)]:
+    for variant, grid_mode in [(0, 0), (1, 2), (3, 4), (5, 2), (6, 1), (5, 4), (7, 2), (8, 1), (7, 4)]:
         b = cm.Batch(p, n, cm.MIXED)
         sc = W.conductance_scales(4, n, 3, 0.9, 1.1)
         for k, name in enumerate(HET[model]):
