@@ -57,9 +57,11 @@ MIXED_BYTES_PER_CELL_STEP = 2 * (15 * 4 + 3 * 8) + 2 * 8 + 3 * 4
 MIXED_KERNELS = ["tt2_mixed_kernel<256>", "tt2_mixed_kernel<128>", "tt2_mixed_kernel<256,3>",
                  "tt2_mixed_kernel<512>", "tt2_mixed_kernel<64>", "mixed_staged_kernel<5,256>",
                  "mixed_staged_kernel<5,128>", "mixed_pipe_kernel<5,256,2>", "mixed_pipe_kernel<5,128,3>"]
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu capture summarised in
-# profiles/mixed_staged_tt2_4M_cells.md (same workload, launch shape 6, grid mode 4).
-MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu captures summarised in
+# profiles/mixed_staged_tt2_4M_cells.md (launch shape 6, grid mode 4) and
+# profiles/mixed_pipe_kernels.md (launch shape 7, grid mode 4), same workload.
+MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808,
+                    "mixed_pipe_kernel<5,256,2>": 436_254_208 + 325_440_768}
 # tt2_fp64_kernel: 18 FP64 states r+w (288 B), Vm r+w (16 B), 3 FP64 conductances (24 B).
 FP64_BYTES_PER_CELL_STEP = 2 * 18 * 8 + 2 * 8 + 3 * 8
 WORKLOAD = "tt2006-epi-precision-form-2048x2048"
