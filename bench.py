@@ -96,6 +96,17 @@ TISSUE_MIXED_BYTES = 168 + 16 + 12 + 56 + 4 + 8 + 8 + 4
 # FP64 form: 18 states r+w (288 B), Vm r + w (16 B), 3 conductances (24 B), 7 x (4 + 8 B) (84 B),
 # stimulus time (8 B), activation time (8 B), neighbours (8 B).
 TISSUE_FP64_BYTES = 288 + 16 + 24 + 84 + 8 + 8 + 8
+# The tissue leg with another cell model (--tissue-model): the same operator, stimulus protocol
+# and per-node bytes with the model's own state planes (mixed: FP32 planes + pairs r+w; FP64:
+# states r+w) in place of TT2's 168 / 288 B. Stimulus twice the model's single-cell amplitude.
+TISSUE_MODELS = {
+    "tt2": dict(model=5, label="tt2006-epi", het="TT2_HETERO", stim="TT2_STIM_NA", stim_text="2 x -52 pA/pF",
+                mixed=TISSUE_MIXED_BYTES, fp64=TISSUE_FP64_BYTES),
+    "ord": dict(model=12, label="ord2011-endo", het="ORD_HETERO", stim="ORD_STIM", stim_text="2 x -50 uA/uF",
+                mixed=TISSUE_MIXED_BYTES - 168 + 2 * 47 * 4, fp64=TISSUE_FP64_BYTES - 288 + 2 * 41 * 8),
+    "tomek": dict(model=14, label="tomek2019-endo", het="TOM_HETERO", stim="TOM_STIM", stim_text="2 x -53 uA/uF",
+                  mixed=TISSUE_MIXED_BYTES - 168 + 2 * 50 * 4, fp64=TISSUE_FP64_BYTES - 288 + 2 * 44 * 8),
+}
 FULL_CELLS = 1 << 24
 FULL_INSTANCES = 64
 FULL_BCL = 0.5
@@ -670,21 +681,27 @@ def tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     and activation times (cm_batch_run_diffuse) on a 4,194,304-node slab; the same step split
     into cm_diffusion_apply + cm_batch_step_update_act beside it; the FP64 form."""
     from cardiomechanics_gb300 import workloads as W
+    tm = TISSUE_MODELS[args.tissue_model]
+    hetn = getattr(W, tm["het"])
     nx, ny, nz = TISSUE_DIMS if args.tissue_dims is None else tuple(args.tissue_dims)
     n = nx * ny * nz
     rp, col, val = W.grid_laplacian(nx, ny, nz)
-    d = cm.Diffusion(rp, col, val, uniform_scale=W.COUPLING_SCALE[5])
+    d = cm.Diffusion(rp, col, val, uniform_scale=W.COUPLING_SCALE[tm["model"]])
     del rp, col, val
-    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    p = cm.Params(tm["model"], None, DT)
     sc = W.conductance_scales(5, n, 3, 0.95, 1.05)
     tb = torch.tensor(np.where(np.arange(n) % nx < 3, 0.0, 1e9), device="cuda")
-    out = {"workload": f"tt2006-epi-slab-{nx}x{ny}x{nz}", "nodes": n, "grid_mm": 0.1, "D_mm2_per_ms": 0.1,
-           "operator": "7-point finite differences, no-flux faces", "stimulus": "x < 3 planes, 2 x -52 pA/pF x 1 ms"}
-    kw = dict(textlen=1e-3, bcl=1e9, amplitude=2 * W.TT2_STIM_NA, act_threshold=-0.02, vm_range=0.2)
+    amp = 2 * getattr(W, tm["stim"])
+    out = {"workload": f"{tm['label']}-slab-{nx}x{ny}x{nz}", "nodes": n, "grid_mm": 0.1, "D_mm2_per_ms": 0.1,
+           "operator": "7-point finite differences, no-flux faces",
+           "stimulus": f"x < 3 planes, {tm['stim_text']} x 1 ms"}
+    kw = dict(textlen=1e-3, bcl=1e9, amplitude=amp, act_threshold=-0.02, vm_range=0.2)
     for prec, steps, name in ((cm.MIXED, args.tissue_steps, "fused_mixed"), (cm.FP64, args.fp64_steps, "fused_fp64")):
         b = cm.Batch(p, n, prec, stream=stream.cuda_stream)
-        for k, h in enumerate(W.TT2_HETERO):
+        for k, h in enumerate(hetn):
             b.add_hetero_value(h, p.get(h) * sc[k])
+        if prec == cm.MIXED and args.launch:  # 5 or 6: the double-buffered staged kernel
+            b.set_launch(*(int(x) for x in args.launch.split(",")))
         vm = torch.tensor(b.init_vm(), device="cuda")
         act = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
         tbc = tb.clone()
@@ -697,7 +714,7 @@ def tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind):
         e1.record(stream)
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
-        bps = TISSUE_MIXED_BYTES if prec == cm.MIXED else TISSUE_FP64_BYTES
+        bps = tm["mixed"] if prec == cm.MIXED else tm["fp64"]
         achieved = bps * n * steps / sec / 1e9
         out[name] = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
                      "activated": int((act >= 0).sum().item()), "audit_mask": b.audit(),
@@ -708,7 +725,7 @@ def tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind):
         torch.cuda.empty_cache()
     # the split form a caller would write without the fused entry point (mixed batch, device arrays)
     b = cm.Batch(p, n, cm.MIXED, stream=stream.cuda_stream)
-    for k, h in enumerate(W.TT2_HETERO):
+    for k, h in enumerate(hetn):
         b.add_hetero_value(h, p.get(h) * sc[k])
     vm = torch.tensor(b.init_vm(), device="cuda")
     act = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
@@ -807,6 +824,8 @@ def main():
     ap.add_argument("--tissue-steps", type=int, default=500, help="timed steps of the coupled (tissue) leg")
     ap.add_argument("--tissue-dims", type=int, nargs=3, default=None, help="slab size (fewer nodes only for captures)")
     ap.add_argument("--no-tissue", action="store_true")
+    ap.add_argument("--tissue-model", default="tt2", choices=list(TISSUE_MODELS),
+                    help="cell model of the tissue leg (the headline run uses tt2)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

@@ -84,6 +84,63 @@ __device__ __forceinline__ float crn_mixed_cell(const DevBatch &b, I c, float V,
   return dV;
 }
 
+// Monodomain coupling current of cell c: scale_c * (A x)_c with A's row c in its 32-row slice
+// (acCELLerate.cpp:1849 MatMult and 1880-1887 conversion). Padding entries of a slice carry
+// value 0 and the row's own column. The first kCouplingBatch entries of the row are fetched in
+// two rounds -- all columns and values, then all neighbour potentials -- so a row costs two
+// memory latencies rather than two per entry; longer rows continue entry by entry.
+constexpr int kCouplingBatch = 8;
+
+// FP64: entries summed in CSR order.
+__device__ __forceinline__ double coupling_fp64(const StepIO &io, const double *x, int64_t c) {
+  const int64_t s = c >> 5;
+  const int64_t e0 = io.sl_ptr[s] + (c & 31), e1 = io.sl_ptr[s + 1];
+  int32_t cj[kCouplingBatch];
+  double aj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) {
+    const int64_t e = e0 + 32 * k;
+    cj[k] = e < e1 ? io.sl_col[e] : (int32_t)c;
+    aj[k] = e < e1 ? io.sl_val64[e] : 0.0;
+  }
+  double xj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) xj[k] = __ldg(x + cj[k]);
+  double acc = 0.0;
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++)
+    if (e0 + 32 * k < e1) acc += aj[k] * xj[k];
+  for (int64_t e = e0 + 32 * kCouplingBatch; e < e1; e += 32) acc += io.sl_val64[e] * __ldg(x + io.sl_col[e]);
+  return acc * (io.dscale64 ? __ldg(io.dscale64 + c) : io.dscale_u);
+}
+
+// Mixed form: rowsum_c x_c + sum_j A_cj (x_j - x_c) on the previous step's hi plane; the
+// differences of neighbouring potentials are small, so FP32 keeps them (the plain sum would
+// cancel a diagonal ~6 orders above the result at rest).
+template <typename I>
+__device__ __forceinline__ float coupling_f32(const StepIO &io, I c) {
+  const float *x = io.vm_hi;
+  const int64_t s = (int64_t)c >> 5;
+  const int64_t e0 = io.sl_ptr[s] + (c & 31), e1 = io.sl_ptr[s + 1];
+  int32_t cj[kCouplingBatch];
+  float aj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) {
+    const int64_t e = e0 + 32 * k;
+    cj[k] = e < e1 ? io.sl_col[e] : (int32_t)c;
+    aj[k] = e < e1 ? io.sl_val32[e] : 0.f;
+  }
+  const float xc = x[c];
+  float xj[kCouplingBatch];
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) xj[k] = x[cj[k]];
+  float acc = __ldg(io.rowsum32 + c) * xc;
+#pragma unroll
+  for (int k = 0; k < kCouplingBatch; k++) acc += aj[k] * (xj[k] - xc);
+  for (int64_t e = e0 + 32 * kCouplingBatch; e < e1; e += 32) acc += io.sl_val32[e] * (x[io.sl_col[e]] - xc);
+  return acc * (io.dscale32 ? __ldg(io.dscale32 + c) : (float)io.dscale_u);
+}
+
 // O'Hara-Rudy state stores over a batch's device memory (see ord_calc): every state read
 // and written in place as ord_calc reaches it.
 struct ORDStore64 {

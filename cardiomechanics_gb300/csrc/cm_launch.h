@@ -77,11 +77,12 @@ struct StepIO {
   float *vm_hi_out = nullptr, *vm_lo_out = nullptr;  // mixed: new Vm planes (nullptr: in place)
 };
 
-// Coupled runs of TT2 / Courtemanche mixed batches through the staged kernel (cm_staged.cu):
-// the tile's operator slices are staged with its state. false when the batch or the operator
+// Coupled runs of mixed batches through the staged kernels (cm_staged.cu): the tile's operator
+// slices are staged with its state; the producer/consumer pipeline unless a TT2 / Courtemanche
+// batch chose the double-buffered kernel (variant 5 or 6). false when the batch or the operator
 // does not fit (then the register kernel runs).
 bool coupled_staged_supported(const DevBatch &b, const StepIO &io);
-cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, cudaStream_t s);
+cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, int variant, cudaStream_t s);
 
 // y = scale * (A x) for a coupling operator (cm_diffusion_apply); io carries the operator.
 cudaError_t launch_diffusion_apply(const StepIO &io, const double *x, double *y, int64_t n, cudaStream_t s);

@@ -213,6 +213,66 @@ cudaError_t launch_pipe_m(const DevBatch &b, const StepIO &io, int blocks_per_sm
 // pair goes to the other pair of planes.
 constexpr int kCoupledWmax = 16;  // widest operator slice staged (entries per row)
 
+// The update of one cell of a staged coupled tile: the stimulus by the driver's rule
+// (CellModel.h:405-419) with per-cell times, the cell update with i_external = stimulus +
+// coupling current `cpl`, the range check and the activation time. tb, a0: the cell's stimulus
+// time and activation entry, read before the stage wait.
+template <int kModel, int kThreads>
+__device__ __forceinline__ void coupled_update(const DevBatch &b, const StepIO &io, const float *S,
+                                               const int (&het_pos)[6], int c, double tb, double a0, float cpl) {
+  float stim = (float)io.iext_uniform;
+  if (io.tb_cell) {
+    stim = 0.f;
+    if (io.t >= tb) {
+      stim = (float)io.amp;
+      if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
+    }
+  }
+  const Acc v = staged_cell<kModel, kThreads>(b, S, het_pos, c, stim + cpl, io.vm_hi_out, io.vm_lo_out);
+  uint32_t audit = 0;
+  if (io.vm_range > 0.0 && fabsf(v.hi) > (float)io.vm_range) audit |= 32u;
+  if (io.act && a0 == -1.0 && v.hi >= (float)io.act_threshold) io.act[c] = io.act_time;
+  if (audit) {
+    atomicOr(b.audit_cell + c, audit);
+    atomicOr(b.audit_or, audit);
+  }
+}
+
+// One cell of a staged coupled tile whose operator entries are staged too (base + NVMAX *
+// kThreads: columns, then values; off: the tile's slice entry offsets): the coupling current
+// rowsum x_c + sum_j A_cj (x_j - x_c) from the stage and the neighbours' previous hi words, then
+// coupled_update.
+template <int kModel, int kThreads>
+__device__ __forceinline__ void coupled_cell(const DevBatch &b, const StepIO &io, const float *base, const int *off,
+                                             const int (&het_pos)[6], int rs_pos, int sc_pos, int c, double tb,
+                                             double a0) {
+  constexpr int NS = StagedVars<kModel>::kState;
+  constexpr int NVMAX = NS + 2 + 6 + 2;
+  const int W = io.sl_wmax;
+  const int tid = threadIdx.x;
+  const float *S = base + tid;
+  const int32_t *ecol = (const int32_t *)(base + (size_t)NVMAX * kThreads);
+  const float *eval = base + (size_t)NVMAX * kThreads + (size_t)W * kThreads;
+  const int sl = tid >> 5, lane = tid & 31;
+  const int o0 = off[sl] + lane, o1 = off[sl + 1];
+  const float xc = S[NS * kThreads];
+  int32_t cj[kCoupledWmax];
+  float aj[kCoupledWmax], xj[kCoupledWmax];
+#pragma unroll
+  for (int k = 0; k < kCoupledWmax; k++) {
+    const int e = o0 + 32 * k;
+    cj[k] = e < o1 ? ecol[e] : c;
+    aj[k] = e < o1 ? eval[e] : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < kCoupledWmax; k++) xj[k] = io.vm_hi[cj[k]];
+  float acc = S[rs_pos * kThreads] * xc;
+#pragma unroll
+  for (int k = 0; k < kCoupledWmax; k++) acc += aj[k] * (xj[k] - xc);
+  const float scale = sc_pos >= 0 ? S[sc_pos * kThreads] : (float)io.dscale_u;
+  coupled_update<kModel, kThreads>(b, io, S, het_pos, c, tb, a0, acc * scale);
+}
+
 template <int kModel, int kThreads>
 __global__ void __launch_bounds__(kThreads, 2) coupled_staged_kernel(const DevBatch b, const StepIO io) {
   constexpr int NS = StagedVars<kModel>::kState;
@@ -289,47 +349,145 @@ __global__ void __launch_bounds__(kThreads, 2) coupled_staged_kernel(const DevBa
       if (next < n_tiles) mbar_wait(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
       return;
     }
-    const float *base = stage + (size_t)buf * buf_floats;
-    const float *S = base + threadIdx.x;
     if (c >= n) continue;
-    // coupling current: rowsum x_c + sum_j A_cj (x_j - x_c), entries from the stage
-    const int32_t *ecol = (const int32_t *)(base + (size_t)NVMAX * kThreads);
-    const float *eval = base + (size_t)NVMAX * kThreads + (size_t)W * kThreads;
-    const int sl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int o0 = s_off[buf][sl] + lane, o1 = s_off[buf][sl + 1];
-    const float xc = S[NS * kThreads];
-    int32_t cj[kCoupledWmax];
-    float aj[kCoupledWmax], xj[kCoupledWmax];
+    coupled_cell<kModel, kThreads>(b, io, stage + (size_t)buf * buf_floats, s_off[buf], het_pos, rs_pos, sc_pos, c,
+                                   tb, a0);
+  }
+}
+
+// Coupled runs through the producer/consumer pipeline of mixed_pipe_kernel. kStagedOps: the
+// tile's operator entries, row sums and scales are staged too (the producer reads the tile's
+// slice offsets and writes them to the stage's offset row before the stage's `full` arrival,
+// which releases them to the consumers). Otherwise a consumer forms its cell's coupling current
+// from global memory (coupling_f32) before it waits for the stage, so the entry and neighbour
+// reads overlap the stage's copies, and the stage holds the state, Vm and conductances only.
+template <int kModel, int kThreads, int kStages, bool kStagedOps>
+__global__ void __launch_bounds__(kThreads + 32, kThreads == 256 ? 2 : 3) coupled_pipe_kernel(const DevBatch b,
+                                                                                           const StepIO io) {
+  constexpr int NS = StagedVars<kModel>::kState;
+  constexpr int NVMAX = NS + 2 + 6 + 2;
+  constexpr int kSlices = kThreads / 32;
+  constexpr int kWarps = kThreads / 32;
+  extern __shared__ __align__(128) float stage[];  // [kStages][buf_floats]
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+  __shared__ int s_off[kStages][kSlices + 1];
+  const int64_t ld = b.ld;
+  const int n = (int)b.n;
+  const int n_tiles = (n + kThreads - 1) / kThreads;
+  const int64_t n_slices = ((int64_t)n + 31) / 32;
+  const int W = io.sl_wmax;
+  int het_pos[6];
+  int nv = NS + 2;
 #pragma unroll
-    for (int k = 0; k < kCoupledWmax; k++) {
-      const int e = o0 + 32 * k;
-      cj[k] = e < o1 ? ecol[e] : c;
-      aj[k] = e < o1 ? eval[e] : 0.f;
+  for (int k = 0; k < 6; k++) het_pos[k] = b.het[k] ? nv++ : -1;
+  const int rs_pos = kStagedOps ? nv++ : -1;
+  const int sc_pos = (kStagedOps && io.dscale32) ? nv++ : -1;
+  const uint32_t plane_bytes = (uint32_t)nv * kThreads * 4u;
+  const size_t buf_floats =
+      kStagedOps ? (size_t)NVMAX * kThreads + 2 * (size_t)W * kThreads : (size_t)nv * kThreads;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < kStages; k++) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], kWarps);
     }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x >= kThreads) {  // the producer warp: lane 0 issues, the other lanes leave
+    if (threadIdx.x != kThreads) return;
+    int it = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
+      const int st = it % kStages;
+      const int64_t c0 = (int64_t)t * kThreads;
+      int64_t so[kSlices + 1];  // read before the wait: the offsets do not depend on the stage
+      if (kStagedOps) {
+        const int64_t s0 = c0 / 32, s1 = s0 + kSlices < n_slices ? s0 + kSlices : n_slices;
 #pragma unroll
-    for (int k = 0; k < kCoupledWmax; k++) xj[k] = io.vm_hi[cj[k]];
-    float acc = S[rs_pos * kThreads] * xc;
-#pragma unroll
-    for (int k = 0; k < kCoupledWmax; k++) acc += aj[k] * (xj[k] - xc);
-    const float scale = sc_pos >= 0 ? S[sc_pos * kThreads] : (float)io.dscale_u;
-    float stim = (float)io.iext_uniform;  // the driver's rule (CellModel.h:405-419), per-cell times
-    if (io.tb_cell) {
-      stim = 0.f;
-      if (io.t >= tb) {
-        stim = (float)io.amp;
-        if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
+        for (int k = 0; k <= kSlices; k++) so[k] = io.sl_ptr[s0 + k < s1 ? s0 + k : s1];
+      }
+      if (it >= kStages && !mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1))) {
+        atomicOr(b.audit_or, kAuditTimeout);
+        for (int j = it - kStages; j < it; j++)
+          if (j >= 0) mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1));
+        return;
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      float *dst = stage + st * buf_floats;
+      uint32_t ent_bytes = 0;
+      if (kStagedOps) {
+        for (int k = 0; k <= kSlices; k++) s_off[st][k] = (int)(so[k] - so[0]);
+        ent_bytes = (uint32_t)(so[kSlices] - so[0]) * 4u;
+      }
+      mbar_expect_tx(&full[st], plane_bytes + 2u * ent_bytes);
+      for (int v = 0; v < NS; v++) bulk_g2s(dst + v * kThreads, b.s32 + v * ld + c0, kThreads * 4u, &full[st]);
+      bulk_g2s(dst + NS * kThreads, io.vm_hi + c0, kThreads * 4u, &full[st]);
+      bulk_g2s(dst + (NS + 1) * kThreads, io.vm_lo + c0, kThreads * 4u, &full[st]);
+      for (int k = 0; k < 6; k++)
+        if (het_pos[k] >= 0)
+          bulk_g2s(dst + het_pos[k] * kThreads, (const float *)b.het[k] + c0, kThreads * 4u, &full[st]);
+      if (kStagedOps) {
+        bulk_g2s(dst + rs_pos * kThreads, io.rowsum32 + c0, kThreads * 4u, &full[st]);
+        if (sc_pos >= 0) bulk_g2s(dst + sc_pos * kThreads, io.dscale32 + c0, kThreads * 4u, &full[st]);
+        if (ent_bytes) {
+          float *ent = dst + (size_t)NVMAX * kThreads;
+          bulk_g2s(ent, io.sl_col + so[0], ent_bytes, &full[st]);
+          bulk_g2s(ent + (size_t)W * kThreads, io.sl_val32 + so[0], ent_bytes, &full[st]);
+        }
       }
     }
-    const float iext = stim + acc * scale;
-    const Acc v = staged_cell<kModel, kThreads>(b, S, het_pos, c, iext, io.vm_hi_out, io.vm_lo_out);
-    uint32_t audit = 0;
-    if (io.vm_range > 0.0 && fabsf(v.hi) > (float)io.vm_range) audit |= 32u;
-    if (io.act && a0 == -1.0 && v.hi >= (float)io.act_threshold) io.act[c] = io.act_time;
-    if (audit) {
-      atomicOr(b.audit_cell + c, audit);
-      atomicOr(b.audit_or, audit);
-    }
+    return;
   }
+  const int lane = threadIdx.x & 31;
+  int it = 0;
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
+    const int st = it % kStages;
+    const int c = t * kThreads + threadIdx.x;
+    const double tb = (io.tb_cell && c < n) ? io.tb_cell[c] : 0.0;
+    const double a0 = (io.act && c < n) ? io.act[c] : 0.0;
+    float cpl = 0.f;
+    if (!kStagedOps && c < n) cpl = coupling_f32<int>(io, c);
+    if (!mbar_wait(&full[st], (uint32_t)((it / kStages) & 1))) {
+      atomicOr(b.audit_or, kAuditTimeout);
+      return;
+    }
+    if (c < n) {
+      if (kStagedOps)
+        coupled_cell<kModel, kThreads>(b, io, stage + st * buf_floats, s_off[st], het_pos, rs_pos, sc_pos, c, tb,
+                                       a0);
+      else
+        coupled_update<kModel, kThreads>(b, io, stage + st * buf_floats + threadIdx.x, het_pos, c, tb, a0, cpl);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+  }
+}
+
+template <int kModel, int kThreads, int kStages, bool kStagedOps>
+cudaError_t launch_coupled_pipe_t(const DevBatch &b, const StepIO &io, cudaStream_t s) {
+  constexpr int NS = StagedVars<kModel>::kState;
+  constexpr int NVMAX = NS + 2 + 6 + 2;
+  int nv = NS + 2;
+  for (int k = 0; k < 6; k++) nv += b.het[k] ? 1 : 0;
+  const size_t smem = kStagedOps ? (size_t)kStages * ((size_t)NVMAX * kThreads + 2 * (size_t)io.sl_wmax * kThreads) *
+                                       sizeof(float)
+                                 : (size_t)kStages * nv * kThreads * sizeof(float);
+  const size_t smem_max =
+      kStagedOps ? (size_t)kStages * ((size_t)NVMAX * kThreads + 2 * (size_t)kCoupledWmax * kThreads) * sizeof(float)
+                 : (size_t)kStages * (NS + 2 + 6) * kThreads * sizeof(float);
+  auto kern = coupled_pipe_kernel<kModel, kThreads, kStages, kStagedOps>;
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)kern, (int)smem_max, done);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads + 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const int n_tiles = (int)((b.n + kThreads - 1) / kThreads);
+  int grid = sm_count() * per_sm;
+  if (grid > n_tiles) grid = n_tiles;
+  if (grid < 1) grid = 1;
+  kern<<<grid, kThreads + 32, smem, s>>>(b, io);
+  return cudaGetLastError();
 }
 
 template <int kModel>
@@ -352,14 +510,34 @@ cudaError_t launch_coupled_t(const DevBatch &b, const StepIO &io, cudaStream_t s
 }  // namespace
 
 bool coupled_staged_supported(const DevBatch &b, const StepIO &io) {
-  return (b.model == 5 || b.model == 2) && b.precision == 1 && io.sl_ptr && io.sl_val32 && io.rowsum32 &&
+  return (b.model == 5 || b.model == 2 || b.model == 12 || b.model == 14) && b.precision == 1 && io.sl_ptr && io.sl_val32 && io.rowsum32 &&
          io.sl_wmax >= 1 && io.sl_wmax <= kCoupledWmax && io.vm_hi && io.vm_hi_out && io.vm_lo == io.vm_hi + b.ld &&
          io.vm_lo_out == io.vm_hi_out + b.ld && !io.iext && b.ld % 256 == 0 && b.n < (int64_t)1 << 30;
 }
 
-cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, cudaStream_t s) {
+cudaError_t launch_coupled_staged(const DevBatch &b, const StepIO &io, int variant, cudaStream_t s) {
   if (b.n == 0) return cudaSuccess;
-  return b.model == 5 ? launch_coupled_t<5>(b, io, s) : launch_coupled_t<2>(b, io, s);
+  // variant (cm_batch_set_launch) past the register shapes: 0, 1 the double-buffered kernel
+  // (TT2 / Courtemanche); 2 the pipeline with the operator staged; 3 the pipeline with the
+  // coupling current from global memory. Otherwise the faster of the two pipelines on a
+  // 4,194,304-node slab: operator staged for TT2 / Courtemanche (92 % of measured HBM against
+  // 74 %), coupling from global memory with 256-cell tiles for O'Hara-Rudy and Tomek (their
+  // stages with the operator fit two blocks per SM only with 128-cell tiles: 79 % against 78 %,
+  // 77 % against 73 %).
+  const int k = variant - n_register_shapes();
+  const bool staged_ops = k == 2 || (k != 3 && (b.model == 5 || b.model == 2));
+  switch (b.model) {
+    case 12:
+      return staged_ops ? launch_coupled_pipe_t<12, 128, 2, true>(b, io, s) : launch_coupled_pipe_t<12, 256, 2, false>(b, io, s);
+    case 14:
+      return staged_ops ? launch_coupled_pipe_t<14, 128, 2, true>(b, io, s) : launch_coupled_pipe_t<14, 256, 2, false>(b, io, s);
+    case 5:
+      if (k == 0 || k == 1) return launch_coupled_t<5>(b, io, s);
+      return staged_ops ? launch_coupled_pipe_t<5, 256, 2, true>(b, io, s) : launch_coupled_pipe_t<5, 256, 2, false>(b, io, s);
+    default:
+      if (k == 0 || k == 1) return launch_coupled_t<2>(b, io, s);
+      return staged_ops ? launch_coupled_pipe_t<2, 256, 2, true>(b, io, s) : launch_coupled_pipe_t<2, 256, 2, false>(b, io, s);
+  }
 }
 
 bool staged_supported(const DevBatch &b, const StepIO &io) {
