@@ -7,6 +7,7 @@
 namespace cm {
 
 static constexpr uint32_t kAuditTimeout = 64u;
+static constexpr uint32_t kAuditInternal = 128u;  // a kernel's own consistency check failed; work skipped
 static constexpr uint32_t kSpinLimit = 1u << 26;
 
 static __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }

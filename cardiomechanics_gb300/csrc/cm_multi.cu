@@ -183,11 +183,176 @@ __global__ void __launch_bounds__(kT, 2)
   }
 }
 
+// The staged step as a producer/consumer pipeline (as mixed_pipe_kernel): one extra warp
+// schedules the block's sub-tiles (the next one of its tile, or a new tile from the counter),
+// copies the instance's descriptor into the stage's descriptor slot when the instance changes,
+// advances the instance's stimulus clock, and issues the sub-tile's bulk copies; the kT / 32
+// consumer warps integrate. Stages pass through `full` and `empty` mbarriers; the end of the
+// work is a stage whose tile index is -1. Every wait is bounded: a consumer whose `full` wait
+// runs out sets CM_AUDIT_TIMEOUT in the first instance's audit word and leaves; the producer then
+// runs out on `empty`, does the same, waits (bounded) for the copies nobody took and leaves.
+// Two consistency checks skip work instead of touching memory outside an instance: the producer
+// issues no copy for a sub-tile outside its instance (audit bit 256), a consumer warp integrates
+// no cell when its stage's descriptor is not its tile's instance's (audit bit 128).
+template <int kT, int kStages>
+__global__ void __launch_bounds__(kT + 32, 2)
+    multi_pipe_kernel(const MultiInst *__restrict__ insts, const MultiTile *__restrict__ tiles, int n_tiles,
+                      const MultiClock *__restrict__ clk_cur, MultiClock *__restrict__ clk_next,
+                      unsigned int *__restrict__ counter, unsigned int *__restrict__ counter_next) {
+  constexpr int NVMAX = StagedVars<2>::kState + 2 + 6;  // the larger model
+  constexpr int kWarps = kT / 32;
+  extern __shared__ __align__(128) float stage[];      // [kStages][NVMAX][kT]
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+  __shared__ __align__(16) DevBatch sd[kStages];
+  __shared__ int s_tile[kStages], s_sub[kStages], s_inst[kStages];
+  __shared__ float s_iext[kStages];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *counter_next = 0;  // the next step's counter
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < kStages; k++) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], kWarps);
+      s_inst[k] = -1;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x >= kT) {  // the producer warp
+    const int lane = threadIdx.x - kT;
+    int tile = -1, sub = 0, count = 0;
+    for (int it = 0;; it++) {
+      const int st = it % kStages;
+      int nt = tile, nsub = sub + 1;
+      if (lane == 0 && (tile < 0 || (int64_t)nsub * kT >= count)) {
+        const int a = (int)atomicAdd(counter, 1u);
+        nt = a < n_tiles ? a : -1;
+        nsub = 0;
+      }
+      nt = __shfl_sync(0xffffffffu, nt, 0);
+      nsub = __shfl_sync(0xffffffffu, nsub, 0);
+      int ok = 1;
+      if (lane == 0 && it >= kStages) ok = mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1)) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) {
+          atomicOr(insts[0].d.audit_or, kAuditTimeout);
+          for (int j = it - kStages; j < it; j++)
+            if (j >= 0) mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1));
+        }
+        return;
+      }
+      if (nt < 0) {  // no work left: an empty stage tells the consumers
+        if (lane == 0) {
+          s_tile[st] = -1;
+          mbar_arrive(&full[st]);
+        }
+        return;
+      }
+      const MultiTile T = tiles[nt];
+      const MultiInst *I = insts + T.inst;
+      // lane 0 decides whether the stage's descriptor slot needs this instance's descriptor and
+      // tells the warp: a lane that read s_inst itself could see lane 0's update of it below
+      // and skip its share of the copy
+      int need = lane == 0 ? (s_inst[st] != T.inst) : 0;
+      need = __shfl_sync(0xffffffffu, need, 0);
+      if (need) {  // the instance's descriptor into this stage's slot
+        const int4 *src = reinterpret_cast<const int4 *>(&I->d);
+        int4 *dst = reinterpret_cast<int4 *>(&sd[st]);
+        for (int k = lane; k < (int)(sizeof(DevBatch) / sizeof(int4)); k += 32) dst[k] = src[k];
+      }
+      if (lane == 0) {
+        s_inst[st] = T.inst;
+        s_tile[st] = nt;
+        s_sub[st] = nsub;
+        const MultiClock ck = clk_cur[T.inst];
+        s_iext[st] = ck.t >= ck.tb ? (float)I->amp : 0.f;
+        if (T.start == 0 && nsub == 0) {  // reference driver clock (CellModel.h:405-419)
+          MultiClock nx;
+          nx.t = ck.t + I->dt;
+          nx.tb = (ck.t >= ck.tb && ck.t >= ck.tb + I->textlen) ? ck.tb + I->bcl : ck.tb;
+          clk_next[T.inst] = nx;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        const int64_t ld = I->d.ld;
+        const int model = I->d.model;
+        const int ns = model == 5 ? StagedVars<5>::kState : StagedVars<2>::kState;
+        int nh = 0;
+        for (int k = 0; k < 6; k++) nh += I->d.het[k] ? 1 : 0;
+        const int64_t c0 = (int64_t)T.start + (int64_t)nsub * kT;
+        float *dst = stage + (size_t)st * NVMAX * kT;
+        if (c0 < 0 || c0 + kT > ld || (model != 5 && model != 2)) {  // a sub-tile outside its instance
+          atomicOr(I->d.audit_or, kAuditInternal << 1);
+          s_tile[st] = -2;  // the consumers skip it
+          mbar_arrive(&full[st]);
+          tile = nt;
+          sub = nsub;
+          count = T.count;
+          continue;
+        }
+        mbar_expect_tx(&full[st], (uint32_t)(ns + 2 + nh) * kT * 4u);
+        for (int v = 0; v < ns; v++) bulk_g2s(dst + v * kT, I->d.s32 + v * ld + c0, kT * 4u, &full[st]);
+        bulk_g2s(dst + ns * kT, I->vm_hi + c0, kT * 4u, &full[st]);
+        bulk_g2s(dst + (ns + 1) * kT, I->vm_lo + c0, kT * 4u, &full[st]);
+        int pos = ns + 2;
+        for (int k = 0; k < 6; k++)
+          if (I->d.het[k]) bulk_g2s(dst + (pos++) * kT, (const float *)I->d.het[k] + c0, kT * 4u, &full[st]);
+      }
+      tile = nt;
+      sub = nsub;
+      count = T.count;
+    }
+  }
+  const int lane = threadIdx.x & 31;
+  for (int it = 0;; it++) {
+    const int st = it % kStages;
+    if (!mbar_wait(&full[st], (uint32_t)((it / kStages) & 1))) {
+      atomicOr(insts[0].d.audit_or, kAuditTimeout);
+      return;
+    }
+    const int tile = s_tile[st];
+    if (tile == -1) break;
+    if (tile < 0) {  // skipped by the producer's check
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
+      continue;
+    }
+    const DevBatch &b = sd[st];
+    const MultiTile T = tiles[tile];
+    const MultiInst *I = insts + T.inst;
+    // the stage's descriptor must be its tile's instance's (decided for the whole warp)
+    const bool bad = b.s32 != I->d.s32 || b.ld != I->d.ld || b.model != I->d.model ||
+                     b.audit_cell != I->d.audit_cell || b.rows32 != I->d.rows32 || b.eca32 != I->d.eca32 || b.audit_or != I->d.audit_or;
+    if (__any_sync(0xffffffffu, bad)) {
+      if (lane == 0) {
+        atomicOr(I->d.audit_or, kAuditInternal);
+        mbar_arrive(&empty[st]);
+      }
+      continue;
+    }
+    int het_pos[6];
+    int pos = b.model == 5 ? StagedVars<5>::kState + 2 : StagedVars<2>::kState + 2;
+#pragma unroll
+    for (int k = 0; k < 6; k++) het_pos[k] = b.het[k] ? pos++ : -1;
+    const float *S = stage + (size_t)st * NVMAX * kT + threadIdx.x;
+    const int c = T.start + s_sub[st] * kT + (int)threadIdx.x;
+    if (c < T.start + T.count) {
+      if (b.model == 5) staged_cell<5, kT>(b, S, het_pos, c, s_iext[st], I->vm_hi, I->vm_lo);
+      else staged_cell<2, kT>(b, S, het_pos, c, s_iext[st], I->vm_hi, I->vm_lo);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+  }
+}
+
 struct MShape {
   int block, minb;
-  bool staged;
+  bool staged, pipe;
 };
-constexpr MShape kMShapes[] = {{256, 2, false}, {128, 5, false}, {512, 1, false}, {128, 2, true}, {256, 2, true}};
+constexpr MShape kMShapes[] = {{256, 2, false, false}, {128, 5, false, false}, {512, 1, false, false},
+                               {128, 2, true, false},  {256, 2, true, false},  {256, 2, true, true},
+                               {128, 2, true, true}};
 
 template <int kT>
 cudaError_t launch_multi_staged(const MultiLaunch &L, const MultiClock *cur, MultiClock *nxt, unsigned int *cnt,
@@ -197,6 +362,17 @@ cudaError_t launch_multi_staged(const MultiLaunch &L, const MultiClock *cur, Mul
   cudaError_t e = smem_limit((const void *)multi_staged_kernel<kT>, (int)smem, done);
   if (e != cudaSuccess) return e;
   multi_staged_kernel<kT><<<L.grid, kT, smem, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next);
+  return cudaGetLastError();
+}
+
+template <int kT, int kStages>
+cudaError_t launch_multi_pipe(const MultiLaunch &L, const MultiClock *cur, MultiClock *nxt, unsigned int *cnt,
+                              unsigned int *cnt_next, cudaStream_t s) {
+  constexpr size_t smem = (size_t)kStages * (StagedVars<2>::kState + 2 + 6) * kT * sizeof(float);
+  static std::atomic<uint64_t> done{0};
+  cudaError_t e = smem_limit((const void *)multi_pipe_kernel<kT, kStages>, (int)smem, done);
+  if (e != cudaSuccess) return e;
+  multi_pipe_kernel<kT, kStages><<<L.grid, kT + 32, smem, s>>>(L.insts, L.tiles, L.n_tiles, cur, nxt, cnt, cnt_next);
   return cudaGetLastError();
 }
 
@@ -214,6 +390,9 @@ cudaError_t launch_multi(const MultiLaunch &L, int parity, cudaStream_t s) {
   int shape = L.shape;
   if (shape >= 0 && shape < n_multi_shapes() && kMShapes[shape].staged) {
     if (L.tile_cells % kMShapes[shape].block == 0) {
+      if (kMShapes[shape].pipe)
+        return kMShapes[shape].block == 128 ? launch_multi_pipe<128, 3>(L, cur, nxt, cnt, cnt_next, s)
+                                            : launch_multi_pipe<256, 2>(L, cur, nxt, cnt, cnt_next, s);
       return kMShapes[shape].block == 128 ? launch_multi_staged<128>(L, cur, nxt, cnt, cnt_next, s)
                                           : launch_multi_staged<256>(L, cur, nxt, cnt, cnt_next, s);
     }

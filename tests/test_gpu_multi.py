@@ -54,9 +54,11 @@ def test_multi_equals_single(gpu):
         b.run(v, 1000, **s)
         b.run(v, steps - 1000, **continued(s, 1000))
         ref_v.append(v)
-    # shapes 0-2: plain loads; 3-4: bulk-copy staged sub-tiles of 128 / 256 cells (the 1000-cell
-    # tiles of the last case are not whole sub-tiles: the launcher takes the plain kernel)
-    cases = [(0, 2048, 2), (1, 1024, 4), (2, 4096, 1), (3, 1024, 4), (4, 2048, 2), (3, 4096, 8), (4, 1000, 2)]
+    # shapes 0-2: plain loads; 3-4: bulk-copy staged sub-tiles of 128 / 256 cells; 5-6: the same
+    # as producer/consumer pipelines of 256 / 128 cells (the 1000-cell tiles of the last case are
+    # not whole sub-tiles: the launcher takes the plain kernel)
+    cases = [(0, 2048, 2), (1, 1024, 4), (2, 4096, 1), (3, 1024, 4), (4, 2048, 2), (3, 4096, 8), (5, 2048, 2),
+             (6, 1024, 3), (5, 4096, 4), (4, 1000, 2)]
     for shape, tile, bps in cases:
         mb = build(cm, sizes, models)
         multi = cm.Multi(mb)
@@ -93,3 +95,26 @@ def test_multi_rejects_fp64(gpu):
     with pytest.raises(cm.CMError) as e:
         cm.Multi([b])
     assert e.value.code == -7
+
+
+def test_pipeline_shapes_with_many_instances_per_block(gpu):
+    """The pipelined shapes (5, 6) on 160 small instances, so that every block moves between
+    instances many times and reuses its stage descriptor slots: the same cells as the
+    double-buffered shape 4, and no consistency-check bit (128, 256) in any audit word."""
+    cm = gpu
+    rng = np.random.default_rng(11)
+    sizes = [int(x) for x in rng.integers(300, 3000, 160)]
+    models = [cm.TENTUSSCHER2 if i % 3 else cm.COURTEMANCHE for i in range(160)]
+    st = stims(cm, models)
+    out = []
+    for shape, tile, bps in [(4, 1024, 1), (5, 1024, 1), (6, 1024, 1), (5, 1024, 4)]:
+        mb = build(cm, sizes, models)
+        multi = cm.Multi(mb)
+        multi.set_launch(tile, shape, bps)
+        vms = [b.init_vm() for b in mb]
+        multi.run(vms, 300, st)
+        assert all(b.audit() == 0 for b in mb), shape
+        out.append(vms)
+    for vms in out[1:]:
+        for a, b in zip(vms, out[0]):
+            assert np.abs(a - b).max() <= 1e-6
