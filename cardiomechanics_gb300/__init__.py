@@ -56,6 +56,7 @@ ABI_SYMBOLS = (
     "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
     "cm_batch_run_surrogate", "cm_mlp_forward_static", "cm_surrogate_flush_audit",
     "cm_diffusion_create", "cm_diffusion_destroy", "cm_diffusion_apply", "cm_batch_run_diffuse",
+    "cm_backup_write", "cm_backup_read",
 )
 
 
@@ -136,6 +137,10 @@ def lib() -> ctypes.CDLL:
     L.cm_multi_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.cm_multi_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.cm_backup_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp),
+                                  ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.cm_backup_read.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                 ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t]
     fp = ctypes.POINTER(ctypes.c_float)
     L.cm_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, vp]
     L.cm_mlp_destroy.argtypes = [vp]
@@ -470,6 +475,39 @@ class Multi:
 
     def set_launch(self, tile_cells, shape=0, blocks_per_sm=2):
         _check(lib().cm_multi_set_launch(self._h, tile_cells, shape, blocks_per_sm))
+
+
+def _backup_args(batches, vms, node_ids):
+    batches = list(batches)
+    parts = (ctypes.c_void_p * len(batches))(*[b._h.value for b in batches])
+    vs = [_f64(v, b.n, "Vm") for v, b in zip(vms, batches)]
+    vptr = (ctypes.c_void_p * len(vs))(*[_ptr(v) for v in vs])
+    ids = None
+    if node_ids is not None:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.int64) for a in node_ids]
+        for a, b in zip(arrs, batches):
+            if a is not None and a.size != b.n:
+                raise ValueError("node_ids: one index per cell of its part")
+        ids = (ctypes.c_void_p * len(arrs))(*[None if a is None else a.ctypes.data for a in arrs])
+        ids._keep = arrs
+    return batches, parts, vptr, ids
+
+
+def backup_write(path, time_str, batches, vms, node_ids=None):
+    """acCELLerate backup file (acCELLerate.cpp:1616-1661) of the parts' nodes: header lines, then
+    per node its Vm and its cell model's reference block. node_ids: per part the global index of
+    each of its cells, or None for consecutive parts."""
+    batches, parts, vptr, ids = _backup_args(batches, vms, node_ids)
+    _check(lib().cm_backup_write(str(path).encode(), str(time_str).encode(), len(batches), parts, ids, vptr))
+
+
+def backup_read(path, batches, vms, node_ids=None) -> str:
+    """Reads an acCELLerate backup file (acCELLerate.cpp:1511-1614) into the parts' states and Vm
+    arrays; returns its time string."""
+    batches, parts, vptr, ids = _backup_args(batches, vms, node_ids)
+    buf = ctypes.create_string_buffer(64)
+    _check(lib().cm_backup_read(str(path).encode(), len(batches), parts, ids, vptr, buf, 64))
+    return buf.value.decode()
 
 
 def _f32(a, n, name):

@@ -245,6 +245,27 @@ int cm_diffusion_apply(cm_diffusion_t d, const double *x, double *y);
 int cm_batch_run_diffuse(cm_batch_t b, cm_diffusion_t d, double *Vm, int64_t n_steps, const cm_stimulus *stim,
                          double vm_range, double *act, double act_threshold);
 
+/* ------------------------------------------------------------------ backup files */
+/* acCELLerate backup files (acCELLerate::WriteBackup / ReadBackup, acCELLerate.cpp:1511-1661):
+ * the line "acCELLerateBackupVersion1.0", the line "<time> <number of nodes>", then for every
+ * node in order its Vm (one double) and its cell model's block (GetBase()/GetSize(): the
+ * CM_LAYOUT_REF_BLOCK doubles), in the machine's byte order as the reference writes them on
+ * Linux x86-64 and aarch64 (kaWrite swaps bytes only where KA_LITTLE_ENDIAN is defined,
+ * Lattice/kaMachineOS.h:91-92, i.e. 32-bit x86). One file covers all parts (the materials'
+ * batches): part p holds the nodes node_ids[p][0 .. n_cells-1] (global indices), or, when
+ * node_ids or node_ids[p] is NULL, the next n_cells nodes after the previous part's. Every node
+ * 0 .. n_total-1 must belong to exactly one part. Vm[p]: that part's n_cells values (host or
+ * device). A block's stored currents are what cm_batch_get_state gives (zero unless the FP64
+ * batch keeps diagnostics); reading takes the states and ignores them, as Calc overwrites them. */
+int cm_backup_write(const char *path, const char *time_str, int n_parts, const cm_batch_t *parts,
+                    const int64_t *const *node_ids, const double *const *Vm);
+/* Reads such a file into the parts (their states and Vm). Checks the version line (as the
+ * reference, case-insensitively), the node count against the parts' total and the file size
+ * against the parts' block sizes (acCELLerate.cpp:1575-1578): CM_ERR_FILE on any mismatch.
+ * time_out (may be NULL) receives the time string, at most time_cap bytes with the NUL. */
+int cm_backup_read(const char *path, int n_parts, const cm_batch_t *parts, const int64_t *const *node_ids,
+                   double *const *Vm, char *time_out, size_t time_cap);
+
 /* ------------------------------------------------------------------ batched form */
 /* Many batches (instances) of uneven size and mixed model -- e.g. the per-material cell
  * populations of acCELLerate (acltCellModel.cpp:64-126) or independent simulations -- advanced

@@ -1,7 +1,7 @@
 """Generate the golden vectors in this folder by running the reference's own CellModel
 library (compiled from the reference sources by oracle/Makefile, target `ref`).
 
-    python tests/golden/make_golden.py [tt2] [crn] [ord] [tom]   # needs the reference tree (CM_REFERENCE_TREE)
+    python tests/golden/make_golden.py [tt2] [crn] [ord] [tom] [backup]   # needs the reference tree (CM_REFERENCE_TREE)
 
 Outputs (all seeded, deterministic):
   params_tt2_epi.json / params_crn.json  resolved parameter sets after Init + Calculate
@@ -15,6 +15,8 @@ Outputs (all seeded, deterministic):
                     file per cell type, step_ord_<v>.npz)
   trace_<m>.npz     multi-beat driver runs of jittered cells: Vm every 100 steps and the
                     final state blocks (O'Hara-Rudy: trace_ord_<v>.npz)
+  backup_mixed.abp  an acCELLerate backup file of seven nodes of three models (+ .npz with the
+                    parts' blocks, Vm and node indices)
 """
 from __future__ import annotations
 
@@ -156,6 +158,37 @@ def dump_trace(ref, model, variant=None):
                         trace=tr, final_state=cells.get_state(), final_vm=vm)
 
 
+BACKUP_VERSION = "acCELLerateBackupVersion1.0"  # acCELLerate.cpp:74
+
+
+def dump_backup(ref):
+    """A seven-node acCELLerate backup file with three materials interleaved (TT2 epi at nodes 0, 3,
+    6; Courtemanche at 1, 4; O'Hara-Rudy endo at 2, 5), written as acCELLerate::WriteBackup does
+    (acCELLerate.cpp:1616-1661: the version line, "<time> <nodes>", then per node its Vm and its
+    model's GetBase() block as raw doubles), from blocks and potentials of the reference's own
+    models after 50 ms of pacing. Also stores the parts' blocks, Vm and node indices."""
+    parts = [(O.TT2, None, [0, 3, 6]), (O.CRN, None, [1, 4]), (O.ORD, "endo", [2, 5])]
+    n_total = sum(len(ids) for _, _, ids in parts)
+    rec = {}
+    out = {}
+    for model, variant, ids in parts:
+        cells = ref.create(model, DT, len(ids), ev=ev_of(model, variant))
+        vm = np.full(len(ids), cells.init_vm())
+        cells.run(vm, 5000, DT, textbegin=0.0, textlen=stim_len(model), bcl=1.0, amp=amp(model))
+        blk = cells.get_state()
+        if model == O.ORD:
+            blk[:, 4] = 0.0  # h_CaMK_fast, never set by the reference's Init
+        key = tag(model, variant)
+        out[f"blocks_{key}"], out[f"vm_{key}"], out[f"ids_{key}"] = blk, vm, np.array(ids, dtype=np.int64)
+        for k, g in enumerate(ids):
+            rec[g] = np.concatenate([[vm[k]], blk[k]]).astype("<f8").tobytes()
+    with open(OUT / "backup_mixed.abp", "wb") as f:
+        f.write(f"{BACKUP_VERSION}\n0.05 {n_total}\n".encode())
+        for g in range(n_total):
+            f.write(rec[g])
+    np.savez_compressed(OUT / "backup_mixed.npz", time="0.05", **out)
+
+
 def main(which):
     ref = O.Ref()
     port = O.Port()
@@ -175,7 +208,10 @@ def main(which):
             dump_step(ref, model, v)
             dump_trace(ref, model, v)
             print("wrote golden vectors for", O.MODEL_NAMES[model], v)
+    if "backup" in which:
+        dump_backup(ref)
+        print("wrote the backup file fixture")
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"tt2", "crn", "ord", "tom"})
+    main(set(sys.argv[1:]) or {"tt2", "crn", "ord", "tom", "backup"})

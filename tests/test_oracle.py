@@ -124,3 +124,21 @@ def test_port_is_bitwise_reference(port, ref, model):
     Sr = cells.get_state()
     cols = [c for c in range(B.shape[1]) if not (model == O.TT2 and c == 22)]
     assert np.array_equal(B[:, cols], Sr[:, cols])
+
+
+def test_backup_fixture_layout():
+    """The backup-file fixture (tests/golden/make_golden.py backup) is laid out as
+    acCELLerate::WriteBackup writes (acCELLerate.cpp:1616-1661): two header lines, then per node
+    Vm and the model's block, nodes in global order."""
+    data = (O.GOLDEN / "backup_mixed.abp").read_bytes()
+    g = np.load(O.GOLDEN / "backup_mixed.npz")
+    head = b"acCELLerateBackupVersion1.0\n0.05 7\n"
+    assert data.startswith(head)
+    nodes = {}
+    for key in ("tt2", "crn", "ord_endo"):
+        for k, gid in enumerate(g[f"ids_{key}"]):
+            nodes[int(gid)] = np.concatenate([[g[f"vm_{key}"][k]], g[f"blocks_{key}"][k]])
+    body = np.frombuffer(data[len(head):], "<f8")
+    expect = np.concatenate([nodes[i] for i in range(7)])
+    assert np.array_equal(body, expect)
+    assert [nodes[i].size - 1 for i in range(3)] == [36, 22, 59]  # TT2, Courtemanche, O'Hara-Rudy blocks
