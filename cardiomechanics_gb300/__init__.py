@@ -56,7 +56,8 @@ ABI_SYMBOLS = (
     "cm_surrogate_fit", "cm_surrogate_blob_size", "cm_surrogate_get_blob", "cm_surrogate_set_blob",
     "cm_batch_run_surrogate", "cm_mlp_forward_static", "cm_surrogate_flush_audit",
     "cm_diffusion_create", "cm_diffusion_destroy", "cm_diffusion_apply", "cm_batch_run_diffuse",
-    "cm_backup_write", "cm_backup_read",
+    "cm_backup_write", "cm_backup_read", "cm_theta_create", "cm_theta_destroy", "cm_theta_solve",
+    "cm_batch_run_theta",
 )
 
 
@@ -76,6 +77,14 @@ class Stimulus(ctypes.Structure):
     _fields_ = [("t0", ctypes.c_double), ("textbegin", ctypes.c_double),
                 ("textbegin_per_cell", ctypes.POINTER(ctypes.c_double)), ("textlen", ctypes.c_double),
                 ("bcl", ctypes.c_double), ("amplitude", ctypes.c_double)]
+
+
+class ThetaStats(ctypes.Structure):
+    _fields_ = [("solves", ctypes.c_int64), ("iterations", ctypes.c_int64), ("max_iterations", ctypes.c_int64),
+                ("not_converged", ctypes.c_int64), ("last_norm", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class SurrogateStats(ctypes.Structure):
@@ -137,6 +146,11 @@ def lib() -> ctypes.CDLL:
     L.cm_multi_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.cm_multi_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.cm_theta_create.argtypes = [ctypes.POINTER(vp), vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    L.cm_theta_destroy.argtypes = [vp]
+    L.cm_theta_solve.argtypes = [vp, vp, ctypes.POINTER(ThetaStats)]
+    L.cm_batch_run_theta.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), ctypes.c_double, vp, ctypes.c_double,
+                                     ctypes.POINTER(ThetaStats)]
     L.cm_backup_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp),
                                   ctypes.POINTER(vp), ctypes.POINTER(vp)]
     L.cm_backup_read.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp),
@@ -394,6 +408,21 @@ class Batch:
         _check(lib().cm_batch_run_diffuse(self._h, diffusion._h, _ptr(Vm), int(n_steps), ctypes.byref(st),
                                           vm_range, _ptr(act), act_threshold))
 
+    def run_theta(self, theta, Vm, n_steps, *, textbegin=0.0, textlen=1e-3, bcl=1.0, amplitude=0.0, t0=0.0,
+                  textbegin_per_cell=None, vm_range=0.0, act=None, act_threshold=-0.02):
+        """n_steps implicit finite-element monodomain steps (acCELLerate::IntraStep with IntraRHS):
+        cell update with the stimulus, Vm += dVm, range check, the solve of `theta`, activation
+        times. Vm and act updated in place; returns the solves' statistics."""
+        Vm = _f64(Vm, self.n, "Vm")
+        act = _f64(act, self.n, "act")
+        tbc = _per_cell_times(textbegin_per_cell, self.n)
+        st = Stimulus(t0, textbegin, None if tbc is None else ctypes.cast(_ptr(tbc), ctypes.POINTER(ctypes.c_double)),
+                      textlen, bcl, amplitude)
+        stats = ThetaStats()
+        _check(lib().cm_batch_run_theta(self._h, theta._h, _ptr(Vm), int(n_steps), ctypes.byref(st), vm_range,
+                                        _ptr(act), act_threshold, ctypes.byref(stats)))
+        return stats.as_dict()
+
     def audit(self, per_cell: bool = False):
         m = ctypes.c_uint32()
         pc = np.zeros(self.n, np.uint32) if per_cell else None
@@ -436,6 +465,34 @@ class Diffusion:
             y = np.zeros(self.n)
         _check(lib().cm_diffusion_apply(self._h, _ptr(x), _ptr(y)))
         return y
+
+
+class Theta:
+    """The implicit finite-element step's solve (acCELLerate::IntraStep with IntraRHS): x <- A^-1 (R x)
+    by Jacobi-preconditioned conjugate gradients in FP64. lhs, rhs: Diffusion operators of A and R
+    built with uniform_scale 1 (kept alive by this object)."""
+
+    def __init__(self, lhs, rhs, rtol=1e-6, atol=1e-6, max_iter=1000):
+        self.lhs, self.rhs = lhs, rhs
+        h = ctypes.c_void_p()
+        _check(lib().cm_theta_create(ctypes.byref(h), lhs._h, rhs._h, float(rtol), float(atol), int(max_iter)))
+        self._h = h
+        self.n = lhs.n
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cm_theta_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def solve(self, x):
+        """x <- A^-1 (R x) in place (float64 array or tensor); returns the solve's statistics."""
+        x = _f64(x, self.n, "x")
+        stats = ThetaStats()
+        _check(lib().cm_theta_solve(self._h, _ptr(x), ctypes.byref(stats)))
+        return stats.as_dict()
 
 
 class Multi:

@@ -13,29 +13,6 @@
 
 using namespace cm;
 
-struct cm_diffusion_s {
-  int64_t n = 0, n_slices = 0, entries = 0;
-  int wmax = 0;  // widest slice
-  int64_t *sl_ptr = nullptr;  // n_slices + 1 entry offsets
-  int32_t *sl_col = nullptr;
-  double *val64 = nullptr;
-  float *val32 = nullptr;     // off-diagonal entries only (the diagonal is in rowsum32)
-  float *rowsum32 = nullptr;  // sum of the row's entries, formed in FP64
-  double *scale64 = nullptr;
-  float *scale32 = nullptr;
-  double uniform = 0.0;
-  void fill(StepIO &io, bool fp32) const {
-    io.sl_ptr = sl_ptr;
-    io.sl_col = sl_col;
-    io.sl_val64 = fp32 ? nullptr : val64;
-    io.sl_val32 = fp32 ? val32 : nullptr;
-    io.rowsum32 = rowsum32;
-    io.dscale64 = scale64;
-    io.dscale32 = scale32;
-    io.dscale_u = uniform;
-    io.sl_wmax = wmax;
-  }
-};
 
 namespace {
 

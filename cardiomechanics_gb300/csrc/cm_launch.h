@@ -101,6 +101,42 @@ cudaError_t launch_staged(const DevBatch &b, const StepIO &io, int threads, int 
 // The staged kernel as a producer/consumer pipeline (one bulk-copy warp, mbarrier hand-over).
 cudaError_t launch_pipe(const DevBatch &b, const StepIO &io, int threads, int blocks_per_sm, cudaStream_t s);
 int n_register_shapes();  // variants below this index are the register kernels
+
+// The implicit finite-element step's solver (cm_theta.cu): operators in the 32-row slices of
+// cm_diffusion_s, the conjugate-gradient vectors, per-block partial sums (G blocks; rz and zz
+// double-buffered by iteration parity), the tolerances and the device-side outcome.
+struct ThetaOp {
+  const int64_t *ptr = nullptr;
+  const int32_t *col = nullptr;
+  const double *val = nullptr;
+  int64_t n = 0;
+};
+struct ThetaVecs {
+  double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+  const double *dinv = nullptr;
+};
+struct ThetaPart {
+  double *bb = nullptr, *pq = nullptr, *rz = nullptr, *zz = nullptr;  // G, G, 2 G, 2 G
+  int G = 0;
+};
+struct ThetaCfg {
+  double rtol = 1e-6, atol = 1e-6, dtol = 1e4;
+};
+struct ThetaStat {
+  int done;   // 0 running or out of iterations, 1 converged, 2 diverged, 3 breakdown
+  int iters;  // iterations taken
+  double znorm;  // the last preconditioned residual norm
+};
+int theta_grid();
+cudaError_t launch_theta_dinv(const ThetaOp &A, double *dinv, int *bad, cudaStream_t s);
+// r, z, p from x (b = R x), q = A p, and the test on the initial residual
+cudaError_t launch_theta_init(const ThetaOp &A, const ThetaOp &R, const ThetaVecs &v, const ThetaPart &P,
+                              const ThetaCfg &cfg, ThetaStat *st, cudaStream_t s);
+// iterations k0 .. k0 + count - 1 (each a no-op once the device-side outcome is set)
+cudaError_t launch_theta_iters(const ThetaOp &A, const ThetaVecs &v, const ThetaPart &P, const ThetaCfg &cfg,
+                               ThetaStat *st, int k0, int count, cudaStream_t s);
+// activation times after the solve (acCELLerate.cpp:1997-2005)
+cudaError_t launch_theta_act(const double *x, double *act, int64_t n, double thr, double t, cudaStream_t s);
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.
 cudaError_t launch_probe(const double *vm, const float *vm_hi, const float *vm_lo, const int64_t *probe,
                          int64_t n_probe, double *out, int64_t stride, int64_t k, cudaStream_t s);

@@ -129,3 +129,53 @@ def grid_laplacian(nx: int, ny: int, nz: int = 1, d_over_h2: float = 1.0e4):
     keep = C >= 0
     rowptr = np.concatenate([[0], np.cumsum(keep.sum(axis=1))]).astype(np.int64)
     return rowptr, C[keep].astype(np.int32), V[keep].astype(np.float64)
+
+
+def fe_q1_grid(nx: int, ny: int, nz: int = 1, h: float = 1.0e-4, sigma: float = 0.1):
+    """Mass M and stiffness K (conductivity sigma [S/m]) of bilinear (nz = 1) or trilinear
+    finite elements on a structured grid of nx x ny (x nz) nodes with spacing h [m], node
+    l = x + nx (y + ny z), assembled as Kronecker products of the 1-D linear-element matrices
+    (exact for tensor-product Q1 elements). Returns scipy CSR matrices (M, K)."""
+    import scipy.sparse as sp
+
+    def one_d(m):
+        e = np.ones(m)
+        mass = sp.diags([e[:-1], 4 * e, e[:-1]], [-1, 0, 1]).tolil() * (h / 6.0)
+        mass[0, 0] = mass[m - 1, m - 1] = 2 * h / 6.0
+        stiff = sp.diags([-e[:-1], 2 * e, -e[:-1]], [-1, 0, 1]).tolil() / h
+        stiff[0, 0] = stiff[m - 1, m - 1] = 1.0 / h
+        return mass.tocsr(), stiff.tocsr()
+
+    dims = [nx, ny] + ([nz] if nz > 1 else [])
+    mk = [one_d(m) for m in dims]
+    M = mk[-1][0]
+    for m, _ in reversed(mk[:-1]):
+        M = sp.kron(M, m, format="csr")
+    K = None
+    for d in range(len(dims)):
+        term = None
+        for k in reversed(range(len(dims))):
+            f = mk[k][1] if k == d else mk[k][0]
+            term = f if term is None else sp.kron(term, f, format="csr")
+        K = term if K is None else K + term
+    K = (sigma * K).tocsr()
+    M.sort_indices()
+    K.sort_indices()
+    return M.tocsr(), K
+
+
+def theta_operators(M, K, dt: float, cm_beta: float = 0.01 * 1.4e5, theta: float = 0.5):
+    """The reference's theta-scheme operators (acCELLerate.cpp:541-653): A = C_m beta/dt M + theta K
+    (Intra.A) and R = C_m beta/dt M - (1 - theta) K (IntraRHS), both on the union of M's and K's
+    patterns, in CSR with sorted columns. Default C_m beta: 1 uF/cm^2 x 1400/cm."""
+    a = cm_beta / dt
+    A = (a * M + theta * K).tocsr()
+    R = (a * M - (1.0 - theta) * K).tocsr()
+    A.sort_indices()
+    R.sort_indices()
+    return A, R
+
+
+def csr_arrays(S):
+    """(rowptr int64, col int32, val float64) of a scipy CSR matrix."""
+    return S.indptr.astype(np.int64), S.indices.astype(np.int32), S.data.astype(np.float64)

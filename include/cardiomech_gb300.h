@@ -245,6 +245,40 @@ int cm_diffusion_apply(cm_diffusion_t d, const double *x, double *y);
 int cm_batch_run_diffuse(cm_batch_t b, cm_diffusion_t d, double *Vm, int64_t n_steps, const cm_stimulus *stim,
                          double vm_range, double *act, double act_threshold);
 
+/* ------------------------------------------------------------------ implicit step */
+/* The finite-element path of acCELLerate::IntraStep (IntraRHS set, acCELLerate.cpp:1951-1993):
+ * after the cell update, b = R x and the solve A x = b with A = C_m beta/dt M + theta K (the
+ * reference's Intra.A) and R = C_m beta/dt M - (1 - theta) K (its IntraRHS), both given as
+ * cm_diffusion_t operators built with uniform_scale 1 (the handle borrows them: destroy it
+ * first). A must be symmetric positive definite with a positive diagonal: the solve is
+ * conjugate gradients with the Jacobi preconditioner in FP64 from the current x as initial guess
+ * (the reference: GMRES with block Jacobi, nonzero initial guess, PETScLSE.h:370-381), stopped
+ * by PETSc's default test on the preconditioned residual, ||D^-1 r|| < max(rtol ||D^-1 b||,
+ * atol), after max_iter iterations, or as divergence at dtol = 1e4 (acCELLerate.cpp:19-24 use
+ * rtol = atol = 1e-6, max_iter = 1000). */
+typedef struct cm_theta_s *cm_theta_t;
+typedef struct {
+  int64_t solves;          /* solves accounted */
+  int64_t iterations;      /* their iterations in total */
+  int64_t max_iterations;  /* the most any of them took */
+  int64_t not_converged;   /* solves that ended without meeting the test */
+  double last_norm;        /* the last solve's final preconditioned residual norm */
+} cm_theta_stats;
+
+int cm_theta_create(cm_theta_t *out, cm_diffusion_t lhs, cm_diffusion_t rhs, double rtol, double atol,
+                    int max_iter);
+int cm_theta_destroy(cm_theta_t t);
+/* x <- A^-1 (R x); x: n doubles, host or device. stats (may be NULL) accumulates. CM_ERR_NUMERIC
+ * when the solve diverged or broke down; a solve that ran out of iterations returns CM_OK and
+ * counts in stats->not_converged (the reference prints a warning and goes on). */
+int cm_theta_solve(cm_theta_t t, double *x, cm_theta_stats *stats);
+/* n_steps implicit monodomain steps of batch b: the cell update with the stimulus protocol (as
+ * cm_batch_run; no coupling current on this path), Vm += dVm with the range check (vm_range > 0),
+ * the solve, and activation times after it (act: n doubles or NULL; entries -1 whose new Vm
+ * reaches act_threshold get the step's time). Vm: n doubles, host or device, updated in place. */
+int cm_batch_run_theta(cm_batch_t b, cm_theta_t t, double *Vm, int64_t n_steps, const cm_stimulus *stim,
+                       double vm_range, double *act, double act_threshold, cm_theta_stats *stats);
+
 /* ------------------------------------------------------------------ backup files */
 /* acCELLerate backup files (acCELLerate::WriteBackup / ReadBackup, acCELLerate.cpp:1511-1661):
  * the line "acCELLerateBackupVersion1.0", the line "<time> <number of nodes>", then for every
