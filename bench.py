@@ -753,6 +753,69 @@ def tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     return out
 
 
+# Implicit finite-element leg: trilinear elements on a 128 x 128 x 64 node slab (1,048,576 nodes,
+# 0.1 mm, sigma 0.1 S/m, C_m beta = 1 uF/cm^2 x 1400/cm, theta 0.5, the reference's rtol = atol =
+# 1e-6). Bytes per node of one CG iteration: kernel a reads p, q, r, x, D^-1 and writes x, r, z
+# (64 B); kernel b reads z, p, q, writes p, q and reads A's row: 27 entries of (4 + 8) B (364 B).
+THETA_DIMS = (128, 128, 64)
+THETA_ITER_BYTES = 64 + 5 * 8 + 27 * 12
+
+
+def theta_leg(cm, torch, stream, args, hbm_peak, peak_kind):
+    """The implicit finite-element monodomain step (acCELLerate::IntraStep with IntraRHS): TT2 mixed
+    cell update + Godunov step + the solve of (C_m beta/dt M + theta K) x = (C_m beta/dt M - (1 -
+    theta) K) x by Jacobi-preconditioned CG, per step; activation times."""
+    from cardiomechanics_gb300 import workloads as W
+    nx, ny, nz = THETA_DIMS if args.theta_dims is None else tuple(args.theta_dims)
+    n = nx * ny * nz
+    t0 = time.perf_counter()
+    M, K = W.fe_q1_grid(nx, ny, nz)
+    A, R = W.theta_operators(M, K, DT)
+    del M, K
+    dA, dR = cm.Diffusion(*W.csr_arrays(A)), cm.Diffusion(*W.csr_arrays(R))
+    nnz_row = A.nnz / n
+    del A, R
+    setup_s = time.perf_counter() - t0
+    th = cm.Theta(dA, dR)
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    b = cm.Batch(p, n, cm.MIXED, stream=stream.cuda_stream)
+    sc = W.conductance_scales(5, n, 3, 0.95, 1.05)
+    for k, h in enumerate(W.TT2_HETERO):
+        b.add_hetero_value(h, p.get(h) * sc[k])
+    tb = torch.tensor(np.where(np.arange(n) % nx < 3, 0.0, 1e9), device="cuda")
+    vm = torch.tensor(b.init_vm(), device="cuda")
+    act = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    kw = dict(textlen=1e-3, bcl=1e9, amplitude=2 * W.TT2_STIM_NA, vm_range=0.2, act_threshold=-0.02)
+    b.run_theta(th, vm, 3, textbegin_per_cell=tb, act=act, **kw)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    steps = args.theta_steps
+    e0.record(stream)
+    st = b.run_theta(th, vm, steps, t0=3 * DT, textbegin_per_cell=tb, act=act, **kw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    iters = st["iterations"] / max(1, st["solves"])
+    # per step: the cell update (TT2 mixed, FP64 Vm in/out: 168 + 16 + 12 B), the solve's setup
+    # (R and A rows, x, r, z, p, q: 2 x 27 x 12 + 6 x 8 B) and its iterations
+    step_bytes = (168 + 16 + 12) + (2 * 27 * 12 + 6 * 8) + iters * THETA_ITER_BYTES
+    achieved = step_bytes * n * steps / sec / 1e9
+    out = {"workload": f"tt2006-epi-fe-slab-{nx}x{ny}x{nz}", "nodes": n, "nnz_per_row": nnz_row,
+           "elements": "trilinear hexahedra, h 0.1 mm, sigma 0.1 S/m, C_m beta 1 uF/cm^2 x 1400/cm, theta 0.5",
+           "solver": "CG + Jacobi, FP64, rtol = atol = 1e-6 (PETSc default test, preconditioned norm)",
+           "value": n * steps / sec, "unit": "node-steps/s", "steps": steps, "ms_per_step": 1e3 * sec / steps,
+           "cg_iterations_per_step": iters, "max_iterations": st["max_iterations"],
+           "not_converged": st["not_converged"], "activated": int((act >= 0).sum().item()),
+           "gpu_launches_per_step": 1 + 2 + 2 * iters + 1,
+           "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                   "peak_kind": peak_kind, "bytes_per_node_step": step_bytes},
+           "setup_s_host": setup_s}
+    del th, dA, dR, b, vm, act, tb
+    torch.cuda.empty_cache()
+    return out
+
+
 def precision_leg(cm, torch, stream, args, hbm_peak, peak_kind):
     """Precision form: 4,194,304 cells, the HBM-bound plain kernel (autotuned launch shape)."""
     p, b = make_batch(cm, cm.MIXED, stream.cuda_stream)
@@ -804,7 +867,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
-                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tomek", "tissue"],
+                    choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tomek", "tissue",
+                             "theta"],
                     help="run one leg only (profiler captures); the contract's JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
@@ -824,6 +888,9 @@ def main():
     ap.add_argument("--tissue-steps", type=int, default=500, help="timed steps of the coupled (tissue) leg")
     ap.add_argument("--tissue-dims", type=int, nargs=3, default=None, help="slab size (fewer nodes only for captures)")
     ap.add_argument("--no-tissue", action="store_true")
+    ap.add_argument("--theta-steps", type=int, default=200, help="timed steps of the implicit FE leg")
+    ap.add_argument("--theta-dims", type=int, nargs=3, default=None, help="FE slab nodes (fewer only for captures)")
+    ap.add_argument("--no-theta", action="store_true")
     ap.add_argument("--tissue-model", default="tt2", choices=list(TISSUE_MODELS),
                     help="cell model of the tissue leg (the headline run uses tt2)")
     args = ap.parse_args()
@@ -856,6 +923,9 @@ def main():
         return
     if args.only == "tissue":
         print(json.dumps(tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
+        return
+    if args.only == "theta":
+        print(json.dumps(theta_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
         return
     if args.only in ("ord", "tomek"):
         leg = "ohara_rudy" if args.only == "ord" else "tomek"
@@ -894,6 +964,7 @@ def main():
     if not args.no_batched:
         bat = batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind)
     tissue = None if args.no_tissue else tissue_leg(cm, torch, stream, args, hbm_peak, peak_kind)
+    theta = None if args.no_theta else theta_leg(cm, torch, stream, args, hbm_peak, peak_kind)
     ionic = {}
     for leg in IONIC_LEGS:
         ionic[leg] = None if args.no_ord else ionic_leg(
@@ -932,6 +1003,7 @@ def main():
             "ohara_rudy": ionic["ohara_rudy"],
             "tomek": ionic["tomek"],
             "tissue": tissue,
+            "theta": theta,
             "fp32_fma_peak_tflops_measured": fp32_peak,
             "cpu_baseline": cpu,
             "gpu_launches": full["gpu_launches"],

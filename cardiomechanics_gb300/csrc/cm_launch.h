@@ -126,15 +126,19 @@ struct ThetaStat {
   int done;   // 0 running or out of iterations, 1 converged, 2 diverged, 3 breakdown
   int iters;  // iterations taken
   double znorm;  // the last preconditioned residual norm
+  int ka, kb;    // the iteration index, handed from kernel a to b and from b to the next a
 };
 int theta_grid();
 cudaError_t launch_theta_dinv(const ThetaOp &A, double *dinv, int *bad, cudaStream_t s);
 // r, z, p from x (b = R x), q = A p, and the test on the initial residual
 cudaError_t launch_theta_init(const ThetaOp &A, const ThetaOp &R, const ThetaVecs &v, const ThetaPart &P,
                               const ThetaCfg &cfg, ThetaStat *st, cudaStream_t s);
-// iterations k0 .. k0 + count - 1 (each a no-op once the device-side outcome is set)
+// count more iterations (each a no-op once the device-side outcome is set)
 cudaError_t launch_theta_iters(const ThetaOp &A, const ThetaVecs &v, const ThetaPart &P, const ThetaCfg &cfg,
-                               ThetaStat *st, int k0, int count, cudaStream_t s);
+                               ThetaStat *st, int max_iter, int count, cudaStream_t s);
+// the iterations as a conditional while node of a graph: launched once per solve, no host reads
+cudaError_t build_theta_graph(const ThetaOp &A, const ThetaVecs &v, const ThetaPart &P, const ThetaCfg &cfg,
+                              ThetaStat *st, int max_iter, cudaGraphExec_t *exec);
 // activation times after the solve (acCELLerate.cpp:1997-2005)
 cudaError_t launch_theta_act(const double *x, double *act, int64_t n, double thr, double t, cudaStream_t s);
 // Copies Vm[probe[i]] into out[i * stride + k] for i < n_probe.

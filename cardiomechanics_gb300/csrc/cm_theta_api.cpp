@@ -22,7 +22,12 @@ struct cm_theta_s {
   int *bad = nullptr;
   ThetaCfg cfg;
   int max_iter = 1000;
-  int chunk = 8;  // iterations launched between two reads of the outcome
+  int last_iters = 7;  // iterations of the last solve (the fallback's first chunk)
+  cudaGraphExec_t loop = nullptr;  // the iterations as a conditional while node, for x == loop_x
+  double *loop_x = nullptr;
+  bool no_graph = false;           // the conditional node could not be built: chunks of launches
+  ThetaStat *ring = nullptr;       // pinned outcome records of cm_batch_run_theta
+  double *xbuf = nullptr;          // cm_theta_solve's device copy of a host x (one address: one graph)
   int G = 0;
   ThetaOp op(const cm_diffusion_s *d) const {
     ThetaOp o;
@@ -55,32 +60,61 @@ struct cm_theta_s {
 
 namespace {
 
+constexpr int kRing = 64;  // solves between two reads of their outcomes in cm_batch_run_theta
+
 void free_theta(cm_theta_s *t) {
+  if (t->loop) cudaGraphExecDestroy(t->loop);
   cudaFree(t->vec);
   cudaFree(t->part);
   cudaFree(t->st);
   cudaFree(t->bad);
   cudaFreeHost(t->st_host);
+  cudaFreeHost(t->ring);
+  cudaFree(t->xbuf);
   delete t;
 }
 
-// One solve on stream s, x on the device; the outcome into *out (host).
-int theta_solve(cm_theta_s *t, double *x, cudaStream_t s, ThetaStat *out) {
+// Enqueues one solve on stream s (x on the device): the setup kernels, then the iterations as
+// one launch of the conditional-loop graph. Returns with the outcome still on the device (t->st)
+// unless the graph could not be built, in which case chunks of iterations are launched with a
+// read of the outcome after each (*synced = true, outcome in *t->st_host).
+int theta_enqueue(cm_theta_s *t, double *x, cudaStream_t s, bool *synced) {
   const ThetaOp A = t->op(t->lhs), R = t->op(t->rhs);
   const ThetaVecs v = t->vecs(x);
   const ThetaPart P = t->parts();
+  *synced = false;
   CK(launch_theta_init(A, R, v, P, t->cfg, t->st, s));
-  CK(cudaMemcpyAsync(t->st_host, t->st, sizeof(ThetaStat), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  if (!t->no_graph && (t->loop == nullptr || t->loop_x != x)) {
+    if (t->loop) {
+      CK(cudaStreamSynchronize(s));
+      cudaGraphExecDestroy(t->loop);
+      t->loop = nullptr;
+    }
+    cudaError_t e = build_theta_graph(A, v, P, t->cfg, t->st, t->max_iter, &t->loop);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      t->loop = nullptr;
+      t->no_graph = true;
+    } else {
+      t->loop_x = x;
+    }
+  }
+  if (t->loop) {
+    CK(cudaGraphLaunch(t->loop, s));
+    return CM_OK;
+  }
   int k = 0;
-  while (!t->st_host->done && k < t->max_iter) {
-    const int c = std::min(t->chunk, t->max_iter - k);
-    CK(launch_theta_iters(A, v, P, t->cfg, t->st, k, c, s));
+  int c = std::max(1, std::min(t->last_iters + 1, 32));
+  do {
+    c = std::min(c, t->max_iter - k);
+    CK(launch_theta_iters(A, v, P, t->cfg, t->st, t->max_iter, c, s));
     k += c;
+    c = 4;
     CK(cudaMemcpyAsync(t->st_host, t->st, sizeof(ThetaStat), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-  }
-  *out = *t->st_host;
+  } while (!t->st_host->done && k < t->max_iter);
+  t->last_iters = t->st_host->iters;
+  *synced = true;
   return CM_OK;
 }
 
@@ -146,20 +180,22 @@ int cm_theta_solve(cm_theta_t t, double *x, cm_theta_stats *stats) {
   const bool host = !is_device_ptr(x);
   double *dx = x;
   if (host) {
-    CK(cudaMalloc(&dx, n * sizeof(double)));
-    cudaError_t e = cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      cudaFree(dx);
-      return cuda_fail(e, "cm_theta_solve");
-    }
+    if (!t->xbuf) CK(cudaMalloc(&t->xbuf, n * sizeof(double)));
+    dx = t->xbuf;
+    CK(cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice));
   }
   ThetaStat o{};
-  int rc = theta_solve(t, dx, nullptr, &o);
+  bool synced = false;
+  int rc = theta_enqueue(t, dx, nullptr, &synced);
+  if (!rc && !synced) {
+    cudaError_t e = cudaMemcpy(t->st_host, t->st, sizeof(ThetaStat), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cm_theta_solve");
+  }
+  if (!rc) o = *t->st_host;
   if (!rc && host) {
     cudaError_t e = cudaMemcpy(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) rc = cuda_fail(e, "cm_theta_solve");
   }
-  if (host) cudaFree(dx);
   if (rc) return rc;
   account(stats, o);
   if (o.done == 2 || o.done == 3)
@@ -192,6 +228,8 @@ int cm_batch_run_theta(cm_batch_t b, cm_theta_t t, double *Vm, int64_t n_steps, 
   if (per_cell && (rc = per_cell_times(b, stim->textbegin_per_cell, b->stream, &tb_cell))) return rc;
   // the cell update and Godunov step in place (acCELLerate.cpp:1904-1949): no coupling current
   // (B = 0 on the implicit path, 1860-1862), the stimulus as the conditions give it
+  if (!t->ring) CK(cudaMallocHost(&t->ring, kRing * sizeof(ThetaStat)));
+  ThetaStat *ring = t->ring;
   StepIO io;
   io.vm = x;
   io.vm_out = x;
@@ -212,14 +250,22 @@ int cm_batch_run_theta(cm_batch_t b, cm_theta_t t, double *Vm, int64_t n_steps, 
       io.iext_uniform = i_ext;
     }
     CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, b->stream));
-    ThetaStat o{};
-    if ((rc = theta_solve(t, x, b->stream, &o))) return rc;
-    account(stats, o);
-    if (o.done == 2 || o.done == 3)
-      return fail(CM_ERR_NUMERIC, std::string(o.done == 2 ? "the solve diverged" : "the solve broke down") +
-                                      " at step " + std::to_string(s));
+    bool synced = false;
+    if ((rc = theta_enqueue(t, x, b->stream, &synced))) return rc;
+    // the outcomes go to a ring of pinned records, read every kRing steps (no read per step)
+    const int slot = (int)(s % kRing);
+    CK(cudaMemcpyAsync(ring + slot, t->st, sizeof(ThetaStat), cudaMemcpyDeviceToHost, b->stream));
     if (dact) CK(launch_theta_act(x, dact, n, act_threshold, t_now, b->stream));
     t_now += b->ps.dt;
+    if (slot == kRing - 1 || s == n_steps - 1) {
+      CK(cudaStreamSynchronize(b->stream));
+      for (int j = 0; j <= slot; j++) {
+        account(stats, ring[j]);
+        if (ring[j].done == 2 || ring[j].done == 3)
+          return fail(CM_ERR_NUMERIC, std::string(ring[j].done == 2 ? "the solve diverged" : "the solve broke down") +
+                                          " at step " + std::to_string(s - slot + j));
+      }
+    }
   }
   if (host_vm) CK(cudaMemcpyAsync(Vm, x, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (host_act) CK(cudaMemcpyAsync(act, dact, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
