@@ -500,7 +500,8 @@ BATCHED_BCL = 1.0
 # Algorithmic bytes per cell-step of the batched kernel (no per-cell conductances: each
 # instance has its own parameter set): state planes and the Vm hi/lo pair read and written.
 MULTI_KERNELS = ["multi_kernel<256>", "multi_kernel<128>", "multi_kernel<512>", "multi_staged_kernel<128>",
-                 "multi_staged_kernel<256>"]
+                 "multi_staged_kernel<256>", "multi_pipe_kernel<256,2>", "multi_pipe_kernel<128,3>",
+                 "multi_pipe_kernel<256,3>", "multi_pipe_kernel<128,4>"]
 BATCHED_BYTES = {"TenTusscher2": 2 * 21 * 4 + 2 * 8, "CourtemancheEtAl": 2 * 25 * 4 + 2 * 8}
 
 

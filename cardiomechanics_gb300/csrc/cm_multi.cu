@@ -349,10 +349,11 @@ __global__ void __launch_bounds__(kT + 32, 2)
 struct MShape {
   int block, minb;
   bool staged, pipe;
+  int stages;  // the pipelines' stage count
 };
-constexpr MShape kMShapes[] = {{256, 2, false, false}, {128, 5, false, false}, {512, 1, false, false},
-                               {128, 2, true, false},  {256, 2, true, false},  {256, 2, true, true},
-                               {128, 2, true, true}};
+constexpr MShape kMShapes[] = {{256, 2, false, false, 0}, {128, 5, false, false, 0}, {512, 1, false, false, 0},
+                               {128, 2, true, false, 0},  {256, 2, true, false, 0},  {256, 2, true, true, 2},
+                               {128, 2, true, true, 3},   {256, 2, true, true, 3},   {128, 2, true, true, 4}};
 
 template <int kT>
 cudaError_t launch_multi_staged(const MultiLaunch &L, const MultiClock *cur, MultiClock *nxt, unsigned int *cnt,
@@ -390,9 +391,15 @@ cudaError_t launch_multi(const MultiLaunch &L, int parity, cudaStream_t s) {
   int shape = L.shape;
   if (shape >= 0 && shape < n_multi_shapes() && kMShapes[shape].staged) {
     if (L.tile_cells % kMShapes[shape].block == 0) {
-      if (kMShapes[shape].pipe)
-        return kMShapes[shape].block == 128 ? launch_multi_pipe<128, 3>(L, cur, nxt, cnt, cnt_next, s)
-                                            : launch_multi_pipe<256, 2>(L, cur, nxt, cnt, cnt_next, s);
+      if (kMShapes[shape].pipe) {
+        const bool b128 = kMShapes[shape].block == 128;
+        switch (kMShapes[shape].stages) {
+          case 2: return launch_multi_pipe<256, 2>(L, cur, nxt, cnt, cnt_next, s);
+          case 3: return b128 ? launch_multi_pipe<128, 3>(L, cur, nxt, cnt, cnt_next, s)
+                              : launch_multi_pipe<256, 3>(L, cur, nxt, cnt, cnt_next, s);
+          default: return launch_multi_pipe<128, 4>(L, cur, nxt, cnt, cnt_next, s);
+        }
+      }
       return kMShapes[shape].block == 128 ? launch_multi_staged<128>(L, cur, nxt, cnt, cnt_next, s)
                                           : launch_multi_staged<256>(L, cur, nxt, cnt, cnt_next, s);
     }

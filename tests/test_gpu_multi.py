@@ -98,7 +98,7 @@ def test_multi_rejects_fp64(gpu):
 
 
 def test_pipeline_shapes_with_many_instances_per_block(gpu):
-    """The pipelined shapes (5, 6) on 160 small instances, so that every block moves between
+    """The pipelined shapes (5-8) on 160 small instances, so that every block moves between
     instances many times and reuses its stage descriptor slots: the same cells as the
     double-buffered shape 4, and no consistency-check bit (128, 256) in any audit word."""
     cm = gpu
@@ -107,7 +107,7 @@ def test_pipeline_shapes_with_many_instances_per_block(gpu):
     models = [cm.TENTUSSCHER2 if i % 3 else cm.COURTEMANCHE for i in range(160)]
     st = stims(cm, models)
     out = []
-    for shape, tile, bps in [(4, 1024, 1), (5, 1024, 1), (6, 1024, 1), (5, 1024, 4)]:
+    for shape, tile, bps in [(4, 1024, 1), (5, 1024, 1), (6, 1024, 1), (5, 1024, 4), (7, 1024, 2), (8, 2048, 2)]:
         mb = build(cm, sizes, models)
         multi = cm.Multi(mb)
         multi.set_launch(tile, shape, bps)
