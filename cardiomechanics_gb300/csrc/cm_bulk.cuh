@@ -29,6 +29,12 @@ static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint
       : "memory");
 }
 
+// Bulk prefetch of [src, src + bytes) into L2 (no completion to wait for); src 16-byte aligned,
+// bytes a multiple of 16.
+static __device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
+
 static __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }

@@ -400,10 +400,21 @@ __global__ void __launch_bounds__(kThreads + 32, kThreads == 256 ? 2 : 3) couple
       const int st = it % kStages;
       const int64_t c0 = (int64_t)t * kThreads;
       int64_t so[kSlices + 1];  // read before the wait: the offsets do not depend on the stage
-      if (kStagedOps) {
+      {
         const int64_t s0 = c0 / 32, s1 = s0 + kSlices < n_slices ? s0 + kSlices : n_slices;
 #pragma unroll
         for (int k = 0; k <= kSlices; k++) so[k] = io.sl_ptr[s0 + k < s1 ? s0 + k : s1];
+      }
+      if (!kStagedOps) {
+        // the consumers read the tile's operator entries, row sums and scales themselves: bring
+        // them into L2 ahead of them (each run starts on a 128-byte boundary, whole slices)
+        const uint32_t eb = (uint32_t)(so[kSlices] - so[0]) * 4u;
+        if (eb) {
+          bulk_prefetch_l2(io.sl_col + so[0], eb);
+          bulk_prefetch_l2(io.sl_val32 + so[0], eb);
+        }
+        bulk_prefetch_l2(io.rowsum32 + c0, kThreads * 4u);
+        if (io.dscale32) bulk_prefetch_l2(io.dscale32 + c0, kThreads * 4u);
       }
       if (it >= kStages && !mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1))) {
         atomicOr(b.audit_or, kAuditTimeout);
