@@ -218,17 +218,51 @@ __global__ void __launch_bounds__(kT + 32, 2)
   __syncthreads();
   if (threadIdx.x >= kT) {  // the producer warp
     const int lane = threadIdx.x - kT;
-    int tile = -1, sub = 0, count = 0;
+    int tile = -1, sub = 0;
+    // the current tile's records (lane 0), read once per tile, before the stage wait
+    MultiTile T{};
+    int64_t ld = 0;
+    int ns = 0, nh = 0;
+    bool bad = false;
+    const float *s32 = nullptr, *vhi = nullptr, *vlo = nullptr;
+    const float *hp[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float iext = 0.f;
     for (int it = 0;; it++) {
       const int st = it % kStages;
       int nt = tile, nsub = sub + 1;
-      if (lane == 0 && (tile < 0 || (int64_t)nsub * kT >= count)) {
+      if (lane == 0 && (tile < 0 || (int64_t)nsub * kT >= T.count)) {
         const int a = (int)atomicAdd(counter, 1u);
         nt = a < n_tiles ? a : -1;
         nsub = 0;
+        if (nt >= 0) {
+          T = tiles[nt];
+          const MultiInst *I = insts + T.inst;
+          ld = I->d.ld;
+          const int model = I->d.model;
+          ns = model == 5 ? StagedVars<5>::kState : StagedVars<2>::kState;
+          bad = model != 5 && model != 2;
+          s32 = I->d.s32;
+          vhi = I->vm_hi;
+          vlo = I->vm_lo;
+          nh = 0;
+#pragma unroll
+          for (int k = 0; k < 6; k++) {
+            hp[k] = (const float *)I->d.het[k];
+            nh += hp[k] ? 1 : 0;
+          }
+          const MultiClock ck = clk_cur[T.inst];
+          iext = ck.t >= ck.tb ? (float)I->amp : 0.f;
+          if (T.start == 0) {  // reference driver clock (CellModel.h:405-419), once per instance
+            MultiClock nx;
+            nx.t = ck.t + I->dt;
+            nx.tb = (ck.t >= ck.tb && ck.t >= ck.tb + I->textlen) ? ck.tb + I->bcl : ck.tb;
+            clk_next[T.inst] = nx;
+          }
+        }
       }
       nt = __shfl_sync(0xffffffffu, nt, 0);
       nsub = __shfl_sync(0xffffffffu, nsub, 0);
+      const int inst = __shfl_sync(0xffffffffu, T.inst, 0);
       int ok = 1;
       if (lane == 0 && it >= kStages) ok = mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1)) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -247,61 +281,44 @@ __global__ void __launch_bounds__(kT + 32, 2)
         }
         return;
       }
-      const MultiTile T = tiles[nt];
-      const MultiInst *I = insts + T.inst;
       // lane 0 decides whether the stage's descriptor slot needs this instance's descriptor and
       // tells the warp: a lane that read s_inst itself could see lane 0's update of it below
       // and skip its share of the copy
-      int need = lane == 0 ? (s_inst[st] != T.inst) : 0;
+      int need = lane == 0 ? (s_inst[st] != inst) : 0;
       need = __shfl_sync(0xffffffffu, need, 0);
       if (need) {  // the instance's descriptor into this stage's slot
-        const int4 *src = reinterpret_cast<const int4 *>(&I->d);
+        const int4 *src = reinterpret_cast<const int4 *>(&insts[inst].d);
         int4 *dst = reinterpret_cast<int4 *>(&sd[st]);
         for (int k = lane; k < (int)(sizeof(DevBatch) / sizeof(int4)); k += 32) dst[k] = src[k];
       }
       if (lane == 0) {
-        s_inst[st] = T.inst;
+        s_inst[st] = inst;
         s_tile[st] = nt;
         s_sub[st] = nsub;
-        const MultiClock ck = clk_cur[T.inst];
-        s_iext[st] = ck.t >= ck.tb ? (float)I->amp : 0.f;
-        if (T.start == 0 && nsub == 0) {  // reference driver clock (CellModel.h:405-419)
-          MultiClock nx;
-          nx.t = ck.t + I->dt;
-          nx.tb = (ck.t >= ck.tb && ck.t >= ck.tb + I->textlen) ? ck.tb + I->bcl : ck.tb;
-          clk_next[T.inst] = nx;
-        }
+        s_iext[st] = iext;
       }
       __syncwarp();
       if (lane == 0) {
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        const int64_t ld = I->d.ld;
-        const int model = I->d.model;
-        const int ns = model == 5 ? StagedVars<5>::kState : StagedVars<2>::kState;
-        int nh = 0;
-        for (int k = 0; k < 6; k++) nh += I->d.het[k] ? 1 : 0;
         const int64_t c0 = (int64_t)T.start + (int64_t)nsub * kT;
         float *dst = stage + (size_t)st * NVMAX * kT;
-        if (c0 < 0 || c0 + kT > ld || (model != 5 && model != 2)) {  // a sub-tile outside its instance
-          atomicOr(I->d.audit_or, kAuditInternal << 1);
+        if (c0 < 0 || c0 + kT > ld || bad) {  // a sub-tile outside its instance
+          atomicOr(insts[inst].d.audit_or, kAuditInternal << 1);
           s_tile[st] = -2;  // the consumers skip it
           mbar_arrive(&full[st]);
-          tile = nt;
-          sub = nsub;
-          count = T.count;
-          continue;
+        } else {
+          mbar_expect_tx(&full[st], (uint32_t)(ns + 2 + nh) * kT * 4u);
+          for (int v = 0; v < ns; v++) bulk_g2s(dst + v * kT, s32 + v * ld + c0, kT * 4u, &full[st]);
+          bulk_g2s(dst + ns * kT, vhi + c0, kT * 4u, &full[st]);
+          bulk_g2s(dst + (ns + 1) * kT, vlo + c0, kT * 4u, &full[st]);
+          int pos = ns + 2;
+#pragma unroll
+          for (int k = 0; k < 6; k++)
+            if (hp[k]) bulk_g2s(dst + (pos++) * kT, hp[k] + c0, kT * 4u, &full[st]);
         }
-        mbar_expect_tx(&full[st], (uint32_t)(ns + 2 + nh) * kT * 4u);
-        for (int v = 0; v < ns; v++) bulk_g2s(dst + v * kT, I->d.s32 + v * ld + c0, kT * 4u, &full[st]);
-        bulk_g2s(dst + ns * kT, I->vm_hi + c0, kT * 4u, &full[st]);
-        bulk_g2s(dst + (ns + 1) * kT, I->vm_lo + c0, kT * 4u, &full[st]);
-        int pos = ns + 2;
-        for (int k = 0; k < 6; k++)
-          if (I->d.het[k]) bulk_g2s(dst + (pos++) * kT, (const float *)I->d.het[k] + c0, kT * 4u, &full[st]);
       }
       tile = nt;
       sub = nsub;
-      count = T.count;
     }
   }
   const int lane = threadIdx.x & 31;
