@@ -95,6 +95,20 @@ inline bool is_device_ptr(const void *p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// The device's address of page-locked host memory (cudaHostAlloc / cudaHostRegister, mapped
+// into the device's address space), or nullptr for any other pointer. Kernels read and write such
+// memory directly over the host link, with no staging copy.
+inline double *mapped_host_ptr(void *p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<double *>(at.devicePointer);
+}
+
 // Grows the batch's four staging buffers to n doubles each.
 inline int ensure_stage(cm_batch_s *b, int64_t n) {
   if (b->stage_n >= n) return CM_OK;

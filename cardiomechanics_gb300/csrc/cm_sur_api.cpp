@@ -151,12 +151,18 @@ int check_batch(cm_batch_s *b) {
   return CM_OK;
 }
 
-// Vm planes of a batch for a run: split from the caller's doubles (staged if on the host)
+// Vm planes of a batch for a run: split from the caller's doubles. Page-locked host memory is
+// read (and later written) by the split/join kernels themselves over the host link; other host
+// memory goes through a staging copy.
 int planes_in(cm_batch_s *b, double *Vm, double **dvm, bool &host_vm, cudaStream_t s) {
   const int64_t n = b->d.n;
   host_vm = !is_device_ptr(Vm);
   *dvm = Vm;
-  if (host_vm) {
+  double *mapped = host_vm ? mapped_host_ptr(Vm) : nullptr;
+  if (mapped) {
+    host_vm = false;  // the kernels reach it: no copy back either
+    *dvm = mapped;
+  } else if (host_vm) {
     if (b->stage_n < n) {
       for (auto &p : b->stage) {
         cudaFree(p);

@@ -219,3 +219,27 @@ def test_surrogate_per_cell_stimulus(trained):
     st = both.run_surrogate(sur, v, n_macro, textbegin_per_cell=tbc, **kw)
     assert st["surrogate"] > 0.9 * 2 * n * n_macro
     np.testing.assert_allclose(v, np.concatenate(sep), rtol=0, atol=1e-9)
+
+
+def test_surrogate_host_vm_forms(trained):
+    """Vm in page-locked host memory (read and written by the library's kernels over the host
+    link), in pageable host memory (staged) and on the device give the same cells bit for bit."""
+    import torch
+    cm, p, sur, _ = trained
+    n, n_macro = 1000, 300
+    kw = dict(textbegin=0.0, textlen=1e-3, bcl=0.5, amplitude=AMP, audit_mod=0)
+    out = []
+    for form in ("device", "pinned", "pageable"):
+        b, _ = population(cm, p, n, seed=70)
+        v0 = b.init_vm()
+        if form == "device":
+            v = torch.tensor(v0, device="cuda")
+        elif form == "pinned":
+            v = torch.tensor(v0).pin_memory()
+        else:
+            v = v0
+        for k in range(3):  # three calls: the host copy must be current after each
+            t0 = k * n_macro * S * DT
+            b.run_surrogate(sur, v, n_macro, t0=t0, **dict(kw, textbegin=0.0))
+        out.append(v.cpu().numpy() if hasattr(v, "cpu") else v.copy())
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
