@@ -505,7 +505,7 @@ MULTI_KERNELS = ["multi_kernel<256>", "multi_kernel<128>", "multi_kernel<512>", 
 BATCHED_BYTES = {"TenTusscher2": 2 * 21 * 4 + 2 * 8, "CourtemancheEtAl": 2 * 25 * 4 + 2 * 8}
 
 
-def batched_leg(cm, torch, stream, steps, warmup, hbm_peak, peak_kind, n_inst=256):
+def batched_leg(cm, torch, stream, steps, warmup, hbm_peak, peak_kind, n_inst=256, launch=None):
     """Batched form: 256 instances (log-uniform 1k..1M cells, ten Tusscher 2006 or Courtemanche
     1998, own parameter set with six conductances x U[0.8, 1.2], stimulus phase U[0, BCL)),
     advanced in lock step by one persistent launch per step, replayed from a CUDA graph, launch
@@ -524,7 +524,12 @@ def batched_leg(cm, torch, stream, steps, warmup, hbm_peak, peak_kind, n_inst=25
         stims.append({"textbegin": d["phase"] * BATCHED_BCL, "textlen": 1e-3 if tt2 else 2e-3, "bcl": BATCHED_BCL,
                       "amplitude": W.TT2_STIM_NA if tt2 else W.CRN_STIM_PAPF})
     multi = cm.Multi(batches, stream=stream.cuda_stream)
-    tuned = multi.autotune(5)
+    if launch:  # tile_cells,shape,blocks_per_sm (profiler captures)
+        tc, sh, bps = (int(x) for x in launch.split(","))
+        multi.set_launch(tc, sh, bps)
+        tuned = {"tile_cells": tc, "shape": sh, "blocks_per_sm": bps, "ms_per_step": None}
+    else:
+        tuned = multi.autotune(5)
     multi.run(vms, warmup, [dict(s, t0=0.0) for s in stims])
     timed = []
     for s in stims:
@@ -875,6 +880,8 @@ def main():
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--multi-launch", default=None,
+                    help="fixed batched launch 'tile_cells,shape,blocks_per_sm' (skips tuning; captures)")
     ap.add_argument("--batched-steps", type=int, default=640, help="timed steps of the batched form")
     ap.add_argument("--batched-instances", type=int, default=256,
                     help="instances of the batched form (fewer only for profiler captures)")
@@ -912,7 +919,7 @@ def main():
 
     if args.only == "batched":
         print(json.dumps(batched_leg(cm, torch, stream, args.batched_steps, 32, hbm_peak, peak_kind,
-                                     args.batched_instances)), flush=True)
+                                     args.batched_instances, args.multi_launch)), flush=True)
         return
     if args.only == "fp64":
         _, b64 = make_batch(cm, cm.FP64, stream.cuda_stream)
