@@ -1,5 +1,5 @@
 // Pipe-peak measurement kernels: the FP64 plain kernels are bound by the FP64 pipe, whose
-// GB300 rate is not in the driver's measured peaks. Each thread runs 8 independent FMA
+// GB300 rate the measured copy-bandwidth and GEMM peaks do not give. Each thread runs 8 independent FMA
 // chains (enough to cover the pipe latency at full occupancy); the result is written so the
 // chains are not dead code.
 #include <cuda_bf16.h>
