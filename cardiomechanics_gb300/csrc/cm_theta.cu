@@ -19,12 +19,21 @@ namespace cm {
 
 namespace {
 
+// Resident blocks per SM: 3 (80 registers) measured 2-3 % faster per step than 4 (64 registers,
+// spills in the iteration kernels), 6 and 8 15-30 % slower (the entry rounds spill).
+#ifndef CM_THETA_BLOCKS_PER_SM
+#define CM_THETA_BLOCKS_PER_SM 3
+#endif
+#ifndef CM_THETA_ROUND
+#define CM_THETA_ROUND 8
+#endif
 constexpr int kThetaThreads = 256;
+constexpr int kThetaBlocks = CM_THETA_BLOCKS_PER_SM;  // resident blocks per SM (register budget)
 
 // Row l of a sliced operator times x, entries added in CSR order. The entries are fetched in
 // rounds of kRound (all columns and values, then all gathered x), so a row of 27 entries costs
 // about eight memory latencies rather than 54.
-constexpr int kRound = 8;
+constexpr int kRound = CM_THETA_ROUND;
 __device__ __forceinline__ double sell_row(const ThetaOp &A, const double *x, int64_t l) {
   const int64_t s = l >> 5;
   const int64_t e1 = A.ptr[s + 1];
@@ -100,7 +109,7 @@ __device__ __forceinline__ void totals(const double *const (&src)[N], int G, dou
 }
 
 // r = R x - A x, z = D^-1 r, p = z; partials ||D^-1 R x||^2, r.z, z.z
-__global__ void __launch_bounds__(kThetaThreads, 4) theta_init_kernel(ThetaOp A, ThetaOp R, ThetaVecs v, ThetaPart P) {
+__global__ void __launch_bounds__(kThetaThreads, kThetaBlocks) theta_init_kernel(ThetaOp A, ThetaOp R, ThetaVecs v, ThetaPart P) {
   double acc[3] = {0.0, 0.0, 0.0};
   for (int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; l < A.n; l += (int64_t)gridDim.x * blockDim.x) {
     const double b = sell_row(R, v.x, l);
@@ -120,7 +129,7 @@ __global__ void __launch_bounds__(kThetaThreads, 4) theta_init_kernel(ThetaOp A,
 }
 
 // q = A z (p = z); partial p.q; the test on the initial residual
-__global__ void __launch_bounds__(kThetaThreads, 4) theta_q0_kernel(ThetaOp A, ThetaVecs v, ThetaPart P, ThetaCfg cfg,
+__global__ void __launch_bounds__(kThetaThreads, kThetaBlocks) theta_q0_kernel(ThetaOp A, ThetaVecs v, ThetaPart P, ThetaCfg cfg,
                                                                  ThetaStat *st) {
   const double *const src[2] = {P.bb, P.zz + P.G};
   double tot[2];
@@ -149,7 +158,7 @@ __global__ void __launch_bounds__(kThetaThreads, 4) theta_q0_kernel(ThetaOp A, T
 // iteration k, kernel a. k comes from st->kb, which only the previous kernel b writes; block 0
 // passes it on in st->ka, which only the next kernel b reads (a block never reads a word that
 // another block of the same launch writes).
-__global__ void __launch_bounds__(kThetaThreads, 4) theta_a_kernel(ThetaVecs v, ThetaPart P, ThetaStat *st, int64_t n) {
+__global__ void __launch_bounds__(kThetaThreads, kThetaBlocks) theta_a_kernel(ThetaVecs v, ThetaPart P, ThetaStat *st, int64_t n) {
   if (st->done) return;
   const int k = st->kb;
   if (blockIdx.x == 0 && threadIdx.x == 0) st->ka = k;
@@ -202,7 +211,7 @@ __global__ void __launch_bounds__(kThetaThreads, 4) theta_a_kernel(ThetaVecs v, 
 
 // iteration k, kernel b: the test, and the end of the loop of a conditional graph node (h != 0)
 // when the solve converged, diverged, broke down or reached max_iter
-__global__ void __launch_bounds__(kThetaThreads, 4) theta_b_kernel(ThetaOp A, ThetaVecs v, ThetaPart P, ThetaCfg cfg,
+__global__ void __launch_bounds__(kThetaThreads, kThetaBlocks) theta_b_kernel(ThetaOp A, ThetaVecs v, ThetaPart P, ThetaCfg cfg,
                                                                 ThetaStat *st, int max_iter,
                                                                 cudaGraphConditionalHandle h) {
   if (st->done) {
@@ -284,7 +293,7 @@ __global__ void theta_dinv_kernel(ThetaOp A, double *dinv, int *bad) {
 
 }  // namespace
 
-int theta_grid() { return sm_count() * 4; }
+int theta_grid() { return sm_count() * kThetaBlocks; }
 
 cudaError_t launch_theta_dinv(const ThetaOp &A, double *dinv, int *bad, cudaStream_t s) {
   if (A.n == 0) return cudaSuccess;
