@@ -49,6 +49,7 @@ ABI_SYMBOLS = (
     "cm_batch_step_update_act",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
+    "cm_diag_mlp_workspace_rows",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
     "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
     "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
@@ -57,7 +58,7 @@ ABI_SYMBOLS = (
     "cm_batch_run_surrogate", "cm_mlp_forward_static", "cm_surrogate_flush_audit",
     "cm_diffusion_create", "cm_diffusion_destroy", "cm_diffusion_apply", "cm_batch_run_diffuse",
     "cm_backup_write", "cm_backup_read", "cm_theta_create", "cm_theta_destroy", "cm_theta_solve",
-    "cm_batch_run_theta",
+    "cm_batch_run_theta", "cm_surrogate_reset_network",
 )
 
 
@@ -173,6 +174,7 @@ def lib() -> ctypes.CDLL:
     L.cm_surrogate_generate.argtypes = [vp, vp, vp, i64, ctypes.POINTER(Stimulus), i64, i64, ctypes.POINTER(i64)]
     L.cm_surrogate_dataset.argtypes = [vp, ctypes.POINTER(i64), vp, vp]
     L.cm_surrogate_fit.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint64, fp]
+    L.cm_surrogate_reset_network.argtypes = [vp, ctypes.c_uint64]
     L.cm_surrogate_blob_size.argtypes = [vp]
     L.cm_surrogate_blob_size.restype = ctypes.c_int64
     L.cm_surrogate_get_blob.argtypes = [vp, vp]
@@ -181,6 +183,7 @@ def lib() -> ctypes.CDLL:
                                          ctypes.POINTER(SurrogateStats)]
     L.cm_diag_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), vp]
     L.cm_diag_umma_tile.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
+    L.cm_diag_mlp_workspace_rows.argtypes = [vp, ctypes.POINTER(i64)]
     _lib = L
     return L
 
@@ -679,6 +682,10 @@ class Surrogate:
         loss = ctypes.c_float()
         _check(lib().cm_surrogate_fit(self._h, batch, steps, lr, seed, ctypes.byref(loss)))
         return loss.value
+
+    def reset_network(self, seed):
+        """Fresh network weights from seed, optimiser state cleared; the dataset is kept."""
+        _check(lib().cm_surrogate_reset_network(self._h, int(seed)))
 
     def flush_audit(self, mode=0):
         """Audit the last run's pending sample now; returns its statistics."""

@@ -19,7 +19,7 @@ LIB = OUT / "libcmgb300.so"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["cm_kernels.cu", "cm_staged.cu", "cm_multi.cu", "cm_capi.cpp", "cm_params.cpp", "cm_diag.cu", "cm_mlp.cu", "cm_surrogate.cu", "cm_sur_api.cpp", "cm_noalloc.cu", "cm_diffusion.cpp", "cm_backup.cpp", "cm_theta.cu", "cm_theta_api.cpp"]
+SOURCES = ["cm_kernels.cu", "cm_staged.cu", "cm_multi.cu", "cm_capi.cpp", "cm_params.cpp", "cm_diag.cu", "cm_mlp.cu", "cm_surrogate.cu", "cm_sur_api.cpp", "cm_noalloc.cu", "cm_diffusion.cpp", "cm_backup.cpp", "cm_theta.cu", "cm_theta_api.cpp", "cm_print.cpp"]
 
 
 def _compile(src: str, extra: list[str]) -> Path:

@@ -467,6 +467,106 @@ int cm_batch_set_state(cm_batch_t b, int layout, const double *buf) {
   return soa_to_device(b, soa);
 }
 
+int cm_batch_get_cell(cm_batch_t b, int64_t cell, int layout, double *out) {
+  if (!b || !out) return fail(CM_ERR_ARG, "NULL argument");
+  if (layout != CM_LAYOUT_SOA && layout != CM_LAYOUT_REF_BLOCK) return fail(CM_ERR_ARG, "unknown layout");
+  if (cell < 0 || cell >= b->d.n) return fail(CM_ERR_ARG, "cell index out of range");
+  const int ns = b->ps.spec->n_state, nb = b->ps.spec->ref_block_doubles;
+  const int64_t ld = b->d.ld;
+  CK(cudaStreamSynchronize(b->stream));
+  // the cell's column of every state plane in one strided copy
+  std::vector<double> soa(ns);
+  if (b->d.precision == CM_PREC_FP64) {
+    CK(cudaMemcpy2D(soa.data(), sizeof(double), b->d.s64 + cell, ld * sizeof(double), sizeof(double), ns,
+                    cudaMemcpyDeviceToHost));
+  } else {
+    const int nw = n_fp32_vars(b->d.model);
+    std::vector<float> w(nw);
+    CK(cudaMemcpy2D(w.data(), sizeof(float), b->d.s32 + cell, ld * sizeof(float), sizeof(float), nw,
+                    cudaMemcpyDeviceToHost));
+    for (int k = 0; k < ns; k++) {
+      bool pair;
+      int slot;
+      mixed_slot(b->d.model, k, pair, slot);
+      soa[k] = pair ? acc_to_double(Acc{w[slot], w[slot + 1]}) : (double)w[slot];
+    }
+  }
+  if (layout == CM_LAYOUT_SOA) {
+    memcpy(out, soa.data(), ns * sizeof(double));
+    return CM_OK;
+  }
+  std::fill(out, out + nb, 0.0);
+  for (int k = 0; k < ns; k++) out[ref_block_index(b->d.model, k)] = soa[k];
+  if (b->diag) {
+    const int nd = diag_count(b->d.model);
+    std::vector<double> dg(nd);
+    CK(cudaMemcpy2D(dg.data(), sizeof(double), b->diag + cell, ld * sizeof(double), sizeof(double), nd,
+                    cudaMemcpyDeviceToHost));
+    for (int k = 0; k < nd; k++) out[diag_block_pos(b->d.model, k)] = dg[k];
+  }
+  return CM_OK;
+}
+
+int cm_batch_set_cell(cm_batch_t b, int64_t cell, int layout, const double *in) {
+  if (!b || !in) return fail(CM_ERR_ARG, "NULL argument");
+  if (layout != CM_LAYOUT_SOA && layout != CM_LAYOUT_REF_BLOCK) return fail(CM_ERR_ARG, "unknown layout");
+  if (cell < 0 || cell >= b->d.n) return fail(CM_ERR_ARG, "cell index out of range");
+  const int ns = b->ps.spec->n_state;
+  const int64_t ld = b->d.ld;
+  std::vector<double> soa(ns);
+  for (int k = 0; k < ns; k++) soa[k] = layout == CM_LAYOUT_SOA ? in[k] : in[ref_block_index(b->d.model, k)];
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->d.precision == CM_PREC_FP64) {
+    CK(cudaMemcpy2D(b->d.s64 + cell, ld * sizeof(double), soa.data(), sizeof(double), sizeof(double), ns,
+                    cudaMemcpyHostToDevice));
+    return CM_OK;
+  }
+  const int nw = n_fp32_vars(b->d.model);
+  std::vector<float> w(nw, 0.f);
+  for (int k = 0; k < ns; k++) {
+    bool pair;
+    int slot;
+    mixed_slot(b->d.model, k, pair, slot);
+    const Acc a = acc_from_double(soa[k]);
+    w[slot] = pair ? a.hi : (float)soa[k];
+    if (pair) w[slot + 1] = a.lo;
+  }
+  CK(cudaMemcpy2D(b->d.s32 + cell, ld * sizeof(float), w.data(), sizeof(float), sizeof(float), nw,
+                  cudaMemcpyHostToDevice));
+  return CM_OK;
+}
+
+int cm_batch_calc_cell(cm_batch_t b, int64_t cell, double dt, double V, double i_ext, double stretch, double *dV) {
+  if (!b || !dV) return fail(CM_ERR_ARG, "NULL argument");
+  if (cell < 0 || cell >= b->d.n) return fail(CM_ERR_ARG, "cell index out of range");
+  if (dt != b->ps.dt)
+    return fail(CM_ERR_ARG, "dt differs from the parameter set's dt (" + std::to_string(b->ps.dt) +
+                                "): the lookup tables depend on dt; create a parameter set for this dt");
+  int rc;
+  if ((rc = ensure_stage(b, 4))) return rc;
+  // the batch seen from this cell: every per-cell plane starts at the cell, one cell long
+  DevBatch d = b->d;
+  d.n = 1;
+  const size_t het_word = d.precision == CM_PREC_FP64 ? sizeof(double) : sizeof(float);
+  if (d.s64) d.s64 += cell;
+  if (d.s32) d.s32 += cell;
+  for (auto &h : d.het)
+    if (h) h = (const char *)h + cell * het_word;
+  if (d.audit_cell) d.audit_cell += cell;
+  if (d.diag) d.diag += cell;
+  const double io_in[3] = {V, i_ext, stretch};
+  CK(cudaMemcpyAsync(b->stage[0], io_in, sizeof(io_in), cudaMemcpyHostToDevice, b->stream));
+  StepIO io;
+  io.vm = b->stage[0];
+  io.iext = b->stage[0] + 1;
+  io.stretch = b->stage[0] + 2;
+  io.dvm = b->stage[0] + 3;
+  CK(launch_step(d, io, 0, 0, b->stream));
+  CK(cudaMemcpyAsync(dV, b->stage[0] + 3, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return CM_OK;
+}
+
 int cm_batch_step(cm_batch_t b, double dt, const double *Vm, const double *i_ext, const double *stretch, double *dVm) {
   if (!b || !Vm || !dVm) return fail(CM_ERR_ARG, "NULL argument");
   if (dt != b->ps.dt)

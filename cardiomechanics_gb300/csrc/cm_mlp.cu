@@ -153,9 +153,12 @@ __global__ void transpose_bf16(const __nv_bfloat16 *__restrict__ in, __nv_bfloat
   }
 }
 
-// dY = 2 (Y - T) / (n * n_out) on the real outputs (padding columns and rows masked), loss sum.
+// dY = 2 (Y - T) / (n * n_out) on the real outputs (padding columns and rows masked); each
+// block's share of the loss goes to loss_part[block] (summed in block order by mse_total, so the
+// reported loss is the same on every run).
+constexpr int kMseBlocks = 256;
 __global__ void mse_grad(const float *__restrict__ Y, const float *__restrict__ T, int n, int n_real_rows, int n_out,
-                         int ldy, __nv_bfloat16 *__restrict__ dY, float *loss) {
+                         int ldy, __nv_bfloat16 *__restrict__ dY, float *loss_part) {
   __shared__ float red[256];
   float s = 0.f;
   const float scale = 2.f / ((float)n_real_rows * (float)n_out);
@@ -174,7 +177,14 @@ __global__ void mse_grad(const float *__restrict__ Y, const float *__restrict__ 
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(loss, red[0] / ((float)n_real_rows * (float)n_out));
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0] / ((float)n_real_rows * (float)n_out);
+}
+
+__global__ void mse_total(float *__restrict__ loss_part, int n_part, float *__restrict__ loss) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float s = 0.f;
+  for (int i = 0; i < n_part; i++) s += loss_part[i];
+  *loss = s;
 }
 
 // db[c] = sum_r dZ[r][c]
@@ -271,7 +281,11 @@ cudaError_t Mlp::init(int n_in_, int n_hidden_, int n_out_, uint64_t seed, cudaS
   MCK(cudaMalloc(&m2, n_params * sizeof(float)));
   MCK(cudaMalloc(&wb, n_params * sizeof(__nv_bfloat16)));
   MCK(cudaMalloc(&wt, n_params * sizeof(__nv_bfloat16)));
-  MCK(cudaMalloc(&loss, sizeof(float)));
+  MCK(cudaMalloc(&loss, (1 + kMseBlocks) * sizeof(float)));
+  return reset(seed);
+}
+
+cudaError_t Mlp::reset(uint64_t seed) {
   MCK(cudaMemsetAsync(m1, 0, n_params * sizeof(float), stream));
   MCK(cudaMemsetAsync(m2, 0, n_params * sizeof(float), stream));
   // Glorot-uniform weights from a counter-based generator, zero biases; padded rows/cols zero
@@ -415,8 +429,9 @@ cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
   pack_inputs<<<1024, 256, 0, stream>>>(X, (int)n, n_in, rows, in_pad, B.X);
   MCK(cudaGetLastError());
   MCK(forward_rows(B, rows));
-  MCK(cudaMemsetAsync(loss, 0, sizeof(float), stream));
-  mse_grad<<<256, 256, 0, stream>>>(B.Y, T, rows, (int)n, n_out, out_pad, B.dY, loss);
+  mse_grad<<<kMseBlocks, 256, 0, stream>>>(B.Y, T, rows, (int)n, n_out, out_pad, B.dY, loss + 1);
+  MCK(cudaGetLastError());
+  mse_total<<<1, 32, 0, stream>>>(loss + 1, kMseBlocks, loss);
   MCK(cudaGetLastError());
   // dZ2 = (dY W3) * (1 - H2^2): A = dY (rows x out_pad), B-operand rows = W3^T (H x out_pad)
   EpiArgs e{};

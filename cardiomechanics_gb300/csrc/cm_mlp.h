@@ -27,6 +27,8 @@ struct Mlp {
   };
 
   cudaError_t init(int n_in, int n_hidden, int n_out, uint64_t seed, cudaStream_t s);
+  // fresh Glorot-uniform weights from seed, zero biases, optimiser state cleared
+  cudaError_t reset(uint64_t seed);
   void release();
   cudaError_t sync_bf16();  // after host-side weight changes
   // X: n x n_in (device, FP32); Y: n x n_out (device, FP32)

@@ -17,6 +17,7 @@ using namespace cm;
 
 struct cm_mlp_s {
   Mlp m;
+  int device = -1;  // the device the network's memory lives on (current at creation)
 };
 
 struct cm_surrogate_s {
@@ -38,6 +39,7 @@ struct cm_surrogate_s {
   // generation scratch
   float *gX = nullptr, *gC = nullptr, *gOld = nullptr, *gT = nullptr;
   uint8_t *gkeep = nullptr;
+  int64_t *gchunk = nullptr;  // per-chunk counts, then offsets, of the ordered append
   int64_t gcap = 0;
   // run scratch
   int *fallback = nullptr;
@@ -227,7 +229,8 @@ int cm_mlp_create(cm_mlp_t *out, int n_in, int n_hidden, int n_out, uint64_t see
   *out = nullptr;
   auto *m = new (std::nothrow) cm_mlp_s();
   if (!m) return fail(CM_ERR_NOMEM, "host allocation failed");
-  cudaError_t e = m->m.init(n_in, n_hidden, n_out, seed, (cudaStream_t)stream);
+  cudaError_t e = cudaGetDevice(&m->device);
+  if (e == cudaSuccess) e = m->m.init(n_in, n_hidden, n_out, seed, (cudaStream_t)stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) {
     m->m.release();
@@ -335,7 +338,7 @@ int cm_surrogate_destroy(cm_surrogate_t s) {
   s->net.m.release();
   for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
                   (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
-                  (void *)s->gkeep, (void *)s->fallback, (void *)s->snap, (void *)s->n_snap, (void *)s->n_fallback,
+                  (void *)s->gkeep, (void *)s->gchunk, (void *)s->fallback, (void *)s->snap, (void *)s->n_snap, (void *)s->n_fallback,
                   (void *)s->totals,
                   (void *)s->audit_err, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block,
                   (void *)s->rows_fine32, (void *)s->eca_fine32})
@@ -387,6 +390,7 @@ int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64
   if (e == cudaSuccess) e = cudaMalloc(&s->totals, 3 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&s->audit_err, sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->bias_block, 288 * sizeof(float));
+  if (e == cudaSuccess) e = cudaGetDevice(&s->net.device);
   if (e == cudaSuccess) e = s->net.m.init(kSurIn, kSurH, kSurOut, seed, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) rc = cuda_fail(e, "cm_surrogate_create");
@@ -399,6 +403,14 @@ int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64
     return rc;
   }
   *out = s;
+  return CM_OK;
+}
+
+int cm_surrogate_reset_network(cm_surrogate_t s, uint64_t seed) {
+  if (!s) return fail(CM_ERR_ARG, "NULL surrogate");
+  CK(s->net.m.reset(seed));
+  CK(cudaStreamSynchronize(s->stream));
+  s->fitted = false;
   return CM_OK;
 }
 
@@ -438,12 +450,14 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
     s->cap = max_pairs;
   }
   if (n_sample > s->gcap) {
-    for (void *p : {(void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT, (void *)s->gkeep}) cudaFree(p);
+    for (void *p : {(void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT, (void *)s->gkeep, (void *)s->gchunk})
+      cudaFree(p);
     CK(cudaMalloc(&s->gX, n_sample * kSurIn * sizeof(float)));
     CK(cudaMalloc(&s->gC, n_sample * kSurOut * sizeof(float)));
     CK(cudaMalloc(&s->gOld, n_sample * 8 * sizeof(float)));
     CK(cudaMalloc(&s->gT, n_sample * kSurOut * sizeof(float)));
     CK(cudaMalloc(&s->gkeep, n_sample));
+    CK(cudaMalloc(&s->gchunk, sur_append_scratch_words(n_sample) * sizeof(int64_t)));
     s->gcap = n_sample;
   }
   double *dvm;
@@ -495,7 +509,7 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
     pa.macro_ms = (float)(s->coarse_ps.dt * 1000.0);
     pa.stim_on = on ? 1 : 0;
     CK(launch_sur_post(pa, st));
-    CK(launch_sur_append(s->gX, s->gT, s->gkeep, n_sample, s->dX, s->dT, s->d_count, s->cap, st));
+    CK(launch_sur_append(s->gX, s->gT, s->gkeep, n_sample, s->dX, s->dT, s->d_count, s->cap, s->gchunk, st));
   }
   if ((rc = planes_out(b, Vm, dvm, host_vm, st))) return rc;
   unsigned long long have = 0;
@@ -816,6 +830,12 @@ int cm_mlp_forward_static(cm_mlp_t m, const float *X, int64_t n, float *Y) {
   if (n == 0) return CM_OK;
   if (!is_device_ptr(X) || !is_device_ptr(Y))
     return fail(CM_ERR_ARG, "cm_mlp_forward_static takes device arrays only (staging host arrays would allocate)");
+  // the scratch address is looked up for the current device: it must be the network's
+  int dev = -1;
+  CK(cudaGetDevice(&dev));
+  if (dev != m->device)
+    return fail(CM_ERR_ARG, "cm_mlp_forward_static: the current device (" + std::to_string(dev) +
+                                ") is not the one the network was created on (" + std::to_string(m->device) + ")");
   void *scratch = nullptr;
   size_t bytes = 0;
   CK(static_scratch(&scratch, &bytes));
@@ -826,6 +846,12 @@ int cm_mlp_forward_static(cm_mlp_t m, const float *X, int64_t n, float *Y) {
                                 " rows for this network)");
   CK(m->m.forward_in_scratch(scratch, X, n, Y));
   CK(cudaStreamSynchronize(m->m.stream));
+  return CM_OK;
+}
+
+int cm_diag_mlp_workspace_rows(void *m, int64_t *rows) {
+  if (!m || !rows) return fail(CM_ERR_ARG, "NULL argument");
+  *rows = ((cm_mlp_s *)m)->m.ws_rows;
   return CM_OK;
 }
 

@@ -264,16 +264,92 @@ __global__ void __launch_bounds__(128) sur_post_kernel(const SurPostArgs a) {
   }
 }
 
-// Appends the kept (feature, target) pairs of one generation step to the dataset.
-__global__ void sur_append_kernel(const float *__restrict__ X, const float *__restrict__ T,
-                                  const uint8_t *__restrict__ keep, int64_t n, float *__restrict__ dX,
-                                  float *__restrict__ dT, unsigned long long *count, int64_t cap) {
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    if (!keep[k]) continue;
-    const unsigned long long slot = atomicAdd(count, 1ull);
-    if ((int64_t)slot >= cap) continue;
-    for (int i = 0; i < kSurIn; i++) dX[slot * kSurIn + i] = X[k * kSurIn + i];
-    for (int i = 0; i < kSurOut; i++) dT[slot * kSurOut + i] = T[k * kSurOut + i];
+// Appends the kept (feature, target) pairs of one generation step to the dataset in sample
+// order, so the dataset (and the cut at its capacity) is the same on every run: pass 1 counts the
+// kept pairs of each chunk of kAppendChunk samples, pass 2 (one block) turns the counts into
+// dataset offsets after the pairs already held, pass 3 writes each chunk's pairs at its offset.
+constexpr int kAppendThreads = 128, kAppendPer = 8, kAppendChunk = kAppendThreads * kAppendPer;
+
+__global__ void __launch_bounds__(kAppendThreads) sur_append_count_kernel(const uint8_t *__restrict__ keep, int64_t n,
+                                                                          int64_t *__restrict__ chunk_count) {
+  const int64_t n_chunks = (n + kAppendChunk - 1) / kAppendChunk;
+  for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+    int cnt = 0;
+    for (int i = threadIdx.x; i < kAppendChunk; i += kAppendThreads) {
+      const int64_t k = c * kAppendChunk + i;
+      cnt += (k < n && keep[k]) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    __shared__ int warp_cnt[kAppendThreads / 32];
+    if ((threadIdx.x & 31) == 0) warp_cnt[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < kAppendThreads / 32; w++) t += warp_cnt[w];
+      chunk_count[c] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// One block of 1024 threads: exclusive prefix sums of the chunk counts, offset by the pairs
+// the dataset already holds; the total is added to the dataset count.
+__global__ void __launch_bounds__(1024) sur_append_scan_kernel(int64_t *__restrict__ chunk_count, int64_t n_chunks,
+                                                               unsigned long long *count) {
+  __shared__ int64_t part[1024];
+  __shared__ int64_t base;
+  if (threadIdx.x == 0) base = (int64_t)*count;
+  __syncthreads();
+  for (int64_t c0 = 0; c0 < n_chunks; c0 += 1024) {
+    const int64_t c = c0 + threadIdx.x;
+    const int64_t v = c < n_chunks ? chunk_count[c] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+      const int64_t add = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (c < n_chunks) chunk_count[c] = base + part[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 0) base += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = (unsigned long long)base;
+}
+
+__global__ void __launch_bounds__(kAppendThreads) sur_append_kernel(
+    const float *__restrict__ X, const float *__restrict__ T, const uint8_t *__restrict__ keep, int64_t n,
+    const int64_t *__restrict__ chunk_offset, float *__restrict__ dX, float *__restrict__ dT, int64_t cap) {
+  __shared__ int warp_cnt[kAppendThreads / 32];
+  const int64_t n_chunks = (n + kAppendChunk - 1) / kAppendChunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+    // thread t owns samples [t * kAppendPer, (t + 1) * kAppendPer) of the chunk
+    const int64_t k0 = c * kAppendChunk + (int64_t)threadIdx.x * kAppendPer;
+    int mine = 0;
+    for (int i = 0; i < kAppendPer; i++) mine += (k0 + i < n && keep[k0 + i]) ? 1 : 0;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_cnt[warp] = incl;
+    __syncthreads();
+    int before = incl - mine;
+    for (int w = 0; w < warp; w++) before += warp_cnt[w];
+    int64_t slot = chunk_offset[c] + before;
+    for (int i = 0; i < kAppendPer; i++) {
+      const int64_t k = k0 + i;
+      if (k >= n || !keep[k]) continue;
+      if (slot < cap) {
+        for (int j = 0; j < kSurIn; j++) dX[slot * kSurIn + j] = X[k * kSurIn + j];
+        for (int j = 0; j < kSurOut; j++) dT[slot * kSurOut + j] = T[k * kSurOut + j];
+      }
+      slot++;
+    }
+    __syncthreads();
   }
 }
 
@@ -637,11 +713,16 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
 
 }  // namespace
 
+int64_t sur_append_scratch_words(int64_t n) { return (n + kAppendChunk - 1) / kAppendChunk; }
+
 cudaError_t launch_sur_append(const float *X, const float *T, const uint8_t *keep, int64_t n, float *dX, float *dT,
-                              unsigned long long *count, int64_t cap, cudaStream_t s) {
+                              unsigned long long *count, int64_t cap, int64_t *chunk_scratch, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int64_t g = (n + 127) / 128;
-  sur_append_kernel<<<(unsigned)(g < 4096 ? g : 4096), 128, 0, s>>>(X, T, keep, n, dX, dT, count, cap);
+  const int64_t n_chunks = sur_append_scratch_words(n);
+  const unsigned g = (unsigned)(n_chunks < 4096 ? n_chunks : 4096);
+  sur_append_count_kernel<<<g, kAppendThreads, 0, s>>>(keep, n, chunk_scratch);
+  sur_append_scan_kernel<<<1, 1024, 0, s>>>(chunk_scratch, n_chunks, count);
+  sur_append_kernel<<<g, kAppendThreads, 0, s>>>(X, T, keep, n, chunk_scratch, dX, dT, cap);
   return cudaGetLastError();
 }
 

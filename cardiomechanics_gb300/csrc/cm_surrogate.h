@@ -130,8 +130,10 @@ cudaError_t launch_sur_plain(const SurPlainArgs &a, int max_cells, cudaStream_t 
 cudaError_t launch_sur_audit(const SurAuditArgs &a, cudaStream_t s);
 cudaError_t launch_sur_gen(const SurGenArgs &a, cudaStream_t s);
 cudaError_t launch_sur_post(const SurPostArgs &a, cudaStream_t s);
+// Ordered append of the kept pairs; chunk_scratch holds sur_append_scratch_words(n) words.
+int64_t sur_append_scratch_words(int64_t n);
 cudaError_t launch_sur_append(const float *X, const float *T, const uint8_t *keep, int64_t n, float *dX, float *dT,
-                              unsigned long long *count, int64_t cap, cudaStream_t s);
+                              unsigned long long *count, int64_t cap, int64_t *chunk_scratch, cudaStream_t s);
 cudaError_t launch_sur_normalize(const float *X, const float *T, int64_t n, const SurNorm &norm, float *nX, float *nT,
                                  cudaStream_t s);
 

@@ -77,7 +77,12 @@ enum {
   CM_AUDIT_CARANGE = 4u,      /* [Ca]i index outside the ECa table (TT2): clamped */
   CM_AUDIT_GATE = 8u,         /* a gate left [0, 1] */
   CM_AUDIT_SURROGATE = 16u,   /* surrogate step rejected; plain integrator used */
-  CM_AUDIT_VMRANGE = 32u      /* |Vm| above the caller's vm_range after a fused update */
+  CM_AUDIT_VMRANGE = 32u,     /* |Vm| above the caller's vm_range after a fused update */
+  CM_AUDIT_TIMEOUT = 64u,     /* a bounded device wait (bulk copy, tensor-core completion) ran
+                                 out: the kernel left its remaining work undone and returned */
+  CM_AUDIT_STAGE = 128u,      /* batched launch: a staged descriptor was not its tile's
+                                 instance's; that sub-tile was skipped */
+  CM_AUDIT_TILE = 256u        /* batched launch: a sub-tile outside its instance; skipped */
 };
 
 typedef struct cm_params_s *cm_params_t;
@@ -162,6 +167,30 @@ int cm_batch_init_vm(cm_batch_t b, double *Vm);
  * n_state_vars) doubles. */
 int cm_batch_get_state(cm_batch_t b, int layout, double *buf);
 int cm_batch_set_state(cm_batch_t b, int layout, const double *buf);
+
+/* One cell of a batch, for per-node code written against vbElphyModel (the slow path; the
+ * C++ view in cardiomech_gb300_elphy.hpp is built on these three). */
+/* The cell's state as GetBase()/GetSize() hold it (CM_LAYOUT_REF_BLOCK: ref_block_doubles
+ * doubles, diagnostic slots as in cm_batch_get_state) or its n_state_vars values (SOA order).
+ * out: host memory. Replaces reading vbElphyModel::GetBase() (ElphyModelBasis.h:206-207). */
+int cm_batch_get_cell(cm_batch_t b, int64_t cell, int layout, double *out);
+/* Writes one cell's state from a block in the given layout (host memory): ReadStatus / Set
+ * into that cell (ElphyModelBasis.h:243-253). Diagnostic slots of a block are not read. */
+int cm_batch_set_cell(cm_batch_t b, int64_t cell, int layout, const double *in);
+/* One Calc of one cell, *dV = Calc(dt, V, i_ext, stretch, 1) (ElphyModelBasis.h:264), its
+ * state updated in place on the device: vbElphyModel::Calc for node `cell`. dt must equal the
+ * parameter set's dt. One launch and two small copies per call: use cm_batch_step for loops. */
+int cm_batch_calc_cell(cm_batch_t b, int64_t cell, double dt, double V, double i_ext, double stretch, double *dV);
+/* Column names after "t" and "V_m" of vbElphyModel::Print (long_form 0) or LongPrint (1), as
+ * GetParameterNames / GetLongParameterNames give them (TenTusscher2.cpp:959-999,
+ * CourtemancheEtAl.cpp:241-265). Returns the count; names (NULL: count only) receive static
+ * strings. TenTusscher2 and Courtemanche; other models give CM_ERR_UNSUPPORTED. */
+int cm_model_print_names(int model, int long_form, const char **names, int cap);
+/* The same columns' values for one cell at membrane voltage V [V] (Print: TenTusscher2.cpp:
+ * 908-957, CourtemancheEtAl.cpp:189-239), as the reference prints them after t and V. Stored
+ * currents (TT2 Array[0..16], Courtemanche I_SAC) are those of the last step of an FP64 batch
+ * with diagnostics on (cm_batch_set_diagnostics), else 0. Returns the count. */
+int cm_batch_print_values(cm_batch_t b, int64_t cell, double V, int long_form, double *values, int cap);
 
 /* One Calc for every cell: dVm[c] = Calc(dt, Vm[c], i_ext[c], stretch[c], 1), state updated
  * in place (acCELLerate.cpp:1757-1770). dt must equal the parameter set's dt (the tables
@@ -351,7 +380,10 @@ int cm_mlp_forward(cm_mlp_t m, const float *X, int64_t n, float *Y);
    (11,904 rows for the 22-128-128-19 surrogate network, in_pad = out_pad = 32); larger n is
    rejected with CM_ERR_ARG and a message giving the limit. Nothing in that array has to start
    at zero. The first call on a device (with that device current) looks the array's address up
-   and loads it there; make that first call before any stream capture. The array is shared by
+   and loads it there; make that first call before any stream capture. The looked-up address is
+   kept for the life of the process: it assumes the device's primary context lives as long as
+   the process (no cudaDeviceReset between calls). The current device must be the one the
+   network was created on; otherwise the call returns CM_ERR_ARG. The array is shared by
    every caller in the process: two calls that overlap in time, from two threads or on
    unordered streams, corrupt each other's results. Runs on the MLP's stream and returns after
    it has finished, like cm_mlp_forward. */
@@ -382,6 +414,10 @@ int cm_surrogate_mlp(cm_surrogate_t s, cm_mlp_t *mlp);
  * residual target; appends up to max_pairs pairs in total. n_pairs: pairs held afterwards. */
 int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_macro, const cm_stimulus *stim,
                           int64_t cell_stride, int64_t max_pairs, int64_t *n_pairs);
+/* Fresh network weights drawn from seed (Glorot-uniform, zero biases) and the optimiser state
+ * cleared; the training pairs are kept. Lets one dataset train several candidate networks
+ * (seeds) so that a caller keeps the one with the smallest error on held-out cells. */
+int cm_surrogate_reset_network(cm_surrogate_t s, uint64_t seed);
 /* Number of pairs held; X (n x 22) / T (n x 19) receive them when not NULL. */
 int cm_surrogate_dataset(cm_surrogate_t s, int64_t *n_pairs, float *X, float *T);
 /* Feature/target normalisation from the data, then `steps` Adam steps on minibatches. Then

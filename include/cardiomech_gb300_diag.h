@@ -3,6 +3,7 @@
  * pipe; this gives the measured denominator of their roofline. */
 #ifndef CARDIOMECH_GB300_DIAG_H
 #define CARDIOMECH_GB300_DIAG_H
+#include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -18,6 +19,10 @@ int cm_diag_fma_peak(int fp64, double *tflops, void *stream);
  * 128 x k and B n x k, row-major BF16 device arrays; D is 128 x n FP32 (device). n in {32, 64,
  * 128}, k in {32, 64, 128}. Checks the tensor-core path against a host product. */
 int cm_diag_umma_tile(const void *A, const void *B, int n, int k, float *D, void *stream);
+
+/* Rows of allocated workspace a network (cm_mlp_t) holds for its forward and training passes:
+ * lets a test see that an entry point which must not allocate left it unchanged. */
+int cm_diag_mlp_workspace_rows(void *mlp, int64_t *rows);
 
 #ifdef __cplusplus
 }

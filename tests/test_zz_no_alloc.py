@@ -13,6 +13,13 @@ def _err(L):
     return L.cm_last_error().decode()
 
 
+def _ws_rows(L, net):
+    import ctypes
+    rows = ctypes.c_int64(-1)
+    assert L.cm_diag_mlp_workspace_rows(net._h, ctypes.byref(rows)) == 0, _err(L)
+    return rows.value
+
+
 def test_static_forward_matches_forward_twice(gpu):
     import torch
     L = gpu.lib()
@@ -31,6 +38,8 @@ def test_static_forward_matches_forward_twice(gpu):
     n0, X0, _, Ys0 = cases[0]
     assert L.cm_mlp_forward_static(net._h, X0.data_ptr(), n0, Ys0[0].data_ptr()) == 0, _err(L)  # first use
     torch.cuda.synchronize()
+    ws0 = _ws_rows(L, net)
+    # device-wide free memory: a secondary check that assumes nothing else uses this GPU meanwhile
     free0, _ = torch.cuda.mem_get_info()
     for k, (n, X, Y_ref, Ys) in enumerate(cases):
         for j in range(2):  # two calls in a row
@@ -39,6 +48,8 @@ def test_static_forward_matches_forward_twice(gpu):
             assert L.cm_mlp_forward_static(net._h, X.data_ptr(), n, Ys[j].data_ptr()) == 0, _err(L)
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
+    # the network's own workspace did not grow (the primary check), nor did device memory in use
+    assert _ws_rows(L, net) == ws0, (ws0, _ws_rows(L, net))
     assert free1 == free0, (free0, free1)
     for n, X, Y_ref, Ys in cases:
         ref = Y_ref.cpu().numpy()
