@@ -57,9 +57,8 @@ MIXED_BYTES_PER_CELL_STEP = 2 * (15 * 4 + 3 * 8) + 2 * 8 + 3 * 4
 MIXED_KERNELS = ["tt2_mixed_kernel<256>", "tt2_mixed_kernel<128>", "tt2_mixed_kernel<256,3>",
                  "tt2_mixed_kernel<512>", "tt2_mixed_kernel<64>", "mixed_staged_kernel<5,256>",
                  "mixed_staged_kernel<5,128>", "mixed_pipe_kernel<5,256,2>", "mixed_pipe_kernel<5,128,3>"]
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu captures summarised in
-# profiles/mixed_staged_tt2_4M_cells.md (launch shape 6, grid mode 4) and
-# profiles/mixed_pipe_kernels.md (launch shape 7, grid mode 4), same workload.
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch on this workload, from ncu captures
+# (launch shape 6, grid mode 4 and launch shape 7, grid mode 4).
 MEASURED_TRAFFIC = {"mixed_staged_kernel<5,128>": 436_239_360 + 327_127_808,
                     "mixed_pipe_kernel<5,256,2>": 436_254_208 + 325_440_768}
 # tt2_fp64_kernel: 18 FP64 states r+w (288 B), Vm r+w (16 B), 3 FP64 conductances (24 B).
@@ -113,6 +112,13 @@ FULL_BCL = 0.5
 FULL_SEED = 31       # instance sizes and phases
 FULL_HET_SEED = 7    # per-cell conductances
 FULL_AUDIT_MOD = 100
+# Accuracy of the headline's own network: ACC_CELLS cells drawn from the headline population
+# (seed ACC_SEED) run by the learned step and by the oracle over ACC_T_END seconds (five beats
+# after every first stimulus), compared every macro step
+ACC_SEED = 53
+ACC_CELLS = 256
+ACC_T_END = 3.0
+ACC_BEATS = 5
 FULL_WORKLOAD = "tt2006-epi-full-form-16.7M-cells-64-instances"
 # Algorithmic bytes of one macro step: every cell's 21 state planes and Vm pair read and
 # written plus 3 conductances read by sur_step (196 B), and the listed cells' 10 plain fine
@@ -121,7 +127,7 @@ SUR_BYTES_PER_CELL = 2 * (21 * 4 + 2 * 4) + 3 * 4
 SUR_PLAIN_BYTES_PER_LISTED_CELL = 10 * SUR_BYTES_PER_CELL + 4
 # MLP FLOPs per cell of one macro step on the tensor core (padded shapes 32-128-128-32)
 SUR_MLP_FLOPS_PER_CELL = 2 * (128 * 32 + 128 * 128 + 32 * 128)
-# ncu (profiles/sur_step_tc_tt2_1M_cells.md): DRAM bytes of one macro-step launch over 1,048,576
+# ncu: DRAM bytes of one macro-step launch over 1,048,576
 # cells at steady state, scaled by cells
 SUR_STEP_TRAFFIC_PER_CELL = (110_488_832 + 37_235_712) / 1_048_576
 
@@ -234,10 +240,37 @@ def time_device_steps(torch, cm, b, stream, vm, steps, warmup, t0):
     return ev0.elapsed_time(ev1) / 1e3
 
 
+def headline_sample(k, seed=None):
+    """k distinct cells of the headline population (seeded draw over the 16,777,216), with their
+    conductance scales (3, k) and first stimulus times (their instance's phase x BCL)."""
+    from cardiomechanics_gb300 import workloads as W
+    seed = ACC_SEED if seed is None else seed
+    draw = (W.uniform(seed, np.arange(4 * k, dtype=np.uint64)) * FULL_CELLS).astype(np.int64)
+    idx = np.unique(draw)[:k]
+    inst = W.full_form_instances(FULL_SEED, FULL_INSTANCES, FULL_CELLS)
+    ends = np.cumsum([d["n"] for d in inst])
+    phases = np.array([inst[i]["phase"] for i in np.searchsorted(ends, idx, side="right")]) * FULL_BCL
+    sc = W.conductance_scales(FULL_HET_SEED, FULL_CELLS, 3, 0.85, 1.15, cells=idx)
+    return idx, sc, phases
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), for the baseline's description."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 class CPUSample:
     """The oracle (C restatement of the reference Calc, FP64: the reference's plain method) on a
-    bounded sample of the headline workload: its first `cells` cells (all in instance 0, with
-    that instance's stimulus phase), advanced `steps` time steps per call, all host threads."""
+    bounded sample of the headline workload: `cells` cells drawn from its 16,777,216 (seeded),
+    each with its own conductances and its instance's first stimulus time, all host threads."""
 
     def __init__(self, cells=4096, threads=None):
         import oracle as O
@@ -248,73 +281,101 @@ class CPUSample:
         self.cells = cells
         self.P = self.port.param_vector(O.TT2, O.load_params(O.TT2))
         self.T = self.port.tables(O.TT2, self.P, DT)
-        sc = W.conductance_scales(FULL_HET_SEED, FULL_CELLS, 3, 0.85, 1.15, cells=np.arange(cells))
-        self.tb = W.full_form_instances(FULL_SEED, FULL_INSTANCES, FULL_CELLS)[0]["phase"] * FULL_BCL
+        _, sc, self.tb = headline_sample(cells)
         names = self.port.param_names(O.TT2)
         self.het = {k: self.P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
         self.B = self.port.init_state(O.TT2, self.P, cells)
         self.vm = np.full(cells, self.port.init_vm(O.TT2, self.P))
         self.t = 0.0
 
-    def advance(self, steps):
-        """Advance the sample; returns elapsed seconds."""
+    def advance(self, steps, rows=None, rec_every=0):
+        """Advance the sample (or its rows `rows`) `steps` steps of the driver loop; returns
+        (elapsed seconds, Vm trace of the rows when rec_every > 0)."""
+        sl = slice(None) if rows is None else rows
+        B = np.ascontiguousarray(self.B[sl])
+        vm = np.ascontiguousarray(self.vm[sl])
+        tb = np.ascontiguousarray(self.tb[sl])
+        het = {k: np.ascontiguousarray(v[sl]) for k, v in self.het.items()}
         t0 = time.perf_counter()
-        self.port.run(self.O.TT2, self.P, self.T, self.B, self.vm, steps, DT, t0=self.t, textbegin=self.tb,
-                      textlen=1e-3, bcl=FULL_BCL, amp=self.W.TT2_STIM_NA, het=self.het, n_threads=self.threads)
-        self.t, self.tb = advance_protocol(self.t, self.tb, steps, FULL_BCL)
-        return time.perf_counter() - t0
+        tr = self.port.run(self.O.TT2, self.P, self.T, B, vm, steps, DT, t0=self.t, textlen=1e-3, bcl=FULL_BCL,
+                           amp=self.W.TT2_STIM_NA, het=het, textbegin_per_cell=tb, rec_every=rec_every,
+                           n_threads=self.threads)
+        el = time.perf_counter() - t0
+        self.B[sl], self.vm[sl] = B, vm
+        if rows is None:  # the driver's protocol state after these steps (the port only reads it)
+            t = self.t
+            for _ in range(steps):
+                adv = (t >= self.tb) & (t >= self.tb + 1e-3)
+                self.tb = np.where(adv, self.tb + FULL_BCL, self.tb)
+                t += DT
+            self.t = t
+        return el, tr
 
-    def describe(self, steps, seconds):
-        return {"unit": UNIT, "cores": self.threads, "kind": "port",
-                "sample": f"first {self.cells} of the {FULL_CELLS} cells x {steps} fine steps of 0.01 ms (oracle "
-                          f"C restatement of the reference Calc in FP64, {self.threads} threads, {seconds:.1f} s)"}
+    def describe(self, cell_steps, seconds, what):
+        return {"unit": UNIT, "cores": self.threads, "kind": "port", "cpu": cpu_model(),
+                "sample": f"{self.cells} of the {FULL_CELLS} headline cells (seeded draw, own conductances and "
+                          f"stimulus phases), {what}: {cell_steps:.3g} cell-steps of the oracle C restatement of "
+                          f"the reference Calc in FP64 on {self.threads} threads, {seconds:.1f} s"}
 
 
-def cpu_baseline(seconds=10.0, cells=4096):
-    """Oracle throughput on the host cores over about `seconds` of work; cell-steps/s."""
+def cpu_baseline(cells=4096):
+    """Oracle throughput on the host cores over the accuracy protocol (3.0 s simulated: five
+    beats after every first stimulus) for `cells` headline cells; the first ACC_CELLS of them
+    are recorded every macro step and returned as the FP64 reference of the accuracy check."""
     smp = CPUSample(cells)
-    done, el = 0, 0.0
-    while el < seconds:
-        el += smp.advance(500)
-        done += 500
-    d = smp.describe(done, el)
-    d["value"] = cells * done / el
-    return d
+    steps = int(round(ACC_T_END / DT))
+    el_a, traces = smp.advance(steps, rows=slice(0, ACC_CELLS), rec_every=SUR_SUBSTEPS)
+    el_b, _ = smp.advance(steps, rows=slice(ACC_CELLS, cells))
+    el = el_a + el_b
+    d = smp.describe(cells * steps, el, f"{ACC_T_END:.1f} s simulated")
+    d["value"] = cells * steps / el
+    return d, traces
 
 
 def run_reference(args):
     """The reference arm: the reference's CPU path (the oracle port of its Calc; the reference
-    sources are not on the GPU host) on all host cores. Each step advances the cell sample by a
-    chunk sized so that warmup + steps take about a minute and a half in total."""
+    sources are not on the GPU host) on all host cores, on the headline's config. One step
+    advances a sample of the headline cells by a chunk of fine steps sized so that warmup +
+    steps take about a minute and a half; ms_per_step is that step's own measured time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle as O
     O.build_port()
     smp = CPUSample(4096)
-    rate = smp.cells * 200 / smp.advance(200)  # calibration
+    el, _ = smp.advance(200)  # calibration
+    rate = smp.cells * 200 / el
     total = args.steps + args.warmup
     chunk = int(max(1, min(5000, rate * 90.0 / max(1, total) / smp.cells)))
     for _ in range(args.warmup):
         smp.advance(chunk)
-    times = [smp.advance(chunk) for _ in range(args.steps)]
+    times = [smp.advance(chunk)[0] for _ in range(args.steps)]
     v = float(np.median([smp.cells * chunk / t for t in times]))
-    cb = smp.describe(chunk * args.steps, float(sum(times)))
+    cb = smp.describe(smp.cells * chunk * args.steps, float(sum(times)), f"{chunk} fine steps per timed step")
     cb["value"] = v
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * FULL_CELLS * SUR_SUBSTEPS / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.median(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": FULL_WORKLOAD, "cells": FULL_CELLS, "dt_ms": DT * 1e3, "bcl_ms": FULL_BCL * 1e3,
-                       "method": "the reference's plain FP64 Rush-Larsen Calc (oracle restatement), all host cores",
-                       "note": f"CPU: each step advances a {smp.cells}-cell sample {chunk} fine steps; "
-                               f"ms_per_step is the time one step of all {FULL_CELLS} cells would take"},
+            "config": headline_config(world),
+            "method": "the reference's plain FP64 Rush-Larsen Calc (oracle restatement), all host cores",
+            "step": f"one step advances {smp.cells} headline cells by {chunk} fine steps of 0.01 ms",
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-SUR_CELLS = 1 << 20
-SUR_BCL = 0.5
-SUR_SUBSTEPS = 10
+def headline_config(world):
+    """The headline's `config` (the same dict on both arms)."""
+    from cardiomechanics_gb300 import workloads as W
+    sizes = np.array([d["n"] for d in W.full_form_instances(FULL_SEED, FULL_INSTANCES, FULL_CELLS)])
+    return {"workload": FULL_WORKLOAD, "cells": FULL_CELLS,
+            "instances": {"n": FULL_INSTANCES, "min_cells": int(sizes.min()), "max_cells": int(sizes.max())},
+            "model": "TenTusscher2 epi", "dt_ms": DT * 1e3, "macro_step_ms": SUR_SUBSTEPS * DT * 1e3,
+            "cell_steps_per_step": FULL_CELLS * SUR_SUBSTEPS, "bcl_ms": FULL_BCL * 1e3,
+            "stimulus": "-52 pA/pF x 1 ms, per-instance phase U[0, BCL)",
+            "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.85,1.15] per cell",
+            "method": "learned macro step (coarse step + 22-128-128-19 BF16 MLP on tcgen05), "
+                      "plain FP32 fallback, 1% FP64 audit",
+            "l2": "state ~2 GB > 129 MB L2 (no flush needed)", "parallelism": f"replicas{world}"}
 
 
 def advance_protocol(t, tb, n_fine, bcl, textlen=1e-3):
@@ -326,31 +387,18 @@ def advance_protocol(t, tb, n_fine, bcl, textlen=1e-3):
     return t, tb
 
 
-def train_surrogate(cm, stream, gen_frac=1.0):
-    """A surrogate trained here, untimed, on the plain integrator's trajectories: populations of
-    2048 jittered (+-15 %) cells paced at BCL 500, 800 and 1000 ms, every 4th cell sampled, up to
-    2e7 pairs; 6000 Adam steps at 1e-3 then 4000 at 3e-4."""
-    from cardiomechanics_gb300 import workloads as W
-    t0 = time.perf_counter()
+def train_surrogate(cm, stream, seeds=(1, 2, 3)):
+    """The surrogate used by the learned legs, trained here (untimed) on the plain integrator's
+    trajectories and selected on held-out cells (`learned.train_and_select`: one dataset,
+    one network per seed, three correction sets each, the candidate with the smallest trace error
+    against the FP64 kernel kept). Deterministic: the same seeds give the same network."""
+    from cardiomechanics_gb300 import learned as L
     p = cm.Params(cm.TENTUSSCHER2, None, DT)
     sur = cm.Surrogate(p, substeps=SUR_SUBSTEPS, seed=1, stream=stream.cuda_stream)
-    pairs = 0
-    for seed, bcl, beats in ((11, 0.5, 4), (12, 0.8, 3), (13, 1.0, 2)):  # three pacing rates
-        tb_ = cm.Batch(p, 2048, cm.MIXED, stream=stream.cuda_stream)
-        sc = W.conductance_scales(seed, 2048, 3, 0.85, 1.15)
-        for k, name in enumerate(W.TT2_HETERO):
-            tb_.add_hetero_value(name, p.get(name) * sc[k])
-        v = tb_.init_vm()
-        n_macro = max(1, int(round(beats * bcl / (SUR_SUBSTEPS * DT)) * gen_frac))
-        pairs = sur.generate(tb_, v, n_macro, textlen=1e-3, bcl=bcl, amplitude=W.TT2_STIM_NA, cell_stride=4,
-                             max_pairs=20_000_000)
-    sur.fit(batch=4096, steps=max(1, int(6000 * gen_frac)), lr=1e-3, seed=1)
-    loss = sur.fit(batch=8192, steps=max(1, int(4000 * gen_frac)), lr=3e-4, seed=2)
-    names = ["Vm", "m", "h", "j", "xr1", "xr2", "xs", "r", "s", "d", "f", "f2", "fCa", "Rq", "Ca_i", "CaSS", "CaSR",
-             "Na_i", "K_i"]
-    applied = sur.get_blob()[63:82]
-    return p, sur, {"pairs": pairs, "final_normalised_mse": loss, "seconds": time.perf_counter() - t0,
-                    "corrected_outputs": [nm for nm, a in zip(names, applied) if a > 0]}
+    rep = L.train_and_select(cm, p, sur, seeds=seeds, stream=stream)
+    applied = sur.get_blob()[L.APPLIED]
+    rep["corrected_outputs"] = [nm for nm, a in zip(L.OUTPUT_NAMES, applied) if a > 0]
+    return p, sur, rep
 
 
 def learned_leg(cm, torch, stream, p, sur, steps, warmup):
@@ -423,6 +471,17 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
         torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
     t = advance_protocol(t, 0.0, steps * SUR_SUBSTEPS, 1e9)[0]
+    # ---- the same window with the coarse step alone (the method without the network)
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    c0.record(stream)
+    stats_c = b.run_surrogate(sur, vm, steps, t0=t, textbegin_per_cell=tbc,
+                              **dict(kw, mode=cm.SUR_COARSE_ONLY | cm.SUR_AUDIT_FP64))
+    c1.record(stream)
+    torch.cuda.synchronize()
+    sec_c = c0.elapsed_time(c1) / 1e3
+    t = advance_protocol(t, 0.0, steps * SUR_SUBSTEPS, 1e9)[0]
     value = FULL_CELLS * SUR_SUBSTEPS * steps / sec
     ms = 1e3 * sec / steps
     listed = stats["fallback"] / max(1, steps)  # cells the plain integrator advanced per macro step
@@ -469,6 +528,18 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     del b64, v64
     torch.cuda.empty_cache()
     fp64_value = FULL_CELLS * fp64_steps / sec64
+
+    # ---- accuracy of this network on ACC_CELLS cells of this population (own conductances and
+    # phases), five beats, every macro step: learned step and coarse step alone; the FP64 kernel
+    # on the same cells (the oracle's traces come from the CPU leg)
+    from cardiomechanics_gb300 import learned as L
+    idx, _, ph = headline_sample(ACC_CELLS)
+    acc_tr, acc_stats = {}, {}
+    for name, mode in (("learned", cm.SUR_AUDIT_FP64), ("coarse_only", cm.SUR_COARSE_ONLY | cm.SUR_AUDIT_FP64)):
+        acc_tr[name], acc_stats[name] = L.surrogate_traces(cm, p, sur, ACC_CELLS, FULL_HET_SEED, ph, ACC_T_END, 1,
+                                                           mode, stream, cells=idx, audit_mod=FULL_AUDIT_MOD)
+    ref64 = L.fp64_traces(cm, p, ACC_CELLS, FULL_HET_SEED, ph, ACC_T_END, 1, stream, cells=idx)
+    vs_kernel = {k: L.trace_errors(v, ref64, ph, SUR_SUBSTEPS * DT, ACC_BEATS) for k, v in acc_tr.items()}
     return {
         "value": value, "seconds": sec, "ms_per_step": ms, "stats": stats, "clocks": clk.summary(),
         "roofline": {"bound": "hbm", "kernel": "sur_step_tc_kernel<4, audit> (4 groups; group 3 audits first)",
@@ -479,7 +550,7 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
                      "traffic_note": "ncu DRAM bytes of one 1,048,576-cell launch, scaled by cells",
                      "tensor": {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s", "frac": tflops / tpk,
                                 "peak_kind": tpk_kind, "flops_per_launch": FULL_CELLS * SUR_MLP_FLOPS_PER_CELL},
-                     "issue_bound": "see profiles/sur_step_tc_tt2_1M_cells.md"},
+                     "bound_note": "issue-bound: neither HBM nor the tensor pipe limits this kernel"},
         "sur_plain_kernel": {"ms_per_launch": ms_p, "listed_cells_per_launch": listed,
                              "algorithmic_bytes_per_launch": listed * SUR_PLAIN_BYTES_PER_LISTED_CELL},
         "e2e": {"value": FULL_CELLS * SUR_SUBSTEPS * e2e_steps / e2e_sec, "unit": UNIT,
@@ -492,6 +563,12 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
                        "bound": "fp64 pipe"},
         "gpu_launches": 2 * steps + 2,
         "instances": {"n": FULL_INSTANCES, "min_cells": int(sizes.min()), "max_cells": int(sizes.max())},
+        "fallback_fraction": stats["fallback"] / (FULL_CELLS * steps),
+        "coarse_only": {"value": FULL_CELLS * SUR_SUBSTEPS * steps / sec_c, "unit": UNIT, "ms_per_step": 1e3 * sec_c / steps,
+                        "fallback_fraction": stats_c["fallback"] / (FULL_CELLS * steps),
+                        "note": "the same timed window and cells with the coarse step alone (no network)"},
+        "accuracy_traces": acc_tr, "accuracy_stats": acc_stats, "accuracy_phases": ph,
+        "accuracy_vs_fp64_kernel": vs_kernel,
     }
 
 
@@ -870,7 +947,6 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--mixed-steps", type=int, default=2000, help="timed steps of the precision form")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
                     choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tomek", "tissue",
@@ -885,8 +961,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=640, help="timed steps of the batched form")
     ap.add_argument("--batched-instances", type=int, default=256,
                     help="instances of the batched form (fewer only for profiler captures)")
-    ap.add_argument("--sur-train-frac", type=float, default=1.0,
-                    help="fraction of the surrogate's training run (profiling captures only; accuracy needs 1)")
+    ap.add_argument("--sur-seeds", type=int, default=3,
+                    help="network seeds trained and compared on held-out cells (fewer only for captures)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
     ap.add_argument("--ord-steps", type=int, default=500,
                     help="timed steps of the O'Hara-Rudy and Tomek mixed forms")
@@ -940,7 +1016,7 @@ def main():
         print(json.dumps(ionic_leg(cm, torch, stream, args, hbm_peak, peak_kind, leg,
                                    cpu_seconds=0.0 if args.no_cpu else 5.0)), flush=True)
         return
-    p, sur, training = train_surrogate(cm, stream, args.sur_train_frac)
+    p, sur, training = train_surrogate(cm, stream, tuple(range(1, args.sur_seeds + 1)))
     if args.only == "surrogate":
         out = learned_leg(cm, torch, stream, p, sur, args.sur_steps, 20)
         out["training"] = training
@@ -959,7 +1035,9 @@ def main():
     value = world * FULL_CELLS * SUR_SUBSTEPS * args.steps / sec
     if args.only == "full":
         if rank == 0:
-            print(json.dumps(full), flush=True)
+            acc = headline_accuracy(full, None)
+            print(json.dumps({k: v for k, v in full.items() if not k.startswith("accuracy_")} | {"accuracy": acc}),
+                  flush=True)
         return
     fp32_peak = cm.fma_peak_tflops(False, stream.cuda_stream)
     fp64_peak = cm.fma_peak_tflops(True, stream.cuda_stream)
@@ -978,25 +1056,28 @@ def main():
         ionic[leg] = None if args.no_ord else ionic_leg(
             cm, torch, stream, args, hbm_peak, peak_kind, leg, fp64_peak,
             cpu_seconds=5.0 if (rank == 0 and not args.no_cpu) else 0.0)
-    cpu = None
+    cpu, oracle_traces = None, None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(seconds=args.cpu_seconds)
+        cpu, oracle_traces = cpu_baseline()
+    accuracy = headline_accuracy(full, oracle_traces)
 
     if rank == 0:
         fp64 = full["plain_fp64"]
         fp64["fp64_fma_peak_tflops_measured"] = fp64_peak
+        unmet = None if accuracy["pass"] else (
+            "the network of this run misses the accuracy bars on the headline's own cells: "
+            + json.dumps(accuracy["learned"]))
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": value if unmet is None else None, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16 (f64 audit)", "data": "synthetic",
-            "config": {"workload": FULL_WORKLOAD, "cells": FULL_CELLS, "instances": full["instances"],
-                       "model": "TenTusscher2 epi", "dt_ms": DT * 1e3, "macro_step_ms": SUR_SUBSTEPS * DT * 1e3,
-                       "cell_steps_per_step": FULL_CELLS * SUR_SUBSTEPS, "bcl_ms": FULL_BCL * 1e3,
-                       "stimulus": "-52 pA/pF x 1 ms, per-instance phase U[0, BCL)",
-                       "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.85,1.15] per cell",
-                       "method": "learned macro step (coarse step + 22-128-128-19 BF16 MLP on tcgen05), "
-                                 "plain FP32 fallback, 1% FP64 audit",
-                       "l2": "state ~2 GB > 129 MB L2 (no flush needed)", "parallelism": f"replicas{world}"},
+            "config": headline_config(world),
+            "accuracy": accuracy,
+            "value_if_accuracy_unmet": value if unmet is not None else None,
+            "value_unmet_reason": unmet,
+            "coarse_only": dict(full["coarse_only"], accuracy=accuracy["coarse_only"]),
+            "fallback_fraction": full["fallback_fraction"],
             "plain_fp64": fp64,
             "speedup_vs_plain_fp64": value / world / fp64["value"],
             "surrogate_stats": full["stats"],
@@ -1020,6 +1101,29 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def headline_accuracy(full, oracle_traces):
+    """Trace errors of the headline's network and of the coarse step alone on ACC_CELLS headline
+    cells: against the oracle (the FP64 restatement of the reference Calc run on the host cores)
+    when its traces exist, else against the FP64 kernel; the bars are APD90 <= 1 ms and RMS Vm
+    <= 0.5 mV."""
+    from cardiomechanics_gb300 import learned as L
+    ph = full["accuracy_phases"]
+    if oracle_traces is not None:
+        ref_name = "oracle (FP64 C restatement of the reference Calc, host cores)"
+        err = {k: L.trace_errors(v, oracle_traces, ph, SUR_SUBSTEPS * DT, ACC_BEATS)
+               for k, v in full["accuracy_traces"].items()}
+    else:
+        ref_name = "plain FP64 kernel"
+        err = full["accuracy_vs_fp64_kernel"]
+    ok = err["learned"]["apd90_max_ms"] <= L.APD_BAR_MS and err["learned"]["rms_vm_mv_max"] <= L.RMS_BAR_MV
+    return {"cells": ACC_CELLS, "beats": ACC_BEATS, "bcl_ms": FULL_BCL * 1e3, "t_end_s": ACC_T_END,
+            "sample_ms": SUR_SUBSTEPS * DT * 1e3, "reference": ref_name, "cells_from": "the headline population "
+            f"(seeded draw {ACC_SEED}, own conductances and phases)", "learned": err["learned"],
+            "coarse_only": err["coarse_only"], "vs_fp64_kernel": full["accuracy_vs_fp64_kernel"],
+            "learned_stats": full["accuracy_stats"]["learned"],
+            "bars": {"apd90_ms": L.APD_BAR_MS, "rms_vm_mv": L.RMS_BAR_MV}, "pass": bool(ok)}
 
 
 def cm_stim():

@@ -39,10 +39,10 @@ static __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// true when the phase with the given parity has completed; false after kSpinLimit polls
-static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// true when the phase with the given parity has completed; false after `limit` polls
+static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit = kSpinLimit) {
   const uint32_t a = smem_u32(bar);
-  for (uint32_t i = 0; i < kSpinLimit; i++) {
+  for (uint32_t i = 0; i < limit; i++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -467,6 +467,15 @@ int cm_batch_set_state(cm_batch_t b, int layout, const double *buf) {
   return soa_to_device(b, soa);
 }
 
+int cm_diag_batch_wait_check(void *batch, int64_t skip_tile, uint32_t spin_limit) {
+  cm_batch_t b = (cm_batch_t)batch;
+  if (!b) return fail(CM_ERR_ARG, "NULL batch");
+  if (skip_tile < -1) return fail(CM_ERR_ARG, "skip_tile: a tile index or -1");
+  b->d.fault_skip_tile = skip_tile;
+  b->d.spin_limit = spin_limit ? spin_limit : (1u << 26);
+  return CM_OK;
+}
+
 int cm_batch_get_cell(cm_batch_t b, int64_t cell, int layout, double *out) {
   if (!b || !out) return fail(CM_ERR_ARG, "NULL argument");
   if (layout != CM_LAYOUT_SOA && layout != CM_LAYOUT_REF_BLOCK) return fail(CM_ERR_ARG, "unknown layout");

@@ -33,6 +33,11 @@ struct alignas(16) DevBatch {
   unsigned int *audit_or = nullptr;
   double *diag = nullptr;  // FP64 only: TT2 and ORd 17 x ld diagnostic currents; CRN 1 x ld (I_SAC); Tomek 40 x ld
   int variant = 0, grid_mode = 0;  // launch shape chosen by cm_batch_autotune
+  // Bounded waits of the bulk-copy kernels: polls before a wait gives up (CM_AUDIT_TIMEOUT).
+  uint32_t spin_limit = 1u << 26;
+  // Test hook (cm_diag_batch_wait_check): the staged pipeline and the learned macro step issue
+  // no copy for this tile, so the wait for it runs out; -1: every tile is copied.
+  int64_t fault_skip_tile = -1;
   TT2Consts<double> tt2_64;
   TT2Consts<float> tt2_32;
   CRNConsts<double> crn_64;

@@ -139,13 +139,14 @@ __global__ void __launch_bounds__(kThreads + 32, 2) mixed_pipe_kernel(const DevB
     int it = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
       const int st = it % kStages;
-      if (it >= kStages && !mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1))) {
+      if (it >= kStages && !mbar_wait(&empty[st], (uint32_t)((it / kStages - 1) & 1), b.spin_limit)) {
         atomicOr(b.audit_or, kAuditTimeout);
         // the copies of the last kStages tiles may still be landing: wait for them, bounded
         for (int j = it - kStages; j < it; j++)
-          if (j >= 0) mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1));
+          if (j >= 0) mbar_wait(&full[j % kStages], (uint32_t)((j / kStages) & 1), b.spin_limit);
         return;
       }
+      if (t == b.fault_skip_tile) continue;  // test hook: this stage's copy is never issued
       asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
       float *dst = stage + st * buf_floats;
       const int64_t c0 = (int64_t)t * kThreads;
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(kThreads + 32, 2) mixed_pipe_kernel(const DevB
   int it = 0;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, it++) {
     const int st = it % kStages;
-    if (!mbar_wait(&full[st], (uint32_t)((it / kStages) & 1))) {
+    if (!mbar_wait(&full[st], (uint32_t)((it / kStages) & 1), b.spin_limit)) {
       atomicOr(b.audit_or, kAuditTimeout);
       return;
     }

@@ -462,11 +462,25 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   auto grab = [&]() -> int {  // the block's next tile (leader threads)
     return (int)blockIdx.x + atomicAdd(&s_next, 1) * (int)gridDim.x;
   };
-  auto issue = [&](int tile) {  // the tile's 21 state planes
+  // The tile's 21 state planes, issued by the group's first warp: lane 0 posts the byte count,
+  // then lane v copies plane v (one bulk copy per lane instead of 21 from one thread).
+  auto issue = [&](int tile) {
+    if (tile == fb.fault_skip_tile) return;  // test hook: this tile's copy is never issued
     const int64_t c0 = (int64_t)tile * kTcCells;
-    mbar_expect_tx(&bar_stage[g], (uint32_t)kTcStageVars * kTcCells * 4u);
-    for (int v = 0; v < kTcStageVars; v++)
-      bulk_g2s(stage + v * kTcCells, fb.s32 + v * ld + c0, kTcCells * 4u, &bar_stage[g]);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    if (lane == 0) mbar_expect_tx(&bar_stage[g], (uint32_t)kTcStageVars * kTcCells * 4u);
+    __syncwarp();
+    if (lane < kTcStageVars) bulk_g2s(stage + lane * kTcCells, fb.s32 + lane * ld + c0, kTcCells * 4u, &bar_stage[g]);
+  };
+  const bool issuer = (threadIdx.x & 127) < 32;  // the group's first warp
+  auto next_tile = [&]() {  // the issuing warp takes the group's next tile and starts its copies
+    int tn = 0;
+    if (lane == 0) {
+      tn = grab();
+      s_tile[g] = tn;
+    }
+    tn = __shfl_sync(0xffffffffu, tn, 0);
+    if (tn < n_tiles) issue(tn);
   };
   if (threadIdx.x == 0) s_next = 0;
   if (leader && g < kGroups) {
@@ -515,11 +529,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   if (kAudit && g == kGroups - 1) {  // the audit group: entries of the previous step's snapshot
     audit_range(prev, blockIdx.x * 128 + r, gridDim.x * 128);
   }
-  if (leader) {
-    const int t0 = grab();
-    s_tile[g] = t0;
-    if (t0 < n_tiles) issue(t0);
-  }
+  if (issuer) next_tile();
   group_sync(g);
   int t = s_tile[g];
   const float macro_ms = a.coarse.dt * 1000.f;
@@ -528,7 +538,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
   const uint32_t act_s = smem_u32(act), w1_s = smem_u32(W1), w2_s = smem_u32(W2), w3_s = smem_u32(W3);
   const uint32_t ones_s = smem_u32(ONES), b2_s = smem_u32(B2T);
   auto wait_mma = [&]() {
-    if (!mbar_wait(&bar_mma[g], pm)) {
+    if (!mbar_wait(&bar_mma[g], pm, fb.spin_limit)) {
       s_abort[g] = 1;
       atomicOr(fb.audit_or, kAuditTimeout);
     }
@@ -541,18 +551,28 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     group_sync(g);
   };
   while (t < n_tiles) {
-    if (!mbar_wait(&bar_stage[g], ps)) {
+    const int c = t * kTcCells + r;
+    const bool valid = c < n;
+    // loads that do not come through the stage go first: their latency overlaps the stage wait
+    Acc vm{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};  // c < ld: in the planes for padding cells too
+    const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
+    TT2Het_<float> g6;
+    g6.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
+    g6.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + cc) : C.g_Kr;
+    g6.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + cc) : C.g_K1;
+    g6.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + cc) : C.g_Ks;
+    g6.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + cc) : C.g_to;
+    g6.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + cc) : C.g_CaL;
+    if (!mbar_wait(&bar_stage[g], ps, fb.spin_limit)) {
       s_abort[g] = 1;
       atomicOr(fb.audit_or, kAuditTimeout);
     }
     ps ^= 1u;
     group_sync(g);
     if (s_abort[g]) {
-      mbar_wait(&bar_stage[g], ps ^ 1u);  // the copy that timed out: one more bounded wait
+      mbar_wait(&bar_stage[g], ps ^ 1u, fb.spin_limit);  // the copy that timed out: one more bounded wait
       break;
     }
-    const int c = t * kTcCells + r;
-    const bool valid = c < n;
     const float *S = stage + r;
     Cell q;
     q.x.m = S[0]; q.x.h = S[kTcCells]; q.x.j = S[2 * kTcCells]; q.x.xr1 = S[3 * kTcCells];
@@ -562,22 +582,10 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     q.CaSR = Acc{S[15 * kTcCells], S[16 * kTcCells]};
     q.Na = Acc{S[17 * kTcCells], S[18 * kTcCells]};
     q.K = Acc{S[19 * kTcCells], S[20 * kTcCells]};
-    Acc vm{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};  // c < ld: in the planes for padding cells too
-    const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
-    q.g.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
-    q.g.g_Kr = het[H2_g_Kr] ? __ldg(het[H2_g_Kr] + cc) : C.g_Kr;
-    q.g.g_K1 = het[H2_g_K1] ? __ldg(het[H2_g_K1] + cc) : C.g_K1;
-    q.g.g_Ks = het[H2_g_Ks] ? __ldg(het[H2_g_Ks] + cc) : C.g_Ks;
-    q.g.g_to = het[H2_g_to] ? __ldg(het[H2_g_to] + cc) : C.g_to;
-    q.g.g_CaL = het[H2_g_CaL] ? __ldg(het[H2_g_CaL] + cc) : C.g_CaL;
-    group_sync(g);  // the stage is free: the next tile's copies overlap this tile's work
-    if (leader) {
-      const int tn = grab();
-      s_tile[g] = tn;
-      if (tn < n_tiles) {
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        issue(tn);
-      }
+    q.g = g6;
+    if (!mlp_on) {  // the stage is free: the next tile's copies overlap this tile's work
+      group_sync(g);
+      if (issuer) next_tile();
     }
     if (mlp_on) {  // features of the initial state -> row r of the 128 x 32 input tile
       float f[kSurIn];
@@ -596,7 +604,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
 #pragma unroll
       for (int qd = 0; qd < 4; qd++)
         sts128(act + umma::kmajor_index(r, 8 * qd, 32), xb[4 * qd], xb[4 * qd + 1], xb[4 * qd + 2], xb[4 * qd + 3]);
-      operands_ready();
+      operands_ready();  // also: every thread has read its state from the stage
       if (leader) {  // layer 1: D = X W1^T (K = 32), computed while the coarse step runs
         umma::fence_after_sync();
         constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
@@ -605,6 +613,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
           umma::mma_bf16(tacc_mma, umma::smem_desc(act_s + s * 256u, 128u, 512u), umma::smem_desc(w1_s + s * 256u, 128u, 512u), id, s);
         umma::commit(&bar_mma[g]);
       }
+      if (issuer) next_tile();  // the stage is free: the next tile's copies overlap this tile's work
     }
     // coarse physics step (registers only)
     float oc[kSurOut], inc[4];

@@ -20,6 +20,15 @@ int cm_diag_fma_peak(int fp64, double *tflops, void *stream);
  * 128}, k in {32, 64, 128}. Checks the tensor-core path against a host product. */
 int cm_diag_umma_tile(const void *A, const void *B, int n, int k, float *D, void *stream);
 
+/* Test hook for the bounded waits (a cm_batch_t as `batch`): the batch's next launches of the
+ * staged pipeline (mixed batches, launch shapes 7 and 8) and of the learned macro step issue no
+ * bulk copy for tile skip_tile (-1: none), so the wait for that tile's data runs out, and every
+ * such wait gives up after spin_limit polls (0: the default, 2^26). A wait that runs out sets
+ * CM_AUDIT_TIMEOUT in the batch's audit mask; the kernel then waits (bounded) for the copies it
+ * did issue, frees what it holds and returns, leaving that tile's work undone. Nothing faults
+ * or hangs. Call with (-1, 0) to restore normal operation. */
+int cm_diag_batch_wait_check(void *batch, int64_t skip_tile, uint32_t spin_limit);
+
 /* Rows of allocated workspace a network (cm_mlp_t) holds for its forward and training passes:
  * lets a test see that an entry point which must not allocate left it unchanged. */
 int cm_diag_mlp_workspace_rows(void *mlp, int64_t *rows);

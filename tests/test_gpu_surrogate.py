@@ -1,14 +1,20 @@
-"""Learned macro step, end to end on the GPU: training pairs from the plain integrator, fit on
-the tensor cores, then a held-out population run with the surrogate against the FP64 oracle.
+"""Learned macro step, end to end on the GPU: training pairs from the plain integrator, networks
+fitted on the tensor cores for three seeds, the candidate with the smallest trace error on
+selection cells kept (`learned.train_and_select`), then held-out cells with per-cell stimulus
+phases run with the surrogate against the FP64 oracle.
 
-Bars (the benchmark spec): APD90 within 1 ms and RMS Vm within 0.5 mV of the FP64 oracle. The
-ablation shows what the network adds: the same run with the coarse step alone (the method
-without the network) must be less accurate."""
+Bars (the benchmark spec): APD90 within 1 ms and RMS Vm within 0.5 mV of the FP64 oracle. The gain is
+shown on whole traces: the same held-out cells run with the coarse step alone (the method
+without the network) are less accurate than with the selected network."""
+import hashlib
+import os
+
 import numpy as np
 import pytest
 
 import oracle as O
 from cardiomechanics_gb300 import analysis as A
+from cardiomechanics_gb300 import learned as L
 from cardiomechanics_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -33,22 +39,19 @@ def continued(t, tb, steps, bcl, textlen=1e-3):
     return t, tb
 
 
+def sha(blob):
+    return hashlib.sha256(np.ascontiguousarray(blob, np.float32).tobytes()).hexdigest()
+
+
 @pytest.fixture(scope="module")
 def trained(gpu):
     cm = gpu
     p = cm.Params(cm.TENTUSSCHER2, None, DT)
     sur = cm.Surrogate(p, substeps=S, seed=1)
-    # paced populations at three cycle lengths (4, 3 and 2 beats), every 4th cell sampled
-    n = 0
-    for seed, bcl, beats in ((11, 0.5, 4), (12, 0.8, 3), (13, 1.0, 2)):
-        b, _ = population(cm, p, 2048, seed=seed)
-        vm = b.init_vm()
-        n = sur.generate(b, vm, int(round(beats * bcl / (S * DT))), textlen=1e-3, bcl=bcl, amplitude=AMP,
-                         cell_stride=4, max_pairs=20_000_000)
-    assert n > 10_000_000
-    l1 = sur.fit(batch=4096, steps=6000, lr=1e-3, seed=1)
-    l2 = sur.fit(batch=8192, steps=4000, lr=3e-4, seed=2)
-    return cm, p, sur, (l1, l2)
+    rep = L.train_and_select(cm, p, sur, seeds=(1, 2, 3))
+    assert rep["pairs"] > 10_000_000
+    print("selected", rep["selected"], "coarse only", rep["coarse_only"])
+    return cm, p, sur, rep
 
 
 def run_traces(cm, b, sur, vm, n_macro, bcl, mode):
@@ -66,48 +69,54 @@ def run_traces(cm, b, sur, vm, n_macro, bcl, mode):
     return tr, stats
 
 
+def test_training_is_deterministic(trained):
+    """The same seed gives the same network: two fits on the dataset of this surrogate, and a fit
+    on a dataset generated again by another surrogate, give blobs with one sha256."""
+    cm, p, sur, rep = trained
+    selected = sur.get_blob()
+    seed = rep["selected"]["seed"]
+    L.fit(sur, seed)
+    a = sha(sur.get_blob())
+    L.fit(sur, seed)
+    b = sha(sur.get_blob())
+    other = cm.Surrogate(p, substeps=S, seed=1)
+    assert L.generate(cm, p, other) == rep["pairs"]
+    L.fit(other, seed)
+    c = sha(other.get_blob())
+    sur.set_blob(selected)
+    assert a == b == c
+
+
 def test_surrogate_accuracy_and_gain(trained, port):
-    cm, p, sur, losses = trained
-    # normalised MSE averaged over outputs; outputs the coarse step already gets exactly are
-    # FP32 round-off noise (MSE ~1 after normalisation), so only check that training converged
-    assert np.isfinite(losses[1]) and losses[1] < 0.6, losses
-    n, bcl, beats = 128, 0.8, 2
-    n_macro = int(round(beats * bcl / (S * DT)))
-    # held-out population (other seed)
-    b0, sc = population(cm, p, n, seed=99)
+    """Held-out cells (their own conductances and per-cell stimulus phases in [0, BCL)), five
+    beats at BCL 500 ms from the initial state, FP64 audit on: the selected network meets both
+    bars against the FP64 oracle, and its largest APD90 and RMS Vm errors are below those of the
+    coarse step alone on the same cells."""
+    cm, p, sur, rep = trained
+    n, beats, t_end = 256, 5, 3.0
+    het_seed = 99
+    ph = W.uniform(98, np.arange(n, dtype=np.uint64)) * L.BCL
     names = port.param_names(O.TT2)
     P = port.param_vector(O.TT2, O.load_params(O.TT2))
+    sc = W.conductance_scales(het_seed, n, 3, 0.85, 1.15)
     het = {k: P[names.index(k)] * sc[i] for i, k in enumerate(W.TT2_HETERO)}
-    T = port.tables(O.TT2, P, DT)
     B = port.init_state(O.TT2, P, n)
     vo = np.full(n, port.init_vm(O.TT2, P))
-    tro = port.run(O.TT2, P, T, B, vo, n_macro * S, DT, textlen=1e-3, bcl=bcl, amp=AMP, het=het, rec_every=S,
-                   n_threads=8)
-    tro = np.concatenate([tro, vo[:, None]], axis=1)
+    tro = port.run(O.TT2, P, port.tables(O.TT2, P, DT), B, vo, int(round(t_end / DT)) + 1, DT, textlen=1e-3,
+                   bcl=L.BCL, amp=AMP, het=het, textbegin_per_cell=ph, rec_every=S, n_threads=os.cpu_count() or 8)
     res = {}
-    for mode in (0, 1):
-        b, _ = population(cm, p, n, seed=99)
-        vm = b.init_vm()
-        tr, stats = run_traces(cm, b, sur, vm, n_macro, bcl, mode)
-        u, a = A.beat_markers(tr, S * DT, [k * bcl for k in range(beats)])
-        uo, ao = A.beat_markers(tro, S * DT, [k * bcl for k in range(beats)])
-        rms = np.sqrt(((tr - tro) ** 2).mean(axis=1)) * 1e3
-        res[mode] = dict(apd=np.nanmax(np.abs(a - ao)) * 1e3, rms=rms.max(), up=np.nanmax(np.abs(u - uo)) * 1e3,
-                         sur=sum(s["surrogate"] for s in stats), fb=sum(s["fallback"] for s in stats),
-                         audit=max(s["max_audit_err_mv"] for s in stats))
-        assert np.all(np.isfinite(a)), mode
-    print("surrogate", res)
-    assert res[0]["sur"] > 0.9 * n * n_macro  # most cell-macro-steps use the learned step
-    # the network's outputs pass the range audit: few fallbacks beyond the coarse-only run's
-    # (stimulus, fast upstroke, audit sample)
-    assert res[0]["fb"] <= 1.5 * res[1]["fb"], res
-    # spec bars against the FP64 oracle, with the network
-    assert res[0]["apd"] <= 1.0 and res[0]["rms"] <= 0.5, res
-    # what the network gains: on the rotating audit sample the learned macro step is compared with
-    # ten plain fine steps from the same state; with the network that error is several times
-    # smaller than with the coarse step alone
-    assert res[0]["audit"] < 0.5 * res[1]["audit"], res
-    assert res[1]["apd"] <= 1.0 and res[1]["rms"] <= 0.5, res
+    for name, mode in (("learned", cm.SUR_AUDIT_FP64), ("coarse", cm.SUR_COARSE_ONLY | cm.SUR_AUDIT_FP64)):
+        tr, st = L.surrogate_traces(cm, p, sur, n, het_seed, ph, t_end, 1, mode)
+        res[name] = dict(L.trace_errors(tr, tro, ph, S * DT, beats), **st)
+    print("held out", res)
+    lrn, crs = res["learned"], res["coarse"]
+    assert lrn["surrogate"] > 0.9 * lrn["cell_macro_steps"]  # most cell-macro-steps take the learned step
+    assert lrn["fallback"] <= 1.5 * crs["fallback"]          # its steps pass the range audit
+    assert lrn["max_audit_err_mv"] < 1.0
+    # north-star bars against the FP64 oracle
+    assert lrn["missing_beats"] == 0 and lrn["apd90_max_ms"] <= 1.0 and lrn["rms_vm_mv_max"] <= 0.5, res
+    # what the network buys over the coarse step alone, on whole traces
+    assert lrn["apd90_max_ms"] < crs["apd90_max_ms"] and lrn["rms_vm_mv_max"] < crs["rms_vm_mv_max"], res
 
 
 def test_surrogate_blob_roundtrip(trained):
@@ -159,6 +168,17 @@ def test_inference_kernel_matches_network(trained):
     can round to the neighbouring BF16 value on one side only; the tolerance is 10 % of the
     output's scale plus 8 units in the last place of the state's FP32 value."""
     cm, p, sur, _ = trained
+    selected = sur.get_blob()
+    every = selected.copy()
+    every[L.APPLIED] = every[44:63]  # every output's correction applied, at its target scale
+    sur.set_blob(every)
+    try:
+        _inference_check(cm, p, sur)
+    finally:
+        sur.set_blob(selected)
+
+
+def _inference_check(cm, p, sur):
     n = 1000
     b, sc = population(cm, p, n, seed=97)
     vm = b.init_vm()
@@ -183,7 +203,7 @@ def test_inference_kernel_matches_network(trained):
                   S0["Na_i"], S0["K_i"], np.log(sc[0]), np.log(sc[1]), np.log(sc[2])], axis=1)
     blob = sur.get_blob()
     mu, inv_sd, sd_y, apply_y = blob[:22], blob[22:44], blob[44:63], blob[63:82]
-    assert apply_y[0] > 0  # the Vm correction is one the network predicts
+    assert np.all(apply_y > 0)
     Y = sur.mlp.forward(((F - mu) * inv_sd).astype(np.float32)).astype(np.float64)
     got = [(va - vb) * 1e3] + [sa[idx[k]] - sb[idx[k]] for k in outs]
     scale = [np.abs(v0 * 1e3)] + [np.abs(sb[idx[k]]) for k in outs]
