@@ -106,6 +106,9 @@ TISSUE_MODELS = {
     "tomek": dict(model=14, label="tomek2019-endo", het="TOM_HETERO", stim="TOM_STIM", stim_text="2 x -53 uA/uF",
                   mixed=TISSUE_MIXED_BYTES - 168 + 2 * 50 * 4, fp64=TISSUE_FP64_BYTES - 288 + 2 * 44 * 8),
 }
+SUR_CELLS = 1 << 20   # the learned form (config 4)
+SUR_BCL = 0.5
+SUR_SUBSTEPS = 10     # fine steps per macro step
 FULL_CELLS = 1 << 24
 FULL_INSTANCES = 64
 FULL_BCL = 0.5
@@ -246,7 +249,8 @@ def headline_sample(k, seed=None):
     from cardiomechanics_gb300 import workloads as W
     seed = ACC_SEED if seed is None else seed
     draw = (W.uniform(seed, np.arange(4 * k, dtype=np.uint64)) * FULL_CELLS).astype(np.int64)
-    idx = np.unique(draw)[:k]
+    _, first = np.unique(draw, return_index=True)
+    idx = draw[np.sort(first)[:k]]  # the first k distinct cells in draw order
     inst = W.full_form_instances(FULL_SEED, FULL_INSTANCES, FULL_CELLS)
     ends = np.cumsum([d["n"] for d in inst])
     phases = np.array([inst[i]["phase"] for i in np.searchsorted(ends, idx, side="right")]) * FULL_BCL
@@ -395,19 +399,26 @@ def train_surrogate(cm, stream, seeds=(1, 2, 3)):
     from cardiomechanics_gb300 import learned as L
     p = cm.Params(cm.TENTUSSCHER2, None, DT)
     sur = cm.Surrogate(p, substeps=SUR_SUBSTEPS, seed=1, stream=stream.cuda_stream)
+    if not seeds:  # profiler captures only: an untrained network with a zero output layer
+        prm = sur.mlp.get_params()
+        prm[4][:] = 0.0
+        prm[5][:] = 0.0
+        sur.mlp.set_params(prm)
+        return p, sur, {"untrained": "zero output layer (capture run: the step equals the coarse step)"}
     rep = L.train_and_select(cm, p, sur, seeds=seeds, stream=stream)
     applied = sur.get_blob()[L.APPLIED]
     rep["corrected_outputs"] = [nm for nm, a in zip(L.OUTPUT_NAMES, applied) if a > 0]
     return p, sur, rep
 
 
-def learned_leg(cm, torch, stream, p, sur, steps, warmup):
+def learned_leg(cm, torch, stream, p, sur, steps, warmup, cells=None):
     """Learned form: 1,048,576 jittered (+-15 %) ten Tusscher cells paced together at BCL 500 ms,
     timed over `steps` macro steps of 10 x 0.01 ms (one macro step = 10 cell-steps per cell),
     mixed-precision audit of 1 % of the cells."""
     from cardiomechanics_gb300 import workloads as W
-    b = cm.Batch(p, SUR_CELLS, cm.MIXED, stream=stream.cuda_stream)
-    sc = W.conductance_scales(5, SUR_CELLS, 3, 0.85, 1.15)
+    n_cells = cells or SUR_CELLS
+    b = cm.Batch(p, n_cells, cm.MIXED, stream=stream.cuda_stream)
+    sc = W.conductance_scales(5, n_cells, 3, 0.85, 1.15)
     for k, name in enumerate(W.TT2_HETERO):
         b.add_hetero_value(name, p.get(name) * sc[k])
     vm = torch.tensor(b.init_vm(), device="cuda")
@@ -422,7 +433,7 @@ def learned_leg(cm, torch, stream, p, sur, steps, warmup):
     e1.record(stream)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
-    return {"value": SUR_CELLS * SUR_SUBSTEPS * steps / sec, "unit": UNIT, "cells": SUR_CELLS,
+    return {"value": n_cells * SUR_SUBSTEPS * steps / sec, "unit": UNIT, "cells": n_cells,
             "macro_steps": steps, "substeps": SUR_SUBSTEPS, "ms_per_macro_step": 1e3 * sec / steps,
             "bcl_ms": SUR_BCL * 1e3, "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.85,1.15]",
             "audit": "1 % rotating, mixed precision", "stats": stats, "gpu_launches": 2 * steps + 2}
@@ -662,6 +673,76 @@ def plain_small_leg(cm, torch, stream, steps=2000):
     return {"value": n * steps / sec, "unit": UNIT, "cells": n, "steps": steps, "ms_per_step": 1e3 * sec / steps,
             "precision": "FP64", "conductance_jitter": "g_Na,g_Kr,g_K1 x U[0.95,1.05] seed 1", "bcl_ms": 1000.0,
             "note": "65,536 cells leave most of the GPU's FP64 pipes idle; the 4.2M-cell figure is plain_fp64"}
+
+
+CRN_CELLS = 2048 * 2048
+# Courtemanche single-batch kernels: mixed 17 FP32 states + 4 compensated pairs r+w (200 B), Vm
+# pair r+w (16 B), 3 FP32 conductances (12 B); FP64 21 states r+w (336 B), Vm r+w (16 B), 3 FP64
+# conductances (24 B)
+CRN_MIXED_BYTES_PER_CELL_STEP = 2 * (17 + 8) * 4 + 2 * 8 + 3 * 4
+CRN_FP64_BYTES_PER_CELL_STEP = 2 * 21 * 8 + 2 * 8 + 3 * 8
+
+
+def crn_leg(cm, torch, stream, args, hbm_peak, peak_kind):
+    """Courtemanche 1998 single-batch kernels: 4,194,304 atrial cells, g_Na/g_to/g_CaL x U[0.9,
+    1.1], 20 pA/pF for 2 ms every 1000 ms; the mixed form at each launch shape the autotuner
+    tries on it (the autotuner's pick reported) and the FP64 form, each with its HBM fraction."""
+    from cardiomechanics_gb300 import workloads as W
+    n = args.crn_cells
+    p = cm.Params(cm.COURTEMANCHE, None, DT)
+    out = {"cells": n, "bcl_ms": 1000.0}
+    for prec, steps, nbytes in ((cm.MIXED, args.crn_steps, CRN_MIXED_BYTES_PER_CELL_STEP),
+                                (cm.FP64, max(3, args.crn_steps // 50), CRN_FP64_BYTES_PER_CELL_STEP)):
+        b = cm.Batch(p, n, prec, stream=stream.cuda_stream)
+        sc = W.conductance_scales(4, n, 3, 0.9, 1.1)
+        for k, name in enumerate(W.CRN_HETERO):
+            b.add_hetero_value(name, p.get(name) * sc[k])
+        shape = None
+        if prec == cm.MIXED:
+            shape = b.autotune(args.tune_steps)[0] if args.launch is None else None
+            if args.launch is not None:
+                v, g = (int(x) for x in args.launch.split(","))
+                b.set_launch(v, g)
+                shape = v * 100 + g
+        vm = torch.tensor(b.init_vm(), device="cuda")
+        kw = dict(textbegin=0.0, textlen=2e-3, bcl=1.0, amplitude=W.CRN_STIM_PAPF)
+        b.run(vm, 3, **kw)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(vm, steps, t0=3 * DT, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        gbs = nbytes * n * steps / sec / 1e9
+        key = "mixed" if prec == cm.MIXED else "fp64"
+        out[key] = {"value": n * steps / sec, "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * sec / steps,
+                    "bytes_per_cell_step": nbytes, "achieved_gbs": gbs, "hbm_frac": gbs / hbm_peak,
+                    "peak_kind": peak_kind, "launch_shape": shape}
+        del b, vm
+        torch.cuda.empty_cache()
+    return out
+
+
+def training_leg(cm, torch, stream, args):
+    """The surrogate's training kernels alone (profiler captures): the dataset generation
+    (plain mixed steps, pair recording, ordered append) and one network's fit, each timed."""
+    from cardiomechanics_gb300 import learned as L
+    p = cm.Params(cm.TENTUSSCHER2, None, DT)
+    sur = cm.Surrogate(p, substeps=SUR_SUBSTEPS, seed=1, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pairs = L.generate(cm, p, sur, stream)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    steps = args.fit_steps
+    sur.reset_network(1)
+    loss = sur.fit(batch=4096, steps=steps, lr=1e-3, seed=3)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"pairs": pairs, "generate_s": t1 - t0, "fit_steps": steps, "fit_s": t2 - t1,
+            "ms_per_adam_step": 1e3 * (t2 - t1) / max(1, steps), "loss": loss, "batch": 4096}
 
 
 class IonicCPUSample:
@@ -950,9 +1031,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",
                     choices=["all", "full", "mixed", "fp64", "surrogate", "batched", "ord", "tomek", "tissue",
-                             "theta"],
+                             "theta", "crn", "train"],
                     help="run one leg only (profiler captures); the contract's JSON line is printed for 'all'")
     ap.add_argument("--tune-steps", type=int, default=10)
+    ap.add_argument("--crn-steps", type=int, default=500, help="timed steps of the Courtemanche mixed form")
+    ap.add_argument("--crn-cells", type=int, default=CRN_CELLS, help="Courtemanche cells (fewer only for captures)")
+    ap.add_argument("--fit-steps", type=int, default=2000, help="Adam steps of the training leg")
     ap.add_argument("--sur-steps", type=int, default=5000, help="timed macro steps of the 1M-cell learned form")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -962,7 +1046,12 @@ def main():
     ap.add_argument("--batched-instances", type=int, default=256,
                     help="instances of the batched form (fewer only for profiler captures)")
     ap.add_argument("--sur-seeds", type=int, default=3,
-                    help="network seeds trained and compared on held-out cells (fewer only for captures)")
+                    help="network seeds trained and compared on held-out cells (0: an untrained zero-output "
+                         "network, for profiler captures only)")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy traces (captures only)")
+    ap.add_argument("--sur-cells", type=int, default=None, help="cells of the learned leg (default 1,048,576)")
+    ap.add_argument("--gen-steps", type=int, default=None,
+                    help="macro steps per training population in the training leg (captures; default: all)")
     ap.add_argument("--launch", default=None, help="fixed mixed-kernel launch shape 'variant,grid_mode' (skips tuning)")
     ap.add_argument("--ord-steps", type=int, default=500,
                     help="timed steps of the O'Hara-Rudy and Tomek mixed forms")
@@ -1011,6 +1100,12 @@ def main():
     if args.only == "theta":
         print(json.dumps(theta_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
         return
+    if args.only == "crn":
+        print(json.dumps(crn_leg(cm, torch, stream, args, hbm_peak, peak_kind)), flush=True)
+        return
+    if args.only == "train":
+        print(json.dumps(training_leg(cm, torch, stream, args)), flush=True)
+        return
     if args.only in ("ord", "tomek"):
         leg = "ohara_rudy" if args.only == "ord" else "tomek"
         print(json.dumps(ionic_leg(cm, torch, stream, args, hbm_peak, peak_kind, leg,
@@ -1018,7 +1113,7 @@ def main():
         return
     p, sur, training = train_surrogate(cm, stream, tuple(range(1, args.sur_seeds + 1)))
     if args.only == "surrogate":
-        out = learned_leg(cm, torch, stream, p, sur, args.sur_steps, 20)
+        out = learned_leg(cm, torch, stream, p, sur, args.sur_steps, 20, args.sur_cells)
         out["training"] = training
         print(json.dumps(out), flush=True)
         return
@@ -1045,6 +1140,7 @@ def main():
     del sur
     torch.cuda.empty_cache()
     prec = precision_leg(cm, torch, stream, args, hbm_peak, peak_kind)
+    crn = crn_leg(cm, torch, stream, args, hbm_peak, peak_kind)
     small = plain_small_leg(cm, torch, stream)
     bat = None
     if not args.no_batched:
@@ -1087,6 +1183,7 @@ def main():
             "sur_plain_kernel": full["sur_plain_kernel"],
             "precision_form": prec,
             "plain_small": small,
+            "courtemanche": crn,
             "learned_form": learned,
             "batched": bat,
             "ohara_rudy": ionic["ohara_rudy"],

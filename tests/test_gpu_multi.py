@@ -118,3 +118,53 @@ def test_pipeline_shapes_with_many_instances_per_block(gpu):
     for vms in out[1:]:
         for a, b in zip(vms, out[0]):
             assert np.abs(a - b).max() <= 1e-6
+
+
+def test_mixed_models_against_oracle(gpu, port):
+    """One batched launch per step over ten Tusscher 2006 and Courtemanche instances (own sizes,
+    conductances and stimulus phases; the 3-stage 256-cell pipeline, multi_pipe_kernel<256, 3>)
+    against the oracle's FP64 driver loop for each model (TenTusscher2.cpp:615-906,
+    CourtemancheEtAl.cpp:85-187, CellModel.h:405-420): 3000 steps (30 ms, through each
+    instance's stimulus and upstroke) in five segments, Vm compared after every segment at the
+    mixed form's tolerance, and the APD-scale states after the last."""
+    import oracle as O
+    cm = gpu
+    sizes = [4096, 2048, 1536, 3072]
+    models = [cm.TENTUSSCHER2, cm.COURTEMANCHE, cm.TENTUSSCHER2, cm.COURTEMANCHE]
+    st = [dict(textbegin=tb, textlen=1e-3 if m == cm.TENTUSSCHER2 else 2e-3, bcl=0.3,
+               amplitude=W.TT2_STIM_NA if m == cm.TENTUSSCHER2 else W.CRN_STIM_PAPF)
+          for tb, m in zip((0.0, 0.004, 0.011, 0.017), models)]
+    mb = build(cm, sizes, models)
+    multi = cm.Multi(mb)
+    multi.set_launch(2048, 7, 2)
+    vms = [b.init_vm() for b in mb]
+    ref = []
+    for i, (n, m) in enumerate(zip(sizes, models)):
+        om = O.TT2 if m == cm.TENTUSSCHER2 else O.CRN
+        P = port.param_vector(om, O.load_params(om))
+        names = port.param_names(om)
+        sc = W.conductance_scales(5 + i, n, 3, 0.8, 1.2)
+        hn = W.TT2_HETERO if m == cm.TENTUSSCHER2 else W.CRN_HETERO
+        het = {k: P[names.index(k)] * sc[j] for j, k in enumerate(hn)}
+        ref.append(dict(om=om, P=P, T=port.tables(om, P, 1e-5), B=port.init_state(om, P, n),
+                        v=np.full(n, port.init_vm(om, P)), het=het))
+    seg, worst = 600, 0.0
+    for k in range(5):
+        cur = [continued(s, k * seg) for s in st]
+        multi.run(vms, seg, cur)
+        for i, r in enumerate(ref):
+            port.run(r["om"], r["P"], r["T"], r["B"], r["v"], seg, 1e-5, t0=cur[i]["t0"],
+                     textbegin=cur[i]["textbegin"], textlen=st[i]["textlen"], bcl=st[i]["bcl"],
+                     amp=st[i]["amplitude"], het=r["het"], n_threads=8)
+            err = float(np.abs(vms[i] - r["v"]).max())
+            worst = max(worst, err)
+            # FP32 gates and currents: within 1 mV through the upstroke, as the precision form
+            assert err <= 1e-3, (k, i, err)
+    assert all(b.audit() == 0 for b in mb)
+    # slow accumulators after 30 ms, in the reference block layout: TT2 CaSR, Na_i, K_i (slots 1,
+    # 3, 4, TenTusscher2.h:77); Courtemanche Ca_up, Ca_rel (slots 1, 2)
+    for i, (b, r) in enumerate(zip(mb, ref)):
+        cols = [1, 3, 4] if models[i] == cm.TENTUSSCHER2 else [1, 2]
+        blk = b.get_state(cm.LAYOUT_REF_BLOCK).reshape(r["B"].shape)
+        np.testing.assert_allclose(blk[:, cols], r["B"][:, cols], rtol=1e-3)
+    print("multi vs oracle: worst |dVm|", worst * 1e3, "mV")
