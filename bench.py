@@ -733,7 +733,7 @@ def training_leg(cm, torch, stream, args):
     sur = cm.Surrogate(p, substeps=SUR_SUBSTEPS, seed=1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    pairs = L.generate(cm, p, sur, stream)
+    pairs = L.generate(cm, p, sur, stream, args.gen_steps)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     steps = args.fit_steps

@@ -60,14 +60,18 @@ def population(cm, p, n, het_seed, precision, stream=None, cells=None):
     return b
 
 
-def generate(cm, p, sur, stream=None):
-    """Training pairs of the populations in TRAINING; returns the number of pairs held."""
+def generate(cm, p, sur, stream=None, max_macro=None):
+    """Training pairs of the populations in TRAINING; returns the number of pairs held.
+    max_macro caps the macro steps per population (profiler captures only)."""
     n = 0
     for seed, bcl, tb, t_end, stride in TRAINING:
         b = population(cm, p, TRAINING_CELLS, seed, cm.MIXED, stream)
         v = b.init_vm()
-        n = sur.generate(b, v, int(round(t_end / (SUBSTEPS * DT))), textbegin=tb, textlen=1e-3, bcl=bcl,
-                         amplitude=W.TT2_STIM_NA, cell_stride=stride, max_pairs=MAX_PAIRS)
+        n_macro = int(round(t_end / (SUBSTEPS * DT)))
+        if max_macro is not None:
+            n_macro = min(n_macro, max_macro)
+        n = sur.generate(b, v, n_macro, textbegin=tb, textlen=1e-3, bcl=bcl, amplitude=W.TT2_STIM_NA,
+                         cell_stride=stride, max_pairs=MAX_PAIRS)
     return n
 
 
