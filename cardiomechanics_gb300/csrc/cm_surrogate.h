@@ -41,7 +41,9 @@ struct SurKernelArgs {
   TT2Consts<float> coarse;       // constants for the macro step S * dt
   const float *rows_coarse;      // FP32 voltage table rows for S * dt
   const float *eca;              // ECa table (dt independent)
-  float *vm_hi, *vm_lo;          // Vm planes (lo = hi + ld)
+  double *vm;                    // the caller's Vm [V], device or page-locked host memory: read and
+                                 // written once per macro step (as a compensated pair in between)
+  int vm_device;                 // vm is device memory with a 16-byte aligned base (L2 prefetch)
   SurNorm norm;
   const __nv_bfloat16 *w1, *w2, *w3;  // BF16 network: W1 [128][32], W2 [128][128], W3 [32][128]
   const float *bias;             // b1 [128], b2 [128], b3 [32]
@@ -71,7 +73,7 @@ constexpr int kSnapPlanes = 21 + 2 + 6 + 1;
 
 struct SurPlainArgs {
   DevBatch fine;
-  float *vm_hi, *vm_lo;
+  double *vm;                    // as SurKernelArgs::vm
   const int *list;
   const unsigned int *n_list;
   int substeps;
