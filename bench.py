@@ -13,7 +13,8 @@ set; per-cell stimulus times carry the phases). Inputs are synthetic (seeded); t
 
 value         cell-steps/s of the headline, state resident in HBM (CUDA events, batch stream)
 e2e           the same through the C ABI with Vm in pinned HOST memory, one
-              cm_batch_run_surrogate call per macro step (Vm copied in and out every step)
+              cm_batch_run_surrogate call per macro step (Vm read from and written to page-locked
+              host memory by the macro-step kernels every step)
 plain_fp64    the plain FP64 kernel (the reference's arithmetic) on the same 16.7M cells
 roofline      the macro-step kernel (timed by the library's CUDA events) against measured HBM,
               with its tensor-core fraction beside it
@@ -505,7 +506,7 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     tpk, tpk_kind = bf16_peak()
 
     # ---- end to end: one C-ABI call per macro step with the cells' Vm in pinned HOST memory
-    # (copied in and out by the call); the stimulus times stay on the device
+    # (read and written there by the call's kernels); the stimulus times stay on the device
     vm_h = vm.cpu().pin_memory()
     del vm
     torch.cuda.synchronize()

@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -50,6 +51,8 @@ struct EpiArgs {
 };
 
 // C = A B^T, A: M x K (lda), B: N x K (ldb), K % 32 == 0. 64x64 block tile, 4 warps of 32x32.
+// gridDim.z > 1 (EPI_F32 only): block z sums k in [z K / gridDim.z, (z + 1) K / gridDim.z) and
+// writes its partial product to the z-th M x ldc slice of out_f32 (split K).
 template <int EPI>
 __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__ A, int lda,
                                                const __nv_bfloat16 *__restrict__ B, int ldb, int M, int N, int K,
@@ -62,7 +65,9 @@ __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
   float acc[2][4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  const int kc = K / (int)gridDim.z;  // a multiple of BK (the launcher checks)
+  const int kbeg = (int)blockIdx.z * kc, kend = kbeg + kc;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
     // 64 rows x 32 bf16 = 4 chunks of 16 B per row; 256 chunks per operand, 2 per thread
     for (int i = tid; i < 256; i += 128) {
       const int r = i >> 2, cc = (i & 3) * 8;
@@ -132,7 +137,7 @@ __global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__
           const float h = __bfloat162float(e.h[o]);
           e.out_bf16[o] = __float2bfloat16(v * (1.f - h * h));
         } else {
-          e.out_f32[o] = v;
+          e.out_f32[(size_t)blockIdx.z * (size_t)M * e.ldc + o] = v;
         }
       }
 }
@@ -157,6 +162,10 @@ __global__ void transpose_bf16(const __nv_bfloat16 *__restrict__ in, __nv_bfloat
 // block's share of the loss goes to loss_part[block] (summed in block order by mse_total, so the
 // reported loss is the same on every run).
 constexpr int kMseBlocks = 256;
+// Weight-gradient GEMMs split K (the minibatch rows) into up to kMaxSplits parts of 256 rows;
+// column sums use up to kColsumParts row blocks. Partial sums live in Mlp::part.
+constexpr int kMaxSplits = 32, kColsumParts = 64;
+constexpr size_t kPartFloats = (size_t)kMaxSplits * 128 * 128;
 __global__ void mse_grad(const float *__restrict__ Y, const float *__restrict__ T, int n, int n_real_rows, int n_out,
                          int ldy, __nv_bfloat16 *__restrict__ dY, float *loss_part) {
   __shared__ float red[256];
@@ -187,13 +196,24 @@ __global__ void mse_total(float *__restrict__ loss_part, int n_part, float *__re
   *loss = s;
 }
 
-// db[c] = sum_r dZ[r][c]
-__global__ void colsum_bf16(const __nv_bfloat16 *__restrict__ dZ, int rows, int cols, float *__restrict__ db) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
-  float s = 0.f;
-  for (int r = 0; r < rows; r++) s += __bfloat162float(dZ[(size_t)r * cols + c]);
-  db[c] = s;
+// db[c] = sum_r dZ[r][c] in two passes with a fixed order: block b sums rows [b R, (b + 1) R)
+// of every column into part[b][c], then one block sums the parts in block order.
+__global__ void colsum_part(const __nv_bfloat16 *__restrict__ dZ, int rows, int cols, int rows_per_block,
+                            float *__restrict__ part) {
+  const int r0 = blockIdx.x * rows_per_block, r1 = min(rows, r0 + rows_per_block);
+  for (int c = threadIdx.x; c < cols; c += blockDim.x) {
+    float s = 0.f;
+    for (int r = r0; r < r1; r++) s += __bfloat162float(dZ[(size_t)r * cols + c]);
+    part[(size_t)blockIdx.x * cols + c] = s;
+  }
+}
+
+__global__ void sum_parts(const float *__restrict__ part, int n_parts, int n, float *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < n_parts; z++) s += part[(size_t)z * n + i];
+    out[i] = s;
+  }
 }
 
 // Adam on FP32 master weights (Kingma & Ba 2015), then the BF16 operand copy.
@@ -244,6 +264,34 @@ cudaError_t gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ld
   return cudaGetLastError();
 }
 
+// C (M x ldc, FP32) = A B^T with K split over `splits` blocks per tile (weight gradients: K = the
+// minibatch rows, M and N at most 128), partial products in `part`, summed in split order.
+cudaError_t gemm_f32_split(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
+                           float *C, int ldc, float *part, int splits, cudaStream_t s) {
+  splits = std::min(splits, (int)(kPartFloats / ((size_t)M * ldc)));
+  if (splits < 1 || K % (32 * splits)) splits = 1;
+  EpiArgs e{};
+  e.out_f32 = splits > 1 ? part : C;
+  e.ldc = ldc;
+  dim3 grid((N + 63) / 64, (M + 63) / 64, splits);
+  gemm_nt<EPI_F32><<<grid, 128, 0, s>>>(A, lda, B, ldb, M, N, K, e);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess || splits == 1) return err;
+  const int n = M * ldc;
+  sum_parts<<<(n + 255) / 256, 256, 0, s>>>(part, splits, n, C);
+  return cudaGetLastError();
+}
+
+cudaError_t colsum(const __nv_bfloat16 *dZ, int rows, int cols, float *db, float *part, cudaStream_t s) {
+  const int rows_per_block = rows > 64 * kColsumParts ? (rows + kColsumParts - 1) / kColsumParts : 64;
+  const int blocks = (rows + rows_per_block - 1) / rows_per_block;
+  colsum_part<<<blocks, 128, 0, s>>>(dZ, rows, cols, rows_per_block, part);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  sum_parts<<<1, 128, 0, s>>>(part, blocks, cols, db);
+  return cudaGetLastError();
+}
+
 cudaError_t transpose(const __nv_bfloat16 *in, __nv_bfloat16 *out, int rows, int cols, cudaStream_t s) {
   dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
   transpose_bf16<<<grid, block, 0, s>>>(in, out, rows, cols);
@@ -282,6 +330,7 @@ cudaError_t Mlp::init(int n_in_, int n_hidden_, int n_out_, uint64_t seed, cudaS
   MCK(cudaMalloc(&wb, n_params * sizeof(__nv_bfloat16)));
   MCK(cudaMalloc(&wt, n_params * sizeof(__nv_bfloat16)));
   MCK(cudaMalloc(&loss, (1 + kMseBlocks) * sizeof(float)));
+  MCK(cudaMalloc(&part, kPartFloats * sizeof(float)));
   return reset(seed);
 }
 
@@ -324,8 +373,10 @@ cudaError_t Mlp::sync_bf16() {
 }
 
 void Mlp::release() {
-  for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)wt, (void *)loss, (void *)ws})
+  for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)wt, (void *)loss, (void *)ws,
+                  (void *)part})
     cudaFree(p);
+  part = nullptr;
   w = g = m1 = m2 = nullptr;
   wb = wt = nullptr;
   loss = nullptr;
@@ -449,19 +500,13 @@ cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
   MCK(transpose(B.H1, B.H1T, rows, H, stream));
   MCK(transpose(B.dZ1, B.dZ1T, rows, H, stream));
   MCK(transpose(B.X, B.XT, rows, in_pad, stream));
-  EpiArgs f{};
-  f.out_f32 = g + off[4];
-  f.ldc = H;
-  MCK(gemm<EPI_F32>(B.dYT, rows, B.H2T, rows, out_pad, H, rows, f, stream));
-  f.out_f32 = g + off[2];
-  f.ldc = H;
-  MCK(gemm<EPI_F32>(B.dZ2T, rows, B.H1T, rows, H, H, rows, f, stream));
-  f.out_f32 = g + off[0];
-  f.ldc = in_pad;
-  MCK(gemm<EPI_F32>(B.dZ1T, rows, B.XT, rows, H, in_pad, rows, f, stream));
-  colsum_bf16<<<(out_pad + 127) / 128, 128, 0, stream>>>(B.dY, rows, out_pad, g + off[5]);
-  colsum_bf16<<<(H + 127) / 128, 128, 0, stream>>>(B.dZ2, rows, H, g + off[3]);
-  colsum_bf16<<<(H + 127) / 128, 128, 0, stream>>>(B.dZ1, rows, H, g + off[1]);
+  const int splits = rows >= 512 ? std::min(kMaxSplits, rows / 256) : 1;
+  MCK(gemm_f32_split(B.dYT, rows, B.H2T, rows, out_pad, H, rows, g + off[4], H, part, splits, stream));
+  MCK(gemm_f32_split(B.dZ2T, rows, B.H1T, rows, H, H, rows, g + off[2], H, part, splits, stream));
+  MCK(gemm_f32_split(B.dZ1T, rows, B.XT, rows, H, in_pad, rows, g + off[0], in_pad, part, splits, stream));
+  MCK(colsum(B.dY, rows, out_pad, g + off[5], part, stream));
+  MCK(colsum(B.dZ2, rows, H, g + off[3], part, stream));
+  MCK(colsum(B.dZ1, rows, H, g + off[1], part, stream));
   return cudaGetLastError();
 }
 

@@ -18,6 +18,7 @@ struct Mlp {
   size_t off[6] = {}, size[6] = {}, n_params = 0;  // W1 b1 W2 b2 W3 b3 (padded shapes)
   float *loss = nullptr;
   void *ws = nullptr;
+  float *part = nullptr;  // partial sums of the split weight-gradient GEMMs and column sums
   int ws_rows = 0;
   int step = 0;
 

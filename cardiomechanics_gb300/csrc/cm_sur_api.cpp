@@ -182,36 +182,33 @@ int planes_in(cm_batch_s *b, double *Vm, double **dvm, bool &host_vm, cudaStream
   return CM_OK;
 }
 
-// The caller's Vm as the macro-step kernels take it: device memory and page-locked host memory
-// directly (the kernels read and write each cell's Vm once per macro step), other host memory
-// through a staging copy (copied back by vm_out).
-int vm_in(cm_batch_s *b, double *Vm, double **dvm, bool &staged, cudaStream_t s) {
-  const int64_t n = b->d.n;
-  staged = false;
-  *dvm = Vm;
-  if (is_device_ptr(Vm)) return CM_OK;
-  if (double *mapped = mapped_host_ptr(Vm)) {
-    *dvm = mapped;
-    return CM_OK;
-  }
-  int rc = ensure_stage(b, n);
-  if (rc) return rc;
-  staged = true;
-  *dvm = b->stage[0];
-  CK(cudaMemcpyAsync(*dvm, Vm, n * sizeof(double), cudaMemcpyHostToDevice, s));
-  return CM_OK;
-}
-
-int vm_out(cm_batch_s *b, double *Vm, const double *dvm, bool staged, cudaStream_t s) {
-  if (staged) CK(cudaMemcpyAsync(Vm, dvm, b->d.n * sizeof(double), cudaMemcpyDeviceToHost, s));
-  return CM_OK;
-}
-
 int planes_out(cm_batch_s *b, double *Vm, double *dvm, bool host_vm, cudaStream_t s) {
   const int64_t n = b->d.n;
   CK(launch_vm_join(b->vm_planes, b->vm_planes + b->d.ld, dvm, n, s));
   if (host_vm) CK(cudaMemcpyAsync(Vm, dvm, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   return CM_OK;
+}
+
+// The caller's Vm as the macro-step kernels take it: page-locked host memory directly (the
+// kernels read and write each cell's FP64 Vm once per macro step over the host link: no split and
+// join kernel per call); device memory, and other host memory through a staging copy, as the
+// device planes of the compensated pair (split once per call, joined by vm_out).
+int vm_in(cm_batch_s *b, double *Vm, double **direct, double **dvm, bool &host_vm, cudaStream_t s) {
+  *direct = nullptr;
+  if (!is_device_ptr(Vm)) {
+    if (double *mapped = mapped_host_ptr(Vm)) {
+      *direct = mapped;
+      *dvm = mapped;
+      host_vm = false;
+      return CM_OK;
+    }
+  }
+  return planes_in(b, Vm, dvm, host_vm, s);
+}
+
+int vm_out(cm_batch_s *b, double *Vm, double *dvm, const double *direct, bool host_vm, cudaStream_t s) {
+  if (direct) return CM_OK;
+  return planes_out(b, Vm, dvm, host_vm, s);
 }
 
 // The audit of one snapshot buffer (its entries, FP64 or mixed), as the kernels take it.
@@ -700,9 +697,10 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   // (the pending sample of the previous call, or nothing: its counter is zero)
   int wbuf = s->pending >= 0 ? (s->pending ^ 1) : 0;
   if (s->pending < 0) CK(cudaMemsetAsync(s->n_snap, 0, 2 * sizeof(unsigned int), st));
-  double *dvm;
-  bool staged;
-  if ((rc = vm_in(b, Vm, &dvm, staged, st))) return rc;
+  double *dvm, *direct;
+  bool host_vm = false;
+  if ((rc = vm_in(b, Vm, &direct, &dvm, host_vm, st))) return rc;
+  float *hi = direct ? nullptr : b->vm_planes, *lo = direct ? nullptr : b->vm_planes + b->d.ld;
   const cm_stimulus stv = stim ? *stim : cm_stimulus{0, 1e300, nullptr, 0, 0, 0};
   double t = stv.t0, tb = stv.textbegin;
   SurKernelArgs ka{};
@@ -710,13 +708,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.coarse = s->coarse;
   ka.rows_coarse = s->rows_coarse;
   ka.eca = s->eca;
-  ka.vm = dvm;
-  {
-    cudaPointerAttributes at;
-    const bool dev = cudaPointerGetAttributes(&at, dvm) == cudaSuccess && at.type == cudaMemoryTypeDevice;
-    if (!dev) cudaGetLastError();
-    ka.vm_device = dev && ((uintptr_t)dvm % 16 == 0) ? 1 : 0;
-  }
+  ka.vm = direct;
+  ka.vm_hi = direct ? nullptr : hi;
+  ka.vm_lo = direct ? nullptr : lo;
   ka.norm = s->norm;
   ka.w1 = s->net.m.wb + s->net.m.off[0];
   ka.w2 = s->net.m.wb + s->net.m.off[2];
@@ -741,7 +735,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.bias = bias;
   SurPlainArgs pa{};
   pa.fine = b->d;
-  pa.vm = dvm;
+  pa.vm = direct;
+  pa.vm_hi = ka.vm_hi;
+  pa.vm_lo = ka.vm_lo;
   pa.list = s->fallback;
   pa.n_list = s->n_fallback;
   pa.substeps = s->substeps;
@@ -807,7 +803,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   // the last step's sample is audited by the next run's first macro step, or by
   // cm_surrogate_flush_audit
   if (audit_mod > 0 && n_macro > 0) s->pending = wbuf ^ 1;
-  rc = vm_out(b, Vm, dvm, staged, st);
+  rc = vm_out(b, Vm, dvm, direct, host_vm, st);
   unsigned long long tot[3] = {0, 0, 0};
   float aerr = 0;
   unsigned int mask = 0;

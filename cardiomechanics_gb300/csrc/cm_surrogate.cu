@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
   const unsigned int n = *a.n_list;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int c = a.list[i];
-    Acc v = acc_from_double(a.vm[c]);
+    Acc v = a.vm ? acc_from_double(a.vm[c]) : Acc{a.vm_hi[c], a.vm_lo[c]};
     uint32_t audit = 0;
     double tb = a.tb_cell ? a.tb_cell[c] : 0.0;
     for (int k = 0; k < a.substeps; k++) {
@@ -136,7 +136,12 @@ __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
       acc_add(v, tt2_mixed_cell<int>(a.fine, c, v.hi, iext, audit));
     }
     if (a.tb_cell) a.tb_cell[c] = tb;
-    a.vm[c] = acc_to_double(v);
+    if (a.vm) {
+      a.vm[c] = acc_to_double(v);
+    } else {
+      a.vm_hi[c] = v.hi;
+      a.vm_lo[c] = v.lo;
+    }
     if (!isfinite(v.hi)) audit |= 1u;
     if (audit) {
       atomicOr(a.fine.audit_cell + c, audit);
@@ -471,18 +476,22 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     __syncwarp();
     if (lane < kTcStageVars) bulk_g2s(stage + lane * kTcCells, fb.s32 + lane * ld + c0, kTcCells * 4u, &bar_stage[g]);
   };
-  // The block's tile one round of grabs after `tile` goes to L2 ahead of its stage copy and its
-  // Vm and conductance loads (lane v: state plane v, then Vm and the per-cell conductances; whole
-  // 16-byte chunks inside each array).
+  // The block's tile two rounds of grabs after `tile` goes to L2 ahead of its stage copy and its
+  // Vm and conductance loads (lane v: state plane v, then the Vm planes and the per-cell
+  // conductances; whole 16-byte chunks inside each array). Issued by the group's second warp:
+  // the first issues the stage copies and the MMAs.
   auto prefetch_ahead = [&](int tile) {
-    const int ahead = tile + kGroups * (int)gridDim.x;
+    const int ahead = tile + 2 * kGroups * (int)gridDim.x;
     if (ahead >= n_tiles) return;
     const int64_t c0 = (int64_t)ahead * kTcCells;
     const int64_t cells = min((int64_t)kTcCells, (int64_t)n - c0);
     if (lane < kTcStageVars) {
       bulk_prefetch_l2(fb.s32 + lane * ld + c0, kTcCells * 4u);
-    } else if (lane == kTcStageVars) {  // device Vm only
-      if (a.vm_device && cells * 8 >= 16) bulk_prefetch_l2(a.vm + c0, (uint32_t)((cells * 8) & ~15));
+    } else if (lane == kTcStageVars) {  // the device Vm planes (hi, then lo)
+      if (!a.vm) {
+        bulk_prefetch_l2(a.vm_hi + c0, kTcCells * 4u);
+        bulk_prefetch_l2(a.vm_lo + c0, kTcCells * 4u);
+      }
     } else if (lane < kTcStageVars + 4) {
       const float *h = het[lane == kTcStageVars + 1 ? H2_g_Na : (lane == kTcStageVars + 2 ? H2_g_Kr : H2_g_K1)];
       if (h && cells * 4 >= 16) bulk_prefetch_l2(h + c0, (uint32_t)((cells * 4) & ~15));
@@ -496,10 +505,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       s_tile[g] = tn;
     }
     tn = __shfl_sync(0xffffffffu, tn, 0);
-    if (tn < n_tiles) {
-      issue(tn);
-      prefetch_ahead(tn);
-    }
+    if (tn < n_tiles) issue(tn);
   };
   if (threadIdx.x == 0) s_next = 0;
   if (leader && g < kGroups) {
@@ -569,12 +575,15 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     umma::fence_before_sync();
     group_sync(g);
   };
+  const bool prefetcher = (threadIdx.x & 127) >= 32 && (threadIdx.x & 127) < 64;  // the group's second warp
   while (t < n_tiles) {
+    if (prefetcher) prefetch_ahead(t);
     const int c = t * kTcCells + r;
     const bool valid = c < n;
     // loads that do not come through the stage go first: their latency overlaps the stage wait
-    // Vm of the caller's array (plain load: it may be page-locked host memory); padding cells 0
-    const Acc vm = acc_from_double(valid ? a.vm[c] : 0.0);
+    // Vm: the device planes (c < ld: padding cells too), or the caller's page-locked host array
+    // (plain load; padding cells 0)
+    const Acc vm = a.vm ? acc_from_double(valid ? a.vm[c] : 0.0) : Acc{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};
     const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
     TT2Het_<float> g6;
     g6.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
@@ -704,7 +713,12 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
           Acc nvm = vm;
           apply(nq, nvm, on, inc, corr);
           store_cell(fb, c, nq);
-          a.vm[c] = acc_to_double(nvm);
+          if (a.vm) {
+            a.vm[c] = acc_to_double(nvm);
+          } else {
+            a.vm_hi[c] = nvm.hi;
+            a.vm_lo[c] = nvm.lo;
+          }
           pred = (nvm.hi + nvm.lo) * 1000.f;
           took = true;
         }

@@ -41,9 +41,11 @@ struct SurKernelArgs {
   TT2Consts<float> coarse;       // constants for the macro step S * dt
   const float *rows_coarse;      // FP32 voltage table rows for S * dt
   const float *eca;              // ECa table (dt independent)
-  double *vm;                    // the caller's Vm [V], device or page-locked host memory: read and
-                                 // written once per macro step (as a compensated pair in between)
-  int vm_device;                 // vm is device memory with a 16-byte aligned base (L2 prefetch)
+  // Vm [V], one of two forms: the caller's FP64 array in page-locked host memory, read and
+  // written once per macro step (vm != nullptr), or device FP32 planes holding the compensated
+  // pair (vm_hi, vm_lo; split from and joined into the caller's array once per call)
+  double *vm;
+  float *vm_hi, *vm_lo;
   SurNorm norm;
   const __nv_bfloat16 *w1, *w2, *w3;  // BF16 network: W1 [128][32], W2 [128][128], W3 [32][128]
   const float *bias;             // b1 [128], b2 [128], b3 [32]
@@ -73,7 +75,8 @@ constexpr int kSnapPlanes = 21 + 2 + 6 + 1;
 
 struct SurPlainArgs {
   DevBatch fine;
-  double *vm;                    // as SurKernelArgs::vm
+  double *vm;                    // as SurKernelArgs
+  float *vm_hi, *vm_lo;
   const int *list;
   const unsigned int *n_list;
   int substeps;
