@@ -476,27 +476,6 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     __syncwarp();
     if (lane < kTcStageVars) bulk_g2s(stage + lane * kTcCells, fb.s32 + lane * ld + c0, kTcCells * 4u, &bar_stage[g]);
   };
-  // The block's tile two rounds of grabs after `tile` goes to L2 ahead of its stage copy and its
-  // Vm and conductance loads (lane v: state plane v, then the Vm planes and the per-cell
-  // conductances; whole 16-byte chunks inside each array). Issued by the group's second warp:
-  // the first issues the stage copies and the MMAs.
-  auto prefetch_ahead = [&](int tile) {
-    const int ahead = tile + 2 * kGroups * (int)gridDim.x;
-    if (ahead >= n_tiles) return;
-    const int64_t c0 = (int64_t)ahead * kTcCells;
-    const int64_t cells = min((int64_t)kTcCells, (int64_t)n - c0);
-    if (lane < kTcStageVars) {
-      bulk_prefetch_l2(fb.s32 + lane * ld + c0, kTcCells * 4u);
-    } else if (lane == kTcStageVars) {  // the device Vm planes (hi, then lo)
-      if (!a.vm) {
-        bulk_prefetch_l2(a.vm_hi + c0, kTcCells * 4u);
-        bulk_prefetch_l2(a.vm_lo + c0, kTcCells * 4u);
-      }
-    } else if (lane < kTcStageVars + 4) {
-      const float *h = het[lane == kTcStageVars + 1 ? H2_g_Na : (lane == kTcStageVars + 2 ? H2_g_Kr : H2_g_K1)];
-      if (h && cells * 4 >= 16) bulk_prefetch_l2(h + c0, (uint32_t)((cells * 4) & ~15));
-    }
-  };
   const bool issuer = (threadIdx.x & 127) < 32;  // the group's first warp
   auto next_tile = [&]() {  // the issuing warp takes the group's next tile and starts its copies
     int tn = 0;
@@ -575,9 +554,8 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     umma::fence_before_sync();
     group_sync(g);
   };
-  const bool prefetcher = (threadIdx.x & 127) >= 32 && (threadIdx.x & 127) < 64;  // the group's second warp
+  int t_next = n_tiles;
   while (t < n_tiles) {
-    if (prefetcher) prefetch_ahead(t);
     const int c = t * kTcCells + r;
     const bool valid = c < n;
     // loads that do not come through the stage go first: their latency overlaps the stage wait
@@ -658,6 +636,9 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       wait_mma();
       tc_hidden_epilogue(tacc, act, r);
       operands_ready();
+      // the issuing warp wrote the group's next tile index before it reached this barrier (and
+      // writes the one after only past the next tile's first barrier, which this warp must reach)
+      t_next = s_tile[g];
       if (leader) {  // layer 2: D = H1 W2^T, K = 128
         umma::fence_after_sync();
         constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
@@ -743,8 +724,12 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     if (listed) a.fallback[slot] = c;
     warp_count(a.n_fallback_total, listed, lane);
     warp_count(a.n_sur, took, lane);
-    group_sync(g);  // the leader's next tile index is visible
-    t = s_tile[g];
+    if (mlp_on) {
+      t = t_next;
+    } else {
+      group_sync(g);  // the issuing warp's next tile index is visible
+      t = s_tile[g];
+    }
   }
   umma::fence_before_sync();
   __syncthreads();
