@@ -131,9 +131,10 @@ SUR_BYTES_PER_CELL = 2 * (21 * 4 + 2 * 4) + 3 * 4
 SUR_PLAIN_BYTES_PER_LISTED_CELL = 10 * SUR_BYTES_PER_CELL + 4
 # MLP FLOPs per cell of one macro step on the tensor core (padded shapes 32-128-128-32)
 SUR_MLP_FLOPS_PER_CELL = 2 * (128 * 32 + 128 * 128 + 32 * 128)
-# ncu: DRAM bytes of one macro-step launch over 1,048,576
-# cells at steady state, scaled by cells
-SUR_STEP_TRAFFIC_PER_CELL = (110_488_832 + 37_235_712) / 1_048_576
+# ncu: dram__bytes_read + dram__bytes_write of one macro-step launch over 4,194,304 cells (state
+# 0.8 GB, six times the L2) on a plateau step, per cell: 0.94 of the algorithmic 196 B (the last
+# tiles' writes are still in L2 when the launch ends); scaled by cells
+SUR_STEP_TRAFFIC_PER_CELL = (441_412_864 + 330_322_944) / 4_194_304
 
 
 def dist_env():
@@ -559,7 +560,8 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
                      "unit": "GB/s", "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": algo,
                      "traffic": SUR_STEP_TRAFFIC_PER_CELL * FULL_CELLS,
-                     "traffic_note": "ncu DRAM bytes of one 1,048,576-cell launch, scaled by cells",
+                     "traffic_note": "ncu DRAM read+write bytes of one 4,194,304-cell launch on a plateau step, "
+                                     "scaled by cells: 0.94 of the algorithmic bytes",
                      "tensor": {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s", "frac": tflops / tpk,
                                 "peak_kind": tpk_kind, "flops_per_launch": FULL_CELLS * SUR_MLP_FLOPS_PER_CELL},
                      "bound_note": "issue-bound: neither HBM nor the tensor pipe limits this kernel"},
