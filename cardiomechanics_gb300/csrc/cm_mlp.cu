@@ -1,5 +1,5 @@
 // The surrogate's MLP (n_in -> H -> H -> n_out, tanh): BF16 operands with FP32 accumulation on
-// the tensor cores (mma.sync m16n8k16), FP32 master weights and Adam. Training runs as a
+// the tcgen05 tensor cores (accumulators in tensor memory), FP32 master weights and Adam. Training runs as a
 // sequence of small GEMMs with fused epilogues:
 //   forward   Z1 = X W1^T + b1, H1 = tanh Z1;  Z2 = H1 W2^T + b2, H2 = tanh Z2;  Y = H2 W3^T + b3
 //   loss      L = mean over samples and real outputs of (Y - T)^2, dY = dL/dY (padding masked)
@@ -16,21 +16,13 @@
 #include <cstdint>
 #include <vector>
 
+#include "cm_bulk.cuh"
 #include "cm_mlp.h"
+#include "cm_umma.cuh"
 
 namespace cm {
 
 namespace {
-
-__device__ __forceinline__ uint32_t ld_u32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 // tanh of two FP32 values as one packed BF16 pair (tanh.approx.bf16x2), low half = x
 __device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
@@ -50,96 +42,114 @@ struct EpiArgs {
   int ldc;
 };
 
-// C = A B^T, A: M x K (lda), B: N x K (ldb), K % 32 == 0. 64x64 block tile, 4 warps of 32x32.
-// gridDim.z > 1 (EPI_F32 only): block z sums k in [z K / gridDim.z, (z + 1) K / gridDim.z) and
-// writes its partial product to the z-th M x ldc slice of out_f32 (split K).
-template <int EPI>
-__global__ void __launch_bounds__(128) gemm_nt(const __nv_bfloat16 *__restrict__ A, int lda,
+// The products on the tcgen05 tensor core: C = A B^T over K-major BF16 rows in global
+// memory. A block of 128 threads owns a 128-row tile of C and up to 128 of its columns; K is
+// staged slice by slice (kTcKs at a time) into shared memory in the tensor core's K-major,
+// no-swizzle layout (the learned macro step's; checked by cm_diag_umma_tile), one thread issues
+// the slice's MMAs into a tensor-memory accumulator and commits them to an mbarrier, and after
+// the last slice each thread reads its row back (tcgen05.ld: thread i = row i = TMEM lane i) into
+// the epilogue. gridDim.z > 1 (EPI_F32): split K, one partial product per z slice of out_f32.
+// kTrans (EPI_F32): the block computes C^T's tile and stores it transposed, for products whose
+// own M is below 128 (dW3 = dY^T H2 as (H2^T dY)^T). Waits are bounded; a timeout sets *err.
+constexpr int kTcKs = 64;
+
+template <int EPI, bool kTrans>
+__global__ void __launch_bounds__(128) gemm_tc(const __nv_bfloat16 *__restrict__ A, int lda,
                                                const __nv_bfloat16 *__restrict__ B, int ldb, int M, int N, int K,
-                                               EpiArgs e) {
-  constexpr int BM = 64, BN = 64, BK = 32, LDS = BK + 8;
-  __shared__ __align__(16) __nv_bfloat16 As[BM][LDS];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN][LDS];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, t = lane & 3;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  float acc[2][4][4] = {};
-  const int kc = K / (int)gridDim.z;  // a multiple of BK (the launcher checks)
-  const int kbeg = (int)blockIdx.z * kc, kend = kbeg + kc;
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    // 64 rows x 32 bf16 = 4 chunks of 16 B per row; 256 chunks per operand, 2 per thread
-    for (int i = tid; i < 256; i += 128) {
-      const int r = i >> 2, cc = (i & 3) * 8;
-      uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-      if (m0 + r < M) va = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * lda + k0 + cc);
-      if (n0 + r < N) vb = *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + r) * ldb + k0 + cc);
-      *reinterpret_cast<uint4 *>(&As[r][cc]) = va;
-      *reinterpret_cast<uint4 *>(&Bs[r][cc]) = vb;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
-#pragma unroll
-      for (int mi = 0; mi < 2; mi++) {
-        const int r = wm + mi * 16 + g;
-        af[mi][0] = ld_u32(&As[r][kk + 2 * t]);
-        af[mi][1] = ld_u32(&As[r + 8][kk + 2 * t]);
-        af[mi][2] = ld_u32(&As[r][kk + 2 * t + 8]);
-        af[mi][3] = ld_u32(&As[r + 8][kk + 2 * t + 8]);
-      }
-#pragma unroll
-      for (int ni = 0; ni < 4; ni++) {
-        const int c = wn + ni * 8 + g;
-        bfr[ni][0] = ld_u32(&Bs[c][kk + 2 * t]);
-        bfr[ni][1] = ld_u32(&Bs[c][kk + 2 * t + 8]);
-      }
-#pragma unroll
-      for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++) mma_bf16(acc[mi][ni], af[mi], bfr[ni]);
-    }
-    __syncthreads();
+                                               EpiArgs e, unsigned int *err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tslot;
+  __nv_bfloat16 *sA = (__nv_bfloat16 *)smem;
+  __nv_bfloat16 *sB = sA + 128 * kTcKs;
+  const int warp = threadIdx.x >> 5;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+  const int nt = min(128, N - n0);                                   // columns of this tile
+  const uint32_t ncols = nt <= 32 ? 32u : (nt <= 64 ? 64u : 128u);   // MMA N = TMEM columns
+  const int kc = K / (int)gridDim.z, kbeg = (int)blockIdx.z * kc, kend = kbeg + kc;
+  const int ks = kc % kTcKs == 0 ? kTcKs : 32;                        // kc is a multiple of 32
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (EPI == EPI_BIAS_TANH) {  // column pairs: one packed BF16 tanh per pair, as in inference
+  if (warp == 0) umma::tmem_alloc(&tslot, ncols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = tslot;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int chunks = ks / 8;  // 16-byte chunks of a staged row
+  for (int k0 = kbeg; k0 < kend && ok; k0 += ks) {
+    for (int i = threadIdx.x; i < 128 * chunks; i += 128) {
+      const int r = i / chunks, c = i - r * chunks;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (m0 + r < M) v = *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + r) * lda + k0 + 8 * c);
+      *reinterpret_cast<uint4 *>(sA + umma::kmajor_index(r, 8 * c, ks)) = v;
+    }
+    for (int i = threadIdx.x; i < (int)ncols * chunks; i += 128) {
+      const int r = i / chunks, c = i - r * chunks;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r < nt) v = *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + r) * ldb + k0 + 8 * c);
+      *reinterpret_cast<uint4 *>(sB + umma::kmajor_index(r, 8 * c, ks)) = v;
+    }
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (threadIdx.x == 0) {
+      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB), sbo = (uint32_t)(ks / 8) * 128u;
+      const uint32_t idesc = umma::idesc_bf16_f32(128, (int)ncols);
+      for (int st = 0; st < ks / 16; st++)
+        umma::mma_bf16(tmem, umma::smem_desc(a0 + st * 256u, 128u, sbo), umma::smem_desc(b0 + st * 256u, 128u, sbo),
+                       idesc, (k0 > kbeg || st > 0) ? 1u : 0u);
+      umma::commit(&bar);
+    }
+    // the slice's MMAs are complete: their sums are in TMEM and the stage may be rewritten
+    ok = __syncthreads_and(mbar_wait(&bar, phase) ? 1 : 0) != 0;
+    phase ^= 1u;
+    umma::fence_after_sync();
+  }
+  if (ok) {
+    const int m = m0 + warp * 32 + (int)(threadIdx.x & 31);  // this thread's row = TMEM lane
+    for (int c0 = 0; c0 < nt; c0 += 32) {
+      float v[32];
+      umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (m >= M) continue;
 #pragma unroll
-    for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-      for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const int m = m0 + wm + mi * 16 + g + h * 8;
-          const int n = n0 + wn + ni * 8 + 2 * t;
-          if (m >= M || n >= N) continue;  // N is even, so n + 1 < N too
-          // hidden biases in BF16, as the inference kernel feeds them to the tensor core
+      for (int j = 0; j < 32; j += 2) {
+        const int n = n0 + c0 + j;
+        if (n >= N) break;  // N is a multiple of 32: pairs never straddle it
+        if (EPI == EPI_BIAS_TANH) {  // hidden biases in BF16, as the inference kernel feeds them
           const float b0 = __bfloat162float(__float2bfloat16(e.bias[n]));
           const float b1 = __bfloat162float(__float2bfloat16(e.bias[n + 1]));
-          *reinterpret_cast<uint32_t *>(e.out_bf16 + (size_t)m * e.ldc + n) =
-              tanh2_bf16(acc[mi][ni][2 * h] + b0, acc[mi][ni][2 * h + 1] + b1);
-        }
-    return;
-  }
-#pragma unroll
-  for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-    for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int m = m0 + wm + mi * 16 + g + (q >> 1) * 8;
-        const int n = n0 + wn + ni * 8 + 2 * t + (q & 1);
-        if (m >= M || n >= N) continue;
-        float v = acc[mi][ni][q];
-        const size_t o = (size_t)m * e.ldc + n;
-        if (EPI == EPI_BIAS_F32) {
-          e.out_f32[o] = v + e.bias[n];
-        } else if (EPI == EPI_DTANH) {
-          const float h = __bfloat162float(e.h[o]);
-          e.out_bf16[o] = __float2bfloat16(v * (1.f - h * h));
+          *reinterpret_cast<uint32_t *>(e.out_bf16 + (size_t)m * e.ldc + n) = tanh2_bf16(v[j] + b0, v[j + 1] + b1);
         } else {
-          e.out_f32[(size_t)blockIdx.z * (size_t)M * e.ldc + o] = v;
+#pragma unroll
+          for (int q = 0; q < 2; q++) {
+            const int nn = n + q;
+            if (EPI == EPI_BIAS_F32) {
+              e.out_f32[(size_t)m * e.ldc + nn] = v[j + q] + e.bias[nn];
+            } else if (EPI == EPI_DTANH) {
+              const size_t o = (size_t)m * e.ldc + nn;
+              const float h = __bfloat162float(e.h[o]);
+              e.out_bf16[o] = __float2bfloat16(v[j + q] * (1.f - h * h));
+            } else if (kTrans) {  // C^T's element (m, nn) is C's (nn, m); C has N rows
+              e.out_f32[(size_t)blockIdx.z * (size_t)N * e.ldc + (size_t)nn * e.ldc + m] = v[j + q];
+            } else {
+              e.out_f32[(size_t)blockIdx.z * (size_t)M * e.ldc + (size_t)m * e.ldc + nn] = v[j + q];
+            }
+          }
         }
       }
+    }
+  } else {
+    if (threadIdx.x == 0) atomicOr(err, 1u);
+    mbar_wait(&bar, phase ^ 1u);  // the slice that ran out: one more bounded wait before TMEM is freed
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_free(tmem, ncols);
 }
 
 // out[c][r] = in[r][c] for a rows x cols BF16 matrix.
@@ -256,26 +266,31 @@ __global__ void gather_rows(const float *__restrict__ X, const float *__restrict
   for (int c = threadIdx.x; c < n_out; c += blockDim.x) Tb[(size_t)r * n_out + c] = T[s * n_out + c];
 }
 
-template <int EPI>
-cudaError_t gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, EpiArgs e,
-                 cudaStream_t s) {
-  dim3 grid((N + 63) / 64, (M + 63) / 64);
-  gemm_nt<EPI><<<grid, 128, 0, s>>>(A, lda, B, ldb, M, N, K, e);
+// C = A B^T on the tcgen05 tensor core (gemm_tc); rows of A and B 16-byte aligned, N a multiple
+// of 32, K a multiple of 32 * splits.
+template <int EPI, bool kTrans = false>
+cudaError_t gemm_tcgen05(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
+                         EpiArgs e, int splits, unsigned int *err, cudaStream_t s) {
+  if (splits < 1 || K % (32 * splits) || lda % 8 || ldb % 8 || N % 32) return cudaErrorInvalidValue;
+  dim3 grid((N + 127) / 128, (M + 127) / 128, splits);
+  gemm_tc<EPI, kTrans><<<grid, 128, 2 * 128 * kTcKs * sizeof(__nv_bfloat16), s>>>(A, lda, B, ldb, M, N, K, e, err);
   return cudaGetLastError();
 }
 
 // C (M x ldc, FP32) = A B^T with K split over `splits` blocks per tile (weight gradients: K = the
-// minibatch rows, M and N at most 128), partial products in `part`, summed in split order.
+// minibatch rows, M and N at most 128), partial products in `part`, summed in split order. A
+// product with fewer than 128 rows but more columns is computed as its transpose (a full
+// 128-row tensor-core tile) and stored transposed.
 cudaError_t gemm_f32_split(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
-                           float *C, int ldc, float *part, int splits, cudaStream_t s) {
+                           float *C, int ldc, float *part, int splits, unsigned int *tc_err, cudaStream_t s) {
   splits = std::min(splits, (int)(kPartFloats / ((size_t)M * ldc)));
   if (splits < 1 || K % (32 * splits)) splits = 1;
   EpiArgs e{};
   e.out_f32 = splits > 1 ? part : C;
   e.ldc = ldc;
-  dim3 grid((N + 63) / 64, (M + 63) / 64, splits);
-  gemm_nt<EPI_F32><<<grid, 128, 0, s>>>(A, lda, B, ldb, M, N, K, e);
-  cudaError_t err = cudaGetLastError();
+  cudaError_t err = M < 128 && N > M
+                        ? gemm_tcgen05<EPI_F32, true>(B, ldb, A, lda, N, M, K, e, splits, tc_err, s)
+                        : gemm_tcgen05<EPI_F32, false>(A, lda, B, ldb, M, N, K, e, splits, tc_err, s);
   if (err != cudaSuccess || splits == 1) return err;
   const int n = M * ldc;
   sum_parts<<<(n + 255) / 256, 256, 0, s>>>(part, splits, n, C);
@@ -331,6 +346,8 @@ cudaError_t Mlp::init(int n_in_, int n_hidden_, int n_out_, uint64_t seed, cudaS
   MCK(cudaMalloc(&wt, n_params * sizeof(__nv_bfloat16)));
   MCK(cudaMalloc(&loss, (1 + kMseBlocks) * sizeof(float)));
   MCK(cudaMalloc(&part, kPartFloats * sizeof(float)));
+  MCK(cudaMalloc(&tc_err, sizeof(unsigned int)));
+  MCK(cudaMemsetAsync(tc_err, 0, sizeof(unsigned int), stream));
   return reset(seed);
 }
 
@@ -374,9 +391,10 @@ cudaError_t Mlp::sync_bf16() {
 
 void Mlp::release() {
   for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)wt, (void *)loss, (void *)ws,
-                  (void *)part})
+                  (void *)part, (void *)tc_err})
     cudaFree(p);
   part = nullptr;
+  tc_err = nullptr;
   w = g = m1 = m2 = nullptr;
   wb = wt = nullptr;
   loss = nullptr;
@@ -429,15 +447,24 @@ cudaError_t Mlp::forward_rows(const Buffers &B, int rows) {
   e.bias = w + off[1];
   e.out_bf16 = B.H1;
   e.ldc = H;
-  MCK(gemm<EPI_BIAS_TANH>(B.X, in_pad, wb + off[0], in_pad, rows, H, in_pad, e, stream));
+  MCK(gemm_tcgen05<EPI_BIAS_TANH>(B.X, in_pad, wb + off[0], in_pad, rows, H, in_pad, e, 1, tc_err, stream));
   e.bias = w + off[3];
   e.out_bf16 = B.H2;
-  MCK(gemm<EPI_BIAS_TANH>(B.H1, H, wb + off[2], H, rows, H, H, e, stream));
+  MCK(gemm_tcgen05<EPI_BIAS_TANH>(B.H1, H, wb + off[2], H, rows, H, H, e, 1, tc_err, stream));
   EpiArgs e3{};
   e3.bias = w + off[5];
   e3.out_f32 = B.Y;
   e3.ldc = out_pad;
-  return gemm<EPI_BIAS_F32>(B.H2, H, wb + off[4], H, rows, out_pad, H, e3, stream);
+  return gemm_tcgen05<EPI_BIAS_F32>(B.H2, H, wb + off[4], H, rows, out_pad, H, e3, 1, tc_err, stream);
+}
+
+cudaError_t Mlp::check_tc() {
+  unsigned int h = 0;
+  MCK(cudaMemcpyAsync(&h, tc_err, sizeof(h), cudaMemcpyDeviceToHost, stream));
+  MCK(cudaStreamSynchronize(stream));
+  if (!h) return cudaSuccess;
+  MCK(cudaMemsetAsync(tc_err, 0, sizeof(unsigned int), stream));
+  return cudaErrorLaunchTimeout;
 }
 
 cudaError_t Mlp::forward(const float *X, int64_t n, float *Y) {
@@ -450,7 +477,7 @@ cudaError_t Mlp::forward(const float *X, int64_t n, float *Y) {
   // Y (rows x out_pad) -> caller's n x n_out
   MCK(cudaMemcpy2DAsync(Y, n_out * sizeof(float), B.Y, out_pad * sizeof(float), n_out * sizeof(float), n,
                         cudaMemcpyDeviceToDevice, stream));
-  return cudaSuccess;
+  return check_tc();
 }
 
 size_t Mlp::forward_scratch_bytes_per_row() const {
@@ -470,7 +497,7 @@ cudaError_t Mlp::forward_in_scratch(void *scratch, const float *X, int64_t n, fl
   MCK(forward_rows(B, rows));
   MCK(cudaMemcpy2DAsync(Y, n_out * sizeof(float), B.Y, out_pad * sizeof(float), n_out * sizeof(float), n,
                         cudaMemcpyDeviceToDevice, stream));
-  return cudaSuccess;
+  return check_tc();
 }
 
 cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
@@ -489,10 +516,10 @@ cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
   e.out_bf16 = B.dZ2;
   e.h = B.H2;
   e.ldc = H;
-  MCK(gemm<EPI_DTANH>(B.dY, out_pad, wt + off[4], out_pad, rows, H, out_pad, e, stream));
+  MCK(gemm_tcgen05<EPI_DTANH>(B.dY, out_pad, wt + off[4], out_pad, rows, H, out_pad, e, 1, tc_err, stream));
   e.out_bf16 = B.dZ1;
   e.h = B.H1;
-  MCK(gemm<EPI_DTANH>(B.dZ2, H, wt + off[2], H, rows, H, H, e, stream));
+  MCK(gemm_tcgen05<EPI_DTANH>(B.dZ2, H, wt + off[2], H, rows, H, H, e, 1, tc_err, stream));
   // weight gradients: dW = dZ^T A_prev, K = rows
   MCK(transpose(B.dY, B.dYT, rows, out_pad, stream));
   MCK(transpose(B.H2, B.H2T, rows, H, stream));
@@ -501,9 +528,9 @@ cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
   MCK(transpose(B.dZ1, B.dZ1T, rows, H, stream));
   MCK(transpose(B.X, B.XT, rows, in_pad, stream));
   const int splits = rows >= 512 ? std::min(kMaxSplits, rows / 256) : 1;
-  MCK(gemm_f32_split(B.dYT, rows, B.H2T, rows, out_pad, H, rows, g + off[4], H, part, splits, stream));
-  MCK(gemm_f32_split(B.dZ2T, rows, B.H1T, rows, H, H, rows, g + off[2], H, part, splits, stream));
-  MCK(gemm_f32_split(B.dZ1T, rows, B.XT, rows, H, in_pad, rows, g + off[0], in_pad, part, splits, stream));
+  MCK(gemm_f32_split(B.dYT, rows, B.H2T, rows, out_pad, H, rows, g + off[4], H, part, splits, tc_err, stream));
+  MCK(gemm_f32_split(B.dZ2T, rows, B.H1T, rows, H, H, rows, g + off[2], H, part, splits, tc_err, stream));
+  MCK(gemm_f32_split(B.dZ1T, rows, B.XT, rows, H, in_pad, rows, g + off[0], in_pad, part, splits, tc_err, stream));
   MCK(colsum(B.dY, rows, out_pad, g + off[5], part, stream));
   MCK(colsum(B.dZ2, rows, H, g + off[3], part, stream));
   MCK(colsum(B.dZ1, rows, H, g + off[1], part, stream));
@@ -559,6 +586,7 @@ cudaError_t Mlp::train(const float *X, const float *T, int64_t n, int batch, int
   }
   cudaFree(idx);
   if (final_loss) *final_loss = lcnt ? lsum / lcnt : 0.f;
+  if (err == cudaSuccess) err = check_tc();
   return err;
 }
 

@@ -19,6 +19,9 @@ struct Mlp {
   float *loss = nullptr;
   void *ws = nullptr;
   float *part = nullptr;  // partial sums of the split weight-gradient GEMMs and column sums
+  unsigned int *tc_err = nullptr;  // set by a tensor-core GEMM whose bounded wait ran out
+  // cudaErrorLaunchTimeout if a tensor-core GEMM since the last check ran out of its wait
+  cudaError_t check_tc();
   int ws_rows = 0;
   int step = 0;
 

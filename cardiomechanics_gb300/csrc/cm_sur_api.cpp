@@ -336,7 +336,7 @@ int cm_mlp_loss_grad(cm_mlp_t m, const float *X, const float *T, int64_t n, floa
   cudaError_t e = m->m.loss_grad(dX, dT, n);
   float l = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&l, m->m.loss, sizeof(float), cudaMemcpyDeviceToHost, m->m.stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(m->m.stream);
+  if (e == cudaSuccess) e = m->m.check_tc();
   cudaFree(o1);
   cudaFree(o2);
   if (e != cudaSuccess) return cuda_fail(e, "cm_mlp_loss_grad");
