@@ -183,13 +183,15 @@ int cm_batch_set_cell(cm_batch_t b, int64_t cell, int layout, const double *in);
 int cm_batch_calc_cell(cm_batch_t b, int64_t cell, double dt, double V, double i_ext, double stretch, double *dV);
 /* Column names after "t" and "V_m" of vbElphyModel::Print (long_form 0) or LongPrint (1), as
  * GetParameterNames / GetLongParameterNames give them (TenTusscher2.cpp:959-999,
- * CourtemancheEtAl.cpp:241-265). Returns the count; names (NULL: count only) receive static
- * strings. TenTusscher2 and Courtemanche; other models give CM_ERR_UNSUPPORTED. */
+ * CourtemancheEtAl.cpp:241-265, OHaraRudy.cpp:693-740, Tomek.cpp:686-733). Returns the count;
+ * names (NULL: count only) receive static strings. */
 int cm_model_print_names(int model, int long_form, const char **names, int cap);
-/* The same columns' values for one cell at membrane voltage V [V] (Print: TenTusscher2.cpp:
- * 908-957, CourtemancheEtAl.cpp:189-239), as the reference prints them after t and V. Stored
- * currents (TT2 Array[0..16], Courtemanche I_SAC) are those of the last step of an FP64 batch
- * with diagnostics on (cm_batch_set_diagnostics), else 0. Returns the count. */
+/* The same columns' values for one cell at membrane voltage V [V] (Print / LongPrint:
+ * TenTusscher2.cpp:908-957, CourtemancheEtAl.cpp:189-239, OHaraRudy.cpp:665-691,
+ * Tomek.cpp:658-684), as the reference prints them after t and V. Stored values (TT2
+ * Array[0..16], Courtemanche I_SAC, the O'Hara-Rudy and Tomek currents and Tomek's I_Na rates)
+ * are those of the last step of an FP64 batch with diagnostics on (cm_batch_set_diagnostics),
+ * else 0. Returns the count. */
 int cm_batch_print_values(cm_batch_t b, int64_t cell, double V, int long_form, double *values, int cap);
 
 /* One Calc for every cell: dVm[c] = Calc(dt, Vm[c], i_ext[c], stretch[c], 1), state updated

@@ -205,13 +205,14 @@ class CellView : public Base {
   double GetKo() override { return nodes_->param("K_o"); }
   int GetSize() override { return nodes_->block_doubles() * (int)sizeof(double); }
   double *GetBase() override { return nodes_->pull_block(cell_); }
-  /* Volume() in m^3 as the models define it: TenTusscher2 Vcell (TenTusscher2.h:197),
-   * Courtemanche Vcell_outside * 1e-18 (CourtemancheEtAl.h:50). */
+  /* Volume() as the models define it: TenTusscher2 Vcell (TenTusscher2.h:197), Courtemanche
+   * Vcell_outside * 1e-18 (CourtemancheEtAl.h:50), O'Hara-Rudy and Tomek the constant of
+   * OHaraRudy.h:65 and Tomek.h:66. */
   double Volume() override {
     const int m = nodes_->info().model;
     if (m == CM_MODEL_TENTUSSCHER2) return nodes_->param("Vcell");
     if (m == CM_MODEL_COURTEMANCHE) return nodes_->param("Vcell_outside") * 1e-18;
-    throw Error("Volume: not provided for this model by the view");
+    return 1.15606568e-12;
   }
   double GetAmplitude() override { return nodes_->info().amplitude; }
   double GetStimTime() override { return nodes_->info().stim_time; }

@@ -185,6 +185,43 @@ int main() {
   }
   cm_batch_destroy(bc);
   cm_params_destroy(pc);
+
+  // O'Hara-Rudy (12) and Tomek (14), FP64 with the stored values on: LongPrint has the
+  // reference's column count, the state columns read back as the view's getters, the stored
+  // currents are those of the last Calc (non-zero after a stimulated step)
+  const int models[2] = {12, 14};
+  const size_t want[2] = {2 + 41 + 17, 2 + 48 + 33};
+  for (int q = 0; q < 2; q++) {
+    cm_params_t po;
+    cm_batch_t bo;
+    CHECK(cm_params_create(&po, models[q], nullptr, dt) == 0 && cm_batch_create(&bo, po, 1, CM_PREC_FP64, nullptr) == 0,
+          "%s", cm_last_error());
+    cm_batch_set_diagnostics(bo, 1);
+    auto onodes = std::make_shared<cmgb::BatchNodes>(po, bo);
+    View ov(onodes, 0);
+    double vo = ov.GetVm();
+    for (int st = 0; st < 200; st++) vo += ov.Calc(dt, vo, st < 100 ? -53.0 : 0.0, 1.0, 1);
+    std::vector<std::string> on{"t", "V_m"};
+    ov.GetLongParameterNames(on);
+    CHECK(on.size() == want[q] && on[2] == "m" && on.back() == "I_SAC", "model %d names (%zu)", models[q], on.size());
+    std::ostringstream oss;
+    ov.LongPrint(oss, 0.002, vo);
+    std::istringstream iss(oss.str());
+    std::vector<double> oc;
+    while (iss >> x) oc.push_back(x);
+    CHECK(oc.size() == on.size(), "model %d LongPrint columns %zu", models[q], oc.size());
+    if (oc.size() == on.size()) {
+      int nai = -1;
+      for (size_t k = 0; k < on.size(); k++)
+        if (on[k] == "Na_i") nai = (int)k;
+      CHECK(nai > 0 && std::fabs(oc[nai] - ov.GetNai()) <= 1e-5 * ov.GetNai(), "model %d Na_i column", models[q]);
+      double stored = 0;
+      for (size_t k = on.size() - 5; k < on.size(); k++) stored += std::fabs(oc[k]);
+      CHECK(stored > 0, "model %d stored currents are zero", models[q]);
+    }
+    cm_batch_destroy(bo);
+    cm_params_destroy(po);
+  }
   cm_batch_destroy(b);
   cm_batch_destroy(ref);
   cm_params_destroy(p);
