@@ -49,7 +49,8 @@ ABI_SYMBOLS = (
     "cm_batch_step_update_act",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
-    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check",
+    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check", "cm_model_print_names", "cm_batch_print_values",
+    "cm_batch_get_cell", "cm_batch_set_cell", "cm_batch_calc_cell",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
     "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
     "cm_mlp_get_grads", "cm_mlp_forward", "cm_mlp_loss_grad", "cm_mlp_adam_step", "cm_surrogate_create",
@@ -185,6 +186,11 @@ def lib() -> ctypes.CDLL:
     L.cm_diag_umma_tile.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
     L.cm_diag_mlp_workspace_rows.argtypes = [vp, ctypes.POINTER(i64)]
     L.cm_diag_batch_wait_check.argtypes = [vp, i64, ctypes.c_uint32]
+    L.cm_model_print_names.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int]
+    L.cm_batch_print_values.argtypes = [vp, i64, ctypes.c_double, ctypes.c_int, dp, ctypes.c_int]
+    L.cm_batch_get_cell.argtypes = [vp, i64, ctypes.c_int, dp]
+    L.cm_batch_set_cell.argtypes = [vp, i64, ctypes.c_int, dp]
+    L.cm_batch_calc_cell.argtypes = [vp, i64, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
     _lib = L
     return L
 

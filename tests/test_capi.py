@@ -189,3 +189,21 @@ def test_ap_markers_on_synthetic_trace():
     assert abs(apd[0] - (t90 - tu[0])) < 1e-9
     tu2, apd2, _ = A.ap_markers(np.full((1, 100), -0.08), dt, 0.0)
     assert np.isnan(tu2[0]) and np.isnan(apd2[0])
+
+
+def test_print_columns(cmlib):
+    """Print / LongPrint column names of the four models, in the reference's order and count
+    (GetParameterNames / GetLongParameterNames): the per-node view and GetResVal rely on them."""
+    import ctypes
+    L = cmlib.lib()
+    want = {5: (19, 17, "m", "I_tot"), 2: (21, 19, "m", "I_SAC"), 12: (41, 17, "m", "I_SAC"),
+            14: (48, 33, "m", "I_SAC")}
+    for model, (n_short, n_long, first, last) in want.items():
+        assert L.cm_model_print_names(model, 0, None, 0) == n_short
+        n = L.cm_model_print_names(model, 1, None, 0)
+        assert n == n_short + n_long
+        names = (ctypes.c_char_p * n)()
+        assert L.cm_model_print_names(model, 1, names, n) == n
+        got = [x.decode() for x in names]
+        assert got[0] == first and got[-1] == last and len(set(got)) == n, (model, got)
+    assert L.cm_model_print_names(13, 0, None, 0) < 0
