@@ -49,7 +49,7 @@ ABI_SYMBOLS = (
     "cm_batch_step_update_act",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
-    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check", "cm_model_print_names", "cm_batch_print_values",
+    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check", "cm_diag_fp64_math", "cm_model_print_names", "cm_batch_print_values",
     "cm_batch_get_cell", "cm_batch_set_cell", "cm_batch_calc_cell",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
     "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
@@ -186,6 +186,7 @@ def lib() -> ctypes.CDLL:
     L.cm_diag_umma_tile.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]
     L.cm_diag_mlp_workspace_rows.argtypes = [vp, ctypes.POINTER(i64)]
     L.cm_diag_batch_wait_check.argtypes = [vp, i64, ctypes.c_uint32]
+    L.cm_diag_fp64_math.argtypes = [vp, vp, i64, vp, vp]
     L.cm_model_print_names.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int]
     L.cm_batch_print_values.argtypes = [vp, i64, ctypes.c_double, ctypes.c_int, dp, ctypes.c_int]
     L.cm_batch_get_cell.argtypes = [vp, i64, ctypes.c_int, dp]
@@ -236,6 +237,19 @@ def fma_peak_tflops(fp64: bool, stream=None) -> float:
     v = ctypes.c_double()
     _check(lib().cm_diag_fma_peak(int(fp64), ctypes.byref(v), None if stream is None else ctypes.c_void_p(int(stream))))
     return v.value
+
+
+def fp64_math(x, y):
+    """The FP64 cell-model steps' exp(x), log(y) and x / y beside the CUDA library's, for float64
+    CUDA tensors x, y of one length: returns a (6, n) float64 numpy array, rows exp64, log64,
+    div64, exp, log, division."""
+    if x.shape != y.shape or str(x.dtype) != "torch.float64" or str(y.dtype) != "torch.float64" \
+            or not x.is_cuda or not y.is_cuda:
+        raise ValueError("fp64_math: x and y must be float64 CUDA tensors of one shape")
+    x, y = x.contiguous(), y.contiguous()
+    out = x.new_empty((x.numel(), 6))
+    _check(lib().cm_diag_fp64_math(_ptr(x), _ptr(y), x.numel(), _ptr(out), None))
+    return out.cpu().numpy().T.copy()
 
 
 def model_info(model: int) -> Info:

@@ -16,7 +16,7 @@ __device__ __forceinline__ double stim_for_cell(const StepIO &io, int64_t c) {
   if (io.tb_cell) {
     const double tb = io.tb_cell[c];
     double i_ext = 0.0;
-    if (io.t >= tb) {
+    if (f64_ge(io.t, tb)) {  // integer compare: no FP64-pipe instruction per cell
       i_ext = io.amp;
       if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
     }

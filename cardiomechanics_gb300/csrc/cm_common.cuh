@@ -250,14 +250,65 @@ CM_HD void acc_add(Acc &a, float d) {
   a.hi = h;
 }
 
+// Double <-> compensated pair. On the device the conversions are done on the bit patterns with
+// integer instructions: on GB300 every FP64-pipe instruction, conversions included, issues at 2
+// per clock per SM (1/64 of the FP32 rate), so the four conversions and the subtraction of the
+// plain form cost a kernel that reads FP64 Vm every step more than its memory traffic does.
+// acc_from_double gives the plain form's pair (hi = x rounded to FP32, lo = the remainder rounded
+// to FP32) for 2^-74 <= |x| < 2^127, except that a remainder of exactly half an FP32 ulp of x
+// rounds hi away from zero instead of to even; other values take the plain form.
+// acc_to_double widens both halves exactly and adds them once: the plain form's result.
 CM_HD Acc acc_from_double(double x) {
+#ifdef __CUDA_ARCH__
+  const uint32_t hw = (uint32_t)__double2hiint(x), lw = (uint32_t)__double2loint(x);
+  const int E = (int)((hw >> 20) & 0x7ffu);  // biased FP64 exponent
+  if (E >= 949 && E <= 1149) {
+    const uint32_t s = hw & 0x80000000u;
+    const uint32_t lr = lw + 0x10000000u;  // + half an ulp of the 24-bit significand
+    const uint32_t hr = hw + (lr < lw ? 1u : 0u);
+    const uint32_t er = (hr >> 20) & 0x7ffu;  // one more than E where the significand carried out
+    const uint32_t hi = s | ((er - 896u) << 23) | ((hr & 0xfffffu) << 3) | (lr >> 29);
+    // the low 29 significand bits as a signed remainder in [-2^28, 2^28), in units of 2^(E-1075)
+    int rem = ((int)((lw & 0x1fffffffu) << 3)) >> 3;
+    rem = s ? -rem : rem;
+    const float lo = __int2float_rn(rem) * __uint_as_float((uint32_t)(E - 948) << 23);
+    return Acc{__uint_as_float(hi), lo};
+  }
+#endif
   Acc a;
   a.hi = (float)x;
   a.lo = (float)(x - (double)a.hi);
   return a;
 }
 
-CM_HD double acc_to_double(Acc a) { return (double)a.hi + (double)a.lo; }
+// FP32 -> FP64 widening on the bit pattern (exact); zero, inf and NaN included, subnormal
+// inputs take the conversion instruction.
+CM_HD double f32_widen(float f) {
+#ifdef __CUDA_ARCH__
+  const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu, s = u & 0x80000000u, m = u & 0x7fffffu;
+  if (e == 0u && m != 0u) return (double)f;
+  const uint32_t E = e == 0u ? 0u : (e == 255u ? 2047u : e + 896u);
+  return __hiloint2double((int)(s | (E << 20) | (m >> 3)), (int)(m << 29));
+#else
+  return (double)f;
+#endif
+}
+
+CM_HD double acc_to_double(Acc a) { return f32_widen(a.hi) + f32_widen(a.lo); }
+
+// a >= b for non-NaN doubles, on the bit patterns (no FP64 instruction): the sign-magnitude
+// patterns mapped to a two's-complement order; +0 and -0 compare equal.
+CM_HD bool f64_ge(double a, double b) {
+#ifdef __CUDA_ARCH__
+  long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if (((ia | ib) & 0x7fffffffffffffffll) == 0) return true;
+  ia ^= (ia >> 63) & 0x7fffffffffffffffll;
+  ib ^= (ib >> 63) & 0x7fffffffffffffffll;
+  return ia >= ib;
+#else
+  return a >= b;
+#endif
+}
 
 // New free concentration increment of a rapidly buffered species. The reference solves
 // x^2 + b x - c = 0 for the new free value x given total = x_old + B x_old/(x_old+K) + dT

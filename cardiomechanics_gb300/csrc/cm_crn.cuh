@@ -3,6 +3,7 @@
 #pragma once
 
 #include "cm_common.cuh"
+#include "cm_fp64_math.cuh"
 
 namespace cm {
 
@@ -28,12 +29,15 @@ CM_HD R clamp01(R x) {
 CM_HD double crn_calc_fp64(const CRNConsts<double> &C, const double *__restrict__ row, CRNCell<double> &c,
                            double &Ca_up, double &Ca_rel, double &Na_i, double &K_i, const CRNHet_<double> &g,
                            double V, double i_external, double stretch, double &I_SAC_out, uint32_t &audit) {
+  using fp64::ddiv;  // the FP64 exp, log and division of cm_fp64_math.cuh (within 1 ulp)
+  using fp64::dexp;
+  using fp64::dlog;
   const double tinc = C.dt_ms;
   const double V_int = V * 1000.0;
-  const double dNa_i = 1.0 / Na_i;
-  const double VmE_Na = V_int - (C.RTdF * log(C.Na_o * dNa_i));
-  const double VmE_K = V_int - (C.RTdF * log(C.K_o / K_i));
-  const double VmE_Ca = V_int - (C.RTd2F * log(C.Ca_o / c.Ca_i));
+  const double dNa_i = ddiv(1.0, Na_i);
+  const double VmE_Na = V_int - (C.RTdF * dlog(C.Na_o * dNa_i));
+  const double VmE_K = V_int - (C.RTdF * dlog(ddiv(C.K_o, K_i)));
+  const double VmE_Ca = V_int - (C.RTd2F * dlog(ddiv(C.Ca_o, c.Ca_i)));
   c.m = clamp01(row[CR_m_m] + (c.m - row[CR_m_m]) * row[CR_exptau_m]);
   c.h = row[CR_m_h] + (c.h - row[CR_m_h]) * row[CR_exptau_h];
   c.j = row[CR_m_j] + (c.j - row[CR_m_j]) * row[CR_exptau_j];
@@ -45,7 +49,7 @@ CM_HD double crn_calc_fp64(const CRNConsts<double> &C, const double *__restrict_
   c.Xs = row[CR_m_Xs] + (c.Xs - row[CR_m_Xs]) * row[CR_exptau_Xs];
   c.d = row[CR_m_d] + (c.d - row[CR_m_d]) * row[CR_exptau_d];
   c.f = row[CR_m_f] + (c.f - row[CR_m_f]) * row[CR_exptau_f];
-  c.f_Ca += (1.0 / (1.0 + c.Ca_i * 2857.1429) - c.f_Ca) * 0.5 * tinc;
+  c.f_Ca += (ddiv(1.0, 1.0 + c.Ca_i * 2857.1429) - c.f_Ca) * 0.5 * tinc;
   c.w = row[CR_m_w] + (c.w - row[CR_m_w]) * row[CR_exptau_w];
 
   const double I_Na = g.g_Na * c.m * c.m * c.m * c.h * c.j * VmE_Na;
@@ -58,35 +62,35 @@ CM_HD double crn_calc_fp64(const CRNConsts<double> &C, const double *__restrict_
   const double I_bNa = g.g_bNa * VmE_Na;
   const double I_bCa = g.g_bCa * VmE_Ca;
   const double temp = C.k_mNai * dNa_i;
-  const double I_NaK = row[CR_CNaK] / (1.0 + temp * sqrt(temp));
-  const double I_pCa = C.I_pCamax * c.Ca_i / (c.Ca_i + C.k_mpCa);
+  const double I_NaK = ddiv(row[CR_CNaK], 1.0 + temp * sqrt(temp));
+  const double I_pCa = ddiv(C.I_pCamax * c.Ca_i, c.Ca_i + C.k_mpCa);
   const double I_NaCa = row[CR_CNaCa] * ((Na_i * Na_i * Na_i * C.Ca_o) - row[CR_expVm] * c.Ca_i);
   const double I_rel = C.k_rel * c.u * c.u * c.v * c.w * (Ca_rel - c.Ca_i);
-  const double I_up = C.I_upmax * c.Ca_i / (c.Ca_i + C.k_up);
+  const double I_up = ddiv(C.I_upmax * c.Ca_i, c.Ca_i + C.k_up);
   const double I_upleak = C.kupleak * Ca_up;
   const double I_tr = (Ca_up - Ca_rel) * C.dt_tr;
-  double I_SAC = C.G_sac * (V_int - C.E_sac) / (1. + C.K_sac * exp(-C.alpha * (stretch - 1.)));
+  double I_SAC = ddiv(C.G_sac * (V_int - C.E_sac), 1. + C.K_sac * dexp(-C.alpha * (stretch - 1.)));
   I_SAC *= C.ISAC_SWITCH;
   const double Ca_T50 = C.Ca_T50 + C.beta1 * ((stretch < 1.2 ? stretch : 1.2) - 1.);
-  const double x = 1000 * c.Ca_i / Ca_T50;
+  const double x = ddiv(1000 * c.Ca_i, Ca_T50);
   const double px = C.n_TRPN == 2.0 ? x * x : pow(x, C.n_TRPN);
   const double dCaTRPN = C.k_TRPN * (px * (1. - c.Ca_TRPN) - c.Ca_TRPN);
   c.Ca_TRPN += tinc * dCaTRPN;
   Ca_up += tinc * (I_up - I_tr * C.VreldVup - I_upleak);
-  Ca_rel += tinc * ((I_tr - I_rel) / (1.0 + C.csqnkm / (Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn)));
+  Ca_rel += tinc * ddiv(I_tr - I_rel, 1.0 + ddiv(C.csqnkm, Ca_rel * Ca_rel + Ca_rel * C.kmcsqnm2 + C.kkmcsqn));
   Na_i += tinc * (-3.0 * I_NaK - 3.0 * I_NaCa - I_bNa - I_Na) * C.CmdFvi;
   K_i += tinc * (2.0 * I_NaK - I_K1 - I_to - I_Kur - I_Kr - I_Ks) * C.CmdFvi;
   double B1 = ((2.0 * I_NaCa - I_pCa - I_CaL - I_bCa) * .5 * C.CmdFvi) + ((I_upleak - I_up) * C.VupdVi + I_rel * C.VreldVi);
   B1 -= C.TRPNmax * dCaTRPN;
-  const double B2 = 1.0 + (C.cmdnkm / ((c.Ca_i * c.Ca_i) + (c.Ca_i * C.kmcmdnm2) + C.kkmcmdn));
-  const double dCa_i = B1 / B2;
+  const double B2 = 1.0 + ddiv(C.cmdnkm, (c.Ca_i * c.Ca_i) + (c.Ca_i * C.kmcmdnm2) + C.kkmcmdn);
+  const double dCa_i = ddiv(B1, B2);
   c.Ca_i += tinc * dCa_i;
-  const double Fn = exp(-(C.Vrel * I_rel - (0.5 * I_CaL - 0.2 * I_NaCa) * C.Cmd2F) * 731.5289);
-  const double m_u = 1.0 / (1.0 + Fn * C.exp250);
+  const double Fn = dexp(-(C.Vrel * I_rel - (0.5 * I_CaL - 0.2 * I_NaCa) * C.Cmd2F) * 731.5289);
+  const double m_u = ddiv(1.0, 1.0 + Fn * C.exp250);
   c.u += (m_u - c.u) * 0.125 * tinc;
-  const double m_v = 1.0 - 1.0 / (1.0 + Fn * C.exp50);
+  const double m_v = 1.0 - ddiv(1.0, 1.0 + Fn * C.exp50);
   const double t_v = 1.91 + 2.09 * m_u;
-  c.v += (m_v - c.v) * tinc / t_v;
+  c.v += ddiv((m_v - c.v) * tinc, t_v);
   const double I_tot =
       I_Na + I_CaL + I_pCa + I_K1 + I_to + I_Kur + I_Kr + I_Ks + I_bNa + I_bCa + I_NaK + I_NaCa + I_SAC - i_external;
   I_SAC_out = I_SAC;

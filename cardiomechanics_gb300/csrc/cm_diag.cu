@@ -2,11 +2,13 @@
 // GB300 rate the measured copy-bandwidth and GEMM peaks do not give. Each thread runs 8 independent FMA
 // chains (enough to cover the pipe latency at full occupancy); the result is written so the
 // chains are not dead code.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/cardiomech_gb300_diag.h"
 #include "cm_bulk.cuh"
+#include "cm_fp64_math.cuh"
 #include "cm_umma.cuh"
 
 namespace {
@@ -52,6 +54,21 @@ int measure(double *tflops, void *stream, int iters) {
   const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return 0;
+}
+
+// out[6 i + ...]: exp64(x), log64(y), div64(x, y), then the library's exp(x), log(y), x / y
+__global__ void fp64_math_kernel(const double *__restrict__ x, const double *__restrict__ y, int64_t n,
+                                 double *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = x[i], b = y[i];
+    double *o = out + 6 * i;
+    o[0] = cm::fp64::exp64(a);
+    o[1] = cm::fp64::log64(b);
+    o[2] = cm::fp64::div64(a, b);
+    o[3] = exp(a);
+    o[4] = log(b);
+    o[5] = a / b;
+  }
 }
 
 }  // namespace
@@ -131,4 +148,14 @@ extern "C" int cm_diag_umma_tile(const void *A, const void *B, int n, int k, flo
 extern "C" int cm_diag_fma_peak(int fp64, double *tflops, void *stream) {
   if (!tflops) return CM_DIAG_ERR;
   return fp64 ? measure<double>(tflops, stream, 4096) : measure<float>(tflops, stream, 65536);
+}
+
+extern "C" int cm_diag_fp64_math(const double *x, const double *y, int64_t n, double *out, void *stream) {
+  if (!x || !y || !out || n < 0) return CM_DIAG_ERR;
+  if (n == 0) return 0;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  fp64_math_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(x, y, n, out);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : CM_DIAG_ERR;
 }

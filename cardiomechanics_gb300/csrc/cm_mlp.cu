@@ -111,35 +111,57 @@ __global__ void __launch_bounds__(128) gemm_tc(const __nv_bfloat16 *__restrict__
     umma::fence_after_sync();
   }
   if (ok) {
+    // thread = row m: each 32-column chunk of the row is one contiguous 64 or 128 B run, written
+    // (and, for EPI_DTANH, read) with 16-byte accesses; N is a multiple of 32, so chunks are whole
     const int m = m0 + warp * 32 + (int)(threadIdx.x & 31);  // this thread's row = TMEM lane
     for (int c0 = 0; c0 < nt; c0 += 32) {
       float v[32];
       umma::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       if (m >= M) continue;
-#pragma unroll
-      for (int j = 0; j < 32; j += 2) {
-        const int n = n0 + c0 + j;
-        if (n >= N) break;  // N is a multiple of 32: pairs never straddle it
+      const int n = n0 + c0;
+      if (EPI == EPI_BIAS_TANH || EPI == EPI_DTANH) {
+        uint32_t w[16];
         if (EPI == EPI_BIAS_TANH) {  // hidden biases in BF16, as the inference kernel feeds them
-          const float b0 = __bfloat162float(__float2bfloat16(e.bias[n]));
-          const float b1 = __bfloat162float(__float2bfloat16(e.bias[n + 1]));
-          *reinterpret_cast<uint32_t *>(e.out_bf16 + (size_t)m * e.ldc + n) = tanh2_bf16(v[j] + b0, v[j + 1] + b1);
-        } else {
 #pragma unroll
-          for (int q = 0; q < 2; q++) {
-            const int nn = n + q;
-            if (EPI == EPI_BIAS_F32) {
-              e.out_f32[(size_t)m * e.ldc + nn] = v[j + q] + e.bias[nn];
-            } else if (EPI == EPI_DTANH) {
-              const size_t o = (size_t)m * e.ldc + nn;
-              const float h = __bfloat162float(e.h[o]);
-              e.out_bf16[o] = __float2bfloat16(v[j + q] * (1.f - h * h));
-            } else if (kTrans) {  // C^T's element (m, nn) is C's (nn, m); C has N rows
-              e.out_f32[(size_t)blockIdx.z * (size_t)N * e.ldc + (size_t)nn * e.ldc + m] = v[j + q];
-            } else {
-              e.out_f32[(size_t)blockIdx.z * (size_t)M * e.ldc + (size_t)m * e.ldc + nn] = v[j + q];
-            }
+          for (int j = 0; j < 32; j += 2) {
+            const float b0 = __bfloat162float(__float2bfloat16(e.bias[n + j]));
+            const float b1 = __bfloat162float(__float2bfloat16(e.bias[n + j + 1]));
+            w[j / 2] = tanh2_bf16(v[j] + b0, v[j + 1] + b1);
           }
+        } else {
+          uint4 hv[4];
+          const uint4 *hp = reinterpret_cast<const uint4 *>(e.h + (size_t)m * e.ldc + n);
+#pragma unroll
+          for (int q = 0; q < 4; q++) hv[q] = hp[q];
+          const __nv_bfloat16 *hb = reinterpret_cast<const __nv_bfloat16 *>(hv);
+#pragma unroll
+          for (int j = 0; j < 32; j += 2) {
+            const float h0 = __bfloat162float(hb[j]), h1 = __bfloat162float(hb[j + 1]);
+            const __nv_bfloat16 o0 = __float2bfloat16(v[j] * (1.f - h0 * h0));
+            const __nv_bfloat16 o1 = __float2bfloat16(v[j + 1] * (1.f - h1 * h1));
+            w[j / 2] = (uint32_t)__bfloat16_as_ushort(o0) | ((uint32_t)__bfloat16_as_ushort(o1) << 16);
+          }
+        }
+        uint4 *op = reinterpret_cast<uint4 *>(e.out_bf16 + (size_t)m * e.ldc + n);
+#pragma unroll
+        for (int q = 0; q < 4; q++) op[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+      } else if (kTrans) {  // C^T's element (m, n + j) is C's (n + j, m); C has N rows: coalesced over m
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          e.out_f32[(size_t)blockIdx.z * (size_t)N * e.ldc + (size_t)(n + j) * e.ldc + m] = v[j];
+      } else {
+        float *op = EPI == EPI_BIAS_F32 ? e.out_f32 + (size_t)m * e.ldc + n
+                                        : e.out_f32 + (size_t)blockIdx.z * (size_t)M * e.ldc + (size_t)m * e.ldc + n;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          float4 o = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          if (EPI == EPI_BIAS_F32) {
+            o.x += e.bias[n + 4 * q];
+            o.y += e.bias[n + 4 * q + 1];
+            o.z += e.bias[n + 4 * q + 2];
+            o.w += e.bias[n + 4 * q + 3];
+          }
+          reinterpret_cast<float4 *>(op)[q] = o;
         }
       }
     }
@@ -272,6 +294,9 @@ template <int EPI, bool kTrans = false>
 cudaError_t gemm_tcgen05(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
                          EpiArgs e, int splits, unsigned int *err, cudaStream_t s) {
   if (splits < 1 || K % (32 * splits) || lda % 8 || ldb % 8 || N % 32) return cudaErrorInvalidValue;
+  // the epilogue's 16-byte row accesses
+  if ((uintptr_t)e.out_bf16 % 16 || (uintptr_t)e.out_f32 % 16 || (uintptr_t)e.h % 16 || e.ldc % 8)
+    return cudaErrorInvalidValue;
   dim3 grid((N + 127) / 128, (M + 127) / 128, splits);
   gemm_tc<EPI, kTrans><<<grid, 128, 2 * 128 * kTcKs * sizeof(__nv_bfloat16), s>>>(A, lda, B, ldb, M, N, K, e, err);
   return cudaGetLastError();
@@ -381,6 +406,7 @@ cudaError_t Mlp::reset(uint64_t seed) {
 }
 
 cudaError_t Mlp::sync_bf16() {
+  version++;
   to_bf16<<<(unsigned)((n_params + 255) / 256), 256, 0, stream>>>(w, wb, (int)n_params);
   MCK(cudaGetLastError());
   // transposed copies for the backward products: W3^T (H x out_pad), W2^T (H x H)
@@ -539,6 +565,7 @@ cudaError_t Mlp::loss_grad(const float *X, const float *T, int64_t n) {
 
 cudaError_t Mlp::adam_step(float lr, float b1, float b2, float eps) {
   step++;
+  version++;
   const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
   adam<<<(unsigned)((n_params + 255) / 256), 256, 0, stream>>>(w, g, m1, m2, wb, (int)n_params, lr, b1, b2, eps, c1,
                                                                  c2);

@@ -16,6 +16,7 @@ struct Mlp {
   float *w = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
   __nv_bfloat16 *wb = nullptr, *wt = nullptr;
   size_t off[6] = {}, size[6] = {}, n_params = 0;  // W1 b1 W2 b2 W3 b3 (padded shapes)
+  uint64_t version = 0;  // advanced by every change of the weights (reset, sync_bf16, adam_step)
   float *loss = nullptr;
   void *ws = nullptr;
   float *part = nullptr;  // partial sums of the split weight-gradient GEMMs and column sums

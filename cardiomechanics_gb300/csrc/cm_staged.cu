@@ -224,7 +224,7 @@ __device__ __forceinline__ void coupled_update(const DevBatch &b, const StepIO &
   float stim = (float)io.iext_uniform;
   if (io.tb_cell) {
     stim = 0.f;
-    if (io.t >= tb) {
+    if (f64_ge(io.t, tb)) {  // integer compare: no FP64-pipe instruction per cell
       stim = (float)io.amp;
       if (io.t >= tb + io.textlen) io.tb_cell[c] = tb + io.bcl;
     }
@@ -232,7 +232,9 @@ __device__ __forceinline__ void coupled_update(const DevBatch &b, const StepIO &
   const Acc v = staged_cell<kModel, kThreads>(b, S, het_pos, c, stim + cpl, io.vm_hi_out, io.vm_lo_out);
   uint32_t audit = 0;
   if (io.vm_range > 0.0 && fabsf(v.hi) > (float)io.vm_range) audit |= 32u;
-  if (io.act && a0 == -1.0 && v.hi >= (float)io.act_threshold) io.act[c] = io.act_time;
+  // a0 == -1.0 (not yet activated), compared on the bit pattern
+  if (io.act && __double_as_longlong(a0) == (long long)0xbff0000000000000ull && v.hi >= (float)io.act_threshold)
+    io.act[c] = io.act_time;
   if (audit) {
     atomicOr(b.audit_cell + c, audit);
     atomicOr(b.audit_or, audit);

@@ -53,14 +53,22 @@ struct cm_surrogate_s {
   // FP32 constants and tables of the fine step (the mixed-form audit)
   TT2Consts<float> fine32{};
   float *rows_fine32 = nullptr, *eca_fine32 = nullptr;
-  unsigned int *n_fallback = nullptr;
-  unsigned long long *totals = nullptr;  // n_sur, n_fallback_total, n_audit
-  float *audit_err = nullptr;
+  // the run's counters in one 32-byte device block (one memset clears them, one copy reads them):
+  // totals = n_sur, n_fallback_total, n_audit; then the largest audit error and the macro step's
+  // fallback count (the fallback kernel's list length)
+  unsigned long long *totals = nullptr;
+  float *audit_err = nullptr;          // in the block, after totals
+  unsigned int *n_fallback = nullptr;  // in the block, after audit_err
+  bool counters_zeroed = false;        // the block was cleared at the end of the last run
+  unsigned long long *host_res = nullptr;  // page-locked: the block and the batch's audit mask
   float *bias_block = nullptr;  // b1 | b2 | b3 of the network, contiguous (the inference kernel's layout)
+  uint64_t bias_version = ~0ull;  // the network's weight version bias_block was copied from
   std::vector<cudaEvent_t> ev;  // 3 per macro step of a chunk: kernel timing of runs
 };
 
 namespace {
+
+constexpr size_t kCounterBytes = 4 * sizeof(unsigned long long);
 
 // unpadded <-> padded parameter blocks of an Mlp
 void unpadded_sizes(const Mlp &m, size_t sz[6]) {
@@ -357,12 +365,12 @@ int cm_surrogate_destroy(cm_surrogate_t s) {
   if (!s) return CM_OK;
   cudaStreamSynchronize(s->stream);
   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+  if (s->host_res) cudaFreeHost(s->host_res);
   s->net.m.release();
   for (void *p : {(void *)s->rows_coarse, (void *)s->eca, (void *)s->dX, (void *)s->dT, (void *)s->nX,
                   (void *)s->nT, (void *)s->d_count, (void *)s->gX, (void *)s->gC, (void *)s->gOld, (void *)s->gT,
-                  (void *)s->gkeep, (void *)s->gchunk, (void *)s->fallback, (void *)s->snap, (void *)s->n_snap, (void *)s->n_fallback,
-                  (void *)s->totals,
-                  (void *)s->audit_err, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block,
+                  (void *)s->gkeep, (void *)s->gchunk, (void *)s->fallback, (void *)s->snap, (void *)s->n_snap,
+                  (void *)s->totals, (void *)s->rows_fine64, (void *)s->eca_fine64, (void *)s->bias_block,
                   (void *)s->rows_fine32, (void *)s->eca_fine32})
     cudaFree(p);
   delete s;
@@ -408,9 +416,12 @@ int cm_surrogate_create(cm_surrogate_t *out, cm_params_t p, int substeps, uint64
   }
   if (e == cudaSuccess) e = cudaMalloc(&s->d_count, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(s->d_count, 0, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&s->n_fallback, sizeof(unsigned int));
-  if (e == cudaSuccess) e = cudaMalloc(&s->totals, 3 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&s->audit_err, sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->totals, kCounterBytes);
+  if (e == cudaSuccess) {
+    s->audit_err = reinterpret_cast<float *>(s->totals + 3);
+    s->n_fallback = reinterpret_cast<unsigned int *>(s->totals + 3) + 1;
+    e = cudaMallocHost(&s->host_res, kCounterBytes + 16);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&s->bias_block, 288 * sizeof(float));
   if (e == cudaSuccess) e = cudaGetDevice(&s->net.device);
   if (e == cudaSuccess) e = s->net.m.init(kSurIn, kSurH, kSurOut, seed, s->stream);
@@ -674,8 +685,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     CK(cudaMalloc(&s->fallback, std::max<int64_t>(1, n) * sizeof(int)));
     s->rcap = n;
   }
-  CK(cudaMemsetAsync(s->totals, 0, 3 * sizeof(unsigned long long), st));
-  CK(cudaMemsetAsync(s->audit_err, 0, sizeof(float), st));
+  // the counters: cleared at the end of the last run (behind its result copy), else here
+  if (!s->counters_zeroed) CK(cudaMemsetAsync(s->totals, 0, kCounterBytes, st));
+  s->counters_zeroed = false;
   const bool audit_fp64 = (mode & CM_SUR_AUDIT_FP64) != 0;
   const int64_t snap_need = audit_mod > 0 ? (n + audit_mod - 1) / audit_mod + 32 : 32;
   if (snap_need > s->snap_cap || audit_mod == 0) {
@@ -727,11 +739,15 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.g0_Na = (float)s->fine.get("g_Na");
   ka.g0_Kr = (float)s->fine.get("g_Kr");
   ka.g0_K1 = (float)s->fine.get("g_K1");
-  // biases as one contiguous FP32 block b1 | b2 | b3 (the kernel's layout)
+  // biases as one contiguous FP32 block b1 | b2 | b3 (the kernel's layout), copied again only
+  // when the network's weights have changed since
   float *bias = s->bias_block;
-  CK(cudaMemcpyAsync(bias, s->net.m.w + s->net.m.off[1], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
-  CK(cudaMemcpyAsync(bias + 128, s->net.m.w + s->net.m.off[3], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
-  CK(cudaMemcpyAsync(bias + 256, s->net.m.w + s->net.m.off[5], 32 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  if (s->bias_version != s->net.m.version) {
+    CK(cudaMemcpyAsync(bias, s->net.m.w + s->net.m.off[1], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(bias + 128, s->net.m.w + s->net.m.off[3], 128 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(bias + 256, s->net.m.w + s->net.m.off[5], 32 * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    s->bias_version = s->net.m.version;
+  }
   ka.bias = bias;
   SurPlainArgs pa{};
   pa.fine = b->d;
@@ -778,8 +794,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     ka.snap = s->snap + (size_t)buf * kSnapPlanes * s->snap_cap;
     ka.n_snap = s->n_snap + buf;
     const SurAuditArgs aa = audit_args(s, buf ^ 1, audit_fp64);  // the previous step's sample
-    e = cudaMemsetAsync(s->n_fallback, 0, sizeof(unsigned int), st);
+    if (mstep > 0) e = cudaMemsetAsync(s->n_fallback, 0, sizeof(unsigned int), st);  // step 0: cleared above
     // the two kernels bracketed by events; every kEvChunk steps the chunk's times are summed
+    // (the last chunk's after the final synchronisation below)
     const int j = (int)(mstep % kEvChunk);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j], st);
     if (e == cudaSuccess) e = launch_sur_step(ka, audit_mod > 0 ? &aa : nullptr, n, st);
@@ -788,7 +805,7 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
     if (e == cudaSuccess && audit_mod > 0) e = cudaMemsetAsync(s->n_snap + (buf ^ 1), 0, sizeof(unsigned int), st);
     if (e == cudaSuccess) e = launch_sur_plain(pa, (int)n, st);
     if (e == cudaSuccess) e = cudaEventRecord(s->ev[3 * j + 2], st);
-    if (e == cudaSuccess && (j == kEvChunk - 1 || mstep == n_macro - 1)) {
+    if (e == cudaSuccess && j == kEvChunk - 1 && mstep != n_macro - 1) {
       e = cudaEventSynchronize(s->ev[3 * j + 2]);
       for (int i = 0; i <= j && e == cudaSuccess; i++) {
         float a = 0.f, b2 = 0.f;
@@ -804,17 +821,33 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   // cm_surrogate_flush_audit
   if (audit_mod > 0 && n_macro > 0) s->pending = wbuf ^ 1;
   rc = vm_out(b, Vm, dvm, direct, host_vm, st);
-  unsigned long long tot[3] = {0, 0, 0};
-  float aerr = 0;
-  unsigned int mask = 0;
+  // the counters and the audit mask into page-locked memory, then the counters cleared for the
+  // next run, all behind the last kernels: one synchronisation ends the call
+  unsigned long long *res = s->host_res;
   if (!rc) {
-    e = cudaMemcpyAsync(tot, s->totals, sizeof(tot), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&aerr, s->audit_err, sizeof(float), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&mask, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(res, s->totals, kCounterBytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res + 4, b->audit_or, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->totals, 0, kCounterBytes, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) s->counters_zeroed = true;
+    if (e == cudaSuccess && n_macro > 0) {  // the last chunk's kernel times
+      const int jl = (int)((n_macro - 1) % kEvChunk);
+      for (int i = 0; i <= jl && e == cudaSuccess; i++) {
+        float a = 0.f, b2 = 0.f;
+        e = cudaEventElapsedTime(&a, s->ev[3 * i], s->ev[3 * i + 1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&b2, s->ev[3 * i + 1], s->ev[3 * i + 2]);
+        ms_step += a;
+        ms_plain += b2;
+      }
+    }
     if (e != cudaSuccess) rc = cuda_fail(e, "surrogate run");
   }
   if (rc) return rc;
+  unsigned long long tot[3] = {res[0], res[1], res[2]};
+  float aerr;
+  unsigned int mask;
+  std::memcpy(&aerr, res + 3, sizeof(float));
+  std::memcpy(&mask, res + 4, sizeof(unsigned int));
   if (stats) {
     stats->cell_macro_steps = n * n_macro;
     stats->surrogate = (int64_t)tot[0];
@@ -833,8 +866,8 @@ int cm_surrogate_flush_audit(cm_surrogate_t s, int mode, cm_surrogate_stats *sta
   if (stats) *stats = cm_surrogate_stats{};
   if (s->pending < 0) return CM_OK;
   cudaStream_t st = s->stream;
-  CK(cudaMemsetAsync(s->totals, 0, 3 * sizeof(unsigned long long), st));
-  CK(cudaMemsetAsync(s->audit_err, 0, sizeof(float), st));
+  s->counters_zeroed = false;
+  CK(cudaMemsetAsync(s->totals, 0, kCounterBytes, st));
   int rc = flush_pending(s, (mode & CM_SUR_AUDIT_FP64) != 0, st);
   if (rc) return rc;
   unsigned long long tot[3] = {0, 0, 0};

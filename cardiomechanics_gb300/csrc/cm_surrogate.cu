@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     if (valid) {
       coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
       const float rate = fabsf(inc[0]) / macro_ms;
-      const bool stim = a.stim_on || (a.tb_cell && a.t_last >= a.tb_cell[c]);
+      const bool stim = a.stim_on || (a.tb_cell && f64_ge(a.t_last, a.tb_cell[c]));
       fall = stim || !(rate <= a.gate_mv_per_ms);
     }
     float y[32];

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "cm_common.cuh"
+#include "cm_fp64_math.cuh"
 
 namespace cm {
 
@@ -41,15 +42,24 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
     audit |= 4u;
     Caitab = Caitab < 0 ? 0 : kRows - 1;
   }
-  const double EK = C.RTONF * log(C.K_o / K_i);
+  // E_X = RT/F ln(X_o / X_i) as RT/F (ln X_o - ln X_i), ln X_o precomputed; AK1 / (AK1 + BK1)
+  // over one denominator. The FP64 exp, log and division are the table-driven / Newton forms of
+  // cm_fp64_math.cuh (within 1 ulp of the library's): on GB300 this step is bound by its count of
+  // FP64-pipe instructions.
+  using fp64::ddiv;
+  using fp64::dexp;
+  using fp64::dlog;
+  const double EK = C.RTONF * (C.logKo - dlog(K_i));
   const double VminEK = svolt - EK;
-  const double ENa = C.RTONF * log(C.Na_o / Na_i);
+  const double ENa = C.RTONF * (C.logNao - dlog(Na_i));
   const double VminENa = svolt - ENa;
-  const double EKs = C.RTONF * log((C.K_o + C.pKNaNao) / (K_i + C.pKNa * Na_i));
-  const double AK1 = 0.1 / (1. + exp(0.06 * (VminEK - 200)));
-  const double BK1 = (3. * exp(0.0002 * (VminEK + 100)) + exp(0.1 * (VminEK - 10))) / (1. + exp(-0.5 * (VminEK)));
-  const double rec_iK1 = AK1 / (AK1 + BK1);
-  const double I_pCa = C.g_pCa * c.Ca_i / (C.KpCa + c.Ca_i);
+  const double EKs = C.RTONF * (C.logKoNao - dlog(K_i + C.pKNa * Na_i));
+  // rec_iK1 = AK1/(AK1+BK1), AK1 = 0.1/(1+e1), BK1 = (3 e2 + e3)/(1+e4)
+  const double e1 = dexp(0.06 * (VminEK - 200)), e2 = dexp(0.0002 * (VminEK + 100));
+  const double e3 = dexp(0.1 * (VminEK - 10)), e4 = dexp(-0.5 * (VminEK));
+  const double a1 = 0.1 * (1. + e4);
+  const double rec_iK1 = ddiv(a1, a1 + (3. * e2 + e3) * (1. + e1));
+  const double I_pCa = ddiv(C.g_pCa * c.Ca_i, C.KpCa + c.Ca_i);
   const double I_pK = row[T2_rec_ipK] * VminEK;
   const double I_to = g.g_to * c.r * c.s * VminEK;
   const double I_Kr = g.g_Kr * C.sqrtKo54 * c.xr1 * c.xr2 * VminEK;
@@ -61,33 +71,35 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
   const double I_Na = g.g_Na * c.m * c.m * c.m * c.h * c.j * VminENa;
   const double I_CaL = g.g_CaL * c.d * c.f * c.f2 * c.fCa * ((row[T2_CaL_P1] * c.CaSS) - row[T2_CaL_P2]);
   const double I_NaCa = C.kNaCa * row[T2_NaCa_P1] * Na_i * Na_i * Na_i - C.kNaCa * row[T2_NaCa_P2] * c.Ca_i;
-  const double I_NaK = C.knak * C.KoKmK * (Na_i / (Na_i + C.KmNa)) * row[T2_NaK_P1];
+  const double I_NaK = C.knak * C.KoKmK * ddiv(Na_i, Na_i + C.KmNa) * row[T2_NaK_P1];
   const double I_tot = I_K + I_K1 + I_to + I_Na + I_bNa + I_CaL + I_bCa + I_NaK + I_NaCa + I_pCa + I_pK - i_external;
 
   const double Caisquare = c.Ca_i * c.Ca_i;
   const double CaSSsquare = c.CaSS * c.CaSS;
-  const double ECaSR = C.EC / CaSR;
-  const double kCaSR = C.max_sr - ((C.max_sr - C.min_sr) / (1 + ECaSR * ECaSR));
+  // kCaSR = max_sr - (max_sr - min_sr)/(1 + (EC/CaSR)^2) over one denominator
+  const double CaSR2 = CaSR * CaSR;
+  const double kCaSR = C.max_sr - ddiv((C.max_sr - C.min_sr) * CaSR2, CaSR2 + C.EC * C.EC);
   const double k2 = C.ks2 * kCaSR;
-  const double k1 = C.ks1 / kCaSR;
   const double dRq = 1000.0 * ((-k2 * c.CaSS * c.Rq) + (C.k4 * (1.0 - c.Rq)));
   c.Rq += C.dt * dRq;
-  const double O = k1 * CaSSsquare * c.Rq / (C.k3 + k1 * CaSSsquare);
+  // O = k1 CaSS^2 Rq / (k3 + k1 CaSS^2) with k1 = ks1 / kCaSR, over one denominator
+  const double k1C2 = C.ks1 * CaSSsquare;
+  const double O = ddiv(k1C2 * c.Rq, C.k3 * kCaSR + k1C2);
   const double I_rel = C.Vrel * O * (CaSR - c.CaSS);
   const double I_leak = 0.00036 * (CaSR - c.Ca_i);
   const double I_xfer = C.Vxfer * (c.CaSS - c.Ca_i);
-  const double SERCA = C.Vmaxup / (1. + (C.Kupsquare / Caisquare));
+  const double SERCA = ddiv(C.Vmaxup * Caisquare, Caisquare + C.Kupsquare);
   const double dCaSR = C.dt1000 * (SERCA - I_rel - I_leak);
-  const double CaCSQN = C.Bufsr * CaSR / (CaSR + C.Kbufsr);
+  const double CaCSQN = ddiv(C.Bufsr * CaSR, CaSR + C.Kbufsr);
   const double bjsr = C.Bufsr - CaCSQN - dCaSR - CaSR + C.Kbufsr;
   const double cjsr = C.Kbufsr * (CaCSQN + dCaSR + CaSR);
   CaSR = (sqrt(bjsr * bjsr + 4 * cjsr) - bjsr) * 0.5;
-  const double CaSSBuf = C.Bufss * c.CaSS / (c.CaSS + C.Kbufss);
+  const double CaSSBuf = ddiv(C.Bufss * c.CaSS, c.CaSS + C.Kbufss);
   const double dCaSS = C.dt1000 * (-I_xfer * C.VcVss + I_rel * C.VsrVss + (-I_CaL * C.inversevssF2 * C.Cm));
   const double bjss = C.Bufss - CaSSBuf - dCaSS - c.CaSS + C.Kbufss;
   const double cjss = C.Kbufss * (CaSSBuf + dCaSS + c.CaSS);
   c.CaSS = (sqrt(bjss * bjss + 4. * cjss) - bjss) * 0.5;
-  const double CaBuf = C.Bufc * c.Ca_i / (c.Ca_i + C.Kbufc);
+  const double CaBuf = ddiv(C.Bufc * c.Ca_i, c.Ca_i + C.Kbufc);
   const double dCai =
       C.dt1000 * ((-(I_bCa + I_pCa - 2 * I_NaCa) * C.inverseviF2 * C.Cm) - (SERCA - I_leak) * C.invVcdVsr + I_xfer);
   const double bc = C.BufcPKbufc - CaBuf - dCai - c.Ca_i;
@@ -98,7 +110,7 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
   const double dKi = -(-i_external + I_K1 + I_to + I_K - 2 * I_NaK + I_pK) * C.inverseviF * C.Cm;
   K_i += C.dt * dKi * 1000.0;
   const double CaSS005 = c.CaSS * 20.0;
-  const double den = 1.0 / (1.0 + CaSS005 * CaSS005);
+  const double den = ddiv(1.0, 1.0 + CaSS005 * CaSS005);
   const double FCa_INF = 0.6 * den + 0.4;
   const double taufca = 0.080 * den + 0.002;
 
@@ -113,7 +125,7 @@ CM_HD double tt2_calc_fp64(const TT2Consts<double> &C, const double *__restrict_
   c.d = row[T2_d_inf] - (row[T2_d_inf] - c.d) * row[T2_exptau_d];
   c.f = row[T2_f_inf] - (row[T2_f_inf] - c.f) * row[T2_exptau_f];
   c.f2 = row[T2_f2_inf] - (row[T2_f2_inf] - c.f2) * row[T2_exptau_f2];
-  c.fCa = FCa_INF - (FCa_INF - c.fCa) * exp(-C.dt / taufca);
+  c.fCa = FCa_INF - (FCa_INF - c.fCa) * dexp(-ddiv(C.dt, taufca));
   if (kDiag) {
     double *a = diag->v;
     a[0] = I_Na; a[1] = I_CaL; a[2] = I_bCa; a[3] = I_pCa; a[4] = I_to; a[5] = I_Ks; a[6] = I_Kr;

@@ -33,6 +33,12 @@ int cm_diag_batch_wait_check(void *batch, int64_t skip_tile, uint32_t spin_limit
  * lets a test see that an entry point which must not allocate left it unchanged. */
 int cm_diag_mlp_workspace_rows(void *mlp, int64_t *rows);
 
+/* The FP64 exp, log and division of the FP64 cell-model steps (table-driven exp and log, Newton
+ * division from the approximate reciprocal) beside the CUDA library's, on device arrays x, y of
+ * n values: out (device, 6 n values) holds, per i, exp64(x), log64(y), div64(x, y), exp(x),
+ * log(y), x / y. For accuracy tests. */
+int cm_diag_fp64_math(const double *x, const double *y, int64_t n, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,56 @@
+"""The FP64 exp, log and division of the FP64 cell-model steps (csrc/cm_fp64_math.cuh) against
+the CUDA library's and against extended-precision host values.
+
+The plain FP64 ten Tusscher step (reference TenTusscher2.cpp:615-906) evaluates 5 exponentials,
+3 logarithms and 11 divisions per cell and step; on GB300 the step is bound by its FP64-pipe
+instruction count, so it uses table-driven exp/log and a Newton division instead of the library
+forms. These must stay within 1 ulp of the correctly rounded value over the argument ranges the
+cell models produce and beyond."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ulps(a, b):
+    """|a - b| in units in the last place: the difference of the float64 bit patterns, taken in
+    int64 (same-sign values)."""
+    return np.abs(a.view(np.int64) - b.view(np.int64))
+
+
+def _cases(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.concatenate([
+        rng.uniform(-60.0, 60.0, n),              # the cell models' exponents (scaled mV, tau ratios)
+        rng.uniform(-699.0, 699.0, n // 4),       # the whole fast range
+        np.array([0.0, -0.0, 1e-300, -1e-300, 1e-17, 0.5, -0.5, 700.0, -700.0, 709.0, -745.0]),
+    ])
+    y = np.concatenate([
+        np.exp(rng.uniform(-12.0, 12.0, n)),      # concentrations, sums of rates
+        np.exp(rng.uniform(-690.0, 690.0, n // 4)),
+        np.array([1.0, 2.0, 0.5, 1.0 + 2.0**-52, 1.0 - 2.0**-53, 138.0, 8.0, 5.4, 1e-300, 3.0, 7.0]),
+    ])
+    return x, y
+
+
+def test_fp64_math_against_library_and_extended(gpu):
+    import torch
+    cm = gpu
+    x, y = _cases(1 << 17, 11)
+    r = cm.fp64_math(torch.tensor(x, device="cuda"), torch.tensor(y, device="cuda"))
+    exp64, log64, div64, exp_lib, log_lib, div_lib = r
+    # the library's and ours: within 1 ulp of each other
+    assert _ulps(exp64, exp_lib).max() <= 1
+    assert _ulps(log64, log_lib).max() <= 1
+    # division: the IEEE quotient (the device's and numpy's are both correctly rounded)
+    assert np.array_equal(div_lib, x / y)
+    assert _ulps(div64, div_lib).max() <= 1
+    assert np.mean(div64 == div_lib) > 0.999
+    # against extended precision, rounded to float64: at most 1 ulp
+    ld = np.longdouble
+    ref_exp = np.exp(x.astype(ld)).astype(np.float64)
+    ref_log = np.log(y.astype(ld)).astype(np.float64)
+    assert _ulps(exp64, ref_exp).max() <= 1
+    assert _ulps(log64, ref_log).max() <= 1
+    assert np.mean(exp64 == ref_exp) > 0.99
+    assert np.mean(log64 == ref_log) > 0.99

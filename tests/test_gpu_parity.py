@@ -1,8 +1,10 @@
 """GPU parity: the CUDA kernels through the C ABI against the oracle and the golden vectors.
 
 Tolerances:
-  FP64 batches  one Calc: rtol 1e-11 (CUDA's exp/log differ from glibc by a few ulp and the
-                kernel fuses multiply-adds); 1000 ms traces: |dVm| <= 1e-5 mV, APD90 and
+  FP64 batches  one Calc: states rtol 1e-11 (the kernel's exp, log and division are within 1 ulp
+                of glibc's, some quotients are taken over one denominator and multiply-adds are
+                fused); dV and the diagnostic currents rtol 1e-10 (I_tot is a sum of currents
+                that cancel to ~1e-6 of their size); 1000 ms traces: |dVm| <= 1e-5 mV, APD90 and
                 upstroke within 1e-3 ms of the oracle.
   mixed batches APD90 within 1 ms, upstroke within 0.1 ms, RMS Vm error <= 0.5 mV per cell.
 """
@@ -25,6 +27,10 @@ AMP = {5: W.TT2_STIM_NA, 2: W.CRN_STIM_PAPF, 12: W.ORD_STIM, 14: W.TOM_STIM}
 TLEN = {5: 1e-3, 2: 2e-3, 12: 1e-3, 14: 1e-3}
 
 
+# the diagnostic currents of the reference block: TT2 Array[0..16] (I_Na ... I_tot) at slots 5..21
+DIAG_COLS = {5: tuple(range(5, 22))}
+
+
 def ref_block_cols(model):
     # TT2 Array[17] is never written by the reference
     return [c for c in range(36) if c != 22] if model == 5 else list(range(22))
@@ -45,7 +51,10 @@ def test_one_step_known_answers_fp64(gpu, model):
     dV = b.calc(dt, np.ascontiguousarray(g["vm"]), np.ascontiguousarray(g["i_ext"]))
     S = b.get_state(cm.LAYOUT_REF_BLOCK)
     cols = ref_block_cols(model)
-    np.testing.assert_allclose(S[:, cols], g["state_out"][:, cols], rtol=1e-11, atol=1e-250)
+    cur = [c for c in cols if c in DIAG_COLS.get(model, ())]
+    st = [c for c in cols if c not in cur]
+    np.testing.assert_allclose(S[:, st], g["state_out"][:, st], rtol=1e-11, atol=1e-250)
+    np.testing.assert_allclose(S[:, cur], g["state_out"][:, cur], rtol=1e-10, atol=1e-250)
     np.testing.assert_allclose(dV, g["dvm"], rtol=1e-10, atol=1e-16)
     # rows at the table edges stay in bounds; out-of-table voltages raise the audit bit
     assert b.audit() & cm.AUDIT_VRANGE == 0
