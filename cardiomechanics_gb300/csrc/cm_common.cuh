@@ -251,44 +251,56 @@ CM_HD void acc_add(Acc &a, float d) {
 }
 
 // Double <-> compensated pair. On the device the conversions are done on the bit patterns with
-// integer instructions: on GB300 every FP64-pipe instruction, conversions included, issues at 2
-// per clock per SM (1/64 of the FP32 rate), so the four conversions and the subtraction of the
-// plain form cost a kernel that reads FP64 Vm every step more than its memory traffic does.
-// acc_from_double gives the plain form's pair (hi = x rounded to FP32, lo = the remainder rounded
-// to FP32) for 2^-74 <= |x| < 2^127, except that a remainder of exactly half an FP32 ulp of x
-// rounds hi away from zero instead of to even; other values take the plain form.
-// acc_to_double widens both halves exactly and adds them once: the plain form's result.
+// integer instructions and selects, with no branch: on GB300 every FP64-pipe instruction,
+// conversions included, issues at 2 per clock per SM (1/64 of the FP32 rate), so the four
+// conversions and the subtraction of the plain form cost a kernel that reads FP64 Vm every step
+// more than its memory traffic does (and a rare-case branch to the plain form is if-converted by
+// the compiler into running it always). acc_from_double gives the plain form's pair (hi = x
+// rounded to FP32, lo = the remainder rounded to FP32) for 2^-74 <= |x| < 2^127, except that a
+// remainder of exactly half an FP32 ulp of x rounds hi away from zero instead of to even; below
+// that lo is 0 (|x| < 2^-74) and hi a signed zero (|x| < 2^-126), above it hi is infinite; NaN
+// stays NaN. acc_to_double widens both halves exactly and adds them once: the plain form's
+// result.
 CM_HD Acc acc_from_double(double x) {
 #ifdef __CUDA_ARCH__
   const uint32_t hw = (uint32_t)__double2hiint(x), lw = (uint32_t)__double2loint(x);
+  const uint32_t s = hw & 0x80000000u;
   const int E = (int)((hw >> 20) & 0x7ffu);  // biased FP64 exponent
-  if (E >= 949 && E <= 1149) {
-    const uint32_t s = hw & 0x80000000u;
-    const uint32_t lr = lw + 0x10000000u;  // + half an ulp of the 24-bit significand
-    const uint32_t hr = hw + (lr < lw ? 1u : 0u);
-    const uint32_t er = (hr >> 20) & 0x7ffu;  // one more than E where the significand carried out
-    const uint32_t hi = s | ((er - 896u) << 23) | ((hr & 0xfffffu) << 3) | (lr >> 29);
-    // the low 29 significand bits as a signed remainder in [-2^28, 2^28), in units of 2^(E-1075)
-    int rem = ((int)((lw & 0x1fffffffu) << 3)) >> 3;
-    rem = s ? -rem : rem;
-    const float lo = __int2float_rn(rem) * __uint_as_float((uint32_t)(E - 948) << 23);
-    return Acc{__uint_as_float(hi), lo};
-  }
-#endif
+  const uint32_t lr = lw + 0x10000000u;      // + half an ulp of the 24-bit significand
+  const uint32_t hr = hw + (lr < lw ? 1u : 0u);
+  const uint32_t er = (hr >> 20) & 0x7ffu;   // one more than E where the significand carried out
+  uint32_t hi = s | ((er - 896u) << 23) | ((hr & 0xfffffu) << 3) | (lr >> 29);
+  // the low 29 significand bits as a signed remainder in [-2^28, 2^28), in units of 2^(E-1075)
+  int rem = ((int)((lw & 0x1fffffffu) << 3)) >> 3;
+  rem = s ? -rem : rem;
+  float lo = __int2float_rn(rem) * __uint_as_float((uint32_t)(E - 948) << 23);
+  const bool inf_or_nan = E == 0x7ff, nan = inf_or_nan && ((hw & 0xfffffu) | lw);
+  lo = (E >= 949 && er <= 1150u) ? lo : 0.f;
+  hi = E < 897 ? s : hi;
+  hi = er > 1150u || inf_or_nan ? (s | 0x7f800000u) : hi;
+  hi = nan ? (s | 0x7fc00000u) : hi;
+  return Acc{__uint_as_float(hi), lo};
+#else
   Acc a;
   a.hi = (float)x;
   a.lo = (float)(x - (double)a.hi);
   return a;
+#endif
 }
 
-// FP32 -> FP64 widening on the bit pattern (exact); zero, inf and NaN included, subnormal
-// inputs take the conversion instruction.
+// FP32 -> FP64 widening on the bit pattern (exact, zero, subnormal, inf and NaN included).
 CM_HD double f32_widen(float f) {
 #ifdef __CUDA_ARCH__
   const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu, s = u & 0x80000000u, m = u & 0x7fffffu;
-  if (e == 0u && m != 0u) return (double)f;
-  const uint32_t E = e == 0u ? 0u : (e == 255u ? 2047u : e + 896u);
-  return __hiloint2double((int)(s | (E << 20) | (m >> 3)), (int)(m << 29));
+  uint32_t h = s | ((e + 896u) << 20) | (m >> 3), l = m << 29;  // normal: exponent + 1023 - 127
+  // subnormal: m 2^-149 = 2^(p-149) (1 + fraction), p = the index of m's leading one
+  const int p = 31 - __clz(m | 1u);
+  const uint32_t fs = (m << (23 - p)) & 0x7fffffu;
+  const uint32_t hs = s | ((uint32_t)(p + 874) << 20) | (fs >> 3), ls = fs << 29;
+  h = e == 255u ? (s | 0x7ff00000u | (m >> 3)) : h;
+  h = e == 0u ? (m ? hs : s) : h;
+  l = e == 0u ? (m ? ls : 0u) : l;
+  return __hiloint2double((int)h, (int)l);
 #else
   return (double)f;
 #endif
