@@ -555,13 +555,17 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     group_sync(g);
   };
   int t_next = n_tiles;
+  double vm_pf = 0.0;    // page-locked host Vm of this thread's cell of the next tile, loaded early
+  bool have_pf = false;
   while (t < n_tiles) {
     const int c = t * kTcCells + r;
     const bool valid = c < n;
     // loads that do not come through the stage go first: their latency overlaps the stage wait
     // Vm: the device planes (c < ld: padding cells too), or the caller's page-locked host array
-    // (plain load; padding cells 0)
-    const Acc vm = a.vm ? acc_from_double(valid ? a.vm[c] : 0.0) : Acc{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};
+    // (plain load, or the one issued during the last tile; padding cells 0)
+    const Acc vm = a.vm ? acc_from_double(have_pf ? vm_pf : (valid ? a.vm[c] : 0.0))
+                        : Acc{__ldg(a.vm_hi + c), __ldg(a.vm_lo + c)};
+    have_pf = false;
     const int cc = valid ? c : 0;  // conductance planes: the tile's padding cells read cell 0
     TT2Het_<float> g6;
     g6.g_Na = het[H2_g_Na] ? __ldg(het[H2_g_Na] + cc) : C.g_Na;
@@ -639,6 +643,11 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       // the issuing warp wrote the group's next tile index before it reached this barrier (and
       // writes the one after only past the next tile's first barrier, which this warp must reach)
       t_next = s_tile[g];
+      if (a.vm) {  // host Vm of the next tile: the link's latency overlaps layers 2 and 3
+        const int cn = t_next * kTcCells + r;
+        vm_pf = (t_next < n_tiles && cn < n) ? a.vm[cn] : 0.0;
+        have_pf = true;
+      }
       if (leader) {  // layer 2: D = H1 W2^T, K = 128
         umma::fence_after_sync();
         constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
