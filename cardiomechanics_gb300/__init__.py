@@ -49,7 +49,7 @@ ABI_SYMBOLS = (
     "cm_batch_step_update_act",
     "cm_batch_set_state", "cm_batch_step", "cm_batch_step_update", "cm_batch_run", "cm_batch_audit",
     "cm_batch_autotune", "cm_batch_set_launch", "cm_diag_fma_peak", "cm_diag_umma_tile",
-    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check", "cm_diag_fp64_math", "cm_model_print_names", "cm_batch_print_values",
+    "cm_diag_mlp_workspace_rows", "cm_diag_batch_wait_check", "cm_diag_fp64_math", "cm_diag_pair_convert", "cm_model_print_names", "cm_batch_print_values",
     "cm_batch_get_cell", "cm_batch_set_cell", "cm_batch_calc_cell",
     "cm_multi_create", "cm_multi_destroy", "cm_multi_run", "cm_multi_autotune", "cm_multi_set_launch",
     "cm_mlp_create", "cm_mlp_destroy", "cm_mlp_n_params", "cm_mlp_get_params", "cm_mlp_set_params",
@@ -187,6 +187,7 @@ def lib() -> ctypes.CDLL:
     L.cm_diag_mlp_workspace_rows.argtypes = [vp, ctypes.POINTER(i64)]
     L.cm_diag_batch_wait_check.argtypes = [vp, i64, ctypes.c_uint32]
     L.cm_diag_fp64_math.argtypes = [vp, vp, i64, vp, vp]
+    L.cm_diag_pair_convert.argtypes = [vp, i64, vp, vp, vp, vp, vp]
     L.cm_model_print_names.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int]
     L.cm_batch_print_values.argtypes = [vp, i64, ctypes.c_double, ctypes.c_int, dp, ctypes.c_int]
     L.cm_batch_get_cell.argtypes = [vp, i64, ctypes.c_int, dp]
@@ -250,6 +251,22 @@ def fp64_math(x, y):
     out = x.new_empty((x.numel(), 6))
     _check(lib().cm_diag_fp64_math(_ptr(x), _ptr(y), x.numel(), _ptr(out), None))
     return out.cpu().numpy().T.copy()
+
+
+def pair_convert(x):
+    """The mixed kernels' double <-> (hi, lo) FP32 pair conversions on a float64 CUDA tensor x:
+    returns numpy arrays hi, lo (float32), back = hi + lo and widened = (double)(float)x (float64)."""
+    import torch
+    if str(x.dtype) != "torch.float64" or not x.is_cuda:
+        raise ValueError("pair_convert: x must be a float64 CUDA tensor")
+    x = x.contiguous()
+    n = x.numel()
+    hi = torch.empty(n, dtype=torch.float32, device=x.device)
+    lo = torch.empty_like(hi)
+    back = torch.empty(n, dtype=torch.float64, device=x.device)
+    wid = torch.empty_like(back)
+    _check(lib().cm_diag_pair_convert(_ptr(x), n, _ptr(hi), _ptr(lo), _ptr(back), _ptr(wid), None))
+    return hi.cpu().numpy(), lo.cpu().numpy(), back.cpu().numpy(), wid.cpu().numpy()
 
 
 def model_info(model: int) -> Info:

@@ -256,10 +256,10 @@ CM_HD void acc_add(Acc &a, float d) {
 // conversions and the subtraction of the plain form cost a kernel that reads FP64 Vm every step
 // more than its memory traffic does (and a rare-case branch to the plain form is if-converted by
 // the compiler into running it always). acc_from_double gives the plain form's pair (hi = x
-// rounded to FP32, lo = the remainder rounded to FP32) for 2^-74 <= |x| < 2^127, except that a
-// remainder of exactly half an FP32 ulp of x rounds hi away from zero instead of to even; below
-// that lo is 0 (|x| < 2^-74) and hi a signed zero (|x| < 2^-126), above it hi is infinite; NaN
-// stays NaN. acc_to_double widens both halves exactly and adds them once: the plain form's
+// rounded to FP32, lo = the remainder rounded to FP32) for 2^-74 <= |x| < 2^128, except that a
+// remainder of exactly half an FP32 ulp of x rounds hi away from zero instead of to even (the pair
+// still sums to x); below that lo is 0 (|x| < 2^-74) and hi a signed zero (|x| < 2^-126); where
+// hi rounds past the FP32 range it is infinite and lo 0; NaN stays NaN. acc_to_double widens both halves exactly and adds them once: the plain form's
 // result.
 CM_HD Acc acc_from_double(double x) {
 #ifdef __CUDA_ARCH__

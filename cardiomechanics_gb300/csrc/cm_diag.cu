@@ -71,6 +71,18 @@ __global__ void fp64_math_kernel(const double *__restrict__ x, const double *__r
   }
 }
 
+// The compensated-pair conversions of the mixed kernels (integer forms on the device)
+__global__ void pair_kernel(const double *__restrict__ x, int64_t n, float *__restrict__ hi, float *__restrict__ lo,
+                            double *__restrict__ back, double *__restrict__ widened) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cm::Acc a = cm::acc_from_double(x[i]);
+    hi[i] = a.hi;
+    lo[i] = a.lo;
+    back[i] = cm::acc_to_double(a);
+    widened[i] = cm::f32_widen((float)x[i]);
+  }
+}
+
 }  // namespace
 
 // D (128 x N, FP32) = A (128 x K) * B (N x K)^T on the tcgen05 tensor core, operands staged in
@@ -155,6 +167,17 @@ extern "C" int cm_diag_fp64_math(const double *x, const double *y, int64_t n, do
   if (n == 0) return 0;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
   fp64_math_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(x, y, n, out);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  return e == cudaSuccess ? 0 : CM_DIAG_ERR;
+}
+
+extern "C" int cm_diag_pair_convert(const double *x, int64_t n, float *hi, float *lo, double *back, double *widened,
+                                    void *stream) {
+  if (!x || !hi || !lo || !back || !widened || n < 0) return CM_DIAG_ERR;
+  if (n == 0) return 0;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  pair_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(x, n, hi, lo, back, widened);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   return e == cudaSuccess ? 0 : CM_DIAG_ERR;

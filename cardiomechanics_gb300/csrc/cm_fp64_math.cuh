@@ -5,8 +5,9 @@
 // GB300 in units of one DFMA's issue cost: exp 14.9 -> exp64 11.7, log 28.7 -> log64 13.8,
 // a / b 8.3 -> div64 6.5; the TT2 FP64 step went from 1.03e9 to 1.36e9 cell-steps/s with them
 // (and its quotients over shared denominators), Courtemanche's from 1.20e9 to 1.46e9. (The
-// O'Hara-Rudy and Tomek FP64 steps, with ~50 exponentials each, measured 2 % slower with them
-// and keep the library forms.)
+// O'Hara-Rudy and Tomek FP64 steps, with ~50 exponentials and ~60-95 divisions each, measured 2 %
+// slower with all three and 3 % slower with the division and log alone, and keep the library
+// forms.)
 // Accuracy: exp64 and log64 within 1 ulp of the CUDA functions and of the correctly rounded
 // value (equal to it for over 99 % of arguments), div64 equal to the IEEE quotient on every
 // sampled operand pair (tests/test_gpu_fp64_math.py checks all three against extended-precision

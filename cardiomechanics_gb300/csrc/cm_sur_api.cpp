@@ -462,6 +462,7 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
   if (rc) return rc;
   if (b->ps.dt != s->fine.dt) return fail(CM_ERR_ARG, "batch dt differs from the surrogate's fine dt");
   const int64_t n = b->d.n;
+  if (n > 0x7fffffff) return fail(CM_ERR_ARG, "training-data generation takes at most 2^31 - 1 cells");
   const int64_t n_sample = (n + cell_stride - 1) / cell_stride;
   cudaStream_t st = b->stream;
   // dataset capacity (grows, keeping what is there)
@@ -499,7 +500,8 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
   float *hi = b->vm_planes, *lo = b->vm_planes + b->d.ld;
   const cm_stimulus stv = stim ? *stim : cm_stimulus{0, 1e300, nullptr, 0, 0, 0};
   double t = stv.t0, tb = stv.textbegin;
-  const float g0_Na = (float)s->fine.get("g_Na"), g0_Kr = (float)s->fine.get("g_Kr"), g0_K1 = (float)s->fine.get("g_K1");
+  const float inv_g0_Na = (float)(1.0 / s->fine.get("g_Na")), inv_g0_Kr = (float)(1.0 / s->fine.get("g_Kr")),
+              inv_g0_K1 = (float)(1.0 / s->fine.get("g_K1"));
   float iext[64];
   for (int64_t mstep = 0; mstep < n_macro; mstep++) {
     SurGenArgs ga{};
@@ -515,18 +517,22 @@ int cm_surrogate_generate(cm_surrogate_t s, cm_batch_t b, double *Vm, int64_t n_
     ga.X = s->gX;
     ga.C = s->gC;
     ga.Old = s->gOld;
-    ga.g0_Na = g0_Na;
-    ga.g0_Kr = g0_Kr;
-    ga.g0_K1 = g0_K1;
+    ga.inv_g0_Na = inv_g0_Na;
+    ga.inv_g0_Kr = inv_g0_Kr;
+    ga.inv_g0_K1 = inv_g0_K1;
     CK(launch_sur_gen(ga, st));
     const bool on = protocol_steps(stim ? &stv : nullptr, s->substeps, s->fine.dt, t, tb, iext);
-    for (int k = 0; k < s->substeps; k++) {
-      StepIO io;
-      io.vm_hi = hi;
-      io.vm_lo = lo;
-      io.iext_uniform = iext[k];
-      CK(launch_step(b->d, io, b->d.variant, b->d.grid_mode, st));
-    }
+    // the macro step's fine steps of every cell in one launch (Vm in registers between them; the
+    // same per-step update as the batch's step kernel)
+    SurPlainArgs fa{};
+    fa.fine = b->d;
+    fa.vm_hi = hi;
+    fa.vm_lo = lo;
+    fa.list = nullptr;
+    fa.n_all = (int)n;
+    fa.substeps = s->substeps;
+    for (int k = 0; k < s->substeps; k++) fa.iext[k] = iext[k];
+    CK(launch_sur_plain(fa, (int)n, st));
     SurPostArgs pa{};
     pa.fine = b->d;
     pa.vm_hi = hi;
@@ -736,9 +742,9 @@ int cm_batch_run_surrogate(cm_batch_t b, cm_surrogate_t s, double *Vm, int64_t n
   ka.n_fallback_total = s->totals + 1;
   ka.snap_cap = (int)s->snap_cap;
   ka.n_sur = s->totals;
-  ka.g0_Na = (float)s->fine.get("g_Na");
-  ka.g0_Kr = (float)s->fine.get("g_Kr");
-  ka.g0_K1 = (float)s->fine.get("g_K1");
+  ka.inv_g0_Na = (float)(1.0 / s->fine.get("g_Na"));
+  ka.inv_g0_Kr = (float)(1.0 / s->fine.get("g_Kr"));
+  ka.inv_g0_K1 = (float)(1.0 / s->fine.get("g_K1"));
   // biases as one contiguous FP32 block b1 | b2 | b3 (the kernel's layout), copied again only
   // when the network's weights have changed since
   float *bias = s->bias_block;

@@ -58,17 +58,20 @@ __device__ __forceinline__ void outputs(const Cell &q, const Acc &vm, float o[kS
   o[14] = q.x.Ca_i; o[15] = q.x.CaSS; o[16] = q.CaSR.hi; o[17] = q.Na.hi; o[18] = q.K.hi;
 }
 
-__device__ __forceinline__ void features(const Cell &q, float vm_mv, float g0_Na, float g0_Kr, float g0_K1,
-                                         float f[kSurIn]) {
+// The logarithms are the SFU's (relative error ~2^-21): the features reach the network as BF16
+// (8 significant bits), and the library logf and division cost the issue-bound macro step ~5 %
+// of its instructions.
+__device__ __forceinline__ void features(const Cell &q, float vm_mv, float inv_g0_Na, float inv_g0_Kr,
+                                         float inv_g0_K1, float f[kSurIn]) {
   f[0] = vm_mv;
   f[1] = q.x.m; f[2] = q.x.h; f[3] = q.x.j; f[4] = q.x.xr1; f[5] = q.x.xr2; f[6] = q.x.xs; f[7] = q.x.r;
   f[8] = q.x.s; f[9] = q.x.d; f[10] = q.x.f; f[11] = q.x.f2; f[12] = q.x.fCa; f[13] = q.x.Rq;
-  f[14] = logf(fmaxf(q.x.Ca_i, 1e-12f));
-  f[15] = logf(fmaxf(q.x.CaSS, 1e-12f));
+  f[14] = __logf(fmaxf(q.x.Ca_i, 1e-12f));
+  f[15] = __logf(fmaxf(q.x.CaSS, 1e-12f));
   f[16] = q.CaSR.hi; f[17] = q.Na.hi; f[18] = q.K.hi;
-  f[19] = logf(q.g.g_Na / g0_Na);
-  f[20] = logf(q.g.g_Kr / g0_Kr);
-  f[21] = logf(q.g.g_K1 / g0_K1);
+  f[19] = __logf(q.g.g_Na * inv_g0_Na);
+  f[20] = __logf(q.g.g_Kr * inv_g0_Kr);
+  f[21] = __logf(q.g.g_K1 * inv_g0_K1);
 }
 
 // Exact-ish increment of a compensated accumulator: the hi difference is exact for nearby
@@ -118,9 +121,9 @@ __device__ __forceinline__ uint32_t tanh2_bf16(float x, float y) {
 }
 
 __global__ void __launch_bounds__(128) sur_plain_kernel(const SurPlainArgs a) {
-  const unsigned int n = *a.n_list;
+  const unsigned int n = a.list ? *a.n_list : (unsigned int)a.n_all;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int c = a.list[i];
+    const int c = a.list ? a.list[i] : (int)i;
     Acc v = a.vm ? acc_from_double(a.vm[c]) : Acc{a.vm_hi[c], a.vm_lo[c]};
     uint32_t audit = 0;
     double tb = a.tb_cell ? a.tb_cell[c] : 0.0;
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(128) sur_gen_kernel(const SurGenArgs a) {
     load_cell(a.fine, c, q);
     const Acc vm{a.vm_hi[c], a.vm_lo[c]};
     float f[kSurIn], oc[kSurOut], inc[4];
-    features(q, (vm.hi + vm.lo) * 1000.f, a.g0_Na, a.g0_Kr, a.g0_K1, f);
+    features(q, (vm.hi + vm.lo) * 1000.f, a.inv_g0_Na, a.inv_g0_Kr, a.inv_g0_K1, f);
     coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
     // accumulator quantities carry their coarse increment; the others their coarse value
     oc[0] = inc[0];
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
     }
     if (mlp_on) {  // features of the initial state -> row r of the 128 x 32 input tile
       float f[kSurIn];
-      features(q, (vm.hi + vm.lo) * 1000.f, a.g0_Na, a.g0_Kr, a.g0_K1, f);
+      features(q, (vm.hi + vm.lo) * 1000.f, a.inv_g0_Na, a.inv_g0_Kr, a.inv_g0_K1, f);
       uint32_t xb[16];
 #pragma unroll
       for (int j = 0; j < 16; j++) {

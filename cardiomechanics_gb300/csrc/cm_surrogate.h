@@ -62,7 +62,7 @@ struct SurKernelArgs {
   unsigned int *n_snap;
   int snap_cap;
   unsigned long long *n_sur;     // cells advanced by the surrogate (over all macro steps)
-  float g0_Na, g0_Kr, g0_K1;     // parameter-set conductances (feature reference)
+  float inv_g0_Na, inv_g0_Kr, inv_g0_K1;  // 1 / the parameter-set conductances (feature reference)
   // per-cell stimulus protocol (else stim_on for all cells): first stimulus time by cell, and
   // the time of the macro step's last fine step; a cell is stimulated when t_last >= tb_cell[c]
   const double *tb_cell;
@@ -77,8 +77,9 @@ struct SurPlainArgs {
   DevBatch fine;
   double *vm;                    // as SurKernelArgs
   float *vm_hi, *vm_lo;
-  const int *list;
+  const int *list;               // the cells to advance; null: cells 0 .. n_all - 1
   const unsigned int *n_list;
+  int n_all;
   int substeps;
   float iext[64];                // per fine step of the macro step
   // per-cell stimulus protocol (else iext[] for all cells): the reference driver's logic per
@@ -112,7 +113,7 @@ struct SurGenArgs {
   int64_t n_sample;
   float *X, *C;                  // features and coarse result per sample (kSurIn, kSurOut)
   float *Old;                    // Vm, CaSR, Na_i, K_i hi/lo words at the macro-step start (8)
-  float g0_Na, g0_Kr, g0_K1;
+  float inv_g0_Na, inv_g0_Kr, inv_g0_K1;
 };
 
 struct SurPostArgs {

@@ -39,6 +39,13 @@ int cm_diag_mlp_workspace_rows(void *mlp, int64_t *rows);
  * log(y), x / y. For accuracy tests. */
 int cm_diag_fp64_math(const double *x, const double *y, int64_t n, double *out, void *stream);
 
+/* The compensated FP32 pair conversions of the mixed kernels, on device arrays of n values: hi,
+ * lo = the pair of x (FP32 head rounded to nearest, FP32 remainder), back = hi + lo in FP64,
+ * widened = (double)(float)x, computed with the integer bit-pattern forms the kernels use.
+ * For tests. */
+int cm_diag_pair_convert(const double *x, int64_t n, float *hi, float *lo, double *back, double *widened,
+                         void *stream);
+
 #ifdef __cplusplus
 }
 #endif

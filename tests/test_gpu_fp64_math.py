@@ -54,3 +54,48 @@ def test_fp64_math_against_library_and_extended(gpu):
     assert _ulps(log64, ref_log).max() <= 1
     assert np.mean(exp64 == ref_exp) > 0.99
     assert np.mean(log64 == ref_log) > 0.99
+
+
+def test_pair_conversions(gpu):
+    """The mixed kernels' FP64 <-> compensated FP32 pair conversions, done on the bit patterns with
+    integer instructions: the pair of the FP64-instruction form (hi = x rounded to FP32, lo = the
+    rounded remainder), exact widening of every FP32 value, and the documented edge cases."""
+    import torch
+    cm = gpu
+    rng = np.random.default_rng(5)
+    normal = np.concatenate([
+        rng.uniform(-0.1, 0.06, 1 << 16),                       # Vm [V]
+        rng.choice([-1.0, 1.0], 1 << 15) * np.exp(rng.uniform(np.log(2.0**-73), np.log(2.0**127), 1 << 15)),
+    ])
+    ties = np.array([1.0 + 2.0**-24, -(1.0 + 2.0**-24), 3.0 * 2.0**-25 + 2.0**-1])  # remainder exactly half an ulp
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-40, -1e-40, 2.0**-100, 3e38, -3.4e38, 1e39, -1e300,
+                        1.5e-45, 2.0**-127])
+    x = np.concatenate([normal, ties, special])
+    hi, lo, back, wid = cm.pair_convert(torch.tensor(x, device="cuda"))
+    n = normal.size
+    h32 = normal.astype(np.float32)
+    assert np.array_equal(hi[:n], h32)
+    assert np.array_equal(lo[:n], (normal - h32.astype(np.float64)).astype(np.float32))
+    assert np.array_equal(back[:n], hi[:n].astype(np.float64) + lo[:n].astype(np.float64))
+    assert np.all(np.abs(back[:n] - normal) <= np.abs(normal) * 2.0**-48)
+    # ties: hi rounded away from zero, the pair still exact
+    t = slice(n, n + ties.size)
+    assert np.all(np.abs(hi[t]) >= np.abs(ties.astype(np.float32)))
+    assert np.array_equal(hi[t].astype(np.float64) + lo[t].astype(np.float64), ties)
+    # edge cases
+    s = slice(n + ties.size, None)
+    hs, ls = hi[s], lo[s]
+    assert hs[0] == 0 and not np.signbit(hs[0]) and hs[1] == 0 and np.signbit(hs[1]) and ls[0] == 0 and ls[1] == 0
+    assert hs[2] == np.inf and hs[3] == -np.inf and ls[2] == 0 and ls[3] == 0
+    assert np.isnan(hs[4])
+    assert hs[5] == 0 and not np.signbit(hs[5]) and hs[6] == 0 and np.signbit(hs[6])   # |x| < 2^-126: signed zero
+    assert hs[7] == np.float32(2.0**-100) and ls[7] == 0                              # |x| < 2^-74: lo = 0
+    assert hs[8] == np.float32(3e38) and np.isfinite(hs[8])
+    assert hs[9] == np.float32(-3.4e38)
+    assert hs[10] == np.inf and hs[11] == -np.inf and ls[10] == 0 and ls[11] == 0
+    # widening: exact for every FP32 value, subnormal, zero, inf and NaN included
+    f = x.astype(np.float32)
+    ok = ~np.isnan(f)
+    assert np.array_equal(wid[ok], f[ok].astype(np.float64))
+    assert np.array_equal(np.signbit(wid[ok]), np.signbit(f[ok]))
+    assert np.all(np.isnan(wid[~ok]))
