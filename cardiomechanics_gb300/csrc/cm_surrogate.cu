@@ -582,10 +582,15 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       atomicOr(fb.audit_or, kAuditTimeout);
     }
     ps ^= 1u;
-    group_sync(g);
-    if (s_abort[g]) {
-      mbar_wait(&bar_stage[g], ps ^ 1u, fb.spin_limit);  // the copy that timed out: one more bounded wait
-      break;
+    // the group agrees on a timeout at its next barrier: here without the network, after the
+    // features in the learned mode (a thread whose wait ran out computes them from whatever the
+    // stage holds; nothing of it leaves shared memory)
+    if (!mlp_on) {
+      group_sync(g);
+      if (s_abort[g]) {
+        mbar_wait(&bar_stage[g], ps ^ 1u, fb.spin_limit);  // the copy that timed out: one more bounded wait
+        break;
+      }
     }
     const float *S = stage + r;
     Cell q;
@@ -619,6 +624,10 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       for (int qd = 0; qd < 4; qd++)
         sts128(act + umma::kmajor_index(r, 8 * qd, 32), xb[4 * qd], xb[4 * qd + 1], xb[4 * qd + 2], xb[4 * qd + 3]);
       operands_ready();  // also: every thread has read its state from the stage
+      if (s_abort[g]) {
+        mbar_wait(&bar_stage[g], ps ^ 1u, fb.spin_limit);  // the copy that timed out: one more bounded wait
+        break;
+      }
       if (leader) {  // layer 1: D = X W1^T (K = 32), computed while the coarse step runs
         umma::fence_after_sync();
         constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
