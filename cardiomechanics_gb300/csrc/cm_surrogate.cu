@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
         mbar_wait(&bar_stage[g], ps ^ 1u, fb.spin_limit);  // the copy that timed out: one more bounded wait
         break;
       }
-      if (leader) {  // layer 1: D = X W1^T (K = 32), computed while the coarse step runs
+      if (leader) {  // layer 1: D = X W1^T (K = 32)
         umma::fence_after_sync();
         constexpr uint32_t id = umma::idesc_bf16_f32(128, 128);
 #pragma unroll
@@ -638,15 +638,19 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
       }
       if (issuer) next_tile();  // the stage is free: the next tile's copies overlap this tile's work
     }
-    // coarse physics step (registers only)
+    // coarse physics step (registers only): in the learned mode while the tensor core computes
+    // hidden layer 2, the longest of the three products
     float oc[kSurOut], inc[4];
     bool fall = !valid;
-    if (valid) {
-      coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
-      const float rate = fabsf(inc[0]) / macro_ms;
-      const bool stim = a.stim_on || (a.tb_cell && f64_ge(a.t_last, a.tb_cell[c]));
-      fall = stim || !(rate <= a.gate_mv_per_ms);
-    }
+    auto coarse_step = [&]() {
+      if (valid) {
+        coarse(a.coarse, a.rows_coarse, a.eca, q, vm, oc, inc);
+        const float rate = fabsf(inc[0]) / macro_ms;
+        const bool stim = a.stim_on || (a.tb_cell && f64_ge(a.t_last, a.tb_cell[c]));
+        fall = stim || !(rate <= a.gate_mv_per_ms);
+      }
+    };
+    if (!mlp_on) coarse_step();
     float y[32];
     if (mlp_on) {
       wait_mma();
@@ -670,6 +674,7 @@ __global__ void __launch_bounds__(512, 1) sur_step_tc_kernel(const SurKernelArgs
         umma::mma_bf16(tacc_mma, umma::smem_desc(ones_s, 128u, 256u), umma::smem_desc(b2_s, 128u, 256u), id, 1u);
         umma::commit(&bar_mma[g]);
       }
+      coarse_step();
       wait_mma();
       tc_hidden_epilogue(tacc, act, r);
       operands_ready();
