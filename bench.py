@@ -1029,7 +1029,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=10)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=200, help="timed C-ABI calls (one macro step each) of the end-to-end figure")
     ap.add_argument("--mixed-steps", type=int, default=2000, help="timed steps of the precision form")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", default="all",

@@ -47,7 +47,7 @@ __device__ __forceinline__ double exp64(double x) {
   const double p = fma(q, r * r, r);  // e^r - 1
   const double th = __ldg(kExp2Hi + j);
   const double y = th + fma(th, p, __ldg(kExp2Lo + j));  // in [0.99, 2.02): 2^m keeps it normal
-  return __hiloint2double(__double2hiint(y) + (m << 20), __double2loint(y));
+  return __hiloint2double(__double2hiint(y) + (int)((unsigned int)m << 20), __double2loint(y));
 }
 
 // ln x for positive normal finite x (else log). Tang's table-driven method (P. T. P. Tang, ACM
