@@ -439,8 +439,9 @@ __device__ __forceinline__ void warp_count(unsigned long long *counter, bool pre
 }
 
 // Per group and tile: the features of the cells' initial state go to the tensor core first
-// (layer-1 MMA issued), the coarse physics step runs while it computes, then the three layers'
-// epilogues and MMAs alternate; the network's correction is applied to the coarse result.
+// (layer-1 MMA), then the layers' epilogues and MMAs alternate, with the coarse physics step
+// computed while the tensor core runs layer 2 (the longest product); the network's correction is
+// applied to the coarse result.
 // The block's tiles (blockIdx.x + k * gridDim.x) go to its groups through a shared-memory counter,
 // so a group that starts late still takes an even share. kAudit: group kGroups - 1 first audits
 // the previous macro step's snapshots (prev) -- on the FP64 pipe the MLP groups leave idle --
