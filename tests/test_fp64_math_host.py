@@ -1,8 +1,10 @@
-"""The FP64 exp, log and division of the FP64 cell-model steps (csrc/cm_fp64_math.cuh), checked on
-the host: the committed tables equal their generator's output, and the device algorithms,
-emulated operation by operation (every fused multiply-add rounded once, exactly as the device
-rounds it), stay within 1 ulp of the correctly rounded value. The GPU test
-(tests/test_gpu_fp64_math.py) runs the compiled functions themselves."""
+"""The FP64 exp, log and division of the FP64 cell-model steps (csrc/cm_fp64_math.cuh) and the
+compensated-pair conversions of the mixed kernels (csrc/cm_common.cuh), checked on the host: the
+committed tables equal their generator's output, and the device algorithms, emulated operation by
+operation (every fused multiply-add rounded once, exactly as the device rounds it; the pair
+conversion's integer steps on the bit patterns), stay within 1 ulp of the correctly rounded value
+and give the FP64-instruction form's pair. The GPU tests (tests/test_gpu_fp64_math.py) run the
+compiled functions themselves."""
 import io
 import math
 import random
@@ -136,3 +138,63 @@ def test_division_from_any_reciprocal_within_2_to_minus_20():
         r0 = (1.0 / b) * (1.0 + rng.uniform(-1.0, 1.0) * 2.0**-20)
         q = div64(a, b, r0)
         assert ulps(q, a / b) <= 1, (a, b)
+
+
+# ---- the compensated-pair conversions of csrc/cm_common.cuh (device integer forms), emulated
+
+def _f32_bits(u):
+    return struct.unpack("<f", struct.pack("<I", u & 0xFFFFFFFF))[0]
+
+
+def _to_f32(x):
+    return struct.unpack("<f", struct.pack("<f", x))[0]
+
+
+def acc_from_double(x):
+    """cm::acc_from_double's device form, step by step (integer arithmetic on the bit pattern)."""
+    b = bits(x) & 0xFFFFFFFFFFFFFFFF
+    hw, lw = b >> 32, b & 0xFFFFFFFF
+    s = hw & 0x80000000
+    e = (hw >> 20) & 0x7FF
+    lr = (lw + 0x10000000) & 0xFFFFFFFF
+    hr = (hw + (1 if lr < lw else 0)) & 0xFFFFFFFF
+    er = (hr >> 20) & 0x7FF
+    hi = (s | (((er - 896) & 0xFFFFFFFF) << 23) | ((hr & 0xFFFFF) << 3) | (lr >> 29)) & 0xFFFFFFFF
+    rem = ((lw & 0x1FFFFFFF) << 3) & 0xFFFFFFFF
+    rem = (rem - (1 << 32) if rem >= 1 << 31 else rem) >> 3
+    rem = -rem if s else rem
+    lo = 0.0
+    if 949 <= e and er <= 1150:
+        lo = _to_f32(_to_f32(float(rem)) * 2.0 ** (e - 1075))  # I2F rounds once; the scale is exact
+    inf_or_nan = e == 0x7FF
+    nan = inf_or_nan and ((hw & 0xFFFFF) | lw) != 0
+    if e < 897:
+        hi = s
+    if er > 1150 or inf_or_nan:
+        hi = s | 0x7F800000
+    if nan:
+        hi = s | 0x7FC00000
+    return _f32_bits(hi), lo
+
+
+def test_pair_conversion_emulated():
+    rng = random.Random(13)
+    xs = [rng.uniform(-0.1, 0.06) for _ in range(3000)]
+    xs += [rng.choice([-1.0, 1.0]) * math.exp(rng.uniform(math.log(2.0**-73), math.log(2.0**127))) for _ in range(3000)]
+    for x in xs:
+        hi, lo = acc_from_double(x)
+        h32 = _to_f32(x)
+        ulp32 = math.ldexp(1.0, math.frexp(h32)[1] - 24)  # FP32 spacing at h32
+        if abs(Fraction(x) - Fraction(h32)) * 2 == Fraction(ulp32):
+            continue  # exact ties round away from zero here, to even in FP32: checked below
+        assert hi == h32, x
+        assert lo == _to_f32(x - h32), x
+    # ties keep the pair exact
+    for x in (1.0 + 2.0**-24, -(1.0 + 2.0**-24), 0.5 + 3.0 * 2.0**-25):
+        hi, lo = acc_from_double(x)
+        assert Fraction(hi) + Fraction(lo) == Fraction(x) and abs(hi) >= abs(_to_f32(x))
+    # edge cases
+    assert acc_from_double(0.0) == (0.0, 0.0) and math.copysign(1.0, acc_from_double(-0.0)[0]) == -1.0
+    assert acc_from_double(1e-40)[0] == 0.0 and acc_from_double(2.0**-100) == (2.0**-100, 0.0)
+    assert acc_from_double(1e39)[0] == math.inf and acc_from_double(-1e300)[0] == -math.inf
+    assert math.isnan(acc_from_double(math.nan)[0]) and acc_from_double(math.inf)[0] == math.inf
