@@ -562,6 +562,9 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
                      "traffic": SUR_STEP_TRAFFIC_PER_CELL * FULL_CELLS,
                      "traffic_note": "ncu DRAM read+write bytes of one 4,194,304-cell launch on a plateau step, "
                                      "scaled by cells: 0.94 of the algorithmic bytes",
+                     "algorithmic_bytes_note": "196 B per cell: 21 state planes and the Vm pair read and written, "
+                                               "3 conductances read; the 8 B per-cell first-stimulus time the step "
+                                               "also reads is not counted",
                      "tensor": {"achieved": tflops, "peak": tpk, "unit": "TFLOP/s", "frac": tflops / tpk,
                                 "peak_kind": tpk_kind, "flops_per_launch": FULL_CELLS * SUR_MLP_FLOPS_PER_CELL},
                      "bound_note": "issue-bound: neither HBM nor the tensor pipe limits this kernel"},
