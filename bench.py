@@ -515,8 +515,11 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
+    e2e_fb = e2e_cms = 0
     for _ in range(e2e_steps):
-        b.run_surrogate(sur, vm_h, 1, t0=t, textbegin_per_cell=tbc, **kw)
+        st = b.run_surrogate(sur, vm_h, 1, t0=t, textbegin_per_cell=tbc, **kw)
+        e2e_fb += st["fallback"]
+        e2e_cms += st["cell_macro_steps"]
         for _k in range(SUR_SUBSTEPS):
             t += DT
     f1.record(stream)
@@ -572,6 +575,7 @@ def full_form_leg(cm, torch, stream, p, sur, steps, warmup, e2e_steps, fp64_step
                              "algorithmic_bytes_per_launch": listed * SUR_PLAIN_BYTES_PER_LISTED_CELL},
         "e2e": {"value": FULL_CELLS * SUR_SUBSTEPS * e2e_steps / e2e_sec, "unit": UNIT,
                 "h2d_bytes_per_step": 8 * FULL_CELLS, "d2h_bytes_per_step": 8 * FULL_CELLS, "steps": e2e_steps,
+                "fallback_fraction": e2e_fb / max(1, e2e_cms),
                 "api": "cm_batch_run_surrogate per macro step, Vm in pinned host memory; per-cell stimulus "
                        "times kept on the device (advanced in place by the library)"},
         "plain_fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * sec64 / fp64_steps,
